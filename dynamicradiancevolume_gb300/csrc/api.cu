@@ -1,0 +1,392 @@
+// api.cu — the extern "C" entry points of include/drv.h: context lifetime,
+// resident buffers and the per-frame stage sequence of the reference's
+// Renderer::Draw (renderer.cpp:539-594). Every entry point validates its
+// arguments, enqueues work on the context stream and returns a drv_status; no
+// exception crosses the ABI.
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "drv_internal.h"
+
+using drv::Context;
+
+struct DrvContext : Context {};
+
+namespace {
+
+drv_status fail(DrvContext* ctx, drv_status st, const std::string& msg) {
+  if (ctx) ctx->last_error = msg;
+  return st;
+}
+
+drv_status cuda_check(DrvContext* ctx, cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return DRV_OK;
+  return fail(ctx, DRV_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define DRV_TRY_CUDA(ctx, expr)                              \
+  do {                                                       \
+    drv_status _st = cuda_check((ctx), (expr), #expr);       \
+    if (_st != DRV_OK) return _st;                           \
+  } while (0)
+
+int ilog2(int v) {
+  int l = 0;
+  while ((1 << (l + 1)) <= v) ++l;
+  return l;
+}
+
+bool is_pow2(int v) { return v > 0 && (v & (v - 1)) == 0; }
+
+void release(Context* c) {
+  cudaFree(c->entries);
+  cudaFree(c->atlas);
+  cudaFree(c->counter);
+  cudaFree(c->voxel_bits);
+  cudaFree(c->mips);
+  for (int l = 0; l < DRV_MAX_LIGHTS; ++l) {
+    for (int k = 1; k < drv::kMaxRsmLevels; ++k) {
+      cudaFree(c->rsm[l].flux[k]);
+      cudaFree(c->rsm[l].normal[k]);
+      cudaFree(c->rsm[l].dls[k]);
+    }
+    cudaFree(c->vpls[l]);
+    cudaFree(c->cones[l]);
+  }
+  cudaFree(c->d_boxes);
+  cudaFreeHost(c->h_boxes);
+  if (c->stream) cudaStreamDestroy(c->stream);
+}
+
+drv_status validate_config(const DrvConfig* c, std::string& why) {
+  if (c->width < 1 || c->height < 1) return why = "width/height must be positive", DRV_ERR_INVALID_ARG;
+  if (c->sh_order != 1 && c->sh_order != 2) return why = "sh_order must be 1 or 2", DRV_ERR_INVALID_ARG;
+  if (c->n_cascades < 1 || c->n_cascades > DRV_MAX_CASCADES) return why = "n_cascades must be 1..4", DRV_ERR_INVALID_ARG;
+  if (c->cav_res < 2 || c->cav_res > 256) return why = "cav_res must be 2..256", DRV_ERR_INVALID_ARG;
+  if (!is_pow2(c->voxel_res) || c->voxel_res < 32 || c->voxel_res > 1024)
+    return why = "voxel_res must be a power of two in 32..1024", DRV_ERR_INVALID_ARG;
+  if (c->max_caches < 1) return why = "max_caches must be positive", DRV_ERR_INVALID_ARG;
+  if (c->max_cone_steps < 1 || c->max_cone_steps > 4096) return why = "max_cone_steps must be 1..4096", DRV_ERR_INVALID_ARG;
+  if (c->max_lights < 1 || c->max_lights > DRV_MAX_LIGHTS) return why = "max_lights must be 1..16", DRV_ERR_INVALID_ARG;
+  if (!is_pow2(c->max_rsm_resolution) || c->max_rsm_resolution > 4096)
+    return why = "max_rsm_resolution must be a power of two <= 4096", DRV_ERR_INVALID_ARG;
+  if (c->precision != DRV_PRECISION_FP32) return why = "precision mode not available", DRV_ERR_NOT_SUPPORTED;
+  if (c->visibility != DRV_VISIBILITY_CONE) return why = "visibility mode not available", DRV_ERR_NOT_SUPPORTED;
+  if (c->sh2_sign != DRV_SH2_SIGN_REFERENCE && c->sh2_sign != DRV_SH2_SIGN_FIXED)
+    return why = "sh2_sign must be 0 or 1", DRV_ERR_INVALID_ARG;
+  return DRV_OK;
+}
+
+bool views_ok(const DrvGBufferView* g, const DrvConfig& c) {
+  return g && g->depth && g->normal && g->albedo && g->width == c.width && g->height == c.height &&
+         (g->normal_format == DRV_NORMAL_RG16I || g->normal_format == DRV_NORMAL_F32X3);
+}
+
+}  // namespace
+
+extern "C" {
+
+int drv_struct_sizes(uint32_t* out, int capacity) {
+  const uint32_t s[] = {sizeof(DrvConfig),     sizeof(DrvCascade),    sizeof(DrvVolumeInfo), sizeof(DrvPerFrame),
+                        sizeof(DrvSpotLight),  sizeof(DrvLightDesc),  sizeof(DrvCamera),     sizeof(DrvBox),
+                        sizeof(DrvScene),      sizeof(DrvGBufferView), sizeof(DrvGBufferOut), sizeof(DrvRSMView),
+                        sizeof(DrvRSMOut),     sizeof(DrvVPL),        sizeof(DrvShadowCone), sizeof(DrvCacheCounter),
+                        sizeof(DrvBuffers)};
+  int n = (int)(sizeof(s) / sizeof(s[0]));
+  if (!out) return n;
+  int k = capacity < n ? capacity : n;
+  for (int i = 0; i < k; ++i) out[i] = s[i];
+  return k;
+}
+
+drv_status drv_create(const DrvConfig* cfg, DrvContext** out) {
+  if (!cfg || !out) return DRV_ERR_INVALID_ARG;
+  *out = nullptr;
+  std::string why;
+  drv_status st = validate_config(cfg, why);
+  if (st != DRV_OK) return st;
+  DrvContext* c = new (std::nothrow) DrvContext();
+  if (!c) return DRV_ERR_CUDA;
+  c->cfg = *cfg;
+  auto bail = [&](cudaError_t e) {
+    release(c);
+    delete c;
+    (void)e;
+    return DRV_ERR_CUDA;
+  };
+  cudaError_t e;
+  if ((e = cudaGetDevice(&c->device)) != cudaSuccess) return bail(e);
+  if ((e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device)) != cudaSuccess) return bail(e);
+  if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) return bail(e);
+  // LightCacheBuffer: 64 B (SH1) or 128 B (SH2) entries (lightcache.glsl:33-76).
+  c->entry_stride = cfg->sh_order == 2 ? 128u : 64u;
+  if ((e = cudaMalloc(&c->entries, (size_t)cfg->max_caches * c->entry_stride)) != cudaSuccess) return bail(e);
+  c->atlas_words = (size_t)cfg->n_cascades * cfg->cav_res * cfg->cav_res * cfg->cav_res;
+  if ((e = cudaMalloc(&c->atlas, c->atlas_words * 4)) != cudaSuccess) return bail(e);
+  // counter (16 B) + ticket + error word, one allocation.
+  if ((e = cudaMalloc(&c->counter, 32)) != cudaSuccess) return bail(e);
+  c->scratch_words = reinterpret_cast<uint32_t*>(c->counter + 1);
+  if ((e = cudaMemset(c->counter, 0, 32)) != cudaSuccess) return bail(e);
+  // Voxel level 0 (bitmask) and FP32 mips.
+  const int N = cfg->voxel_res;
+  c->voxel_words = (size_t)N * N * N / 32;
+  if ((e = cudaMalloc(&c->voxel_bits, c->voxel_words * 4)) != cudaSuccess) return bail(e);
+  c->n_voxel_levels = ilog2(N) + 1;
+  size_t off = 0;
+  for (int l = 1; l < c->n_voxel_levels; ++l) {
+    c->mip_offset[l] = off;
+    size_t n = (size_t)(N >> l);
+    off += n * n * n;
+  }
+  if ((e = cudaMalloc(&c->mips, off * 4)) != cudaSuccess) return bail(e);
+  // RSM chains (levels below the caller's render-resolution level) and VPLs.
+  const int R = cfg->max_rsm_resolution;
+  for (int l = 0; l < cfg->max_lights; ++l) {
+    for (int k = 1; (R >> k) >= 1 && k < drv::kMaxRsmLevels; ++k) {
+      size_t n = (size_t)(R >> k) * (R >> k);
+      if ((e = cudaMalloc(&c->rsm[l].flux[k], n * 12)) != cudaSuccess) return bail(e);
+      if ((e = cudaMalloc(&c->rsm[l].normal[k], n * 4)) != cudaSuccess) return bail(e);
+      if ((e = cudaMalloc(&c->rsm[l].dls[k], n * 8)) != cudaSuccess) return bail(e);
+    }
+    if ((e = cudaMalloc(&c->vpls[l], (size_t)R * R * sizeof(DrvVPL))) != cudaSuccess) return bail(e);
+    if ((e = cudaMalloc(&c->cones[l], (size_t)R * R * sizeof(DrvShadowCone))) != cudaSuccess) return bail(e);
+  }
+  c->box_capacity = 512;
+  if ((e = cudaMallocHost(&c->h_boxes, c->box_capacity * sizeof(DrvBox))) != cudaSuccess) return bail(e);
+  if ((e = cudaMalloc(&c->d_boxes, c->box_capacity * sizeof(DrvBox))) != cudaSuccess) return bail(e);
+  c->resident_boxes = -1;
+  *out = c;
+  return DRV_OK;
+}
+
+drv_status drv_destroy(DrvContext* ctx) {
+  if (!ctx) return DRV_ERR_INVALID_ARG;
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  release(ctx);
+  delete ctx;
+  return DRV_OK;
+}
+
+drv_status drv_set_stream(DrvContext* ctx, void* stream) {
+  if (!ctx) return DRV_ERR_INVALID_ARG;
+  ctx->user_stream = (cudaStream_t)stream;
+  return DRV_OK;
+}
+
+const char* drv_last_error_string(DrvContext* ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+
+drv_status drv_get_error(DrvContext* ctx, uint32_t* bits) {
+  if (!ctx || !bits) return DRV_ERR_INVALID_ARG;
+  DRV_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->s()));
+  DRV_TRY_CUDA(ctx, cudaMemcpy(bits, ctx->scratch_words + 1, 4, cudaMemcpyDeviceToHost));
+  return DRV_OK;
+}
+
+drv_status drv_sync(DrvContext* ctx) {
+  if (!ctx) return DRV_ERR_INVALID_ARG;
+  uint32_t bits = 0;
+  drv_status st = drv_get_error(ctx, &bits);
+  if (st != DRV_OK) return st;
+  if (bits & DRV_DEVERR_CAPACITY) return fail(ctx, DRV_ERR_CAPACITY, "more light caches requested than max_caches");
+  if (bits & DRV_DEVERR_TIMEOUT) return fail(ctx, DRV_ERR_TIMEOUT, "a bounded device-side wait gave up");
+  if (bits & DRV_DEVERR_BOUNDS) return fail(ctx, DRV_ERR_INVALID_ARG, "device-side bounds check failed");
+  return DRV_OK;
+}
+
+drv_status drv_get_buffers(DrvContext* ctx, DrvBuffers* o) {
+  if (!ctx || !o) return DRV_ERR_INVALID_ARG;
+  std::memset(o, 0, sizeof(*o));
+  o->cache_entries = ctx->entries;
+  o->entry_stride = ctx->entry_stride;
+  o->cav_atlas = ctx->atlas;
+  o->counter = ctx->counter;
+  o->voxel_bits = ctx->voxel_bits;
+  for (int l = 1; l < ctx->n_voxel_levels && l < 16; ++l) o->voxel_mips[l] = ctx->mips + ctx->mip_offset[l];
+  o->n_voxel_levels = ctx->n_voxel_levels;
+  for (int l = 0; l < DRV_MAX_LIGHTS; ++l) {
+    o->vpls[l] = ctx->vpls[l];
+    o->cones[l] = ctx->cones[l];
+    o->n_vpls[l] = ctx->n_vpls[l];
+  }
+  o->n_lights = ctx->n_lights;
+  return DRV_OK;
+}
+
+drv_status drv_get_cache_count(DrvContext* ctx, uint32_t* out) {
+  if (!ctx || !out) return DRV_ERR_INVALID_ARG;
+  DrvCacheCounter h;
+  DRV_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->s()));
+  DRV_TRY_CUDA(ctx, cudaMemcpy(&h, ctx->counter, sizeof(h), cudaMemcpyDeviceToHost));
+  *out = (uint32_t)(h.total_light_cache_count < 0 ? 0 : h.total_light_cache_count);
+  return drv_sync(ctx);
+}
+
+drv_status drv_set_scene(DrvContext* ctx, const DrvScene* scene) {
+  if (!ctx || !scene || !scene->boxes || scene->n_boxes < 1) return DRV_ERR_INVALID_ARG;
+  if (scene->n_boxes > ctx->box_capacity) return fail(ctx, DRV_ERR_INVALID_ARG, "scene has more than 512 boxes");
+  if (ctx->resident_boxes == scene->n_boxes &&
+      std::memcmp(ctx->h_boxes, scene->boxes, scene->n_boxes * sizeof(DrvBox)) == 0)
+    return DRV_OK;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  DRV_TRY_CUDA(ctx, cudaStreamIsCapturing(ctx->s(), &cs));
+  if (cs != cudaStreamCaptureStatusNone)
+    return fail(ctx, DRV_ERR_INVALID_ARG, "scene changed while the stream is being captured");
+  DRV_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->s()));
+  std::memcpy(ctx->h_boxes, scene->boxes, scene->n_boxes * sizeof(DrvBox));
+  DRV_TRY_CUDA(ctx, cudaMemcpyAsync(ctx->d_boxes, ctx->h_boxes, scene->n_boxes * sizeof(DrvBox),
+                                    cudaMemcpyHostToDevice, ctx->s()));
+  DRV_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->s()));
+  ctx->resident_boxes = scene->n_boxes;
+  return DRV_OK;
+}
+
+drv_status drv_raycast_gbuffer(DrvContext* ctx, const DrvScene* scene, const DrvCamera* cam, const DrvPerFrame* frame,
+                               int32_t w, int32_t h, const DrvGBufferOut* out) {
+  if (!ctx || !scene || !cam || !frame || !out || !out->depth || !out->albedo || w < 1 || h < 1)
+    return DRV_ERR_INVALID_ARG;
+  drv_status st = drv_set_scene(ctx, scene);
+  if (st != DRV_OK) return st;
+  const double ty = std::tan(cam->fov_y_deg * (3.14159265358979323846 / 180.0) * 0.5);
+  drv::RayFrame rf = drv::make_ray_frame(cam->position, cam->direction, cam->up, ty * cam->aspect, ty);
+  return cuda_check(ctx, drv::launch_raycast_gbuffer(ctx->s(), ctx->d_boxes, scene->n_boxes, rf, frame->view_projection,
+                                                     w, h, *out),
+                    "raycast_gbuffer");
+}
+
+drv_status drv_raycast_rsm(DrvContext* ctx, const DrvScene* scene, const DrvSpotLight* light, const DrvRSMOut* out) {
+  if (!ctx || !scene || !light || !out || !out->flux || !out->normal || !out->depth_lin_sq) return DRV_ERR_INVALID_ARG;
+  if (light->rsm_render_resolution < 1) return DRV_ERR_INVALID_ARG;
+  drv_status st = drv_set_scene(ctx, scene);
+  if (st != DRV_OK) return st;
+  return cuda_check(ctx, drv::launch_raycast_rsm(ctx->s(), ctx->d_boxes, scene->n_boxes, *light, *out), "raycast_rsm");
+}
+
+// ShadowMap::PrepareRSM (renderer.cpp:1300-1339): successive 2x2 reductions,
+// down to the deepest level the light reads (read lod + shadow lod).
+drv_status drv_prepare_rsm(DrvContext* ctx, int32_t li, const DrvSpotLight* L, const DrvRSMView* v) {
+  if (!ctx || !L || !v || !v->flux || !v->normal || !v->depth_lin_sq) return DRV_ERR_INVALID_ARG;
+  if (li < 0 || li >= ctx->cfg.max_lights) return fail(ctx, DRV_ERR_INVALID_ARG, "light index out of range");
+  const int R = v->resolution;
+  if (!is_pow2(R) || R != L->rsm_render_resolution || R > ctx->cfg.max_rsm_resolution)
+    return fail(ctx, DRV_ERR_INVALID_ARG, "RSM resolution must equal rsm_render_resolution (power of two, <= max)");
+  if (L->rsm_read_resolution < 1 || R % L->rsm_read_resolution != 0)
+    return fail(ctx, DRV_ERR_INVALID_ARG, "rsm_read_resolution must divide the RSM resolution");
+  const int read_lod = ilog2(R / L->rsm_read_resolution);
+  const int shadow_lod = (int)L->indirect_shadow_lod;
+  const int deepest = read_lod + shadow_lod;
+  if ((R >> deepest) < 1) return fail(ctx, DRV_ERR_INVALID_ARG, "indirect shadow lod beyond the RSM chain");
+  drv::RsmChain& ch = ctx->rsm[li];
+  ch.res0 = R;
+  ch.n_levels = deepest + 1;
+  ch.flux[0] = const_cast<float*>(v->flux);
+  ch.normal[0] = const_cast<int16_t*>(v->normal);
+  ch.dls[0] = const_cast<float*>(v->depth_lin_sq);
+  for (int k = 0; k < deepest; ++k) {
+    DRV_TRY_CUDA(ctx, drv::launch_downsample_rsm(ctx->s(), R >> k, ch.flux[k], ch.normal[k], ch.dls[k], ch.flux[k + 1],
+                                                 ch.normal[k + 1], ch.dls[k + 1]));
+  }
+  return DRV_OK;
+}
+
+drv_status drv_extract_vpls(DrvContext* ctx, int32_t li, const DrvSpotLight* L) {
+  if (!ctx || !L) return DRV_ERR_INVALID_ARG;
+  if (li < 0 || li >= ctx->cfg.max_lights) return fail(ctx, DRV_ERR_INVALID_ARG, "light index out of range");
+  drv::RsmChain& ch = ctx->rsm[li];
+  if (ch.res0 != L->rsm_render_resolution || ch.n_levels < 1)
+    return fail(ctx, DRV_ERR_INVALID_ARG, "drv_prepare_rsm must run for this light first");
+  const int R = L->rsm_read_resolution;
+  const int read_lod = ilog2(ch.res0 / R);
+  const int shadow_level = read_lod + (int)L->indirect_shadow_lod;
+  if (shadow_level >= ch.n_levels) return fail(ctx, DRV_ERR_INVALID_ARG, "RSM chain too short for the shadow lod");
+  if (L->indirect_shadow_sample_interval < 1) return DRV_ERR_INVALID_ARG;
+  DRV_TRY_CUDA(ctx, drv::launch_extract_vpls(ctx->s(), *L, R, ch.flux[read_lod], ch.normal[read_lod], ch.dls[read_lod],
+                                             ch.dls[shadow_level], ctx->vpls[li], ctx->cones[li]));
+  ctx->n_vpls[li] = R * R;
+  ctx->interval[li] = L->indirect_shadow_sample_interval;
+  ctx->n_cones[li] = (R * R + L->indirect_shadow_sample_interval - 1) / L->indirect_shadow_sample_interval;
+  if (li + 1 > ctx->n_lights) ctx->n_lights = li + 1;
+  return DRV_OK;
+}
+
+drv_status drv_voxelize(DrvContext* ctx, const DrvScene* scene, const DrvVolumeInfo* vol) {
+  if (!ctx || !scene || !vol) return DRV_ERR_INVALID_ARG;
+  drv_status st = drv_set_scene(ctx, scene);
+  if (st != DRV_OK) return st;
+  return cuda_check(ctx, drv::launch_voxelize(ctx->s(), ctx->d_boxes, scene->n_boxes, *vol, ctx->cfg.voxel_res,
+                                              ctx->voxel_bits),
+                    "voxelize");
+}
+
+drv_status drv_build_opacity_mips(DrvContext* ctx) {
+  if (!ctx) return DRV_ERR_INVALID_ARG;
+  return cuda_check(ctx, drv::launch_build_mips(ctx->s(), ctx->cfg.voxel_res, ctx->voxel_bits, ctx->mips,
+                                                ctx->mip_offset, ctx->n_voxel_levels),
+                    "build_opacity_mips");
+}
+
+// Renderer::AllocateCaches: clear counter and atlas (renderer.cpp:968-970),
+// then cacheGather.comp + cachePrepareLighting.comp in one launch.
+drv_status drv_allocate_caches(DrvContext* ctx, const DrvGBufferView* g, const DrvPerFrame* f, const DrvVolumeInfo* vol) {
+  if (!ctx || !f || !vol) return DRV_ERR_INVALID_ARG;
+  if (!views_ok(g, ctx->cfg)) return fail(ctx, DRV_ERR_INVALID_ARG, "G-buffer view does not match the config");
+  DRV_TRY_CUDA(ctx, cudaMemsetAsync(ctx->counter, 0, 32, ctx->s()));
+  DRV_TRY_CUDA(ctx, cudaMemsetAsync(ctx->atlas, 0, ctx->atlas_words * 4, ctx->s()));
+  return cuda_check(ctx, drv::launch_allocate(ctx->s(), ctx->cfg, *vol, *f, g->depth, g->width, g->height, ctx->atlas,
+                                              ctx->entries, ctx->entry_stride, ctx->counter, ctx->scratch_words,
+                                              ctx->scratch_words + 1),
+                    "allocate_caches");
+}
+
+drv_status drv_light_caches(DrvContext* ctx, const DrvSpotLight* lights, int32_t n_lights, const DrvVolumeInfo* vol,
+                            const DrvPerFrame* frame) {
+  if (!ctx || !lights || !vol || !frame) return DRV_ERR_INVALID_ARG;
+  if (n_lights < 0 || n_lights > ctx->cfg.max_lights) return fail(ctx, DRV_ERR_INVALID_ARG, "bad light count");
+  drv::LightLaunch ll{};
+  ll.n_lights = n_lights;
+  for (int l = 0; l < n_lights; ++l) {
+    if (ctx->n_vpls[l] != lights[l].rsm_read_resolution * lights[l].rsm_read_resolution)
+      return fail(ctx, DRV_ERR_INVALID_ARG, "drv_extract_vpls must run for every light first");
+    ll.lights[l].vpls = ctx->vpls[l];
+    ll.lights[l].cones = ctx->cones[l];
+    ll.lights[l].n_vpls = ctx->n_vpls[l];
+    ll.lights[l].interval = ctx->interval[l];
+  }
+  return cuda_check(ctx, drv::launch_light_caches(ctx->s(), ctx->cfg, *vol, ll, ctx->counter, ctx->entries,
+                                                  ctx->entry_stride, ctx->voxel_bits, ctx->mips, ctx->mip_offset,
+                                                  ctx->num_sms),
+                    "light_caches");
+}
+
+drv_status drv_apply(DrvContext* ctx, const DrvGBufferView* g, const DrvPerFrame* f, const DrvVolumeInfo* vol,
+                     float* out_rgb) {
+  if (!ctx || !f || !vol || !out_rgb) return DRV_ERR_INVALID_ARG;
+  if (!views_ok(g, ctx->cfg)) return fail(ctx, DRV_ERR_INVALID_ARG, "G-buffer view does not match the config");
+  return cuda_check(ctx, drv::launch_apply(ctx->s(), ctx->cfg, *vol, *f, *g, ctx->atlas, ctx->entries,
+                                           ctx->entry_stride, ctx->counter, out_rgb),
+                    "apply");
+}
+
+// Renderer::Draw, DYN_RADIANCE_VOLUME branch (renderer.cpp:539-594), plus the
+// RSM preparation of DrawShadowMaps (renderer.cpp:801-810).
+drv_status drv_frame(DrvContext* ctx, const DrvScene* scene, const DrvGBufferView* g, const DrvPerFrame* f,
+                     const DrvVolumeInfo* vol, const DrvSpotLight* lights, const DrvRSMView* rsms, int32_t n_lights,
+                     float* out_rgb) {
+  if (!ctx || !scene || !g || !f || !vol || (n_lights > 0 && (!lights || !rsms)) || !out_rgb)
+    return DRV_ERR_INVALID_ARG;
+  drv_status st;
+  for (int l = 0; l < n_lights; ++l) {
+    if ((st = drv_prepare_rsm(ctx, l, &lights[l], &rsms[l])) != DRV_OK) return st;
+    if ((st = drv_extract_vpls(ctx, l, &lights[l])) != DRV_OK) return st;
+  }
+  if (ctx->cfg.indirect_shadow) {
+    if ((st = drv_voxelize(ctx, scene, vol)) != DRV_OK) return st;
+    if ((st = drv_build_opacity_mips(ctx)) != DRV_OK) return st;
+  }
+  if ((st = drv_allocate_caches(ctx, g, f, vol)) != DRV_OK) return st;
+  if ((st = drv_light_caches(ctx, lights, n_lights, vol, f)) != DRV_OK) return st;
+  return drv_apply(ctx, g, f, vol, out_rgb);
+}
+
+}  // extern "C"

@@ -1,0 +1,106 @@
+// drv_internal.h — context layout and kernel launchers shared by the
+// translation units of libdrv_gb300.so. Not part of the public ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "../../include/drv.h"
+
+namespace drv {
+
+constexpr int kMaxVoxelLevels = 16;
+constexpr int kMaxRsmLevels = 16;
+
+struct RsmChain {
+  int res0 = 0;      // render resolution
+  int n_levels = 0;  // levels res0, res0/2, ..., 1
+  float* flux[kMaxRsmLevels] = {};
+  int16_t* normal[kMaxRsmLevels] = {};
+  float* dls[kMaxRsmLevels] = {};
+};
+
+// Per-light arguments of the light stage.
+struct LightArgs {
+  const DrvVPL* vpls;
+  const DrvShadowCone* cones;
+  int n_vpls;
+  int interval;  // IndirectShadowComputationSampleInterval
+};
+
+struct LightLaunch {
+  LightArgs lights[DRV_MAX_LIGHTS];
+  int n_lights;
+};
+
+// Ray frame of a pinhole camera: direction = normalize(fwd + nx*right + ny*up).
+struct RayFrame {
+  float origin[3];
+  float fwd[3];
+  float right[3];  // already scaled by tan(fov_x / 2)
+  float up[3];     // already scaled by tan(fov_y / 2)
+};
+
+struct Context {
+  DrvConfig cfg{};
+  cudaStream_t stream = nullptr;       // owned
+  cudaStream_t user_stream = nullptr;  // set by drv_set_stream, borrowed
+  cudaStream_t s() const { return user_stream ? user_stream : stream; }
+  int device = 0;
+  int num_sms = 0;
+  std::string last_error;
+
+  // Caches (LightCacheBuffer, CAV atlas, counter).
+  void* entries = nullptr;
+  uint32_t entry_stride = 0;
+  uint32_t* atlas = nullptr;
+  size_t atlas_words = 0;
+  DrvCacheCounter* counter = nullptr;
+  uint32_t* scratch_words = nullptr;  // [0] alloc ticket, [1] device error bits
+  // Voxels.
+  uint32_t* voxel_bits = nullptr;
+  size_t voxel_words = 0;
+  float* mips = nullptr;  // levels 1..L concatenated (FP32)
+  size_t mip_offset[kMaxVoxelLevels] = {};
+  int n_voxel_levels = 0;
+  // RSM + VPLs per light.
+  RsmChain rsm[DRV_MAX_LIGHTS];
+  DrvVPL* vpls[DRV_MAX_LIGHTS] = {};
+  DrvShadowCone* cones[DRV_MAX_LIGHTS] = {};
+  int n_vpls[DRV_MAX_LIGHTS] = {};
+  int n_cones[DRV_MAX_LIGHTS] = {};
+  int interval[DRV_MAX_LIGHTS] = {};
+  int n_lights = 0;
+  // Scene boxes: pinned staging + device copy.
+  DrvBox* h_boxes = nullptr;
+  DrvBox* d_boxes = nullptr;
+  int box_capacity = 0;
+  int resident_boxes = -1;  // boxes currently on the device (-1: none)
+};
+
+RayFrame make_ray_frame(const float pos[3], const float dir[3], const float up[3], double tan_x, double tan_y);
+
+// ---- launchers (each returns cudaGetLastError() of its launch) -----------
+cudaError_t launch_raycast_gbuffer(cudaStream_t s, const DrvBox* boxes, int n_boxes, RayFrame rf,
+                                   const float* view_proj, int w, int h, DrvGBufferOut out);
+cudaError_t launch_raycast_rsm(cudaStream_t s, const DrvBox* boxes, int n_boxes, const DrvSpotLight& L, DrvRSMOut out);
+cudaError_t launch_downsample_rsm(cudaStream_t s, int res, const float* flux, const int16_t* nrm, const float* dls,
+                                  float* fo, int16_t* no, float* dlo);
+cudaError_t launch_extract_vpls(cudaStream_t s, const DrvSpotLight& L, int res, const float* flux, const int16_t* nrm,
+                                const float* dls, const float* dls_shadow, DrvVPL* vpls, DrvShadowCone* cones);
+cudaError_t launch_voxelize(cudaStream_t s, const DrvBox* boxes, int n_boxes, const DrvVolumeInfo& vol, int n,
+                            uint32_t* bits);
+cudaError_t launch_build_mips(cudaStream_t s, int n, const uint32_t* bits, float* mips, const size_t* offsets,
+                              int n_levels);
+cudaError_t launch_allocate(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const DrvPerFrame& f,
+                            const float* depth, int w, int h, uint32_t* atlas, void* entries, uint32_t entry_stride,
+                            DrvCacheCounter* counter, uint32_t* ticket, uint32_t* err);
+cudaError_t launch_light_caches(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const LightLaunch& ll,
+                                const DrvCacheCounter* counter, void* entries, uint32_t entry_stride,
+                                const uint32_t* bits, const float* mips, const size_t* mip_offsets, int num_sms);
+cudaError_t launch_apply(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const DrvPerFrame& f,
+                         const DrvGBufferView& g, const uint32_t* atlas, const void* entries, uint32_t entry_stride,
+                         const DrvCacheCounter* counter, float* out_rgb);
+
+}  // namespace drv

@@ -1,0 +1,146 @@
+// k_alloc.cu — Renderer::AllocateCaches (renderer.cpp:951-992):
+// cacheGather.comp (16x16 workgroups, shared-memory neighbour dedupe, corner
+// lock by compare-and-swap, compaction by an atomic counter) and
+// cachePrepareLighting.comp (indirect-dispatch arguments), the latter folded
+// into the last CTA of the same launch through a completion ticket.
+#include "drv_device.cuh"
+#include "drv_internal.h"
+
+namespace drv {
+namespace {
+
+constexpr int kTile = 16;  // LOCAL_SIZE, cacheGather.comp:11
+
+struct AllocParams {
+  DrvVolumeInfo vol;
+  DrvPerFrame frame;
+  const float* depth;
+  int w, h;
+  int res, n_cascades;
+  int transitions;
+  uint32_t max_caches;
+  uint32_t* atlas;
+  float4* entries;
+  int entry_vec4;  // entry stride in float4 units
+  DrvCacheCounter* counter;
+  uint32_t* ticket;
+  uint32_t* err;
+};
+
+// AllocateCaches, cacheGather.comp:32-91. Corners outside the atlas are
+// skipped (the reference performs an image atomic there, which GL defines to
+// do nothing and return 0, and then allocates an entry nobody can address).
+__device__ void allocate_cell(const AllocParams& p, int coord, int cascade) {
+  const int res = p.res, res2 = res * res, res3 = res2 * res;
+  const int aw = p.n_cascades * res;
+  const int base = coord - res3 * cascade;
+  const int bz = base / res2, by = (base - bz * res2) / res, bx = base % res;
+  const DrvCascade& k = p.vol.cascades[cascade];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    // Corner order of cacheGather.comp:34-44: (0,0,0) (0,1,0) (0,0,1) (0,1,1) (1,...)
+    const int lx = bx + (i >> 2), ly = by + (i & 1), lz = bz + ((i >> 1) & 1);
+    const int ax = lx + cascade * res;
+    if (ax >= aw || ly >= res || lz >= res) continue;
+    uint32_t* slot = p.atlas + ((size_t)lz * res + ly) * aw + ax;
+    if (atomicCAS(slot, 0u, 0xFFFFFFFFu) != 0u) continue;
+    uint32_t idx = (uint32_t)atomicAdd(&p.counter->total_light_cache_count, 1);
+    if (idx >= p.max_caches) {
+      raise_error(p.err, DRV_DEVERR_CAPACITY);  // slot stays locked = empty for apply
+      continue;
+    }
+    float4* e = p.entries + (size_t)idx * p.entry_vec4;
+    e[0] = make_float4(__fadd_rn(__fmul_rn((float)lx, k.world_voxel_size), k.min[0]),
+                       __fadd_rn(__fmul_rn((float)ly, k.world_voxel_size), k.min[1]),
+                       __fadd_rn(__fmul_rn((float)lz, k.world_voxel_size), k.min[2]), 0.0f);
+    for (int v = 1; v < p.entry_vec4; ++v) e[v] = make_float4(0.f, 0.f, 0.f, 0.f);
+    *slot = idx + 1u;  // +1: zero means "cleared" (cacheGather.comp:88)
+  }
+}
+
+__global__ void __launch_bounds__(kTile* kTile) allocate_kernel(AllocParams p) {
+  __shared__ int list1[kTile][kTile];
+  __shared__ int list2[kTile][kTile];
+  const int lx = threadIdx.x, ly = threadIdx.y;
+  const int px = blockIdx.x * kTile + lx, py = blockIdx.y * kTile + ly;
+  list1[lx][ly] = -1;
+  list2[lx][ly] = -1;
+  __syncthreads();
+  int own = -1, own2 = -1, cascade = -1;
+  if (px < p.w && py < p.h) {
+    float d = p.depth[(size_t)py * p.w + px];
+    if (d > 0.0001f) {
+      float wp[3];
+      reconstruct_world(p.frame, px, py, p.w, p.h, d, wp);
+      cascade = select_cascade(p.vol, p.n_cascades, wp);
+      own = cache_1d_coord(p.vol, p.res, cascade, wp);
+      list1[lx][ly] = own;
+      if (p.transitions) {
+        float t = cascade_transition(p.vol, cascade, wp);
+        if (t > 0.0f && cascade < p.n_cascades - 1) {
+          own2 = cache_1d_coord(p.vol, p.res, cascade + 1, wp);
+          list2[lx][ly] = own2;
+        }
+      }
+    }
+  }
+  __syncthreads();
+  // cacheGather.comp:141-150: allocate unless the up, left or up-left
+  // neighbour registered the same cell; the vector equality of :146 holds
+  // only for thread (0,0), so the other threads of row 0 / column 0 compare
+  // against themselves and never allocate (kept as in the reference).
+  {
+    const int ux = max(0, lx - 1), uy = max(0, ly - 1);
+    const bool self = (ux == lx && uy == ly);
+    if (((list1[lx][uy] != own && list1[ux][ly] != own && list1[ux][uy] != own) || self) && own != -1)
+      allocate_cell(p, own, cascade);
+  }
+  // cacheGather.comp:153-162: transition cells, looking down/right.
+  if (p.transitions) {
+    const int dx = min(kTile - 1, lx + 1), dy = min(kTile - 1, ly + 1);
+    const bool corner = (dx == kTile - 1 && dy == kTile - 1);
+    if (((list2[lx][dy] != own2 && list2[dx][ly] != own2 && list2[dx][dy] != own2) || corner) && own2 != -1)
+      allocate_cell(p, own2, cascade + 1);
+  }
+  // cachePrepareLighting.comp, run by the last CTA to finish.
+  __threadfence();
+  __syncthreads();
+  if (lx == 0 && ly == 0) {
+    const uint32_t n_blocks = gridDim.x * gridDim.y;
+    if (atomicAdd(p.ticket, 1u) == n_blocks - 1u) {
+      int count = atomicAdd(&p.counter->total_light_cache_count, 0);
+      uint32_t lit = min((uint32_t)count, p.max_caches);
+      p.counter->groups_x = (lit + DRV_LIGHTING_THREADS_PER_GROUP - 1) / DRV_LIGHTING_THREADS_PER_GROUP;
+      p.counter->groups_y = 1;
+      p.counter->groups_z = 1;
+    }
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_allocate(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const DrvPerFrame& f,
+                            const float* depth, int w, int h, uint32_t* atlas, void* entries, uint32_t entry_stride,
+                            DrvCacheCounter* counter, uint32_t* ticket, uint32_t* err) {
+  AllocParams p;
+  p.vol = vol;
+  p.frame = f;
+  p.depth = depth;
+  p.w = w;
+  p.h = h;
+  p.res = cfg.cav_res;
+  p.n_cascades = cfg.n_cascades;
+  p.transitions = cfg.cascade_transition > 0.0f;
+  p.max_caches = cfg.max_caches;
+  p.atlas = atlas;
+  p.entries = (float4*)entries;
+  p.entry_vec4 = (int)(entry_stride / 16);
+  p.counter = counter;
+  p.ticket = ticket;
+  p.err = err;
+  dim3 block(kTile, kTile), grid((w + kTile - 1) / kTile, (h + kTile - 1) / kTile);
+  allocate_kernel<<<grid, block, 0, s>>>(p);
+  return cudaGetLastError();
+}
+
+}  // namespace drv

@@ -1,0 +1,158 @@
+// k_apply.cu — Renderer::ApplyCaches (renderer.cpp:1047-1079) / cacheApply.frag:
+// per pixel, trilinear interpolation of the irradiance of the 8 surrounding
+// light caches (SampleCacheIrradiance, lightcache.glsl:137-179) times
+// albedo / pi, with the optional cascade-transition blend.
+//
+// The reference reads the atlas and the entries without bounds checks
+// (cacheApply.frag:264-284); here a corner outside the atlas, or whose slot is
+// 0 (never allocated) or 0xFFFFFFFF (locked by a capacity overflow),
+// contributes zero irradiance and its weight is not redistributed.
+#include <cmath>
+
+#include "drv_device.cuh"
+#include "drv_internal.h"
+
+namespace drv {
+namespace {
+
+struct ApplyParams {
+  DrvVolumeInfo vol;
+  DrvPerFrame frame;
+  const float* depth;
+  const void* normal;
+  int normal_format;
+  const float* albedo;
+  int w, h;
+  int res, n_cascades, transitions, sh2;
+  const uint32_t* atlas;
+  const float* entries;
+  int stride_floats;
+  const DrvCacheCounter* counter;
+  uint32_t max_caches;
+  float cl[5];  // ShCosLobeFactor0, 1, 2n2_p1_n1, 20, 2p2
+  float* out;
+};
+
+__device__ __forceinline__ f3 lighting(const ApplyParams& p, const float wp[3], int c, f3 n, uint32_t n_caches) {
+  const DrvCascade& k = p.vol.cascades[c];
+  float a[3];
+  int a0[3];
+  float t[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    a[i] = __fdiv_rn(__fsub_rn(wp[i], k.min[i]), k.world_voxel_size);
+    a0[i] = __float2int_rz(fminf(fmaxf(a[i], -1e9f), 1e9f));
+    t[i] = a[i] - (float)a0[i];
+  }
+  const int aw = p.n_cascades * p.res;
+  // Per-normal factors of SampleCacheIrradiance.
+  const float f0 = p.cl[0];
+  const float f1y = p.cl[1] * n.y, f1z = p.cl[1] * n.z, f1x = p.cl[1] * n.x;
+  const float f4 = p.cl[2] * n.x * n.y, f5 = p.cl[2] * n.y * n.z, f6 = p.cl[3] * (n.z * n.z * 3.0f - 1.0f);
+  const float f7 = p.cl[2] * n.x * n.z, f8 = p.cl[4] * (n.x * n.x - n.y * n.y);
+  f3 irr = mkf3(0.f, 0.f, 0.f);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    // Corner order of cacheApply.frag:219-230: x fastest.
+    const int ox = i & 1, oy = (i >> 1) & 1, oz = i >> 2;
+    const float w = (ox ? t[0] : 1.0f - t[0]) * (oy ? t[1] : 1.0f - t[1]) * (oz ? t[2] : 1.0f - t[2]);
+    const int x = a0[0] + ox + p.res * c, y = a0[1] + oy, z = a0[2] + oz;
+    if (x < 0 || y < 0 || z < 0 || x >= aw || y >= p.res || z >= p.res) continue;
+    const uint32_t addr = __ldg(p.atlas + ((size_t)z * p.res + y) * aw + x);
+    if (addr == 0u || addr > n_caches) continue;  // also rejects 0xFFFFFFFF
+    const float4* e = reinterpret_cast<const float4*>(p.entries + (size_t)(addr - 1u) * p.stride_floats);
+    const float4 q1 = __ldg(e + 1), q2 = __ldg(e + 2), q3 = __ldg(e + 3);
+    // q1 = {SH1neg1, SH00_r}, q2 = {SH10, SH00_g}, q3 = {SH1pos1, SH00_b}
+    float er = q1.w * f0 - q1.x * f1y + q2.x * f1z - q3.x * f1x;
+    float eg = q2.w * f0 - q1.y * f1y + q2.y * f1z - q3.y * f1x;
+    float eb = q3.w * f0 - q1.z * f1y + q2.z * f1z - q3.z * f1x;
+    if (p.sh2) {
+      const float4 q4 = __ldg(e + 4), q5 = __ldg(e + 5), q6 = __ldg(e + 6), q7 = __ldg(e + 7);
+      // q4 = {SH2neg2, SH20_r}, q5 = {SH2neg1, SH20_g}, q6 = {SH2pos1, SH20_b}, q7 = {SH2pos2, pad}
+      er += -q4.x * f4 + q5.x * f5 + q4.w * f6 + q6.x * f7 + q7.x * f8;
+      eg += -q4.y * f4 + q5.y * f5 + q5.w * f6 + q6.y * f7 + q7.y * f8;
+      eb += -q4.z * f4 + q5.z * f5 + q6.w * f6 + q6.z * f7 + q7.z * f8;
+    }
+    irr.x += fmaxf(er, 0.0f) * w;
+    irr.y += fmaxf(eg, 0.0f) * w;
+    irr.z += fmaxf(eb, 0.0f) * w;
+  }
+  return irr;
+}
+
+__global__ void __launch_bounds__(256) apply_kernel(ApplyParams p) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= p.w || y >= p.h) return;
+  const size_t i = (size_t)y * p.w + x;
+  float* o = p.out + 3 * i;
+  const float d = __ldg(p.depth + i);
+  if (d < 0.00001f) {  // cacheApply.frag:304-307 (discard)
+    o[0] = o[1] = o[2] = 0.0f;
+    return;
+  }
+  const uint32_t n_caches = min((uint32_t)max(p.counter->total_light_cache_count, 0), p.max_caches);
+  float wp[3];
+  reconstruct_world(p.frame, x, y, p.w, p.h, d, wp);
+  const int c = select_cascade(p.vol, p.n_cascades, wp);
+  f3 n;
+  if (p.normal_format == DRV_NORMAL_RG16I) {
+    const int16_t* q = reinterpret_cast<const int16_t*>(p.normal) + 2 * i;
+    n = unpack_normal16i(q[0], q[1]);
+  } else {
+    const float* q = reinterpret_cast<const float*>(p.normal) + 3 * i;
+    n = mkf3(q[0], q[1], q[2]);
+  }
+  const float inv_pi = 1.0f / DRV_SHADER_PI;
+  const f3 alb = mkf3(__ldg(p.albedo + 3 * i) * inv_pi, __ldg(p.albedo + 3 * i + 1) * inv_pi,
+                      __ldg(p.albedo + 3 * i + 2) * inv_pi);
+  f3 irr = lighting(p, wp, c, n, n_caches);
+  f3 col = mkf3(irr.x * alb.x, irr.y * alb.y, irr.z * alb.z);
+  if (p.transitions) {
+    const float t = cascade_transition(p.vol, c, wp);
+    if (t > 0.0f && c < p.n_cascades - 1) {
+      f3 irr2 = lighting(p, wp, c + 1, n, n_caches);
+      f3 col2 = mkf3(irr2.x * alb.x, irr2.y * alb.y, irr2.z * alb.z);
+      col = col * (1.0f - t) + col2 * t;  // mix(), cacheApply.frag:359
+    }
+  }
+  o[0] = col.x;
+  o[1] = col.y;
+  o[2] = col.z;
+}
+
+}  // namespace
+
+cudaError_t launch_apply(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const DrvPerFrame& f,
+                         const DrvGBufferView& g, const uint32_t* atlas, const void* entries, uint32_t entry_stride,
+                         const DrvCacheCounter* counter, float* out_rgb) {
+  ApplyParams p;
+  p.vol = vol;
+  p.frame = f;
+  p.depth = g.depth;
+  p.normal = g.normal;
+  p.normal_format = g.normal_format;
+  p.albedo = g.albedo;
+  p.w = g.width;
+  p.h = g.height;
+  p.res = cfg.cav_res;
+  p.n_cascades = cfg.n_cascades;
+  p.transitions = cfg.cascade_transition > 0.0f;
+  p.sh2 = cfg.sh_order == 2;
+  p.atlas = atlas;
+  p.entries = (const float*)entries;
+  p.stride_floats = (int)(entry_stride / 4);
+  p.counter = counter;
+  p.max_caches = cfg.max_caches;
+  const double kPi = 3.14159265358979323846;
+  p.cl[0] = (float)(std::sqrt(kPi) / 2.0);
+  p.cl[1] = (float)std::sqrt(kPi / 3.0);
+  p.cl[2] = (float)((cfg.sh2_sign == DRV_SH2_SIGN_FIXED ? 1.0 : -1.0) * std::sqrt(15.0 * kPi) / 8.0);
+  p.cl[3] = (float)(std::sqrt(5.0 * kPi) / 16.0);
+  p.cl[4] = (float)(std::sqrt(15.0 * kPi) / 16.0);
+  p.out = out_rgb;
+  dim3 block(16, 16), grid((g.width + 15) / 16, (g.height + 15) / 16);
+  apply_kernel<<<grid, block, 0, s>>>(p);
+  return cudaGetLastError();
+}
+
+}  // namespace drv

@@ -1,0 +1,202 @@
+// k_voxel.cu — VoxelizeScene (voxelization.cpp:90-142, voxelize.{vert,geom,frag})
+// for the procedural box scene, and the opacity mip chain (voxelmipmap.comp:8-13,
+// voxelization.cpp:155-172).
+//
+// Level 0 is a binary surface-voxel grid stored as a bitmask (bit x&31 of
+// word ((z*N + y)*N + x) / 32). Levels 1..L are FP32 means of their 8
+// children; every level is an exact dyadic rational (count / 8^l with
+// 8^l <= 2^24 for N <= 256), so FP32 holds them exactly.
+#include "drv_device.cuh"
+#include "drv_internal.h"
+
+namespace drv {
+namespace {
+
+constexpr int kMaxBoxes = 512;
+
+struct Face {
+  int16_t axis, k, u0, u1, v0, v1;
+};
+
+// Face rectangle -> covered voxel ranges (binary32 mirror). For an
+// axis-aligned face the dominant axis is its normal axis and the
+// conservative raster (voxelize.geom:201-225 + voxelize.frag:280-283) covers
+// every voxel square that touches the closed rectangle; the depth gradient is
+// zero, so the +-1 depth voxels of voxelize.frag:295-313 never trigger.
+__device__ __forceinline__ bool make_face(const DrvBox& b, int axis, int side, const float* vm, float vs, int N,
+                                          Face& f) {
+  int ua = (axis + 1) % 3, va = (axis + 2) % 3;
+  float plane = side ? b.max[axis] : b.min[axis];
+  float kc = __fdiv_rn(__fsub_rn(plane, vm[axis]), vs);
+  if (!(kc >= 0.0f) || !(kc < (float)N)) return false;
+  float lu = __fdiv_rn(__fsub_rn(b.min[ua], vm[ua]), vs), hu = __fdiv_rn(__fsub_rn(b.max[ua], vm[ua]), vs);
+  float lv = __fdiv_rn(__fsub_rn(b.min[va], vm[va]), vs), hv = __fdiv_rn(__fsub_rn(b.max[va], vm[va]), vs);
+  int u0 = max(0, (int)ceilf(lu) - 1), u1 = min(N - 1, (int)floorf(hu));
+  int v0 = max(0, (int)ceilf(lv) - 1), v1 = min(N - 1, (int)floorf(hv));
+  if (u0 > u1 || v0 > v1) return false;
+  f.axis = (int16_t)axis;
+  f.k = (int16_t)(int)kc;
+  f.u0 = (int16_t)u0;
+  f.u1 = (int16_t)u1;
+  f.v0 = (int16_t)v0;
+  f.v1 = (int16_t)v1;
+  return true;
+}
+
+__device__ __forceinline__ uint32_t range_mask(int lo, int hi, int base) {
+  // bits [lo, hi] of the 32-voxel run starting at x = base
+  int a = max(lo, base), b = min(hi, base + 31);
+  if (a > b) return 0u;
+  int n = b - a + 1;
+  uint32_t m = n == 32 ? 0xFFFFFFFFu : ((1u << n) - 1u);
+  return m << (a - base);
+}
+
+// One CTA per z-slab: gather the faces that touch the slab, then every thread
+// writes whole 32-voxel words (each word once, coalesced).
+__global__ void __launch_bounds__(256) voxelize_kernel(const DrvBox* __restrict__ boxes, int n_boxes, DrvVolumeInfo vol,
+                                                       int N, uint32_t* __restrict__ bits) {
+  __shared__ Face faces[kMaxBoxes * 6];
+  __shared__ int n_faces;
+  const int z = blockIdx.x;
+  if (threadIdx.x == 0) n_faces = 0;
+  __syncthreads();
+  for (int f = threadIdx.x; f < n_boxes * 6; f += blockDim.x) {
+    Face fc;
+    if (!make_face(boxes[f / 6], (f % 6) >> 1, f & 1, vol.volume_world_min, vol.voxel_size_in_world, N, fc)) continue;
+    bool touches = (fc.axis == 2 && fc.k == z) || (fc.axis == 0 && z >= fc.v0 && z <= fc.v1) ||
+                   (fc.axis == 1 && z >= fc.u0 && z <= fc.u1);
+    if (touches) faces[atomicAdd(&n_faces, 1)] = fc;
+  }
+  __syncthreads();
+  const int wpr = N / 32;  // words per row
+  const int nf = n_faces;
+  for (int w = threadIdx.x; w < N * wpr; w += blockDim.x) {
+    int y = w / wpr, base = (w % wpr) * 32;
+    uint32_t m = 0u;
+    for (int f = 0; f < nf; ++f) {
+      Face fc = faces[f];
+      if (fc.axis == 2) {  // plane z = k: x in [u0,u1], y in [v0,v1]
+        if (y >= fc.v0 && y <= fc.v1) m |= range_mask(fc.u0, fc.u1, base);
+      } else if (fc.axis == 0) {  // plane x = k: y in [u0,u1], z in [v0,v1]
+        if (y >= fc.u0 && y <= fc.u1) m |= range_mask(fc.k, fc.k, base);
+      } else {  // plane y = k: z in [u0,u1], x in [v0,v1]
+        if (y == fc.k) m |= range_mask(fc.v0, fc.v1, base);
+      }
+    }
+    bits[((size_t)z * N + y) * wpr + (w % wpr)] = m;
+  }
+}
+
+struct MipOffsets {
+  size_t off[kMaxVoxelLevels];
+};
+
+// Fused mips over one B^3 level-0 block (B = min(32, N)): levels 1..log2(B)
+// computed in shared memory from one read of the block's bits.
+__global__ void __launch_bounds__(256) mips_kernel(int N, int B, const uint32_t* __restrict__ bits,
+                                                   float* __restrict__ mips, MipOffsets mo) {
+  __shared__ uint32_t sbits[32 * 32];  // B rows x B slices of (B <= 32)-voxel runs
+  __shared__ float lv[2][16 * 16 * 16];
+  const int nbx = N / B;
+  const int bx = blockIdx.x % nbx, by = (blockIdx.x / nbx) % nbx, bz = blockIdx.x / (nbx * nbx);
+  for (int i = threadIdx.x; i < B * B; i += blockDim.x) {
+    int y = i % B, z = i / B;
+    int gx = bx * B, gy = by * B + y, gz = bz * B + z;
+    size_t bit = ((size_t)gz * N + gy) * N + gx;
+    uint32_t word = bits[bit >> 5];
+    sbits[i] = B == 32 ? word : ((word >> (bit & 31)) & ((1u << B) - 1u));
+  }
+  __syncthreads();
+  // Level 1 from bits.
+  int n = B / 2;
+  for (int i = threadIdx.x; i < n * n * n; i += blockDim.x) {
+    int x = i % n, y = (i / n) % n, z = i / (n * n);
+    int c = 0;
+#pragma unroll
+    for (int dz = 0; dz < 2; ++dz)
+#pragma unroll
+      for (int dy = 0; dy < 2; ++dy) {
+        uint32_t w = sbits[(2 * z + dz) * B + (2 * y + dy)];
+        c += __popc((w >> (2 * x)) & 3u);
+      }
+    float v = (float)c * 0.125f;
+    lv[0][i] = v;
+    int gn = N / 2;
+    size_t g = ((size_t)(bz * n + z) * gn + (by * n + y)) * gn + (bx * n + x);
+    mips[mo.off[1] + g] = v;
+  }
+  __syncthreads();
+  // Levels 2 .. log2(B).
+  int cur = 0, level = 1;
+  for (int m = n / 2; m >= 1; m /= 2) {
+    ++level;
+    for (int i = threadIdx.x; i < m * m * m; i += blockDim.x) {
+      int x = i % m, y = (i / m) % m, z = i / (m * m);
+      int p = 2 * m;
+      float s = 0.0f;
+#pragma unroll
+      for (int dz = 0; dz < 2; ++dz)
+#pragma unroll
+        for (int dy = 0; dy < 2; ++dy)
+#pragma unroll
+          for (int dx = 0; dx < 2; ++dx) s += lv[cur][((2 * z + dz) * p + (2 * y + dy)) * p + (2 * x + dx)];
+      float v = s * 0.125f;
+      lv[cur ^ 1][i] = v;
+      int gn = N >> level;
+      size_t g = ((size_t)(bz * m + z) * gn + (by * m + y)) * gn + (bx * m + x);
+      mips[mo.off[level] + g] = v;
+    }
+    __syncthreads();
+    cur ^= 1;
+  }
+}
+
+// Remaining levels above log2(B), from the level written by mips_kernel.
+__global__ void __launch_bounds__(256) mips_tail_kernel(int N, int first_level, int last_level, float* __restrict__ mips,
+                                                        MipOffsets mo) {
+  for (int level = first_level; level <= last_level; ++level) {
+    int m = N >> level, p = m * 2;
+    const float* src = mips + mo.off[level - 1];
+    float* dst = mips + mo.off[level];
+    for (int i = threadIdx.x; i < m * m * m; i += blockDim.x) {
+      int x = i % m, y = (i / m) % m, z = i / (m * m);
+      float s = 0.0f;
+      for (int dz = 0; dz < 2; ++dz)
+        for (int dy = 0; dy < 2; ++dy)
+          for (int dx = 0; dx < 2; ++dx) s += src[((size_t)(2 * z + dz) * p + (2 * y + dy)) * p + (2 * x + dx)];
+      dst[i] = s * 0.125f;
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_voxelize(cudaStream_t s, const DrvBox* boxes, int n_boxes, const DrvVolumeInfo& vol, int n,
+                            uint32_t* bits) {
+  if (n_boxes > kMaxBoxes || n < 32 || (n & 31)) return cudaErrorInvalidValue;
+  voxelize_kernel<<<n, 256, 0, s>>>(boxes, n_boxes, vol, n, bits);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_build_mips(cudaStream_t s, int n, const uint32_t* bits, float* mips, const size_t* offsets,
+                              int n_levels) {
+  MipOffsets mo{};
+  for (int i = 0; i < n_levels && i < kMaxVoxelLevels; ++i) mo.off[i] = offsets[i];
+  int B = n < 32 ? n : 32;
+  int lb = 0;
+  while ((1 << (lb + 1)) <= B) ++lb;
+  int blocks = (n / B) * (n / B) * (n / B);
+  mips_kernel<<<blocks, 256, 0, s>>>(n, B, bits, mips, mo);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  int L = n_levels - 1;
+  if (L > lb) {
+    mips_tail_kernel<<<1, 256, 0, s>>>(n, lb + 1, L, mips, mo);
+    e = cudaGetLastError();
+  }
+  return e;
+}
+
+}  // namespace drv

@@ -1,0 +1,265 @@
+"""Workloads and a thin host driver over the C ABI.
+
+`Workload` names a synthetic, seeded scene configuration (the reference's
+assimp scenes are replaced by a procedural box room). `Pipeline` owns one
+DrvContext plus the device buffers of one frame's inputs (G-buffer, RSMs) and
+output, and calls the stage entry points in the order of the reference's
+Renderer::Draw. Device memory is allocated through torch (plumbing only);
+every computation is a kernel of libdrv_gb300.so.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass, replace
+
+from . import abi, check, load
+
+
+@dataclass(frozen=True)
+class Workload:
+    name: str
+    width: int
+    height: int
+    n_boxes: int
+    voxel_res: int
+    n_lights: int
+    rsm_resolution: int
+    rsm_read_lod: int
+    shadow_lod: int
+    n_cascades: int
+    cascade_world_size0: float
+    cav_res: int
+    sh_order: int
+    max_cone_steps: int
+    max_caches: int
+    cascade_transition: float = 2.0
+    indirect_shadow: int = 1
+    seed: int = 1
+    box_size: tuple = (0.05, 0.3)
+    albedo: tuple = (0.2, 0.9)
+
+    @property
+    def n_vpls(self) -> int:
+        r = self.rsm_resolution >> self.rsm_read_lod
+        return self.n_lights * r * r
+
+
+WORKLOADS = {
+    # Plain method, small: 256^2 G-buffer, 12 boxes, 64^3 voxels, one spot
+    # light with a 32^2 RSM (1024 VPLs), one 32^3 cascade, SH1, 16 cone steps.
+    "c1_small": Workload("c1_small", 256, 256, 12, 64, 1, 32, 0, 0, 1, 2.0, 32, 1, 16, 65536,
+                         cascade_transition=0.0),
+    # Plain method at production size: 1920x1080, 64 boxes, 256^3 voxels,
+    # 3 lights x 512^2 RSM read at 64^2 (12288 VPLs), 4 cascades of 32^3, SH2,
+    # up to 32 cone steps, one cone per VPL-cache pair.
+    "c2_production": Workload("c2_production", 1920, 1080, 64, 256, 3, 512, 3, 0, 4, 0.25, 32, 2, 32, 262144),
+    # The headline case: C2 with one light (4096 VPLs) at 1080p.
+    "ns_1080p_4096": Workload("ns_1080p_4096", 1920, 1080, 64, 256, 1, 512, 3, 0, 4, 0.25, 32, 2, 32, 262144),
+}
+
+
+def make_config(w: Workload) -> abi.DrvConfig:
+    lib = load()
+    cfg = abi.DrvConfig()
+    lib.drv_default_config(C.byref(cfg))
+    cfg.width, cfg.height = w.width, w.height
+    cfg.sh_order = w.sh_order
+    cfg.indirect_shadow = w.indirect_shadow
+    cfg.max_cone_steps = w.max_cone_steps
+    cfg.cascade_transition = w.cascade_transition
+    cfg.n_cascades = w.n_cascades
+    cfg.cav_res = w.cav_res
+    for c in range(abi.MAX_CASCADES):
+        cfg.cascade_world_size[c] = w.cascade_world_size0 * (2.0 ** c)
+    cfg.voxel_res = w.voxel_res
+    cfg.max_caches = w.max_caches
+    cfg.max_lights = w.n_lights
+    cfg.max_rsm_resolution = w.rsm_resolution
+    return cfg
+
+
+@dataclass
+class HostFrame:
+    """Host-side description of one frame: scene, camera, lights, UBO mirrors."""
+    workload: Workload
+    config: abi.DrvConfig
+    boxes: C.Array
+    scene: abi.DrvScene
+    camera: abi.DrvCamera
+    frame: abi.DrvPerFrame
+    light_descs: list
+    lights: C.Array
+    volume: abi.DrvVolumeInfo
+
+
+def host_frame(w: Workload, seed: int | None = None) -> HostFrame:
+    lib = load()
+    seed = w.seed if seed is None else seed
+    cfg = make_config(w)
+    boxes = (abi.DrvBox * (w.n_boxes + 1))()
+    scene = abi.DrvScene()
+    check(lib.drv_generate_scene(seed, w.n_boxes, w.box_size[0], w.box_size[1], w.albedo[0], w.albedo[1], boxes,
+                                 C.byref(scene)))
+    cam = abi.DrvCamera()
+    check(lib.drv_generate_camera(seed, C.byref(scene), w.width / w.height, C.byref(cam)))
+    frame = abi.DrvPerFrame()
+    check(lib.drv_prepare_camera(C.byref(cam), C.byref(frame)))
+    descs = []
+    lights = (abi.DrvSpotLight * w.n_lights)()
+    for l in range(w.n_lights):
+        d = abi.DrvLightDesc()
+        check(lib.drv_generate_light(seed * 31 + l, C.byref(scene), w.rsm_resolution, w.rsm_read_lod, w.shadow_lod,
+                                     C.byref(d)))
+        check(lib.drv_prepare_light(C.byref(d), C.byref(lights[l])))
+        descs.append(d)
+    vol = abi.DrvVolumeInfo()
+    check(lib.drv_compute_volume_info(C.byref(cfg), scene.aabb_min, scene.aabb_max, cam.position, C.byref(vol)))
+    return HostFrame(w, cfg, boxes, scene, cam, frame, descs, lights, vol)
+
+
+class Pipeline:
+    """One DrvContext + device buffers for one frame of a workload."""
+
+    def __init__(self, hf: HostFrame, device: str = "cuda", normal_format: int = abi.NORMAL_RG16I):
+        import torch
+        self.torch = torch
+        self.lib = load()
+        self.hf = hf
+        w = hf.workload
+        self.device = torch.device(device)
+        self.ctx = C.c_void_p()
+        check(self.lib.drv_create(C.byref(hf.config), C.byref(self.ctx)))
+        self.stream = torch.cuda.current_stream(self.device)
+        check(self.lib.drv_set_stream(self.ctx, C.c_void_p(self.stream.cuda_stream)), self.ctx)
+        H, W = w.height, w.width
+        dev = self.device
+        self.depth = torch.zeros((H, W), dtype=torch.float32, device=dev)
+        self.normal16 = torch.zeros((H, W, 2), dtype=torch.int16, device=dev)
+        self.normal32 = torch.zeros((H, W, 3), dtype=torch.float32, device=dev)
+        self.albedo = torch.zeros((H, W, 3), dtype=torch.float32, device=dev)
+        self.out = torch.zeros((H, W, 3), dtype=torch.float32, device=dev)
+        R = w.rsm_resolution
+        self.rsm_flux = [torch.zeros((R, R, 3), dtype=torch.float32, device=dev) for _ in range(w.n_lights)]
+        self.rsm_normal = [torch.zeros((R, R, 2), dtype=torch.int16, device=dev) for _ in range(w.n_lights)]
+        self.rsm_dls = [torch.zeros((R, R, 2), dtype=torch.float32, device=dev) for _ in range(w.n_lights)]
+        self.normal_format = normal_format
+        self.gview = abi.DrvGBufferView(W, H, self.depth.data_ptr(),
+                                        (self.normal16 if normal_format == abi.NORMAL_RG16I else self.normal32).data_ptr(),
+                                        normal_format, self.albedo.data_ptr())
+        self.rsm_views = (abi.DrvRSMView * w.n_lights)()
+        for l in range(w.n_lights):
+            self.rsm_views[l] = abi.DrvRSMView(R, self.rsm_flux[l].data_ptr(), self.rsm_normal[l].data_ptr(),
+                                               self.rsm_dls[l].data_ptr())
+
+    def close(self):
+        if self.ctx:
+            self.lib.drv_destroy(self.ctx)
+            self.ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _c(self, st):
+        check(st, self.ctx)
+
+    # -- input producers (the reference's raster passes) --------------------
+    def raycast_inputs(self):
+        hf, lib = self.hf, self.lib
+        out = abi.DrvGBufferOut(self.depth.data_ptr(), self.normal16.data_ptr(), self.normal32.data_ptr(),
+                                self.albedo.data_ptr())
+        self._c(lib.drv_raycast_gbuffer(self.ctx, C.byref(hf.scene), C.byref(hf.camera), C.byref(hf.frame),
+                                        hf.workload.width, hf.workload.height, C.byref(out)))
+        for l in range(hf.workload.n_lights):
+            ro = abi.DrvRSMOut(self.rsm_flux[l].data_ptr(), self.rsm_normal[l].data_ptr(), self.rsm_dls[l].data_ptr())
+            self._c(lib.drv_raycast_rsm(self.ctx, C.byref(hf.scene), C.byref(hf.lights[l]), C.byref(ro)))
+
+    # -- stages ---------------------------------------------------------------
+    def prepare_and_extract(self):
+        for l in range(self.hf.workload.n_lights):
+            self._c(self.lib.drv_prepare_rsm(self.ctx, l, C.byref(self.hf.lights[l]), C.byref(self.rsm_views[l])))
+            self._c(self.lib.drv_extract_vpls(self.ctx, l, C.byref(self.hf.lights[l])))
+
+    def voxelize(self):
+        self._c(self.lib.drv_voxelize(self.ctx, C.byref(self.hf.scene), C.byref(self.hf.volume)))
+        self._c(self.lib.drv_build_opacity_mips(self.ctx))
+
+    def allocate(self):
+        self._c(self.lib.drv_allocate_caches(self.ctx, C.byref(self.gview), C.byref(self.hf.frame),
+                                             C.byref(self.hf.volume)))
+
+    def light(self):
+        self._c(self.lib.drv_light_caches(self.ctx, self.hf.lights, self.hf.workload.n_lights,
+                                          C.byref(self.hf.volume), C.byref(self.hf.frame)))
+
+    def apply(self, out=None):
+        out = self.out if out is None else out
+        self._c(self.lib.drv_apply(self.ctx, C.byref(self.gview), C.byref(self.hf.frame), C.byref(self.hf.volume),
+                                   C.c_void_p(out.data_ptr())))
+
+    def frame(self, out=None):
+        out = self.out if out is None else out
+        self._c(self.lib.drv_frame(self.ctx, C.byref(self.hf.scene), C.byref(self.gview), C.byref(self.hf.frame),
+                                   C.byref(self.hf.volume), self.hf.lights, self.rsm_views, self.hf.workload.n_lights,
+                                   C.c_void_p(out.data_ptr())))
+
+    def sync(self):
+        self._c(self.lib.drv_sync(self.ctx))
+
+    def cache_count(self) -> int:
+        n = C.c_uint32()
+        self._c(self.lib.drv_get_cache_count(self.ctx, C.byref(n)))
+        return n.value
+
+    def buffers(self) -> abi.DrvBuffers:
+        b = abi.DrvBuffers()
+        self._c(self.lib.drv_get_buffers(self.ctx, C.byref(b)))
+        return b
+
+    # -- device buffer readback (tests) -------------------------------------
+    def _dev_tensor(self, ptr: int, numel: int, dtype):
+        """Copies `numel` elements at device address `ptr` into a new tensor."""
+        torch = self.torch
+        typestr = {torch.float32: "<f4", torch.int32: "<i4", torch.int16: "<i2", torch.uint8: "|u1"}[dtype]
+
+        class _View:
+            __cuda_array_interface__ = {"shape": (numel,), "typestr": typestr, "data": (int(ptr), False),
+                                        "version": 3, "strides": None}
+
+        torch.cuda.synchronize(self.device)
+        return torch.as_tensor(_View(), device=self.device).clone()
+
+    def read_entries(self, count: int):
+        b = self.buffers()
+        floats = b.entry_stride // 4
+        return self._dev_tensor(b.cache_entries, count * floats, self.torch.float32).view(count, floats)
+
+    def read_atlas(self):
+        w = self.hf.workload
+        b = self.buffers()
+        n = w.n_cascades * w.cav_res ** 3
+        return self._dev_tensor(b.cav_atlas, n, self.torch.int32).view(w.cav_res, w.cav_res, w.n_cascades * w.cav_res)
+
+    def read_voxel_bits(self):
+        N = self.hf.workload.voxel_res
+        return self._dev_tensor(self.buffers().voxel_bits, N ** 3 // 32, self.torch.int32)
+
+    def read_mip(self, level: int):
+        N = self.hf.workload.voxel_res
+        n = N >> level
+        return self._dev_tensor(self.buffers().voxel_mips[level], n ** 3, self.torch.float32).view(n, n, n)
+
+    def read_vpls(self, light: int):
+        b = self.buffers()
+        return self._dev_tensor(b.vpls[light], b.n_vpls[light] * 12, self.torch.float32).view(-1, 12)
+
+    def read_cones(self, light: int, n: int):
+        b = self.buffers()
+        return self._dev_tensor(b.cones[light], n * 4, self.torch.float32).view(-1, 4)
+
+
+def scaled(w: Workload, **kw) -> Workload:
+    return replace(w, **kw)

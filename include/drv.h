@@ -1,0 +1,365 @@
+/*
+ * drv.h — C ABI of the GB300 dynamic-radiance-volume indirect-lighting path.
+ *
+ * The path is the per-frame stage sequence of Wumpf/DynamicRadianceVolume's
+ * `Renderer::Draw` (DynamicRadianceVolume/rendering/renderer.cpp:539-594):
+ *
+ *   RSM downsample + VPL extraction  (downsamplersm.frag, cacheLightingRSM.comp:135-163)
+ *   VoxelizeScene + opacity mips     (voxelization.cpp:90-176, voxelize.*, voxelmipmap.comp)
+ *   AllocateCaches                   (renderer.cpp:951-992, cacheGather.comp, cachePrepareLighting.comp)
+ *   LightCachesRSM                   (renderer.cpp:899-933, cacheLightingRSM.comp)
+ *   ApplyCaches                      (renderer.cpp:1047-1079, cacheApply.frag, lightcache.glsl:137-183)
+ *
+ * In the reference these are private `Renderer` methods driving GLSL
+ * programs; here each is an `extern "C"` entry point over plain device
+ * pointers, asynchronous on the context's CUDA stream. No function throws;
+ * every function returns a drv_status. Device-side failures (cache capacity
+ * overflow, bounded waits that ran out) are latched into a device error word
+ * and surface from drv_sync / drv_get_cache_count / drv_get_error.
+ *
+ * Conventions (the reference's, see each struct):
+ *  - 4x4 matrices are 16 floats, row-major, applied as M * v (column vector).
+ *    This equals the reference's GLSL `vec4 * mat4` with row-major ei::Mat4x4
+ *    uploaded as-is (e.g. cacheGather.comp:118).
+ *  - Images are row-major, x fastest; row 0 is the bottom row (GL texture
+ *    origin). 3D images are x fastest, then y, then z.
+ *  - Depth is reversed-Z in [0,1] (0 = cleared/far, renderer.cpp:113-117).
+ */
+#ifndef DRV_H_
+#define DRV_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DRV_ABI_VERSION 1
+#define DRV_MAX_CASCADES 4   /* MAX_NUM_ADDRESS_VOLUME_CASCADES, globalubos.glsl:43 */
+#define DRV_MAX_LIGHTS 16    /* maxExpectedLights, renderer.cpp:80 */
+#define DRV_LIGHTING_THREADS_PER_GROUP 64 /* lightcache.glsl:95 */
+
+typedef enum drv_status {
+  DRV_OK = 0,
+  DRV_ERR_INVALID_ARG = 1,
+  DRV_ERR_CAPACITY = 2,   /* more caches requested than DrvConfig.max_caches */
+  DRV_ERR_CUDA = 3,
+  DRV_ERR_TIMEOUT = 4,    /* a bounded device-side wait gave up */
+  DRV_ERR_NOT_SUPPORTED = 5,
+  DRV_ERR_NUMERIC = 6     /* non-finite value found in an input */
+} drv_status;
+
+/* Device error-word bits (drv_get_error). */
+#define DRV_DEVERR_CAPACITY 0x1u
+#define DRV_DEVERR_TIMEOUT 0x2u
+#define DRV_DEVERR_BOUNDS 0x4u
+
+typedef enum drv_sh2_sign {
+  /* Host constants exactly as renderer.cpp:296-300 uploads them
+   * (ShCosLobeFactor2n2_p1_n1 = -sqrt(15 pi)/8). */
+  DRV_SH2_SIGN_REFERENCE = 0,
+  /* Mathematically correct band-2 cosine-lobe factor (+sqrt(15 pi)/8). */
+  DRV_SH2_SIGN_FIXED = 1
+} drv_sh2_sign;
+
+typedef enum drv_precision {
+  DRV_PRECISION_FP32 = 0,      /* FP32 storage, FP32 accumulation */
+  DRV_PRECISION_BF16 = 1       /* BF16 VPL flux/normal + cache SH, FP16 mips, Kahan FP32 accumulation */
+} drv_precision;
+
+typedef enum drv_visibility {
+  DRV_VISIBILITY_CONE = 0,      /* voxel cone trace, cacheLightingRSM.comp:167-232 */
+  DRV_VISIBILITY_SURROGATE = 1  /* BF16 MLP surrogate with cone-trace fallback */
+} drv_visibility;
+
+typedef enum drv_normal_format {
+  DRV_NORMAL_RG16I = 0,   /* PackNormal16I, utils.glsl:83-89 (reference layout) */
+  DRV_NORMAL_F32X3 = 1
+} drv_normal_format;
+
+/* Compile-time specialisations and setters of the reference's Renderer
+ * (renderer.hpp:63-142, renderer.cpp:197-246). */
+typedef struct DrvConfig {
+  int32_t width, height;            /* BackbufferResolution */
+  int32_t sh_order;                 /* 1: INDDIFFUSE_VIA_SH1, 2: INDDIFFUSE_VIA_SH2 */
+  int32_t indirect_shadow;          /* INDIRECT_SHADOW */
+  int32_t max_cone_steps;           /* cone loop bound, 32 in cacheLightingRSM.comp:211 */
+  float cascade_transition;         /* CAVTransitionZoneSize; <= 0 disables ADDRESSVOL_CASCADE_TRANSITIONS */
+  int32_t n_cascades;               /* 1..4 */
+  int32_t cav_res;                  /* AddressVolumeResolution */
+  float cascade_world_size[DRV_MAX_CASCADES]; /* m_CAVCascadeWorldSize */
+  int32_t voxel_res;                /* VoxelResolution (power of two) */
+  uint32_t max_caches;              /* MaxNumLightCaches */
+  int32_t precision;                /* drv_precision */
+  int32_t visibility;               /* drv_visibility */
+  float surrogate_conf_threshold;   /* confidence below which the cone tracer re-traces a pair */
+  int32_t sh2_sign;                 /* drv_sh2_sign */
+  int32_t max_lights;               /* lights per frame, <= DRV_MAX_LIGHTS */
+  int32_t max_rsm_resolution;       /* largest RSMRenderResolution any light will use */
+} DrvConfig;
+
+/* CAVCascade, globalubos.glsl:48-58 (std140, 64 B). */
+typedef struct DrvCascade {
+  float min[3];
+  float world_voxel_size;
+  float max[3];
+  float _pad0;
+  float decision_min[3];
+  float _pad1;
+  float decision_max[3];
+  float _pad2;
+} DrvCascade;
+
+/* VolumeInfo UBO, globalubos.glsl:62-75. */
+typedef struct DrvVolumeInfo {
+  float volume_world_min[3];
+  float voxel_size_in_world;
+  float volume_world_max[3];
+  float cav_transition_zone_size;
+  DrvCascade cascades[DRV_MAX_CASCADES];
+} DrvVolumeInfo;
+
+/* PerFrame UBO, globalubos.glsl:33-42 (the fields the path reads). */
+typedef struct DrvPerFrame {
+  float view_projection[16];
+  float inverse_view_projection[16];
+  float camera_position[3];
+  float _pad0;
+  float camera_direction[3];
+  float _pad1;
+} DrvPerFrame;
+
+/* SpotLight UBO, globalubos.glsl:85-110, filled by drv_prepare_light
+ * (Renderer::PrepareLights, renderer.cpp:664-725). */
+typedef struct DrvSpotLight {
+  float intensity[3];
+  float shadow_normal_offset;
+  float shadow_bias;
+  float position[3];
+  float direction[3];
+  float cos_half_angle;
+  float view_projection[16];
+  float inverse_view_projection[16];
+  int32_t rsm_render_resolution;
+  int32_t rsm_read_resolution;
+  float val_area_factor;
+  float indirect_shadow_lod;
+  float indirect_shadow_block_size;
+  int32_t indirect_shadow_sample_interval;
+  float indirect_shadow_super_val_width;
+  float indirect_shadow_sampling_offset;
+} DrvSpotLight;
+
+/* Light description, scene/light.hpp:8-54 (spot lights only, as the
+ * reference asserts at renderer.cpp:672). */
+typedef struct DrvLightDesc {
+  float intensity[3];
+  float position[3];
+  float direction[3];
+  float half_angle;                 /* radians */
+  uint32_t rsm_resolution;          /* power of two */
+  uint32_t rsm_read_lod;
+  uint32_t indirect_shadow_lod;
+  float near_plane, far_plane;      /* Light::nearPlane/farPlane, scene.cpp:6-7 */
+} DrvLightDesc;
+
+/* Camera (camera/camera.hpp:8-30). fov_y in degrees; the projection is
+ * DX-style reversed-Z (far and near swapped, camera.hpp:27-28). */
+typedef struct DrvCamera {
+  float position[3];
+  float direction[3];
+  float up[3];
+  float fov_y_deg;
+  float aspect;
+  float near_plane, far_plane;
+} DrvCamera;
+
+/* Procedural scene primitive: an axis-aligned box. `inward` boxes are rooms
+ * (rays hit their inside faces, normals point inward). The reference loads
+ * meshes through assimp; the procedural box scene replaces them. */
+typedef struct DrvBox {
+  float min[3];
+  float max[3];
+  float albedo[3];
+  int32_t inward;
+} DrvBox;
+
+typedef struct DrvScene {
+  int32_t n_boxes;
+  const DrvBox* boxes;              /* host pointer */
+  float aabb_min[3];                /* Scene::GetBoundingBox, scene.cpp:36-48 */
+  float aabb_max[3];
+} DrvScene;
+
+/* G-buffer (renderer.cpp:466-471), device pointers, width*height texels. */
+typedef struct DrvGBufferView {
+  int32_t width, height;
+  const float* depth;               /* D32F reversed-Z */
+  const void* normal;               /* drv_normal_format */
+  int32_t normal_format;
+  const float* albedo;              /* RGB F32 (linear) */
+} DrvGBufferView;
+
+/* Writable G-buffer for the ray-cast producer. */
+typedef struct DrvGBufferOut {
+  float* depth;
+  int16_t* normal_rg16i;            /* may be NULL */
+  float* normal_f32;                /* may be NULL */
+  float* albedo;
+} DrvGBufferOut;
+
+/* One level of a reflective shadow map (renderer.cpp:1288-1297), device
+ * pointers, resolution^2 texels: flux RGB (already divided by pi), packed
+ * normal RG16I, (distance, distance^2). */
+typedef struct DrvRSMView {
+  int32_t resolution;
+  const float* flux;
+  const int16_t* normal;
+  const float* depth_lin_sq;
+} DrvRSMView;
+
+typedef struct DrvRSMOut {
+  float* flux;
+  int16_t* normal;
+  float* depth_lin_sq;
+} DrvRSMOut;
+
+/* One virtual area light as the light stage consumes it (LightInfo,
+ * cacheLightingRSM.comp:34-40), 48 B. */
+typedef struct DrvVPL {
+  float flux[3];
+  float disc_area;
+  float position[3];
+  float _pad0;
+  float normal[3];
+  float _pad1;
+} DrvVPL;
+
+/* Per-block indirect-shadow cone source (cacheLightingRSM.comp:171-192):
+ * average VAL position and distToSphereRad. */
+typedef struct DrvShadowCone {
+  float average_val_position[3];
+  float dist_to_sphere_rad;
+} DrvShadowCone;
+
+/* Counter buffer, lightcache.glsl:83-90. */
+typedef struct DrvCacheCounter {
+  uint32_t groups_x, groups_y, groups_z;
+  int32_t total_light_cache_count;
+} DrvCacheCounter;
+
+/* Read-only views of the context's device buffers (for callers that render
+ * debug views or compare results). */
+typedef struct DrvBuffers {
+  void* cache_entries;              /* LightCacheEntry std430: 64 B (SH1) or 128 B (SH2) stride; BF16 precision: see entry_stride */
+  uint32_t entry_stride;
+  uint32_t* cav_atlas;              /* R32UI [n_cascades*res][res][res], x fastest */
+  DrvCacheCounter* counter;
+  uint32_t* voxel_bits;             /* level 0 as a bitmask, bit (x&31) of word ((z*N+y)*N+x)/32 */
+  void* voxel_mips[16];             /* levels 1..L (index 1..L), float (FP32) or half (BF16 precision) */
+  int32_t n_voxel_levels;           /* levels including 0 */
+  DrvVPL* vpls[DRV_MAX_LIGHTS];     /* FP32 VPL array per light, Morton order */
+  DrvShadowCone* cones[DRV_MAX_LIGHTS];
+  int32_t n_vpls[DRV_MAX_LIGHTS];
+  int32_t n_lights;
+} DrvBuffers;
+
+typedef struct DrvContext DrvContext;
+
+/* ---- lifetime ----------------------------------------------------------
+ * Replaces Renderer::Renderer / SetMaxCacheCount / SetCAVCascades /
+ * Voxelization(...) resource creation (renderer.cpp:26-120, 248-288,
+ * 1174-1193; voxelization.cpp:22-68). */
+drv_status drv_create(const DrvConfig* cfg, DrvContext** out_ctx);
+drv_status drv_destroy(DrvContext* ctx);
+drv_status drv_set_stream(DrvContext* ctx, void* cuda_stream);
+drv_status drv_sync(DrvContext* ctx);
+const char* drv_last_error_string(DrvContext* ctx);
+drv_status drv_get_error(DrvContext* ctx, uint32_t* out_bits);
+drv_status drv_get_buffers(DrvContext* ctx, DrvBuffers* out);
+void drv_default_config(DrvConfig* cfg);
+int drv_abi_version(void);
+/* sizeof of the ABI structs in the order DrvConfig, DrvCascade,
+ * DrvVolumeInfo, DrvPerFrame, DrvSpotLight, DrvLightDesc, DrvCamera, DrvBox,
+ * DrvScene, DrvGBufferView, DrvGBufferOut, DrvRSMView, DrvRSMOut, DrvVPL,
+ * DrvShadowCone, DrvCacheCounter, DrvBuffers (for binding checks). Returns
+ * the number of sizes written. */
+int drv_struct_sizes(uint32_t* out, int capacity);
+
+/* ---- host-side parameter setup ------------------------------------------
+ * Renderer::UpdateVolumeUBO (renderer.cpp:346-431). */
+drv_status drv_compute_volume_info(const DrvConfig* cfg, const float aabb_min[3], const float aabb_max[3],
+                                   const float camera_position[3], DrvVolumeInfo* out);
+/* Renderer::PrepareLights (renderer.cpp:664-725). */
+drv_status drv_prepare_light(const DrvLightDesc* light, DrvSpotLight* out);
+/* Renderer::UpdatePerFrameUBO (renderer.cpp:324-344) with the camera of camera/camera.hpp:27-30. */
+drv_status drv_prepare_camera(const DrvCamera* cam, DrvPerFrame* out);
+/* Seeded procedural scene: an inward unit-cube room plus n_boxes boxes with
+ * sizes U[size_min,size_max] per axis and albedo U[albedo_min,albedo_max]. */
+drv_status drv_generate_scene(uint64_t seed, int32_t n_boxes, float size_min, float size_max,
+                              float albedo_min, float albedo_max, DrvBox* out_boxes /* n_boxes+1 */,
+                              DrvScene* out_scene);
+/* Seeded camera and spot light inside the unit room, clear of the scene's
+ * boxes (scene may be NULL). */
+drv_status drv_generate_camera(uint64_t seed, const DrvScene* scene, float aspect, DrvCamera* out);
+drv_status drv_generate_light(uint64_t seed, const DrvScene* scene, uint32_t rsm_resolution, uint32_t rsm_read_lod,
+                              uint32_t indirect_shadow_lod, DrvLightDesc* out);
+
+/* ---- input producers (replace the reference's raster passes) -------------
+ * G-buffer fill (fillgbuffer.frag, renderer.cpp:760-776) as a ray cast. */
+drv_status drv_raycast_gbuffer(DrvContext* ctx, const DrvScene* scene, const DrvCamera* camera,
+                               const DrvPerFrame* frame, int32_t width, int32_t height, const DrvGBufferOut* out);
+/* RSM fill (fillrsm.frag:24-62) as a ray cast from the spot light. */
+drv_status drv_raycast_rsm(DrvContext* ctx, const DrvScene* scene, const DrvSpotLight* light,
+                           const DrvRSMOut* out);
+
+/* ---- the per-frame stages ----------------------------------------------- */
+/* ShadowMap::PrepareRSM + downsamplersm.frag (renderer.cpp:1300-1339): build
+ * the RSM mip chain of light `light_index` from its render-resolution level
+ * down to 1x1 inside the context. */
+drv_status drv_prepare_rsm(DrvContext* ctx, int32_t light_index, const DrvSpotLight* light,
+                           const DrvRSMView* full_res);
+/* VPL extraction at RSMReadResolution (cacheLightingRSM.comp:141-158) and the
+ * per-block shadow cone sources (cacheLightingRSM.comp:171-192). Requires
+ * drv_prepare_rsm for the same light. */
+drv_status drv_extract_vpls(DrvContext* ctx, int32_t light_index, const DrvSpotLight* light);
+/* Makes the scene resident on the device (the reference keeps its meshes in
+ * GL buffers). drv_voxelize / drv_raycast_* call it implicitly; a changed
+ * scene is uploaded synchronously, so during CUDA-graph capture the scene must
+ * already be resident. */
+drv_status drv_set_scene(DrvContext* ctx, const DrvScene* scene);
+/* Voxelization::VoxelizeScene (voxelization.cpp:90-142): surface voxels of the
+ * scene into the level-0 bitmask. */
+drv_status drv_voxelize(DrvContext* ctx, const DrvScene* scene, const DrvVolumeInfo* vol);
+/* voxelmipmap.comp + voxelization.cpp:155-172: the full opacity mip chain. */
+drv_status drv_build_opacity_mips(DrvContext* ctx);
+/* Renderer::AllocateCaches (renderer.cpp:951-992): clear counter + atlas,
+ * cacheGather.comp, cachePrepareLighting.comp. */
+drv_status drv_allocate_caches(DrvContext* ctx, const DrvGBufferView* gbuffer, const DrvPerFrame* frame,
+                               const DrvVolumeInfo* vol);
+/* Renderer::LightCachesRSM (renderer.cpp:899-933): all lights accumulated into
+ * the cache SH (the reference dispatches once per light with `+=`). */
+drv_status drv_light_caches(DrvContext* ctx, const DrvSpotLight* lights, int32_t n_lights,
+                            const DrvVolumeInfo* vol, const DrvPerFrame* frame);
+/* Renderer::ApplyCaches (renderer.cpp:1047-1079, cacheApply.frag): indirect
+ * diffuse radiance per pixel into out_rgb (device, width*height*3 floats,
+ * written, not blended; pixels with depth < 1e-5 get 0). */
+drv_status drv_apply(DrvContext* ctx, const DrvGBufferView* gbuffer, const DrvPerFrame* frame,
+                     const DrvVolumeInfo* vol, float* out_rgb);
+/* All stages of one frame on the context stream (Renderer::Draw,
+ * DYN_RADIANCE_VOLUME branch, renderer.cpp:539-594): voxelize (if indirect
+ * shadow), mips, per-light RSM prepare + VPL extraction, allocate, light,
+ * apply. Device pointers only; capturable in a CUDA graph. */
+drv_status drv_frame(DrvContext* ctx, const DrvScene* scene, const DrvGBufferView* gbuffer,
+                     const DrvPerFrame* frame, const DrvVolumeInfo* vol,
+                     const DrvSpotLight* lights, const DrvRSMView* rsms, int32_t n_lights,
+                     float* out_rgb);
+/* Optional cache-count readback (renderer.cpp:960-966). Synchronises. */
+drv_status drv_get_cache_count(DrvContext* ctx, uint32_t* out_count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DRV_H_ */

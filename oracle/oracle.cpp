@@ -1,0 +1,939 @@
+// oracle.cpp — CPU FP64 restatement of the DynamicRadianceVolume per-frame
+// indirect-lighting path. TEST INFRASTRUCTURE ONLY (see oracle.h).
+//
+// Compiled with -ffp-contract=off: the binary32 "mirror" helpers below must
+// round every operation on its own, exactly as the CUDA kernels do with
+// __fmul_rn/__fadd_rn/__fdiv_rn.
+//
+// All reference paths are relative to the DynamicRadianceVolume project.
+#include "oracle.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+// utils.glsl:1 defines PI as this literal; the lighting math uses it.
+constexpr double kShaderPi = 3.14159265358979;
+constexpr double kPi = 3.14159265358979323846;
+
+struct d3 {
+  double x, y, z;
+};
+inline d3 mk(double x, double y, double z) { return {x, y, z}; }
+inline d3 operator+(d3 a, d3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline d3 operator-(d3 a, d3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline d3 operator*(d3 a, double s) { return {a.x * s, a.y * s, a.z * s}; }
+inline double dot(d3 a, d3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline d3 cross(d3 a, d3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+inline double length(d3 a) { return std::sqrt(dot(a, a)); }
+inline d3 normalize(d3 a) { return a * (1.0 / length(a)); }
+inline double saturate(double x) { return x < 0.0 ? 0.0 : (x > 1.0 ? 1.0 : x); }
+inline d3 ld3(const float* p) { return {p[0], p[1], p[2]}; }
+inline d3 ld3(const double* p) { return {p[0], p[1], p[2]}; }
+
+// ---------------------------------------------------------------------------
+// binary32 mirror: M * (x, y, z, 1) with a fixed left-to-right order, each
+// product and sum rounded separately (the kernels use the same order).
+inline float mrow(const float* r, float x, float y, float z) {
+  float a = r[0] * x;
+  float b = r[1] * y;
+  float s = a + b;
+  float c = r[2] * z;
+  s = s + c;
+  return s + r[3];
+}
+
+// World position from a depth-buffer sample (cacheGather.comp:113-119,
+// cacheApply.frag:310-311), binary32.
+inline void reconstruct_world_f32(const DrvPerFrame* f, int px, int py, int w, int h, float depth, float out[3]) {
+  float sx = (float)px + 0.5f;
+  float sy = (float)py + 0.5f;
+  float nx = sx / (float)w;
+  float ny = sy / (float)h;
+  nx = nx * 2.0f;
+  ny = ny * 2.0f;
+  nx = nx - 1.0f;
+  ny = ny - 1.0f;
+  const float* M = f->inverse_view_projection;
+  float X = mrow(M + 0, nx, ny, depth);
+  float Y = mrow(M + 4, nx, ny, depth);
+  float Z = mrow(M + 8, nx, ny, depth);
+  float W = mrow(M + 12, nx, ny, depth);
+  out[0] = X / W;
+  out[1] = Y / W;
+  out[2] = Z / W;
+}
+
+// ComputeAddressVolumeCascade, lightcache.glsl:109-122 (binary32 compares).
+inline int select_cascade_f32(const DrvVolumeInfo* v, int n_cascades, const float p[3]) {
+  int c = 0;
+  for (; c < n_cascades - 1; ++c) {
+    const DrvCascade& k = v->cascades[c];
+    bool inside = p[0] <= k.decision_max[0] && p[1] <= k.decision_max[1] && p[2] <= k.decision_max[2] &&
+                  p[0] >= k.decision_min[0] && p[1] >= k.decision_min[1] && p[2] >= k.decision_min[2];
+    if (inside) break;
+  }
+  return c;
+}
+
+// ComputeAddressVolumeCascadeTransition, lightcache.glsl:125-134 (binary32).
+inline float cascade_transition_f32(const DrvVolumeInfo* v, int c, const float p[3]) {
+  const DrvCascade& k = v->cascades[c];
+  float dmax0 = k.decision_max[0] - p[0], dmax1 = k.decision_max[1] - p[1], dmax2 = k.decision_max[2] - p[2];
+  float dmin0 = p[0] - k.decision_min[0], dmin1 = p[1] - k.decision_min[1], dmin2 = p[2] - k.decision_min[2];
+  float m = std::min(std::min(std::min(dmax0, dmax1), dmax2), std::min(std::min(dmin0, dmin1), dmin2));
+  float denom = k.world_voxel_size * v->cav_transition_zone_size;
+  float q = m / denom;
+  float t = 1.0f - q;
+  return t < 0.0f ? 0.0f : (t > 1.0f ? 1.0f : t);
+}
+
+// clamp(ivec3(v), 0, res-1) where ivec3 truncates toward zero.
+inline int trunc_clamp(float v, int res) {
+  if (!(v > 0.0f)) return 0;
+  if (v >= (float)(res - 1)) return res - 1;
+  return (int)v;
+}
+
+// GetCache1DCoord, cacheGather.comp:20-30 (binary32).
+inline int cache_1d_coord_f32(const DrvVolumeInfo* v, int res, int c, const float p[3]) {
+  const DrvCascade& k = v->cascades[c];
+  int ix = trunc_clamp((p[0] - k.min[0]) / k.world_voxel_size, res);
+  int iy = trunc_clamp((p[1] - k.min[1]) / k.world_voxel_size, res);
+  int iz = trunc_clamp((p[2] - k.min[2]) / k.world_voxel_size, res);
+  return ix + iy * res + iz * res * res + c * res * res * res;
+}
+
+// Matrices -----------------------------------------------------------------
+struct m4 {
+  double m[16];
+};
+m4 mul(const m4& a, const m4& b) {
+  m4 r;
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) {
+      double s = 0;
+      for (int k = 0; k < 4; ++k) s += a.m[i * 4 + k] * b.m[k * 4 + j];
+      r.m[i * 4 + j] = s;
+    }
+  return r;
+}
+bool invert(const m4& a, m4& out) {
+  // Gauss-Jordan with partial pivoting in FP64.
+  double t[4][8];
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 8; ++j) t[i][j] = j < 4 ? a.m[i * 4 + j] : (j - 4 == i ? 1.0 : 0.0);
+  for (int c = 0; c < 4; ++c) {
+    int p = c;
+    for (int r = c + 1; r < 4; ++r)
+      if (std::fabs(t[r][c]) > std::fabs(t[p][c])) p = r;
+    if (t[p][c] == 0.0) return false;
+    if (p != c)
+      for (int j = 0; j < 8; ++j) std::swap(t[p][j], t[c][j]);
+    double inv = 1.0 / t[c][c];
+    for (int j = 0; j < 8; ++j) t[c][j] *= inv;
+    for (int r = 0; r < 4; ++r)
+      if (r != c) {
+        double f = t[r][c];
+        if (f != 0.0)
+          for (int j = 0; j < 8; ++j) t[r][j] -= f * t[c][j];
+      }
+  }
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) out.m[i * 4 + j] = t[i][j + 4];
+  return true;
+}
+// Look-at basis: +z forward (DX-style, left-handed), up fallback when the
+// direction is (anti)parallel to the requested up.
+void basis(d3 dir, d3 up, d3& right, d3& up_out, d3& fwd) {
+  fwd = normalize(dir);
+  if (std::fabs(dot(normalize(up), fwd)) > 0.999) up = std::fabs(fwd.z) < 0.9 ? mk(0, 0, 1) : mk(1, 0, 0);
+  right = normalize(cross(up, fwd));
+  up_out = cross(fwd, right);
+}
+m4 view_matrix(d3 pos, d3 dir, d3 up) {
+  d3 r, u, f;
+  basis(dir, up, r, u, f);
+  m4 v = {{r.x, r.y, r.z, -dot(r, pos), u.x, u.y, u.z, -dot(u, pos), f.x, f.y, f.z, -dot(f, pos), 0, 0, 0, 1}};
+  return v;
+}
+// ei::perspectiveDX(fov, aspect, far, near) with near/far swapped: reversed-Z,
+// depth 1 at the near plane, 0 at the far plane (camera.hpp:27-28).
+m4 proj_reversed(double fovy, double aspect, double n, double f) {
+  double sy = 1.0 / std::tan(fovy * 0.5), sx = sy / aspect;
+  double A = n / (n - f), B = n * f / (f - n);
+  m4 p = {{sx, 0, 0, 0, 0, sy, 0, 0, 0, 0, A, B, 0, 0, 1, 0}};
+  return p;
+}
+void store(const m4& a, float* out) {
+  for (int i = 0; i < 16; ++i) out[i] = (float)a.m[i];
+}
+
+// Ray vs. axis-aligned boxes; returns box index or -1, hit distance, axis.
+int trace(const DrvBox* boxes, int n, d3 o, d3 d, double& t_hit, int& axis_hit) {
+  int best = -1;
+  t_hit = 1e300;
+  double oo[3] = {o.x, o.y, o.z}, dd[3] = {d.x, d.y, d.z};
+  for (int b = 0; b < n; ++b) {
+    double tn = -1e300, tf = 1e300;
+    int an = 0, af = 0;
+    bool miss = false;
+    for (int a = 0; a < 3; ++a) {
+      if (dd[a] == 0.0) {
+        if (oo[a] < boxes[b].min[a] || oo[a] > boxes[b].max[a]) miss = true;
+        continue;
+      }
+      double t0 = (boxes[b].min[a] - oo[a]) / dd[a];
+      double t1 = (boxes[b].max[a] - oo[a]) / dd[a];
+      if (t0 > t1) std::swap(t0, t1);
+      if (t0 > tn) { tn = t0; an = a; }
+      if (t1 < tf) { tf = t1; af = a; }
+    }
+    if (miss || tn > tf) continue;
+    double t;
+    int ax;
+    if (boxes[b].inward) {
+      t = tf;
+      ax = af;
+    } else {
+      t = tn;
+      ax = an;
+    }
+    if (t > 1e-6 && t < t_hit) {
+      t_hit = t;
+      best = b;
+      axis_hit = ax;
+    }
+  }
+  return best;
+}
+
+// Texture-space helpers -----------------------------------------------------
+inline int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+inline double voxel_l0(int N, const uint32_t* bits, int x, int y, int z) {
+  size_t i = ((size_t)z * N + y) * N + x;
+  return (bits[i >> 5] >> (i & 31)) & 1u ? 1.0 : 0.0;
+}
+
+size_t mip_offset(int N, int level) {  // offset of `level` (>= 1) in the concatenated mips
+  size_t off = 0;
+  for (int l = 1; l < level; ++l) {
+    size_t n = (size_t)(N >> l);
+    off += n * n * n;
+  }
+  return off;
+}
+
+inline double texel(int N, const uint32_t* bits, const double* mips, int level, int x, int y, int z) {
+  if (level == 0) return voxel_l0(N, bits, x, y, z);
+  int n = N >> level;
+  return mips[mip_offset(N, level) + ((size_t)z * n + y) * n + x];
+}
+
+// LINEAR filter within one level with CLAMP_TO_EDGE (GL 4.5 §8.14.2).
+double trilinear(int N, const uint32_t* bits, const double* mips, int level, const double s[3]) {
+  int n = N >> level;
+  int i0[3];
+  double a[3];
+  for (int k = 0; k < 3; ++k) {
+    double u = s[k] * n - 0.5;
+    double f = std::floor(u);
+    i0[k] = (int)f;
+    a[k] = u - f;
+  }
+  double r = 0.0;
+  for (int dz = 0; dz < 2; ++dz)
+    for (int dy = 0; dy < 2; ++dy)
+      for (int dx = 0; dx < 2; ++dx) {
+        double w = (dx ? a[0] : 1 - a[0]) * (dy ? a[1] : 1 - a[1]) * (dz ? a[2] : 1 - a[2]);
+        int x = clampi(i0[0] + dx, 0, n - 1), y = clampi(i0[1] + dy, 0, n - 1), z = clampi(i0[2] + dz, 0, n - 1);
+        r += w * texel(N, bits, mips, level, x, y, z);
+      }
+  return r;
+}
+
+int ilog2(int v) {
+  int l = 0;
+  while ((1 << (l + 1)) <= v) ++l;
+  return l;
+}
+
+// Bilinear sample of a 2-channel RSM level (sampler2D LINEAR, CLAMP).
+void bilinear2(int n, const float* img, double u, double v, double out[2]) {
+  double x = u * n - 0.5, y = v * n - 0.5;
+  double fx = std::floor(x), fy = std::floor(y);
+  int x0 = (int)fx, y0 = (int)fy;
+  double ax = x - fx, ay = y - fy;
+  out[0] = out[1] = 0;
+  for (int dy = 0; dy < 2; ++dy)
+    for (int dx = 0; dx < 2; ++dx) {
+      double w = (dx ? ax : 1 - ax) * (dy ? ay : 1 - ay);
+      int xx = clampi(x0 + dx, 0, n - 1), yy = clampi(y0 + dy, 0, n - 1);
+      out[0] += w * img[((size_t)yy * n + xx) * 2 + 0];
+      out[1] += w * img[((size_t)yy * n + xx) * 2 + 1];
+    }
+}
+
+d3 unproject_dir(const float* inv_vp, double u, double v, d3 from) {
+  // vec4(uv*2-1, 0, 1) * InverseLightViewProjection (cacheLightingRSM.comp:154-155)
+  double x = u * 2.0 - 1.0, y = v * 2.0 - 1.0;
+  double c[4];
+  for (int r = 0; r < 4; ++r) c[r] = inv_vp[r * 4 + 0] * x + inv_vp[r * 4 + 1] * y + inv_vp[r * 4 + 3];
+  d3 p = mk(c[0] / c[3], c[1] / c[3], c[2] / c[3]);
+  return normalize(p - from);
+}
+
+void set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}
+
+}  // namespace
+
+extern "C" {
+
+// cacheLightingRSM.comp:46-62
+void orc_morton_decode(uint32_t morton, uint32_t* x, uint32_t* y) {
+  uint32_t c[2] = {morton, morton >> 1};
+  for (int i = 0; i < 2; ++i) {
+    uint32_t v = c[i] & 0x55555555u;
+    v = (v | (v >> 1)) & 0x33333333u;
+    v = (v | (v >> 2)) & 0x0f0f0f0fu;
+    v = (v | (v >> 4)) & 0x00ff00ffu;
+    v = (v | (v >> 8)) & 0x0000ffffu;
+    c[i] = v;
+  }
+  *x = c[0];
+  *y = c[1];
+}
+
+// PackNormal / PackNormal16I, utils.glsl:61-89. The conversion to a 16-bit
+// integer target saturates to [-32768, 32767] (the reference writes +32768
+// for n.z = 1 into an RG16I target, which GL leaves undefined).
+void orc_pack_normal16i(const double n[3], int16_t out[2]) {
+  double px = n[0] == 0.0 ? ((n[1] > 0) - (n[1] < 0)) * kShaderPi / 2 : std::atan2(n[1], n[0]);
+  double py = n[2];
+  // (x / PI) * 32768, the same product as the reference's x * (32768 / PI),
+  // ordered so that axis-aligned normals pack exactly on every side.
+  double vx = std::trunc((px / kShaderPi) * 32768.0);
+  double vy = std::trunc(py * 32768.0);
+  if (!(vx == vx)) vx = 0;
+  if (!(vy == vy)) vy = 0;
+  out[0] = (int16_t)std::max(-32768.0, std::min(32767.0, vx));
+  out[1] = (int16_t)std::max(-32768.0, std::min(32767.0, vy));
+}
+
+// UnpackNormal16I / UnpackNormal, utils.glsl:44-58.
+void orc_unpack_normal16i(const int16_t packed[2], double out[3]) {
+  double px = packed[0] * (kShaderPi / 32768.0);
+  double py = packed[1] * (1.0 / 32768.0);
+  double sin_phi = std::sqrt(1.0 - py * py);
+  d3 v = normalize(mk(std::cos(px) * sin_phi, std::sin(px) * sin_phi, py));
+  out[0] = v.x;
+  out[1] = v.y;
+  out[2] = v.z;
+}
+
+// Renderer::UpdateConstantUBO, renderer.cpp:296-306.
+void orc_sh_constants(int sh2_sign, double cl[5], double ev[5]) {
+  cl[0] = std::sqrt(kPi) / 2.0;
+  cl[1] = std::sqrt(kPi / 3.0);
+  cl[2] = (sh2_sign == DRV_SH2_SIGN_FIXED ? 1.0 : -1.0) * std::sqrt(15.0 * kPi) / 8.0;
+  cl[3] = std::sqrt(5.0 * kPi) / 16.0;
+  cl[4] = std::sqrt(15.0 * kPi) / 16.0;
+  ev[0] = 1.0 / (2.0 * std::sqrt(kPi));
+  ev[1] = std::sqrt(3.0) / (2.0 * std::sqrt(kPi));
+  ev[2] = std::sqrt(15.0 / (4.0 * kPi));
+  ev[3] = std::sqrt(5.0 / (16.0 * kPi));
+  ev[4] = std::sqrt(15.0 / (16.0 * kPi));
+}
+
+// SampleCacheIrradiance, lightcache.glsl:137-179.
+void orc_sh_irradiance(int sh_order, int sh2_sign, const double* sh, const double nn[3], double out[3]) {
+  double cl[5], ev[5];
+  orc_sh_constants(sh2_sign, cl, ev);
+  double nx = nn[0], ny = nn[1], nz = nn[2];
+  for (int ch = 0; ch < 3; ++ch) {
+    double e = sh[0 * 3 + ch] * cl[0];
+    e -= sh[1 * 3 + ch] * (cl[1] * ny);
+    e += sh[2 * 3 + ch] * (cl[1] * nz);
+    e -= sh[3 * 3 + ch] * (cl[1] * nx);
+    if (sh_order == 2) {
+      e -= sh[4 * 3 + ch] * (cl[2] * nx * ny);
+      e += sh[5 * 3 + ch] * (cl[2] * ny * nz);
+      e += sh[6 * 3 + ch] * (cl[3] * (nz * nz * 3.0 - 1.0));
+      e += sh[7 * 3 + ch] * (cl[2] * nx * nz);
+      e += sh[8 * 3 + ch] * (cl[4] * (nx * nx - ny * ny));
+    }
+    out[ch] = std::max(e, 0.0);
+  }
+}
+
+// textureLod(VoxelVolume, s, lod) with the LINEAR/LINEAR/LINEAR CLAMP sampler
+// bound at renderer.cpp:916-917 (GL 4.5 §8.14: lambda <= 0 magnifies on the
+// base level; otherwise LINEAR_MIPMAP_LINEAR between floor/ceil levels,
+// clamped to the last level).
+double orc_sample_voxels(int N, const uint32_t* bits, const double* mips, const double s[3], double lod) {
+  int q = ilog2(N);
+  if (!(lod > 0.0)) return trilinear(N, bits, mips, 0, s);
+  if (lod >= q) return trilinear(N, bits, mips, q, s);
+  double fl = std::floor(lod);
+  int d1 = (int)fl;
+  double fr = lod - fl;
+  double t1 = trilinear(N, bits, mips, d1, s);
+  if (fr == 0.0) return t1;
+  double t2 = trilinear(N, bits, mips, d1 + 1, s);
+  return (1.0 - fr) * t1 + fr * t2;
+}
+
+// cacheLightingRSM.comp:103-104, 195-230.
+double orc_cone_shadow(const DrvVolumeInfo* vol, int N, const uint32_t* bits, const double* mips, const double cp[3],
+                       const double av[3], double dsr, int max_steps) {
+  d3 world = ld3(cp);
+  d3 vmin = ld3(vol->volume_world_min);
+  double vs = vol->voxel_size_in_world;
+  d3 voxel_pos = (world - vmin) * (1.0 / (vs * N));
+  d3 to = ld3(av) - world;
+  double light_dist = length(to);
+  to = to * (1.0 / light_dist);
+  d3 dir_in_voxel = to * (1.0 / N);
+  d3 cur = voxel_pos + dir_in_voxel * 2.0;
+  double occlusion = 0.0, step = 1.0, dist = 0.0;
+  double goal = light_dist / vs - 2.0;
+  double k = 2.0 / (1.0 - dsr);
+  for (int s = 0; s < max_steps; ++s) {
+    cur = cur + dir_in_voxel * step;
+    dist += step;
+    double radius = dist * dsr;
+    double p[3] = {cur.x, cur.y, cur.z};
+    double occ = orc_sample_voxels(N, bits, mips, p, std::log2(radius));
+    occlusion += (1.0 - occlusion) * occ;
+    if (dist >= goal) break;
+    step = std::max(1.0, radius * k);
+  }
+  return saturate(1.0 - occlusion);
+}
+
+// Renderer::PrepareLights, renderer.cpp:664-725 (float host math as there;
+// matrices computed in FP64 and rounded, a convention shared with the product).
+void orc_prepare_light(const DrvLightDesc* L, DrvSpotLight* o) {
+  std::memset(o, 0, sizeof(*o));
+  for (int i = 0; i < 3; ++i) {
+    o->intensity[i] = L->intensity[i];
+    o->position[i] = L->position[i];
+  }
+  d3 dir = normalize(ld3(L->direction));
+  o->direction[0] = (float)dir.x;
+  o->direction[1] = (float)dir.y;
+  o->direction[2] = (float)dir.z;
+  o->shadow_normal_offset = 0.01f;
+  o->shadow_bias = 0.0001f;
+  o->cos_half_angle = cosf(L->half_angle);
+  m4 v = view_matrix(ld3(L->position), dir, mk(0, 1, 0));
+  m4 p = proj_reversed(2.0 * L->half_angle, 1.0, L->near_plane, L->far_plane);
+  m4 vp = mul(p, v), inv;
+  invert(vp, inv);
+  store(vp, o->view_projection);
+  store(inv, o->inverse_view_projection);
+  int r = 1;
+  while ((uint32_t)r < L->rsm_resolution) r <<= 1;
+  o->rsm_render_resolution = r;
+  int read = r >> L->rsm_read_lod;
+  o->rsm_read_resolution = read;
+  float clip_w = sinf(L->half_angle) * L->near_plane * 2.0f;
+  float vaf = clip_w * clip_w / (L->near_plane * L->near_plane * (float)read * (float)read);
+  o->val_area_factor = vaf;
+  o->indirect_shadow_lod = (float)L->indirect_shadow_lod;
+  float bs = (float)(1 << L->indirect_shadow_lod);
+  o->indirect_shadow_block_size = bs;
+  o->indirect_shadow_sample_interval = (int)(bs * bs);
+  o->indirect_shadow_super_val_width = sqrtf(vaf) * bs;
+  o->indirect_shadow_sampling_offset = 0.5f + sqrtf(2.0f) * bs / 2.0f;
+}
+
+// Renderer::UpdatePerFrameUBO, renderer.cpp:324-344, camera.hpp:27-30.
+void orc_prepare_camera(const DrvCamera* c, DrvPerFrame* o) {
+  std::memset(o, 0, sizeof(*o));
+  d3 dir = normalize(ld3(c->direction));
+  m4 v = view_matrix(ld3(c->position), dir, ld3(c->up));
+  m4 p = proj_reversed(c->fov_y_deg * (kPi / 180.0), c->aspect, c->near_plane, c->far_plane);
+  m4 vp = mul(p, v), inv;
+  invert(vp, inv);
+  store(vp, o->view_projection);
+  store(inv, o->inverse_view_projection);
+  for (int i = 0; i < 3; ++i) o->camera_position[i] = c->position[i];
+  o->camera_direction[0] = (float)dir.x;
+  o->camera_direction[1] = (float)dir.y;
+  o->camera_direction[2] = (float)dir.z;
+}
+
+// Renderer::UpdateVolumeUBO, renderer.cpp:346-431 ("simple version"), float.
+void orc_compute_volume_info(const DrvConfig* cfg, const float amin[3], const float amax[3], const float cam[3],
+                             DrvVolumeInfo* o) {
+  std::memset(o, 0, sizeof(*o));
+  float mn[3], mx[3], ext[3];
+  for (int i = 0; i < 3; ++i) {
+    mn[i] = amin[i] - 0.001f;
+    mx[i] = amax[i] + 0.001f;
+    ext[i] = mx[i] - mn[i];
+  }
+  float largest = std::max(std::max(ext[0], ext[1]), ext[2]);
+  for (int i = 0; i < 3; ++i) {
+    float grow = largest - ext[i];
+    mx[i] = mx[i] + grow;
+    o->volume_world_min[i] = mn[i];
+    o->volume_world_max[i] = mx[i];
+  }
+  o->voxel_size_in_world = (mx[0] - mn[0]) / (float)cfg->voxel_res;
+  o->cav_transition_zone_size = cfg->cascade_transition;
+  for (int c = 0; c < cfg->n_cascades; ++c) {
+    float size = cfg->cascade_world_size[c];
+    float cell = size / (float)cfg->cav_res;
+    DrvCascade& k = o->cascades[c];
+    k.world_voxel_size = cell;
+    for (int i = 0; i < 3; ++i) {
+      float snapped = roundf(cam[i] / cell) * cell;
+      float half = size * 0.5f;
+      k.min[i] = snapped - half;
+      k.max[i] = snapped + half;
+      float off = cell * 1.5f;
+      k.decision_min[i] = (cam[i] - half) + off;
+      k.decision_max[i] = (cam[i] + half) - off;
+    }
+  }
+}
+
+// fillgbuffer.frag:21-43 as a ray cast (no normal maps: the shading normal is
+// the face normal; base colour is the box albedo).
+void orc_raycast_gbuffer(const DrvBox* boxes, int n, const DrvPerFrame* f, const DrvCamera* cam, int W, int H,
+                         float* depth, int16_t* n16, float* n32, float* alb) {
+  d3 r, u, fw;
+  basis(ld3(cam->direction), ld3(cam->up), r, u, fw);
+  double ty = std::tan(cam->fov_y_deg * (kPi / 180.0) * 0.5), tx = ty * cam->aspect;
+  d3 o = ld3(cam->position);
+#pragma omp parallel for schedule(static)
+  for (int y = 0; y < H; ++y)
+    for (int x = 0; x < W; ++x) {
+      size_t i = (size_t)y * W + x;
+      double nx = ((x + 0.5) / W) * 2.0 - 1.0, ny = ((y + 0.5) / H) * 2.0 - 1.0;
+      d3 d = normalize(fw + r * (nx * tx) + u * (ny * ty));
+      double t;
+      int ax = 0;
+      int b = trace(boxes, n, o, d, t, ax);
+      if (b < 0) {
+        depth[i] = 0.0f;
+        if (n16) n16[2 * i] = n16[2 * i + 1] = 0;
+        if (n32) n32[3 * i] = n32[3 * i + 1] = n32[3 * i + 2] = 0.0f;
+        for (int c = 0; c < 3; ++c) alb[3 * i + c] = 0.0f;
+        continue;
+      }
+      d3 p = o + d * t;
+      double cz = 0, cw = 0;
+      const float* M = f->view_projection;
+      cz = M[8] * p.x + M[9] * p.y + M[10] * p.z + M[11];
+      cw = M[12] * p.x + M[13] * p.y + M[14] * p.z + M[15];
+      depth[i] = (float)(cz / cw);
+      double nrm[3] = {0, 0, 0};
+      double dd[3] = {d.x, d.y, d.z};
+      nrm[ax] = dd[ax] > 0 ? -1.0 : 1.0;
+      if (n16) orc_pack_normal16i(nrm, n16 + 2 * i);
+      if (n32)
+        for (int c = 0; c < 3; ++c) n32[3 * i + c] = (float)nrm[c];
+      for (int c = 0; c < 3; ++c) alb[3 * i + c] = boxes[b].albedo[c];
+    }
+}
+
+// fillrsm.frag:24-62 (+ lightingfunctions.glsl:3-15) as a ray cast from the
+// spot light through each RSM texel centre; the ray direction is the one the
+// VPL reconstruction uses (unprojection at depth 0, cacheLightingRSM.comp:154-155).
+void orc_raycast_rsm(const DrvBox* boxes, int n, const DrvSpotLight* L, float* flux, int16_t* n16, float* dls) {
+  int R = L->rsm_render_resolution;
+  d3 o = ld3(L->position);
+  d3 ldir = ld3(L->direction);
+  double cos_half = L->cos_half_angle;
+#pragma omp parallel for schedule(static)
+  for (int y = 0; y < R; ++y)
+    for (int x = 0; x < R; ++x) {
+      size_t i = (size_t)y * R + x;
+      d3 d = unproject_dir(L->inverse_view_projection, (x + 0.5) / R, (y + 0.5) / R, o);
+      double th;
+      int ax = 0;
+      int b = trace(boxes, n, o, d, th, ax);
+      if (b < 0) {
+        flux[3 * i] = flux[3 * i + 1] = flux[3 * i + 2] = 0.0f;
+        n16[2 * i] = n16[2 * i + 1] = 0;
+        dls[2 * i] = dls[2 * i + 1] = 0.0f;
+        continue;
+      }
+      d3 p = o + d * th;
+      d3 to_light = o - p;
+      double dist = length(to_light);
+      to_light = to_light * (1.0 / dist);
+      double cos_to_light = saturate(dot(to_light * -1.0, ldir));
+      double total_sr = 2.0 * kShaderPi * (1.0 - cos_half);
+      double pixel_sr = total_sr * cos_to_light / R / R;
+      double falloff = saturate(cos_to_light - cos_half) / (1.0 - cos_half);
+      for (int c = 0; c < 3; ++c)
+        flux[3 * i + c] = (float)(boxes[b].albedo[c] * L->intensity[c] * (falloff * pixel_sr / kShaderPi));
+      dls[2 * i] = (float)dist;
+      dls[2 * i + 1] = (float)(dist * dist);
+      double nrm[3] = {0, 0, 0};
+      double dd[3] = {d.x, d.y, d.z};
+      nrm[ax] = dd[ax] > 0 ? -1.0 : 1.0;
+      orc_pack_normal16i(nrm, n16 + 2 * i);
+    }
+}
+
+// downsamplersm.frag:15-33: flux = sum of the 2x2 children (textureGather),
+// normal = PackNormal16I(normalize(sum of unpacked)), (d, d^2) = bilinear at
+// the shared corner = mean of the 4 children.
+void orc_downsample_rsm(int res, const float* flux, const int16_t* nrm, const float* dls, float* fo, int16_t* no,
+                        float* dlo) {
+  int h = res / 2;
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < h; ++x) {
+      double fs[3] = {0, 0, 0}, ns[3] = {0, 0, 0}, ds[2] = {0, 0};
+      for (int dy = 0; dy < 2; ++dy)
+        for (int dx = 0; dx < 2; ++dx) {
+          size_t j = (size_t)(2 * y + dy) * res + (2 * x + dx);
+          for (int c = 0; c < 3; ++c) fs[c] += flux[3 * j + c];
+          double un[3];
+          orc_unpack_normal16i(nrm + 2 * j, un);
+          for (int c = 0; c < 3; ++c) ns[c] += un[c];
+          ds[0] += dls[2 * j];
+          ds[1] += dls[2 * j + 1];
+        }
+      size_t i = (size_t)y * h + x;
+      for (int c = 0; c < 3; ++c) fo[3 * i + c] = (float)fs[c];
+      double len = std::sqrt(ns[0] * ns[0] + ns[1] * ns[1] + ns[2] * ns[2]);
+      if (len > 0.0) {
+        double nn[3] = {ns[0] / len, ns[1] / len, ns[2] / len};
+        orc_pack_normal16i(nn, no + 2 * i);
+      } else {
+        no[2 * i] = no[2 * i + 1] = 0;
+      }
+      dlo[2 * i] = (float)(ds[0] * 0.25);
+      dlo[2 * i + 1] = (float)(ds[1] * 0.25);
+    }
+}
+
+// cacheLightingRSM.comp:141-158 (VPL) and 168-192 (shadow cone source).
+void orc_extract_vpls(const DrvSpotLight* L, int R, const float* flux, const int16_t* nrm, const float* dls,
+                      const float* dls_shadow, double* vo, double* co) {
+  d3 lp = ld3(L->position);
+  int n = R * R;
+  for (int i = 0; i < n; ++i) {
+    uint32_t x, y;
+    orc_morton_decode((uint32_t)i, &x, &y);
+    size_t t = (size_t)y * R + x;
+    double u = (x + 0.5) / R, v = (y + 0.5) / R;
+    double d = dls[2 * t];
+    for (int c = 0; c < 3; ++c) vo[10 * i + c] = flux[3 * t + c];
+    vo[10 * i + 3] = d * d * L->val_area_factor;
+    d3 p = lp + unproject_dir(L->inverse_view_projection, u, v, lp) * d;
+    vo[10 * i + 4] = p.x;
+    vo[10 * i + 5] = p.y;
+    vo[10 * i + 6] = p.z;
+    double un[3];
+    orc_unpack_normal16i(nrm + 2 * t, un);
+    vo[10 * i + 7] = un[0];
+    vo[10 * i + 8] = un[1];
+    vo[10 * i + 9] = un[2];
+  }
+  int interval = L->indirect_shadow_sample_interval;
+  int lod = (int)L->indirect_shadow_lod;
+  int rs = R >> lod;
+  for (int b = 0; b * interval < n; ++b) {
+    uint32_t x, y;
+    orc_morton_decode((uint32_t)(b * interval), &x, &y);
+    double u = (x + (double)L->indirect_shadow_sampling_offset) / R;
+    double v = (y + (double)L->indirect_shadow_sampling_offset) / R;
+    double dd[2];
+    bilinear2(rs, dls_shadow, u, v, dd);
+    d3 avg = lp + unproject_dir(L->inverse_view_projection, u, v, lp) * dd[0];
+    // depthVariance can round below zero; clamped (sqrt of a negative is
+    // undefined in GLSL).
+    double var = std::max(0.0, dd[1] - dd[0] * dd[0]);
+    double dsr = std::max((double)L->indirect_shadow_super_val_width, std::sqrt(var) * 2.0 / dd[0]);
+    co[4 * b + 0] = avg.x;
+    co[4 * b + 1] = avg.y;
+    co[4 * b + 2] = avg.z;
+    co[4 * b + 3] = dsr;
+  }
+}
+
+// voxelize.{vert,geom,frag}: conservative surface voxelization. For an
+// axis-aligned face the dominant axis is its normal axis, the depth gradient
+// is zero (no +-1 depth voxels, voxelize.frag:295-313) and the dilated
+// triangles with their half-voxel raster AABB (voxelize.geom:201-225,
+// voxelize.frag:280-283) cover every voxel whose square touches the face
+// rectangle (closed intervals). Binary32 mirror with the kernel.
+void orc_voxelize(const DrvBox* boxes, int n, const DrvVolumeInfo* vol, int N, uint32_t* bits) {
+  size_t words = ((size_t)N * N * N + 31) / 32;
+  std::memset(bits, 0, words * 4);
+  const float* vm = vol->volume_world_min;
+  float vs = vol->voxel_size_in_world;
+  for (int b = 0; b < n; ++b)
+    for (int axis = 0; axis < 3; ++axis)
+      for (int side = 0; side < 2; ++side) {
+        int ua = (axis + 1) % 3, va = (axis + 2) % 3;
+        float plane = side ? boxes[b].max[axis] : boxes[b].min[axis];
+        float kc = (plane - vm[axis]) / vs;
+        if (!(kc >= 0.0f) || !(kc < (float)N)) continue;
+        int k = (int)kc;
+        float lo_u = (boxes[b].min[ua] - vm[ua]) / vs, hi_u = (boxes[b].max[ua] - vm[ua]) / vs;
+        float lo_v = (boxes[b].min[va] - vm[va]) / vs, hi_v = (boxes[b].max[va] - vm[va]) / vs;
+        int u0 = std::max(0, (int)std::ceil(lo_u) - 1), u1 = std::min(N - 1, (int)std::floor(hi_u));
+        int v0 = std::max(0, (int)std::ceil(lo_v) - 1), v1 = std::min(N - 1, (int)std::floor(hi_v));
+        for (int vv = v0; vv <= v1; ++vv)
+          for (int uu = u0; uu <= u1; ++uu) {
+            int c[3];
+            c[axis] = k;
+            c[ua] = uu;
+            c[va] = vv;
+            size_t i = ((size_t)c[2] * N + c[1]) * N + c[0];
+            bits[i >> 5] |= 1u << (i & 31);
+          }
+      }
+}
+
+// voxelmipmap.comp:8-13: a linear sample at the corner shared by 8 children
+// is their mean (stored as R8 in the reference; kept exact here).
+void orc_build_mips(int N, const uint32_t* bits, double* mips) {
+  int L = ilog2(N);
+  for (int l = 1; l <= L; ++l) {
+    int n = N >> l;
+    double* dst = mips + mip_offset(N, l);
+    for (int z = 0; z < n; ++z)
+      for (int y = 0; y < n; ++y)
+        for (int x = 0; x < n; ++x) {
+          double s = 0;
+          for (int dz = 0; dz < 2; ++dz)
+            for (int dy = 0; dy < 2; ++dy)
+              for (int dx = 0; dx < 2; ++dx) s += texel(N, bits, mips, l - 1, 2 * x + dx, 2 * y + dy, 2 * z + dz);
+          dst[((size_t)z * n + y) * n + x] = s / 8.0;
+        }
+  }
+}
+
+// cacheGather.comp:32-164 executed workgroup by workgroup (16x16 tiles).
+int orc_allocate_caches(const DrvConfig* cfg, const DrvVolumeInfo* vol, const DrvPerFrame* f, int W, int H,
+                        const float* depth, uint32_t* atlas, float* pos, uint32_t* count_out) {
+  const int res = cfg->cav_res, nC = cfg->n_cascades;
+  const int res2 = res * res, res3 = res2 * res;
+  const int AW = nC * res;  // atlas width
+  std::memset(atlas, 0, (size_t)AW * res * res * 4);
+  const bool transitions = cfg->cascade_transition > 0.0f;
+  uint32_t count = 0;
+  int status = DRV_OK;
+  // AllocateCaches, cacheGather.comp:32-91. Out-of-atlas corners are skipped.
+  auto allocate = [&](int coord, int cascade) {
+    static const int off[8][3] = {{0, 0, 0}, {0, 1, 0}, {0, 0, 1}, {0, 1, 1}, {1, 0, 0}, {1, 1, 0}, {1, 0, 1}, {1, 1, 1}};
+    int base = coord - res3 * cascade;
+    int bz = base / res2, by = (base - bz * res2) / res, bx = base % res;
+    for (int i = 0; i < 8; ++i) {
+      int lx = bx + off[i][0], ly = by + off[i][1], lz = bz + off[i][2];
+      int ax = lx + cascade * res;
+      if (ax >= AW || ly >= res || lz >= res) continue;
+      size_t a = ((size_t)lz * res + ly) * AW + ax;
+      if (atlas[a] != 0u) continue;
+      atlas[a] = 0xFFFFFFFFu;
+      uint32_t idx = count++;
+      if (idx >= cfg->max_caches) {
+        status = DRV_ERR_CAPACITY;
+        continue;  // stays locked; apply treats it as empty
+      }
+      const DrvCascade& k = vol->cascades[cascade];
+      float fx = (float)lx * k.world_voxel_size;
+      float fy = (float)ly * k.world_voxel_size;
+      float fz = (float)lz * k.world_voxel_size;
+      pos[3 * idx + 0] = fx + k.min[0];
+      pos[3 * idx + 1] = fy + k.min[1];
+      pos[3 * idx + 2] = fz + k.min[2];
+      atlas[a] = idx + 1;
+    }
+  };
+  const int TS = 16;
+  int tiles_x = (W + TS - 1) / TS, tiles_y = (H + TS - 1) / TS;
+  int list1[TS][TS], list2[TS][TS], own1[TS][TS], own2[TS][TS], casc[TS][TS];
+  for (int ty = 0; ty < tiles_y; ++ty)
+    for (int tx = 0; tx < tiles_x; ++tx) {
+      for (int ly = 0; ly < TS; ++ly)
+        for (int lx = 0; lx < TS; ++lx) {
+          list1[lx][ly] = list2[lx][ly] = -1;
+          own1[lx][ly] = own2[lx][ly] = -1;
+          casc[lx][ly] = -1;
+          int px = tx * TS + lx, py = ty * TS + ly;
+          if (px >= W || py >= H) continue;
+          float d = depth[(size_t)py * W + px];
+          if (!(d > 0.0001f)) continue;
+          float p[3];
+          reconstruct_world_f32(f, px, py, W, H, d, p);
+          int c = select_cascade_f32(vol, nC, p);
+          casc[lx][ly] = c;
+          own1[lx][ly] = list1[lx][ly] = cache_1d_coord_f32(vol, res, c, p);
+          if (transitions) {
+            float t = cascade_transition_f32(vol, c, p);
+            if (t > 0.0f && c < nC - 1) own2[lx][ly] = list2[lx][ly] = cache_1d_coord_f32(vol, res, c + 1, p);
+          }
+        }
+      // Threads run in x-fastest order within the tile (the allocation index
+      // order is not part of the contract; only the set is).
+      for (int ly = 0; ly < TS; ++ly)
+        for (int lx = 0; lx < TS; ++lx) {
+          int own = own1[lx][ly];
+          int ux = std::max(0, lx - 1), uy = std::max(0, ly - 1);
+          bool self = (ux == lx && uy == ly);
+          if (((list1[lx][uy] != own && list1[ux][ly] != own && list1[ux][uy] != own) || self) && own != -1)
+            allocate(own, casc[lx][ly]);
+          if (transitions) {
+            int own_b = own2[lx][ly];
+            int dx = std::min(TS - 1, lx + 1), dy = std::min(TS - 1, ly + 1);
+            bool corner = (dx == TS - 1 && dy == TS - 1);
+            if (((list2[lx][dy] != own_b && list2[dx][ly] != own_b && list2[dx][dy] != own_b) || corner) &&
+                own_b != -1)
+              allocate(own_b, casc[lx][ly] + 1);
+          }
+        }
+    }
+  *count_out = count;
+  return status;
+}
+
+// cacheLightingRSM.comp:80-374, all lights accumulated (the reference
+// dispatches once per light and adds into the entries).
+void orc_light_caches(const DrvConfig* cfg, const DrvVolumeInfo* vol, int n_caches, const float* positions,
+                      int n_lights, const DrvSpotLight* lights, const double* const* vpls,
+                      const double* const* cones, const int* n_vpls, const uint32_t* bits, const double* mips,
+                      double* sh_out, int n_threads) {
+  set_threads(n_threads);
+  double cl[5], ev[5];
+  orc_sh_constants(DRV_SH2_SIGN_REFERENCE, cl, ev);
+  const bool sh2 = cfg->sh_order == 2;
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int c = 0; c < n_caches; ++c) {
+    double acc[27];
+    for (int k = 0; k < 27; ++k) acc[k] = 0.0;
+    d3 wp = ld3(positions + 3 * c);
+    double cp[3] = {wp.x, wp.y, wp.z};
+    for (int l = 0; l < n_lights; ++l) {
+      const double* V = vpls[l];
+      const double* C = cones[l];
+      int interval = lights[l].indirect_shadow_sample_interval;
+      double shadowing = 1.0;
+      for (int j = 0; j < n_vpls[l]; ++j) {
+        if (cfg->indirect_shadow && j % interval == 0) {
+          const double* cone = C + 4 * (j / interval);
+          shadowing = orc_cone_shadow(vol, cfg->voxel_res, bits, mips, cp, cone, cone[3], cfg->max_cone_steps);
+        }
+        const double* v = V + 10 * j;
+        d3 to = mk(v[4], v[5], v[6]) - wp;
+        double d2 = dot(to, to);
+        to = to * (1.0 / std::sqrt(d2));
+        double f = saturate(-dot(mk(v[7], v[8], v[9]), to)) * shadowing;
+        double s = f / (d2 + v[3]);
+        for (int ch = 0; ch < 3; ++ch) {
+          double L = v[ch] * s;
+          acc[0 * 3 + ch] += ev[0] * L;
+          acc[1 * 3 + ch] -= (ev[1] * to.y) * L;
+          acc[2 * 3 + ch] += (ev[1] * to.z) * L;
+          acc[3 * 3 + ch] -= (ev[1] * to.x) * L;
+          if (sh2) {
+            acc[4 * 3 + ch] -= (ev[2] * to.x * to.y) * L;
+            acc[5 * 3 + ch] += (ev[2] * to.y * to.z) * L;
+            acc[6 * 3 + ch] += (ev[3] * (to.z * to.z * 3.0 - 1.0)) * L;
+            acc[7 * 3 + ch] += (ev[2] * to.x * to.z) * L;
+            acc[8 * 3 + ch] += (ev[4] * (to.x * to.x - to.y * to.y)) * L;
+          }
+        }
+      }
+    }
+    for (int k = 0; k < 27; ++k) sh_out[(size_t)c * 27 + k] = acc[k];
+  }
+}
+
+// cacheApply.frag:204-294 (ComputeLightingFromCaches) and :296-362 (main).
+// Corners outside the atlas, or whose atlas slot holds 0 (never allocated) or
+// 0xFFFFFFFF (locked, capacity overflow), contribute zero irradiance; their
+// weight is not redistributed (GL robust access returns zeros there).
+void orc_apply(const DrvConfig* cfg, const DrvVolumeInfo* vol, const DrvPerFrame* f, int W, int H, const float* depth,
+               const void* normal, int normal_format, const float* albedo, const uint32_t* atlas, int n_caches,
+               const double* sh, double* out, int n_threads) {
+  set_threads(n_threads);
+  const int res = cfg->cav_res, nC = cfg->n_cascades, AW = nC * res;
+  const bool transitions = cfg->cascade_transition > 0.0f;
+  auto lighting = [&](const float p[3], int c, const double n[3], const double alb[3], double col[3]) {
+    static const int off[8][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {1, 1, 0}, {0, 0, 1}, {1, 0, 1}, {0, 1, 1}, {1, 1, 1}};
+    const DrvCascade& k = vol->cascades[c];
+    float a[3];
+    int a0[3];
+    double t[3];
+    for (int i = 0; i < 3; ++i) {
+      a[i] = (p[i] - k.min[i]) / k.world_voxel_size;
+      a0[i] = (int)std::trunc(std::max(-1e9f, std::min(1e9f, a[i])));
+      t[i] = (double)a[i] - (double)a0[i];
+    }
+    double irr[3] = {0, 0, 0};
+    for (int i = 0; i < 8; ++i) {
+      double w = (off[i][0] ? t[0] : 1 - t[0]) * (off[i][1] ? t[1] : 1 - t[1]) * (off[i][2] ? t[2] : 1 - t[2]);
+      int x = a0[0] + off[i][0], y = a0[1] + off[i][1], z = a0[2] + off[i][2];
+      x += res * c;
+      if (x < 0 || y < 0 || z < 0 || x >= AW || y >= res || z >= res) continue;
+      uint32_t addr = atlas[((size_t)z * res + y) * AW + x];
+      if (addr == 0u || addr == 0xFFFFFFFFu || addr > (uint32_t)n_caches) continue;
+      double e[3];
+      orc_sh_irradiance(cfg->sh_order, cfg->sh2_sign, sh + (size_t)(addr - 1) * 27, n, e);
+      for (int ch = 0; ch < 3; ++ch) irr[ch] += e[ch] * w;
+    }
+    for (int ch = 0; ch < 3; ++ch) col[ch] = irr[ch] * alb[ch] / kShaderPi;
+  };
+#pragma omp parallel for schedule(static)
+  for (int y = 0; y < H; ++y)
+    for (int x = 0; x < W; ++x) {
+      size_t i = (size_t)y * W + x;
+      double* o = out + 3 * i;
+      o[0] = o[1] = o[2] = 0.0;
+      float d = depth[i];
+      if (d < 0.00001f) continue;
+      float p[3];
+      reconstruct_world_f32(f, x, y, W, H, d, p);
+      int c = select_cascade_f32(vol, nC, p);
+      double n[3];
+      if (normal_format == DRV_NORMAL_RG16I) {
+        orc_unpack_normal16i((const int16_t*)normal + 2 * i, n);
+      } else {
+        const float* nf = (const float*)normal + 3 * i;
+        n[0] = nf[0];
+        n[1] = nf[1];
+        n[2] = nf[2];
+      }
+      double alb[3] = {albedo[3 * i], albedo[3 * i + 1], albedo[3 * i + 2]};
+      double col[3];
+      lighting(p, c, n, alb, col);
+      if (transitions) {
+        float t = cascade_transition_f32(vol, c, p);
+        if (t > 0.0f && c < nC - 1) {
+          double col2[3];
+          lighting(p, c + 1, n, alb, col2);
+          for (int ch = 0; ch < 3; ++ch) col[ch] = col[ch] * (1.0 - t) + col2[ch] * t;
+        }
+      }
+      o[0] = col[0];
+      o[1] = col[1];
+      o[2] = col[2];
+    }
+}
+
+}  // extern "C"

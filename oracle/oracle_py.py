@@ -1,0 +1,254 @@
+"""ctypes binding of the FP64 oracle (oracle/_build/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, the smoke check and the
+CPU-baseline leg of bench.py, as the checker. Arrays are numpy; layouts are
+those of include/drv.h.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_build" / "liboracle.so"
+
+_lib = None
+
+
+def build() -> Path:
+    r = subprocess.run(["make", "-s", "-C", str(HERE)], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
+    return LIB
+
+
+def _abi():
+    import sys
+    sys.path.insert(0, str(HERE.parent))
+    from dynamicradiancevolume_gb300 import abi  # struct layouts only (pure ctypes, no library load)
+    return abi
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB.exists():
+        build()
+    abi = _abi()
+    lib = C.CDLL(str(LIB))
+    P, VP, I, D = C.POINTER, C.c_void_p, C.c_int, C.c_double
+    sig = {
+        "orc_morton_decode": (None, [C.c_uint32, P(C.c_uint32), P(C.c_uint32)]),
+        "orc_pack_normal16i": (None, [P(D), P(C.c_int16)]),
+        "orc_unpack_normal16i": (None, [P(C.c_int16), P(D)]),
+        "orc_sh_constants": (None, [I, P(D), P(D)]),
+        "orc_sh_irradiance": (None, [I, I, P(D), P(D), P(D)]),
+        "orc_sample_voxels": (D, [I, VP, VP, P(D), D]),
+        "orc_cone_shadow": (D, [P(abi.DrvVolumeInfo), I, VP, VP, P(D), P(D), D, I]),
+        "orc_prepare_light": (None, [P(abi.DrvLightDesc), P(abi.DrvSpotLight)]),
+        "orc_prepare_camera": (None, [P(abi.DrvCamera), P(abi.DrvPerFrame)]),
+        "orc_compute_volume_info": (None, [P(abi.DrvConfig), P(C.c_float), P(C.c_float), P(C.c_float),
+                                           P(abi.DrvVolumeInfo)]),
+        "orc_raycast_gbuffer": (None, [P(abi.DrvBox), I, P(abi.DrvPerFrame), P(abi.DrvCamera), I, I, VP, VP, VP, VP]),
+        "orc_raycast_rsm": (None, [P(abi.DrvBox), I, P(abi.DrvSpotLight), VP, VP, VP]),
+        "orc_downsample_rsm": (None, [I, VP, VP, VP, VP, VP, VP]),
+        "orc_extract_vpls": (None, [P(abi.DrvSpotLight), I, VP, VP, VP, VP, VP, VP]),
+        "orc_voxelize": (None, [P(abi.DrvBox), I, P(abi.DrvVolumeInfo), I, VP]),
+        "orc_build_mips": (None, [I, VP, VP]),
+        "orc_allocate_caches": (I, [P(abi.DrvConfig), P(abi.DrvVolumeInfo), P(abi.DrvPerFrame), I, I, VP, VP, VP,
+                                    P(C.c_uint32)]),
+        "orc_light_caches": (None, [P(abi.DrvConfig), P(abi.DrvVolumeInfo), I, VP, I, P(abi.DrvSpotLight),
+                                    P(VP), P(VP), P(I), VP, VP, VP, I]),
+        "orc_apply": (None, [P(abi.DrvConfig), P(abi.DrvVolumeInfo), P(abi.DrvPerFrame), I, I, VP, VP, I, VP, VP, I,
+                             VP, VP, I]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _p(a: np.ndarray):
+    assert a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def n_mip_values(N: int) -> int:
+    s, l = 0, 1
+    while (N >> l) >= 1:
+        s += (N >> l) ** 3
+        l += 1
+    return s
+
+
+def mip_level(mips: np.ndarray, N: int, level: int) -> np.ndarray:
+    off = sum((N >> l) ** 3 for l in range(1, level))
+    n = N >> level
+    return mips[off:off + n ** 3].reshape(n, n, n)
+
+
+# -- wrappers ---------------------------------------------------------------
+def morton_decode(m: int):
+    x, y = C.c_uint32(), C.c_uint32()
+    load().orc_morton_decode(m, C.byref(x), C.byref(y))
+    return x.value, y.value
+
+
+def pack_normal16i(n) -> tuple:
+    a = (C.c_double * 3)(*n)
+    o = (C.c_int16 * 2)()
+    load().orc_pack_normal16i(a, o)
+    return o[0], o[1]
+
+
+def unpack_normal16i(p) -> np.ndarray:
+    a = (C.c_int16 * 2)(*p)
+    o = (C.c_double * 3)()
+    load().orc_unpack_normal16i(a, o)
+    return np.array(o[:])
+
+
+def sh_constants(sh2_sign: int):
+    cl, ev = (C.c_double * 5)(), (C.c_double * 5)()
+    load().orc_sh_constants(sh2_sign, cl, ev)
+    return np.array(cl[:]), np.array(ev[:])
+
+
+def sh_irradiance(sh_order: int, sh2_sign: int, sh27, n) -> np.ndarray:
+    sh = (C.c_double * 27)(*np.asarray(sh27, dtype=np.float64).ravel())
+    nn = (C.c_double * 3)(*n)
+    o = (C.c_double * 3)()
+    load().orc_sh_irradiance(sh_order, sh2_sign, sh, nn, o)
+    return np.array(o[:])
+
+
+def prepare_light(desc):
+    abi = _abi()
+    o = abi.DrvSpotLight()
+    load().orc_prepare_light(C.byref(desc), C.byref(o))
+    return o
+
+
+def prepare_camera(cam):
+    abi = _abi()
+    o = abi.DrvPerFrame()
+    load().orc_prepare_camera(C.byref(cam), C.byref(o))
+    return o
+
+
+def compute_volume_info(cfg, amin, amax, cam_pos):
+    abi = _abi()
+    o = abi.DrvVolumeInfo()
+    f3 = C.c_float * 3
+    load().orc_compute_volume_info(C.byref(cfg), f3(*amin), f3(*amax), f3(*cam_pos), C.byref(o))
+    return o
+
+
+def raycast_gbuffer(boxes, n_boxes, frame, cam, W, H):
+    depth = np.zeros((H, W), np.float32)
+    n16 = np.zeros((H, W, 2), np.int16)
+    n32 = np.zeros((H, W, 3), np.float32)
+    alb = np.zeros((H, W, 3), np.float32)
+    load().orc_raycast_gbuffer(boxes, n_boxes, C.byref(frame), C.byref(cam), W, H, _p(depth), _p(n16), _p(n32),
+                               _p(alb))
+    return depth, n16, n32, alb
+
+
+def raycast_rsm(boxes, n_boxes, light):
+    R = light.rsm_render_resolution
+    flux = np.zeros((R, R, 3), np.float32)
+    n16 = np.zeros((R, R, 2), np.int16)
+    dls = np.zeros((R, R, 2), np.float32)
+    load().orc_raycast_rsm(boxes, n_boxes, C.byref(light), _p(flux), _p(n16), _p(dls))
+    return flux, n16, dls
+
+
+def downsample_rsm(flux, n16, dls):
+    R = flux.shape[0]
+    h = R // 2
+    fo = np.zeros((h, h, 3), np.float32)
+    no = np.zeros((h, h, 2), np.int16)
+    do = np.zeros((h, h, 2), np.float32)
+    load().orc_downsample_rsm(R, _p(np.ascontiguousarray(flux)), _p(np.ascontiguousarray(n16)),
+                              _p(np.ascontiguousarray(dls)), _p(fo), _p(no), _p(do))
+    return fo, no, do
+
+
+def rsm_chain(flux, n16, dls, levels: int):
+    chain = [(flux, n16, dls)]
+    for _ in range(levels):
+        chain.append(downsample_rsm(*chain[-1]))
+    return chain
+
+
+def extract_vpls(light, flux, n16, dls, dls_shadow):
+    R = flux.shape[0]
+    n = R * R
+    interval = light.indirect_shadow_sample_interval
+    vpl = np.zeros((n, 10), np.float64)
+    cones = np.zeros(((n + interval - 1) // interval, 4), np.float64)
+    load().orc_extract_vpls(C.byref(light), R, _p(np.ascontiguousarray(flux)), _p(np.ascontiguousarray(n16)),
+                            _p(np.ascontiguousarray(dls)), _p(np.ascontiguousarray(dls_shadow)), _p(vpl), _p(cones))
+    return vpl, cones
+
+
+def voxelize(boxes, n_boxes, vol, N):
+    bits = np.zeros(N ** 3 // 32, np.uint32)
+    load().orc_voxelize(boxes, n_boxes, C.byref(vol), N, _p(bits))
+    return bits
+
+
+def build_mips(N, bits):
+    mips = np.zeros(n_mip_values(N), np.float64)
+    load().orc_build_mips(N, _p(np.ascontiguousarray(bits, dtype=np.uint32)), _p(mips))
+    return mips
+
+
+def sample_voxels(N, bits, mips, s, lod) -> float:
+    return load().orc_sample_voxels(N, _p(bits), _p(mips), (C.c_double * 3)(*s), lod)
+
+
+def cone_shadow(vol, N, bits, mips, cache_pos, avg, dsr, max_steps) -> float:
+    return load().orc_cone_shadow(C.byref(vol), N, _p(bits), _p(mips), (C.c_double * 3)(*cache_pos),
+                                  (C.c_double * 3)(*avg), dsr, max_steps)
+
+
+def allocate_caches(cfg, vol, frame, depth):
+    H, W = depth.shape
+    atlas = np.zeros((cfg.cav_res, cfg.cav_res, cfg.n_cascades * cfg.cav_res), np.uint32)
+    pos = np.zeros((cfg.max_caches, 3), np.float32)
+    count = C.c_uint32()
+    st = load().orc_allocate_caches(C.byref(cfg), C.byref(vol), C.byref(frame), W, H,
+                                    _p(np.ascontiguousarray(depth, dtype=np.float32)), _p(atlas), _p(pos),
+                                    C.byref(count))
+    n = min(count.value, cfg.max_caches)
+    return st, atlas, pos[:n].copy(), count.value
+
+
+def light_caches(cfg, vol, positions, lights, vpls, cones, bits, mips, n_threads=0):
+    positions = np.ascontiguousarray(positions, dtype=np.float32)
+    n = positions.shape[0]
+    L = len(vpls)
+    sh = np.zeros((n, 27), np.float64)
+    vp = (C.c_void_p * L)(*[v.ctypes.data for v in vpls])
+    cp = (C.c_void_p * L)(*[c.ctypes.data for c in cones])
+    nv = (C.c_int * L)(*[v.shape[0] for v in vpls])
+    load().orc_light_caches(C.byref(cfg), C.byref(vol), n, _p(positions), L, lights, vp, cp, nv, _p(bits), _p(mips),
+                            _p(sh), n_threads)
+    return sh
+
+
+def apply(cfg, vol, frame, depth, normal, normal_format, albedo, atlas, sh, n_threads=0):
+    H, W = depth.shape
+    out = np.zeros((H, W, 3), np.float64)
+    sh = np.ascontiguousarray(sh, dtype=np.float64)
+    load().orc_apply(C.byref(cfg), C.byref(vol), C.byref(frame), W, H, _p(np.ascontiguousarray(depth)),
+                     _p(np.ascontiguousarray(normal)), normal_format, _p(np.ascontiguousarray(albedo)),
+                     _p(np.ascontiguousarray(atlas, dtype=np.uint32)), sh.shape[0], _p(sh), _p(out), n_threads)
+    return out
