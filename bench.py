@@ -131,10 +131,11 @@ def sh_flops_per_pair(sh_order: int) -> int:
 
 def kernel_launches_per_frame(w) -> int:
     # per light: (read_lod + shadow_lod) downsample passes + 1 extraction;
-    # voxelize 1 + mips (1, +1 tail above 32^3); allocate 1; light 1; apply 1.
+    # voxelize 1 + mips (1, +1 tail above 32^3) + corner grid 1; allocate 1;
+    # light 1; apply 1.
     n = w.n_lights * (w.rsm_read_lod + w.shadow_lod + 1)
     if w.indirect_shadow:
-        n += 1 + (2 if w.voxel_res > 32 else 1)
+        n += 1 + (2 if w.voxel_res > 32 else 1) + 1
     return n + 3
 
 

@@ -114,7 +114,8 @@ class DrvCacheCounter(C.Structure):
 
 class DrvBuffers(C.Structure):
     _fields_ = [("cache_entries", C.c_void_p), ("entry_stride", C.c_uint32), ("cav_atlas", C.c_void_p),
-                ("counter", C.c_void_p), ("voxel_bits", C.c_void_p), ("voxel_mips", C.c_void_p * 16),
+                ("counter", C.c_void_p), ("voxel_bits", C.c_void_p), ("voxel_corners", C.c_void_p),
+                ("voxel_mips", C.c_void_p * 16),
                 ("n_voxel_levels", C.c_int32), ("vpls", C.c_void_p * MAX_LIGHTS),
                 ("cones", C.c_void_p * MAX_LIGHTS), ("n_vpls", C.c_int32 * MAX_LIGHTS), ("n_lights", C.c_int32)]
 

@@ -46,6 +46,9 @@ void release(Context* c) {
   cudaFree(c->counter);
   cudaFree(c->voxel_bits);
   cudaFree(c->mips);
+  cudaFree(c->vox_corners);
+  cudaFree(c->light_scratch);
+  cudaFree(c->light_tickets);
   for (int l = 0; l < DRV_MAX_LIGHTS; ++l) {
     for (int k = 1; k < drv::kMaxRsmLevels; ++k) {
       cudaFree(c->rsm[l].flux[k]);
@@ -141,6 +144,13 @@ drv_status drv_create(const DrvConfig* cfg, DrvContext** out) {
     off += n * n * n;
   }
   if ((e = cudaMalloc(&c->mips, off * 4)) != cudaSuccess) return bail(e);
+  if ((e = cudaMalloc(&c->vox_corners, (size_t)N * N * N)) != cudaSuccess) return bail(e);
+  // Light-stage chunk partials and per-cache tickets (tickets are reset by the
+  // kernel that consumes them, so they are zeroed once here).
+  if ((e = cudaMalloc(&c->light_scratch, (size_t)cfg->max_caches * drv::kMaxLightChunks * 27 * 4)) != cudaSuccess)
+    return bail(e);
+  if ((e = cudaMalloc(&c->light_tickets, (size_t)cfg->max_caches * 4)) != cudaSuccess) return bail(e);
+  if ((e = cudaMemset(c->light_tickets, 0, (size_t)cfg->max_caches * 4)) != cudaSuccess) return bail(e);
   // RSM chains (levels below the caller's render-resolution level) and VPLs.
   const int R = cfg->max_rsm_resolution;
   for (int l = 0; l < cfg->max_lights; ++l) {
@@ -203,6 +213,7 @@ drv_status drv_get_buffers(DrvContext* ctx, DrvBuffers* o) {
   o->cav_atlas = ctx->atlas;
   o->counter = ctx->counter;
   o->voxel_bits = ctx->voxel_bits;
+  o->voxel_corners = ctx->vox_corners;
   for (int l = 1; l < ctx->n_voxel_levels && l < 16; ++l) o->voxel_mips[l] = ctx->mips + ctx->mip_offset[l];
   o->n_voxel_levels = ctx->n_voxel_levels;
   for (int l = 0; l < DRV_MAX_LIGHTS; ++l) {
@@ -321,9 +332,10 @@ drv_status drv_voxelize(DrvContext* ctx, const DrvScene* scene, const DrvVolumeI
 
 drv_status drv_build_opacity_mips(DrvContext* ctx) {
   if (!ctx) return DRV_ERR_INVALID_ARG;
-  return cuda_check(ctx, drv::launch_build_mips(ctx->s(), ctx->cfg.voxel_res, ctx->voxel_bits, ctx->mips,
-                                                ctx->mip_offset, ctx->n_voxel_levels),
-                    "build_opacity_mips");
+  DRV_TRY_CUDA(ctx, drv::launch_build_mips(ctx->s(), ctx->cfg.voxel_res, ctx->voxel_bits, ctx->mips, ctx->mip_offset,
+                                            ctx->n_voxel_levels));
+  return cuda_check(ctx, drv::launch_build_corners(ctx->s(), ctx->cfg.voxel_res, ctx->voxel_bits, ctx->vox_corners),
+                    "build_corners");
 }
 
 // Renderer::AllocateCaches: clear counter and atlas (renderer.cpp:968-970),
@@ -354,8 +366,8 @@ drv_status drv_light_caches(DrvContext* ctx, const DrvSpotLight* lights, int32_t
     ll.lights[l].interval = ctx->interval[l];
   }
   return cuda_check(ctx, drv::launch_light_caches(ctx->s(), ctx->cfg, *vol, ll, ctx->counter, ctx->entries,
-                                                  ctx->entry_stride, ctx->voxel_bits, ctx->mips, ctx->mip_offset,
-                                                  ctx->num_sms),
+                                                  ctx->entry_stride, ctx->vox_corners, ctx->mips, ctx->mip_offset,
+                                                  ctx->light_scratch, ctx->light_tickets, ctx->num_sms),
                     "light_caches");
 }
 

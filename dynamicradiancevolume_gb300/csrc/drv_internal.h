@@ -12,6 +12,7 @@ namespace drv {
 
 constexpr int kMaxVoxelLevels = 16;
 constexpr int kMaxRsmLevels = 16;
+constexpr int kMaxLightChunks = 8;  // VPL-block chunks per cache in the light stage
 
 struct RsmChain {
   int res0 = 0;      // render resolution
@@ -61,6 +62,7 @@ struct Context {
   // Voxels.
   uint32_t* voxel_bits = nullptr;
   size_t voxel_words = 0;
+  uint8_t* vox_corners = nullptr;  // level 0, corner-packed bytes in 4^3 bricks
   float* mips = nullptr;  // levels 1..L concatenated (FP32)
   size_t mip_offset[kMaxVoxelLevels] = {};
   int n_voxel_levels = 0;
@@ -77,7 +79,12 @@ struct Context {
   DrvBox* d_boxes = nullptr;
   int box_capacity = 0;
   int resident_boxes = -1;  // boxes currently on the device (-1: none)
+  // Light-stage partial sums: [max_caches * kMaxLightChunks][27] and a ticket per cache.
+  float* light_scratch = nullptr;
+  uint32_t* light_tickets = nullptr;
 };
+
+int light_chunks(int total_blocks);
 
 RayFrame make_ray_frame(const float pos[3], const float dir[3], const float up[3], double tan_x, double tan_y);
 
@@ -93,12 +100,14 @@ cudaError_t launch_voxelize(cudaStream_t s, const DrvBox* boxes, int n_boxes, co
                             uint32_t* bits);
 cudaError_t launch_build_mips(cudaStream_t s, int n, const uint32_t* bits, float* mips, const size_t* offsets,
                               int n_levels);
+cudaError_t launch_build_corners(cudaStream_t s, int n, const uint32_t* bits, uint8_t* corners);
 cudaError_t launch_allocate(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const DrvPerFrame& f,
                             const float* depth, int w, int h, uint32_t* atlas, void* entries, uint32_t entry_stride,
                             DrvCacheCounter* counter, uint32_t* ticket, uint32_t* err);
 cudaError_t launch_light_caches(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const LightLaunch& ll,
                                 const DrvCacheCounter* counter, void* entries, uint32_t entry_stride,
-                                const uint32_t* bits, const float* mips, const size_t* mip_offsets, int num_sms);
+                                const uint8_t* corners, const float* mips, const size_t* mip_offsets, float* scratch,
+                                uint32_t* tickets, int num_sms);
 cudaError_t launch_apply(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const DrvPerFrame& f,
                          const DrvGBufferView& g, const uint32_t* atlas, const void* entries, uint32_t entry_stride,
                          const DrvCacheCounter* counter, float* out_rgb);

@@ -171,7 +171,38 @@ __global__ void __launch_bounds__(256) mips_tail_kernel(int N, int first_level, 
   }
 }
 
+// Corner-packed level 0 (see voxel_sample.cuh): byte (x, y, z) = the 8 voxels
+// (x + dx, y + dy, z + dz) with +1 clamped to N - 1, bit dx | dy << 1 | dz << 2,
+// stored in 4x4x4 bricks; one thread per byte, written in brick order.
+__global__ void __launch_bounds__(256) corners_kernel(int N, int log2n, const uint32_t* __restrict__ bits,
+                                                      uint8_t* __restrict__ out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t total = (uint32_t)N * N * N;
+  if (i >= total) return;
+  const int lnb = log2n - 2, nb = N >> 2;
+  const uint32_t brick = i >> 6, in = i & 63u;
+  const int x = (int)(brick & (nb - 1)) * 4 + (int)(in & 3u);
+  const int y = (int)((brick >> lnb) & (nb - 1)) * 4 + (int)((in >> 2) & 3u);
+  const int z = (int)(brick >> (2 * lnb)) * 4 + (int)(in >> 4);
+  uint32_t b = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const int xx = min(x + (k & 1), N - 1), yy = min(y + ((k >> 1) & 1), N - 1), zz = min(z + (k >> 2), N - 1);
+    const size_t v = ((size_t)zz * N + yy) * N + xx;
+    b |= ((__ldg(bits + (v >> 5)) >> (v & 31)) & 1u) << k;
+  }
+  out[i] = (uint8_t)b;
+}
+
 }  // namespace
+
+cudaError_t launch_build_corners(cudaStream_t s, int n, const uint32_t* bits, uint8_t* corners) {
+  int l = 0;
+  while ((1 << (l + 1)) <= n) ++l;
+  const uint32_t total = (uint32_t)n * n * n;
+  corners_kernel<<<(total + 255) / 256, 256, 0, s>>>(n, l, bits, corners);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_voxelize(cudaStream_t s, const DrvBox* boxes, int n_boxes, const DrvVolumeInfo& vol, int n,
                             uint32_t* bits) {

@@ -257,6 +257,8 @@ typedef struct DrvBuffers {
   uint32_t* cav_atlas;              /* R32UI [n_cascades*res][res][res], x fastest */
   DrvCacheCounter* counter;
   uint32_t* voxel_bits;             /* level 0 as a bitmask, bit (x&31) of word ((z*N+y)*N+x)/32 */
+  uint8_t* voxel_corners;           /* level 0 corner-packed: byte (x,y,z) = voxels (x+dx,y+dy,z+dz), +1 clamped,
+                                       bit dx|dy<<1|dz<<2, stored in 4x4x4 bricks of 64 bytes */
   void* voxel_mips[16];             /* levels 1..L (index 1..L), float (FP32) or half (BF16 precision) */
   int32_t n_voxel_levels;           /* levels including 0 */
   DrvVPL* vpls[DRV_MAX_LIGHTS];     /* FP32 VPL array per light, Morton order */

@@ -163,6 +163,29 @@ def test_opacity_mips_exact(case, request, oracle):
         assert np.array_equal(g.astype(np.float64), oracle.mip_level(mips, r.w.voxel_res, l))
 
 
+@pytest.mark.parametrize("case", ["c1", "c2r"])
+def test_corner_grid_matches_bits(case, request):
+    """The bricked corner-packed level-0 bytes repeat the bitmask exactly."""
+    r = request.getfixturevalue(case)
+    N = r.w.voxel_res
+    b = r.pipe.buffers()
+    g = r.pipe._dev_tensor(b.voxel_corners, N ** 3, r.torch.uint8).cpu().numpy()
+    vox = np.unpackbits(r.bits.view(np.uint8), bitorder="little").reshape(N, N, N)  # [z][y][x]
+    i = np.arange(N ** 3)
+    brick, inn = i >> 6, i & 63
+    nb = N // 4
+    x = (brick % nb) * 4 + (inn & 3)
+    y = ((brick // nb) % nb) * 4 + ((inn >> 2) & 3)
+    z = (brick // (nb * nb)) * 4 + (inn >> 4)
+    exp = np.zeros(N ** 3, np.uint8)
+    for k in range(8):
+        xx = np.minimum(x + (k & 1), N - 1)
+        yy = np.minimum(y + ((k >> 1) & 1), N - 1)
+        zz = np.minimum(z + (k >> 2), N - 1)
+        exp |= (vox[zz, yy, xx] << k).astype(np.uint8)
+    assert np.array_equal(g, exp)
+
+
 def _key_set(positions):
     return set(map(tuple, np.asarray(positions, np.float32).tolist()))
 
@@ -247,13 +270,18 @@ def test_drv_frame_equals_stage_sequence(c1, lib):
 def test_sh2_sign_modes_end_to_end(sign, lib, oracle, cuda):
     w = pipeline.scaled(pipeline.WORKLOADS["c1_small"], sh_order=2)
     r = Run(w, oracle, seed=7, sh2_sign=sign)
-    ref = oracle_frame(r, oracle)
-    assert rel_l2(r.out, ref) < 1e-2
-    other = oracle_frame(r, oracle, sh2_sign=1 - sign)
-    # The modes differ only in the mixed band-2 terms (a small share of a
-    # diffuse image); the GPU must sit measurably closer to its own mode.
-    assert rel_l2(other, ref) > 0
-    assert rel_l2(r.out, ref) < 0.5 * rel_l2(r.out, other)
+    assert rel_l2(r.out, oracle_frame(r, oracle)) < 1e-2
+    # On identical SH inputs the apply tells the two modes apart: the GPU
+    # matches the FP64 apply of its own mode far better than the other mode.
+    cfg_other = abi.DrvConfig.from_buffer_copy(r.hf.config)
+    cfg_other.sh2_sign = 1 - sign
+    own = oracle.apply(r.hf.config, r.hf.volume, r.hf.frame, r.depth, r.n16, abi.NORMAL_RG16I, r.albedo, r.atlas,
+                       r.gpu_sh())
+    other = oracle.apply(cfg_other, r.hf.volume, r.hf.frame, r.depth, r.n16, abi.NORMAL_RG16I, r.albedo, r.atlas,
+                         r.gpu_sh())
+    e_own, e_other = rel_l2(r.out, own), rel_l2(r.out, other)
+    assert e_own < 1e-5
+    assert e_other > 10 * e_own
 
 
 def test_normal_format_f32_matches_rg16i_closely(lib, oracle, cuda):
