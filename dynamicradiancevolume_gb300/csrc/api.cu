@@ -174,6 +174,7 @@ drv_status drv_create(const DrvConfig* cfg, DrvContext** out) {
 drv_status drv_destroy(DrvContext* ctx) {
   if (!ctx) return DRV_ERR_INVALID_ARG;
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->has_user_stream) cudaStreamSynchronize(ctx->user_stream);
   release(ctx);
   delete ctx;
   return DRV_OK;
@@ -182,6 +183,7 @@ drv_status drv_destroy(DrvContext* ctx) {
 drv_status drv_set_stream(DrvContext* ctx, void* stream) {
   if (!ctx) return DRV_ERR_INVALID_ARG;
   ctx->user_stream = (cudaStream_t)stream;
+  ctx->has_user_stream = true;
   return DRV_OK;
 }
 

@@ -46,8 +46,9 @@ struct RayFrame {
 struct Context {
   DrvConfig cfg{};
   cudaStream_t stream = nullptr;       // owned
-  cudaStream_t user_stream = nullptr;  // set by drv_set_stream, borrowed
-  cudaStream_t s() const { return user_stream ? user_stream : stream; }
+  cudaStream_t user_stream = nullptr;  // set by drv_set_stream, borrowed (may be the legacy stream 0)
+  bool has_user_stream = false;
+  cudaStream_t s() const { return has_user_stream ? user_stream : stream; }
   int device = 0;
   int num_sms = 0;
   std::string last_error;

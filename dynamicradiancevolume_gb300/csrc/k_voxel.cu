@@ -173,25 +173,51 @@ __global__ void __launch_bounds__(256) mips_tail_kernel(int N, int first_level, 
 
 // Corner-packed level 0 (see voxel_sample.cuh): byte (x, y, z) = the 8 voxels
 // (x + dx, y + dy, z + dz) with +1 clamped to N - 1, bit dx | dy << 1 | dz << 2,
-// stored in 4x4x4 bricks; one thread per byte, written in brick order.
+// stored in 4x4x4 bricks. One thread per brick: it reads the 5x5 rows of the
+// brick's 5x5x5 neighbourhood from the bitmask and writes its 64 bytes as four
+// 16-byte stores (consecutive threads write consecutive bricks).
 __global__ void __launch_bounds__(256) corners_kernel(int N, int log2n, const uint32_t* __restrict__ bits,
                                                       uint8_t* __restrict__ out) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t total = (uint32_t)N * N * N;
-  if (i >= total) return;
   const int lnb = log2n - 2, nb = N >> 2;
-  const uint32_t brick = i >> 6, in = i & 63u;
-  const int x = (int)(brick & (nb - 1)) * 4 + (int)(in & 3u);
-  const int y = (int)((brick >> lnb) & (nb - 1)) * 4 + (int)((in >> 2) & 3u);
-  const int z = (int)(brick >> (2 * lnb)) * 4 + (int)(in >> 4);
-  uint32_t b = 0;
+  const uint32_t brick = blockIdx.x * blockDim.x + threadIdx.x;
+  if (brick >= (uint32_t)nb * nb * nb) return;
+  const int x0 = (int)(brick & (nb - 1)) * 4;
+  const int y0 = (int)((brick >> lnb) & (nb - 1)) * 4;
+  const int z0 = (int)(brick >> (2 * lnb)) * 4;
+  const int wpr = N >> 5;
+  // rows[dz][dy] = 5 voxel bits x0..x0+4 (x0+4 clamped) of row (y0+dy, z0+dz), clamped
+  uint32_t rows[5][5];
 #pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    const int xx = min(x + (k & 1), N - 1), yy = min(y + ((k >> 1) & 1), N - 1), zz = min(z + (k >> 2), N - 1);
-    const size_t v = ((size_t)zz * N + yy) * N + xx;
-    b |= ((__ldg(bits + (v >> 5)) >> (v & 31)) & 1u) << k;
-  }
-  out[i] = (uint8_t)b;
+  for (int dz = 0; dz < 5; ++dz)
+#pragma unroll
+    for (int dy = 0; dy < 5; ++dy) {
+      const int y = min(y0 + dy, N - 1), z = min(z0 + dz, N - 1);
+      const uint32_t* row = bits + ((size_t)z * N + y) * wpr;
+      const uint32_t w = __ldg(row + (x0 >> 5));
+      uint32_t r = (w >> (x0 & 31)) & 0xFu;
+      const int x4 = min(x0 + 4, N - 1);
+      const uint32_t w4 = (x4 >> 5) == (x0 >> 5) ? w : __ldg(row + (x4 >> 5));
+      r |= ((w4 >> (x4 & 31)) & 1u) << 4;
+      rows[dz][dy] = r;
+    }
+  uint32_t words[16];
+#pragma unroll
+  for (int lz = 0; lz < 4; ++lz)
+#pragma unroll
+    for (int ly = 0; ly < 4; ++ly) {
+      uint32_t wv = 0;
+#pragma unroll
+      for (int lx = 0; lx < 4; ++lx) {
+        uint32_t b = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) b |= ((rows[lz + (k >> 2)][ly + ((k >> 1) & 1)] >> (lx + (k & 1))) & 1u) << k;
+        wv |= b << (8 * lx);
+      }
+      words[lz * 4 + ly] = wv;
+    }
+  uint4* dst = reinterpret_cast<uint4*>(out + (size_t)brick * 64);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) dst[q] = make_uint4(words[4 * q], words[4 * q + 1], words[4 * q + 2], words[4 * q + 3]);
 }
 
 }  // namespace
@@ -199,8 +225,8 @@ __global__ void __launch_bounds__(256) corners_kernel(int N, int log2n, const ui
 cudaError_t launch_build_corners(cudaStream_t s, int n, const uint32_t* bits, uint8_t* corners) {
   int l = 0;
   while ((1 << (l + 1)) <= n) ++l;
-  const uint32_t total = (uint32_t)n * n * n;
-  corners_kernel<<<(total + 255) / 256, 256, 0, s>>>(n, l, bits, corners);
+  const uint32_t bricks = (uint32_t)(n / 4) * (n / 4) * (n / 4);
+  corners_kernel<<<(bricks + 255) / 256, 256, 0, s>>>(n, l, bits, corners);
   return cudaGetLastError();
 }
 

@@ -93,6 +93,11 @@ __device__ __forceinline__ float sample_voxels(const VoxelView& v, float sx, flo
 // Indirect-shadow cone, cacheLightingRSM.comp:195-230: march from the cache
 // toward the block's average VAL position, growing the sample sphere with the
 // distance, front-to-back occlusion, at most max_steps samples.
+//
+// The positions, sphere radii and the exit step depend only on the geometry,
+// never on the voxels, so four steps are laid out first and their four
+// fetches issued together; the occlusion is then composited in step order,
+// which gives the same value as the step-by-step loop.
 __device__ __forceinline__ float cone_shadow(const VoxelView& v, float voxel_size, int max_steps, float cx, float cy,
                                              float cz, float px, float py, float pz, float ax, float ay, float az,
                                              float dsr) {
@@ -105,16 +110,25 @@ __device__ __forceinline__ float cone_shadow(const VoxelView& v, float voxel_siz
   float occlusion = 0.0f, step = 1.0f, dist = 0.0f;
   const float goal = light_dist / voxel_size - 2.0f;
   const float k = 2.0f / (1.0f - dsr);
-  for (int s = 0; s < max_steps; ++s) {
-    qx += dx * step;
-    qy += dy * step;
-    qz += dz * step;
-    dist += step;
-    const float radius = dist * dsr;
-    const float occ = sample_voxels(v, qx, qy, qz, __log2f(radius));
-    occlusion += (1.0f - occlusion) * occ;
-    if (dist >= goal) break;
-    step = fmaxf(1.0f, radius * k);
+  bool done = false;
+  for (int s = 0; s < max_steps && !done; s += 4) {
+    float occ[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      occ[u] = 0.0f;
+      if (!done && s + u < max_steps) {
+        qx += dx * step;
+        qy += dy * step;
+        qz += dz * step;
+        dist += step;
+        const float radius = dist * dsr;
+        occ[u] = sample_voxels(v, qx, qy, qz, __log2f(radius));
+        if (dist >= goal) done = true;
+        step = fmaxf(1.0f, radius * k);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) occlusion += (1.0f - occlusion) * occ[u];
   }
   return fminf(fmaxf(1.0f - occlusion, 0.0f), 1.0f);
 }

@@ -130,7 +130,9 @@ class Pipeline:
         self.device = torch.device(device)
         self.ctx = C.c_void_p()
         check(self.lib.drv_create(C.byref(hf.config), C.byref(self.ctx)))
-        self.stream = torch.cuda.current_stream(self.device)
+        # A dedicated stream: every stage of this pipeline is ordered on it, and
+        # callers time it with events recorded on the same stream.
+        self.stream = torch.cuda.Stream(self.device)
         check(self.lib.drv_set_stream(self.ctx, C.c_void_p(self.stream.cuda_stream)), self.ctx)
         H, W = w.height, w.width
         dev = self.device
