@@ -8,15 +8,16 @@
 //  - the shadow blocks of all lights (IndirectShadowComputationSampleInterval
 //    consecutive VPLs share one cone) form one index space, cut into
 //    `n_chunks` chunks;
-//  - a unit of work is (cache, chunk); a persistent grid walks the units up to
-//    the device-side cache count (no indirect dispatch: graph-capturable);
-//  - inside a unit, the 128 threads take blocks round-robin: every lane's cone
+//  - a unit of work is (cache, chunk) and belongs to one warp; a persistent
+//    grid walks the units up to the device-side cache count (no indirect
+//    dispatch: graph-capturable), and warps never wait for each other;
+//  - inside a unit, the 32 lanes take blocks round-robin: every lane's cone
 //    starts at the same cache, so the first steps of all 32 cones of a warp
 //    fetch the same voxel bytes;
-//  - the CTA reduces its 27 partial SH sums (warp shuffles + shared memory);
-//    with several chunks, partials go to a scratch slot per unit and the last
-//    CTA to finish a cache (a ticket counter per cache) adds them in chunk
-//    order, so results do not depend on scheduling, then resets the ticket;
+//  - the warp reduces its 27 partial SH sums with shuffles; with several
+//    chunks, partials go to a scratch slot per unit and the last warp to
+//    finish a cache (a ticket counter per cache) adds them in chunk order, so
+//    results do not depend on scheduling, then resets the ticket;
 //  - the entry's SH is read-modify-written once (`+=`, as the reference's
 //    per-light dispatches accumulate).
 #include <cmath>
@@ -76,15 +77,14 @@ __device__ __forceinline__ void accumulate_vpl(const LightParams& p, float* acc,
   }
 }
 
+// One warp = one unit (cache, chunk); warps never wait for each other.
 template <int NK>
 __global__ void __launch_bounds__(kThreads) light_kernel(LightParams p) {
-  __shared__ float s_red[kWarps][NK * 3];
-  __shared__ float s_sum[NK * 3];
-  __shared__ uint32_t s_last;
   const uint32_t count = min((uint32_t)max(p.counter->total_light_cache_count, 0), p.max_caches);
   const uint32_t n_units = count * (uint32_t)p.n_chunks;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (uint32_t u = blockIdx.x; u < n_units; u += gridDim.x) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t warps = gridDim.x * kWarps;
+  for (uint32_t u = blockIdx.x * kWarps + (threadIdx.x >> 5); u < n_units; u += warps) {
     const uint32_t cache = u / (uint32_t)p.n_chunks;
     const int chunk = (int)(u % (uint32_t)p.n_chunks);
     float* entry = p.entries + (size_t)cache * p.stride_floats;
@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(kThreads) light_kernel(LightParams p) {
     for (int k = 0; k < NK * 3; ++k) acc[k] = 0.0f;
     const int b0 = chunk * p.chunk_blocks, b1 = min(b0 + p.chunk_blocks, p.total_blocks);
     int l = 0;
-    for (int b = b0 + (int)threadIdx.x; b < b1; b += kThreads) {
+    for (int b = b0 + lane; b < b1; b += 32) {
       while (b >= p.block_base[l + 1]) ++l;
       const LightArgs& la = p.ll.lights[l];
       const int lb = b - p.block_base[l];
@@ -110,54 +110,41 @@ __global__ void __launch_bounds__(kThreads) light_kernel(LightParams p) {
       }
       for (int j = 0; j < nv; ++j) accumulate_vpl<NK>(p, acc, la.vpls + v0 + j, cx, cy, cz, shadowing);
     }
-    // CTA reduction of the NK*3 partial sums.
+    // Warp reduction: lane k (< NK*3) ends up holding coefficient k.
+    float mine = 0.0f;
 #pragma unroll
     for (int k = 0; k < NK * 3; ++k) {
       float v = acc[k];
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-      if (lane == 0) s_red[warp][k] = v;
+      if (lane == k) mine = v;
     }
-    __syncthreads();
-    if (threadIdx.x < NK * 3) {
-      float v = 0.0f;
-#pragma unroll
-      for (int w = 0; w < kWarps; ++w) v += s_red[w][threadIdx.x];
-      s_sum[threadIdx.x] = v;
-    }
-    __syncthreads();
     if (p.n_chunks == 1) {
-      if (threadIdx.x < NK * 3) {
-        const int k = threadIdx.x / 3, ch = threadIdx.x % 3;
-        entry[sh_offset(k, ch)] += s_sum[threadIdx.x];
-      }
-    } else {
-      float* slot = p.scratch + (size_t)u * (NK * 3);
-      if (threadIdx.x < NK * 3) slot[threadIdx.x] = s_sum[threadIdx.x];
-      __threadfence();
-      __syncthreads();
-      if (threadIdx.x == 0) s_last = atomicAdd(p.tickets + cache, 1u) == (uint32_t)p.n_chunks - 1u;
-      __syncthreads();
-      if (s_last) {
-        __threadfence();
-        if (threadIdx.x < NK * 3) {
-          const volatile float* base = p.scratch + (size_t)cache * p.n_chunks * (NK * 3);
-          float v = 0.0f;
-          for (int c = 0; c < p.n_chunks; ++c) v += base[c * (NK * 3) + threadIdx.x];
-          const int k = threadIdx.x / 3, ch = threadIdx.x % 3;
-          entry[sh_offset(k, ch)] += v;
-        }
-        if (threadIdx.x == 0) p.tickets[cache] = 0u;
-      }
+      if (lane < NK * 3) entry[sh_offset(lane / 3, lane % 3)] += mine;
+      continue;
     }
-    __syncthreads();
+    if (lane < NK * 3) p.scratch[(size_t)u * (NK * 3) + lane] = mine;
+    __threadfence();
+    uint32_t last = 0;
+    if (lane == 0) last = atomicAdd(p.tickets + cache, 1u) == (uint32_t)p.n_chunks - 1u;
+    last = __shfl_sync(0xffffffffu, last, 0);
+    if (last) {
+      __threadfence();
+      if (lane < NK * 3) {
+        const volatile float* base = p.scratch + (size_t)cache * p.n_chunks * (NK * 3);
+        float v = 0.0f;
+        for (int c = 0; c < p.n_chunks; ++c) v += base[c * (NK * 3) + lane];
+        entry[sh_offset(lane / 3, lane % 3)] += v;
+      }
+      if (lane == 0) p.tickets[cache] = 0u;
+    }
   }
 }
 
 }  // namespace
 
 int light_chunks(int total_blocks) {
-  int n = (total_blocks + 511) / 512;
+  int n = (total_blocks + 255) / 256;
   return n < 1 ? 1 : (n > kMaxLightChunks ? kMaxLightChunks : n);
 }
 

@@ -57,21 +57,19 @@ __device__ __forceinline__ float level0(const VoxelView& v, float sx, float sy, 
 }
 
 __device__ __forceinline__ float level_n(const VoxelView& v, int level, float sx, float sy, float sz) {
-  const int n = v.N >> level;
+  const int ln = v.log2n - level, n = 1 << ln;
   float ux = sx * n - 0.5f, uy = sy * n - 0.5f, uz = sz * n - 0.5f;
   float fx = floorf(ux), fy = floorf(uy), fz = floorf(uz);
   float ax = ux - fx, ay = uy - fy, az = uz - fz;
   int x0 = (int)fx, y0 = (int)fy, z0 = (int)fz;
   const int xa = min(max(x0, 0), n - 1), xb = min(max(x0 + 1, 0), n - 1);
-  const int ya = min(max(y0, 0), n - 1), yb = min(max(y0 + 1, 0), n - 1);
-  const int za = min(max(z0, 0), n - 1), zb = min(max(z0 + 1, 0), n - 1);
+  const int ya = min(max(y0, 0), n - 1) << ln, yb = min(max(y0 + 1, 0), n - 1) << ln;
+  const int za = min(max(z0, 0), n - 1) << (2 * ln), zb = min(max(z0 + 1, 0), n - 1) << (2 * ln);
   const float* m = v.mips + v.off[level];
-  const float* pa = m + ((size_t)za * n) * n;
-  const float* pb = m + ((size_t)zb * n) * n;
-  float t0 = __ldg(pa + ya * n + xa), t1 = __ldg(pa + ya * n + xb);
-  float t2 = __ldg(pa + yb * n + xa), t3 = __ldg(pa + yb * n + xb);
-  float t4 = __ldg(pb + ya * n + xa), t5 = __ldg(pb + ya * n + xb);
-  float t6 = __ldg(pb + yb * n + xa), t7 = __ldg(pb + yb * n + xb);
+  float t0 = __ldg(m + (za | ya | xa)), t1 = __ldg(m + (za | ya | xb));
+  float t2 = __ldg(m + (za | yb | xa)), t3 = __ldg(m + (za | yb | xb));
+  float t4 = __ldg(m + (zb | ya | xa)), t5 = __ldg(m + (zb | ya | xb));
+  float t6 = __ldg(m + (zb | yb | xa)), t7 = __ldg(m + (zb | yb | xb));
   float c00 = t0 + (t1 - t0) * ax, c10 = t2 + (t3 - t2) * ax;
   float c01 = t4 + (t5 - t4) * ax, c11 = t6 + (t7 - t6) * ax;
   float c0 = c00 + (c10 - c00) * ay, c1 = c01 + (c11 - c01) * ay;
@@ -93,11 +91,6 @@ __device__ __forceinline__ float sample_voxels(const VoxelView& v, float sx, flo
 // Indirect-shadow cone, cacheLightingRSM.comp:195-230: march from the cache
 // toward the block's average VAL position, growing the sample sphere with the
 // distance, front-to-back occlusion, at most max_steps samples.
-//
-// The positions, sphere radii and the exit step depend only on the geometry,
-// never on the voxels, so four steps are laid out first and their four
-// fetches issued together; the occlusion is then composited in step order,
-// which gives the same value as the step-by-step loop.
 __device__ __forceinline__ float cone_shadow(const VoxelView& v, float voxel_size, int max_steps, float cx, float cy,
                                              float cz, float px, float py, float pz, float ax, float ay, float az,
                                              float dsr) {
@@ -110,25 +103,15 @@ __device__ __forceinline__ float cone_shadow(const VoxelView& v, float voxel_siz
   float occlusion = 0.0f, step = 1.0f, dist = 0.0f;
   const float goal = light_dist / voxel_size - 2.0f;
   const float k = 2.0f / (1.0f - dsr);
-  bool done = false;
-  for (int s = 0; s < max_steps && !done; s += 4) {
-    float occ[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      occ[u] = 0.0f;
-      if (!done && s + u < max_steps) {
-        qx += dx * step;
-        qy += dy * step;
-        qz += dz * step;
-        dist += step;
-        const float radius = dist * dsr;
-        occ[u] = sample_voxels(v, qx, qy, qz, __log2f(radius));
-        if (dist >= goal) done = true;
-        step = fmaxf(1.0f, radius * k);
-      }
-    }
-#pragma unroll
-    for (int u = 0; u < 4; ++u) occlusion += (1.0f - occlusion) * occ[u];
+  for (int s = 0; s < max_steps; ++s) {
+    qx += dx * step;
+    qy += dy * step;
+    qz += dz * step;
+    dist += step;
+    const float radius = dist * dsr;
+    occlusion += (1.0f - occlusion) * sample_voxels(v, qx, qy, qz, __log2f(radius));
+    if (dist >= goal) break;
+    step = fmaxf(1.0f, radius * k);
   }
   return fminf(fmaxf(1.0f - occlusion, 0.0f), 1.0f);
 }
