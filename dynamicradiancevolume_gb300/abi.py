@@ -159,7 +159,10 @@ PROTOTYPES = {
     "drv_frame": (C.c_int, [VP, P(DrvScene), P(DrvGBufferView), P(DrvPerFrame), P(DrvVolumeInfo),
                             P(DrvSpotLight), P(DrvRSMView), C.c_int32, VP]),
     "drv_get_cache_count": (C.c_int, [VP, P(C.c_uint32)]),
+    "drv_light_caches_static_scratch": (C.c_int, [P(DrvConfig), P(DrvVolumeInfo), P(VP), P(VP), P(C.c_int32),
+                                                  P(C.c_int32), C.c_int32, VP, VP, VP, VP, VP]),
 }
+STATIC_SCRATCH_MAX_CACHES = 4096
 
 
 def header_functions(header: Path) -> list[str]:

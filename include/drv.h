@@ -360,6 +360,31 @@ drv_status drv_frame(DrvContext* ctx, const DrvScene* scene, const DrvGBufferVie
 /* Optional cache-count readback (renderer.cpp:960-966). Synchronises. */
 drv_status drv_get_cache_count(DrvContext* ctx, uint32_t* out_count);
 
+/* ---- allocation-free light stage ------------------------------------------
+ * No counterpart in the reference: the reference renderer always owns its GL
+ * buffers. This is the cache-lighting stage (the kernel behind
+ * drv_light_caches) for callers that cannot allocate device memory — engines
+ * running inside a fixed, pre-reserved GPU memory arena, plug-ins hosted by
+ * them, code recorded into CUDA graphs. It needs no DrvContext and calls no
+ * cudaMalloc: its scratch (per-chunk partial sums and per-cache tickets) is a
+ * fixed array compiled into the library, which every GPU that loads the
+ * library holds until exit (about 3.5 MB). The caller passes every input
+ * (per-light VPL and cone arrays, the corner-packed level-0 voxel bytes and
+ * the FP32 mips 1..L as laid out by drv_build_opacity_mips, the cache counter)
+ * and the output (the cache entries: positions read, SH accumulated with +=)
+ * as device pointers, and the stream to run on.
+ *  - max_caches above DRV_STATIC_SCRATCH_MAX_CACHES returns DRV_ERR_CAPACITY;
+ *  - the first call on a device looks the array up on that device; make it
+ *    before any stream capture;
+ *  - all calls share the array (it keeps the last call's contents; each call
+ *    clears the tickets first): calls that overlap on the GPU race. */
+#define DRV_STATIC_SCRATCH_MAX_CACHES 4096
+drv_status drv_light_caches_static_scratch(const DrvConfig* cfg, const DrvVolumeInfo* vol,
+                                           const DrvVPL* const* vpls, const DrvShadowCone* const* cones,
+                                           const int32_t* n_vpls, const int32_t* intervals, int32_t n_lights,
+                                           const uint8_t* voxel_corners, const float* voxel_mips,
+                                           const DrvCacheCounter* counter, void* cache_entries, void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif
