@@ -52,6 +52,7 @@ struct LightParams {
   float ev[5];        // ShEvaFactor0, 1, 2n2_p1_n1, 20, 2p2 (renderer.cpp:302-306)
 };
 
+// acc points at this thread's column of a [NK*3][kThreads] shared array.
 template <int NK>
 __device__ __forceinline__ void accumulate_vpl(const LightParams& p, float* acc, const DrvVPL* __restrict__ vpl,
                                                float cx, float cy, float cz, float shadowing) {
@@ -71,15 +72,19 @@ __device__ __forceinline__ void accumulate_vpl(const LightParams& p, float* acc,
                        p.ev[3] * (tz * tz * 3.0f - 1.0f), p.ev[2] * tx * tz, p.ev[4] * (tx * tx - ty * ty)};
 #pragma unroll
   for (int k = 0; k < NK; ++k) {
-    acc[3 * k + 0] += bs[k] * L0;
-    acc[3 * k + 1] += bs[k] * L1;
-    acc[3 * k + 2] += bs[k] * L2;
+    acc[(3 * k + 0) * kThreads] += bs[k] * L0;
+    acc[(3 * k + 1) * kThreads] += bs[k] * L1;
+    acc[(3 * k + 2) * kThreads] += bs[k] * L2;
   }
 }
 
-// One warp = one unit (cache, chunk); warps never wait for each other.
+// One warp = one unit (cache, chunk); warps never wait for each other. The
+// SH partial sums live in shared memory (touched once per pair, against
+// hundreds of cone instructions), which keeps the cone loop's register
+// footprint small enough for 8 CTAs per SM.
 template <int NK>
-__global__ void __launch_bounds__(kThreads) light_kernel(LightParams p) {
+__global__ void __launch_bounds__(kThreads, 8) light_kernel(LightParams p) {
+  __shared__ float s_acc[NK * 3 * kThreads];
   const uint32_t count = min((uint32_t)max(p.counter->total_light_cache_count, 0), p.max_caches);
   const uint32_t n_units = count * (uint32_t)p.n_chunks;
   const int lane = threadIdx.x & 31;
@@ -91,9 +96,9 @@ __global__ void __launch_bounds__(kThreads) light_kernel(LightParams p) {
     const float cx = entry[0], cy = entry[1], cz = entry[2];
     const float scale = 1.0f / (p.voxel_size * p.vox.N);
     const float vx = (cx - p.vol_min[0]) * scale, vy = (cy - p.vol_min[1]) * scale, vz = (cz - p.vol_min[2]) * scale;
-    float acc[NK * 3];
+    float* acc = s_acc + threadIdx.x;
 #pragma unroll
-    for (int k = 0; k < NK * 3; ++k) acc[k] = 0.0f;
+    for (int k = 0; k < NK * 3; ++k) acc[k * kThreads] = 0.0f;
     const int b0 = chunk * p.chunk_blocks, b1 = min(b0 + p.chunk_blocks, p.total_blocks);
     int l = 0;
     for (int b = b0 + lane; b < b1; b += 32) {
@@ -114,7 +119,7 @@ __global__ void __launch_bounds__(kThreads) light_kernel(LightParams p) {
     float mine = 0.0f;
 #pragma unroll
     for (int k = 0; k < NK * 3; ++k) {
-      float v = acc[k];
+      float v = acc[k * kThreads];
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
       if (lane == k) mine = v;

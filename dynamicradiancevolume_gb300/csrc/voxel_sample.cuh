@@ -47,6 +47,10 @@ __device__ __forceinline__ float level0(const VoxelView& v, float sx, float sy, 
   y = min(y, n - 1);
   z = min(z, n - 1);
   const uint32_t b = __ldg(v.corners + corner_index(x, y, z, v.log2n));
+  // Trilinear weights sum to one, so eight equal corners give that value
+  // exactly: empty space (the common case) costs no interpolation.
+  if (b == 0u) return 0.0f;
+  if (b == 0xFFu) return 1.0f;
   const float t0 = (float)(b & 1u), t1 = (float)((b >> 1) & 1u), t2 = (float)((b >> 2) & 1u),
               t3 = (float)((b >> 3) & 1u), t4 = (float)((b >> 4) & 1u), t5 = (float)((b >> 5) & 1u),
               t6 = (float)((b >> 6) & 1u), t7 = (float)((b >> 7) & 1u);
