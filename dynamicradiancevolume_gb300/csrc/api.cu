@@ -75,7 +75,8 @@ drv_status validate_config(const DrvConfig* c, std::string& why) {
   if (c->max_lights < 1 || c->max_lights > DRV_MAX_LIGHTS) return why = "max_lights must be 1..16", DRV_ERR_INVALID_ARG;
   if (!is_pow2(c->max_rsm_resolution) || c->max_rsm_resolution > 4096)
     return why = "max_rsm_resolution must be a power of two <= 4096", DRV_ERR_INVALID_ARG;
-  if (c->precision != DRV_PRECISION_FP32) return why = "precision mode not available", DRV_ERR_NOT_SUPPORTED;
+  if (c->precision != DRV_PRECISION_FP32 && c->precision != DRV_PRECISION_BF16)
+    return why = "precision must be DRV_PRECISION_FP32 or DRV_PRECISION_BF16", DRV_ERR_INVALID_ARG;
   if (c->visibility != DRV_VISIBILITY_CONE) return why = "visibility mode not available", DRV_ERR_NOT_SUPPORTED;
   if (c->sh2_sign != DRV_SH2_SIGN_REFERENCE && c->sh2_sign != DRV_SH2_SIGN_FIXED)
     return why = "sh2_sign must be 0 or 1", DRV_ERR_INVALID_ARG;
@@ -123,8 +124,9 @@ drv_status drv_create(const DrvConfig* cfg, DrvContext** out) {
   if ((e = cudaGetDevice(&c->device)) != cudaSuccess) return bail(e);
   if ((e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device)) != cudaSuccess) return bail(e);
   if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) return bail(e);
-  // LightCacheBuffer: 64 B (SH1) or 128 B (SH2) entries (lightcache.glsl:33-76).
-  c->entry_stride = cfg->sh_order == 2 ? 128u : 64u;
+  // LightCacheBuffer: 64 B (SH1) or 128 B (SH2) entries (lightcache.glsl:33-76);
+  // DrvCacheEntryBF16 (64 B) in BF16 precision.
+  c->entry_stride = cfg->precision == DRV_PRECISION_BF16 ? 64u : (cfg->sh_order == 2 ? 128u : 64u);
   if ((e = cudaMalloc(&c->entries, (size_t)cfg->max_caches * c->entry_stride)) != cudaSuccess) return bail(e);
   c->atlas_words = (size_t)cfg->n_cascades * cfg->cav_res * cfg->cav_res * cfg->cav_res;
   if ((e = cudaMalloc(&c->atlas, c->atlas_words * 4)) != cudaSuccess) return bail(e);
@@ -216,7 +218,9 @@ drv_status drv_get_buffers(DrvContext* ctx, DrvBuffers* o) {
   o->counter = ctx->counter;
   o->voxel_bits = ctx->voxel_bits;
   o->voxel_corners = ctx->vox_corners;
-  for (int l = 1; l < ctx->n_voxel_levels && l < 16; ++l) o->voxel_mips[l] = ctx->mips + ctx->mip_offset[l];
+  const size_t texel = ctx->cfg.precision == DRV_PRECISION_BF16 ? 2 : 4;
+  for (int l = 1; l < ctx->n_voxel_levels && l < 16; ++l)
+    o->voxel_mips[l] = static_cast<char*>(ctx->mips) + ctx->mip_offset[l] * texel;
   o->n_voxel_levels = ctx->n_voxel_levels;
   for (int l = 0; l < DRV_MAX_LIGHTS; ++l) {
     o->vpls[l] = ctx->vpls[l];
@@ -315,7 +319,7 @@ drv_status drv_extract_vpls(DrvContext* ctx, int32_t li, const DrvSpotLight* L) 
   if (shadow_level >= ch.n_levels) return fail(ctx, DRV_ERR_INVALID_ARG, "RSM chain too short for the shadow lod");
   if (L->indirect_shadow_sample_interval < 1) return DRV_ERR_INVALID_ARG;
   DRV_TRY_CUDA(ctx, drv::launch_extract_vpls(ctx->s(), *L, R, ch.flux[read_lod], ch.normal[read_lod], ch.dls[read_lod],
-                                             ch.dls[shadow_level], ctx->vpls[li], ctx->cones[li]));
+                                             ch.dls[shadow_level], ctx->vpls[li], ctx->cones[li], ctx->cfg.precision));
   ctx->n_vpls[li] = R * R;
   ctx->interval[li] = L->indirect_shadow_sample_interval;
   ctx->n_cones[li] = (R * R + L->indirect_shadow_sample_interval - 1) / L->indirect_shadow_sample_interval;
@@ -335,7 +339,7 @@ drv_status drv_voxelize(DrvContext* ctx, const DrvScene* scene, const DrvVolumeI
 drv_status drv_build_opacity_mips(DrvContext* ctx) {
   if (!ctx) return DRV_ERR_INVALID_ARG;
   DRV_TRY_CUDA(ctx, drv::launch_build_mips(ctx->s(), ctx->cfg.voxel_res, ctx->voxel_bits, ctx->mips, ctx->mip_offset,
-                                            ctx->n_voxel_levels));
+                                            ctx->n_voxel_levels, ctx->cfg.precision));
   return cuda_check(ctx, drv::launch_build_corners(ctx->s(), ctx->cfg.voxel_res, ctx->voxel_bits, ctx->vox_corners),
                     "build_corners");
 }

@@ -7,6 +7,8 @@
 // contract of the allocation and voxelization stages.
 #pragma once
 
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -156,6 +158,16 @@ __device__ __forceinline__ int sh_offset(int k, int ch) {
     case 7: return 24 + ch;
     default: return 28 + ch;
   }
+}
+
+// BF16 <-> FP32 (round to nearest even) as raw 16-bit storage.
+__device__ __forceinline__ uint16_t to_bf16(float x) { return __bfloat16_as_ushort(__float2bfloat16_rn(x)); }
+__device__ __forceinline__ float from_bf16(uint16_t b) { return __uint_as_float((uint32_t)b << 16); }
+
+// Cell key of a BF16 cache entry: cascade-local corner coordinates (0..256,
+// 9 bits each) + cascade.
+__device__ __forceinline__ uint32_t pack_cell(int x, int y, int z, int c) {
+  return (uint32_t)x | (uint32_t)y << 9 | (uint32_t)z << 18 | (uint32_t)c << 27;
 }
 
 // Atomic OR of device error bits.

@@ -24,7 +24,7 @@ struct RsmChain {
 
 // Per-light arguments of the light stage.
 struct LightArgs {
-  const DrvVPL* vpls;
+  const void* vpls;  // DrvVPL (FP32 precision) or DrvVPLBF16
   const DrvShadowCone* cones;
   int n_vpls;
   int interval;  // IndirectShadowComputationSampleInterval
@@ -64,12 +64,12 @@ struct Context {
   uint32_t* voxel_bits = nullptr;
   size_t voxel_words = 0;
   uint8_t* vox_corners = nullptr;  // level 0, corner-packed bytes in 4^3 bricks
-  float* mips = nullptr;  // levels 1..L concatenated (FP32)
+  void* mips = nullptr;  // levels 1..L concatenated: float (FP32 precision) or half (BF16 precision)
   size_t mip_offset[kMaxVoxelLevels] = {};
   int n_voxel_levels = 0;
   // RSM + VPLs per light.
   RsmChain rsm[DRV_MAX_LIGHTS];
-  DrvVPL* vpls[DRV_MAX_LIGHTS] = {};
+  void* vpls[DRV_MAX_LIGHTS] = {};  // DrvVPL or DrvVPLBF16 per cfg.precision
   DrvShadowCone* cones[DRV_MAX_LIGHTS] = {};
   int n_vpls[DRV_MAX_LIGHTS] = {};
   int n_cones[DRV_MAX_LIGHTS] = {};
@@ -96,18 +96,18 @@ cudaError_t launch_raycast_rsm(cudaStream_t s, const DrvBox* boxes, int n_boxes,
 cudaError_t launch_downsample_rsm(cudaStream_t s, int res, const float* flux, const int16_t* nrm, const float* dls,
                                   float* fo, int16_t* no, float* dlo);
 cudaError_t launch_extract_vpls(cudaStream_t s, const DrvSpotLight& L, int res, const float* flux, const int16_t* nrm,
-                                const float* dls, const float* dls_shadow, DrvVPL* vpls, DrvShadowCone* cones);
+                                const float* dls, const float* dls_shadow, void* vpls, DrvShadowCone* cones, int precision);
 cudaError_t launch_voxelize(cudaStream_t s, const DrvBox* boxes, int n_boxes, const DrvVolumeInfo& vol, int n,
                             uint32_t* bits);
-cudaError_t launch_build_mips(cudaStream_t s, int n, const uint32_t* bits, float* mips, const size_t* offsets,
-                              int n_levels);
+cudaError_t launch_build_mips(cudaStream_t s, int n, const uint32_t* bits, void* mips, const size_t* offsets,
+                              int n_levels, int precision);
 cudaError_t launch_build_corners(cudaStream_t s, int n, const uint32_t* bits, uint8_t* corners);
 cudaError_t launch_allocate(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const DrvPerFrame& f,
                             const float* depth, int w, int h, uint32_t* atlas, void* entries, uint32_t entry_stride,
                             DrvCacheCounter* counter, uint32_t* ticket, uint32_t* err);
 cudaError_t launch_light_caches(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const LightLaunch& ll,
                                 const DrvCacheCounter* counter, void* entries, uint32_t entry_stride,
-                                const uint8_t* corners, const float* mips, const size_t* mip_offsets, float* scratch,
+                                const uint8_t* corners, const void* mips, const size_t* mip_offsets, float* scratch,
                                 uint32_t* tickets, int num_sms);
 cudaError_t launch_apply(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const DrvPerFrame& f,
                          const DrvGBufferView& g, const uint32_t* atlas, const void* entries, uint32_t entry_stride,

@@ -22,6 +22,7 @@ struct AllocParams {
   uint32_t* atlas;
   float4* entries;
   int entry_vec4;  // entry stride in float4 units
+  int bf16;        // DrvCacheEntryBF16 entries (cell key + BF16 SH) instead of LightCacheEntry
   DrvCacheCounter* counter;
   uint32_t* ticket;
   uint32_t* err;
@@ -50,9 +51,13 @@ __device__ void allocate_cell(const AllocParams& p, int coord, int cascade) {
       continue;
     }
     float4* e = p.entries + (size_t)idx * p.entry_vec4;
-    e[0] = make_float4(__fadd_rn(__fmul_rn((float)lx, k.world_voxel_size), k.min[0]),
-                       __fadd_rn(__fmul_rn((float)ly, k.world_voxel_size), k.min[1]),
-                       __fadd_rn(__fmul_rn((float)lz, k.world_voxel_size), k.min[2]), 0.0f);
+    if (p.bf16) {
+      e[0] = make_float4(__uint_as_float(pack_cell(lx, ly, lz, cascade)), 0.f, 0.f, 0.f);
+    } else {
+      e[0] = make_float4(__fadd_rn(__fmul_rn((float)lx, k.world_voxel_size), k.min[0]),
+                         __fadd_rn(__fmul_rn((float)ly, k.world_voxel_size), k.min[1]),
+                         __fadd_rn(__fmul_rn((float)lz, k.world_voxel_size), k.min[2]), 0.0f);
+    }
     for (int v = 1; v < p.entry_vec4; ++v) e[v] = make_float4(0.f, 0.f, 0.f, 0.f);
     *slot = idx + 1u;  // +1: zero means "cleared" (cacheGather.comp:88)
   }
@@ -135,6 +140,7 @@ cudaError_t launch_allocate(cudaStream_t s, const DrvConfig& cfg, const DrvVolum
   p.atlas = atlas;
   p.entries = (float4*)entries;
   p.entry_vec4 = (int)(entry_stride / 16);
+  p.bf16 = cfg.precision == DRV_PRECISION_BF16;
   p.counter = counter;
   p.ticket = ticket;
   p.err = err;

@@ -24,6 +24,7 @@ struct ApplyParams {
   const float* albedo;
   int w, h;
   int res, n_cascades, transitions, sh2;
+  int bf16;  // DrvCacheEntryBF16 entries
   const uint32_t* atlas;
   const float* entries;
   int stride_floats;
@@ -60,18 +61,37 @@ __device__ __forceinline__ f3 lighting(const ApplyParams& p, const float wp[3], 
     if (x < 0 || y < 0 || z < 0 || x >= aw || y >= p.res || z >= p.res) continue;
     const uint32_t addr = __ldg(p.atlas + ((size_t)z * p.res + y) * aw + x);
     if (addr == 0u || addr > n_caches) continue;  // also rejects 0xFFFFFFFF
+    float er, eg, eb;
+    if (p.bf16) {
+      // 27 BF16 values from byte 4 of the 64-byte entry, coefficient-major.
+      const uint4* e = reinterpret_cast<const uint4*>(p.entries + (size_t)(addr - 1u) * p.stride_floats);
+      const uint4 a = __ldg(e), b = __ldg(e + 1), c = __ldg(e + 2), d = __ldg(e + 3);
+      const uint32_t w[16] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x, c.y, c.z, c.w, d.x, d.y, d.z, d.w};
+      float sh[27];
+#pragma unroll
+      for (int j = 0; j < 27; ++j) sh[j] = from_bf16((uint16_t)(w[1 + (j >> 1)] >> (16 * (j & 1))));
+      er = sh[0] * f0 - sh[3] * f1y + sh[6] * f1z - sh[9] * f1x;
+      eg = sh[1] * f0 - sh[4] * f1y + sh[7] * f1z - sh[10] * f1x;
+      eb = sh[2] * f0 - sh[5] * f1y + sh[8] * f1z - sh[11] * f1x;
+      if (p.sh2) {
+        er += -sh[12] * f4 + sh[15] * f5 + sh[18] * f6 + sh[21] * f7 + sh[24] * f8;
+        eg += -sh[13] * f4 + sh[16] * f5 + sh[19] * f6 + sh[22] * f7 + sh[25] * f8;
+        eb += -sh[14] * f4 + sh[17] * f5 + sh[20] * f6 + sh[23] * f7 + sh[26] * f8;
+      }
+    } else {
     const float4* e = reinterpret_cast<const float4*>(p.entries + (size_t)(addr - 1u) * p.stride_floats);
     const float4 q1 = __ldg(e + 1), q2 = __ldg(e + 2), q3 = __ldg(e + 3);
     // q1 = {SH1neg1, SH00_r}, q2 = {SH10, SH00_g}, q3 = {SH1pos1, SH00_b}
-    float er = q1.w * f0 - q1.x * f1y + q2.x * f1z - q3.x * f1x;
-    float eg = q2.w * f0 - q1.y * f1y + q2.y * f1z - q3.y * f1x;
-    float eb = q3.w * f0 - q1.z * f1y + q2.z * f1z - q3.z * f1x;
+    er = q1.w * f0 - q1.x * f1y + q2.x * f1z - q3.x * f1x;
+    eg = q2.w * f0 - q1.y * f1y + q2.y * f1z - q3.y * f1x;
+    eb = q3.w * f0 - q1.z * f1y + q2.z * f1z - q3.z * f1x;
     if (p.sh2) {
       const float4 q4 = __ldg(e + 4), q5 = __ldg(e + 5), q6 = __ldg(e + 6), q7 = __ldg(e + 7);
       // q4 = {SH2neg2, SH20_r}, q5 = {SH2neg1, SH20_g}, q6 = {SH2pos1, SH20_b}, q7 = {SH2pos2, pad}
       er += -q4.x * f4 + q5.x * f5 + q4.w * f6 + q6.x * f7 + q7.x * f8;
       eg += -q4.y * f4 + q5.y * f5 + q5.w * f6 + q6.y * f7 + q7.y * f8;
       eb += -q4.z * f4 + q5.z * f5 + q6.w * f6 + q6.z * f7 + q7.z * f8;
+    }
     }
     irr.x += fmaxf(er, 0.0f) * w;
     irr.y += fmaxf(eg, 0.0f) * w;
@@ -138,6 +158,7 @@ cudaError_t launch_apply(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeIn
   p.n_cascades = cfg.n_cascades;
   p.transitions = cfg.cascade_transition > 0.0f;
   p.sh2 = cfg.sh_order == 2;
+  p.bf16 = cfg.precision == DRV_PRECISION_BF16;
   p.atlas = atlas;
   p.entries = (const float*)entries;
   p.stride_floats = (int)(entry_stride / 4);

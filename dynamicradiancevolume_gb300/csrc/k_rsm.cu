@@ -58,9 +58,10 @@ __device__ __forceinline__ f3 unproject_dir(const DrvSpotLight& L, float u, floa
   return normalize3(mkf3(c0 / c3, c1 / c3, c2 / c3) - ldf3(L.position));
 }
 
+template <bool BF16>
 __global__ void __launch_bounds__(256) extract_kernel(DrvSpotLight L, int R, const float* __restrict__ flux,
                                                       const int16_t* __restrict__ nrm, const float* __restrict__ dls,
-                                                      const float* __restrict__ dls_shadow, DrvVPL* __restrict__ vpls,
+                                                      const float* __restrict__ dls_shadow, void* __restrict__ vpls_out,
                                                       DrvShadowCone* __restrict__ cones) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   int n = R * R;
@@ -72,22 +73,37 @@ __global__ void __launch_bounds__(256) extract_kernel(DrvSpotLight L, int R, con
     size_t t = (size_t)y * R + x;
     float u = (x + 0.5f) / R, v = (y + 0.5f) / R;
     float d = dls[2 * t];
-    DrvVPL o;
-    o.flux[0] = flux[3 * t];
-    o.flux[1] = flux[3 * t + 1];
-    o.flux[2] = flux[3 * t + 2];
-    o.disc_area = d * d * L.val_area_factor;
-    f3 p = lp + unproject_dir(L, u, v) * d;
-    o.position[0] = p.x;
-    o.position[1] = p.y;
-    o.position[2] = p.z;
-    o._pad0 = 0.0f;
-    f3 nn = unpack_normal16i(nrm[2 * t], nrm[2 * t + 1]);
-    o.normal[0] = nn.x;
-    o.normal[1] = nn.y;
-    o.normal[2] = nn.z;
-    o._pad1 = 0.0f;
-    vpls[i] = o;
+    const f3 p = lp + unproject_dir(L, u, v) * d;
+    const f3 nn = unpack_normal16i(nrm[2 * t], nrm[2 * t + 1]);
+    const float area = d * d * L.val_area_factor;
+    if (BF16) {
+      DrvVPLBF16 o;
+      o.position[0] = p.x;
+      o.position[1] = p.y;
+      o.position[2] = p.z;
+      o.disc_area = area;
+      for (int c = 0; c < 3; ++c) o.flux_bf16[c] = to_bf16(flux[3 * t + c]);
+      o.normal_bf16[0] = to_bf16(nn.x);
+      o.normal_bf16[1] = to_bf16(nn.y);
+      o.normal_bf16[2] = to_bf16(nn.z);
+      o._pad = 0u;
+      reinterpret_cast<DrvVPLBF16*>(vpls_out)[i] = o;
+    } else {
+      DrvVPL o;
+      o.flux[0] = flux[3 * t];
+      o.flux[1] = flux[3 * t + 1];
+      o.flux[2] = flux[3 * t + 2];
+      o.disc_area = area;
+      o.position[0] = p.x;
+      o.position[1] = p.y;
+      o.position[2] = p.z;
+      o._pad0 = 0.0f;
+      o.normal[0] = nn.x;
+      o.normal[1] = nn.y;
+      o.normal[2] = nn.z;
+      o._pad1 = 0.0f;
+      reinterpret_cast<DrvVPL*>(vpls_out)[i] = o;
+    }
   }
   const int interval = L.indirect_shadow_sample_interval;
   if (i * interval < n) {
@@ -130,9 +146,13 @@ cudaError_t launch_downsample_rsm(cudaStream_t s, int res, const float* flux, co
 }
 
 cudaError_t launch_extract_vpls(cudaStream_t s, const DrvSpotLight& L, int res, const float* flux, const int16_t* nrm,
-                                const float* dls, const float* dls_shadow, DrvVPL* vpls, DrvShadowCone* cones) {
+                                const float* dls, const float* dls_shadow, void* vpls, DrvShadowCone* cones,
+                                int precision) {
   int n = res * res;
-  extract_kernel<<<(n + 255) / 256, 256, 0, s>>>(L, res, flux, nrm, dls, dls_shadow, vpls, cones);
+  if (precision == DRV_PRECISION_BF16)
+    extract_kernel<true><<<(n + 255) / 256, 256, 0, s>>>(L, res, flux, nrm, dls, dls_shadow, vpls, cones);
+  else
+    extract_kernel<false><<<(n + 255) / 256, 256, 0, s>>>(L, res, flux, nrm, dls, dls_shadow, vpls, cones);
   return cudaGetLastError();
 }
 

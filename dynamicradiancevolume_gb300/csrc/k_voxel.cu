@@ -94,8 +94,18 @@ struct MipOffsets {
 
 // Fused mips over one B^3 level-0 block (B = min(32, N)): levels 1..log2(B)
 // computed in shared memory from one read of the block's bits.
+template <typename T>
+__device__ __forceinline__ void store_mip(T* p, float v);
+template <>
+__device__ __forceinline__ void store_mip<float>(float* p, float v) { *p = v; }
+template <>
+__device__ __forceinline__ void store_mip<__half>(__half* p, float v) { *p = __float2half_rn(v); }
+__device__ __forceinline__ float load_mip(const float* p) { return *p; }
+__device__ __forceinline__ float load_mip(const __half* p) { return __half2float(*p); }
+
+template <typename T>
 __global__ void __launch_bounds__(256) mips_kernel(int N, int B, const uint32_t* __restrict__ bits,
-                                                   float* __restrict__ mips, MipOffsets mo) {
+                                                   T* __restrict__ mips, MipOffsets mo) {
   __shared__ uint32_t sbits[32 * 32];  // B rows x B slices of (B <= 32)-voxel runs
   __shared__ float lv[2][16 * 16 * 16];
   const int nbx = N / B;
@@ -124,7 +134,7 @@ __global__ void __launch_bounds__(256) mips_kernel(int N, int B, const uint32_t*
     lv[0][i] = v;
     int gn = N / 2;
     size_t g = ((size_t)(bz * n + z) * gn + (by * n + y)) * gn + (bx * n + x);
-    mips[mo.off[1] + g] = v;
+    store_mip(mips + mo.off[1] + g, v);
   }
   __syncthreads();
   // Levels 2 .. log2(B).
@@ -145,7 +155,7 @@ __global__ void __launch_bounds__(256) mips_kernel(int N, int B, const uint32_t*
       lv[cur ^ 1][i] = v;
       int gn = N >> level;
       size_t g = ((size_t)(bz * m + z) * gn + (by * m + y)) * gn + (bx * m + x);
-      mips[mo.off[level] + g] = v;
+      store_mip(mips + mo.off[level] + g, v);
     }
     __syncthreads();
     cur ^= 1;
@@ -153,19 +163,22 @@ __global__ void __launch_bounds__(256) mips_kernel(int N, int B, const uint32_t*
 }
 
 // Remaining levels above log2(B), from the level written by mips_kernel.
-__global__ void __launch_bounds__(256) mips_tail_kernel(int N, int first_level, int last_level, float* __restrict__ mips,
+// Levels are computed from the FP32 level below when stored as FP32, and from
+// the stored FP16 values otherwise (the chain a FP16 texture would hold).
+template <typename T>
+__global__ void __launch_bounds__(256) mips_tail_kernel(int N, int first_level, int last_level, T* __restrict__ mips,
                                                         MipOffsets mo) {
   for (int level = first_level; level <= last_level; ++level) {
     int m = N >> level, p = m * 2;
-    const float* src = mips + mo.off[level - 1];
-    float* dst = mips + mo.off[level];
+    const T* src = mips + mo.off[level - 1];
+    T* dst = mips + mo.off[level];
     for (int i = threadIdx.x; i < m * m * m; i += blockDim.x) {
       int x = i % m, y = (i / m) % m, z = i / (m * m);
       float s = 0.0f;
       for (int dz = 0; dz < 2; ++dz)
         for (int dy = 0; dy < 2; ++dy)
-          for (int dx = 0; dx < 2; ++dx) s += src[((size_t)(2 * z + dz) * p + (2 * y + dy)) * p + (2 * x + dx)];
-      dst[i] = s * 0.125f;
+          for (int dx = 0; dx < 2; ++dx) s += load_mip(src + ((size_t)(2 * z + dz) * p + (2 * y + dy)) * p + (2 * x + dx));
+      store_mip(dst + i, s * 0.125f);
     }
     __syncthreads();
   }
@@ -237,20 +250,27 @@ cudaError_t launch_voxelize(cudaStream_t s, const DrvBox* boxes, int n_boxes, co
   return cudaGetLastError();
 }
 
-cudaError_t launch_build_mips(cudaStream_t s, int n, const uint32_t* bits, float* mips, const size_t* offsets,
-                              int n_levels) {
+cudaError_t launch_build_mips(cudaStream_t s, int n, const uint32_t* bits, void* mips, const size_t* offsets,
+                              int n_levels, int precision) {
   MipOffsets mo{};
   for (int i = 0; i < n_levels && i < kMaxVoxelLevels; ++i) mo.off[i] = offsets[i];
   int B = n < 32 ? n : 32;
   int lb = 0;
   while ((1 << (lb + 1)) <= B) ++lb;
   int blocks = (n / B) * (n / B) * (n / B);
-  mips_kernel<<<blocks, 256, 0, s>>>(n, B, bits, mips, mo);
+  const bool half = precision == DRV_PRECISION_BF16;
+  if (half)
+    mips_kernel<__half><<<blocks, 256, 0, s>>>(n, B, bits, (__half*)mips, mo);
+  else
+    mips_kernel<float><<<blocks, 256, 0, s>>>(n, B, bits, (float*)mips, mo);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   int L = n_levels - 1;
   if (L > lb) {
-    mips_tail_kernel<<<1, 256, 0, s>>>(n, lb + 1, L, mips, mo);
+    if (half)
+      mips_tail_kernel<__half><<<1, 256, 0, s>>>(n, lb + 1, L, (__half*)mips, mo);
+    else
+      mips_tail_kernel<float><<<1, 256, 0, s>>>(n, lb + 1, L, (float*)mips, mo);
     e = cudaGetLastError();
   }
   return e;

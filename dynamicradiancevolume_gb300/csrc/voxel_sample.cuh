@@ -11,6 +11,7 @@
 // sample is one byte load. Levels >= 1 are FP32 arrays (x fastest).
 #pragma once
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -18,12 +19,18 @@ namespace drv {
 
 struct VoxelView {
   const uint8_t* corners;  // level 0, N^3 bytes, bricked
-  const float* mips;       // levels 1..L concatenated
+  const void* mips;        // levels 1..L concatenated: float, or __half when half_mips
   uint32_t off[16];        // offset (floats) of level l in `mips`
   int N;                   // level-0 resolution (power of two)
   int log2n;
   int max_level;           // L = log2(N)
+  int half_mips;
 };
+
+__device__ __forceinline__ float mip_texel(const VoxelView& v, uint32_t i) {
+  return v.half_mips ? __half2float(__ldg(static_cast<const __half*>(v.mips) + i))
+                     : __ldg(static_cast<const float*>(v.mips) + i);
+}
 
 // Byte offset of voxel (x, y, z) in the bricked level-0 corner grid.
 __device__ __forceinline__ uint32_t corner_index(int x, int y, int z, int log2n) {
@@ -69,11 +76,11 @@ __device__ __forceinline__ float level_n(const VoxelView& v, int level, float sx
   const int xa = min(max(x0, 0), n - 1), xb = min(max(x0 + 1, 0), n - 1);
   const int ya = min(max(y0, 0), n - 1) << ln, yb = min(max(y0 + 1, 0), n - 1) << ln;
   const int za = min(max(z0, 0), n - 1) << (2 * ln), zb = min(max(z0 + 1, 0), n - 1) << (2 * ln);
-  const float* m = v.mips + v.off[level];
-  float t0 = __ldg(m + (za | ya | xa)), t1 = __ldg(m + (za | ya | xb));
-  float t2 = __ldg(m + (za | yb | xa)), t3 = __ldg(m + (za | yb | xb));
-  float t4 = __ldg(m + (zb | ya | xa)), t5 = __ldg(m + (zb | ya | xb));
-  float t6 = __ldg(m + (zb | yb | xa)), t7 = __ldg(m + (zb | yb | xb));
+  const uint32_t m = v.off[level];
+  float t0 = mip_texel(v, m + (za | ya | xa)), t1 = mip_texel(v, m + (za | ya | xb));
+  float t2 = mip_texel(v, m + (za | yb | xa)), t3 = mip_texel(v, m + (za | yb | xb));
+  float t4 = mip_texel(v, m + (zb | ya | xa)), t5 = mip_texel(v, m + (zb | ya | xb));
+  float t6 = mip_texel(v, m + (zb | yb | xa)), t7 = mip_texel(v, m + (zb | yb | xb));
   float c00 = t0 + (t1 - t0) * ax, c10 = t2 + (t3 - t2) * ax;
   float c01 = t4 + (t5 - t4) * ax, c11 = t6 + (t7 - t6) * ax;
   float c0 = c00 + (c10 - c00) * ay, c1 = c01 + (c11 - c01) * ay;

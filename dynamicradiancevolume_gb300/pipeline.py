@@ -38,6 +38,8 @@ class Workload:
     seed: int = 1
     box_size: tuple = (0.05, 0.3)
     albedo: tuple = (0.2, 0.9)
+    precision: int = abi.PRECISION_FP32
+    visibility: int = abi.VISIBILITY_CONE
 
     @property
     def n_vpls(self) -> int:
@@ -56,6 +58,10 @@ WORKLOADS = {
     "c2_production": Workload("c2_production", 1920, 1080, 64, 256, 3, 512, 3, 0, 4, 0.25, 32, 2, 32, 262144),
     # The headline case: C2 with one light (4096 VPLs) at 1080p.
     "ns_1080p_4096": Workload("ns_1080p_4096", 1920, 1080, 64, 256, 1, 512, 3, 0, 4, 0.25, 32, 2, 32, 262144),
+    # Precision variant of the small configuration: BF16 VPL flux/normal and
+    # cache SH, FP16 opacity mips, FP32 Kahan-compensated accumulation.
+    "c3_precision": Workload("c3_precision", 256, 256, 12, 64, 1, 32, 0, 0, 1, 2.0, 32, 1, 16, 65536,
+                             cascade_transition=0.0, precision=abi.PRECISION_BF16),
 }
 
 
@@ -76,6 +82,8 @@ def make_config(w: Workload) -> abi.DrvConfig:
     cfg.max_caches = w.max_caches
     cfg.max_lights = w.n_lights
     cfg.max_rsm_resolution = w.rsm_resolution
+    cfg.precision = w.precision
+    cfg.visibility = w.visibility
     return cfg
 
 
@@ -239,6 +247,30 @@ class Pipeline:
         floats = b.entry_stride // 4
         return self._dev_tensor(b.cache_entries, count * floats, self.torch.float32).view(count, floats)
 
+    def read_entries_decoded(self, count: int):
+        """(positions [n,3] float32, sh [n,27] float64 in (coefficient, rgb) order)
+        for either entry layout."""
+        import numpy as np
+        raw = self.read_entries(count).cpu().numpy()
+        if self.hf.config.precision == abi.PRECISION_BF16:
+            key = raw[:, 0].view(np.uint32)
+            cell = np.stack([key & 511, (key >> 9) & 511, (key >> 18) & 511], 1).astype(np.float32)
+            casc = (key >> 27).astype(np.int64)
+            vol = self.hf.volume
+            size = np.array([vol.cascades[c].world_voxel_size for c in range(4)], np.float32)[casc]
+            mins = np.array([list(vol.cascades[c].min) for c in range(4)], np.float32)[casc]
+            pos = (cell * size[:, None]).astype(np.float32) + mins
+            bf = raw.view(np.uint16)[:, 2:29].astype(np.uint32) << 16
+            sh = bf.view(np.float32).astype(np.float64)
+            return pos.astype(np.float32), sh
+        off = {0: [7, 11, 15], 1: [4, 5, 6], 2: [8, 9, 10], 3: [12, 13, 14], 4: [16, 17, 18], 5: [20, 21, 22],
+               6: [19, 23, 27], 7: [24, 25, 26], 8: [28, 29, 30]}
+        nk = 9 if self.hf.config.sh_order == 2 else 4
+        sh = np.zeros((raw.shape[0], 27))
+        for k in range(nk):
+            sh[:, 3 * k:3 * k + 3] = raw[:, off[k]]
+        return raw[:, 0:3].copy(), sh
+
     def read_atlas(self):
         w = self.hf.workload
         b = self.buffers()
@@ -252,10 +284,26 @@ class Pipeline:
     def read_mip(self, level: int):
         N = self.hf.workload.voxel_res
         n = N >> level
+        if self.hf.config.precision == abi.PRECISION_BF16:
+            import numpy as np
+            words = (n ** 3 + 1) // 2
+            raw = self._dev_tensor(self.buffers().voxel_mips[level], words, self.torch.float32).cpu().numpy()
+            half = raw.view(np.float16)[:n ** 3]
+            return self.torch.from_numpy(half.astype(np.float32)).view(n, n, n)
         return self._dev_tensor(self.buffers().voxel_mips[level], n ** 3, self.torch.float32).view(n, n, n)
 
     def read_vpls(self, light: int):
+        """VPLs as [n, 12] float32 in the DrvVPL layout (BF16 storage widened)."""
         b = self.buffers()
+        if self.hf.config.precision == abi.PRECISION_BF16:
+            import numpy as np
+            raw = self._dev_tensor(b.vpls[light], b.n_vpls[light] * 8, self.torch.float32).cpu().numpy()
+            raw = raw.reshape(-1, 8)
+            h = raw.view(np.uint16).reshape(-1, 16)[:, 8:14].astype(np.uint32) << 16
+            wide = h.view(np.float32)
+            out = np.zeros((raw.shape[0], 12), np.float32)
+            out[:, 0:3], out[:, 3], out[:, 4:7], out[:, 8:11] = wide[:, 0:3], raw[:, 3], raw[:, 0:3], wide[:, 3:6]
+            return self.torch.from_numpy(out)
         return self._dev_tensor(b.vpls[light], b.n_vpls[light] * 12, self.torch.float32).view(-1, 12)
 
     def read_cones(self, light: int, n: int):

@@ -236,6 +236,28 @@ typedef struct DrvVPL {
   float _pad1;
 } DrvVPL;
 
+/* DRV_PRECISION_BF16 storage of a VPL (32 B): position and disc area stay
+ * FP32 (directions are computed from them), flux and normal are BF16. */
+typedef struct DrvVPLBF16 {
+  float position[3];
+  float disc_area;
+  uint16_t flux_bf16[3];
+  uint16_t normal_bf16[3];
+  uint32_t _pad;
+} DrvVPLBF16;
+
+/* DRV_PRECISION_BF16 cache entry (64 B): the cell it sits on instead of an
+ * FP32 position (x | y << 9 | z << 18 | cascade << 27, cascade-local corner
+ * coordinates; the position is cell * WorldVoxelSize + Min as in
+ * cacheGather.comp:65), then the 27 SH values in BF16, ordered coefficient-
+ * major (SH00, SH1neg1, SH10, SH1pos1, SH2neg2, SH2neg1, SH20, SH2pos1,
+ * SH2pos2), RGB within each; SH1 leaves the last 15 zero. */
+typedef struct DrvCacheEntryBF16 {
+  uint32_t cell;
+  uint16_t sh_bf16[27];
+  uint16_t _pad[3];
+} DrvCacheEntryBF16;
+
 /* Per-block indirect-shadow cone source (cacheLightingRSM.comp:171-192):
  * average VAL position and distToSphereRad. */
 typedef struct DrvShadowCone {
@@ -252,16 +274,16 @@ typedef struct DrvCacheCounter {
 /* Read-only views of the context's device buffers (for callers that render
  * debug views or compare results). */
 typedef struct DrvBuffers {
-  void* cache_entries;              /* LightCacheEntry std430: 64 B (SH1) or 128 B (SH2) stride; BF16 precision: see entry_stride */
+  void* cache_entries;              /* FP32: LightCacheEntry std430, 64 B (SH1) / 128 B (SH2); BF16: DrvCacheEntryBF16 */
   uint32_t entry_stride;
   uint32_t* cav_atlas;              /* R32UI [n_cascades*res][res][res], x fastest */
   DrvCacheCounter* counter;
   uint32_t* voxel_bits;             /* level 0 as a bitmask, bit (x&31) of word ((z*N+y)*N+x)/32 */
   uint8_t* voxel_corners;           /* level 0 corner-packed: byte (x,y,z) = voxels (x+dx,y+dy,z+dz), +1 clamped,
                                        bit dx|dy<<1|dz<<2, stored in 4x4x4 bricks of 64 bytes */
-  void* voxel_mips[16];             /* levels 1..L (index 1..L), float (FP32) or half (BF16 precision) */
+  void* voxel_mips[16];             /* levels 1..L (index 1..L), float (FP32 precision) or half (BF16 precision) */
   int32_t n_voxel_levels;           /* levels including 0 */
-  DrvVPL* vpls[DRV_MAX_LIGHTS];     /* FP32 VPL array per light, Morton order */
+  void* vpls[DRV_MAX_LIGHTS];       /* VPL array per light, Morton order: DrvVPL (FP32) or DrvVPLBF16 */
   DrvShadowCone* cones[DRV_MAX_LIGHTS];
   int32_t n_vpls[DRV_MAX_LIGHTS];
   int32_t n_lights;

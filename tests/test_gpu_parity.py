@@ -52,6 +52,7 @@ class Run:
         self.count = p.cache_count()
         n = min(self.count, w.max_caches)
         self.entries = p.read_entries(n).cpu().numpy()
+        self.positions, self._sh = p.read_entries_decoded(n)
         self.atlas = p.read_atlas().cpu().numpy().view(np.uint32)
         self.vpls = [p.read_vpls(l).cpu().numpy() for l in range(w.n_lights)]
         self.cones = [p.read_cones(l, self.vpls[l].shape[0] // self.hf.lights[l].indirect_shadow_sample_interval)
@@ -81,14 +82,7 @@ class Run:
 
     def gpu_sh(self):
         """27 SH values per entry in the oracle's (k, channel) order."""
-        e = self.entries
-        off = {0: [7, 11, 15], 1: [4, 5, 6], 2: [8, 9, 10], 3: [12, 13, 14], 4: [16, 17, 18], 5: [20, 21, 22],
-               6: [19, 23, 27], 7: [24, 25, 26], 8: [28, 29, 30]}
-        nk = 9 if self.w.sh_order == 2 else 4
-        sh = np.zeros((e.shape[0], 27))
-        for k in range(nk):
-            sh[:, 3 * k:3 * k + 3] = e[:, off[k]]
-        return sh
+        return self._sh
 
 
 @pytest.fixture(scope="module")
@@ -197,14 +191,15 @@ def test_allocation_bit_exact(case, request, oracle):
     assert st == abi.OK
     assert r.count == count
     # same cell set (atomic order normalised by comparing sets of exact positions)
-    assert _key_set(r.entries[:, 0:3]) == _key_set(pos)
+    assert _key_set(r.positions) == _key_set(pos)
     # same atlas occupancy, and every published slot points at an entry at that corner
     assert np.array_equal(r.atlas != 0, atlas != 0)
     g = r.atlas[r.atlas != 0]
     o = atlas[atlas != 0]
-    assert np.array_equal(r.entries[g - 1, 0:3], pos[o - 1])
-    # SH zeroed at allocation then lit: padding words stay zero
-    assert np.all(r.entries[:, 3] == 0)
+    assert np.array_equal(r.positions[g - 1], pos[o - 1])
+    # SH zeroed at allocation then lit: the padding word stays zero
+    if r.hf.config.precision == abi.PRECISION_FP32:
+        assert np.all(r.entries[:, 3] == 0)
 
 
 @pytest.mark.parametrize("case", ["c1", "c2r"])
@@ -212,7 +207,7 @@ def test_light_caches_matches_fp64(case, request, oracle):
     """SH gather + cone-traced shadow on the GPU's own VPLs and voxels, vs FP64."""
     r = request.getfixturevalue(case)
     n = r.entries.shape[0]
-    pos = r.entries[:, 0:3].copy()
+    pos = r.positions.copy()
     mips = oracle.build_mips(r.w.voxel_res, r.bits)
     cones = [c.astype(np.float64) for c in r.cones]
     sh = oracle.light_caches(r.hf.config, r.hf.volume, pos, r.hf.lights, r.gpu_vpls_f64(), cones, r.bits, mips)
@@ -337,7 +332,7 @@ def ns(lib, oracle, cuda):
 def test_ns_allocation_bit_exact_at_full_size(ns, oracle):
     st, atlas, pos, count = oracle.allocate_caches(ns.hf.config, ns.hf.volume, ns.hf.frame, ns.depth)
     assert ns.count == count
-    assert _key_set(ns.entries[:, 0:3]) == _key_set(pos)
+    assert _key_set(ns.positions) == _key_set(pos)
     assert np.array_equal(ns.atlas != 0, atlas != 0)
 
 
@@ -353,7 +348,7 @@ def test_ns_light_sample_matches_fp64(ns, oracle):
     """A seeded sample of 96 caches at full size (256^3 voxels, 32-step cones)."""
     rng = np.random.default_rng(0)
     idx = rng.choice(ns.entries.shape[0], size=min(96, ns.entries.shape[0]), replace=False)
-    pos = ns.entries[idx, 0:3].copy()
+    pos = ns.positions[idx].copy()
     mips = oracle.build_mips(ns.w.voxel_res, ns.bits)
     sh = oracle.light_caches(ns.hf.config, ns.hf.volume, pos, ns.hf.lights, ns.gpu_vpls_f64(),
                              [c.astype(np.float64) for c in ns.cones], ns.bits, mips)
