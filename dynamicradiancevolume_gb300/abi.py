@@ -159,10 +159,20 @@ PROTOTYPES = {
     "drv_frame": (C.c_int, [VP, P(DrvScene), P(DrvGBufferView), P(DrvPerFrame), P(DrvVolumeInfo),
                             P(DrvSpotLight), P(DrvRSMView), C.c_int32, VP]),
     "drv_get_cache_count": (C.c_int, [VP, P(C.c_uint32)]),
+    "drv_set_surrogate_params": (C.c_int, [VP, VP]),
+    "drv_surrogate_make_pairs": (C.c_int, [VP, C.c_uint64, C.c_int32, VP, VP]),
+    "drv_surrogate_train_scratch_floats": (C.c_size_t, [C.c_int32]),
+    "drv_surrogate_train_step": (C.c_int, [VP, VP, C.c_int32, VP, VP, VP, VP, C.c_int32, C.c_float, C.c_float,
+                                           C.c_float, VP, VP]),
+    "drv_surrogate_eval": (C.c_int, [VP, VP, C.c_int32, VP]),
+    "drv_get_surrogate_fallbacks": (C.c_int, [VP, P(C.c_uint32)]),
     "drv_light_caches_static_scratch": (C.c_int, [P(DrvConfig), P(DrvVolumeInfo), P(VP), P(VP), P(C.c_int32),
                                                   P(C.c_int32), C.c_int32, VP, VP, VP, VP, VP]),
 }
 STATIC_SCRATCH_MAX_CACHES = 4096
+SURROGATE_INPUTS = 32
+SURROGATE_PARAMS = 10562
+SURROGATE_ENUMERATE = 0xFFFFFFFFFFFFFFFF
 
 
 def header_functions(header: Path) -> list[str]:

@@ -49,6 +49,8 @@ void release(Context* c) {
   cudaFree(c->vox_corners);
   cudaFree(c->light_scratch);
   cudaFree(c->light_tickets);
+  cudaFree(c->sur_weights);
+  cudaFree(c->sur_fallbacks);
   for (int l = 0; l < DRV_MAX_LIGHTS; ++l) {
     for (int k = 1; k < drv::kMaxRsmLevels; ++k) {
       cudaFree(c->rsm[l].flux[k]);
@@ -77,7 +79,11 @@ drv_status validate_config(const DrvConfig* c, std::string& why) {
     return why = "max_rsm_resolution must be a power of two <= 4096", DRV_ERR_INVALID_ARG;
   if (c->precision != DRV_PRECISION_FP32 && c->precision != DRV_PRECISION_BF16)
     return why = "precision must be DRV_PRECISION_FP32 or DRV_PRECISION_BF16", DRV_ERR_INVALID_ARG;
-  if (c->visibility != DRV_VISIBILITY_CONE) return why = "visibility mode not available", DRV_ERR_NOT_SUPPORTED;
+  if (c->visibility != DRV_VISIBILITY_CONE && c->visibility != DRV_VISIBILITY_SURROGATE)
+    return why = "visibility must be DRV_VISIBILITY_CONE or DRV_VISIBILITY_SURROGATE", DRV_ERR_INVALID_ARG;
+  if (c->visibility == DRV_VISIBILITY_SURROGATE && !c->indirect_shadow)
+    return why = "the visibility surrogate replaces the indirect-shadow cone: indirect_shadow must be on",
+           DRV_ERR_INVALID_ARG;
   if (c->sh2_sign != DRV_SH2_SIGN_REFERENCE && c->sh2_sign != DRV_SH2_SIGN_FIXED)
     return why = "sh2_sign must be 0 or 1", DRV_ERR_INVALID_ARG;
   return DRV_OK;
@@ -165,6 +171,9 @@ drv_status drv_create(const DrvConfig* cfg, DrvContext** out) {
     if ((e = cudaMalloc(&c->vpls[l], (size_t)R * R * sizeof(DrvVPL))) != cudaSuccess) return bail(e);
     if ((e = cudaMalloc(&c->cones[l], (size_t)R * R * sizeof(DrvShadowCone))) != cudaSuccess) return bail(e);
   }
+  if ((e = cudaMalloc(&c->sur_weights, drv::surrogate_weights_bytes())) != cudaSuccess) return bail(e);
+  if ((e = cudaMalloc(&c->sur_fallbacks, 16)) != cudaSuccess) return bail(e);
+  if ((e = cudaMemset(c->sur_fallbacks, 0, 16)) != cudaSuccess) return bail(e);
   c->box_capacity = 512;
   if ((e = cudaMallocHost(&c->h_boxes, c->box_capacity * sizeof(DrvBox))) != cudaSuccess) return bail(e);
   if ((e = cudaMalloc(&c->d_boxes, c->box_capacity * sizeof(DrvBox))) != cudaSuccess) return bail(e);
@@ -349,6 +358,7 @@ drv_status drv_build_opacity_mips(DrvContext* ctx) {
 drv_status drv_allocate_caches(DrvContext* ctx, const DrvGBufferView* g, const DrvPerFrame* f, const DrvVolumeInfo* vol) {
   if (!ctx || !f || !vol) return DRV_ERR_INVALID_ARG;
   if (!views_ok(g, ctx->cfg)) return fail(ctx, DRV_ERR_INVALID_ARG, "G-buffer view does not match the config");
+  ctx->last_volume = *vol;
   DRV_TRY_CUDA(ctx, cudaMemsetAsync(ctx->counter, 0, 32, ctx->s()));
   DRV_TRY_CUDA(ctx, cudaMemsetAsync(ctx->atlas, 0, ctx->atlas_words * 4, ctx->s()));
   return cuda_check(ctx, drv::launch_allocate(ctx->s(), ctx->cfg, *vol, *f, g->depth, g->width, g->height, ctx->atlas,
@@ -370,6 +380,15 @@ drv_status drv_light_caches(DrvContext* ctx, const DrvSpotLight* lights, int32_t
     ll.lights[l].cones = ctx->cones[l];
     ll.lights[l].n_vpls = ctx->n_vpls[l];
     ll.lights[l].interval = ctx->interval[l];
+  }
+  if (ctx->cfg.visibility == DRV_VISIBILITY_SURROGATE) {
+    if (!ctx->sur_ready) return fail(ctx, DRV_ERR_INVALID_ARG, "surrogate visibility needs drv_set_surrogate_params");
+    DRV_TRY_CUDA(ctx, cudaMemsetAsync(ctx->sur_fallbacks, 0, 4, ctx->s()));
+    return cuda_check(ctx, drv::launch_light_surrogate(ctx->s(), ctx->cfg, *vol, ll, ctx->counter, ctx->entries,
+                                                       ctx->entry_stride, ctx->vox_corners, ctx->mips, ctx->mip_offset,
+                                                       ctx->light_scratch, ctx->light_tickets, ctx->sur_weights,
+                                                       ctx->sur_fallbacks, ctx->num_sms),
+                      "light_caches (surrogate)");
   }
   return cuda_check(ctx, drv::launch_light_caches(ctx->s(), ctx->cfg, *vol, ll, ctx->counter, ctx->entries,
                                                   ctx->entry_stride, ctx->vox_corners, ctx->mips, ctx->mip_offset,
@@ -405,6 +424,60 @@ drv_status drv_frame(DrvContext* ctx, const DrvScene* scene, const DrvGBufferVie
   if ((st = drv_allocate_caches(ctx, g, f, vol)) != DRV_OK) return st;
   if ((st = drv_light_caches(ctx, lights, n_lights, vol, f)) != DRV_OK) return st;
   return drv_apply(ctx, g, f, vol, out_rgb);
+}
+
+// ---- learned visibility surrogate ----------------------------------------
+drv_status drv_set_surrogate_params(DrvContext* ctx, const float* params) {
+  if (!ctx || !params) return DRV_ERR_INVALID_ARG;
+  DRV_TRY_CUDA(ctx, drv::launch_pack_surrogate_weights(ctx->s(), params, ctx->sur_weights));
+  ctx->sur_ready = true;
+  return DRV_OK;
+}
+
+drv_status drv_surrogate_eval(DrvContext* ctx, const float* features, int32_t n, float* out) {
+  if (!ctx || !features || !out || n < 0) return DRV_ERR_INVALID_ARG;
+  if (!ctx->sur_ready) return fail(ctx, DRV_ERR_INVALID_ARG, "drv_set_surrogate_params first");
+  if (n == 0) return DRV_OK;
+  return cuda_check(ctx, drv::launch_surrogate_eval(ctx->s(), ctx->sur_weights, features, n, out), "surrogate_eval");
+}
+
+drv_status drv_get_surrogate_fallbacks(DrvContext* ctx, uint32_t* out) {
+  if (!ctx || !out) return DRV_ERR_INVALID_ARG;
+  DRV_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->s()));
+  DRV_TRY_CUDA(ctx, cudaMemcpy(out, ctx->sur_fallbacks, 4, cudaMemcpyDeviceToHost));
+  return DRV_OK;
+}
+
+drv_status drv_surrogate_make_pairs(DrvContext* ctx, uint64_t seed, int32_t n_pairs, float* features,
+                                    float* targets) {
+  if (!ctx || !features || !targets || n_pairs < 0) return DRV_ERR_INVALID_ARG;
+  if (!ctx->cfg.indirect_shadow) return fail(ctx, DRV_ERR_INVALID_ARG, "pairs need the indirect-shadow cone");
+  if (ctx->n_lights < 1) return fail(ctx, DRV_ERR_INVALID_ARG, "drv_extract_vpls must run first");
+  if (n_pairs == 0) return DRV_OK;
+  drv::LightLaunch ll{};
+  ll.n_lights = ctx->n_lights;
+  for (int l = 0; l < ctx->n_lights; ++l) {
+    ll.lights[l].vpls = ctx->vpls[l];
+    ll.lights[l].cones = ctx->cones[l];
+    ll.lights[l].n_vpls = ctx->n_vpls[l];
+    ll.lights[l].interval = ctx->interval[l];
+  }
+  return cuda_check(ctx, drv::launch_surrogate_pairs(ctx->s(), ctx->cfg, ctx->last_volume, ll, ctx->counter,
+                                                     ctx->entries, ctx->entry_stride, ctx->vox_corners, ctx->mips,
+                                                     ctx->mip_offset, seed, n_pairs, features, targets),
+                    "surrogate_make_pairs");
+}
+
+size_t drv_surrogate_train_scratch_floats(int32_t n) { return n > 0 ? drv::surrogate_train_scratch_floats(n) : 0; }
+
+drv_status drv_surrogate_train_step(const float* features, const float* targets, int32_t n, float* params,
+                                    float* adam_m, float* adam_v, float* scratch, int32_t step, float lr,
+                                    float conf_tau, float weight_decay, float* loss_out, void* cuda_stream) {
+  if (!features || !targets || n < 1 || !params || !adam_m || !adam_v || !scratch || step < 1 || !(lr > 0.0f))
+    return DRV_ERR_INVALID_ARG;
+  cudaError_t e = drv::launch_surrogate_train_step((cudaStream_t)cuda_stream, features, targets, n, params, adam_m,
+                                                   adam_v, scratch, step, lr, conf_tau, weight_decay, loss_out);
+  return e == cudaSuccess ? DRV_OK : DRV_ERR_CUDA;
 }
 
 }  // extern "C"

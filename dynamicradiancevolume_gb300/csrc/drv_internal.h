@@ -83,6 +83,11 @@ struct Context {
   // Light-stage partial sums: [max_caches * kMaxLightChunks][27] and a ticket per cache.
   float* light_scratch = nullptr;
   uint32_t* light_tickets = nullptr;
+  // Visibility surrogate: packed BF16 inference weights + re-trace counter.
+  void* sur_weights = nullptr;
+  uint32_t* sur_fallbacks = nullptr;
+  bool sur_ready = false;
+  DrvVolumeInfo last_volume{};  // volume of the last drv_allocate_caches (cache positions refer to it)
 };
 
 int light_chunks(int total_blocks);
@@ -112,5 +117,23 @@ cudaError_t launch_light_caches(cudaStream_t s, const DrvConfig& cfg, const DrvV
 cudaError_t launch_apply(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const DrvPerFrame& f,
                          const DrvGBufferView& g, const uint32_t* atlas, const void* entries, uint32_t entry_stride,
                          const DrvCacheCounter* counter, float* out_rgb);
+
+size_t surrogate_weights_bytes();
+size_t surrogate_train_scratch_floats(int n);
+cudaError_t launch_pack_surrogate_weights(cudaStream_t s, const float* params, void* weights);
+cudaError_t launch_surrogate_eval(cudaStream_t s, const void* weights, const float* X, int n, float* out);
+cudaError_t launch_surrogate_pairs(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol,
+                                   const LightLaunch& ll, const DrvCacheCounter* counter, const void* entries,
+                                   uint32_t entry_stride, const uint8_t* corners, const void* mips,
+                                   const size_t* mip_offsets, uint64_t seed, int n_pairs, float* features,
+                                   float* targets);
+cudaError_t launch_surrogate_train_step(cudaStream_t s, const float* X, const float* Y, int n, float* params,
+                                        float* m, float* v, float* scratch, int step, float lr, float conf_tau,
+                                        float weight_decay, float* loss_out);
+cudaError_t launch_light_surrogate(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol,
+                                   const LightLaunch& ll, const DrvCacheCounter* counter, void* entries,
+                                   uint32_t entry_stride, const uint8_t* corners, const void* mips,
+                                   const size_t* mip_offsets, float* scratch, uint32_t* tickets, const void* weights,
+                                   uint32_t* fallback_count, int num_sms);
 
 }  // namespace drv

@@ -1,0 +1,111 @@
+// surrogate.cuh — the learned visibility surrogate that stands in for the
+// indirect-shadow cone (cacheLightingRSM.comp:167-232): its input features,
+// parameter layout and activation, shared by the pair generator, the trainer
+// and the inference kernel.
+//
+// MLP: 32 inputs -> 64 -> 64 -> 64 -> 2, GELU (tanh form) between layers.
+// Output 0 is the visibility logit (visibility = sigmoid), output 1 the
+// confidence logit: pairs whose sigmoid(confidence) is below the threshold
+// are re-traced with the cone.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "drv_device.cuh"
+#include "voxel_sample.cuh"
+
+namespace drv {
+
+constexpr int kMlpIn = 32;
+constexpr int kMlpHidden = 64;
+constexpr int kMlpOut = 2;
+constexpr int kMlpOutPad = 8;  // layer-4 rows padded to one n8 MMA tile
+constexpr int kFeatures = 22;  // used inputs; the rest are zero
+
+// Parameter offsets (floats) of the flat FP32 master copy; weights are
+// [out][in] row-major (in contiguous), biases follow each weight matrix.
+constexpr int kOffW1 = 0;
+constexpr int kOffB1 = kOffW1 + kMlpHidden * kMlpIn;
+constexpr int kOffW2 = kOffB1 + kMlpHidden;
+constexpr int kOffB2 = kOffW2 + kMlpHidden * kMlpHidden;
+constexpr int kOffW3 = kOffB2 + kMlpHidden;
+constexpr int kOffB3 = kOffW3 + kMlpHidden * kMlpHidden;
+constexpr int kOffW4 = kOffB3 + kMlpHidden;
+constexpr int kOffB4 = kOffW4 + kMlpOut * kMlpHidden;
+constexpr int kMlpParams = kOffB4 + kMlpOut;  // 10562
+
+// GELU, tanh approximation: 0.5 x (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3))).
+__device__ __forceinline__ float gelu(float x) {
+  const float u = 0.7978845608f * (x + 0.044715f * x * x * x);
+  return 0.5f * x * (1.0f + tanhf(u));
+}
+__device__ __forceinline__ float gelu_grad(float x) {
+  const float x2 = x * x;
+  const float u = 0.7978845608f * (x + 0.044715f * x2 * x);
+  const float t = tanhf(u);
+  return 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * 0.7978845608f * (1.0f + 3.0f * 0.044715f * x2);
+}
+__device__ __forceinline__ float sigmoidf(float x) { return 1.0f / (1.0f + __expf(-x)); }
+
+// Distance (in voxels) the cone of cacheLightingRSM.comp:195-228 reaches
+// before it stops: min(goal, the distance after max_steps steps). The step
+// rule is stepSize = max(1, dist * dsr * 2 / (1 - dsr)); it is evaluated here
+// in closed form (unit steps, then geometric growth), which is enough for a
+// feature.
+__device__ __forceinline__ float cone_reach(float goal, float dsr, int max_steps) {
+  const float g = dsr * 2.0f / (1.0f - dsr);  // growth per step once steps exceed one voxel
+  float dist = 0.0f;
+  int s = 0;
+  // unit steps while dist * g < 1
+  const float unit_until = g > 0.0f ? 1.0f / g : 1e30f;
+  const int n_unit = min(max_steps, (int)ceilf(fmaxf(unit_until, 0.0f)) + 1);
+  dist = (float)n_unit;
+  s = n_unit;
+  if (s < max_steps) dist *= __powf(1.0f + g, (float)(max_steps - s));
+  // the march starts 2 voxels out and stops once it passes the goal
+  return fminf(dist, fmaxf(goal, 0.0f)) + 2.0f;
+}
+
+// Input features of one (cache, shadow block) pair. cache/target are world
+// positions, n the first VPL's normal, dsr the cone aperture.
+__device__ __forceinline__ void surrogate_features(const VoxelView& v, float inv_extent, const float vol_min[3],
+                                                   float voxel_size, int max_steps, float cx, float cy, float cz,
+                                                   float tx, float ty, float tz, float nx, float ny, float nz,
+                                                   float dsr, float* f) {
+  const float px = (cx - vol_min[0]) * inv_extent, py = (cy - vol_min[1]) * inv_extent,
+              pz = (cz - vol_min[2]) * inv_extent;
+  const float qx = (tx - vol_min[0]) * inv_extent, qy = (ty - vol_min[1]) * inv_extent,
+              qz = (tz - vol_min[2]) * inv_extent;
+  const float dx = tx - cx, dy = ty - cy, dz = tz - cz;
+  const float len = sqrtf(dx * dx + dy * dy + dz * dz);
+  const float inv_len = 1.0f / fmaxf(len, 1e-20f);
+  const float len_vox = len / voxel_size;
+  const float reach = cone_reach(len_vox - 2.0f, dsr, max_steps);  // voxels from the cache
+  f[0] = px;
+  f[1] = py;
+  f[2] = pz;
+  f[3] = qx;
+  f[4] = qy;
+  f[5] = qz;
+  f[6] = nx;
+  f[7] = ny;
+  f[8] = nz;
+  // 8 opacity samples of mip level 3 along the traced part of the segment.
+  const float reach_norm = fminf(reach * voxel_size * inv_len, 1.0f);
+  const int level = min(3, v.max_level);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const float t = (i + 0.5f) * 0.125f * reach_norm;
+    f[9 + i] = level_n(v, level, px + (qx - px) * t, py + (qy - py) * t, pz + (qz - pz) * t);
+  }
+  f[17] = dsr * 8.0f;
+  f[18] = len_vox * (1.0f / 64.0f);
+  f[19] = dx * inv_len;
+  f[20] = dy * inv_len;
+  f[21] = dz * inv_len;
+#pragma unroll
+  for (int i = kFeatures; i < kMlpIn; ++i) f[i] = 0.0f;
+}
+
+}  // namespace drv

@@ -162,6 +162,15 @@ class Pipeline:
             self.rsm_views[l] = abi.DrvRSMView(R, self.rsm_flux[l].data_ptr(), self.rsm_normal[l].data_ptr(),
                                                self.rsm_dls[l].data_ptr())
 
+    def set_frame(self, hf: HostFrame) -> None:
+        """Switches to another frame of the same workload (scene, camera,
+        lights); the context and buffers are reused."""
+        w0, w1 = self.hf.workload, hf.workload
+        if (w0.width, w0.height, w0.n_lights, w0.rsm_resolution) != (w1.width, w1.height, w1.n_lights,
+                                                                     w1.rsm_resolution):
+            raise ValueError("set_frame needs a frame of the same dimensions")
+        self.hf = hf
+
     def close(self):
         if self.ctx:
             self.lib.drv_destroy(self.ctx)

@@ -382,6 +382,43 @@ drv_status drv_frame(DrvContext* ctx, const DrvScene* scene, const DrvGBufferVie
 /* Optional cache-count readback (renderer.cpp:960-966). Synchronises. */
 drv_status drv_get_cache_count(DrvContext* ctx, uint32_t* out_count);
 
+/* ---- learned visibility surrogate -----------------------------------------
+ * No counterpart in the reference: an MLP (32 inputs -> 64 -> 64 -> 64 -> 2,
+ * GELU; BF16 weights, FP32 accumulation on tensor cores) predicts the
+ * indirect-shadow cone's visibility of a (cache, shadow block) pair plus a
+ * confidence; with DrvConfig.visibility = DRV_VISIBILITY_SURROGATE,
+ * drv_light_caches uses it and re-traces pairs whose confidence is below
+ * DrvConfig.surrogate_conf_threshold with the cone. Parameters are a flat FP32
+ * array of DRV_SURROGATE_PARAMS floats: W1[64][32], b1[64], W2[64][64], b2,
+ * W3[64][64], b3, W4[2][64], b4[2] (weights [out][in]). */
+#define DRV_SURROGATE_INPUTS 32
+#define DRV_SURROGATE_PARAMS 10562
+/* Uploads parameters (device FP32 array) as the context's BF16 inference weights. */
+drv_status drv_set_surrogate_params(DrvContext* ctx, const float* params_device);
+/* Training pairs from the context's current frame (after drv_extract_vpls,
+ * drv_build_opacity_mips and drv_allocate_caches): random (cache, shadow
+ * block) pairs, features[n][32] and the cone-traced visibility targets[n].
+ * seed = DRV_SURROGATE_ENUMERATE lists the pairs in order instead (pair i =
+ * cache i / n_blocks, block i % n_blocks, blocks of all lights in light
+ * order). */
+#define DRV_SURROGATE_ENUMERATE 0xFFFFFFFFFFFFFFFFull
+drv_status drv_surrogate_make_pairs(DrvContext* ctx, uint64_t seed, int32_t n_pairs, float* features,
+                                    float* targets);
+/* Device scratch (floats) one drv_surrogate_train_step over n samples needs. */
+size_t drv_surrogate_train_scratch_floats(int32_t n);
+/* One optimisation step over n samples: fused forward/backward per 64-sample
+ * chunk, then Adam (step >= 1) on params with moments adam_m/adam_v (all
+ * device FP32, DRV_SURROGATE_PARAMS each). loss_out (device, 2 floats, may be
+ * NULL) receives the summed visibility and confidence losses. */
+drv_status drv_surrogate_train_step(const float* features, const float* targets, int32_t n, float* params,
+                                    float* adam_m, float* adam_v, float* scratch, int32_t step, float lr,
+                                    float conf_tau, float weight_decay, float* loss_out, void* cuda_stream);
+/* Evaluates the context's inference weights on n feature rows:
+ * out[n][2] = (visibility, confidence). */
+drv_status drv_surrogate_eval(DrvContext* ctx, const float* features, int32_t n, float* out);
+/* Pairs re-traced with the cone by the last surrogate light stage. Synchronises. */
+drv_status drv_get_surrogate_fallbacks(DrvContext* ctx, uint32_t* out);
+
 /* ---- allocation-free light stage ------------------------------------------
  * No counterpart in the reference: the reference renderer always owns its GL
  * buffers. This is the cache-lighting stage (the kernel behind

@@ -864,6 +864,54 @@ void orc_light_caches(const DrvConfig* cfg, const DrvVolumeInfo* vol, int n_cach
   }
 }
 
+// The SH gather of cacheLightingRSM.comp:234-279 with the shadowing of every
+// (cache, shadow block) pair given (shadow[c * total_blocks + b], blocks of all
+// lights in light order) instead of cone-traced: checks a learned visibility.
+void orc_light_caches_shadowed(const DrvConfig* cfg, int n_caches, const float* positions, int n_lights,
+                               const DrvSpotLight* lights, const double* const* vpls, const int* n_vpls,
+                               const double* shadow, int total_blocks, double* sh_out, int n_threads) {
+  set_threads(n_threads);
+  double cl[5], ev[5];
+  orc_sh_constants(DRV_SH2_SIGN_REFERENCE, cl, ev);
+  const bool sh2 = cfg->sh_order == 2;
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int c = 0; c < n_caches; ++c) {
+    double acc[27];
+    for (int k = 0; k < 27; ++k) acc[k] = 0.0;
+    d3 wp = ld3(positions + 3 * c);
+    int block_base = 0;
+    for (int l = 0; l < n_lights; ++l) {
+      const double* V = vpls[l];
+      const int interval = cfg->indirect_shadow ? lights[l].indirect_shadow_sample_interval : 1;
+      for (int j = 0; j < n_vpls[l]; ++j) {
+        const double shadowing = shadow[(size_t)c * total_blocks + block_base + j / interval];
+        const double* v = V + 10 * j;
+        d3 to = mk(v[4], v[5], v[6]) - wp;
+        double d2 = dot(to, to);
+        to = to * (1.0 / std::sqrt(d2));
+        double f = saturate(-dot(mk(v[7], v[8], v[9]), to)) * shadowing;
+        double s = f / (d2 + v[3]);
+        for (int ch = 0; ch < 3; ++ch) {
+          double L = v[ch] * s;
+          acc[0 * 3 + ch] += ev[0] * L;
+          acc[1 * 3 + ch] -= (ev[1] * to.y) * L;
+          acc[2 * 3 + ch] += (ev[1] * to.z) * L;
+          acc[3 * 3 + ch] -= (ev[1] * to.x) * L;
+          if (sh2) {
+            acc[4 * 3 + ch] -= (ev[2] * to.x * to.y) * L;
+            acc[5 * 3 + ch] += (ev[2] * to.y * to.z) * L;
+            acc[6 * 3 + ch] += (ev[3] * (to.z * to.z * 3.0 - 1.0)) * L;
+            acc[7 * 3 + ch] += (ev[2] * to.x * to.z) * L;
+            acc[8 * 3 + ch] += (ev[4] * (to.x * to.x - to.y * to.y)) * L;
+          }
+        }
+      }
+      block_base += n_vpls[l] / interval;
+    }
+    for (int k = 0; k < 27; ++k) sh_out[(size_t)c * 27 + k] = acc[k];
+  }
+}
+
 // cacheApply.frag:204-294 (ComputeLightingFromCaches) and :296-362 (main).
 // Corners outside the atlas, or whose atlas slot holds 0 (never allocated) or
 // 0xFFFFFFFF (locked, capacity overflow), contribute zero irradiance; their

@@ -88,6 +88,11 @@ int orc_allocate_caches(const DrvConfig* cfg, const DrvVolumeInfo* vol, const Dr
 void orc_light_caches(const DrvConfig* cfg, const DrvVolumeInfo* vol, int n_caches, const float* positions,
                       int n_lights, const DrvSpotLight* lights, const double* const* vpls, const double* const* cones,
                       const int* n_vpls, const uint32_t* bits, const double* mips, double* sh_out, int n_threads);
+/* The same gather with given shadowing per (cache, shadow block) pair:
+ * shadow[c * total_blocks + b], blocks of all lights in light order. */
+void orc_light_caches_shadowed(const DrvConfig* cfg, int n_caches, const float* positions, int n_lights,
+                               const DrvSpotLight* lights, const double* const* vpls, const int* n_vpls,
+                               const double* shadow, int total_blocks, double* sh_out, int n_threads);
 /* cacheApply.frag per pixel; normal is RG16I (normal_format 0) or F32x3. */
 void orc_apply(const DrvConfig* cfg, const DrvVolumeInfo* vol, const DrvPerFrame* frame, int width, int height,
                const float* depth, const void* normal, int normal_format, const float* albedo, const uint32_t* atlas,

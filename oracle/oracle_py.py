@@ -63,6 +63,8 @@ def load():
                                     P(C.c_uint32)]),
         "orc_light_caches": (None, [P(abi.DrvConfig), P(abi.DrvVolumeInfo), I, VP, I, P(abi.DrvSpotLight),
                                     P(VP), P(VP), P(I), VP, VP, VP, I]),
+        "orc_light_caches_shadowed": (None, [P(abi.DrvConfig), I, VP, I, P(abi.DrvSpotLight), P(VP), P(I), VP, I, VP,
+                                             I]),
         "orc_apply": (None, [P(abi.DrvConfig), P(abi.DrvVolumeInfo), P(abi.DrvPerFrame), I, I, VP, VP, I, VP, VP, I,
                              VP, VP, I]),
     }
@@ -241,6 +243,20 @@ def light_caches(cfg, vol, positions, lights, vpls, cones, bits, mips, n_threads
     nv = (C.c_int * L)(*[v.shape[0] for v in vpls])
     load().orc_light_caches(C.byref(cfg), C.byref(vol), n, _p(positions), L, lights, vp, cp, nv, _p(bits), _p(mips),
                             _p(sh), n_threads)
+    return sh
+
+
+def light_caches_shadowed(cfg, positions, lights, vpls, shadow, n_threads=0):
+    """SH gather with per-(cache, block) shadowing [n_caches, total_blocks]."""
+    positions = np.ascontiguousarray(positions, dtype=np.float32)
+    shadow = np.ascontiguousarray(shadow, dtype=np.float64)
+    n = positions.shape[0]
+    L = len(vpls)
+    sh = np.zeros((n, 27), np.float64)
+    vp = (C.c_void_p * L)(*[v.ctypes.data for v in vpls])
+    nv = (C.c_int * L)(*[v.shape[0] for v in vpls])
+    load().orc_light_caches_shadowed(C.byref(cfg), n, _p(positions), L, lights, vp, nv, _p(shadow), shadow.shape[1],
+                                     _p(sh), n_threads)
     return sh
 
 

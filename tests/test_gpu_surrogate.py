@@ -1,0 +1,166 @@
+"""The learned visibility surrogate: training kernels against a PyTorch FP32
+autograd reference, the inference MLP against a PyTorch FP32 reference, and
+the tensor-core light stage against the FP64 gather fed with the MLP's own
+visibilities; with every pair re-traced it must equal the cone-traced stage.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from dynamicradiancevolume_gb300 import abi, pipeline, surrogate
+from test_gpu_parity import Run, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+W_SMALL = pipeline.scaled(pipeline.WORKLOADS["c1_small"], name="c1_surrogate", sh_order=2, max_caches=8192)
+
+
+def torch_mlp(torch, params, X):
+    """FP32 reference of the surrogate MLP (tanh GELU)."""
+    p = params
+    o = 0
+    mats = []
+    for name, shape in surrogate.LAYOUT:
+        n = int(np.prod(shape))
+        mats.append(p[o:o + n].view(*shape))
+        o += n
+    W1, b1, W2, b2, W3, b3, W4, b4 = mats
+    g = lambda z: torch.nn.functional.gelu(z, approximate="tanh")
+    h = g(X @ W1.T + b1)
+    h = g(h @ W2.T + b2)
+    h = g(h @ W3.T + b3)
+    return h @ W4.T + b4
+
+
+def _pairs(lib, pipe, n, seed):
+    torch = pipe.torch
+    X = torch.empty((n, abi.SURROGATE_INPUTS), dtype=torch.float32, device=pipe.device)
+    Y = torch.empty((n,), dtype=torch.float32, device=pipe.device)
+    assert lib.drv_surrogate_make_pairs(pipe.ctx, seed, n, C.c_void_p(X.data_ptr()), C.c_void_p(Y.data_ptr())) == 0
+    pipe.sync()
+    return X, Y
+
+
+@pytest.fixture(scope="module")
+def frame(lib, oracle, cuda):
+    return Run(W_SMALL, oracle, seed=21)
+
+
+def test_pairs_targets_are_cone_visibility(frame, lib):
+    X, Y = _pairs(lib, frame.pipe, 4096, 5)
+    y = Y.cpu().numpy()
+    assert np.all((y >= 0) & (y <= 1))
+    assert 0.05 < y.mean() < 0.999
+    x = X.cpu().numpy()
+    assert np.all(x[:, surrogate.N_IN - 1] == 0)  # padding
+    assert np.all((x[:, 9:17] >= 0) & (x[:, 9:17] <= 1))  # opacity samples
+
+
+def test_train_step_matches_torch_autograd(frame, lib):
+    torch = frame.torch
+    X, Y = _pairs(lib, frame.pipe, 1000, 7)
+    params = torch.from_numpy(surrogate.init_params(3)).to(frame.pipe.device)
+    ref = params.clone().requires_grad_(True)
+    m, v = torch.zeros_like(params), torch.zeros_like(params)
+    scratch = torch.empty(lib.drv_surrogate_train_scratch_floats(1000), dtype=torch.float32, device=params.device)
+    loss = torch.zeros(2, dtype=torch.float32, device=params.device)
+    tau, lr = 0.03, 1e-4
+    p0 = params.clone()
+    st = lib.drv_surrogate_train_step(C.c_void_p(X.data_ptr()), C.c_void_p(Y.data_ptr()), 1000,
+                                      C.c_void_p(params.data_ptr()), C.c_void_p(m.data_ptr()),
+                                      C.c_void_p(v.data_ptr()), C.c_void_p(scratch.data_ptr()), 1, lr, tau, 0.0,
+                                      C.c_void_p(loss.data_ptr()), None)
+    assert st == abi.OK
+    torch.cuda.synchronize()
+    out = torch_mlp(torch, ref, X)
+    vis, conf = torch.sigmoid(out[:, 0]), torch.sigmoid(out[:, 1])
+    ct = ((vis - Y).abs() < tau).float().detach()
+    l0 = torch.nn.functional.binary_cross_entropy(vis, Y, reduction="sum")
+    l1 = torch.nn.functional.binary_cross_entropy(conf, ct, reduction="sum")
+    assert float(loss[0]) == pytest.approx(float(l0), rel=1e-4)
+    assert float(loss[1]) == pytest.approx(float(l1), rel=1e-4)
+    ((l0 + l1) / 1000).backward()
+    g = ref.grad
+    # First Adam step moves each parameter by lr * g / (|g| + eps): the sign of the gradient.
+    step = (p0 - params) / lr
+    big = g.abs() > 1e-5
+    assert bool(big.any())
+    agree = (torch.sign(step[big]) == torch.sign(g[big])).float().mean()
+    assert float(agree) > 0.999
+    assert torch.allclose(step[big], (g / (g.abs() + 1e-8))[big], atol=2e-2)
+
+
+def test_training_reduces_loss(frame, lib):
+    torch = frame.torch
+    X, Y = _pairs(lib, frame.pipe, 65536, 11)
+    losses = []
+    surrogate.train(X, Y, epochs=4, batch=4096, lr=3e-3, log=lambda s: losses.append(float(s.split("BCE ")[1].split(",")[0])))
+    assert len(losses) == 4
+    assert losses[-1] < losses[0]
+
+
+def test_inference_mlp_matches_torch_fp32(frame, lib):
+    torch = frame.torch
+    X, _ = _pairs(lib, frame.pipe, 2048, 13)
+    params = surrogate.init_params(4) * 3.0
+    surrogate.upload(frame.pipe, params)
+    out = torch.empty((2048, 2), dtype=torch.float32, device=frame.pipe.device)
+    assert lib.drv_surrogate_eval(frame.pipe.ctx, C.c_void_p(X.data_ptr()), 2048, C.c_void_p(out.data_ptr())) == 0
+    frame.pipe.sync()
+    # reference with the same BF16-rounded weights and inputs, FP32 arithmetic
+    pb = torch.from_numpy(params).to(X.device).bfloat16().float()
+    ref = torch.sigmoid(torch_mlp(torch, pb, X.bfloat16().float()))
+    assert torch.allclose(out, ref, atol=2e-2)
+    assert float((out - ref).abs().mean()) < 3e-3
+
+
+def _surrogate_run(threshold, params, oracle, seed=21):
+    w = pipeline.scaled(W_SMALL, visibility=abi.VISIBILITY_SURROGATE)
+    hf = pipeline.host_frame(w, seed)
+    hf.config.surrogate_conf_threshold = threshold
+    p = pipeline.Pipeline(hf)
+    surrogate.upload(p, params)
+    p.raycast_inputs()
+    p.prepare_and_extract()
+    p.voxelize()
+    p.allocate()
+    p.light()
+    p.sync()
+    n = p.cache_count()
+    pos, sh = p.read_entries_decoded(n)
+    fb = C.c_uint32()
+    assert p.lib.drv_get_surrogate_fallbacks(p.ctx, C.byref(fb)) == 0
+    return p, pos, sh, fb.value
+
+
+def test_all_pairs_retraced_equals_cone_stage(frame, oracle):
+    params = surrogate.init_params(5)
+    p, pos, sh, fallbacks = _surrogate_run(2.0, params, oracle)  # confidence never reaches 2
+    n_blocks = sum(p.buffers().n_vpls[l] for l in range(W_SMALL.n_lights))
+    assert fallbacks == frame.count * n_blocks
+    assert np.array_equal(pos, frame.positions)
+    assert rel_l2(sh, frame.gpu_sh()) < 1e-5
+    p.close()
+
+
+def test_tensor_core_light_matches_fp64_gather_of_mlp_visibility(frame, lib, oracle):
+    torch = frame.torch
+    params = surrogate.init_params(6) * 2.0
+    p, pos, sh, fallbacks = _surrogate_run(0.0, params, oracle)  # never re-trace
+    assert fallbacks == 0
+    b = p.buffers()
+    n_blocks = sum(b.n_vpls[l] for l in range(W_SMALL.n_lights))
+    n = pos.shape[0]
+    X = torch.empty((n * n_blocks, abi.SURROGATE_INPUTS), dtype=torch.float32, device=p.device)
+    Y = torch.empty((n * n_blocks,), dtype=torch.float32, device=p.device)
+    assert lib.drv_surrogate_make_pairs(p.ctx, abi.SURROGATE_ENUMERATE, n * n_blocks, C.c_void_p(X.data_ptr()),
+                                        C.c_void_p(Y.data_ptr())) == 0
+    out = torch.empty((n * n_blocks, 2), dtype=torch.float32, device=p.device)
+    assert lib.drv_surrogate_eval(p.ctx, C.c_void_p(X.data_ptr()), n * n_blocks, C.c_void_p(out.data_ptr())) == 0
+    p.sync()
+    shadow = out[:, 0].double().cpu().numpy().reshape(n, n_blocks)
+    vpls = [v for v in frame.gpu_vpls_f64()]
+    ref = oracle.light_caches_shadowed(p.hf.config, pos, p.hf.lights, vpls, shadow)
+    assert rel_l2(sh, ref) < 2e-3
+    p.close()
