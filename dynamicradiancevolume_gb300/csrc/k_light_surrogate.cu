@@ -105,8 +105,8 @@ __device__ __forceinline__ void hidden_layer(const uint32_t (&in)[2][KSTEPS][4],
     const float bl = bias[8 * j + 2 * tig], bh = bias[8 * j + 2 * tig + 1];
 #pragma unroll
     for (int m = 0; m < 2; ++m) {
-      const uint32_t lo = pack_bf16x2(gelu(acc[m][0] + bl), gelu(acc[m][1] + bh));
-      const uint32_t hi = pack_bf16x2(gelu(acc[m][2] + bl), gelu(acc[m][3] + bh));
+      const uint32_t lo = pack_bf16x2(gelu_fast(acc[m][0] + bl), gelu_fast(acc[m][1] + bh));
+      const uint32_t hi = pack_bf16x2(gelu_fast(acc[m][2] + bl), gelu_fast(acc[m][3] + bh));
       // n-tile j feeds k-step j/2 of the next layer: even tiles are its low
       // k half (regs 0,1), odd tiles its high half (regs 2,3).
       out[m][j >> 1][(j & 1) * 2 + 0] = lo;
@@ -405,17 +405,17 @@ __global__ void eval_kernel(const MlpWeights* __restrict__ w, const float* __res
   for (int j = 0; j < kMlpHidden; ++j) {
     float s = 0.0f;
     for (int k = 0; k < kMlpIn; ++k) s += from_bf16(w->w1[j * kLd1 + k]) * x[k];
-    h[j] = from_bf16(to_bf16(gelu(s + w->b1[j])));
+    h[j] = from_bf16(to_bf16(gelu_fast(s + w->b1[j])));
   }
   for (int j = 0; j < kMlpHidden; ++j) {
     float s = 0.0f;
     for (int k = 0; k < kMlpHidden; ++k) s += from_bf16(w->w2[j * kLdH + k]) * h[k];
-    h2[j] = from_bf16(to_bf16(gelu(s + w->b2[j])));
+    h2[j] = from_bf16(to_bf16(gelu_fast(s + w->b2[j])));
   }
   for (int j = 0; j < kMlpHidden; ++j) {
     float s = 0.0f;
     for (int k = 0; k < kMlpHidden; ++k) s += from_bf16(w->w3[j * kLdH + k]) * h2[k];
-    h[j] = from_bf16(to_bf16(gelu(s + w->b3[j])));
+    h[j] = from_bf16(to_bf16(gelu_fast(s + w->b3[j])));
   }
   for (int j = 0; j < kMlpOut; ++j) {
     float s = 0.0f;

@@ -21,7 +21,7 @@ constexpr int kMlpIn = 32;
 constexpr int kMlpHidden = 64;
 constexpr int kMlpOut = 2;
 constexpr int kMlpOutPad = 8;  // layer-4 rows padded to one n8 MMA tile
-constexpr int kFeatures = 22;  // used inputs; the rest are zero
+constexpr int kFeatures = 27;  // used inputs; the rest are zero
 
 // Parameter offsets (floats) of the flat FP32 master copy; weights are
 // [out][in] row-major (in contiguous), biases follow each weight matrix.
@@ -48,6 +48,18 @@ __device__ __forceinline__ float gelu_grad(float x) {
 }
 __device__ __forceinline__ float sigmoidf(float x) { return 1.0f / (1.0f + __expf(-x)); }
 
+// GELU for inference: the same tanh form with the hardware tanh
+// approximation (MUFU.TANH), as the BF16 activations it feeds tolerate.
+__device__ __forceinline__ float tanh_fast(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float gelu_fast(float x) {
+  const float u = 0.7978845608f * (x + 0.044715f * x * x * x);
+  return 0.5f * x * (1.0f + tanh_fast(u));
+}
+
 // Distance (in voxels) the cone of cacheLightingRSM.comp:195-228 reaches
 // before it stops: min(goal, the distance after max_steps steps). The step
 // rule is stepSize = max(1, dist * dsr * 2 / (1 - dsr)); it is evaluated here
@@ -68,7 +80,13 @@ __device__ __forceinline__ float cone_reach(float goal, float dsr, int max_steps
 }
 
 // Input features of one (cache, shadow block) pair. cache/target are world
-// positions, n the first VPL's normal, dsr the cone aperture.
+// positions, (px, py, pz) the cache in normalised volume coordinates, n the
+// first VPL's normal, dsr the cone aperture:
+//   0-2 cache, 3-5 cone target (normalised volume coordinates), 6-8 normal,
+//   9-16 eight mip-3 opacity samples along the part of the segment the cone
+//   traces, 17 aperture, 18 length, 19-21 direction, 22-25 the cone's own
+//   first four samples (same positions and LOD as cacheLightingRSM.comp:
+//   211-225), 26 their composited occlusion.
 __device__ __forceinline__ void surrogate_features(const VoxelView& v, float inv_extent, const float vol_min[3],
                                                    float voxel_size, int max_steps, float cx, float cy, float cz,
                                                    float tx, float ty, float tz, float nx, float ny, float nz,
@@ -104,6 +122,27 @@ __device__ __forceinline__ void surrogate_features(const VoxelView& v, float inv
   f[19] = dx * inv_len;
   f[20] = dy * inv_len;
   f[21] = dz * inv_len;
+  // The cone's first four steps, exactly as the tracer takes them.
+  {
+    const float inv_n = 1.0f / (float)v.N;
+    const float sx = dx * inv_len * inv_n, sy = dy * inv_len * inv_n, sz = dz * inv_len * inv_n;
+    float ux = px + sx * 2.0f, uy = py + sy * 2.0f, uz = pz + sz * 2.0f;
+    float step = 1.0f, dist = 0.0f, transmit = 1.0f;
+    const float k = 2.0f / (1.0f - dsr);
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      ux += sx * step;
+      uy += sy * step;
+      uz += sz * step;
+      dist += step;
+      const float radius = dist * dsr;
+      const float occ = (dist - step < len_vox - 2.0f) ? sample_voxels(v, ux, uy, uz, __log2f(radius)) : 0.0f;
+      f[22 + s] = occ;
+      transmit *= 1.0f - occ;
+      step = fmaxf(1.0f, radius * k);
+    }
+    f[26] = 1.0f - transmit;
+  }
 #pragma unroll
   for (int i = kFeatures; i < kMlpIn; ++i) f[i] = 0.0f;
 }

@@ -119,7 +119,7 @@ def generate_pairs(seeds, pairs_per_scene: int, workload=TRAIN_WORKLOAD, device=
     return X, Y
 
 
-def train(X, Y, epochs=8, batch=16384, lr=2e-3, conf_tau=0.03, weight_decay=0.0, seed=0, log=print):
+def train(X, Y, epochs=6, batch=4096, lr=2e-3, conf_tau=0.03, weight_decay=0.0, seed=0, log=print):
     """Adam on the hand-written training kernels; returns FP32 numpy params."""
     import torch
     lib = load()
@@ -174,6 +174,38 @@ def evaluate(pipe, X, Y, threshold: float):
             "p99_err_confident": float(err[confident].quantile(0.99)) if bool(confident.any()) else None}
 
 
+def frame_error(params, seeds, threshold: float, workload=None, device="cuda"):
+    """Final indirect radiance of full frames with surrogate visibility
+    against the same frames with cone visibility (both on the GPU): relative
+    L2 per seed and the share of pairs re-traced."""
+    import torch
+    workload = workload or pipeline.WORKLOADS["ns_1080p_4096"]
+    out = []
+    for seed in seeds:
+        hf_c = pipeline.host_frame(workload, seed)
+        cone = pipeline.Pipeline(hf_c, device=device)
+        cone.raycast_inputs()
+        cone.frame()
+        cone.sync()
+        ref = cone.out.clone()
+        count = cone.cache_count()
+        cone.close()
+        hf_s = pipeline.host_frame(pipeline.scaled(workload, visibility=abi.VISIBILITY_SURROGATE), seed)
+        hf_s.config.surrogate_conf_threshold = threshold
+        sur = pipeline.Pipeline(hf_s, device=device)
+        upload(sur, params)
+        sur.raycast_inputs()
+        sur.frame()
+        sur.sync()
+        fb = C.c_uint32()
+        check(sur.lib.drv_get_surrogate_fallbacks(sur.ctx, C.byref(fb)), sur.ctx)
+        err = float(torch.linalg.vector_norm((sur.out - ref).double()) / torch.linalg.vector_norm(ref.double()))
+        pairs = count * workload.n_vpls
+        out.append({"seed": seed, "rel_l2_vs_cone": err, "retraced_share": fb.value / max(pairs, 1)})
+        sur.close()
+    return out
+
+
 def main(argv=None):
     import torch
     ap = argparse.ArgumentParser()
@@ -181,8 +213,8 @@ def main(argv=None):
     t = sub.add_parser("train")
     t.add_argument("--scenes", type=int, default=200)
     t.add_argument("--pairs", type=int, default=100_000)
-    t.add_argument("--epochs", type=int, default=8)
-    t.add_argument("--batch", type=int, default=16384)
+    t.add_argument("--epochs", type=int, default=6)
+    t.add_argument("--batch", type=int, default=4096)
     t.add_argument("--lr", type=float, default=2e-3)
     t.add_argument("--tau", type=float, default=0.03)
     t.add_argument("--out", type=Path, default=DEFAULT_WEIGHTS)
@@ -203,7 +235,13 @@ def main(argv=None):
     upload(pipe, params)
     stats = evaluate(pipe, Xe, Ye, threshold=0.5)
     pipe.close()
-    print("held-out:", json.dumps(stats))
+    print("held-out pairs:", json.dumps(stats))
+    frames = {}
+    for thr in (0.0, 0.5, 0.8):
+        fe = frame_error(params, list(range(1000, 1000 + args.eval_scenes)), thr)
+        frames[str(thr)] = fe
+        print(f"held-out frames, threshold {thr}:", json.dumps(fe))
+    stats["frames"] = frames
     save(params, args.out, {"trained_on": {"workload": TRAIN_WORKLOAD.name, "scene_seeds": [0, args.scenes - 1],
                                            "pairs": args.scenes * args.pairs, "epochs": args.epochs,
                                            "batch": args.batch, "lr": args.lr, "conf_tau": args.tau,

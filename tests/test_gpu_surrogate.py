@@ -16,8 +16,10 @@ pytestmark = pytest.mark.gpu
 W_SMALL = pipeline.scaled(pipeline.WORKLOADS["c1_small"], name="c1_surrogate", sh_order=2, max_caches=8192)
 
 
-def torch_mlp(torch, params, X):
-    """FP32 reference of the surrogate MLP (tanh GELU)."""
+def torch_mlp(torch, params, X, bf16_activations=False):
+    """FP32 reference of the surrogate MLP (tanh GELU); with
+    bf16_activations the hidden activations are rounded to BF16 as the
+    tensor-core inference path stores them."""
     p = params
     o = 0
     mats = []
@@ -26,7 +28,8 @@ def torch_mlp(torch, params, X):
         mats.append(p[o:o + n].view(*shape))
         o += n
     W1, b1, W2, b2, W3, b3, W4, b4 = mats
-    g = lambda z: torch.nn.functional.gelu(z, approximate="tanh")
+    r = (lambda t: t.bfloat16().float()) if bf16_activations else (lambda t: t)
+    g = lambda z: r(torch.nn.functional.gelu(z, approximate="tanh"))
     h = g(X @ W1.T + b1)
     h = g(h @ W2.T + b2)
     h = g(h @ W3.T + b3)
@@ -53,8 +56,9 @@ def test_pairs_targets_are_cone_visibility(frame, lib):
     assert np.all((y >= 0) & (y <= 1))
     assert 0.05 < y.mean() < 0.999
     x = X.cpu().numpy()
-    assert np.all(x[:, surrogate.N_IN - 1] == 0)  # padding
-    assert np.all((x[:, 9:17] >= 0) & (x[:, 9:17] <= 1))  # opacity samples
+    assert np.all(x[:, 27:] == 0)  # padding
+    assert np.all((x[:, 9:17] >= 0) & (x[:, 9:17] <= 1))  # mip-3 opacity samples
+    assert np.all((x[:, 22:27] >= 0) & (x[:, 22:27] <= 1))  # the cone's first samples and their occlusion
 
 
 def test_train_step_matches_torch_autograd(frame, lib):
@@ -78,8 +82,8 @@ def test_train_step_matches_torch_autograd(frame, lib):
     ct = ((vis - Y).abs() < tau).float().detach()
     l0 = torch.nn.functional.binary_cross_entropy(vis, Y, reduction="sum")
     l1 = torch.nn.functional.binary_cross_entropy(conf, ct, reduction="sum")
-    assert float(loss[0]) == pytest.approx(float(l0), rel=1e-4)
-    assert float(loss[1]) == pytest.approx(float(l1), rel=1e-4)
+    assert float(loss[0]) == pytest.approx(float(l0.detach()), rel=1e-4)
+    assert float(loss[1]) == pytest.approx(float(l1.detach()), rel=1e-4)
     ((l0 + l1) / 1000).backward()
     g = ref.grad
     # First Adam step moves each parameter by lr * g / (|g| + eps): the sign of the gradient.
@@ -103,16 +107,16 @@ def test_training_reduces_loss(frame, lib):
 def test_inference_mlp_matches_torch_fp32(frame, lib):
     torch = frame.torch
     X, _ = _pairs(lib, frame.pipe, 2048, 13)
-    params = surrogate.init_params(4) * 3.0
+    params = surrogate.init_params(4) * 2.0
     surrogate.upload(frame.pipe, params)
     out = torch.empty((2048, 2), dtype=torch.float32, device=frame.pipe.device)
     assert lib.drv_surrogate_eval(frame.pipe.ctx, C.c_void_p(X.data_ptr()), 2048, C.c_void_p(out.data_ptr())) == 0
     frame.pipe.sync()
-    # reference with the same BF16-rounded weights and inputs, FP32 arithmetic
+    # reference with the same BF16-rounded weights, inputs and activations, FP32 arithmetic
     pb = torch.from_numpy(params).to(X.device).bfloat16().float()
-    ref = torch.sigmoid(torch_mlp(torch, pb, X.bfloat16().float()))
-    assert torch.allclose(out, ref, atol=2e-2)
-    assert float((out - ref).abs().mean()) < 3e-3
+    ref = torch.sigmoid(torch_mlp(torch, pb, X.bfloat16().float(), bf16_activations=True))
+    assert torch.allclose(out, ref, atol=1e-2)
+    assert float((out - ref).abs().mean()) < 1e-3
 
 
 def _surrogate_run(threshold, params, oracle, seed=21):
@@ -139,8 +143,10 @@ def test_all_pairs_retraced_equals_cone_stage(frame, oracle):
     p, pos, sh, fallbacks = _surrogate_run(2.0, params, oracle)  # confidence never reaches 2
     n_blocks = sum(p.buffers().n_vpls[l] for l in range(W_SMALL.n_lights))
     assert fallbacks == frame.count * n_blocks
-    assert np.array_equal(pos, frame.positions)
-    assert rel_l2(sh, frame.gpu_sh()) < 1e-5
+    # allocation order is atomic order: compare caches sorted by position
+    a, b = np.lexsort(pos.T[::-1]), np.lexsort(frame.positions.T[::-1])
+    assert np.array_equal(pos[a], frame.positions[b])
+    assert rel_l2(sh[a], frame.gpu_sh()[b]) < 1e-5
     p.close()
 
 
