@@ -24,6 +24,7 @@
 
 #include "drv_device.cuh"
 #include "drv_internal.h"
+#include "light_common.cuh"
 #include "voxel_sample.cuh"
 
 namespace drv {
@@ -54,79 +55,8 @@ struct LightParams {
   float ev[5];        // ShEvaFactor0, 1, 2n2_p1_n1, 20, 2p2 (renderer.cpp:302-306)
 };
 
-struct VplData {
-  float px, py, pz, area, fr, fg, fb, nx, ny, nz;
-};
-
-template <bool BF16>
-__device__ __forceinline__ VplData load_vpl(const void* base, int i) {
-  VplData d;
-  if (BF16) {
-    const uint4* q = reinterpret_cast<const uint4*>(static_cast<const DrvVPLBF16*>(base) + i);
-    const uint4 a = __ldg(q), b = __ldg(q + 1);
-    d.px = __uint_as_float(a.x);
-    d.py = __uint_as_float(a.y);
-    d.pz = __uint_as_float(a.z);
-    d.area = __uint_as_float(a.w);
-    d.fr = from_bf16((uint16_t)(b.x & 0xFFFFu));
-    d.fg = from_bf16((uint16_t)(b.x >> 16));
-    d.fb = from_bf16((uint16_t)(b.y & 0xFFFFu));
-    d.nx = from_bf16((uint16_t)(b.y >> 16));
-    d.ny = from_bf16((uint16_t)(b.z & 0xFFFFu));
-    d.nz = from_bf16((uint16_t)(b.z >> 16));
-  } else {
-    const float4* q = reinterpret_cast<const float4*>(static_cast<const DrvVPL*>(base) + i);
-    const float4 a = __ldg(q), b = __ldg(q + 1), n = __ldg(q + 2);  // {flux, area}, {position}, {normal}
-    d.fr = a.x;
-    d.fg = a.y;
-    d.fb = a.z;
-    d.area = a.w;
-    d.px = b.x;
-    d.py = b.y;
-    d.pz = b.z;
-    d.nx = n.x;
-    d.ny = n.y;
-    d.nz = n.z;
-  }
-  return d;
-}
-
-// acc (and comp, with KAHAN) point at this thread's column of a
-// [NK*3][kThreads] shared array.
-template <int NK, bool KAHAN>
-__device__ __forceinline__ void accumulate_vpl(const LightParams& p, float* acc, float* comp, const VplData& v,
-                                               float cx, float cy, float cz, float shadowing) {
-  float tx = v.px - cx, ty = v.py - cy, tz = v.pz - cz;
-  const float d2 = tx * tx + ty * ty + tz * tz;
-  const float r = rsqrtf(d2);
-  tx *= r;
-  ty *= r;
-  tz *= r;
-  const float f = sat(-(v.nx * tx + v.ny * ty + v.nz * tz)) * shadowing;
-  const float s = f / (d2 + v.area);
-  const float L[3] = {v.fr * s, v.fg * s, v.fb * s};
-  const float bs[9] = {p.ev[0], -p.ev[1] * ty, p.ev[1] * tz, -p.ev[1] * tx, -p.ev[2] * tx * ty, p.ev[2] * ty * tz,
-                       p.ev[3] * (tz * tz * 3.0f - 1.0f), p.ev[2] * tx * tz, p.ev[4] * (tx * tx - ty * ty)};
-#pragma unroll
-  for (int k = 0; k < NK; ++k)
-#pragma unroll
-    for (int ch = 0; ch < 3; ++ch) {
-      const int o = (3 * k + ch) * kThreads;
-      const float x = bs[k] * L[ch];
-      if (KAHAN) {
-        // Kahan-compensated running sum (FP32 accumulation, BF16 storage).
-        const float y = __fsub_rn(x, comp[o]);
-        const float t = __fadd_rn(acc[o], y);
-        comp[o] = __fsub_rn(__fsub_rn(t, acc[o]), y);
-        acc[o] = t;
-      } else {
-        acc[o] += x;
-      }
-    }
-}
-
 // Adds the finished sum of coefficient `lane` to the entry.
-template <int NK, bool BF16>
+template <bool BF16>
 __device__ __forceinline__ void add_to_entry(float* entry, int lane, float v) {
   if (BF16) {
     uint16_t* sh = reinterpret_cast<uint16_t*>(entry + 1);
@@ -136,17 +66,31 @@ __device__ __forceinline__ void add_to_entry(float* entry, int lane, float v) {
   }
 }
 
-// One warp = one unit (cache, chunk); warps never wait for each other. The
-// SH partial sums live in shared memory (touched once per pair, against
+// Shadow block b (global index) -> light and block within the light.
+__device__ __forceinline__ int block_light(const LightParams& p, int b) {
+  int l = 0;
+  while (b >= p.block_base[l + 1]) ++l;
+  return l;
+}
+
+// One warp = one unit (cache, chunk); warps never wait for each other.
+//  - Lanes first test their shadow blocks: a block none of whose VPLs has
+//    positive flux and faces the cache adds exactly zero whatever its
+//    shadowing, so its cone is not traced (the reference traces it).
+//  - Blocks that can contribute go to a per-warp queue; every 32 queued
+//    blocks are traced together, so all lanes march a cone.
+// The SH partial sums live in shared memory (touched once per pair, against
 // hundreds of cone instructions), which keeps the cone loop's register
 // footprint small enough for 8 CTAs per SM.
 template <int NK, bool BF16>
 __global__ void __launch_bounds__(kThreads, 8) light_kernel(LightParams p) {
   constexpr bool KAHAN = BF16;
   __shared__ float s_acc[NK * 3 * kThreads * (KAHAN ? 2 : 1)];
+  __shared__ int s_queue[kWarps][64];
   const uint32_t count = min((uint32_t)max(p.counter->total_light_cache_count, 0), p.max_caches);
   const uint32_t n_units = count * (uint32_t)p.n_chunks;
   const int lane = threadIdx.x & 31;
+  int* queue = s_queue[threadIdx.x >> 5];
   const uint32_t warps = gridDim.x * kWarps;
   for (uint32_t u = blockIdx.x * kWarps + (threadIdx.x >> 5); u < n_units; u += warps) {
     const uint32_t cache = u / (uint32_t)p.n_chunks;
@@ -174,23 +118,51 @@ __global__ void __launch_bounds__(kThreads, 8) light_kernel(LightParams p) {
       acc[k * kThreads] = 0.0f;
       if (KAHAN) comp[k * kThreads] = 0.0f;
     }
-    const int b0 = chunk * p.chunk_blocks, b1 = min(b0 + p.chunk_blocks, p.total_blocks);
-    int l = 0;
-    for (int b = b0 + lane; b < b1; b += 32) {
-      while (b >= p.block_base[l + 1]) ++l;
+    // Traces the cone of block qb and gathers its contributing VPLs.
+    auto trace_block = [&](int qb) {
+      const int l = block_light(p, qb);
       const LightArgs& la = p.ll.lights[l];
-      const int lb = b - p.block_base[l];
-      float shadowing = 1.0f;
-      int v0 = lb, nv = 1;
-      if (p.shadow) {
-        const float4 c = __ldg(reinterpret_cast<const float4*>(la.cones) + lb);
-        shadowing = cone_shadow(p.vox, p.voxel_size, p.max_steps, cx, cy, cz, vx, vy, vz, c.x, c.y, c.z, c.w);
-        v0 = lb * la.interval;
-        nv = la.interval;
+      const int lb = qb - p.block_base[l];
+      const float4 c = __ldg(reinterpret_cast<const float4*>(la.cones) + lb);
+      const float s = cone_shadow(p.vox, p.voxel_size, p.max_steps, cx, cy, cz, vx, vy, vz, c.x, c.y, c.z, c.w);
+      for (int j = 0; j < la.interval; ++j) {
+        const VplData v = load_vpl<BF16>(la.vpls, lb * la.interval + j);
+        const Transfer t = transfer(v, cx, cy, cz);
+        if (contributes(v, t)) accumulate<NK, KAHAN>(p.ev, acc, comp, kThreads, v, t, s);
       }
-      for (int j = 0; j < nv; ++j)
-        accumulate_vpl<NK, KAHAN>(p, acc, comp, load_vpl<BF16>(la.vpls, v0 + j), cx, cy, cz, shadowing);
+    };
+    const int b0 = chunk * p.chunk_blocks, b1 = min(b0 + p.chunk_blocks, p.total_blocks);
+    int queued = 0;
+    for (int base = b0; base < b1; base += 32) {
+      const int b = base + lane;
+      bool live = false;
+      if (b < b1) {
+        const int l = block_light(p, b);
+        const LightArgs& la = p.ll.lights[l];
+        const int lb = b - p.block_base[l];
+        if (p.shadow) {
+          for (int j = 0; j < la.interval && !live; ++j) {
+            const VplData v = load_vpl<BF16>(la.vpls, lb * la.interval + j);
+            live = contributes(v, transfer(v, cx, cy, cz));
+          }
+        } else {  // no indirect shadow: blocks are single VPLs, shadowing 1
+          const VplData v = load_vpl<BF16>(la.vpls, lb);
+          const Transfer t = transfer(v, cx, cy, cz);
+          if (contributes(v, t)) accumulate<NK, KAHAN>(p.ev, acc, comp, kThreads, v, t, 1.0f);
+        }
+      }
+      const uint32_t mask = __ballot_sync(0xffffffffu, live);
+      if (live) queue[queued + __popc(mask & ((1u << lane) - 1u))] = b;
+      queued += __popc(mask);
+      __syncwarp();
+      if (queued >= 32) {
+        trace_block(queue[queued - 32 + lane]);
+        queued -= 32;
+        __syncwarp();
+      }
     }
+    if (lane < queued) trace_block(queue[lane]);
+    __syncwarp();
     // Warp reduction: lane k (< NK*3) ends up holding coefficient k.
     float mine = 0.0f;
 #pragma unroll
@@ -202,7 +174,7 @@ __global__ void __launch_bounds__(kThreads, 8) light_kernel(LightParams p) {
       if (lane == k) mine = v;
     }
     if (p.n_chunks == 1) {
-      if (lane < NK * 3) add_to_entry<NK, BF16>(entry, lane, mine);
+      if (lane < NK * 3) add_to_entry<BF16>(entry, lane, mine);
       continue;
     }
     if (lane < NK * 3) p.scratch[(size_t)u * (NK * 3) + lane] = mine;
@@ -213,10 +185,10 @@ __global__ void __launch_bounds__(kThreads, 8) light_kernel(LightParams p) {
     if (last) {
       __threadfence();
       if (lane < NK * 3) {
-        const volatile float* base = p.scratch + (size_t)cache * p.n_chunks * (NK * 3);
+        const volatile float* sb = p.scratch + (size_t)cache * p.n_chunks * (NK * 3);
         float v = 0.0f;
-        for (int c = 0; c < p.n_chunks; ++c) v += base[c * (NK * 3) + lane];
-        add_to_entry<NK, BF16>(entry, lane, v);
+        for (int c = 0; c < p.n_chunks; ++c) v += sb[c * (NK * 3) + lane];
+        add_to_entry<BF16>(entry, lane, v);
       }
       if (lane == 0) p.tickets[cache] = 0u;
     }

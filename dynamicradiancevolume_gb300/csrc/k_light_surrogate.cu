@@ -20,6 +20,7 @@
 
 #include "drv_device.cuh"
 #include "drv_internal.h"
+#include "light_common.cuh"
 #include "surrogate.cuh"
 #include "voxel_sample.cuh"
 
@@ -115,73 +116,25 @@ __device__ __forceinline__ void hidden_layer(const uint32_t (&in)[2][KSTEPS][4],
   }
 }
 
-template <int NK, bool BF16>
-__device__ __forceinline__ void gather_block(const SurrogateParams& p, float* acc, int b, float cx, float cy,
-                                             float cz, float shadowing);
-
-struct VplData {
-  float px, py, pz, area, fr, fg, fb, nx, ny, nz;
-};
-
-template <bool BF16>
-__device__ __forceinline__ VplData load_vpl(const void* base, int i) {
-  VplData d;
-  if (BF16) {
-    const uint4* q = reinterpret_cast<const uint4*>(static_cast<const DrvVPLBF16*>(base) + i);
-    const uint4 a = __ldg(q), b = __ldg(q + 1);
-    d.px = __uint_as_float(a.x);
-    d.py = __uint_as_float(a.y);
-    d.pz = __uint_as_float(a.z);
-    d.area = __uint_as_float(a.w);
-    d.fr = from_bf16((uint16_t)(b.x & 0xFFFFu));
-    d.fg = from_bf16((uint16_t)(b.x >> 16));
-    d.fb = from_bf16((uint16_t)(b.y & 0xFFFFu));
-    d.nx = from_bf16((uint16_t)(b.y >> 16));
-    d.ny = from_bf16((uint16_t)(b.z & 0xFFFFu));
-    d.nz = from_bf16((uint16_t)(b.z >> 16));
-  } else {
-    const float4* q = reinterpret_cast<const float4*>(static_cast<const DrvVPL*>(base) + i);
-    const float4 a = __ldg(q), bb = __ldg(q + 1), n = __ldg(q + 2);
-    d.fr = a.x;
-    d.fg = a.y;
-    d.fb = a.z;
-    d.area = a.w;
-    d.px = bb.x;
-    d.py = bb.y;
-    d.pz = bb.z;
-    d.nx = n.x;
-    d.ny = n.y;
-    d.nz = n.z;
-  }
-  return d;
+// Shadow block b (global index) -> light index.
+__device__ __forceinline__ int block_light(const SurrogateParams& p, int b) {
+  int l = 0;
+  while (b >= p.block_base[l + 1]) ++l;
+  return l;
 }
 
-// SH gather of all VPLs of shadow block b (global block index) with the given
+// SH gather of the contributing VPLs of shadow block b with the given
 // shadowing; acc is this thread's column of a [NK*3][kThreads] shared array.
 template <int NK, bool BF16>
 __device__ __forceinline__ void gather_block(const SurrogateParams& p, float* acc, int b, float cx, float cy,
                                              float cz, float shadowing) {
-  int l = 0;
-  while (b >= p.block_base[l + 1]) ++l;
+  const int l = block_light(p, b);
   const LightArgs& la = p.ll.lights[l];
   const int lb = b - p.block_base[l];
   for (int j = 0; j < la.interval; ++j) {
     const VplData v = load_vpl<BF16>(la.vpls, lb * la.interval + j);
-    float tx = v.px - cx, ty = v.py - cy, tz = v.pz - cz;
-    const float d2 = tx * tx + ty * ty + tz * tz;
-    const float r = rsqrtf(d2);
-    tx *= r;
-    ty *= r;
-    tz *= r;
-    const float f = sat(-(v.nx * tx + v.ny * ty + v.nz * tz)) * shadowing;
-    const float s = f / (d2 + v.area);
-    const float L[3] = {v.fr * s, v.fg * s, v.fb * s};
-    const float bs[9] = {p.ev[0], -p.ev[1] * ty, p.ev[1] * tz, -p.ev[1] * tx, -p.ev[2] * tx * ty, p.ev[2] * ty * tz,
-                         p.ev[3] * (tz * tz * 3.0f - 1.0f), p.ev[2] * tx * tz, p.ev[4] * (tx * tx - ty * ty)};
-#pragma unroll
-    for (int k = 0; k < NK; ++k)
-#pragma unroll
-      for (int ch = 0; ch < 3; ++ch) acc[(3 * k + ch) * kThreads] += bs[k] * L[ch];
+    const Transfer t = transfer(v, cx, cy, cz);
+    if (contributes(v, t)) accumulate<NK, false>(p.ev, acc, nullptr, kThreads, v, t, shadowing);
   }
 }
 
@@ -191,6 +144,7 @@ struct __align__(16) SurrogateSmem {
   MlpWeights w;
   uint16_t x[kWarps][32 * kLd1];  // per-warp BF16 feature tile, 80-byte rows
   int queue[kWarps][64];          // per-warp re-trace queue
+  int live[kWarps][64];           // per-warp queue of blocks that can contribute
   float acc[NK * 3 * kThreads];   // per-thread SH partial sums, column per thread
 };
 
@@ -238,20 +192,21 @@ __global__ void __launch_bounds__(kThreads) light_surrogate_kernel(SurrogatePara
     float* acc = s_acc + threadIdx.x;
 #pragma unroll
     for (int k = 0; k < NK * 3; ++k) acc[k * kThreads] = 0.0f;
-    int queued = 0;
-    const int b0 = chunk * p.chunk_blocks, b1 = min(b0 + p.chunk_blocks, p.total_blocks);
-    for (int base = b0; base < b1; base += 32) {
-      const int b = base + lane;
-      const bool valid = b < b1;
-      // 1. features -> BF16 tile row `lane`
+    int* live = S.live[warp];
+    int queued = 0, n_live = 0;
+    // Runs the MLP on the n (<= 32) live blocks at live[first ...]: confident
+    // pairs are gathered with the predicted visibility, the others queued for
+    // the cone, which runs once 32 are waiting.
+    auto mlp_batch = [&](int first, int n) {
+      const bool valid = lane < n;
+      const int b = valid ? live[first + lane] : 0;
+      __syncwarp();
       float f[kMlpIn];
-      float4 cone = make_float4(0.f, 0.f, 0.f, 0.f);
       if (valid) {
-        int l = 0;
-        while (b >= p.block_base[l + 1]) ++l;
+        const int l = block_light(p, b);
         const LightArgs& la = p.ll.lights[l];
         const int lb = b - p.block_base[l];
-        cone = __ldg(reinterpret_cast<const float4*>(la.cones) + lb);
+        const float4 cone = __ldg(reinterpret_cast<const float4*>(la.cones) + lb);
         const VplData v = load_vpl<BF16>(la.vpls, lb * la.interval);
         surrogate_features(p.vox, inv_extent, p.vol_min, p.voxel_size, p.max_steps, cx, cy, cz, cone.x, cone.y,
                            cone.z, v.nx, v.ny, v.nz, cone.w, f);
@@ -263,7 +218,6 @@ __global__ void __launch_bounds__(kThreads) light_surrogate_kernel(SurrogatePara
 #pragma unroll
       for (int i = 0; i < kMlpIn / 2; ++i) row[i] = pack_bf16x2(f[2 * i], f[2 * i + 1]);
       __syncwarp();
-      // 2. MLP on tensor cores
       uint32_t a1[2][2][4];
 #pragma unroll
       for (int m = 0; m < 2; ++m)
@@ -287,7 +241,7 @@ __global__ void __launch_bounds__(kThreads) light_surrogate_kernel(SurrogatePara
           mma_bf16(o[1], h1[1][kk], bb0, bb1);
         }
       }
-      // 3. (visibility, confidence) of row `lane`: held by lane 4*(row&7),
+      // (visibility, confidence) of row `lane`: held by lane 4*(row&7),
       // registers 0,1 (rows 0-7 of an m-tile) or 2,3 (rows 8-15).
       const int src = 4 * (lane & 7);
       const float r00 = __shfl_sync(0xffffffffu, o[0][0], src), r01 = __shfl_sync(0xffffffffu, o[0][1], src);
@@ -301,31 +255,51 @@ __global__ void __launch_bounds__(kThreads) light_surrogate_kernel(SurrogatePara
       const float conf = sigmoidf(oc + s_w.b4[1]);
       const bool retrace = valid && !(conf >= p.conf_threshold);
       if (valid && !retrace) gather_block<NK, BF16>(p, acc, b, cx, cy, cz, vis);
-      // 4. queue the uncertain pairs; trace them 32 at a time
       const uint32_t mask = __ballot_sync(0xffffffffu, retrace);
       if (retrace) queue[queued + __popc(mask & ((1u << lane) - 1u))] = b;
       queued += __popc(mask);
       __syncwarp();
       if (queued >= 32) {
         const int qb = queue[queued - 32 + lane];
-        int l = 0;
-        while (qb >= p.block_base[l + 1]) ++l;
+        const int l = block_light(p, qb);
         const float4 c = __ldg(reinterpret_cast<const float4*>(p.ll.lights[l].cones) + (qb - p.block_base[l]));
-        const float s = cone_shadow(p.vox, p.voxel_size, p.max_steps, cx, cy, cz, vx, vy, vz, c.x, c.y, c.z, c.w);
-        gather_block<NK, BF16>(p, acc, qb, cx, cy, cz, s);
+        const float sh = cone_shadow(p.vox, p.voxel_size, p.max_steps, cx, cy, cz, vx, vy, vz, c.x, c.y, c.z, c.w);
+        gather_block<NK, BF16>(p, acc, qb, cx, cy, cz, sh);
         queued -= 32;
         retraced += 32;
         __syncwarp();
       }
+    };
+    const int b0 = chunk * p.chunk_blocks, b1 = min(b0 + p.chunk_blocks, p.total_blocks);
+    for (int base = b0; base < b1; base += 32) {
+      const int b = base + lane;
+      bool is_live = false;
+      if (b < b1) {
+        const int l = block_light(p, b);
+        const LightArgs& la = p.ll.lights[l];
+        const int lb = b - p.block_base[l];
+        for (int j = 0; j < la.interval && !is_live; ++j) {
+          const VplData v = load_vpl<BF16>(la.vpls, lb * la.interval + j);
+          is_live = contributes(v, transfer(v, cx, cy, cz));
+        }
+      }
+      const uint32_t mask = __ballot_sync(0xffffffffu, is_live);
+      if (is_live) live[n_live + __popc(mask & ((1u << lane) - 1u))] = b;
+      n_live += __popc(mask);
+      __syncwarp();
+      if (n_live >= 32) {
+        mlp_batch(n_live - 32, 32);
+        n_live -= 32;
+      }
     }
+    if (n_live > 0) mlp_batch(0, n_live);
     if (queued > 0) {
       if (lane < queued) {
         const int qb = queue[lane];
-        int l = 0;
-        while (qb >= p.block_base[l + 1]) ++l;
+        const int l = block_light(p, qb);
         const float4 c = __ldg(reinterpret_cast<const float4*>(p.ll.lights[l].cones) + (qb - p.block_base[l]));
-        const float s = cone_shadow(p.vox, p.voxel_size, p.max_steps, cx, cy, cz, vx, vy, vz, c.x, c.y, c.z, c.w);
-        gather_block<NK, BF16>(p, acc, qb, cx, cy, cz, s);
+        const float sh = cone_shadow(p.vox, p.voxel_size, p.max_steps, cx, cy, cz, vx, vy, vz, c.x, c.y, c.z, c.w);
+        gather_block<NK, BF16>(p, acc, qb, cx, cy, cz, sh);
       }
       retraced += queued;
       __syncwarp();

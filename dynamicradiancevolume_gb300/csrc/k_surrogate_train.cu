@@ -12,6 +12,7 @@
 
 #include "drv_device.cuh"
 #include "drv_internal.h"
+#include "light_common.cuh"
 #include "surrogate.cuh"
 #include "voxel_sample.cuh"
 
@@ -80,9 +81,37 @@ __global__ void __launch_bounds__(128) pairs_kernel(PairParams p) {
       return;
     }
   } else {
-    const uint64_t h = mix64(p.seed * 0x9E3779B97F4A7C15ull + (uint64_t)i);
-    cache = (uint32_t)(h % count);
-    b = (int)((h >> 32) % (uint64_t)p.total_blocks);
+    // Random pairs that can contribute (positive flux, facing the cache): the
+    // light stage never asks for the visibility of the others.
+    for (int attempt = 0; attempt < 64; ++attempt) {
+      const uint64_t h = mix64(p.seed * 0x9E3779B97F4A7C15ull + (uint64_t)i * 64u + (uint64_t)attempt);
+      cache = (uint32_t)(h % count);
+      b = (int)((h >> 32) % (uint64_t)p.total_blocks);
+      int l = 0;
+      while (b >= p.block_base[l + 1]) ++l;
+      const LightArgs& la = p.ll.lights[l];
+      const int lb = b - p.block_base[l];
+      const float* e = p.entries + (size_t)cache * p.stride_floats;
+      float ex, ey, ez;
+      if (p.bf16) {
+        const uint32_t key = __float_as_uint(e[0]);
+        const int c = (int)(key >> 27);
+        ex = __fadd_rn(__fmul_rn((float)(key & 511u), p.casc_cell[c]), p.casc_min[c][0]);
+        ey = __fadd_rn(__fmul_rn((float)((key >> 9) & 511u), p.casc_cell[c]), p.casc_min[c][1]);
+        ez = __fadd_rn(__fmul_rn((float)((key >> 18) & 511u), p.casc_cell[c]), p.casc_min[c][2]);
+      } else {
+        ex = e[0];
+        ey = e[1];
+        ez = e[2];
+      }
+      bool live = false;
+      for (int j = 0; j < la.interval && !live; ++j) {
+        const VplData v = p.bf16 ? load_vpl<true>(la.vpls, lb * la.interval + j)
+                                 : load_vpl<false>(la.vpls, lb * la.interval + j);
+        live = contributes(v, transfer(v, ex, ey, ez));
+      }
+      if (live) break;
+    }
   }
   int l = 0;
   while (b >= p.block_base[l + 1]) ++l;
