@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="ns_1080p_4096")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--thresholds", type=float, nargs="*", default=[0.5, 0.8],
+                    help="surrogate confidence thresholds to measure")
     return ap.parse_args()
 
 
@@ -204,29 +206,41 @@ def run_reference(args):
 
 
 # ---------------------------------------------------------------- GPU arm
-def run_ours(args):
+def oracle_frame_from(pipe):
+    """FP64 oracle frame from a pipeline's own G-buffer and RSM inputs."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle_py as O
+    w, hf = pipe.hf.workload, pipe.hf
+    depth, n16, alb = (t.cpu().numpy() for t in (pipe.depth, pipe.normal16, pipe.albedo))
+    vp, cones = [], []
+    for l in range(w.n_lights):
+        rsm = tuple(t.cpu().numpy() for t in (pipe.rsm_flux[l], pipe.rsm_normal[l], pipe.rsm_dls[l]))
+        chain = O.rsm_chain(*rsm, w.rsm_read_lod + w.shadow_lod)
+        v, c = O.extract_vpls(hf.lights[l], *chain[w.rsm_read_lod], chain[w.rsm_read_lod + w.shadow_lod][2])
+        vp.append(v)
+        cones.append(c)
+    bits = O.voxelize(hf.boxes, hf.scene.n_boxes, hf.volume, w.voxel_res)
+    mips = O.build_mips(w.voxel_res, bits)
+    cfg = type(hf.config).from_buffer_copy(hf.config)
+    cfg.precision, cfg.visibility = 0, 0
+    st, atlas, pos, count = O.allocate_caches(cfg, hf.volume, hf.frame, depth)
+    sh = O.light_caches(cfg, hf.volume, pos, hf.lights, vp, cones, bits, mips)
+    return O.apply(cfg, hf.volume, hf.frame, depth, n16, 0, alb, atlas, sh)  # 0: RG16I normals
+
+
+def rel_l2(a, b) -> float:
+    import numpy as np
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def measure(pipe, steps, warmup, flush, clocks=None):
+    """Per-stage CUDA-event times of `steps` frames (L2 flushed between them)."""
     import torch
-    import torch.distributed as dist
-    from dynamicradiancevolume_gb300 import pipeline
-
-    ws, rank, local = dist_env()
-    if ws > 1:
-        dist.init_process_group("nccl")
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
-    w = pipeline.WORKLOADS[args.workload]
-    hf = pipeline.host_frame(w)
-    pipe = pipeline.Pipeline(hf, device=str(dev))
-    pipe.raycast_inputs()
-    pipe.frame()
-    pipe.sync()
-    count = pipe.cache_count()
     stream = pipe.stream
-    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MiB > 129 MB L2
+    names = ["rsm+vpl", "voxelize+mips", "allocate", "light", "apply"]
 
-    stage_names = ["rsm+vpl", "voxelize+mips", "allocate", "light", "apply"]
-
-    def staged_frame(ev):
+    def staged(ev):
         ev[0].record(stream)
         pipe.prepare_and_extract()
         ev[1].record(stream)
@@ -239,29 +253,98 @@ def run_ours(args):
         pipe.apply()
         ev[5].record(stream)
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         with torch.cuda.stream(stream):
             flush.zero_()
-        staged_frame([torch.cuda.Event(enable_timing=True) for _ in range(6)])
+        staged([torch.cuda.Event(enable_timing=True) for _ in range(6)])
     pipe.sync()
+    torch.cuda.synchronize(pipe.device)
+    events = []
+    for _ in range(steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()  # L2 flush between timed steps (outside the events)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
+        staged(ev)
+        events.append(ev)
+    torch.cuda.synchronize(pipe.device)
+    pipe.sync()
+    stage_ms = {n: statistics.mean(e[i].elapsed_time(e[i + 1]) for e in events) for i, n in enumerate(names)}
+    frame_ms = statistics.mean(e[0].elapsed_time(e[5]) for e in events)
+    return frame_ms, stage_ms
+
+
+def run_ours(args):
+    import ctypes as C
+    import torch
+    import torch.distributed as dist
+    from dynamicradiancevolume_gb300 import abi, pipeline, surrogate
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    w = pipeline.WORKLOADS[args.workload]
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MiB > 129 MB L2
     if ws > 1:
         dist.barrier()
-    torch.cuda.synchronize(dev)
-    events = []
+
+    # ---- variants: plain FP32 cone, BF16 precision, surrogate visibility
+    variants = {}
+    weights = surrogate.load_params() if surrogate.DEFAULT_WEIGHTS.with_suffix(".bin").exists() else None
+    plan = [("plain_fp32", w, None), ("precision_bf16", pipeline.scaled(w, precision=abi.PRECISION_BF16), None)]
+    if weights is not None:
+        for thr in args.thresholds:
+            plan.append((f"surrogate_t{thr:g}", pipeline.scaled(w, visibility=abi.VISIBILITY_SURROGATE), thr))
+    reference = None
+    pipes = {}
     with ClockSampler(local) as clk:
-        for _ in range(args.steps):
-            with torch.cuda.stream(stream):
-                flush.zero_()  # L2 flush between timed steps (not inside the events)
-            ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
-            staged_frame(ev)
-            events.append(ev)
-        torch.cuda.synchronize(dev)
-    pipe.sync()
-    stage_ms = {n: statistics.mean(e[i].elapsed_time(e[i + 1]) for e in events) for i, n in enumerate(stage_names)}
-    frame_ms = statistics.mean(e[0].elapsed_time(e[5]) for e in events)
-    light_ms = stage_ms["light"]
+        for name, wv, thr in plan:
+            hf = pipeline.host_frame(wv)
+            if thr is not None:
+                hf.config.surrogate_conf_threshold = thr
+            pipe = pipeline.Pipeline(hf, device=str(dev))
+            if thr is not None:
+                surrogate.upload(pipe, weights)
+            pipe.raycast_inputs()
+            pipe.frame()
+            pipe.sync()
+            count = pipe.cache_count()
+            frame_ms, stage_ms = measure(pipe, args.steps, args.warmup, flush)
+            pipe.frame()
+            pipe.sync()
+            info = {"frame_ms": frame_ms, "stage_ms": stage_ms, "caches": count,
+                    "caches_per_s": count / (frame_ms / 1e3),
+                    "caches_lit_per_s_light_stage": count / (stage_ms["light"] / 1e3)}
+            if thr is not None:
+                ev, fb = C.c_uint32(), C.c_uint32()
+                pipe.lib.drv_get_surrogate_stats(pipe.ctx, C.byref(ev), C.byref(fb))
+                blocks = sum(pipe.buffers().n_vpls[l] // hf.lights[l].indirect_shadow_sample_interval
+                             for l in range(w.n_lights))
+                info["threshold"] = thr
+                info["shadow_blocks"] = blocks
+                info["evaluated_pairs"] = ev.value
+                info["retraced_pairs"] = fb.value
+                info["evaluated_share_of_pairs"] = ev.value / max(count * blocks, 1)
+                info["retraced_share_of_evaluated"] = fb.value / max(ev.value, 1)
+            out = pipe.out.cpu().numpy()
+            if reference is None and rank == 0:
+                reference = oracle_frame_from(pipe)
+            if rank == 0:
+                info["rel_l2_vs_fp64"] = rel_l2(out, reference)
+            variants[name] = info
+            pipes[name] = pipe
+    clocks = clk.summary()
+    ok = {n: v for n, v in variants.items() if v.get("rel_l2_vs_fp64", 1.0) <= 0.01}
+    head = max(ok, key=lambda n: ok[n]["caches_per_s"]) if ok else "plain_fp32"
+    pipe = pipes[head]
+    hv = variants[head]
+    for n, p in pipes.items():
+        if n != head:
+            p.close()
 
     # ---- e2e through drv_frame with host buffers (pinned), H2D + D2H inside the region
+    stream = pipe.stream
     host_in = [t.cpu().pin_memory() for t in (pipe.depth, pipe.normal16, pipe.albedo)]
     host_rsm = [[t.cpu().pin_memory() for t in (pipe.rsm_flux[l], pipe.rsm_normal[l], pipe.rsm_dls[l])]
                 for l in range(w.n_lights)]
@@ -298,9 +381,10 @@ def run_ours(args):
         e_times.append(a.elapsed_time(b))
     pipe.sync()
     e2e_ms = statistics.mean(e_times)
+    count = hv["caches"]
 
     # ---- max over ranks (replicas)
-    vals = torch.tensor([frame_ms, e2e_ms, float(count)], dtype=torch.float64, device=dev)
+    vals = torch.tensor([hv["frame_ms"], e2e_ms, float(count)], dtype=torch.float64, device=dev)
     if ws > 1:
         mx = vals.clone()
         dist.all_reduce(mx, op=dist.ReduceOp.MAX)
@@ -308,32 +392,42 @@ def run_ours(args):
         dist.all_reduce(tot, op=dist.ReduceOp.SUM)
         frame_ms_all, e2e_ms_all, caches_all = mx[0].item(), mx[1].item(), tot[2].item()
     else:
-        frame_ms_all, e2e_ms_all, caches_all = frame_ms, e2e_ms, float(count)
+        frame_ms_all, e2e_ms_all, caches_all = hv["frame_ms"], e2e_ms, float(count)
 
     pk = peaks()
-    clocks = clk.summary()
-    # Roofline of the dominant kernel (cache lighting): FP32 SH gather flops
-    # per launch over the measured launch time. The cone-traced shadow adds
-    # voxel-fetch work that this count leaves out.
+    light_ms = hv["stage_ms"]["light"]
     pairs = count * w.n_vpls
+    if head.startswith("surrogate"):
+        # MLP on tensor cores: 2*(32*64 + 64*64 + 64*64 + 64*2) flop per evaluated pair (the
+        # pairs that can contribute; the others need no visibility).
+        evaluated = hv["evaluated_pairs"]
+        mlp_tflops = evaluated * 20736 / (light_ms / 1e3) / 1e12
+        roofline = {"bound": "tensor", "kernel": "light_surrogate_kernel", "achieved": mlp_tflops,
+                    "note": "MLP flops of the evaluated pairs over the whole light stage (cone fallbacks included)",
+                    "peak": pk["bf16_tflops"], "unit": "TFLOP/s", "frac": mlp_tflops / pk["bf16_tflops"],
+                    "traffic": None, "peak_source": pk["source"]}
+    else:
+        light_bytes = count * (16 + (128 if w.sh_order == 2 else 64) * 2) + w.n_vpls * 64
+        roofline = {"bound": "hbm", "kernel": "light_kernel", "achieved": light_bytes / (light_ms / 1e3) / 1e9,
+                    "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": light_bytes / (light_ms / 1e3) / 1e9 / pk["hbm_gbs"],
+                    "traffic": None, "peak_source": pk["source"],
+                    "note": "the cone-traced light stage is FP32/L1-bound, not HBM-bound; see fp32_pipe"}
     light_flop = pairs * sh_flops_per_pair(w.sh_order)
-    light_bytes = count * (16 + (128 if w.sh_order == 2 else 64) * 2) + w.n_vpls * 64
     fp32_peak = 152 * 128 * 2 * (clocks["sm_mhz"] or pk["sm_max_mhz"]) * 1e6 / 1e12
     line = {
         "metric": METRIC, "value": caches_all / (frame_ms_all / 1e3), "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": frame_ms_all, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural box room)",
-        "config": {"workload": w.name, "width": w.width, "height": w.height, "n_vpls": w.n_vpls,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16" if head != "plain_fp32" else "f32",
+        "data": "synthetic (seeded procedural box room)",
+        "config": {"workload": w.name, "variant": head, "width": w.width, "height": w.height, "n_vpls": w.n_vpls,
                    "n_lights": w.n_lights, "voxel_res": w.voxel_res, "cascades": f"{w.n_cascades}x{w.cav_res}^3",
                    "sh_order": w.sh_order, "cone_steps": w.max_cone_steps, "caches": count,
-                   "visibility": "cone", "precision": "fp32", "l2": "flushed between steps (256 MiB write)"},
-        "stage_ms": stage_ms,
-        "caches_lit_per_s_light_stage": count / (light_ms / 1e3),
-        "roofline": {"bound": "hbm", "kernel": "light_kernel", "achieved": light_bytes / (light_ms / 1e3) / 1e9,
-                     "peak": pk["hbm_gbs"], "unit": "GB/s",
-                     "frac": light_bytes / (light_ms / 1e3) / 1e9 / pk["hbm_gbs"], "traffic": None,
-                     "peak_source": pk["source"],
-                     "note": "the cone-traced light stage is FP32/L1-bound, not HBM-bound; see fp32_pipe"},
+                   "l2": "flushed between steps (256 MiB write)"},
+        "rel_l2_vs_fp64": hv.get("rel_l2_vs_fp64"),
+        "stage_ms": hv["stage_ms"],
+        "caches_lit_per_s_light_stage": hv["caches_lit_per_s_light_stage"],
+        "variants": variants,
+        "roofline": roofline,
         "fp32_pipe": {"kernel": "light_kernel", "achieved_tflops": light_flop / (light_ms / 1e3) / 1e12,
                       "peak_tflops": fp32_peak, "frac": light_flop / (light_ms / 1e3) / 1e12 / fp32_peak,
                       "peak_source": "152 SMs x 128 FP32 lanes x 2 x median SM clock (derived, not measured)"},
@@ -344,7 +438,7 @@ def run_ours(args):
     }
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        caches, t, note = cpu_frame(w, hf, threads, cache_sample=256)
+        caches, t, note = cpu_frame(w, pipeline.host_frame(w), threads, cache_sample=256)
         line["cpu_baseline"] = {"value": caches / t, "unit": UNIT, "cores": threads, "kind": "port", "sample": note}
     if rank == 0:
         print(json.dumps(line), flush=True)

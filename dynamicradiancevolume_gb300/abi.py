@@ -166,6 +166,7 @@ PROTOTYPES = {
                                            C.c_float, VP, VP]),
     "drv_surrogate_eval": (C.c_int, [VP, VP, C.c_int32, VP]),
     "drv_get_surrogate_fallbacks": (C.c_int, [VP, P(C.c_uint32)]),
+    "drv_get_surrogate_stats": (C.c_int, [VP, P(C.c_uint32), P(C.c_uint32)]),
     "drv_light_caches_static_scratch": (C.c_int, [P(DrvConfig), P(DrvVolumeInfo), P(VP), P(VP), P(C.c_int32),
                                                   P(C.c_int32), C.c_int32, VP, VP, VP, VP, VP]),
 }

@@ -383,7 +383,7 @@ drv_status drv_light_caches(DrvContext* ctx, const DrvSpotLight* lights, int32_t
   }
   if (ctx->cfg.visibility == DRV_VISIBILITY_SURROGATE) {
     if (!ctx->sur_ready) return fail(ctx, DRV_ERR_INVALID_ARG, "surrogate visibility needs drv_set_surrogate_params");
-    DRV_TRY_CUDA(ctx, cudaMemsetAsync(ctx->sur_fallbacks, 0, 4, ctx->s()));
+    DRV_TRY_CUDA(ctx, cudaMemsetAsync(ctx->sur_fallbacks, 0, 8, ctx->s()));
     return cuda_check(ctx, drv::launch_light_surrogate(ctx->s(), ctx->cfg, *vol, ll, ctx->counter, ctx->entries,
                                                        ctx->entry_stride, ctx->vox_corners, ctx->mips, ctx->mip_offset,
                                                        ctx->light_scratch, ctx->light_tickets, ctx->sur_weights,
@@ -445,6 +445,16 @@ drv_status drv_get_surrogate_fallbacks(DrvContext* ctx, uint32_t* out) {
   if (!ctx || !out) return DRV_ERR_INVALID_ARG;
   DRV_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->s()));
   DRV_TRY_CUDA(ctx, cudaMemcpy(out, ctx->sur_fallbacks, 4, cudaMemcpyDeviceToHost));
+  return DRV_OK;
+}
+
+drv_status drv_get_surrogate_stats(DrvContext* ctx, uint32_t* evaluated, uint32_t* retraced) {
+  if (!ctx || !evaluated || !retraced) return DRV_ERR_INVALID_ARG;
+  uint32_t v[2];
+  DRV_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->s()));
+  DRV_TRY_CUDA(ctx, cudaMemcpy(v, ctx->sur_fallbacks, 8, cudaMemcpyDeviceToHost));
+  *retraced = v[0];
+  *evaluated = v[1];
   return DRV_OK;
 }
 

@@ -62,7 +62,7 @@ struct SurrogateParams {
   uint32_t* tickets;
   const MlpWeights* weights;
   float conf_threshold;
-  uint32_t* fallback_count;  // optional: number of re-traced pairs
+  uint32_t* fallback_count;  // optional: [0] re-traced pairs, [1] pairs the MLP evaluated
   float ev[5];
 };
 
@@ -170,7 +170,7 @@ __global__ void __launch_bounds__(kThreads) light_surrogate_kernel(SurrogatePara
   uint16_t* xt = s_x[warp];
   int* queue = s_queue[warp];
   const float inv_extent = 1.0f / (p.voxel_size * p.vox.N);
-  uint32_t retraced = 0;
+  uint32_t retraced = 0, evaluated = 0;
   for (uint32_t u = blockIdx.x * kWarps + warp; u < n_units; u += warps) {
     const uint32_t cache = u / (uint32_t)p.n_chunks;
     const int chunk = (int)(u % (uint32_t)p.n_chunks);
@@ -199,6 +199,7 @@ __global__ void __launch_bounds__(kThreads) light_surrogate_kernel(SurrogatePara
     // the cone, which runs once 32 are waiting.
     auto mlp_batch = [&](int first, int n) {
       const bool valid = lane < n;
+      evaluated += n;
       const int b = valid ? live[first + lane] : 0;
       __syncwarp();
       float f[kMlpIn];
@@ -341,7 +342,10 @@ __global__ void __launch_bounds__(kThreads) light_surrogate_kernel(SurrogatePara
       if (lane == 0) p.tickets[cache] = 0u;
     }
   }
-  if (p.fallback_count && lane == 0 && retraced) atomicAdd(p.fallback_count, retraced);
+  if (p.fallback_count && lane == 0) {
+    if (retraced) atomicAdd(p.fallback_count, retraced);
+    if (evaluated) atomicAdd(p.fallback_count + 1, evaluated);
+  }
 }
 
 // FP32 master parameters -> padded BF16 inference layout.

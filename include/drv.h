@@ -418,6 +418,10 @@ drv_status drv_surrogate_train_step(const float* features, const float* targets,
 drv_status drv_surrogate_eval(DrvContext* ctx, const float* features, int32_t n, float* out);
 /* Pairs re-traced with the cone by the last surrogate light stage. Synchronises. */
 drv_status drv_get_surrogate_fallbacks(DrvContext* ctx, uint32_t* out);
+/* Pairs the last surrogate light stage evaluated with the MLP (the
+ * (cache, shadow block) pairs that can contribute) and of those re-traced
+ * with the cone. Synchronises. */
+drv_status drv_get_surrogate_stats(DrvContext* ctx, uint32_t* evaluated, uint32_t* retraced);
 
 /* ---- allocation-free light stage ------------------------------------------
  * No counterpart in the reference: the reference renderer always owns its GL
