@@ -131,14 +131,18 @@ def sh_flops_per_pair(sh_order: int) -> int:
     return 51 if sh_order == 1 else 94
 
 
-def kernel_launches_per_frame(w) -> int:
+def kernel_launches_per_frame(w, surrogate: bool = False) -> int:
     # per light: (read_lod + shadow_lod) downsample passes + 1 extraction;
     # voxelize 1 + mips (1, +1 tail above 32^3) + corner grid 1; allocate 1;
-    # light 1; apply 1.
+    # light: cull + cone + gather (+ MLP with the surrogate), or 1 without
+    # indirect shadow; apply 1.
     n = w.n_lights * (w.rsm_read_lod + w.shadow_lod + 1)
     if w.indirect_shadow:
         n += 1 + (2 if w.voxel_res > 32 else 1) + 1
-    return n + 3
+        n += 4 if surrogate else 3
+    else:
+        n += 1
+    return n + 2
 
 
 # ---------------------------------------------------------------- CPU arm
@@ -433,7 +437,7 @@ def run_ours(args):
                       "peak_source": "152 SMs x 128 FP32 lanes x 2 x median SM clock (derived, not measured)"},
         "e2e": {"value": caches_all / (e2e_ms_all / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms_all},
-        "gpu_launches": kernel_launches_per_frame(w) * args.steps,
+        "gpu_launches": kernel_launches_per_frame(w, head.startswith("surrogate")) * args.steps,
         "clocks": clocks,
     }
     if rank == 0 and not args.no_cpu_baseline:

@@ -120,9 +120,16 @@ class DrvBuffers(C.Structure):
                 ("cones", C.c_void_p * MAX_LIGHTS), ("n_vpls", C.c_int32 * MAX_LIGHTS), ("n_lights", C.c_int32)]
 
 
+class DrvTuning(C.Structure):
+    _fields_ = [("light_path", C.c_int32), ("pair_capacity", C.c_uint32), ("cone_ctas_per_sm", C.c_int32),
+                ("gather_ctas_per_sm", C.c_int32), ("reserved", C.c_int32 * 4)]
+
+
+LIGHT_PATH_AUTO, LIGHT_PATH_SINGLE, LIGHT_PATH_SPLIT = 0, 1, 2
+
 STRUCT_ORDER = [DrvConfig, DrvCascade, DrvVolumeInfo, DrvPerFrame, DrvSpotLight, DrvLightDesc, DrvCamera, DrvBox,
                 DrvScene, DrvGBufferView, DrvGBufferOut, DrvRSMView, DrvRSMOut, DrvVPL, DrvShadowCone,
-                DrvCacheCounter, DrvBuffers]
+                DrvCacheCounter, DrvBuffers, DrvTuning]
 
 P = C.POINTER
 VP = C.c_void_p
@@ -167,6 +174,8 @@ PROTOTYPES = {
     "drv_surrogate_eval": (C.c_int, [VP, VP, C.c_int32, VP]),
     "drv_get_surrogate_fallbacks": (C.c_int, [VP, P(C.c_uint32)]),
     "drv_get_surrogate_stats": (C.c_int, [VP, P(C.c_uint32), P(C.c_uint32)]),
+    "drv_set_tuning": (C.c_int, [VP, P(DrvTuning)]),
+    "drv_get_tuning": (C.c_int, [VP, P(DrvTuning)]),
     "drv_light_caches_static_scratch": (C.c_int, [P(DrvConfig), P(DrvVolumeInfo), P(VP), P(VP), P(C.c_int32),
                                                   P(C.c_int32), C.c_int32, VP, VP, VP, VP, VP]),
 }

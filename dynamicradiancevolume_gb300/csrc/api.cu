@@ -3,6 +3,7 @@
 // Renderer::Draw (renderer.cpp:539-594). Every entry point validates its
 // arguments, enqueues work on the context stream and returns a drv_status; no
 // exception crosses the ABI.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -50,7 +51,7 @@ void release(Context* c) {
   cudaFree(c->light_scratch);
   cudaFree(c->light_tickets);
   cudaFree(c->sur_weights);
-  cudaFree(c->sur_fallbacks);
+  cudaFree(c->pair_mem);
   for (int l = 0; l < DRV_MAX_LIGHTS; ++l) {
     for (int k = 1; k < drv::kMaxRsmLevels; ++k) {
       cudaFree(c->rsm[l].flux[k]);
@@ -103,7 +104,7 @@ int drv_struct_sizes(uint32_t* out, int capacity) {
                         sizeof(DrvSpotLight),  sizeof(DrvLightDesc),  sizeof(DrvCamera),     sizeof(DrvBox),
                         sizeof(DrvScene),      sizeof(DrvGBufferView), sizeof(DrvGBufferOut), sizeof(DrvRSMView),
                         sizeof(DrvRSMOut),     sizeof(DrvVPL),        sizeof(DrvShadowCone), sizeof(DrvCacheCounter),
-                        sizeof(DrvBuffers)};
+                        sizeof(DrvBuffers),    sizeof(DrvTuning)};
   int n = (int)(sizeof(s) / sizeof(s[0]));
   if (!out) return n;
   int k = capacity < n ? capacity : n;
@@ -155,10 +156,12 @@ drv_status drv_create(const DrvConfig* cfg, DrvContext** out) {
   if ((e = cudaMalloc(&c->vox_corners, (size_t)N * N * N)) != cudaSuccess) return bail(e);
   // Light-stage chunk partials and per-cache tickets (tickets are reset by the
   // kernel that consumes them, so they are zeroed once here).
-  if ((e = cudaMalloc(&c->light_scratch, (size_t)cfg->max_caches * drv::kMaxLightChunks * 27 * 4)) != cudaSuccess)
+  if ((e = cudaMalloc(&c->light_scratch, (size_t)cfg->max_caches * drv::kMaxLightChunks * (cfg->sh_order == 2 ? 27 : 12) * 4)) !=
+      cudaSuccess)
     return bail(e);
-  if ((e = cudaMalloc(&c->light_tickets, (size_t)cfg->max_caches * 4)) != cudaSuccess) return bail(e);
-  if ((e = cudaMemset(c->light_tickets, 0, (size_t)cfg->max_caches * 4)) != cudaSuccess) return bail(e);
+  // Tickets, then the two words of the dynamic unit counter.
+  if ((e = cudaMalloc(&c->light_tickets, ((size_t)cfg->max_caches + 2) * 4)) != cudaSuccess) return bail(e);
+  if ((e = cudaMemset(c->light_tickets, 0, ((size_t)cfg->max_caches + 2) * 4)) != cudaSuccess) return bail(e);
   // RSM chains (levels below the caller's render-resolution level) and VPLs.
   const int R = cfg->max_rsm_resolution;
   for (int l = 0; l < cfg->max_lights; ++l) {
@@ -172,8 +175,24 @@ drv_status drv_create(const DrvConfig* cfg, DrvContext** out) {
     if ((e = cudaMalloc(&c->cones[l], (size_t)R * R * sizeof(DrvShadowCone))) != cudaSuccess) return bail(e);
   }
   if ((e = cudaMalloc(&c->sur_weights, drv::surrogate_weights_bytes())) != cudaSuccess) return bail(e);
-  if ((e = cudaMalloc(&c->sur_fallbacks, 16)) != cudaSuccess) return bail(e);
-  if ((e = cudaMemset(c->sur_fallbacks, 0, 16)) != cudaSuccess) return bail(e);
+  // Pair list of the split light stage: room for 64 contributing shadow
+  // blocks per cache on average (clamped to [2^20, 2^25] pairs, 20 B each);
+  // caches beyond a full list are traced by the gather itself.
+  {
+    const uint64_t cap = std::min<uint64_t>(std::max<uint64_t>((uint64_t)cfg->max_caches * 64u, 1u << 20), 1u << 25);
+    const size_t bytes = (size_t)cap * 20 + (size_t)cfg->max_caches * 8 + 32;
+    if ((e = cudaMalloc(&c->pair_mem, bytes)) != cudaSuccess) return bail(e);
+    if ((e = cudaMemset(c->pair_mem, 0, bytes)) != cudaSuccess) return bail(e);
+    uint32_t* w = static_cast<uint32_t*>(c->pair_mem);
+    c->pairs.cache = w;
+    c->pairs.block = w + cap;
+    c->pairs.shadow = reinterpret_cast<float*>(w + 2 * cap);
+    c->pairs.order = w + 3 * cap;
+    c->pairs.retrace = w + 4 * cap;
+    c->pairs.info = w + 5 * cap;
+    c->pairs.counters = w + 5 * cap + 2 * (size_t)cfg->max_caches;
+    c->pairs.cap = (uint32_t)cap;
+  }
   c->box_capacity = 512;
   if ((e = cudaMallocHost(&c->h_boxes, c->box_capacity * sizeof(DrvBox))) != cudaSuccess) return bail(e);
   if ((e = cudaMalloc(&c->d_boxes, c->box_capacity * sizeof(DrvBox))) != cudaSuccess) return bail(e);
@@ -381,18 +400,31 @@ drv_status drv_light_caches(DrvContext* ctx, const DrvSpotLight* lights, int32_t
     ll.lights[l].n_vpls = ctx->n_vpls[l];
     ll.lights[l].interval = ctx->interval[l];
   }
-  if (ctx->cfg.visibility == DRV_VISIBILITY_SURROGATE) {
-    if (!ctx->sur_ready) return fail(ctx, DRV_ERR_INVALID_ARG, "surrogate visibility needs drv_set_surrogate_params");
-    DRV_TRY_CUDA(ctx, cudaMemsetAsync(ctx->sur_fallbacks, 0, 8, ctx->s()));
-    return cuda_check(ctx, drv::launch_light_surrogate(ctx->s(), ctx->cfg, *vol, ll, ctx->counter, ctx->entries,
-                                                       ctx->entry_stride, ctx->vox_corners, ctx->mips, ctx->mip_offset,
-                                                       ctx->light_scratch, ctx->light_tickets, ctx->sur_weights,
-                                                       ctx->sur_fallbacks, ctx->num_sms),
-                      "light_caches (surrogate)");
+  const drv::LightScratch scratch{ctx->light_scratch, ctx->light_tickets, ctx->light_tickets + ctx->cfg.max_caches,
+                                  drv::kMaxLightChunks};
+  const bool surrogate = ctx->cfg.visibility == DRV_VISIBILITY_SURROGATE && ctx->cfg.indirect_shadow;
+  if (surrogate && !ctx->sur_ready)
+    return fail(ctx, DRV_ERR_INVALID_ARG, "surrogate visibility needs drv_set_surrogate_params");
+  const bool split = ctx->tuning.light_path != DRV_LIGHT_PATH_SINGLE && drv::light_split_supported(ctx->cfg, ll);
+  if (split) {
+    drv::PairList pairs = ctx->pairs;
+    if (ctx->tuning.pair_capacity) pairs.cap = std::min(pairs.cap, ctx->tuning.pair_capacity);
+    return cuda_check(ctx, drv::launch_light_split(ctx->s(), ctx->cfg, *vol, ll, ctx->counter, ctx->entries,
+                                                   ctx->entry_stride, ctx->vox_corners, ctx->mips, ctx->mip_offset,
+                                                   pairs, surrogate ? ctx->sur_weights : nullptr,
+                                                   ctx->tuning.cone_ctas_per_sm, ctx->tuning.gather_ctas_per_sm,
+                                                   ctx->num_sms),
+                      "light_caches");
   }
+  if (surrogate && ctx->tuning.light_path == DRV_LIGHT_PATH_SINGLE)
+    return fail(ctx, DRV_ERR_INVALID_ARG, "surrogate visibility runs on the split light stage");
+  long blocks = 0;
+  for (int l = 0; l < ll.n_lights; ++l) blocks += ll.lights[l].n_vpls / ll.lights[l].interval;
+  if (surrogate && blocks > drv::kMaxSplitBlocks)
+    return fail(ctx, DRV_ERR_INVALID_ARG, "surrogate visibility supports at most 65536 shadow blocks per frame");
   return cuda_check(ctx, drv::launch_light_caches(ctx->s(), ctx->cfg, *vol, ll, ctx->counter, ctx->entries,
                                                   ctx->entry_stride, ctx->vox_corners, ctx->mips, ctx->mip_offset,
-                                                  ctx->light_scratch, ctx->light_tickets, ctx->num_sms),
+                                                  scratch, ctx->num_sms),
                     "light_caches");
 }
 
@@ -444,17 +476,34 @@ drv_status drv_surrogate_eval(DrvContext* ctx, const float* features, int32_t n,
 drv_status drv_get_surrogate_fallbacks(DrvContext* ctx, uint32_t* out) {
   if (!ctx || !out) return DRV_ERR_INVALID_ARG;
   DRV_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->s()));
-  DRV_TRY_CUDA(ctx, cudaMemcpy(out, ctx->sur_fallbacks, 4, cudaMemcpyDeviceToHost));
+  uint32_t v[2];
+  DRV_TRY_CUDA(ctx, cudaMemcpy(v, ctx->pairs.counters + 3, 8, cudaMemcpyDeviceToHost));
+  *out = v[0] + v[1];
+  return DRV_OK;
+}
+
+drv_status drv_set_tuning(DrvContext* ctx, const DrvTuning* t) {
+  if (!ctx || !t) return DRV_ERR_INVALID_ARG;
+  if (t->light_path < DRV_LIGHT_PATH_AUTO || t->light_path > DRV_LIGHT_PATH_SPLIT || t->cone_ctas_per_sm < 0 ||
+      t->gather_ctas_per_sm < 0 || t->cone_ctas_per_sm > 32 || t->gather_ctas_per_sm > 32)
+    return fail(ctx, DRV_ERR_INVALID_ARG, "bad tuning");
+  ctx->tuning = *t;
+  return DRV_OK;
+}
+
+drv_status drv_get_tuning(DrvContext* ctx, DrvTuning* t) {
+  if (!ctx || !t) return DRV_ERR_INVALID_ARG;
+  *t = ctx->tuning;
   return DRV_OK;
 }
 
 drv_status drv_get_surrogate_stats(DrvContext* ctx, uint32_t* evaluated, uint32_t* retraced) {
   if (!ctx || !evaluated || !retraced) return DRV_ERR_INVALID_ARG;
-  uint32_t v[2];
+  uint32_t v[3];
   DRV_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->s()));
-  DRV_TRY_CUDA(ctx, cudaMemcpy(v, ctx->sur_fallbacks, 8, cudaMemcpyDeviceToHost));
-  *retraced = v[0];
-  *evaluated = v[1];
+  DRV_TRY_CUDA(ctx, cudaMemcpy(v, ctx->pairs.counters + 3, 12, cudaMemcpyDeviceToHost));
+  *retraced = v[0] + v[1];
+  *evaluated = v[2];
   return DRV_OK;
 }
 

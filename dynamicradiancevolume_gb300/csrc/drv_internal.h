@@ -12,7 +12,8 @@ namespace drv {
 
 constexpr int kMaxVoxelLevels = 16;
 constexpr int kMaxRsmLevels = 16;
-constexpr int kMaxLightChunks = 8;  // VPL-block chunks per cache in the light stage
+constexpr int kMaxLightChunks = 32;       // VPL-block chunks per cache in the light stage
+constexpr int kLightChunkMinBlocks = 128;  // shadow blocks per chunk, at least
 
 struct RsmChain {
   int res0 = 0;      // render resolution
@@ -33,6 +34,41 @@ struct LightArgs {
 struct LightLaunch {
   LightArgs lights[DRV_MAX_LIGHTS];
   int n_lights;
+};
+
+// Device scratch of the light stage. partials: [max_caches * max_chunks][27]
+// chunk sums; tickets: one per cache; work: {next unit, retired CTAs}. Tickets
+// and work are zero between launches (each launch leaves them zero).
+struct LightScratch {
+  float* partials;
+  uint32_t* tickets;
+  uint32_t* work;
+  int max_chunks;
+};
+
+// Compacted (cache, shadow block) pairs that can contribute, in the split
+// light stage. Pair i: cache[i], block[i] (kNoPair: unused slot), shadow[i].
+// info[c] = {first pair of cache c, pair count} (count kPairOverflow: the
+// list was full, the gather traces that cache's cones itself).
+// order and retrace list pair indices in the order their cones are traced:
+// narrow cones (every sample on voxel level 0) from the front, wide cones
+// from the back, so that a warp's lanes take the same sampling path.
+// counters (zeroed before each light stage): [0] pairs claimed, [1] narrow
+// and [2] wide cones in order, [3] narrow and [4] wide cones in retrace (the
+// pairs the surrogate is not confident about), [5] pairs the surrogate
+// evaluated.
+constexpr uint32_t kNoPair = 0xFFFFFFFFu;
+constexpr uint32_t kPairOverflow = 0xFFFFFFFFu;
+constexpr int kMaxSplitBlocks = 65536;  // shadow blocks per frame the split stage handles
+struct PairList {
+  uint32_t* cache;
+  uint32_t* block;
+  float* shadow;
+  uint32_t* order;
+  uint32_t* retrace;
+  uint32_t* info;
+  uint32_t* counters;
+  uint32_t cap;
 };
 
 // Ray frame of a pinhole camera: direction = normalize(fwd + nx*right + ny*up).
@@ -83,14 +119,17 @@ struct Context {
   // Light-stage partial sums: [max_caches * kMaxLightChunks][27] and a ticket per cache.
   float* light_scratch = nullptr;
   uint32_t* light_tickets = nullptr;
-  // Visibility surrogate: packed BF16 inference weights + re-trace counter.
+  // Pair list of the split light stage (one allocation, carved up).
+  void* pair_mem = nullptr;
+  PairList pairs{};
+  DrvTuning tuning{};
+  // Visibility surrogate: packed BF16 inference weights.
   void* sur_weights = nullptr;
-  uint32_t* sur_fallbacks = nullptr;
   bool sur_ready = false;
   DrvVolumeInfo last_volume{};  // volume of the last drv_allocate_caches (cache positions refer to it)
 };
 
-int light_chunks(int total_blocks);
+int light_chunks(int total_blocks, int max_chunks);
 
 RayFrame make_ray_frame(const float pos[3], const float dir[3], const float up[3], double tan_x, double tan_y);
 
@@ -112,8 +151,16 @@ cudaError_t launch_allocate(cudaStream_t s, const DrvConfig& cfg, const DrvVolum
                             DrvCacheCounter* counter, uint32_t* ticket, uint32_t* err);
 cudaError_t launch_light_caches(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const LightLaunch& ll,
                                 const DrvCacheCounter* counter, void* entries, uint32_t entry_stride,
-                                const uint8_t* corners, const void* mips, const size_t* mip_offsets, float* scratch,
-                                uint32_t* tickets, int num_sms);
+                                const uint8_t* corners, const void* mips, const size_t* mip_offsets,
+                                const LightScratch& scratch, int num_sms);
+// Split light stage: cull -> (cones | surrogate MLP + cones of the
+// unconfident pairs) -> gather. weights == nullptr: plain cones.
+bool light_split_supported(const DrvConfig& cfg, const LightLaunch& ll);
+cudaError_t launch_light_split(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const LightLaunch& ll,
+                               const DrvCacheCounter* counter, void* entries, uint32_t entry_stride,
+                               const uint8_t* corners, const void* mips, const size_t* mip_offsets,
+                               const PairList& pairs, const void* weights, int cone_ctas_per_sm,
+                               int gather_ctas_per_sm, int num_sms);
 cudaError_t launch_apply(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const DrvPerFrame& f,
                          const DrvGBufferView& g, const uint32_t* atlas, const void* entries, uint32_t entry_stride,
                          const DrvCacheCounter* counter, float* out_rgb);
@@ -130,10 +177,6 @@ cudaError_t launch_surrogate_pairs(cudaStream_t s, const DrvConfig& cfg, const D
 cudaError_t launch_surrogate_train_step(cudaStream_t s, const float* X, const float* Y, int n, float* params,
                                         float* m, float* v, float* scratch, int step, float lr, float conf_tau,
                                         float weight_decay, float* loss_out);
-cudaError_t launch_light_surrogate(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol,
-                                   const LightLaunch& ll, const DrvCacheCounter* counter, void* entries,
-                                   uint32_t entry_stride, const uint8_t* corners, const void* mips,
-                                   const size_t* mip_offsets, float* scratch, uint32_t* tickets, const void* weights,
-                                   uint32_t* fallback_count, int num_sms);
+
 
 }  // namespace drv

@@ -3,23 +3,32 @@
 // into RGB spherical harmonics, with the voxel cone-traced indirect shadow of
 // cacheLightingRSM.comp:167-232.
 //
-// Work decomposition (the reference runs one thread per cache and loops over
-// all VPLs; a frame has only a few thousand caches, too few to fill 152 SMs):
-//  - the shadow blocks of all lights (IndirectShadowComputationSampleInterval
-//    consecutive VPLs share one cone) form one index space, cut into
-//    `n_chunks` chunks;
-//  - a unit of work is (cache, chunk) and belongs to one warp; a persistent
-//    grid walks the units up to the device-side cache count (no indirect
-//    dispatch: graph-capturable), and warps never wait for each other;
-//  - inside a unit, the 32 lanes take blocks round-robin: every lane's cone
-//    starts at the same cache, so the first steps of all 32 cones of a warp
-//    fetch the same voxel bytes;
-//  - the warp reduces its 27 partial SH sums with shuffles; with several
-//    chunks, partials go to a scratch slot per unit and the last warp to
-//    finish a cache (a ticket counter per cache) adds them in chunk order, so
-//    results do not depend on scheduling, then resets the ticket;
-//  - the entry's SH is read-modify-written once (`+=`, as the reference's
-//    per-light dispatches accumulate).
+// The reference runs one thread per cache and loops over all VPLs, tracing
+// one cone per shadow block (IndirectShadowComputationSampleInterval
+// consecutive VPLs). A frame has only a few thousand caches, and per cache
+// only a small share of the blocks can contribute at all (a block none of
+// whose VPLs has positive flux and faces the cache adds exactly zero whatever
+// its shadowing), so the stage is split in three launches:
+//
+//  1. cull_kernel (a CTA per cache): tests every block against the cache and
+//     writes the cache's contributing blocks, in block order, to one
+//     contiguous run of a global pair list (one atomic per cache claims it);
+//  2. cone_kernel (a thread per pair, persistent grid): traces the pair's
+//     cone and stores its shadowing — every warp holds 32 pairs, so no lane
+//     idles on a block that needs no cone, and narrow cones (all samples on
+//     voxel level 0) are traced apart from wide ones (mip samples), so a
+//     warp's lanes take one sampling path; with the learned surrogate, the
+//     MLP (k_light_surrogate.cu) fills in the shadowing first and only the
+//     pairs it is not confident about come here;
+//  3. gather_kernel (a CTA per cache): each thread gathers a fixed subset of
+//     the cache's pairs with their shadowing into SH partial sums in
+//     registers, reduced in a fixed order — the result does not depend on
+//     scheduling — and read-modify-written into the entry once (`+=`, as the
+//     reference's per-light dispatches accumulate).
+//
+// light_kernel, the single-launch form (warp per (cache, chunk) unit, cones
+// traced from a per-warp queue, ticketed chunk reduction), serves the frames
+// without indirect shadow and the allocation-free entry point.
 #include <cmath>
 
 #include "drv_device.cuh"
@@ -28,89 +37,312 @@
 #include "voxel_sample.cuh"
 
 namespace drv {
+
+StageParams make_stage_params(const DrvConfig& cfg, const DrvVolumeInfo& vol, const LightLaunch& ll,
+                              const DrvCacheCounter* counter, void* entries, uint32_t entry_stride,
+                              const uint8_t* corners, const void* mips, const size_t* mip_offsets) {
+  StageParams p;
+  p.ll = ll;
+  p.shadow = cfg.indirect_shadow;
+  int base = 0;
+  for (int l = 0; l < ll.n_lights; ++l) {
+    p.block_base[l] = base;
+    base += p.shadow ? ll.lights[l].n_vpls / ll.lights[l].interval : ll.lights[l].n_vpls;
+  }
+  for (int l = ll.n_lights; l <= DRV_MAX_LIGHTS; ++l) p.block_base[l] = base;
+  p.total_blocks = base;
+  p.max_steps = cfg.max_cone_steps;
+  int L = 0;
+  while ((1 << (L + 1)) <= cfg.voxel_res) ++L;
+  p.vox.corners = corners;
+  p.vox.mips = mips;
+  for (int i = 0; i < 16; ++i) p.vox.off[i] = (uint32_t)(i < kMaxVoxelLevels && mip_offsets ? mip_offsets[i] : 0);
+  p.vox.N = cfg.voxel_res;
+  p.vox.log2n = L;
+  p.vox.max_level = L;
+  p.vox.half_mips = cfg.precision == DRV_PRECISION_BF16;
+  for (int i = 0; i < 3; ++i) p.vol_min[i] = vol.volume_world_min[i];
+  p.voxel_size = vol.voxel_size_in_world;
+  p.inv_extent = 1.0f / (p.voxel_size * (float)cfg.voxel_res);
+  for (int c = 0; c < DRV_MAX_CASCADES; ++c) {
+    p.casc_cell[c] = vol.cascades[c].world_voxel_size;
+    for (int i = 0; i < 3; ++i) p.casc_min[c][i] = vol.cascades[c].min[i];
+  }
+  p.counter = counter;
+  p.max_caches = cfg.max_caches;
+  p.entries = (float*)entries;
+  p.stride_floats = (int)(entry_stride / 4);
+  const double kPi = 3.14159265358979323846;
+  p.ev[0] = (float)(1.0 / (2.0 * std::sqrt(kPi)));
+  p.ev[1] = (float)(std::sqrt(3.0) / (2.0 * std::sqrt(kPi)));
+  p.ev[2] = (float)std::sqrt(15.0 / (4.0 * kPi));
+  p.ev[3] = (float)std::sqrt(5.0 / (16.0 * kPi));
+  p.ev[4] = (float)std::sqrt(15.0 / (16.0 * kPi));
+  return p;
+}
+
 namespace {
 
-constexpr int kThreads = 128;
-constexpr int kWarps = kThreads / 32;
-
-struct LightParams {
-  LightLaunch ll;
-  float casc_min[DRV_MAX_CASCADES][3];  // for BF16 entries: position = cell * size + min (cacheGather.comp:65)
-  float casc_cell[DRV_MAX_CASCADES];
-  int block_base[DRV_MAX_LIGHTS + 1];  // prefix sum of shadow blocks per light
-  int total_blocks;
-  int n_chunks;
-  int chunk_blocks;
-  VoxelView vox;
-  float vol_min[3];
-  float voxel_size;
-  int shadow;
-  int max_steps;
-  const DrvCacheCounter* counter;
-  uint32_t max_caches;
-  float* entries;
-  int stride_floats;
-  float* scratch;     // [max_caches * n_chunks][27] partial sums
-  uint32_t* tickets;  // [max_caches], zero between frames
-  float ev[5];        // ShEvaFactor0, 1, 2n2_p1_n1, 20, 2p2 (renderer.cpp:302-306)
-};
-
-// Adds the finished sum of coefficient `lane` to the entry.
+// Adds the finished sum of coefficient k (channel-interleaved, k < 27) to the entry.
 template <bool BF16>
-__device__ __forceinline__ void add_to_entry(float* entry, int lane, float v) {
+__device__ __forceinline__ void add_to_entry(float* entry, int k, float v) {
   if (BF16) {
     uint16_t* sh = reinterpret_cast<uint16_t*>(entry + 1);
-    sh[lane] = to_bf16(from_bf16(sh[lane]) + v);
+    sh[k] = to_bf16(from_bf16(sh[k]) + v);
   } else {
-    entry[sh_offset(lane / 3, lane % 3)] += v;
+    entry[sh_offset(k / 3, k % 3)] += v;
   }
 }
 
-// Shadow block b (global index) -> light and block within the light.
-__device__ __forceinline__ int block_light(const LightParams& p, int b) {
-  int l = 0;
-  while (b >= p.block_base[l + 1]) ++l;
-  return l;
+// True when some VPL of shadow block b can contribute to the cache.
+template <bool BF16>
+__device__ __forceinline__ bool block_live(const StageParams& p, int b, float cx, float cy, float cz) {
+  const int l = block_light(p, b);
+  const LightArgs& la = p.ll.lights[l];
+  const int lb = b - p.block_base[l];
+  for (int j = 0; j < la.interval; ++j) {
+    const VplData v = load_vpl<BF16>(la.vpls, lb * la.interval + j);
+    if (contributes(v, transfer(v, cx, cy, cz))) return true;
+  }
+  return false;
 }
 
-// One warp = one unit (cache, chunk); warps never wait for each other.
-//  - Lanes first test their shadow blocks: a block none of whose VPLs has
-//    positive flux and faces the cache adds exactly zero whatever its
-//    shadowing, so its cone is not traced (the reference traces it).
-//  - Blocks that can contribute go to a per-warp queue; every 32 queued
-//    blocks are traced together, so all lanes march a cone.
-// The SH partial sums live in shared memory (touched once per pair, against
-// hundreds of cone instructions), which keeps the cone loop's register
-// footprint small enough for 8 CTAs per SM.
+// Shadowing of block b seen from the cache (the reference's cone).
+__device__ __forceinline__ float block_cone(const StageParams& p, int b, float cx, float cy, float cz) {
+  const int l = block_light(p, b);
+  const float4 c = __ldg(reinterpret_cast<const float4*>(p.ll.lights[l].cones) + (b - p.block_base[l]));
+  const float vx = (cx - p.vol_min[0]) * p.inv_extent, vy = (cy - p.vol_min[1]) * p.inv_extent,
+              vz = (cz - p.vol_min[2]) * p.inv_extent;
+  return cone_shadow(p.vox, p.voxel_size, p.max_steps, cx, cy, cz, vx, vy, vz, c.x, c.y, c.z, c.w);
+}
+
+// SH gather of the contributing VPLs of block b with the given shadowing
+// into acc/comp (stride 1: register arrays once inlined).
+template <int NK, bool BF16, bool KAHAN>
+__device__ __forceinline__ void gather_block(const StageParams& p, float* acc, float* comp, int b, float cx, float cy,
+                                             float cz, float shadowing) {
+  const int l = block_light(p, b);
+  const LightArgs& la = p.ll.lights[l];
+  const int lb = b - p.block_base[l];
+  for (int j = 0; j < la.interval; ++j) {
+    const VplData v = load_vpl<BF16>(la.vpls, lb * la.interval + j);
+    const Transfer t = transfer(v, cx, cy, cz);
+    if (contributes(v, t)) accumulate<NK, KAHAN>(p.ev, acc, comp, 1, v, t, shadowing);
+  }
+}
+
+// ------------------------------------------------------------ split stage
+constexpr int kCullThreads = 256;
+constexpr int kCullWarps = kCullThreads / 32;
+
+// CTA per cache: contributing blocks -> a contiguous run of the pair list,
+// and their indices -> the narrow or the wide end of the cone order.
+template <bool BF16>
+__global__ void __launch_bounds__(kCullThreads) cull_kernel(StageParams p, PairList L) {
+  // [W] live words, [W] wide words, [W] exclusive prefix of live counts, [W] of wide counts
+  extern __shared__ uint32_t s_dyn[];
+  __shared__ uint32_t s_warp[2][kCullWarps];
+  __shared__ uint32_t s_base[3], s_over;
+  const int W = (p.total_blocks + 31) >> 5;
+  uint32_t* s_live = s_dyn;
+  uint32_t* s_wide = s_dyn + W;
+  uint32_t* s_pre = s_dyn + 2 * W;
+  uint32_t* s_prew = s_dyn + 3 * W;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int per = (W + kCullThreads - 1) / kCullThreads;  // words per thread in the scan
+  const uint32_t n_caches = cache_count(p);
+  for (uint32_t c = blockIdx.x; c < n_caches; c += gridDim.x) {
+    float cx, cy, cz;
+    cache_position<BF16>(p, c, cx, cy, cz);
+    for (int w = warp; w < W; w += kCullWarps) {
+      const int b = (w << 5) + lane;
+      const bool live = b < p.total_blocks && block_live<BF16>(p, b, cx, cy, cz);
+      bool wide = false;
+      if (live) {
+        const int l = block_light(p, b);
+        wide = wide_cone(__ldg(reinterpret_cast<const float*>(p.ll.lights[l].cones + (b - p.block_base[l])) + 3),
+                         p.max_steps);
+      }
+      const uint32_t m = __ballot_sync(0xffffffffu, live), mw = __ballot_sync(0xffffffffu, wide);
+      if (lane == 0) {
+        s_live[w] = m;
+        s_wide[w] = mw;
+      }
+    }
+    __syncthreads();
+    // Exclusive scans of the live and wide counts (thread t owns words [t*per, t*per + per)).
+    const int w0 = threadIdx.x * per;
+    uint32_t local = 0, localw = 0;
+    for (int k = 0; k < per; ++k)
+      if (w0 + k < W) {
+        local += __popc(s_live[w0 + k]);
+        localw += __popc(s_wide[w0 + k]);
+      }
+    uint32_t incl = local, inclw = localw;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o), tw = __shfl_up_sync(0xffffffffu, inclw, o);
+      if (lane >= o) {
+        incl += t;
+        inclw += tw;
+      }
+    }
+    if (lane == 31) {
+      s_warp[0][warp] = incl;
+      s_warp[1][warp] = inclw;
+    }
+    __syncthreads();
+    uint32_t run = incl - local, runw = inclw - localw, total = 0, totalw = 0;
+#pragma unroll
+    for (int k = 0; k < kCullWarps; ++k) {
+      const uint32_t v = s_warp[0][k], vw = s_warp[1][k];
+      if (k < warp) {
+        run += v;
+        runw += vw;
+      }
+      total += v;
+      totalw += vw;
+    }
+    for (int k = 0; k < per; ++k)
+      if (w0 + k < W) {
+        s_pre[w0 + k] = run;
+        s_prew[w0 + k] = runw;
+        run += __popc(s_live[w0 + k]);
+        runw += __popc(s_wide[w0 + k]);
+      }
+    if (threadIdx.x == 0) {
+      const uint32_t base = total ? atomicAdd(L.counters, total) : 0u;
+      const bool over = (uint64_t)base + total > (uint64_t)L.cap;
+      L.info[2 * c] = base;
+      L.info[2 * c + 1] = over ? kPairOverflow : total;
+      s_base[0] = base;
+      s_over = over;
+      if (!over) {
+        s_base[1] = total - totalw ? atomicAdd(L.counters + 1, total - totalw) : 0u;
+        s_base[2] = totalw ? atomicAdd(L.counters + 2, totalw) : 0u;
+      }
+    }
+    __syncthreads();
+    const uint32_t base = s_base[0];
+    if (!s_over) {
+      const uint32_t base_n = s_base[1], base_w = s_base[2];
+      for (int w = warp; w < W; w += kCullWarps) {
+        const uint32_t m = s_live[w], mw = s_wide[w];
+        if ((m >> lane) & 1u) {
+          const uint32_t below = (1u << lane) - 1u;
+          const uint32_t i = base + s_pre[w] + __popc(m & below);
+          L.cache[i] = c;
+          L.block[i] = (uint32_t)((w << 5) + lane);
+          if ((mw >> lane) & 1u)
+            L.order[L.cap - 1u - (base_w + s_prew[w] + __popc(mw & below))] = i;
+          else
+            L.order[base_n + (s_pre[w] - s_prew[w]) + __popc(m & ~mw & below)] = i;
+        }
+      }
+    } else {
+      // The list is full: the gather traces this cache itself; the claimed
+      // slots below the capacity stay empty.
+      const uint32_t end = (uint32_t)min((uint64_t)base + total, (uint64_t)L.cap);
+      for (uint32_t i = base + threadIdx.x; i < end; i += kCullThreads) L.block[i] = kNoPair;
+    }
+    __syncthreads();
+  }
+}
+
+// Thread per cone, over a cone-order list: `ord` holds n_front narrow cones
+// from its front and n_back wide cones from its back (L.order after the
+// cull, or L.retrace after the surrogate).
+template <bool BF16>
+__global__ void __launch_bounds__(128) cone_kernel(StageParams p, PairList L, const uint32_t* ord, int front_counter) {
+  const uint32_t nf = min(L.counters[front_counter], L.cap), nb = min(L.counters[front_counter + 1], L.cap);
+  const uint32_t n = min(nf + nb, L.cap);
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const uint32_t i = k < nf ? ord[k] : ord[L.cap - 1u - (k - nf)];
+    const uint32_t b = L.block[i];
+    if (b == kNoPair) continue;
+    float cx, cy, cz;
+    cache_position<BF16>(p, L.cache[i], cx, cy, cz);
+    L.shadow[i] = block_cone(p, (int)b, cx, cy, cz);
+  }
+}
+
+constexpr int kGatherThreads = 256;
+constexpr int kGatherWarps = kGatherThreads / 32;
+
+// CTA per cache: SH gather of the cache's pairs with their shadowing.
 template <int NK, bool BF16>
-__global__ void __launch_bounds__(kThreads, 8) light_kernel(LightParams p) {
+__global__ void __launch_bounds__(kGatherThreads) gather_kernel(StageParams p, PairList L) {
+  constexpr bool KAHAN = BF16;  // FP32 accumulation of BF16-stored results, compensated
+  __shared__ float s_red[kGatherWarps][NK * 3];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t n_caches = cache_count(p);
+  for (uint32_t c = blockIdx.x; c < n_caches; c += gridDim.x) {
+    float cx, cy, cz;
+    cache_position<BF16>(p, c, cx, cy, cz);
+    float acc[NK * 3], comp[NK * 3];
+#pragma unroll
+    for (int k = 0; k < NK * 3; ++k) acc[k] = comp[k] = 0.0f;
+    const uint32_t first = L.info[2 * c], count = L.info[2 * c + 1];
+    if (count != kPairOverflow) {
+      for (uint32_t j = threadIdx.x; j < count; j += kGatherThreads) {
+        const uint32_t i = first + j;
+        gather_block<NK, BF16, KAHAN>(p, acc, comp, (int)L.block[i], cx, cy, cz, L.shadow[i]);
+      }
+    } else {
+      for (int b = threadIdx.x; b < p.total_blocks; b += kGatherThreads)
+        if (block_live<BF16>(p, b, cx, cy, cz))
+          gather_block<NK, BF16, KAHAN>(p, acc, comp, b, cx, cy, cz, block_cone(p, b, cx, cy, cz));
+    }
+#pragma unroll
+    for (int k = 0; k < NK * 3; ++k) {
+      float v = KAHAN ? __fsub_rn(acc[k], comp[k]) : acc[k];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) s_red[warp][k] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < NK * 3) {
+      float v = 0.0f;
+#pragma unroll
+      for (int w = 0; w < kGatherWarps; ++w) v += s_red[w][threadIdx.x];
+      add_to_entry<BF16>(p.entries + (size_t)c * p.stride_floats, threadIdx.x, v);
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------ single launch
+constexpr int kThreads = 128;
+constexpr int kWarps = kThreads / 32;
+
+struct FusedParams {
+  StageParams s;
+  int n_chunks;
+  int chunk_blocks;
+  float* scratch;     // [max_caches * n_chunks][NK*3] partial sums
+  uint32_t* tickets;  // [max_caches], zero between launches
+  uint32_t* work;     // unit counter + retired CTAs, zero between launches
+};
+
+// One warp = one unit (cache, chunk), handed out dynamically; lanes take the
+// chunk's blocks round-robin. Blocks that can contribute go to a per-warp
+// queue traced 32 at a time; partial SH sums live in shared memory (touched
+// once per pair) so the cone loop keeps 8 CTAs per SM.
+template <int NK, bool BF16>
+__global__ void __launch_bounds__(kThreads, 8) light_kernel(FusedParams fp) {
+  const StageParams& p = fp.s;
   constexpr bool KAHAN = BF16;
   __shared__ float s_acc[NK * 3 * kThreads * (KAHAN ? 2 : 1)];
   __shared__ int s_queue[kWarps][64];
-  const uint32_t count = min((uint32_t)max(p.counter->total_light_cache_count, 0), p.max_caches);
-  const uint32_t n_units = count * (uint32_t)p.n_chunks;
+  const uint32_t n_units = cache_count(p) * (uint32_t)fp.n_chunks;
   const int lane = threadIdx.x & 31;
   int* queue = s_queue[threadIdx.x >> 5];
-  const uint32_t warps = gridDim.x * kWarps;
-  for (uint32_t u = blockIdx.x * kWarps + (threadIdx.x >> 5); u < n_units; u += warps) {
-    const uint32_t cache = u / (uint32_t)p.n_chunks;
-    const int chunk = (int)(u % (uint32_t)p.n_chunks);
+  for (uint32_t u = next_unit(fp.work, lane); u < n_units; u = next_unit(fp.work, lane)) {
+    const uint32_t cache = u / (uint32_t)fp.n_chunks;
+    const int chunk = (int)(u % (uint32_t)fp.n_chunks);
     float* entry = p.entries + (size_t)cache * p.stride_floats;
     float cx, cy, cz;
-    if (BF16) {
-      const uint32_t key = __float_as_uint(entry[0]);
-      const int c = (int)(key >> 27);
-      const float cell = p.casc_cell[c];
-      cx = __fadd_rn(__fmul_rn((float)(key & 511u), cell), p.casc_min[c][0]);
-      cy = __fadd_rn(__fmul_rn((float)((key >> 9) & 511u), cell), p.casc_min[c][1]);
-      cz = __fadd_rn(__fmul_rn((float)((key >> 18) & 511u), cell), p.casc_min[c][2]);
-    } else {
-      cx = entry[0];
-      cy = entry[1];
-      cz = entry[2];
-    }
-    const float scale = 1.0f / (p.voxel_size * p.vox.N);
-    const float vx = (cx - p.vol_min[0]) * scale, vy = (cy - p.vol_min[1]) * scale, vz = (cz - p.vol_min[2]) * scale;
+    cache_position<BF16>(p, cache, cx, cy, cz);
     float* acc = s_acc + threadIdx.x;
     float* comp = acc + NK * 3 * kThreads;
 #pragma unroll
@@ -118,35 +350,28 @@ __global__ void __launch_bounds__(kThreads, 8) light_kernel(LightParams p) {
       acc[k * kThreads] = 0.0f;
       if (KAHAN) comp[k * kThreads] = 0.0f;
     }
-    // Traces the cone of block qb and gathers its contributing VPLs.
     auto trace_block = [&](int qb) {
+      const float s = block_cone(p, qb, cx, cy, cz);
       const int l = block_light(p, qb);
       const LightArgs& la = p.ll.lights[l];
       const int lb = qb - p.block_base[l];
-      const float4 c = __ldg(reinterpret_cast<const float4*>(la.cones) + lb);
-      const float s = cone_shadow(p.vox, p.voxel_size, p.max_steps, cx, cy, cz, vx, vy, vz, c.x, c.y, c.z, c.w);
       for (int j = 0; j < la.interval; ++j) {
         const VplData v = load_vpl<BF16>(la.vpls, lb * la.interval + j);
         const Transfer t = transfer(v, cx, cy, cz);
         if (contributes(v, t)) accumulate<NK, KAHAN>(p.ev, acc, comp, kThreads, v, t, s);
       }
     };
-    const int b0 = chunk * p.chunk_blocks, b1 = min(b0 + p.chunk_blocks, p.total_blocks);
+    const int b0 = chunk * fp.chunk_blocks, b1 = min(b0 + fp.chunk_blocks, p.total_blocks);
     int queued = 0;
     for (int base = b0; base < b1; base += 32) {
       const int b = base + lane;
       bool live = false;
       if (b < b1) {
-        const int l = block_light(p, b);
-        const LightArgs& la = p.ll.lights[l];
-        const int lb = b - p.block_base[l];
         if (p.shadow) {
-          for (int j = 0; j < la.interval && !live; ++j) {
-            const VplData v = load_vpl<BF16>(la.vpls, lb * la.interval + j);
-            live = contributes(v, transfer(v, cx, cy, cz));
-          }
+          live = block_live<BF16>(p, b, cx, cy, cz);
         } else {  // no indirect shadow: blocks are single VPLs, shadowing 1
-          const VplData v = load_vpl<BF16>(la.vpls, lb);
+          const int l = block_light(p, b);
+          const VplData v = load_vpl<BF16>(p.ll.lights[l].vpls, b - p.block_base[l]);
           const Transfer t = transfer(v, cx, cy, cz);
           if (contributes(v, t)) accumulate<NK, KAHAN>(p.ev, acc, comp, kThreads, v, t, 1.0f);
         }
@@ -173,99 +398,105 @@ __global__ void __launch_bounds__(kThreads, 8) light_kernel(LightParams p) {
       for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
       if (lane == k) mine = v;
     }
-    if (p.n_chunks == 1) {
+    if (fp.n_chunks == 1) {
       if (lane < NK * 3) add_to_entry<BF16>(entry, lane, mine);
       continue;
     }
-    if (lane < NK * 3) p.scratch[(size_t)u * (NK * 3) + lane] = mine;
+    if (lane < NK * 3) fp.scratch[(size_t)u * (NK * 3) + lane] = mine;
     __threadfence();
     uint32_t last = 0;
-    if (lane == 0) last = atomicAdd(p.tickets + cache, 1u) == (uint32_t)p.n_chunks - 1u;
+    if (lane == 0) last = atomicAdd(fp.tickets + cache, 1u) == (uint32_t)fp.n_chunks - 1u;
     last = __shfl_sync(0xffffffffu, last, 0);
     if (last) {
       __threadfence();
       if (lane < NK * 3) {
-        const volatile float* sb = p.scratch + (size_t)cache * p.n_chunks * (NK * 3);
+        const volatile float* sb = fp.scratch + (size_t)cache * fp.n_chunks * (NK * 3);
         float v = 0.0f;
-        for (int c = 0; c < p.n_chunks; ++c) v += sb[c * (NK * 3) + lane];
+        for (int c = 0; c < fp.n_chunks; ++c) v += sb[c * (NK * 3) + lane];
         add_to_entry<BF16>(entry, lane, v);
       }
-      if (lane == 0) p.tickets[cache] = 0u;
+      if (lane == 0) fp.tickets[cache] = 0u;
     }
   }
+  retire_cta(fp.work);
+}
+
+// Launch of CTAs_PER_SM x SMs CTAs (at most what fits), or a full persistent grid.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_grid(void (*kernel)(KArgs...), int threads, size_t smem, cudaStream_t s, int num_sms,
+                        int ctas_per_sm, const Args&... args) {
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  if (ctas_per_sm > 0 && ctas_per_sm < per_sm) per_sm = ctas_per_sm;
+  kernel<<<num_sms * per_sm, threads, smem, s>>>(args...);
+  return cudaGetLastError();
 }
 
 template <int NK, bool BF16>
-void launch_variant(cudaStream_t s, const LightParams& p, int num_sms) {
-  int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, light_kernel<NK, BF16>, kThreads, 0);
-  light_kernel<NK, BF16><<<num_sms * (per_sm < 1 ? 1 : per_sm), kThreads, 0, s>>>(p);
+cudaError_t split_variant(cudaStream_t s, const StageParams& p, const PairList& L, const void* weights,
+                          float conf_threshold, int cone_ctas, int gather_ctas, int num_sms) {
+  cudaError_t e = cudaMemsetAsync(L.counters, 0, 8 * sizeof(uint32_t), s);
+  if (e != cudaSuccess) return e;
+  const size_t cull_smem = (size_t)((p.total_blocks + 31) >> 5) * 4 * sizeof(uint32_t);
+  if ((e = launch_persistent(cull_kernel<BF16>, kCullThreads, cull_smem, s, num_sms, p, L)) != cudaSuccess) return e;
+  if (weights) {
+    if ((e = launch_surrogate_mlp(s, p, L, weights, conf_threshold, BF16, num_sms)) != cudaSuccess) return e;
+    e = launch_grid(cone_kernel<BF16>, 128, 0, s, num_sms, cone_ctas, p, L, (const uint32_t*)L.retrace, 3);
+  } else {
+    e = launch_grid(cone_kernel<BF16>, 128, 0, s, num_sms, cone_ctas, p, L, (const uint32_t*)L.order, 1);
+  }
+  if (e != cudaSuccess) return e;
+  return launch_grid(gather_kernel<NK, BF16>, kGatherThreads, 0, s, num_sms, gather_ctas, p, L);
 }
 
 }  // namespace
 
-int light_chunks(int total_blocks) {
-  int n = (total_blocks + 255) / 256;
-  return n < 1 ? 1 : (n > kMaxLightChunks ? kMaxLightChunks : n);
+int light_chunks(int total_blocks, int max_chunks) {
+  int n = (total_blocks + kLightChunkMinBlocks - 1) / kLightChunkMinBlocks;
+  return n < 1 ? 1 : (n > max_chunks ? max_chunks : n);
 }
 
 cudaError_t launch_light_caches(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const LightLaunch& ll,
                                 const DrvCacheCounter* counter, void* entries, uint32_t entry_stride,
-                                const uint8_t* corners, const void* mips, const size_t* mip_offsets, float* scratch,
-                                uint32_t* tickets, int num_sms) {
-  LightParams p;
-  p.ll = ll;
-  p.shadow = cfg.indirect_shadow;
-  int base = 0;
-  for (int l = 0; l < ll.n_lights; ++l) {
-    p.block_base[l] = base;
-    base += p.shadow ? ll.lights[l].n_vpls / ll.lights[l].interval : ll.lights[l].n_vpls;
-  }
-  for (int l = ll.n_lights; l <= DRV_MAX_LIGHTS; ++l) p.block_base[l] = base;
-  p.total_blocks = base;
-  p.n_chunks = light_chunks(base);
-  p.chunk_blocks = (base + p.n_chunks - 1) / p.n_chunks;
-  int L = 0;
-  while ((1 << (L + 1)) <= cfg.voxel_res) ++L;
-  p.vox.corners = corners;
-  p.vox.mips = mips;
-  for (int i = 0; i < 16; ++i) p.vox.off[i] = (uint32_t)(i < kMaxVoxelLevels ? mip_offsets[i] : 0);
-  p.vox.N = cfg.voxel_res;
-  p.vox.log2n = L;
-  p.vox.max_level = L;
-  for (int i = 0; i < 3; ++i) p.vol_min[i] = vol.volume_world_min[i];
-  p.voxel_size = vol.voxel_size_in_world;
-  p.max_steps = cfg.max_cone_steps;
-  p.counter = counter;
-  p.max_caches = cfg.max_caches;
-  p.entries = (float*)entries;
-  p.stride_floats = (int)(entry_stride / 4);
-  p.scratch = scratch;
-  p.tickets = tickets;
-  const double kPi = 3.14159265358979323846;
-  p.ev[0] = (float)(1.0 / (2.0 * std::sqrt(kPi)));
-  p.ev[1] = (float)(std::sqrt(3.0) / (2.0 * std::sqrt(kPi)));
-  p.ev[2] = (float)std::sqrt(15.0 / (4.0 * kPi));
-  p.ev[3] = (float)std::sqrt(5.0 / (16.0 * kPi));
-  p.ev[4] = (float)std::sqrt(15.0 / (16.0 * kPi));
+                                const uint8_t* corners, const void* mips, const size_t* mip_offsets,
+                                const LightScratch& scratch, int num_sms) {
+  FusedParams fp;
+  fp.s = make_stage_params(cfg, vol, ll, counter, entries, entry_stride, corners, mips, mip_offsets);
+  fp.n_chunks = light_chunks(fp.s.total_blocks, scratch.max_chunks);
+  fp.chunk_blocks = (fp.s.total_blocks + fp.n_chunks - 1) / fp.n_chunks;
+  fp.scratch = scratch.partials;
+  fp.tickets = scratch.tickets;
+  fp.work = scratch.work;
   const bool bf16 = cfg.precision == DRV_PRECISION_BF16;
-  p.vox.half_mips = bf16;
-  for (int c = 0; c < DRV_MAX_CASCADES; ++c) {
-    p.casc_cell[c] = vol.cascades[c].world_voxel_size;
-    for (int i = 0; i < 3; ++i) p.casc_min[c][i] = vol.cascades[c].min[i];
-  }
-  if (cfg.sh_order == 2) {
-    if (bf16)
-      launch_variant<9, true>(s, p, num_sms);
-    else
-      launch_variant<9, false>(s, p, num_sms);
-  } else {
-    if (bf16)
-      launch_variant<4, true>(s, p, num_sms);
-    else
-      launch_variant<4, false>(s, p, num_sms);
-  }
-  return cudaGetLastError();
+  if (cfg.sh_order == 2)
+    return bf16 ? launch_persistent(light_kernel<9, true>, kThreads, 0, s, num_sms, fp)
+                : launch_persistent(light_kernel<9, false>, kThreads, 0, s, num_sms, fp);
+  return bf16 ? launch_persistent(light_kernel<4, true>, kThreads, 0, s, num_sms, fp)
+              : launch_persistent(light_kernel<4, false>, kThreads, 0, s, num_sms, fp);
+}
+
+bool light_split_supported(const DrvConfig& cfg, const LightLaunch& ll) {
+  if (!cfg.indirect_shadow) return false;
+  long blocks = 0;
+  for (int l = 0; l < ll.n_lights; ++l) blocks += ll.lights[l].n_vpls / ll.lights[l].interval;
+  return blocks >= 1 && blocks <= kMaxSplitBlocks;
+}
+
+cudaError_t launch_light_split(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const LightLaunch& ll,
+                               const DrvCacheCounter* counter, void* entries, uint32_t entry_stride,
+                               const uint8_t* corners, const void* mips, const size_t* mip_offsets,
+                               const PairList& pairs, const void* weights, int cone_ctas_per_sm,
+                               int gather_ctas_per_sm, int num_sms) {
+  const StageParams p = make_stage_params(cfg, vol, ll, counter, entries, entry_stride, corners, mips, mip_offsets);
+  const float thr = cfg.surrogate_conf_threshold;
+  const bool bf16 = cfg.precision == DRV_PRECISION_BF16;
+  if (cfg.sh_order == 2)
+    return bf16 ? split_variant<9, true>(s, p, pairs, weights, thr, cone_ctas_per_sm, gather_ctas_per_sm, num_sms)
+                : split_variant<9, false>(s, p, pairs, weights, thr, cone_ctas_per_sm, gather_ctas_per_sm, num_sms);
+  return bf16 ? split_variant<4, true>(s, p, pairs, weights, thr, cone_ctas_per_sm, gather_ctas_per_sm, num_sms)
+              : split_variant<4, false>(s, p, pairs, weights, thr, cone_ctas_per_sm, gather_ctas_per_sm, num_sms);
 }
 
 }  // namespace drv

@@ -1,9 +1,8 @@
-// k_light_surrogate.cu — the cache-lighting stage with the learned visibility
-// surrogate in place of the indirect-shadow cone (cacheLightingRSM.comp:167-232).
-//
-// Same work decomposition as k_light.cu (a warp owns a (cache, chunk) unit,
-// lanes take shadow blocks round-robin, ticketed chunk reduction). Per warp
-// iteration the 32 lanes' pairs form a 32-row batch:
+// k_light_surrogate.cu — the learned visibility surrogate in place of the
+// indirect-shadow cone (cacheLightingRSM.comp:167-232), as the middle pass of
+// the split light stage (k_light.cu): after the cull has listed the
+// (cache, shadow block) pairs that can contribute, mlp_kernel takes them 32
+// per warp:
 //  1. each lane computes its pair's 32 input features (surrogate.cuh) and
 //     stores them as BF16 in the warp's shared-memory tile;
 //  2. the MLP runs on tensor cores with mma.sync m16n8k16 (BF16 in, FP32
@@ -12,10 +11,9 @@
 //     registers; weights are read from shared memory (rows padded so the
 //     fragment loads are bank-conflict free);
 //  3. each lane gets its (visibility, confidence) back by shuffles; confident
-//     pairs use sigmoid(visibility), the others are appended to a per-warp
-//     queue that is cone-traced 32 pairs at a time, so a single uncertain pair
-//     never holds a whole warp in the cone loop;
-//  4. the SH gather is the plain stage's (accumulate_vpl).
+//     pairs store sigmoid(visibility) as their shadowing, the others are
+//     appended to the re-trace list (narrow cones at its front, wide ones at
+//     its back) that cone_kernel then traces.
 #include <cmath>
 
 #include "drv_device.cuh"
@@ -42,29 +40,6 @@ struct __align__(16) MlpWeights {
   float b1[kMlpHidden], b2[kMlpHidden], b3[kMlpHidden], b4[kMlpOutPad];
 };
 
-struct SurrogateParams {
-  LightLaunch ll;
-  int block_base[DRV_MAX_LIGHTS + 1];
-  int total_blocks;
-  int n_chunks;
-  int chunk_blocks;
-  VoxelView vox;
-  float vol_min[3];
-  float voxel_size;
-  int max_steps;
-  float casc_min[DRV_MAX_CASCADES][3];
-  float casc_cell[DRV_MAX_CASCADES];
-  const DrvCacheCounter* counter;
-  uint32_t max_caches;
-  float* entries;
-  int stride_floats;
-  float* scratch;
-  uint32_t* tickets;
-  const MlpWeights* weights;
-  float conf_threshold;
-  uint32_t* fallback_count;  // optional: [0] re-traced pairs, [1] pairs the MLP evaluated
-  float ev[5];
-};
 
 __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
   const uint32_t a = __bfloat16_as_ushort(__float2bfloat16_rn(lo));
@@ -116,236 +91,111 @@ __device__ __forceinline__ void hidden_layer(const uint32_t (&in)[2][KSTEPS][4],
   }
 }
 
-// Shadow block b (global index) -> light index.
-__device__ __forceinline__ int block_light(const SurrogateParams& p, int b) {
-  int l = 0;
-  while (b >= p.block_base[l + 1]) ++l;
-  return l;
-}
-
-// SH gather of the contributing VPLs of shadow block b with the given
-// shadowing; acc is this thread's column of a [NK*3][kThreads] shared array.
-template <int NK, bool BF16>
-__device__ __forceinline__ void gather_block(const SurrogateParams& p, float* acc, int b, float cx, float cy,
-                                             float cz, float shadowing) {
-  const int l = block_light(p, b);
-  const LightArgs& la = p.ll.lights[l];
-  const int lb = b - p.block_base[l];
-  for (int j = 0; j < la.interval; ++j) {
-    const VplData v = load_vpl<BF16>(la.vpls, lb * la.interval + j);
-    const Transfer t = transfer(v, cx, cy, cz);
-    if (contributes(v, t)) accumulate<NK, false>(p.ev, acc, nullptr, kThreads, v, t, shadowing);
-  }
-}
-
-// Dynamic shared memory of one CTA (about 51 KB with SH2).
-template <int NK>
-struct __align__(16) SurrogateSmem {
+// Dynamic shared memory of one CTA (about 36 KB).
+struct __align__(16) MlpSmem {
   MlpWeights w;
   uint16_t x[kWarps][32 * kLd1];  // per-warp BF16 feature tile, 80-byte rows
-  int queue[kWarps][64];          // per-warp re-trace queue
-  int live[kWarps][64];           // per-warp queue of blocks that can contribute
-  float acc[NK * 3 * kThreads];   // per-thread SH partial sums, column per thread
 };
 
-template <int NK, bool BF16>
-__global__ void __launch_bounds__(kThreads) light_surrogate_kernel(SurrogateParams p) {
+// Warp per 32 listed pairs: features -> MLP -> shadowing or re-trace.
+// counters[5] receives the number of pairs evaluated.
+template <bool BF16>
+__global__ void __launch_bounds__(kThreads) mlp_kernel(StageParams p, PairList L, const MlpWeights* weights,
+                                                       float conf_threshold) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  SurrogateSmem<NK>& S = *reinterpret_cast<SurrogateSmem<NK>*>(smem_raw);
-  MlpWeights& s_w = S.w;
-  auto& s_x = S.x;
-  auto& s_queue = S.queue;
-  float* s_acc = S.acc;
+  MlpSmem& S = *reinterpret_cast<MlpSmem*>(smem_raw);
+  const MlpWeights& s_w = S.w;
   {
-    const uint4* src = reinterpret_cast<const uint4*>(p.weights);
-    uint4* dst = reinterpret_cast<uint4*>(&s_w);
+    const uint4* src = reinterpret_cast<const uint4*>(weights);
+    uint4* dst = reinterpret_cast<uint4*>(&S.w);
     for (int i = threadIdx.x; i < (int)(sizeof(MlpWeights) / 16); i += kThreads) dst[i] = src[i];
   }
   __syncthreads();
-  const uint32_t count = min((uint32_t)max(p.counter->total_light_cache_count, 0), p.max_caches);
-  const uint32_t n_units = count * (uint32_t)p.n_chunks;
+  const uint32_t n = min(L.counters[0], L.cap);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int g = lane >> 2, tig = lane & 3;
-  const uint32_t warps = gridDim.x * kWarps;
-  uint16_t* xt = s_x[warp];
-  int* queue = s_queue[warp];
-  const float inv_extent = 1.0f / (p.voxel_size * p.vox.N);
-  uint32_t retraced = 0, evaluated = 0;
-  for (uint32_t u = blockIdx.x * kWarps + warp; u < n_units; u += warps) {
-    const uint32_t cache = u / (uint32_t)p.n_chunks;
-    const int chunk = (int)(u % (uint32_t)p.n_chunks);
-    float* entry = p.entries + (size_t)cache * p.stride_floats;
-    float cx, cy, cz;
-    if (BF16) {
-      const uint32_t key = __float_as_uint(entry[0]);
-      const int c = (int)(key >> 27);
-      cx = __fadd_rn(__fmul_rn((float)(key & 511u), p.casc_cell[c]), p.casc_min[c][0]);
-      cy = __fadd_rn(__fmul_rn((float)((key >> 9) & 511u), p.casc_cell[c]), p.casc_min[c][1]);
-      cz = __fadd_rn(__fmul_rn((float)((key >> 18) & 511u), p.casc_cell[c]), p.casc_min[c][2]);
+  uint16_t* xt = S.x[warp];
+  uint32_t evaluated = 0;
+  for (uint32_t base = (blockIdx.x * kWarps + warp) * 32u; base < n; base += gridDim.x * kWarps * 32u) {
+    const uint32_t i = base + lane;
+    const uint32_t b = i < n ? L.block[i] : kNoPair;
+    const bool valid = b != kNoPair;
+    float f[kMlpIn];
+    bool wide = false;
+    if (valid) {
+      float cx, cy, cz;
+      cache_position<BF16>(p, L.cache[i], cx, cy, cz);
+      const int l = block_light(p, (int)b);
+      const LightArgs& la = p.ll.lights[l];
+      const int lb = (int)b - p.block_base[l];
+      const float4 cone = __ldg(reinterpret_cast<const float4*>(la.cones) + lb);
+      const VplData v = load_vpl<BF16>(la.vpls, lb * la.interval);
+      surrogate_features(p.vox, p.inv_extent, p.vol_min, p.voxel_size, p.max_steps, cx, cy, cz, cone.x, cone.y,
+                         cone.z, v.nx, v.ny, v.nz, cone.w, f);
+      wide = wide_cone(cone.w, p.max_steps);
     } else {
-      cx = entry[0];
-      cy = entry[1];
-      cz = entry[2];
+#pragma unroll
+      for (int k = 0; k < kMlpIn; ++k) f[k] = 0.0f;
     }
-    const float vx = (cx - p.vol_min[0]) * inv_extent, vy = (cy - p.vol_min[1]) * inv_extent,
-                vz = (cz - p.vol_min[2]) * inv_extent;
-    float* acc = s_acc + threadIdx.x;
+    uint32_t* row = reinterpret_cast<uint32_t*>(xt + lane * kLd1);
 #pragma unroll
-    for (int k = 0; k < NK * 3; ++k) acc[k * kThreads] = 0.0f;
-    int* live = S.live[warp];
-    int queued = 0, n_live = 0;
-    // Runs the MLP on the n (<= 32) live blocks at live[first ...]: confident
-    // pairs are gathered with the predicted visibility, the others queued for
-    // the cone, which runs once 32 are waiting.
-    auto mlp_batch = [&](int first, int n) {
-      const bool valid = lane < n;
-      evaluated += n;
-      const int b = valid ? live[first + lane] : 0;
-      __syncwarp();
-      float f[kMlpIn];
-      if (valid) {
-        const int l = block_light(p, b);
-        const LightArgs& la = p.ll.lights[l];
-        const int lb = b - p.block_base[l];
-        const float4 cone = __ldg(reinterpret_cast<const float4*>(la.cones) + lb);
-        const VplData v = load_vpl<BF16>(la.vpls, lb * la.interval);
-        surrogate_features(p.vox, inv_extent, p.vol_min, p.voxel_size, p.max_steps, cx, cy, cz, cone.x, cone.y,
-                           cone.z, v.nx, v.ny, v.nz, cone.w, f);
-      } else {
+    for (int k = 0; k < kMlpIn / 2; ++k) row[k] = pack_bf16x2(f[2 * k], f[2 * k + 1]);
+    __syncwarp();
+    uint32_t a1[2][2][4];
 #pragma unroll
-        for (int i = 0; i < kMlpIn; ++i) f[i] = 0.0f;
-      }
-      uint32_t* row = reinterpret_cast<uint32_t*>(xt + lane * kLd1);
+    for (int m = 0; m < 2; ++m)
 #pragma unroll
-      for (int i = 0; i < kMlpIn / 2; ++i) row[i] = pack_bf16x2(f[2 * i], f[2 * i + 1]);
-      __syncwarp();
-      uint32_t a1[2][2][4];
+      for (int kk = 0; kk < 2; ++kk)
+        ldmatrix_x4(a1[m][kk],
+                    xt + (16 * m + (lane & 7) + ((lane >> 3) & 1) * 8) * kLd1 + 16 * kk + ((lane >> 4) & 1) * 8);
+    __syncwarp();
+    uint32_t h1[2][4][4], h2[2][4][4];
+    hidden_layer<2, kLd1>(a1, s_w.w1, s_w.b1, h1, g, tig);
+    hidden_layer<4, kLdH>(h1, s_w.w2, s_w.b2, h2, g, tig);
+    hidden_layer<4, kLdH>(h2, s_w.w3, s_w.b3, h1, g, tig);
+    float o[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+    {
+      const uint16_t* wr = s_w.w4 + g * kLdH + 2 * tig;
 #pragma unroll
-      for (int m = 0; m < 2; ++m)
-#pragma unroll
-        for (int kk = 0; kk < 2; ++kk)
-          ldmatrix_x4(a1[m][kk], xt + (16 * m + (lane & 7) + ((lane >> 3) & 1) * 8) * kLd1 + 16 * kk +
-                                     ((lane >> 4) & 1) * 8);
-      __syncwarp();
-      uint32_t h1[2][4][4], h2[2][4][4];
-      hidden_layer<2, kLd1>(a1, s_w.w1, s_w.b1, h1, g, tig);
-      hidden_layer<4, kLdH>(h1, s_w.w2, s_w.b2, h2, g, tig);
-      hidden_layer<4, kLdH>(h2, s_w.w3, s_w.b3, h1, g, tig);
-      float o[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
-      {
-        const uint16_t* wr = s_w.w4 + g * kLdH + 2 * tig;
-#pragma unroll
-        for (int kk = 0; kk < 4; ++kk) {
-          const uint32_t bb0 = *reinterpret_cast<const uint32_t*>(wr + 16 * kk);
-          const uint32_t bb1 = *reinterpret_cast<const uint32_t*>(wr + 16 * kk + 8);
-          mma_bf16(o[0], h1[0][kk], bb0, bb1);
-          mma_bf16(o[1], h1[1][kk], bb0, bb1);
-        }
-      }
-      // (visibility, confidence) of row `lane`: held by lane 4*(row&7),
-      // registers 0,1 (rows 0-7 of an m-tile) or 2,3 (rows 8-15).
-      const int src = 4 * (lane & 7);
-      const float r00 = __shfl_sync(0xffffffffu, o[0][0], src), r01 = __shfl_sync(0xffffffffu, o[0][1], src);
-      const float r02 = __shfl_sync(0xffffffffu, o[0][2], src), r03 = __shfl_sync(0xffffffffu, o[0][3], src);
-      const float r10 = __shfl_sync(0xffffffffu, o[1][0], src), r11 = __shfl_sync(0xffffffffu, o[1][1], src);
-      const float r12 = __shfl_sync(0xffffffffu, o[1][2], src), r13 = __shfl_sync(0xffffffffu, o[1][3], src);
-      const bool hi_rows = (lane & 8) != 0;
-      const float ov = lane < 16 ? (hi_rows ? r02 : r00) : (hi_rows ? r12 : r10);
-      const float oc = lane < 16 ? (hi_rows ? r03 : r01) : (hi_rows ? r13 : r11);
-      const float vis = sigmoidf(ov + s_w.b4[0]);
-      const float conf = sigmoidf(oc + s_w.b4[1]);
-      const bool retrace = valid && !(conf >= p.conf_threshold);
-      if (valid && !retrace) gather_block<NK, BF16>(p, acc, b, cx, cy, cz, vis);
-      const uint32_t mask = __ballot_sync(0xffffffffu, retrace);
-      if (retrace) queue[queued + __popc(mask & ((1u << lane) - 1u))] = b;
-      queued += __popc(mask);
-      __syncwarp();
-      if (queued >= 32) {
-        const int qb = queue[queued - 32 + lane];
-        const int l = block_light(p, qb);
-        const float4 c = __ldg(reinterpret_cast<const float4*>(p.ll.lights[l].cones) + (qb - p.block_base[l]));
-        const float sh = cone_shadow(p.vox, p.voxel_size, p.max_steps, cx, cy, cz, vx, vy, vz, c.x, c.y, c.z, c.w);
-        gather_block<NK, BF16>(p, acc, qb, cx, cy, cz, sh);
-        queued -= 32;
-        retraced += 32;
-        __syncwarp();
-      }
-    };
-    const int b0 = chunk * p.chunk_blocks, b1 = min(b0 + p.chunk_blocks, p.total_blocks);
-    for (int base = b0; base < b1; base += 32) {
-      const int b = base + lane;
-      bool is_live = false;
-      if (b < b1) {
-        const int l = block_light(p, b);
-        const LightArgs& la = p.ll.lights[l];
-        const int lb = b - p.block_base[l];
-        for (int j = 0; j < la.interval && !is_live; ++j) {
-          const VplData v = load_vpl<BF16>(la.vpls, lb * la.interval + j);
-          is_live = contributes(v, transfer(v, cx, cy, cz));
-        }
-      }
-      const uint32_t mask = __ballot_sync(0xffffffffu, is_live);
-      if (is_live) live[n_live + __popc(mask & ((1u << lane) - 1u))] = b;
-      n_live += __popc(mask);
-      __syncwarp();
-      if (n_live >= 32) {
-        mlp_batch(n_live - 32, 32);
-        n_live -= 32;
+      for (int kk = 0; kk < 4; ++kk) {
+        const uint32_t bb0 = *reinterpret_cast<const uint32_t*>(wr + 16 * kk);
+        const uint32_t bb1 = *reinterpret_cast<const uint32_t*>(wr + 16 * kk + 8);
+        mma_bf16(o[0], h1[0][kk], bb0, bb1);
+        mma_bf16(o[1], h1[1][kk], bb0, bb1);
       }
     }
-    if (n_live > 0) mlp_batch(0, n_live);
-    if (queued > 0) {
-      if (lane < queued) {
-        const int qb = queue[lane];
-        const int l = block_light(p, qb);
-        const float4 c = __ldg(reinterpret_cast<const float4*>(p.ll.lights[l].cones) + (qb - p.block_base[l]));
-        const float sh = cone_shadow(p.vox, p.voxel_size, p.max_steps, cx, cy, cz, vx, vy, vz, c.x, c.y, c.z, c.w);
-        gather_block<NK, BF16>(p, acc, qb, cx, cy, cz, sh);
+    // (visibility, confidence) of row `lane`: held by lane 4*(row&7),
+    // registers 0,1 (rows 0-7 of an m-tile) or 2,3 (rows 8-15).
+    const int src = 4 * (lane & 7);
+    const float r00 = __shfl_sync(0xffffffffu, o[0][0], src), r01 = __shfl_sync(0xffffffffu, o[0][1], src);
+    const float r02 = __shfl_sync(0xffffffffu, o[0][2], src), r03 = __shfl_sync(0xffffffffu, o[0][3], src);
+    const float r10 = __shfl_sync(0xffffffffu, o[1][0], src), r11 = __shfl_sync(0xffffffffu, o[1][1], src);
+    const float r12 = __shfl_sync(0xffffffffu, o[1][2], src), r13 = __shfl_sync(0xffffffffu, o[1][3], src);
+    const bool hi_rows = (lane & 8) != 0;
+    const float ov = lane < 16 ? (hi_rows ? r02 : r00) : (hi_rows ? r12 : r10);
+    const float oc = lane < 16 ? (hi_rows ? r03 : r01) : (hi_rows ? r13 : r11);
+    const float vis = sigmoidf(ov + s_w.b4[0]);
+    const float conf = sigmoidf(oc + s_w.b4[1]);
+    const bool retrace = valid && !(conf >= conf_threshold);
+    if (valid && !retrace) L.shadow[i] = vis;
+    // Re-traced pairs: narrow cones to the front of L.retrace, wide ones to its back.
+    const uint32_t mn = __ballot_sync(0xffffffffu, retrace && !wide), mw = __ballot_sync(0xffffffffu, retrace && wide);
+    if (mn | mw) {
+      uint32_t fn = 0, fw = 0;
+      if (lane == 0) {
+        if (mn) fn = atomicAdd(L.counters + 3, (uint32_t)__popc(mn));
+        if (mw) fw = atomicAdd(L.counters + 4, (uint32_t)__popc(mw));
       }
-      retraced += queued;
-      __syncwarp();
+      fn = __shfl_sync(0xffffffffu, fn, 0);
+      fw = __shfl_sync(0xffffffffu, fw, 0);
+      const uint32_t below = (1u << lane) - 1u;
+      if (retrace && !wide) L.retrace[fn + __popc(mn & below)] = i;
+      if (retrace && wide) L.retrace[L.cap - 1u - (fw + __popc(mw & below))] = i;
     }
-    // warp reduction + chunk combination (as k_light.cu)
-    float mine = 0.0f;
-#pragma unroll
-    for (int k = 0; k < NK * 3; ++k) {
-      float v = acc[k * kThreads];
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-      if (lane == k) mine = v;
-    }
-    auto add = [&](float v) {
-      if (BF16) {
-        uint16_t* sh = reinterpret_cast<uint16_t*>(entry + 1);
-        sh[lane] = to_bf16(from_bf16(sh[lane]) + v);
-      } else {
-        entry[sh_offset(lane / 3, lane % 3)] += v;
-      }
-    };
-    if (p.n_chunks == 1) {
-      if (lane < NK * 3) add(mine);
-      continue;
-    }
-    if (lane < NK * 3) p.scratch[(size_t)u * (NK * 3) + lane] = mine;
-    __threadfence();
-    uint32_t last = 0;
-    if (lane == 0) last = atomicAdd(p.tickets + cache, 1u) == (uint32_t)p.n_chunks - 1u;
-    last = __shfl_sync(0xffffffffu, last, 0);
-    if (last) {
-      __threadfence();
-      if (lane < NK * 3) {
-        const volatile float* sb = p.scratch + (size_t)cache * p.n_chunks * (NK * 3);
-        float v = 0.0f;
-        for (int c = 0; c < p.n_chunks; ++c) v += sb[c * (NK * 3) + lane];
-        add(v);
-      }
-      if (lane == 0) p.tickets[cache] = 0u;
-    }
+    evaluated += (uint32_t)__popc(__ballot_sync(0xffffffffu, valid));
+    __syncwarp();
   }
-  if (p.fallback_count && lane == 0) {
-    if (retraced) atomicAdd(p.fallback_count, retraced);
-    if (evaluated) atomicAdd(p.fallback_count + 1, evaluated);
-  }
+  if (lane == 0 && evaluated) atomicAdd(L.counters + 5, evaluated);
 }
 
 // FP32 master parameters -> padded BF16 inference layout.
@@ -402,18 +252,6 @@ __global__ void eval_kernel(const MlpWeights* __restrict__ w, const float* __res
   }
 }
 
-template <int NK, bool BF16>
-cudaError_t launch_sur(cudaStream_t s, const SurrogateParams& p, int num_sms) {
-  const int smem = (int)sizeof(SurrogateSmem<NK>);
-  cudaError_t e = cudaFuncSetAttribute(light_surrogate_kernel<NK, BF16>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  if (e != cudaSuccess) return e;
-  int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, light_surrogate_kernel<NK, BF16>, kThreads, smem);
-  light_surrogate_kernel<NK, BF16><<<num_sms * (per_sm < 1 ? 1 : per_sm), kThreads, smem, s>>>(p);
-  return cudaGetLastError();
-}
-
 }  // namespace
 
 size_t surrogate_weights_bytes() { return sizeof(MlpWeights); }
@@ -428,56 +266,13 @@ cudaError_t launch_surrogate_eval(cudaStream_t s, const void* weights, const flo
   return cudaGetLastError();
 }
 
-cudaError_t launch_light_surrogate(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol,
-                                   const LightLaunch& ll, const DrvCacheCounter* counter, void* entries,
-                                   uint32_t entry_stride, const uint8_t* corners, const void* mips,
-                                   const size_t* mip_offsets, float* scratch, uint32_t* tickets, const void* weights,
-                                   uint32_t* fallback_count, int num_sms) {
-  SurrogateParams p;
-  p.ll = ll;
-  int base = 0;
-  for (int l = 0; l < ll.n_lights; ++l) {
-    p.block_base[l] = base;
-    base += ll.lights[l].n_vpls / ll.lights[l].interval;
-  }
-  for (int l = ll.n_lights; l <= DRV_MAX_LIGHTS; ++l) p.block_base[l] = base;
-  p.total_blocks = base;
-  p.n_chunks = light_chunks(base);
-  p.chunk_blocks = (base + p.n_chunks - 1) / p.n_chunks;
-  int L = 0;
-  while ((1 << (L + 1)) <= cfg.voxel_res) ++L;
-  p.vox.corners = corners;
-  p.vox.mips = mips;
-  for (int i = 0; i < 16; ++i) p.vox.off[i] = (uint32_t)(i < kMaxVoxelLevels ? mip_offsets[i] : 0);
-  p.vox.N = cfg.voxel_res;
-  p.vox.log2n = L;
-  p.vox.max_level = L;
-  const bool bf16 = cfg.precision == DRV_PRECISION_BF16;
-  p.vox.half_mips = bf16;
-  for (int i = 0; i < 3; ++i) p.vol_min[i] = vol.volume_world_min[i];
-  p.voxel_size = vol.voxel_size_in_world;
-  p.max_steps = cfg.max_cone_steps;
-  for (int c = 0; c < DRV_MAX_CASCADES; ++c) {
-    p.casc_cell[c] = vol.cascades[c].world_voxel_size;
-    for (int i = 0; i < 3; ++i) p.casc_min[c][i] = vol.cascades[c].min[i];
-  }
-  p.counter = counter;
-  p.max_caches = cfg.max_caches;
-  p.entries = (float*)entries;
-  p.stride_floats = (int)(entry_stride / 4);
-  p.scratch = scratch;
-  p.tickets = tickets;
-  p.weights = (const MlpWeights*)weights;
-  p.conf_threshold = cfg.surrogate_conf_threshold;
-  p.fallback_count = fallback_count;
-  const double kPi = 3.14159265358979323846;
-  p.ev[0] = (float)(1.0 / (2.0 * std::sqrt(kPi)));
-  p.ev[1] = (float)(std::sqrt(3.0) / (2.0 * std::sqrt(kPi)));
-  p.ev[2] = (float)std::sqrt(15.0 / (4.0 * kPi));
-  p.ev[3] = (float)std::sqrt(5.0 / (16.0 * kPi));
-  p.ev[4] = (float)std::sqrt(15.0 / (16.0 * kPi));
-  if (cfg.sh_order == 2) return bf16 ? launch_sur<9, true>(s, p, num_sms) : launch_sur<9, false>(s, p, num_sms);
-  return bf16 ? launch_sur<4, true>(s, p, num_sms) : launch_sur<4, false>(s, p, num_sms);
+cudaError_t launch_surrogate_mlp(cudaStream_t s, const StageParams& p, const PairList& L, const void* weights,
+                                 float conf_threshold, bool bf16, int num_sms) {
+  const size_t smem = sizeof(MlpSmem);
+  auto kernel = bf16 ? mlp_kernel<true> : mlp_kernel<false>;
+  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  return launch_persistent(kernel, kThreads, smem, s, num_sms, p, L, (const MlpWeights*)weights, conf_threshold);
 }
 
 }  // namespace drv

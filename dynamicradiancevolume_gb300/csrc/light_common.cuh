@@ -9,8 +9,88 @@
 #include <stdint.h>
 
 #include "drv_device.cuh"
+#include "drv_internal.h"
+#include "voxel_sample.cuh"
 
 namespace drv {
+
+// Everything a light-stage kernel needs to know about the frame.
+struct StageParams {
+  LightLaunch ll;
+  int block_base[DRV_MAX_LIGHTS + 1];  // prefix sum of shadow blocks per light
+  int total_blocks;
+  int shadow;     // indirect shadow on
+  int max_steps;  // cone steps
+  VoxelView vox;
+  float vol_min[3];
+  float voxel_size;
+  float inv_extent;                     // 1 / (voxel_size * N)
+  float casc_min[DRV_MAX_CASCADES][3];  // BF16 entries store cells: position = cell * size + min
+  float casc_cell[DRV_MAX_CASCADES];
+  const DrvCacheCounter* counter;
+  uint32_t max_caches;
+  float* entries;
+  int stride_floats;
+  float ev[5];  // ShEvaFactor0, 1, 2n2_p1_n1, 20, 2p2 (renderer.cpp:302-306)
+};
+
+// Host: fills StageParams from the stage's arguments (k_light.cu).
+StageParams make_stage_params(const DrvConfig& cfg, const DrvVolumeInfo& vol, const LightLaunch& ll,
+                              const DrvCacheCounter* counter, void* entries, uint32_t entry_stride,
+                              const uint8_t* corners, const void* mips, const size_t* mip_offsets);
+
+// Host: the surrogate's pass over the pair list (k_light_surrogate.cu):
+// shadowing of the confident pairs, the others appended to L.retrace.
+cudaError_t launch_surrogate_mlp(cudaStream_t s, const StageParams& p, const PairList& L, const void* weights,
+                                 float conf_threshold, bool bf16, int num_sms);
+
+// Host: persistent launch (SMs x resident CTAs per SM) of a kernel.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_persistent(void (*kernel)(KArgs...), int threads, size_t smem, cudaStream_t s, int num_sms,
+                              const Args&... args) {
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
+  if (e != cudaSuccess) return e;
+  kernel<<<num_sms * (per_sm < 1 ? 1 : per_sm), threads, smem, s>>>(args...);
+  return cudaGetLastError();
+}
+
+__device__ __forceinline__ uint32_t cache_count(const StageParams& p) {
+  return min((uint32_t)max(p.counter->total_light_cache_count, 0), p.max_caches);
+}
+
+// Shadow block b (global index) -> light.
+__device__ __forceinline__ int block_light(const StageParams& p, int b) {
+  int l = 0;
+  while (b >= p.block_base[l + 1]) ++l;
+  return l;
+}
+
+// True when a cone of this aperture (dsr: sample radius per unit distance)
+// may sample above voxel level 0 within max_steps steps, i.e. its radius
+// passes one voxel. Cones are traced in two groups by this test so that the
+// lanes of a warp take the same sampling path; results do not depend on it.
+__device__ __forceinline__ bool wide_cone(float dsr, int max_steps) {
+  return dsr * (float)(max_steps + 2) > 1.0f;
+}
+
+// World position of cache c (BF16 entries hold the packed cell key).
+template <bool BF16>
+__device__ __forceinline__ void cache_position(const StageParams& p, uint32_t c, float& x, float& y, float& z) {
+  const float* entry = p.entries + (size_t)c * p.stride_floats;
+  if (BF16) {
+    const uint32_t key = __float_as_uint(__ldg(entry));
+    const int k = (int)(key >> 27);
+    const float cell = p.casc_cell[k];
+    x = __fadd_rn(__fmul_rn((float)(key & 511u), cell), p.casc_min[k][0]);
+    y = __fadd_rn(__fmul_rn((float)((key >> 9) & 511u), cell), p.casc_min[k][1]);
+    z = __fadd_rn(__fmul_rn((float)((key >> 18) & 511u), cell), p.casc_min[k][2]);
+  } else {
+    x = __ldg(entry);
+    y = __ldg(entry + 1);
+    z = __ldg(entry + 2);
+  }
+}
 
 struct VplData {
   float px, py, pz, area, fr, fg, fb, nx, ny, nz;
@@ -73,6 +153,27 @@ __device__ __forceinline__ Transfer transfer(const VplData& v, float cx, float c
 // shadow cone need not be traced.
 __device__ __forceinline__ bool contributes(const VplData& v, const Transfer& t) {
   return t.g > 0.0f && (v.fr > 0.0f || v.fg > 0.0f || v.fb > 0.0f);
+}
+
+// Dynamic work distribution of the light stages: work[0] hands out units
+// (one atomic per unit, by lane 0), work[1] counts retired CTAs; the last CTA
+// to retire zeroes both, so every launch starts from zero without a memset.
+__device__ __forceinline__ uint32_t next_unit(uint32_t* work, int lane) {
+  uint32_t u = 0;
+  if (lane == 0) u = atomicAdd(work, 1u);
+  return __shfl_sync(0xffffffffu, u, 0);
+}
+
+// Called by every thread of the CTA once it has no more units.
+__device__ __forceinline__ void retire_cta(uint32_t* work) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(work + 1, 1u) == gridDim.x - 1u) {
+      work[0] = 0u;
+      work[1] = 0u;
+    }
+  }
 }
 
 // SH gather of one VPL, cacheLightingRSM.comp:255-278. acc (and comp with

@@ -16,8 +16,9 @@
 //    (cudaGetSymbolAddress, with the device current); make that first call
 //    before capturing a stream into a CUDA graph;
 //  - all calls share the one array and it keeps the last call's contents:
-//    each call clears the per-cache tickets before its kernel runs, and calls
-//    that overlap on the GPU (different streams, no ordering) race on it;
+//    each call clears the per-cache tickets and the unit counter before its
+//    kernel runs, and calls that overlap on the GPU (different streams, no
+//    ordering) race on it;
 //  - at most DRV_STATIC_SCRATCH_MAX_CACHES caches; a config with a larger
 //    max_caches is rejected with DRV_ERR_CAPACITY.
 #include <mutex>
@@ -26,10 +27,12 @@
 
 namespace {
 
-constexpr size_t kPartialFloats = (size_t)DRV_STATIC_SCRATCH_MAX_CACHES * drv::kMaxLightChunks * 27;
-constexpr size_t kTicketWords = DRV_STATIC_SCRATCH_MAX_CACHES;
+constexpr int kStaticChunks = 8;  // chunks per cache (the context path allows more)
+constexpr size_t kPartialFloats = (size_t)DRV_STATIC_SCRATCH_MAX_CACHES * kStaticChunks * 27;
+constexpr size_t kTicketWords = DRV_STATIC_SCRATCH_MAX_CACHES + 2;
 
-// Partial sums first, then one ticket per cache (reinterpreted as uint32).
+// Partial sums first, then one ticket per cache and the two words of the
+// dynamic unit counter (reinterpreted as uint32).
 static __device__ __align__(256) float g_light_static_scratch[kPartialFloats + kTicketWords];
 
 constexpr int kMaxDevices = 64;
@@ -87,6 +90,7 @@ extern "C" drv_status drv_light_caches_static_scratch(const DrvConfig* cfg, cons
   drv_status st = device_scratch(&scratch, &num_sms);
   if (st != DRV_OK) return st;
   uint32_t* tickets = reinterpret_cast<uint32_t*>(scratch + kPartialFloats);
+  const drv::LightScratch ls{scratch, tickets, tickets + DRV_STATIC_SCRATCH_MAX_CACHES, kStaticChunks};
   cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
   if (cudaMemsetAsync(tickets, 0, kTicketWords * sizeof(uint32_t), s) != cudaSuccess) return DRV_ERR_CUDA;
   // Offsets of mip levels 1..L inside the concatenated FP32 pyramid.
@@ -99,6 +103,6 @@ extern "C" drv_status drv_light_caches_static_scratch(const DrvConfig* cfg, cons
   }
   const uint32_t stride = cfg->sh_order == 2 ? 128u : 64u;
   cudaError_t e = drv::launch_light_caches(s, *cfg, *vol, ll, counter, cache_entries, stride, voxel_corners,
-                                           voxel_mips, offsets, scratch, tickets, num_sms);
+                                           voxel_mips, offsets, ls, num_sms);
   return e == cudaSuccess ? DRV_OK : DRV_ERR_CUDA;
 }

@@ -101,7 +101,10 @@ __device__ __forceinline__ float sample_voxels(const VoxelView& v, float sx, flo
 
 // Indirect-shadow cone, cacheLightingRSM.comp:195-230: march from the cache
 // toward the block's average VAL position, growing the sample sphere with the
-// distance, front-to-back occlusion, at most max_steps samples.
+// distance, front-to-back occlusion, at most max_steps samples. Once the
+// occlusion reaches 1 a further step gives occlusion * (1 - s) + s >= 1 for
+// any sample s in [0, 1], so the clamped result is 0 (to within one rounding)
+// whatever is sampled: the march stops there (the reference marches on).
 __device__ __forceinline__ float cone_shadow(const VoxelView& v, float voxel_size, int max_steps, float cx, float cy,
                                              float cz, float px, float py, float pz, float ax, float ay, float az,
                                              float dsr) {
@@ -121,7 +124,7 @@ __device__ __forceinline__ float cone_shadow(const VoxelView& v, float voxel_siz
     dist += step;
     const float radius = dist * dsr;
     occlusion += (1.0f - occlusion) * sample_voxels(v, qx, qy, qz, __log2f(radius));
-    if (dist >= goal) break;
+    if (dist >= goal || occlusion >= 1.0f) break;
     step = fmaxf(1.0f, radius * k);
   }
   return fminf(fmaxf(1.0f - occlusion, 0.0f), 1.0f);

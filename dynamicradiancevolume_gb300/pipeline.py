@@ -228,6 +228,21 @@ class Pipeline:
     def sync(self):
         self._c(self.lib.drv_sync(self.ctx))
 
+    def set_tuning(self, **knobs) -> abi.DrvTuning:
+        """Sets execution knobs (DrvTuning field names); the others keep their value."""
+        t = abi.DrvTuning()
+        self._c(self.lib.drv_get_tuning(self.ctx, C.byref(t)))
+        for k, v in knobs.items():
+            setattr(t, k, v)
+        self._c(self.lib.drv_set_tuning(self.ctx, C.byref(t)))
+        return t
+
+    def surrogate_stats(self) -> tuple[int, int]:
+        """(pairs the MLP evaluated, pairs re-traced) of the last light stage."""
+        ev, rt = C.c_uint32(), C.c_uint32()
+        self._c(self.lib.drv_get_surrogate_stats(self.ctx, C.byref(ev), C.byref(rt)))
+        return ev.value, rt.value
+
     def cache_count(self) -> int:
         n = C.c_uint32()
         self._c(self.lib.drv_get_cache_count(self.ctx, C.byref(n)))

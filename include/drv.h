@@ -423,6 +423,22 @@ drv_status drv_get_surrogate_fallbacks(DrvContext* ctx, uint32_t* out);
  * with the cone. Synchronises. */
 drv_status drv_get_surrogate_stats(DrvContext* ctx, uint32_t* evaluated, uint32_t* retraced);
 
+/* ---- execution knobs -------------------------------------------------------
+ * No counterpart in the reference (its shaders have fixed work-group sizes).
+ * Knobs change how the GPU is used, not what is computed: results stay the
+ * same up to the order of FP32 summation. Zero fields keep the default. */
+typedef struct DrvTuning {
+  int32_t light_path;      /* DRV_LIGHT_PATH_*: light stage as one launch or as cull, cone, gather */
+  uint32_t pair_capacity;  /* split stage: pairs the list may hold (<= its allocation); caches that do
+                              not fit are traced by the gather itself. 0: the whole allocation */
+  int32_t cone_ctas_per_sm;   /* split stage: CTAs of the cone pass per SM (0: as many as fit) */
+  int32_t gather_ctas_per_sm; /* split stage: CTAs of the gather pass per SM (0: as many as fit) */
+  int32_t reserved[4];
+} DrvTuning;
+enum { DRV_LIGHT_PATH_AUTO = 0, DRV_LIGHT_PATH_SINGLE = 1, DRV_LIGHT_PATH_SPLIT = 2 };
+drv_status drv_set_tuning(DrvContext* ctx, const DrvTuning* tuning);
+drv_status drv_get_tuning(DrvContext* ctx, DrvTuning* tuning);
+
 /* ---- allocation-free light stage ------------------------------------------
  * No counterpart in the reference: the reference renderer always owns its GL
  * buffers. This is the cache-lighting stage (the kernel behind

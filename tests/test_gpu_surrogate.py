@@ -115,8 +115,13 @@ def test_inference_mlp_matches_torch_fp32(frame, lib):
     # reference with the same BF16-rounded weights, inputs and activations, FP32 arithmetic
     pb = torch.from_numpy(params).to(X.device).bfloat16().float()
     ref = torch.sigmoid(torch_mlp(torch, pb, X.bfloat16().float(), bf16_activations=True))
-    assert torch.allclose(out, ref, atol=1e-2)
-    assert float((out - ref).abs().mean()) < 1e-3
+    # tanh.approx GELU vs torch's tanh can push a hidden activation across a
+    # BF16 rounding boundary (one BF16 ulp = 2^-8 relative), so a few rows may
+    # differ by more than the typical error.
+    err = (out - ref).abs()
+    assert float((err <= 1e-2).all(dim=1).float().mean()) >= 0.999
+    assert float(err.max()) < 5e-2
+    assert float(err.mean()) < 1e-3
 
 
 def _surrogate_run(threshold, params, oracle, seed=21):
@@ -135,6 +140,8 @@ def _surrogate_run(threshold, params, oracle, seed=21):
     pos, sh = p.read_entries_decoded(n)
     fb = C.c_uint32()
     assert p.lib.drv_get_surrogate_fallbacks(p.ctx, C.byref(fb)) == 0
+    evaluated, retraced = p.surrogate_stats()
+    assert retraced == fb.value <= evaluated
     return p, pos, sh, fb.value
 
 
@@ -144,6 +151,7 @@ def test_all_pairs_retraced_equals_cone_stage(frame, oracle):
     n_blocks = sum(p.buffers().n_vpls[l] for l in range(W_SMALL.n_lights))
     # every pair that can contribute is re-traced; the others need no visibility
     assert 0 < fallbacks < frame.count * n_blocks
+    assert p.surrogate_stats() == (fallbacks, fallbacks)
     # allocation order is atomic order: compare caches sorted by position
     a, b = np.lexsort(pos.T[::-1]), np.lexsort(frame.positions.T[::-1])
     assert np.array_equal(pos[a], frame.positions[b])
