@@ -31,21 +31,33 @@ struct AllocParams {
 // AllocateCaches, cacheGather.comp:32-91. Corners outside the atlas are
 // skipped (the reference performs an image atomic there, which GL defines to
 // do nothing and return 0, and then allocates an entry nobody can address).
+// The 8 compare-and-swaps are independent, so all are issued before any
+// result is used, and the won corners take consecutive entries from one
+// atomicAdd (entry order is atomic order in the reference as well).
 __device__ void allocate_cell(const AllocParams& p, int coord, int cascade) {
   const int res = p.res, res2 = res * res, res3 = res2 * res;
   const int aw = p.n_cascades * res;
   const int base = coord - res3 * cascade;
   const int bz = base / res2, by = (base - bz * res2) / res, bx = base % res;
   const DrvCascade& k = p.vol.cascades[cascade];
+  uint32_t won = 0;
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
     // Corner order of cacheGather.comp:34-44: (0,0,0) (0,1,0) (0,0,1) (0,1,1) (1,...)
     const int lx = bx + (i >> 2), ly = by + (i & 1), lz = bz + ((i >> 1) & 1);
     const int ax = lx + cascade * res;
-    if (ax >= aw || ly >= res || lz >= res) continue;
-    uint32_t* slot = p.atlas + ((size_t)lz * res + ly) * aw + ax;
-    if (atomicCAS(slot, 0u, 0xFFFFFFFFu) != 0u) continue;
-    uint32_t idx = (uint32_t)atomicAdd(&p.counter->total_light_cache_count, 1);
+    if (ax < aw && ly < res && lz < res &&
+        atomicCAS(p.atlas + ((size_t)lz * res + ly) * aw + ax, 0u, 0xFFFFFFFFu) == 0u)
+      won |= 1u << i;
+  }
+  if (!won) return;
+  const uint32_t first = (uint32_t)atomicAdd(&p.counter->total_light_cache_count, __popc(won));
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    if (!((won >> i) & 1u)) continue;
+    const int lx = bx + (i >> 2), ly = by + (i & 1), lz = bz + ((i >> 1) & 1);
+    uint32_t* slot = p.atlas + ((size_t)lz * res + ly) * aw + (lx + cascade * res);
+    const uint32_t idx = first + __popc(won & ((1u << i) - 1u));
     if (idx >= p.max_caches) {
       raise_error(p.err, DRV_DEVERR_CAPACITY);  // slot stays locked = empty for apply
       continue;

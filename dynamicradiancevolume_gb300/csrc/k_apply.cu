@@ -34,18 +34,39 @@ struct ApplyParams {
   float* out;
 };
 
+// Irradiance of cascade c at wp for normal n: the 8 corner caches weighted
+// trilinearly (SampleCacheIrradiance). Per-axis weights, bounds and atlas
+// offsets are formed once; the 8 atlas words are loaded before any entry so
+// their latencies overlap.
+template <bool BF16, bool SH2>
 __device__ __forceinline__ f3 lighting(const ApplyParams& p, const float wp[3], int c, f3 n, uint32_t n_caches) {
   const DrvCascade& k = p.vol.cascades[c];
-  float a[3];
+  float wgt[3][2];
   int a0[3];
-  float t[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
-    a[i] = __fdiv_rn(__fsub_rn(wp[i], k.min[i]), k.world_voxel_size);
-    a0[i] = __float2int_rz(fminf(fmaxf(a[i], -1e9f), 1e9f));
-    t[i] = a[i] - (float)a0[i];
+    const float a = __fdiv_rn(__fsub_rn(wp[i], k.min[i]), k.world_voxel_size);
+    a0[i] = __float2int_rz(fminf(fmaxf(a, -1e9f), 1e9f));
+    const float t = a - (float)a0[i];
+    wgt[i][0] = 1.0f - t;
+    wgt[i][1] = t;
   }
   const int aw = p.n_cascades * p.res;
+  const int x0 = a0[0] + p.res * c, y0 = a0[1], z0 = a0[2];
+  // Corner (ox, oy, oz) is inside the atlas when each axis is.
+  const bool vx0 = x0 >= 0 && x0 < aw, vx1 = x0 + 1 >= 0 && x0 + 1 < aw;
+  const bool vy0 = y0 >= 0 && y0 < p.res, vy1 = y0 + 1 >= 0 && y0 + 1 < p.res;
+  const bool vz0 = z0 >= 0 && z0 < p.res, vz1 = z0 + 1 >= 0 && z0 + 1 < p.res;
+  const long long base = ((long long)z0 * p.res + y0) * aw + x0;
+  const long long plane = (long long)p.res * aw;
+  uint32_t slot[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    // Corner order of cacheApply.frag:219-230: x fastest.
+    const int ox = i & 1, oy = (i >> 1) & 1, oz = i >> 2;
+    const bool v = (ox ? vx1 : vx0) && (oy ? vy1 : vy0) && (oz ? vz1 : vz0);
+    slot[i] = v ? __ldg(p.atlas + (base + ox + oy * aw + oz * plane)) : 0u;
+  }
   // Per-normal factors of SampleCacheIrradiance.
   const float f0 = p.cl[0];
   const float f1y = p.cl[1] * n.y, f1z = p.cl[1] * n.z, f1x = p.cl[1] * n.x;
@@ -54,44 +75,43 @@ __device__ __forceinline__ f3 lighting(const ApplyParams& p, const float wp[3], 
   f3 irr = mkf3(0.f, 0.f, 0.f);
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
-    // Corner order of cacheApply.frag:219-230: x fastest.
+    const uint32_t addr = slot[i];
+    // unallocated, outside the atlas, or 0xFFFFFFFF (locked by an overflow)
+    const bool live = addr != 0u && addr <= n_caches;
     const int ox = i & 1, oy = (i >> 1) & 1, oz = i >> 2;
-    const float w = (ox ? t[0] : 1.0f - t[0]) * (oy ? t[1] : 1.0f - t[1]) * (oz ? t[2] : 1.0f - t[2]);
-    const int x = a0[0] + ox + p.res * c, y = a0[1] + oy, z = a0[2] + oz;
-    if (x < 0 || y < 0 || z < 0 || x >= aw || y >= p.res || z >= p.res) continue;
-    const uint32_t addr = __ldg(p.atlas + ((size_t)z * p.res + y) * aw + x);
-    if (addr == 0u || addr > n_caches) continue;  // also rejects 0xFFFFFFFF
-    float er, eg, eb;
-    if (p.bf16) {
+    const float w = wgt[0][ox] * wgt[1][oy] * wgt[2][oz];
+    float er = 0.0f, eg = 0.0f, eb = 0.0f;
+    if (!live) {
+    } else if (BF16) {
       // 27 BF16 values from byte 4 of the 64-byte entry, coefficient-major.
       const uint4* e = reinterpret_cast<const uint4*>(p.entries + (size_t)(addr - 1u) * p.stride_floats);
-      const uint4 a = __ldg(e), b = __ldg(e + 1), c = __ldg(e + 2), d = __ldg(e + 3);
-      const uint32_t w[16] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x, c.y, c.z, c.w, d.x, d.y, d.z, d.w};
+      const uint4 a = __ldg(e), b = __ldg(e + 1), cc = __ldg(e + 2), d = __ldg(e + 3);
+      const uint32_t q[16] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, cc.x, cc.y, cc.z, cc.w, d.x, d.y, d.z, d.w};
       float sh[27];
 #pragma unroll
-      for (int j = 0; j < 27; ++j) sh[j] = from_bf16((uint16_t)(w[1 + (j >> 1)] >> (16 * (j & 1))));
+      for (int j = 0; j < 27; ++j) sh[j] = from_bf16((uint16_t)(q[1 + (j >> 1)] >> (16 * (j & 1))));
       er = sh[0] * f0 - sh[3] * f1y + sh[6] * f1z - sh[9] * f1x;
       eg = sh[1] * f0 - sh[4] * f1y + sh[7] * f1z - sh[10] * f1x;
       eb = sh[2] * f0 - sh[5] * f1y + sh[8] * f1z - sh[11] * f1x;
-      if (p.sh2) {
+      if (SH2) {
         er += -sh[12] * f4 + sh[15] * f5 + sh[18] * f6 + sh[21] * f7 + sh[24] * f8;
         eg += -sh[13] * f4 + sh[16] * f5 + sh[19] * f6 + sh[22] * f7 + sh[25] * f8;
         eb += -sh[14] * f4 + sh[17] * f5 + sh[20] * f6 + sh[23] * f7 + sh[26] * f8;
       }
     } else {
-    const float4* e = reinterpret_cast<const float4*>(p.entries + (size_t)(addr - 1u) * p.stride_floats);
-    const float4 q1 = __ldg(e + 1), q2 = __ldg(e + 2), q3 = __ldg(e + 3);
-    // q1 = {SH1neg1, SH00_r}, q2 = {SH10, SH00_g}, q3 = {SH1pos1, SH00_b}
-    er = q1.w * f0 - q1.x * f1y + q2.x * f1z - q3.x * f1x;
-    eg = q2.w * f0 - q1.y * f1y + q2.y * f1z - q3.y * f1x;
-    eb = q3.w * f0 - q1.z * f1y + q2.z * f1z - q3.z * f1x;
-    if (p.sh2) {
-      const float4 q4 = __ldg(e + 4), q5 = __ldg(e + 5), q6 = __ldg(e + 6), q7 = __ldg(e + 7);
-      // q4 = {SH2neg2, SH20_r}, q5 = {SH2neg1, SH20_g}, q6 = {SH2pos1, SH20_b}, q7 = {SH2pos2, pad}
-      er += -q4.x * f4 + q5.x * f5 + q4.w * f6 + q6.x * f7 + q7.x * f8;
-      eg += -q4.y * f4 + q5.y * f5 + q5.w * f6 + q6.y * f7 + q7.y * f8;
-      eb += -q4.z * f4 + q5.z * f5 + q6.w * f6 + q6.z * f7 + q7.z * f8;
-    }
+      const float4* e = reinterpret_cast<const float4*>(p.entries + (size_t)(addr - 1u) * p.stride_floats);
+      const float4 q1 = __ldg(e + 1), q2 = __ldg(e + 2), q3 = __ldg(e + 3);
+      // q1 = {SH1neg1, SH00_r}, q2 = {SH10, SH00_g}, q3 = {SH1pos1, SH00_b}
+      er = q1.w * f0 - q1.x * f1y + q2.x * f1z - q3.x * f1x;
+      eg = q2.w * f0 - q1.y * f1y + q2.y * f1z - q3.y * f1x;
+      eb = q3.w * f0 - q1.z * f1y + q2.z * f1z - q3.z * f1x;
+      if (SH2) {
+        const float4 q4 = __ldg(e + 4), q5 = __ldg(e + 5), q6 = __ldg(e + 6), q7 = __ldg(e + 7);
+        // q4 = {SH2neg2, SH20_r}, q5 = {SH2neg1, SH20_g}, q6 = {SH2pos1, SH20_b}, q7 = {SH2pos2, pad}
+        er += -q4.x * f4 + q5.x * f5 + q4.w * f6 + q6.x * f7 + q7.x * f8;
+        eg += -q4.y * f4 + q5.y * f5 + q5.w * f6 + q6.y * f7 + q7.y * f8;
+        eb += -q4.z * f4 + q5.z * f5 + q6.w * f6 + q6.z * f7 + q7.z * f8;
+      }
     }
     irr.x += fmaxf(er, 0.0f) * w;
     irr.y += fmaxf(eg, 0.0f) * w;
@@ -100,6 +120,7 @@ __device__ __forceinline__ f3 lighting(const ApplyParams& p, const float wp[3], 
   return irr;
 }
 
+template <bool BF16, bool SH2>
 __global__ void __launch_bounds__(256) apply_kernel(ApplyParams p) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
   if (x >= p.w || y >= p.h) return;
@@ -125,12 +146,12 @@ __global__ void __launch_bounds__(256) apply_kernel(ApplyParams p) {
   const float inv_pi = 1.0f / DRV_SHADER_PI;
   const f3 alb = mkf3(__ldg(p.albedo + 3 * i) * inv_pi, __ldg(p.albedo + 3 * i + 1) * inv_pi,
                       __ldg(p.albedo + 3 * i + 2) * inv_pi);
-  f3 irr = lighting(p, wp, c, n, n_caches);
+  f3 irr = lighting<BF16, SH2>(p, wp, c, n, n_caches);
   f3 col = mkf3(irr.x * alb.x, irr.y * alb.y, irr.z * alb.z);
   if (p.transitions) {
     const float t = cascade_transition(p.vol, c, wp);
     if (t > 0.0f && c < p.n_cascades - 1) {
-      f3 irr2 = lighting(p, wp, c + 1, n, n_caches);
+      f3 irr2 = lighting<BF16, SH2>(p, wp, c + 1, n, n_caches);
       f3 col2 = mkf3(irr2.x * alb.x, irr2.y * alb.y, irr2.z * alb.z);
       col = col * (1.0f - t) + col2 * t;  // mix(), cacheApply.frag:359
     }
@@ -172,7 +193,10 @@ cudaError_t launch_apply(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeIn
   p.cl[4] = (float)(std::sqrt(15.0 * kPi) / 16.0);
   p.out = out_rgb;
   dim3 block(16, 16), grid((g.width + 15) / 16, (g.height + 15) / 16);
-  apply_kernel<<<grid, block, 0, s>>>(p);
+  if (p.bf16)
+    p.sh2 ? apply_kernel<true, true><<<grid, block, 0, s>>>(p) : apply_kernel<true, false><<<grid, block, 0, s>>>(p);
+  else
+    p.sh2 ? apply_kernel<false, true><<<grid, block, 0, s>>>(p) : apply_kernel<false, false><<<grid, block, 0, s>>>(p);
   return cudaGetLastError();
 }
 

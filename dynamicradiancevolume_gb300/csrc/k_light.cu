@@ -30,6 +30,8 @@
 // traced from a per-warp queue, ticketed chunk reduction), serves the frames
 // without indirect shadow and the allocation-free entry point.
 #include <cmath>
+#include <mutex>
+#include <vector>
 
 #include "drv_device.cuh"
 #include "drv_internal.h"
@@ -425,10 +427,8 @@ __global__ void __launch_bounds__(kThreads, 8) light_kernel(FusedParams fp) {
 template <typename... KArgs, typename... Args>
 cudaError_t launch_grid(void (*kernel)(KArgs...), int threads, size_t smem, cudaStream_t s, int num_sms,
                         int ctas_per_sm, const Args&... args) {
-  int per_sm = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
-  if (e != cudaSuccess) return e;
-  if (per_sm < 1) per_sm = 1;
+  int per_sm = resident_ctas(reinterpret_cast<const void*>(kernel), threads, smem);
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
   if (ctas_per_sm > 0 && ctas_per_sm < per_sm) per_sm = ctas_per_sm;
   kernel<<<num_sms * per_sm, threads, smem, s>>>(args...);
   return cudaGetLastError();
@@ -452,6 +452,26 @@ cudaError_t split_variant(cudaStream_t s, const StageParams& p, const PairList& 
 }
 
 }  // namespace
+
+int resident_ctas(const void* kernel, int threads, size_t smem) {
+  struct Entry {
+    const void* kernel;
+    int threads, device;
+    size_t smem;
+    int ctas;
+  };
+  static std::mutex mu;
+  static std::vector<Entry> memo;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  std::lock_guard<std::mutex> lock(mu);
+  for (const Entry& e : memo)
+    if (e.kernel == kernel && e.threads == threads && e.smem == smem && e.device == dev) return e.ctas;
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, smem) != cudaSuccess) return 0;
+  memo.push_back(Entry{kernel, threads, dev, smem, n});
+  return n;
+}
 
 int light_chunks(int total_blocks, int max_chunks) {
   int n = (total_blocks + kLightChunkMinBlocks - 1) / kLightChunkMinBlocks;

@@ -15,6 +15,7 @@
 //     appended to the re-trace list (narrow cones at its front, wide ones at
 //     its back) that cone_kernel then traces.
 #include <cmath>
+#include <mutex>
 
 #include "drv_device.cuh"
 #include "drv_internal.h"
@@ -270,8 +271,21 @@ cudaError_t launch_surrogate_mlp(cudaStream_t s, const StageParams& p, const Pai
                                  float conf_threshold, bool bf16, int num_sms) {
   const size_t smem = sizeof(MlpSmem);
   auto kernel = bf16 ? mlp_kernel<true> : mlp_kernel<false>;
-  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  // The attribute belongs to the function (on the current device); setting it
+  // again costs a driver call per launch, so it is set once per device.
+  static std::mutex mu;
+  static uint64_t done[2] = {0, 0};  // bit d: set on device d
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    if (dev >= 64 || !((done[bf16] >> dev) & 1u)) {
+      e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      if (dev < 64) done[bf16] |= 1ull << dev;
+    }
+  }
   return launch_persistent(kernel, kThreads, smem, s, num_sms, p, L, (const MlpWeights*)weights, conf_threshold);
 }
 

@@ -52,39 +52,39 @@ __device__ __forceinline__ uint32_t range_mask(int lo, int hi, int base) {
   return m << (a - base);
 }
 
-// One CTA per z-slab: gather the faces that touch the slab, then every thread
-// writes whole 32-voxel words (each word once, coalesced).
-__global__ void __launch_bounds__(256) voxelize_kernel(const DrvBox* __restrict__ boxes, int n_boxes, DrvVolumeInfo vol,
-                                                       int N, uint32_t* __restrict__ bits) {
-  __shared__ Face faces[kMaxBoxes * 6];
-  __shared__ int n_faces;
-  const int z = blockIdx.x;
-  if (threadIdx.x == 0) n_faces = 0;
-  __syncthreads();
-  for (int f = threadIdx.x; f < n_boxes * 6; f += blockDim.x) {
-    Face fc;
-    if (!make_face(boxes[f / 6], (f % 6) >> 1, f & 1, vol.volume_world_min, vol.voxel_size_in_world, N, fc)) continue;
-    bool touches = (fc.axis == 2 && fc.k == z) || (fc.axis == 0 && z >= fc.v0 && z <= fc.v1) ||
-                   (fc.axis == 1 && z >= fc.u0 && z <= fc.u1);
-    if (touches) faces[atomicAdd(&n_faces, 1)] = fc;
-  }
-  __syncthreads();
+// Box faces x kVoxelSplit CTAs (grid n_boxes*6 by kVoxelSplit): the face's
+// covered voxel rectangle is ORed into the zeroed bitmask, one atomicOr per
+// touched 32-voxel word (per voxel for faces on the x axis, whose rows cross
+// words), the face's items dealt out over its CTAs. OR is order-independent,
+// so the mask does not depend on scheduling.
+constexpr int kVoxelSplit = 16;
+
+__global__ void __launch_bounds__(256) voxelize_kernel(const DrvBox* __restrict__ boxes, DrvVolumeInfo vol, int N,
+                                                       uint32_t* __restrict__ bits) {
+  Face fc;
+  if (!make_face(boxes[blockIdx.x / 6], (blockIdx.x % 6) >> 1, blockIdx.x & 1, vol.volume_world_min,
+                 vol.voxel_size_in_world, N, fc))
+    return;
   const int wpr = N / 32;  // words per row
-  const int nf = n_faces;
-  for (int w = threadIdx.x; w < N * wpr; w += blockDim.x) {
-    int y = w / wpr, base = (w % wpr) * 32;
-    uint32_t m = 0u;
-    for (int f = 0; f < nf; ++f) {
-      Face fc = faces[f];
-      if (fc.axis == 2) {  // plane z = k: x in [u0,u1], y in [v0,v1]
-        if (y >= fc.v0 && y <= fc.v1) m |= range_mask(fc.u0, fc.u1, base);
-      } else if (fc.axis == 0) {  // plane x = k: y in [u0,u1], z in [v0,v1]
-        if (y >= fc.u0 && y <= fc.u1) m |= range_mask(fc.k, fc.k, base);
-      } else {  // plane y = k: z in [u0,u1], x in [v0,v1]
-        if (y == fc.k) m |= range_mask(fc.v0, fc.v1, base);
-      }
+  const int u0 = fc.u0, u1 = fc.u1, v0 = fc.v0, v1 = fc.v1, k = fc.k;
+  if (fc.axis == 0) {  // plane x = k: y in [u0,u1], z in [v0,v1]
+    const int ny = u1 - u0 + 1, nz = v1 - v0 + 1;
+    const uint32_t bit = 1u << (k & 31);
+    for (int i = blockIdx.y * blockDim.x + threadIdx.x; i < ny * nz; i += gridDim.y * blockDim.x) {
+      const int y = u0 + i % ny, z = v0 + i / ny;
+      atomicOr(bits + ((size_t)z * N + y) * wpr + (k >> 5), bit);
     }
-    bits[((size_t)z * N + y) * wpr + (w % wpr)] = m;
+  } else {
+    // axis 2, plane z = k: x in [u0,u1] for rows y in [v0,v1];
+    // axis 1, plane y = k: x in [v0,v1] for slices z in [u0,u1].
+    const int xl = fc.axis == 2 ? u0 : v0, xh = fc.axis == 2 ? u1 : v1;
+    const int rl = fc.axis == 2 ? v0 : u0, rh = fc.axis == 2 ? v1 : u1;
+    const int w0 = xl >> 5, nw = (xh >> 5) - w0 + 1, nr = rh - rl + 1;
+    for (int i = blockIdx.y * blockDim.x + threadIdx.x; i < nw * nr; i += gridDim.y * blockDim.x) {
+      const int w = w0 + i % nw, r = rl + i / nw;
+      const size_t row = fc.axis == 2 ? (size_t)k * N + r : (size_t)r * N + k;
+      atomicOr(bits + row * wpr + w, range_mask(xl, xh, w * 32));
+    }
   }
 }
 
@@ -213,6 +213,11 @@ __global__ void __launch_bounds__(256) corners_kernel(int N, int log2n, const ui
       r |= ((w4 >> (x4 & 31)) & 1u) << 4;
       rows[dz][dy] = r;
     }
+  // Word (lz, ly) holds the bytes lx = 0..3; bit k of byte lx is voxel
+  // lx + (k & 1) of row (ly + (k >> 1 & 1), lz + (k >> 2)). Per k the four
+  // bits (one per lx) are spread to bit positions 0, 8, 16, 24 at once: the
+  // product r * 0x204081 places copies of the 4-bit r at shifts 0, 7, 14, 21
+  // without carries, and the mask keeps bit j of the copy at shift 7j.
   uint32_t words[16];
 #pragma unroll
   for (int lz = 0; lz < 4; ++lz)
@@ -220,11 +225,9 @@ __global__ void __launch_bounds__(256) corners_kernel(int N, int log2n, const ui
     for (int ly = 0; ly < 4; ++ly) {
       uint32_t wv = 0;
 #pragma unroll
-      for (int lx = 0; lx < 4; ++lx) {
-        uint32_t b = 0;
-#pragma unroll
-        for (int k = 0; k < 8; ++k) b |= ((rows[lz + (k >> 2)][ly + ((k >> 1) & 1)] >> (lx + (k & 1))) & 1u) << k;
-        wv |= b << (8 * lx);
+      for (int k = 0; k < 8; ++k) {
+        const uint32_t r = (rows[lz + (k >> 2)][ly + ((k >> 1) & 1)] >> (k & 1)) & 0xFu;
+        wv |= ((r * 0x204081u) & 0x01010101u) << k;
       }
       words[lz * 4 + ly] = wv;
     }
@@ -246,7 +249,9 @@ cudaError_t launch_build_corners(cudaStream_t s, int n, const uint32_t* bits, ui
 cudaError_t launch_voxelize(cudaStream_t s, const DrvBox* boxes, int n_boxes, const DrvVolumeInfo& vol, int n,
                             uint32_t* bits) {
   if (n_boxes > kMaxBoxes || n < 32 || (n & 31)) return cudaErrorInvalidValue;
-  voxelize_kernel<<<n, 256, 0, s>>>(boxes, n_boxes, vol, n, bits);
+  cudaError_t e = cudaMemsetAsync(bits, 0, (size_t)n * n * (n / 32) * sizeof(uint32_t), s);
+  if (e != cudaSuccess || n_boxes == 0) return e;
+  voxelize_kernel<<<dim3(n_boxes * 6, kVoxelSplit), 256, 0, s>>>(boxes, vol, n, bits);
   return cudaGetLastError();
 }
 

@@ -44,14 +44,18 @@ StageParams make_stage_params(const DrvConfig& cfg, const DrvVolumeInfo& vol, co
 cudaError_t launch_surrogate_mlp(cudaStream_t s, const StageParams& p, const PairList& L, const void* weights,
                                  float conf_threshold, bool bf16, int num_sms);
 
-// Host: persistent launch (SMs x resident CTAs per SM) of a kernel.
+// Host: resident CTAs per SM of a kernel at this block size and dynamic
+// shared memory, queried once per (kernel, block, smem) and device.
+int resident_ctas(const void* kernel, int threads, size_t smem);
+
+// Host: persistent launch (SMs x resident CTAs per SM, capped at
+// ctas_per_sm when that is positive) of a kernel.
 template <typename... KArgs, typename... Args>
 cudaError_t launch_persistent(void (*kernel)(KArgs...), int threads, size_t smem, cudaStream_t s, int num_sms,
                               const Args&... args) {
-  int per_sm = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
-  if (e != cudaSuccess) return e;
-  kernel<<<num_sms * (per_sm < 1 ? 1 : per_sm), threads, smem, s>>>(args...);
+  const int per_sm = resident_ctas(reinterpret_cast<const void*>(kernel), threads, smem);
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  kernel<<<num_sms * per_sm, threads, smem, s>>>(args...);
   return cudaGetLastError();
 }
 
