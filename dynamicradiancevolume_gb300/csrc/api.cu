@@ -176,11 +176,11 @@ drv_status drv_create(const DrvConfig* cfg, DrvContext** out) {
   }
   if ((e = cudaMalloc(&c->sur_weights, drv::surrogate_weights_bytes())) != cudaSuccess) return bail(e);
   // Pair list of the split light stage: room for 64 contributing shadow
-  // blocks per cache on average (clamped to [2^20, 2^25] pairs, 20 B each);
+  // blocks per cache on average (clamped to [2^20, 2^25] pairs, 21 B each);
   // caches beyond a full list are traced by the gather itself.
   {
     const uint64_t cap = std::min<uint64_t>(std::max<uint64_t>((uint64_t)cfg->max_caches * 64u, 1u << 20), 1u << 25);
-    const size_t bytes = (size_t)cap * 20 + (size_t)cfg->max_caches * 8 + 32;
+    const size_t bytes = (size_t)cap * 21 + (size_t)cfg->max_caches * 8 + drv::kPairCounters * 4;
     if ((e = cudaMalloc(&c->pair_mem, bytes)) != cudaSuccess) return bail(e);
     if ((e = cudaMemset(c->pair_mem, 0, bytes)) != cudaSuccess) return bail(e);
     uint32_t* w = static_cast<uint32_t*>(c->pair_mem);
@@ -191,6 +191,7 @@ drv_status drv_create(const DrvConfig* cfg, DrvContext** out) {
     c->pairs.retrace = w + 4 * cap;
     c->pairs.info = w + 5 * cap;
     c->pairs.counters = w + 5 * cap + 2 * (size_t)cfg->max_caches;
+    c->pairs.cls = reinterpret_cast<uint8_t*>(c->pairs.counters + drv::kPairCounters);
     c->pairs.cap = (uint32_t)cap;
   }
   c->box_capacity = 512;

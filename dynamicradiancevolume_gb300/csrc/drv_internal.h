@@ -50,22 +50,26 @@ struct LightScratch {
 // light stage. Pair i: cache[i], block[i] (kNoPair: unused slot), shadow[i].
 // info[c] = {first pair of cache c, pair count} (count kPairOverflow: the
 // list was full, the gather traces that cache's cones itself).
-// order and retrace list pair indices in the order their cones are traced:
-// narrow cones (every sample on voxel level 0) from the front, wide cones
-// from the back, so that a warp's lanes take the same sampling path.
-// counters (zeroed before each light stage): [0] pairs claimed, [1] narrow
-// and [2] wide cones in order, [3] narrow and [4] wide cones in retrace (the
-// pairs the surrogate is not confident about), [5] pairs the surrogate
-// evaluated.
+// order lists all pairs by cone class (kConeClasses classes of expected
+// step count and width, cls[i]), so that a warp's lanes march cones of one
+// length that take one sampling path; retrace lists the pairs the surrogate
+// is not confident about, narrow cones (every sample on voxel level 0) from
+// its front, wide ones from its back.
+// counters (zeroed before each light stage): [0] pairs claimed, [3] narrow
+// and [4] wide cones in retrace, [5] pairs the surrogate evaluated,
+// [8 + c] pairs of class c, [8 + kConeClasses + c] class c's scatter cursor.
 constexpr uint32_t kNoPair = 0xFFFFFFFFu;
 constexpr uint32_t kPairOverflow = 0xFFFFFFFFu;
 constexpr int kMaxSplitBlocks = 65536;  // shadow blocks per frame the split stage handles
+constexpr int kConeClasses = 16;
+constexpr int kPairCounters = 8 + 2 * kConeClasses;
 struct PairList {
   uint32_t* cache;
   uint32_t* block;
   float* shadow;
   uint32_t* order;
   uint32_t* retrace;
+  uint8_t* cls;
   uint32_t* info;
   uint32_t* counters;
   uint32_t cap;

@@ -13,13 +13,14 @@
 //  1. cull_kernel (a CTA per cache): tests every block against the cache and
 //     writes the cache's contributing blocks, in block order, to one
 //     contiguous run of a global pair list (one atomic per cache claims it);
-//  2. cone_kernel (a thread per pair, persistent grid): traces the pair's
-//     cone and stores its shadowing — every warp holds 32 pairs, so no lane
-//     idles on a block that needs no cone, and narrow cones (all samples on
-//     voxel level 0) are traced apart from wide ones (mip samples), so a
-//     warp's lanes take one sampling path; with the learned surrogate, the
-//     MLP (k_light_surrogate.cu) fills in the shadowing first and only the
-//     pairs it is not confident about come here;
+//  2. classify_kernel + scatter_kernel order the pairs by cone class (the
+//     number of steps the cone marches and whether it reaches mip samples),
+//     and cone_kernel (a thread per pair, persistent grid) traces the cones
+//     in that order and stores each pair's shadowing: every warp holds 32
+//     pairs, no lane idles on a block that needs no cone, and a warp's lanes
+//     march cones of one length along one sampling path; with the learned
+//     surrogate, the MLP (k_light_surrogate.cu) fills in the shadowing first
+//     and only the pairs it is not confident about are traced;
 //  3. gather_kernel (a CTA per cache): each thread gathers a fixed subset of
 //     the cache's pairs with their shadowing into SH partial sums in
 //     registers, reduced in a fixed order — the result does not depend on
@@ -137,19 +138,15 @@ __device__ __forceinline__ void gather_block(const StageParams& p, float* acc, f
 constexpr int kCullThreads = 256;
 constexpr int kCullWarps = kCullThreads / 32;
 
-// CTA per cache: contributing blocks -> a contiguous run of the pair list,
-// and their indices -> the narrow or the wide end of the cone order.
+// CTA per cache: contributing blocks -> a contiguous run of the pair list.
 template <bool BF16>
 __global__ void __launch_bounds__(kCullThreads) cull_kernel(StageParams p, PairList L) {
-  // [W] live words, [W] wide words, [W] exclusive prefix of live counts, [W] of wide counts
-  extern __shared__ uint32_t s_dyn[];
-  __shared__ uint32_t s_warp[2][kCullWarps];
-  __shared__ uint32_t s_base[3], s_over;
+  extern __shared__ uint32_t s_dyn[];  // [W] ballot words, [W] exclusive prefix of their popcounts
+  __shared__ uint32_t s_warp[kCullWarps];
+  __shared__ uint32_t s_base, s_count;
   const int W = (p.total_blocks + 31) >> 5;
-  uint32_t* s_live = s_dyn;
-  uint32_t* s_wide = s_dyn + W;
-  uint32_t* s_pre = s_dyn + 2 * W;
-  uint32_t* s_prew = s_dyn + 3 * W;
+  uint32_t* s_mask = s_dyn;
+  uint32_t* s_pre = s_dyn + W;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int per = (W + kCullThreads - 1) / kCullThreads;  // words per thread in the scan
   const uint32_t n_caches = cache_count(p);
@@ -159,86 +156,52 @@ __global__ void __launch_bounds__(kCullThreads) cull_kernel(StageParams p, PairL
     for (int w = warp; w < W; w += kCullWarps) {
       const int b = (w << 5) + lane;
       const bool live = b < p.total_blocks && block_live<BF16>(p, b, cx, cy, cz);
-      bool wide = false;
-      if (live) {
-        const int l = block_light(p, b);
-        wide = wide_cone(__ldg(reinterpret_cast<const float*>(p.ll.lights[l].cones + (b - p.block_base[l])) + 3),
-                         p.max_steps);
-      }
-      const uint32_t m = __ballot_sync(0xffffffffu, live), mw = __ballot_sync(0xffffffffu, wide);
-      if (lane == 0) {
-        s_live[w] = m;
-        s_wide[w] = mw;
-      }
+      const uint32_t m = __ballot_sync(0xffffffffu, live);
+      if (lane == 0) s_mask[w] = m;
     }
     __syncthreads();
-    // Exclusive scans of the live and wide counts (thread t owns words [t*per, t*per + per)).
+    // Exclusive scan of the word popcounts (thread t owns words [t*per, t*per + per)).
     const int w0 = threadIdx.x * per;
-    uint32_t local = 0, localw = 0;
+    uint32_t local = 0;
     for (int k = 0; k < per; ++k)
-      if (w0 + k < W) {
-        local += __popc(s_live[w0 + k]);
-        localw += __popc(s_wide[w0 + k]);
-      }
-    uint32_t incl = local, inclw = localw;
+      if (w0 + k < W) local += __popc(s_mask[w0 + k]);
+    uint32_t incl = local;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o), tw = __shfl_up_sync(0xffffffffu, inclw, o);
-      if (lane >= o) {
-        incl += t;
-        inclw += tw;
-      }
+      const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
     }
-    if (lane == 31) {
-      s_warp[0][warp] = incl;
-      s_warp[1][warp] = inclw;
-    }
+    if (lane == 31) s_warp[warp] = incl;
     __syncthreads();
-    uint32_t run = incl - local, runw = inclw - localw, total = 0, totalw = 0;
+    uint32_t run = incl - local, total = 0;
 #pragma unroll
     for (int k = 0; k < kCullWarps; ++k) {
-      const uint32_t v = s_warp[0][k], vw = s_warp[1][k];
-      if (k < warp) {
-        run += v;
-        runw += vw;
-      }
+      const uint32_t v = s_warp[k];
+      if (k < warp) run += v;
       total += v;
-      totalw += vw;
     }
     for (int k = 0; k < per; ++k)
       if (w0 + k < W) {
         s_pre[w0 + k] = run;
-        s_prew[w0 + k] = runw;
-        run += __popc(s_live[w0 + k]);
-        runw += __popc(s_wide[w0 + k]);
+        run += __popc(s_mask[w0 + k]);
       }
     if (threadIdx.x == 0) {
       const uint32_t base = total ? atomicAdd(L.counters, total) : 0u;
       const bool over = (uint64_t)base + total > (uint64_t)L.cap;
       L.info[2 * c] = base;
       L.info[2 * c + 1] = over ? kPairOverflow : total;
-      s_base[0] = base;
-      s_over = over;
-      if (!over) {
-        s_base[1] = total - totalw ? atomicAdd(L.counters + 1, total - totalw) : 0u;
-        s_base[2] = totalw ? atomicAdd(L.counters + 2, totalw) : 0u;
-      }
+      s_base = base;
+      s_count = over ? kPairOverflow : total;
     }
     __syncthreads();
-    const uint32_t base = s_base[0];
-    if (!s_over) {
-      const uint32_t base_n = s_base[1], base_w = s_base[2];
+    const uint32_t base = s_base;
+    if (s_count != kPairOverflow) {
       for (int w = warp; w < W; w += kCullWarps) {
-        const uint32_t m = s_live[w], mw = s_wide[w];
+        const uint32_t m = s_mask[w];
         if ((m >> lane) & 1u) {
-          const uint32_t below = (1u << lane) - 1u;
-          const uint32_t i = base + s_pre[w] + __popc(m & below);
+          const uint32_t i = base + s_pre[w] + __popc(m & ((1u << lane) - 1u));
           L.cache[i] = c;
           L.block[i] = (uint32_t)((w << 5) + lane);
-          if ((mw >> lane) & 1u)
-            L.order[L.cap - 1u - (base_w + s_prew[w] + __popc(mw & below))] = i;
-          else
-            L.order[base_n + (s_pre[w] - s_prew[w]) + __popc(m & ~mw & below)] = i;
         }
       }
     } else {
@@ -251,12 +214,111 @@ __global__ void __launch_bounds__(kCullThreads) cull_kernel(StageParams p, PairL
   }
 }
 
-// Thread per cone, over a cone-order list: `ord` holds n_front narrow cones
-// from its front and n_back wide cones from its back (L.order after the
-// cull, or L.retrace after the surrogate).
+// Cone class of a pair: about how many steps its cone marches when nothing
+// occludes it, in buckets of 4, and whether its radius passes one voxel (mip
+// samples) on the way. cone_shadow steps by max(1, g * dist) with
+// g = 2 dsr / (1 - dsr): unit steps up to dist = 1 / g, then the distance
+// grows by the factor 1 + g per step, until it reaches the goal. Classes
+// only order the cones; results do not depend on them.
+__device__ __forceinline__ int cone_class(float light_dist, float voxel_size, float dsr, int max_steps) {
+  const float goal = fmaxf(light_dist / voxel_size - 2.0f, 1.0f);
+  const float g = 2.0f * dsr / (1.0f - dsr);
+  const float m = g > 0.0f ? fmaxf(1.0f, floorf(1.0f / g)) : 3.0e38f;  // last unit step
+  float n, dist;
+  if (goal <= m) {
+    n = ceilf(goal);
+    dist = n;
+  } else {
+    const float r = __log2f(1.0f + g);
+    n = m + ceilf(__log2f(goal / m) / r);
+    dist = goal;
+  }
+  if (n > (float)max_steps) {
+    n = (float)max_steps;
+    dist = n <= m ? n : m * exp2f((n - m) * __log2f(1.0f + g));
+  }
+  const int len = min(max((int)n - 1, 0) >> 2, kConeClasses / 2 - 1);
+  return (dist * dsr > 1.0f ? kConeClasses / 2 : 0) + len;
+}
+
+constexpr int kClassThreads = 256;
+
+// Thread per listed pair: its cone class; class totals in counters[8 + c].
 template <bool BF16>
-__global__ void __launch_bounds__(128) cone_kernel(StageParams p, PairList L, const uint32_t* ord, int front_counter) {
-  const uint32_t nf = min(L.counters[front_counter], L.cap), nb = min(L.counters[front_counter + 1], L.cap);
+__global__ void __launch_bounds__(kClassThreads) classify_kernel(StageParams p, PairList L) {
+  __shared__ uint32_t s_hist[kConeClasses];
+  if (threadIdx.x < kConeClasses) s_hist[threadIdx.x] = 0u;
+  __syncthreads();
+  const uint32_t n = min(L.counters[0], L.cap);
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint32_t b = L.block[i];
+    uint8_t c = 0xFF;
+    if (b != kNoPair) {
+      float cx, cy, cz;
+      cache_position<BF16>(p, L.cache[i], cx, cy, cz);
+      const int l = block_light(p, (int)b);
+      const float4 cone = __ldg(reinterpret_cast<const float4*>(p.ll.lights[l].cones) + (b - p.block_base[l]));
+      const float tx = cone.x - cx, ty = cone.y - cy, tz = cone.z - cz;
+      c = (uint8_t)cone_class(sqrtf(tx * tx + ty * ty + tz * tz), p.voxel_size, cone.w, p.max_steps);
+      atomicAdd(&s_hist[c], 1u);
+    }
+    L.cls[i] = c;
+  }
+  __syncthreads();
+  if (threadIdx.x < kConeClasses && s_hist[threadIdx.x]) atomicAdd(L.counters + 8 + threadIdx.x, s_hist[threadIdx.x]);
+}
+
+constexpr int kScatterTile = 4 * kClassThreads;
+
+// CTA per tile of kScatterTile pairs (4 per thread): each pair's index goes
+// to its class's region of L.order (regions in class order); a CTA reserves
+// its share of each region with one atomic per class.
+__global__ void __launch_bounds__(kClassThreads) scatter_kernel(PairList L) {
+  __shared__ uint32_t s_region[kConeClasses], s_hist[kConeClasses], s_pos[kConeClasses];
+  const uint32_t n = min(L.counters[0], L.cap);
+  if (threadIdx.x < kConeClasses) {
+    uint32_t region = 0;
+    for (int k = 0; k < (int)threadIdx.x; ++k) region += L.counters[8 + k];
+    s_region[threadIdx.x] = region;
+  }
+  for (uint32_t t0 = blockIdx.x * kScatterTile; t0 < n; t0 += gridDim.x * kScatterTile) {
+    if (threadIdx.x < kConeClasses) s_hist[threadIdx.x] = 0u;
+    __syncthreads();
+    uint8_t c[4];
+    uint32_t rank[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const uint32_t i = t0 + j * kClassThreads + threadIdx.x;
+      c[j] = i < n ? L.cls[i] : (uint8_t)0xFF;
+      rank[j] = c[j] != 0xFF ? atomicAdd(&s_hist[c[j]], 1u) : 0u;
+    }
+    __syncthreads();
+    if (threadIdx.x < kConeClasses) {
+      const uint32_t h = s_hist[threadIdx.x];
+      s_pos[threadIdx.x] = s_region[threadIdx.x] + (h ? atomicAdd(L.counters + 8 + kConeClasses + threadIdx.x, h) : 0u);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (c[j] != 0xFF) L.order[s_pos[c[j]] + rank[j]] = t0 + j * kClassThreads + threadIdx.x;
+    __syncthreads();
+  }
+}
+
+// Thread per cone, over a cone-order list. RETRACE: L.retrace, its n_front
+// narrow cones from the front and n_back wide ones from the back; otherwise
+// L.order, every listed pair in class order.
+template <bool BF16, bool RETRACE>
+__global__ void __launch_bounds__(128) cone_kernel(StageParams p, PairList L) {
+  uint32_t nf = 0, nb = 0;
+  if (RETRACE) {
+    nf = min(L.counters[3], L.cap);
+    nb = min(L.counters[4], L.cap);
+  } else {
+#pragma unroll
+    for (int c = 0; c < kConeClasses; ++c) nf += L.counters[8 + c];
+  }
+  const uint32_t* ord = RETRACE ? L.retrace : L.order;
   const uint32_t n = min(nf + nb, L.cap);
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     const uint32_t i = k < nf ? ord[k] : ord[L.cap - 1u - (k - nf)];
@@ -437,15 +499,17 @@ cudaError_t launch_grid(void (*kernel)(KArgs...), int threads, size_t smem, cuda
 template <int NK, bool BF16>
 cudaError_t split_variant(cudaStream_t s, const StageParams& p, const PairList& L, const void* weights,
                           float conf_threshold, int cone_ctas, int gather_ctas, int num_sms) {
-  cudaError_t e = cudaMemsetAsync(L.counters, 0, 8 * sizeof(uint32_t), s);
+  cudaError_t e = cudaMemsetAsync(L.counters, 0, kPairCounters * sizeof(uint32_t), s);
   if (e != cudaSuccess) return e;
-  const size_t cull_smem = (size_t)((p.total_blocks + 31) >> 5) * 4 * sizeof(uint32_t);
+  const size_t cull_smem = (size_t)((p.total_blocks + 31) >> 5) * 2 * sizeof(uint32_t);
   if ((e = launch_persistent(cull_kernel<BF16>, kCullThreads, cull_smem, s, num_sms, p, L)) != cudaSuccess) return e;
   if (weights) {
     if ((e = launch_surrogate_mlp(s, p, L, weights, conf_threshold, BF16, num_sms)) != cudaSuccess) return e;
-    e = launch_grid(cone_kernel<BF16>, 128, 0, s, num_sms, cone_ctas, p, L, (const uint32_t*)L.retrace, 3);
+    e = launch_grid(cone_kernel<BF16, true>, 128, 0, s, num_sms, cone_ctas, p, L);
   } else {
-    e = launch_grid(cone_kernel<BF16>, 128, 0, s, num_sms, cone_ctas, p, L, (const uint32_t*)L.order, 1);
+    if ((e = launch_persistent(classify_kernel<BF16>, kClassThreads, 0, s, num_sms, p, L)) != cudaSuccess) return e;
+    if ((e = launch_persistent(scatter_kernel, kClassThreads, 0, s, num_sms, L)) != cudaSuccess) return e;
+    e = launch_grid(cone_kernel<BF16, false>, 128, 0, s, num_sms, cone_ctas, p, L);
   }
   if (e != cudaSuccess) return e;
   return launch_grid(gather_kernel<NK, BF16>, kGatherThreads, 0, s, num_sms, gather_ctas, p, L);
