@@ -48,6 +48,7 @@ void release(Context* c) {
   cudaFree(c->voxel_bits);
   cudaFree(c->mips);
   cudaFree(c->vox_corners);
+
   cudaFree(c->light_scratch);
   cudaFree(c->light_tickets);
   cudaFree(c->sur_weights);
@@ -90,9 +91,13 @@ drv_status validate_config(const DrvConfig* c, std::string& why) {
   return DRV_OK;
 }
 
+// Texel arrays must be aligned to their texel's scalar (the RG16I normal is
+// read as one 32-bit word per pixel).
 bool views_ok(const DrvGBufferView* g, const DrvConfig& c) {
   return g && g->depth && g->normal && g->albedo && g->width == c.width && g->height == c.height &&
-         (g->normal_format == DRV_NORMAL_RG16I || g->normal_format == DRV_NORMAL_F32X3);
+         (g->normal_format == DRV_NORMAL_RG16I || g->normal_format == DRV_NORMAL_F32X3) &&
+         reinterpret_cast<uintptr_t>(g->depth) % 4 == 0 && reinterpret_cast<uintptr_t>(g->normal) % 4 == 0 &&
+         reinterpret_cast<uintptr_t>(g->albedo) % 4 == 0;
 }
 
 }  // namespace
@@ -154,6 +159,7 @@ drv_status drv_create(const DrvConfig* cfg, DrvContext** out) {
   }
   if ((e = cudaMalloc(&c->mips, off * 4)) != cudaSuccess) return bail(e);
   if ((e = cudaMalloc(&c->vox_corners, (size_t)N * N * N)) != cudaSuccess) return bail(e);
+
   // Light-stage chunk partials and per-cache tickets (tickets are reset by the
   // kernel that consumes them, so they are zeroed once here).
   if ((e = cudaMalloc(&c->light_scratch, (size_t)cfg->max_caches * drv::kMaxLightChunks * (cfg->sh_order == 2 ? 27 : 12) * 4)) !=
@@ -411,8 +417,8 @@ drv_status drv_light_caches(DrvContext* ctx, const DrvSpotLight* lights, int32_t
     drv::PairList pairs = ctx->pairs;
     if (ctx->tuning.pair_capacity) pairs.cap = std::min(pairs.cap, ctx->tuning.pair_capacity);
     return cuda_check(ctx, drv::launch_light_split(ctx->s(), ctx->cfg, *vol, ll, ctx->counter, ctx->entries,
-                                                   ctx->entry_stride, ctx->vox_corners, ctx->mips, ctx->mip_offset,
-                                                   pairs, surrogate ? ctx->sur_weights : nullptr,
+                                                   ctx->entry_stride, ctx->voxels(), pairs,
+                                                   surrogate ? ctx->sur_weights : nullptr,
                                                    ctx->tuning.cone_ctas_per_sm, ctx->tuning.gather_ctas_per_sm,
                                                    ctx->num_sms),
                       "light_caches");
@@ -424,8 +430,7 @@ drv_status drv_light_caches(DrvContext* ctx, const DrvSpotLight* lights, int32_t
   if (surrogate && blocks > drv::kMaxSplitBlocks)
     return fail(ctx, DRV_ERR_INVALID_ARG, "surrogate visibility supports at most 65536 shadow blocks per frame");
   return cuda_check(ctx, drv::launch_light_caches(ctx->s(), ctx->cfg, *vol, ll, ctx->counter, ctx->entries,
-                                                  ctx->entry_stride, ctx->vox_corners, ctx->mips, ctx->mip_offset,
-                                                  scratch, ctx->num_sms),
+                                                  ctx->entry_stride, ctx->voxels(), scratch, ctx->num_sms),
                     "light_caches");
 }
 
@@ -523,8 +528,8 @@ drv_status drv_surrogate_make_pairs(DrvContext* ctx, uint64_t seed, int32_t n_pa
     ll.lights[l].interval = ctx->interval[l];
   }
   return cuda_check(ctx, drv::launch_surrogate_pairs(ctx->s(), ctx->cfg, ctx->last_volume, ll, ctx->counter,
-                                                     ctx->entries, ctx->entry_stride, ctx->vox_corners, ctx->mips,
-                                                     ctx->mip_offset, seed, n_pairs, features, targets),
+                                                     ctx->entries, ctx->entry_stride, ctx->voxels(), seed, n_pairs,
+                                                     features, targets),
                     "surrogate_make_pairs");
 }
 

@@ -36,6 +36,13 @@ struct LightLaunch {
   int n_lights;
 };
 
+// The voxel pyramid as the cone tracer reads it.
+struct VoxelInputs {
+  const uint8_t* corners = nullptr;     // level 0, corner-packed bytes in 4^3 bricks
+  const void* mips = nullptr;           // levels 1..L concatenated (float, or half with BF16 precision)
+  const size_t* mip_offsets = nullptr;  // texel offset of each level in mips
+};
+
 // Device scratch of the light stage. partials: [max_caches * max_chunks][27]
 // chunk sums; tickets: one per cache; work: {next unit, retired CTAs}. Tickets
 // and work are zero between launches (each launch leaves them zero).
@@ -106,6 +113,7 @@ struct Context {
   uint8_t* vox_corners = nullptr;  // level 0, corner-packed bytes in 4^3 bricks
   void* mips = nullptr;  // levels 1..L concatenated: float (FP32 precision) or half (BF16 precision)
   size_t mip_offset[kMaxVoxelLevels] = {};
+  VoxelInputs voxels() const { return VoxelInputs{vox_corners, mips, mip_offset}; }
   int n_voxel_levels = 0;
   // RSM + VPLs per light.
   RsmChain rsm[DRV_MAX_LIGHTS];
@@ -155,16 +163,14 @@ cudaError_t launch_allocate(cudaStream_t s, const DrvConfig& cfg, const DrvVolum
                             DrvCacheCounter* counter, uint32_t* ticket, uint32_t* err);
 cudaError_t launch_light_caches(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const LightLaunch& ll,
                                 const DrvCacheCounter* counter, void* entries, uint32_t entry_stride,
-                                const uint8_t* corners, const void* mips, const size_t* mip_offsets,
-                                const LightScratch& scratch, int num_sms);
+                                const VoxelInputs& vox, const LightScratch& scratch, int num_sms);
 // Split light stage: cull -> (cones | surrogate MLP + cones of the
 // unconfident pairs) -> gather. weights == nullptr: plain cones.
 bool light_split_supported(const DrvConfig& cfg, const LightLaunch& ll);
 cudaError_t launch_light_split(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const LightLaunch& ll,
                                const DrvCacheCounter* counter, void* entries, uint32_t entry_stride,
-                               const uint8_t* corners, const void* mips, const size_t* mip_offsets,
-                               const PairList& pairs, const void* weights, int cone_ctas_per_sm,
-                               int gather_ctas_per_sm, int num_sms);
+                               const VoxelInputs& vox, const PairList& pairs, const void* weights,
+                               int cone_ctas_per_sm, int gather_ctas_per_sm, int num_sms);
 cudaError_t launch_apply(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const DrvPerFrame& f,
                          const DrvGBufferView& g, const uint32_t* atlas, const void* entries, uint32_t entry_stride,
                          const DrvCacheCounter* counter, float* out_rgb);
@@ -175,9 +181,8 @@ cudaError_t launch_pack_surrogate_weights(cudaStream_t s, const float* params, v
 cudaError_t launch_surrogate_eval(cudaStream_t s, const void* weights, const float* X, int n, float* out);
 cudaError_t launch_surrogate_pairs(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol,
                                    const LightLaunch& ll, const DrvCacheCounter* counter, const void* entries,
-                                   uint32_t entry_stride, const uint8_t* corners, const void* mips,
-                                   const size_t* mip_offsets, uint64_t seed, int n_pairs, float* features,
-                                   float* targets);
+                                   uint32_t entry_stride, const VoxelInputs& vox, uint64_t seed, int n_pairs,
+                                   float* features, float* targets);
 cudaError_t launch_surrogate_train_step(cudaStream_t s, const float* X, const float* Y, int n, float* params,
                                         float* m, float* v, float* scratch, int step, float lr, float conf_tau,
                                         float weight_decay, float* loss_out);

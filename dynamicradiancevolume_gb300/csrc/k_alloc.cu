@@ -1,8 +1,8 @@
 // k_alloc.cu — Renderer::AllocateCaches (renderer.cpp:951-992):
 // cacheGather.comp (16x16 workgroups, shared-memory neighbour dedupe, corner
 // lock by compare-and-swap, compaction by an atomic counter) and
-// cachePrepareLighting.comp (indirect-dispatch arguments), the latter folded
-// into the last CTA of the same launch through a completion ticket.
+// cachePrepareLighting.comp (indirect-dispatch arguments, a one-thread
+// launch after it).
 #include "drv_device.cuh"
 #include "drv_internal.h"
 
@@ -24,7 +24,6 @@ struct AllocParams {
   int entry_vec4;  // entry stride in float4 units
   int bf16;        // DrvCacheEntryBF16 entries (cell key + BF16 SH) instead of LightCacheEntry
   DrvCacheCounter* counter;
-  uint32_t* ticket;
   uint32_t* err;
 };
 
@@ -85,7 +84,7 @@ __global__ void __launch_bounds__(kTile* kTile) allocate_kernel(AllocParams p) {
   __syncthreads();
   int own = -1, own2 = -1, cascade = -1;
   if (px < p.w && py < p.h) {
-    float d = p.depth[(size_t)py * p.w + px];
+    float d = __ldcs(p.depth + (size_t)py * p.w + px);  // read once: streaming
     if (d > 0.0001f) {
       float wp[3];
       reconstruct_world(p.frame, px, py, p.w, p.h, d, wp);
@@ -119,26 +118,21 @@ __global__ void __launch_bounds__(kTile* kTile) allocate_kernel(AllocParams p) {
     if (((list2[lx][dy] != own2 && list2[dx][ly] != own2 && list2[dx][dy] != own2) || corner) && own2 != -1)
       allocate_cell(p, own2, cascade + 1);
   }
-  // cachePrepareLighting.comp, run by the last CTA to finish.
-  __threadfence();
-  __syncthreads();
-  if (lx == 0 && ly == 0) {
-    const uint32_t n_blocks = gridDim.x * gridDim.y;
-    if (atomicAdd(p.ticket, 1u) == n_blocks - 1u) {
-      int count = atomicAdd(&p.counter->total_light_cache_count, 0);
-      uint32_t lit = min((uint32_t)count, p.max_caches);
-      p.counter->groups_x = (lit + DRV_LIGHTING_THREADS_PER_GROUP - 1) / DRV_LIGHTING_THREADS_PER_GROUP;
-      p.counter->groups_y = 1;
-      p.counter->groups_z = 1;
-    }
-  }
+}
+
+// cachePrepareLighting.comp: dispatch size of the lighting pass.
+__global__ void prepare_lighting_kernel(DrvCacheCounter* counter, uint32_t max_caches) {
+  const uint32_t lit = min((uint32_t)max(counter->total_light_cache_count, 0), max_caches);
+  counter->groups_x = (lit + DRV_LIGHTING_THREADS_PER_GROUP - 1) / DRV_LIGHTING_THREADS_PER_GROUP;
+  counter->groups_y = 1;
+  counter->groups_z = 1;
 }
 
 }  // namespace
 
 cudaError_t launch_allocate(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const DrvPerFrame& f,
                             const float* depth, int w, int h, uint32_t* atlas, void* entries, uint32_t entry_stride,
-                            DrvCacheCounter* counter, uint32_t* ticket, uint32_t* err) {
+                            DrvCacheCounter* counter, uint32_t* /*ticket: unused*/, uint32_t* err) {
   AllocParams p;
   p.vol = vol;
   p.frame = f;
@@ -154,10 +148,10 @@ cudaError_t launch_allocate(cudaStream_t s, const DrvConfig& cfg, const DrvVolum
   p.entry_vec4 = (int)(entry_stride / 16);
   p.bf16 = cfg.precision == DRV_PRECISION_BF16;
   p.counter = counter;
-  p.ticket = ticket;
   p.err = err;
   dim3 block(kTile, kTile), grid((w + kTile - 1) / kTile, (h + kTile - 1) / kTile);
   allocate_kernel<<<grid, block, 0, s>>>(p);
+  prepare_lighting_kernel<<<1, 1, 0, s>>>(counter, cfg.max_caches);
   return cudaGetLastError();
 }
 

@@ -126,26 +126,30 @@ __global__ void __launch_bounds__(256) apply_kernel(ApplyParams p) {
   if (x >= p.w || y >= p.h) return;
   const size_t i = (size_t)y * p.w + x;
   float* o = p.out + 3 * i;
-  const float d = __ldg(p.depth + i);
+  // G-buffer texels are read once and the output written once: streaming
+  // (evict-first) accesses keep L1/L2 for the atlas and the cache entries.
+  const float d = __ldcs(p.depth + i);
   if (d < 0.00001f) {  // cacheApply.frag:304-307 (discard)
-    o[0] = o[1] = o[2] = 0.0f;
+    __stcs(o, 0.0f);
+    __stcs(o + 1, 0.0f);
+    __stcs(o + 2, 0.0f);
     return;
   }
+  f3 n;
+  if (p.normal_format == DRV_NORMAL_RG16I) {
+    const int q = __ldcs(reinterpret_cast<const int*>(p.normal) + i);  // two int16, x in the low half
+    n = unpack_normal16i((int16_t)(q & 0xFFFF), (int16_t)(q >> 16));
+  } else {
+    const float* q = reinterpret_cast<const float*>(p.normal) + 3 * i;
+    n = mkf3(__ldcs(q), __ldcs(q + 1), __ldcs(q + 2));
+  }
+  const float inv_pi = 1.0f / DRV_SHADER_PI;
+  const f3 alb = mkf3(__ldcs(p.albedo + 3 * i) * inv_pi, __ldcs(p.albedo + 3 * i + 1) * inv_pi,
+                      __ldcs(p.albedo + 3 * i + 2) * inv_pi);
   const uint32_t n_caches = min((uint32_t)max(p.counter->total_light_cache_count, 0), p.max_caches);
   float wp[3];
   reconstruct_world(p.frame, x, y, p.w, p.h, d, wp);
   const int c = select_cascade(p.vol, p.n_cascades, wp);
-  f3 n;
-  if (p.normal_format == DRV_NORMAL_RG16I) {
-    const int16_t* q = reinterpret_cast<const int16_t*>(p.normal) + 2 * i;
-    n = unpack_normal16i(q[0], q[1]);
-  } else {
-    const float* q = reinterpret_cast<const float*>(p.normal) + 3 * i;
-    n = mkf3(q[0], q[1], q[2]);
-  }
-  const float inv_pi = 1.0f / DRV_SHADER_PI;
-  const f3 alb = mkf3(__ldg(p.albedo + 3 * i) * inv_pi, __ldg(p.albedo + 3 * i + 1) * inv_pi,
-                      __ldg(p.albedo + 3 * i + 2) * inv_pi);
   f3 irr = lighting<BF16, SH2>(p, wp, c, n, n_caches);
   f3 col = mkf3(irr.x * alb.x, irr.y * alb.y, irr.z * alb.z);
   if (p.transitions) {
@@ -156,9 +160,9 @@ __global__ void __launch_bounds__(256) apply_kernel(ApplyParams p) {
       col = col * (1.0f - t) + col2 * t;  // mix(), cacheApply.frag:359
     }
   }
-  o[0] = col.x;
-  o[1] = col.y;
-  o[2] = col.z;
+  __stcs(o, col.x);
+  __stcs(o + 1, col.y);
+  __stcs(o + 2, col.z);
 }
 
 }  // namespace

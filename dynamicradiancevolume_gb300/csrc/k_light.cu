@@ -43,7 +43,7 @@ namespace drv {
 
 StageParams make_stage_params(const DrvConfig& cfg, const DrvVolumeInfo& vol, const LightLaunch& ll,
                               const DrvCacheCounter* counter, void* entries, uint32_t entry_stride,
-                              const uint8_t* corners, const void* mips, const size_t* mip_offsets) {
+                              const VoxelInputs& vox) {
   StageParams p;
   p.ll = ll;
   p.shadow = cfg.indirect_shadow;
@@ -55,15 +55,7 @@ StageParams make_stage_params(const DrvConfig& cfg, const DrvVolumeInfo& vol, co
   for (int l = ll.n_lights; l <= DRV_MAX_LIGHTS; ++l) p.block_base[l] = base;
   p.total_blocks = base;
   p.max_steps = cfg.max_cone_steps;
-  int L = 0;
-  while ((1 << (L + 1)) <= cfg.voxel_res) ++L;
-  p.vox.corners = corners;
-  p.vox.mips = mips;
-  for (int i = 0; i < 16; ++i) p.vox.off[i] = (uint32_t)(i < kMaxVoxelLevels && mip_offsets ? mip_offsets[i] : 0);
-  p.vox.N = cfg.voxel_res;
-  p.vox.log2n = L;
-  p.vox.max_level = L;
-  p.vox.half_mips = cfg.precision == DRV_PRECISION_BF16;
+  p.vox = make_voxel_view(cfg, vox);
   for (int i = 0; i < 3; ++i) p.vol_min[i] = vol.volume_world_min[i];
   p.voxel_size = vol.voxel_size_in_world;
   p.inv_extent = 1.0f / (p.voxel_size * (float)cfg.voxel_res);
@@ -544,10 +536,9 @@ int light_chunks(int total_blocks, int max_chunks) {
 
 cudaError_t launch_light_caches(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const LightLaunch& ll,
                                 const DrvCacheCounter* counter, void* entries, uint32_t entry_stride,
-                                const uint8_t* corners, const void* mips, const size_t* mip_offsets,
-                                const LightScratch& scratch, int num_sms) {
+                                const VoxelInputs& vox, const LightScratch& scratch, int num_sms) {
   FusedParams fp;
-  fp.s = make_stage_params(cfg, vol, ll, counter, entries, entry_stride, corners, mips, mip_offsets);
+  fp.s = make_stage_params(cfg, vol, ll, counter, entries, entry_stride, vox);
   fp.n_chunks = light_chunks(fp.s.total_blocks, scratch.max_chunks);
   fp.chunk_blocks = (fp.s.total_blocks + fp.n_chunks - 1) / fp.n_chunks;
   fp.scratch = scratch.partials;
@@ -570,10 +561,9 @@ bool light_split_supported(const DrvConfig& cfg, const LightLaunch& ll) {
 
 cudaError_t launch_light_split(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const LightLaunch& ll,
                                const DrvCacheCounter* counter, void* entries, uint32_t entry_stride,
-                               const uint8_t* corners, const void* mips, const size_t* mip_offsets,
-                               const PairList& pairs, const void* weights, int cone_ctas_per_sm,
-                               int gather_ctas_per_sm, int num_sms) {
-  const StageParams p = make_stage_params(cfg, vol, ll, counter, entries, entry_stride, corners, mips, mip_offsets);
+                               const VoxelInputs& vox, const PairList& pairs, const void* weights,
+                               int cone_ctas_per_sm, int gather_ctas_per_sm, int num_sms) {
+  const StageParams p = make_stage_params(cfg, vol, ll, counter, entries, entry_stride, vox);
   const float thr = cfg.surrogate_conf_threshold;
   const bool bf16 = cfg.precision == DRV_PRECISION_BF16;
   if (cfg.sh_order == 2)

@@ -316,9 +316,8 @@ __global__ void __launch_bounds__(256) loss_sum_kernel(const float* __restrict__
 
 cudaError_t launch_surrogate_pairs(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol,
                                    const LightLaunch& ll, const DrvCacheCounter* counter, const void* entries,
-                                   uint32_t entry_stride, const uint8_t* corners, const void* mips,
-                                   const size_t* mip_offsets, uint64_t seed, int n_pairs, float* features,
-                                   float* targets) {
+                                   uint32_t entry_stride, const VoxelInputs& vox, uint64_t seed, int n_pairs,
+                                   float* features, float* targets) {
   PairParams p;
   p.ll = ll;
   int base = 0;
@@ -328,15 +327,7 @@ cudaError_t launch_surrogate_pairs(cudaStream_t s, const DrvConfig& cfg, const D
   }
   for (int l = ll.n_lights; l <= DRV_MAX_LIGHTS; ++l) p.block_base[l] = base;
   p.total_blocks = base;
-  int L = 0;
-  while ((1 << (L + 1)) <= cfg.voxel_res) ++L;
-  p.vox.corners = corners;
-  p.vox.mips = mips;
-  for (int i = 0; i < 16; ++i) p.vox.off[i] = (uint32_t)(i < kMaxVoxelLevels ? mip_offsets[i] : 0);
-  p.vox.N = cfg.voxel_res;
-  p.vox.log2n = L;
-  p.vox.max_level = L;
-  p.vox.half_mips = cfg.precision == DRV_PRECISION_BF16;
+  p.vox = make_voxel_view(cfg, vox);
   for (int i = 0; i < 3; ++i) p.vol_min[i] = vol.volume_world_min[i];
   p.voxel_size = vol.voxel_size_in_world;
   p.max_steps = cfg.max_cone_steps;

@@ -34,10 +34,25 @@ struct StageParams {
   float ev[5];  // ShEvaFactor0, 1, 2n2_p1_n1, 20, 2p2 (renderer.cpp:302-306)
 };
 
+// Host: the device view of a voxel pyramid of resolution cfg.voxel_res.
+inline VoxelView make_voxel_view(const DrvConfig& cfg, const VoxelInputs& in) {
+  VoxelView v{};
+  int L = 0;
+  while ((1 << (L + 1)) <= cfg.voxel_res) ++L;
+  v.corners = in.corners;
+  v.mips = in.mips;
+  for (int i = 0; i < 16; ++i) v.off[i] = (uint32_t)(i < kMaxVoxelLevels && in.mip_offsets ? in.mip_offsets[i] : 0);
+  v.N = cfg.voxel_res;
+  v.log2n = L;
+  v.max_level = L;
+  v.half_mips = cfg.precision == DRV_PRECISION_BF16;
+  return v;
+}
+
 // Host: fills StageParams from the stage's arguments (k_light.cu).
 StageParams make_stage_params(const DrvConfig& cfg, const DrvVolumeInfo& vol, const LightLaunch& ll,
                               const DrvCacheCounter* counter, void* entries, uint32_t entry_stride,
-                              const uint8_t* corners, const void* mips, const size_t* mip_offsets);
+                              const VoxelInputs& vox);
 
 // Host: the surrogate's pass over the pair list (k_light_surrogate.cu):
 // shadowing of the confident pairs, the others appended to L.retrace.

@@ -102,7 +102,7 @@ extern "C" drv_status drv_light_caches_static_scratch(const DrvConfig* cfg, cons
     off += n * n * n;
   }
   const uint32_t stride = cfg->sh_order == 2 ? 128u : 64u;
-  cudaError_t e = drv::launch_light_caches(s, *cfg, *vol, ll, counter, cache_entries, stride, voxel_corners,
-                                           voxel_mips, offsets, ls, num_sms);
+  const drv::VoxelInputs vox{voxel_corners, voxel_mips, offsets};
+  cudaError_t e = drv::launch_light_caches(s, *cfg, *vol, ll, counter, cache_entries, stride, vox, ls, num_sms);
   return e == cudaSuccess ? DRV_OK : DRV_ERR_CUDA;
 }

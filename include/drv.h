@@ -192,7 +192,8 @@ typedef struct DrvScene {
   float aabb_max[3];
 } DrvScene;
 
-/* G-buffer (renderer.cpp:466-471), device pointers, width*height texels. */
+/* G-buffer (renderer.cpp:466-471), device pointers, width*height texels;
+ * each array 4-byte aligned (DRV_ERR_INVALID_ARG otherwise). */
 typedef struct DrvGBufferView {
   int32_t width, height;
   const float* depth;               /* D32F reversed-Z */
