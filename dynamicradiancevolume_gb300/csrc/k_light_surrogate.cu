@@ -42,11 +42,6 @@ struct __align__(16) MlpWeights {
 };
 
 
-__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
-  const uint32_t a = __bfloat16_as_ushort(__float2bfloat16_rn(lo));
-  const uint32_t b = __bfloat16_as_ushort(__float2bfloat16_rn(hi));
-  return a | (b << 16);
-}
 
 __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
   asm volatile(
@@ -64,13 +59,15 @@ __device__ __forceinline__ void ldmatrix_x4(uint32_t (&r)[4], const void* smem_r
 }
 
 // One hidden layer for both 16-row m-tiles: in = A fragments [2][KSTEPS][4],
-// out = A fragments of the next layer [2][4][4] after bias + GELU.
+// out = A fragments of the next layer [2][4][4] after bias + GELU. The
+// accumulators start at the bias (D = A B + C with C = bias).
 template <int KSTEPS, int LD>
 __device__ __forceinline__ void hidden_layer(const uint32_t (&in)[2][KSTEPS][4], const uint16_t* w, const float* bias,
                                              uint32_t (&out)[2][4][4], int g, int tig) {
 #pragma unroll
   for (int j = 0; j < kMlpHidden / 8; ++j) {
-    float acc[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+    const float bl = bias[8 * j + 2 * tig], bh = bias[8 * j + 2 * tig + 1];
+    float acc[2][4] = {{bl, bh, bl, bh}, {bl, bh, bl, bh}};
     const uint16_t* wr = w + (8 * j + g) * LD + 2 * tig;
 #pragma unroll
     for (int kk = 0; kk < KSTEPS; ++kk) {
@@ -79,15 +76,12 @@ __device__ __forceinline__ void hidden_layer(const uint32_t (&in)[2][KSTEPS][4],
       mma_bf16(acc[0], in[0][kk], b0, b1);
       mma_bf16(acc[1], in[1][kk], b0, b1);
     }
-    const float bl = bias[8 * j + 2 * tig], bh = bias[8 * j + 2 * tig + 1];
 #pragma unroll
     for (int m = 0; m < 2; ++m) {
-      const uint32_t lo = pack_bf16x2(gelu_fast(acc[m][0] + bl), gelu_fast(acc[m][1] + bh));
-      const uint32_t hi = pack_bf16x2(gelu_fast(acc[m][2] + bl), gelu_fast(acc[m][3] + bh));
       // n-tile j feeds k-step j/2 of the next layer: even tiles are its low
       // k half (regs 0,1), odd tiles its high half (regs 2,3).
-      out[m][j >> 1][(j & 1) * 2 + 0] = lo;
-      out[m][j >> 1][(j & 1) * 2 + 1] = hi;
+      out[m][j >> 1][(j & 1) * 2 + 0] = gelu_bf16x2(pack_bf16x2(acc[m][0], acc[m][1]));
+      out[m][j >> 1][(j & 1) * 2 + 1] = gelu_bf16x2(pack_bf16x2(acc[m][2], acc[m][3]));
     }
   }
 }
@@ -152,8 +146,17 @@ __global__ void __launch_bounds__(kThreads) mlp_kernel(StageParams p, PairList L
     __syncwarp();
     uint32_t h1[2][4][4], h2[2][4][4];
     hidden_layer<2, kLd1>(a1, s_w.w1, s_w.b1, h1, g, tig);
-    hidden_layer<4, kLdH>(h1, s_w.w2, s_w.b2, h2, g, tig);
-    hidden_layer<4, kLdH>(h2, s_w.w3, s_w.b3, h1, g, tig);
+    // Layers 2 and 3 have one shape: one copy of their code (instruction cache).
+#pragma unroll 1
+    for (int layer = 0; layer < 2; ++layer) {
+      hidden_layer<4, kLdH>(h1, layer ? s_w.w3 : s_w.w2, layer ? s_w.b3 : s_w.b2, h2, g, tig);
+#pragma unroll
+      for (int m = 0; m < 2; ++m)
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+          for (int r = 0; r < 4; ++r) h1[m][kk][r] = h2[m][kk][r];
+    }
     float o[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
     {
       const uint16_t* wr = s_w.w4 + g * kLdH + 2 * tig;
@@ -223,29 +226,40 @@ __global__ void pack_weights_kernel(const float* __restrict__ params, MlpWeights
   if (t < kMlpOutPad) w->b4[t] = t < kMlpOut ? params[kOffB4 + t] : 0.0f;
 }
 
-// Evaluates the inference MLP (BF16 weights, same arithmetic as the light
-// kernel's tensor-core path but one row per thread in FP32) for validation.
+// Evaluates the inference MLP for validation: BF16 weights and inputs, FP32
+// sums one row per thread, and the tensor-core path's bias + bf16x2 GELU.
 __global__ void eval_kernel(const MlpWeights* __restrict__ w, const float* __restrict__ X, int n,
                             float* __restrict__ out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   float x[kMlpIn], h[kMlpHidden], h2[kMlpHidden];
   for (int k = 0; k < kMlpIn; ++k) x[k] = from_bf16(to_bf16(X[(size_t)i * kMlpIn + k]));
+  // bias + GELU of a layer's 64 outputs in pairs, as the tensor-core path forms them
+  auto act = [](float* v) {
+    for (int j = 0; j < kMlpHidden; j += 2) {
+      const uint32_t a = gelu_bf16x2(pack_bf16x2(v[j], v[j + 1]));
+      v[j] = __uint_as_float(a << 16);
+      v[j + 1] = __uint_as_float(a & 0xFFFF0000u);
+    }
+  };
   for (int j = 0; j < kMlpHidden; ++j) {
-    float s = 0.0f;
+    float s = w->b1[j];
     for (int k = 0; k < kMlpIn; ++k) s += from_bf16(w->w1[j * kLd1 + k]) * x[k];
-    h[j] = from_bf16(to_bf16(gelu_fast(s + w->b1[j])));
+    h[j] = s;
   }
+  act(h);
   for (int j = 0; j < kMlpHidden; ++j) {
-    float s = 0.0f;
+    float s = w->b2[j];
     for (int k = 0; k < kMlpHidden; ++k) s += from_bf16(w->w2[j * kLdH + k]) * h[k];
-    h2[j] = from_bf16(to_bf16(gelu_fast(s + w->b2[j])));
+    h2[j] = s;
   }
+  act(h2);
   for (int j = 0; j < kMlpHidden; ++j) {
-    float s = 0.0f;
+    float s = w->b3[j];
     for (int k = 0; k < kMlpHidden; ++k) s += from_bf16(w->w3[j * kLdH + k]) * h2[k];
-    h[j] = from_bf16(to_bf16(gelu_fast(s + w->b3[j])));
+    h[j] = s;
   }
+  act(h);
   for (int j = 0; j < kMlpOut; ++j) {
     float s = 0.0f;
     for (int k = 0; k < kMlpHidden; ++k) s += from_bf16(w->w4[j * kLdH + k]) * h[k];

@@ -60,6 +60,34 @@ __device__ __forceinline__ float gelu_fast(float x) {
   return 0.5f * x * (1.0f + tanh_fast(u));
 }
 
+// Two FP32 values -> bf16x2 (lo in the low half), round to nearest even.
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+  uint32_t r;
+  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+  return r;
+}
+
+// GELU of the inference MLP on two BF16 values at once, in bf16x2
+// arithmetic with the hardware tanh: 0.5 x (1 + tanh(x (c0 + c1 x^2))) with
+// c0 = sqrt(2/pi), c1 = 0.044715 c0 rounded to BF16 (0x3F4C, 0x3D12). The
+// activations it produces are stored as BF16 anyway, and the error of BF16
+// arithmetic here is of the order of that rounding.
+__device__ __forceinline__ uint32_t gelu_bf16x2(uint32_t x) {
+  uint32_t y;
+  asm("{\n"
+      ".reg .b32 x2, u, t, h;\n"
+      "mul.rn.bf16x2 x2, %1, %1;\n"
+      "fma.rn.bf16x2 u, x2, %2, %3;\n"
+      "mul.rn.bf16x2 u, u, %1;\n"
+      "tanh.approx.bf16x2 t, u;\n"
+      "mul.rn.bf16x2 h, %1, %4;\n"
+      "fma.rn.bf16x2 %0, h, t, h;\n"
+      "}"
+      : "=r"(y)
+      : "r"(x), "r"(0x3D123D12u), "r"(0x3F4C3F4Cu), "r"(0x3F003F00u));
+  return y;
+}
+
 // Distance (in voxels) the cone of cacheLightingRSM.comp:195-228 reaches
 // before it stops: min(goal, the distance after max_steps steps). The step
 // rule is stepSize = max(1, dist * dsr * 2 / (1 - dsr)); it is evaluated here
