@@ -35,6 +35,12 @@ sys.path.insert(0, str(ROOT))
 METRIC = "caches lit/s and ms/frame at 1080p: plain vs surrogate, at ≤1% rel-L2 vs FP64"
 UNIT = "caches/s"
 
+# DRAM bytes (read + write) per launch of the light stage's top kernels at
+# ns_1080p_4096, from one ncu --set full capture each (cold caches; the
+# commands are in profiles/light_stage_kernels_ns_1080p_4096.md and
+# profiles/mlp_kernel_ns_1080p_4096.md).
+NCU_TRAFFIC = {"cone_kernel": 12_660_736, "mlp_kernel": 7_976_192}
+
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -131,18 +137,25 @@ def sh_flops_per_pair(sh_order: int) -> int:
     return 51 if sh_order == 1 else 94
 
 
+def light_stage_launches(w, surrogate: bool = False) -> int:
+    # split stage: cull, classify, scatter, cone, gather; with the surrogate:
+    # cull, MLP, cone, gather; without indirect shadow: the single kernel.
+    if not w.indirect_shadow:
+        return 1
+    return 4 if surrogate else 5
+
+
 def kernel_launches_per_frame(w, surrogate: bool = False) -> int:
     # per light: (read_lod + shadow_lod) downsample passes + 1 extraction;
-    # voxelize 1 + mips (1, +1 tail above 32^3) + corner grid 1; allocate 1;
-    # light: cull + cone + gather (+ MLP with the surrogate), or 1 without
-    # indirect shadow; apply 1.
+    # voxelize 1 + mips (1, +1 tail above 32^3) + corner grid 1; allocate 2
+    # (allocation, dispatch size); the light stage; apply 1.
     n = w.n_lights * (w.rsm_read_lod + w.shadow_lod + 1)
     if w.indirect_shadow:
         n += 1 + (2 if w.voxel_res > 32 else 1) + 1
-        n += 4 if surrogate else 3
+        n += light_stage_launches(w, surrogate)
     else:
         n += 1
-    return n + 2
+    return n + 3
 
 
 # ---------------------------------------------------------------- CPU arm
@@ -178,7 +191,7 @@ def cpu_frame(w, hf, n_threads: int, cache_sample: int | None):
     t_apply = time.perf_counter() - t2
     note = (f"FP64 oracle frame on {n_threads} host threads; light stage on {sample} of {n} caches"
             + (" (extrapolated linearly)" if sample < n else " (all caches)"))
-    return n, t_fixed + t_light + t_apply, note
+    return n, t_fixed + t_light + t_apply, t_light, note
 
 
 def run_reference(args):
@@ -189,15 +202,17 @@ def run_reference(args):
     w = pipeline.WORKLOADS[args.workload]
     hf = pipeline.host_frame(w)
     threads = os.cpu_count() or 1
-    times, caches, note = [], 0, ""
+    frames, lights, caches, note = [], [], 0, ""
     for i in range(args.warmup + args.steps):
-        caches, t, note = cpu_frame(w, hf, threads, cache_sample=256)
+        caches, t_frame, t_light, note = cpu_frame(w, hf, threads, cache_sample=256)
         if i >= args.warmup:
-            times.append(t)
-    t = statistics.mean(times)
+            frames.append(t_frame)
+            lights.append(t_light)
+    t, tf = statistics.mean(lights), statistics.mean(frames)
     value = caches / t
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+            "warmup": args.warmup, "ms_per_step": t * 1e3, "ms_per_frame": tf * 1e3, "higher_is_better": True,
+            "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded procedural box room)",
             "config": {"workload": w.name, "width": w.width, "height": w.height, "n_vpls": w.n_vpls,
                        "voxel_res": w.voxel_res, "cascades": f"{w.n_cascades}x{w.cav_res}^3", "sh_order": w.sh_order,
@@ -305,6 +320,34 @@ def measure_graph(pipe, steps, warmup, flush):
     return statistics.mean(a.elapsed_time(b) for a, b in ev)
 
 
+def measure_light_graph(pipe, steps, warmup, flush):
+    """Mean ms of `steps` replays of the light stage (drv_light_caches)
+    captured as a CUDA graph, over the frame's own VPLs, voxels and caches
+    (each replay relights every cache; its SH accumulates, as per-light
+    dispatches do). L2 flushed between replays, outside the timed events."""
+    import torch
+    stream = pipe.stream
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=stream):
+        pipe.light()
+    for _ in range(warmup):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            g.replay()
+    torch.cuda.synchronize(pipe.device)
+    ev = []
+    for _ in range(steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            g.replay()
+            b.record(stream)
+        ev.append((a, b))
+    torch.cuda.synchronize(pipe.device)
+    return statistics.mean(a.elapsed_time(b) for a, b in ev)
+
+
 def run_ours(args):
     import ctypes as C
     import torch
@@ -344,11 +387,14 @@ def run_ours(args):
             count = pipe.cache_count()
             frame_ms, stage_ms = measure(pipe, args.steps, args.warmup, flush)
             graph_ms = measure_graph(pipe, args.steps, args.warmup, flush)
+            light_ms = measure_light_graph(pipe, args.steps, args.warmup, flush)
             pipe.frame()
             pipe.sync()
-            info = {"frame_ms": graph_ms, "frame_ms_stream": frame_ms, "stage_ms": stage_ms, "caches": count,
-                    "caches_per_s": count / (graph_ms / 1e3),
-                    "caches_lit_per_s_light_stage": count / (stage_ms["light"] / 1e3)}
+            pipe.light()
+            info = {"caches_lit_per_s": count / (light_ms / 1e3), "light_ms": light_ms, "frame_ms": graph_ms,
+                    "live_pairs": pipe.light_pairs(),
+                    "frame_ms_stream": frame_ms, "stage_ms": stage_ms, "caches": count,
+                    "caches_per_s_of_frame": count / (graph_ms / 1e3)}
             if thr is not None:
                 ev, fb = C.c_uint32(), C.c_uint32()
                 pipe.lib.drv_get_surrogate_stats(pipe.ctx, C.byref(ev), C.byref(fb))
@@ -369,7 +415,7 @@ def run_ours(args):
             pipes[name] = pipe
     clocks = clk.summary()
     ok = {n: v for n, v in variants.items() if v.get("rel_l2_vs_fp64", 1.0) <= 0.01}
-    head = max(ok, key=lambda n: ok[n]["caches_per_s"]) if ok else "plain_fp32"
+    head = max(ok, key=lambda n: ok[n]["caches_lit_per_s"]) if ok else "plain_fp32"
     pipe = pipes[head]
     hv = variants[head]
     for n, p in pipes.items():
@@ -416,65 +462,88 @@ def run_ours(args):
     e2e_ms = statistics.mean(e_times)
     count = hv["caches"]
 
+    # ---- per-kernel times of the headline light stage (non-graph, events between its kernels)
+    pipe.set_tuning(time_kernels=1)
+    kern = {k: [] for k in abi.LIGHT_KERNELS}
+    for i in range(args.warmup + args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        pipe.light()
+        if i >= args.warmup:
+            for k, v in pipe.light_kernel_ms().items():
+                kern[k].append(v)
+    pipe.set_tuning(time_kernels=0)
+    kernel_ms = {k: statistics.mean(v) for k, v in kern.items()}
+
     # ---- max over ranks (replicas)
-    vals = torch.tensor([hv["frame_ms"], e2e_ms, float(count)], dtype=torch.float64, device=dev)
+    vals = torch.tensor([hv["light_ms"], hv["frame_ms"], e2e_ms, float(count)], dtype=torch.float64, device=dev)
     if ws > 1:
         mx = vals.clone()
         dist.all_reduce(mx, op=dist.ReduceOp.MAX)
         tot = vals.clone()
         dist.all_reduce(tot, op=dist.ReduceOp.SUM)
-        frame_ms_all, e2e_ms_all, caches_all = mx[0].item(), mx[1].item(), tot[2].item()
+        light_ms_all, frame_ms_all, e2e_ms_all, caches_all = mx[0].item(), mx[1].item(), mx[2].item(), tot[3].item()
     else:
-        frame_ms_all, e2e_ms_all, caches_all = hv["frame_ms"], e2e_ms, float(count)
+        light_ms_all, frame_ms_all, e2e_ms_all, caches_all = hv["light_ms"], hv["frame_ms"], e2e_ms, float(count)
 
+    # ---- roofline of the light stage's dominant kernel
     pk = peaks()
-    light_ms = hv["stage_ms"]["light"]
-    pairs = count * w.n_vpls
-    if head.startswith("surrogate"):
-        # MLP on tensor cores: 2*(32*64 + 64*64 + 64*64 + 64*2) flop per evaluated pair (the
-        # pairs that can contribute; the others need no visibility).
-        evaluated = hv["evaluated_pairs"]
-        mlp_tflops = evaluated * 20736 / (light_ms / 1e3) / 1e12
-        roofline = {"bound": "tensor", "kernel": "light_surrogate_kernel", "achieved": mlp_tflops,
-                    "note": "MLP flops of the evaluated pairs over the whole light stage (cone fallbacks included)",
-                    "peak": pk["bf16_tflops"], "unit": "TFLOP/s", "frac": mlp_tflops / pk["bf16_tflops"],
-                    "traffic": None, "peak_source": pk["source"]}
+    top = max(kernel_ms, key=kernel_ms.get)
+    top_ms = kernel_ms[top]
+    n_pairs = hv.get("evaluated_pairs") or 0
+    if top == "mlp":
+        flop = n_pairs * 20736  # 2 (32*64 + 64*64 + 64*64 + 64*2) per evaluated pair
+        achieved = flop / (top_ms / 1e3) / 1e12
+        roofline = {"bound": "tensor", "kernel": "mlp_kernel", "achieved": achieved, "peak": pk["bf16_tflops"],
+                    "unit": "TFLOP/s", "frac": achieved / pk["bf16_tflops"],
+                    "traffic": NCU_TRAFFIC["mlp_kernel"] if w.name == "ns_1080p_4096" else None,
+                    "peak_source": pk["source"] + " (bf16_tflops, burst)",
+                    "algorithmic": f"{n_pairs} evaluated pairs x 20736 flop"}
     else:
-        light_bytes = count * (16 + (128 if w.sh_order == 2 else 64) * 2) + w.n_vpls * 64
-        roofline = {"bound": "hbm", "kernel": "light_kernel", "achieved": light_bytes / (light_ms / 1e3) / 1e9,
-                    "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": light_bytes / (light_ms / 1e3) / 1e9 / pk["hbm_gbs"],
-                    "traffic": None, "peak_source": pk["source"],
-                    "note": "the cone-traced light stage is FP32/L1-bound, not HBM-bound; see fp32_pipe"}
-    light_flop = pairs * sh_flops_per_pair(w.sh_order)
-    fp32_peak = 152 * 128 * 2 * (clocks["sm_mhz"] or pk["sm_max_mhz"]) * 1e6 / 1e12
+        # Per traced pair: its order index, the pair (cache, block) and the
+        # shadow it writes = 16 B; cache positions and cones are per cache /
+        # per block and the voxel samples are L1/L2 hits (the cold-cache DRAM
+        # bytes, which include the bricks the cones touch, are `traffic`).
+        pairs_traced = variants[head]["live_pairs"]
+        nbytes = pairs_traced * 16 + count * 16 + w.n_vpls * 16
+        achieved = nbytes / (top_ms / 1e3) / 1e9
+        roofline = {"bound": "hbm", "kernel": f"{top}_kernel", "achieved": achieved, "peak": pk["hbm_gbs"],
+                    "unit": "GB/s", "frac": achieved / pk["hbm_gbs"],
+                    "traffic": NCU_TRAFFIC.get(f"{top}_kernel") if w.name == "ns_1080p_4096" else None,
+                    "peak_source": pk["source"] + " (hbm_gbs)",
+                    "algorithmic": f"{pairs_traced} traced pairs x 16 B + {count} caches x 16 B + {w.n_vpls} cones x 16 B",
+                    "note": "the cone pass is issue-bound (ALU/LSU on L1/L2-resident voxels), far from the HBM "
+                            "roofline; DRAM traffic per launch and issue utilisation are in profiles/"}
     line = {
-        "metric": METRIC, "value": caches_all / (frame_ms_all / 1e3), "unit": UNIT, "n_gpus": ws,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": frame_ms_all, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "bf16" if head != "plain_fp32" else "f32",
+        "metric": METRIC, "value": caches_all / (light_ms_all / 1e3), "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": light_ms_all, "ms_per_frame": frame_ms_all,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16" if head != "plain_fp32" else "f32",
         "data": "synthetic (seeded procedural box room)",
         "config": {"workload": w.name, "variant": head, "width": w.width, "height": w.height, "n_vpls": w.n_vpls,
                    "n_lights": w.n_lights, "voxel_res": w.voxel_res, "cascades": f"{w.n_cascades}x{w.cav_res}^3",
                    "sh_order": w.sh_order, "cone_steps": w.max_cone_steps, "caches": count,
-                   "l2": "flushed between steps (256 MiB write)",
-                   "launch": "each step replays the whole frame captured once as a CUDA graph; "
-                             "stage_ms from a non-graph run with events between stages"},
+                   "step": "the light stage (drv_light_caches) over the frame's VPLs, voxels and caches, "
+                           "captured once as a CUDA graph and replayed; ms_per_frame = the whole frame "
+                           "(drv_frame) replayed the same way",
+                   "l2": "flushed between steps (256 MiB write)"},
         "rel_l2_vs_fp64": hv.get("rel_l2_vs_fp64"),
         "stage_ms": hv["stage_ms"],
-        "caches_lit_per_s_light_stage": hv["caches_lit_per_s_light_stage"],
+        "light_kernel_ms": kernel_ms,
         "variants": variants,
         "roofline": roofline,
-        "fp32_pipe": {"kernel": "light_kernel", "achieved_tflops": light_flop / (light_ms / 1e3) / 1e12,
-                      "peak_tflops": fp32_peak, "frac": light_flop / (light_ms / 1e3) / 1e12 / fp32_peak,
-                      "peak_source": "152 SMs x 128 FP32 lanes x 2 x median SM clock (derived, not measured)"},
         "e2e": {"value": caches_all / (e2e_ms_all / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms_all},
-        "gpu_launches": kernel_launches_per_frame(w, head.startswith("surrogate")) * args.steps,
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms_all,
+                "scope": "whole frame through drv_frame: G-buffer and RSM copied from pinned host memory, "
+                         "radiance copied back, all inside the timed region"},
+        "gpu_launches": light_stage_launches(w, head.startswith("surrogate")) * args.steps,
         "clocks": clocks,
     }
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        caches, t, note = cpu_frame(w, pipeline.host_frame(w), threads, cache_sample=256)
-        line["cpu_baseline"] = {"value": caches / t, "unit": UNIT, "cores": threads, "kind": "port", "sample": note}
+        caches, t_frame, t_light, note = cpu_frame(w, pipeline.host_frame(w), threads, cache_sample=256)
+        line["cpu_baseline"] = {"value": caches / t_light, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": note, "ms_per_frame": t_frame * 1e3}
     if rank == 0:
         print(json.dumps(line), flush=True)
     pipe.close()

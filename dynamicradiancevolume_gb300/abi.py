@@ -122,7 +122,10 @@ class DrvBuffers(C.Structure):
 
 class DrvTuning(C.Structure):
     _fields_ = [("light_path", C.c_int32), ("pair_capacity", C.c_uint32), ("cone_ctas_per_sm", C.c_int32),
-                ("gather_ctas_per_sm", C.c_int32), ("reserved", C.c_int32 * 4)]
+                ("gather_ctas_per_sm", C.c_int32), ("time_kernels", C.c_int32), ("reserved", C.c_int32 * 3)]
+
+
+LIGHT_KERNELS = ("cull", "classify", "scatter", "mlp", "cone", "gather")
 
 
 LIGHT_PATH_AUTO, LIGHT_PATH_SINGLE, LIGHT_PATH_SPLIT = 0, 1, 2
@@ -176,6 +179,8 @@ PROTOTYPES = {
     "drv_get_surrogate_stats": (C.c_int, [VP, P(C.c_uint32), P(C.c_uint32)]),
     "drv_set_tuning": (C.c_int, [VP, P(DrvTuning)]),
     "drv_get_tuning": (C.c_int, [VP, P(DrvTuning)]),
+    "drv_get_light_kernel_ms": (C.c_int, [VP, P(C.c_float)]),
+    "drv_get_light_pairs": (C.c_int, [VP, P(C.c_uint32)]),
     "drv_light_caches_static_scratch": (C.c_int, [P(DrvConfig), P(DrvVolumeInfo), P(VP), P(VP), P(C.c_int32),
                                                   P(C.c_int32), C.c_int32, VP, VP, VP, VP, VP]),
 }

@@ -52,6 +52,8 @@ void release(Context* c) {
   cudaFree(c->light_scratch);
   cudaFree(c->light_tickets);
   cudaFree(c->sur_weights);
+  for (cudaEvent_t e : c->lk_events)
+    if (e) cudaEventDestroy(e);
   cudaFree(c->pair_mem);
   for (int l = 0; l < DRV_MAX_LIGHTS; ++l) {
     for (int k = 1; k < drv::kMaxRsmLevels; ++k) {
@@ -416,12 +418,24 @@ drv_status drv_light_caches(DrvContext* ctx, const DrvSpotLight* lights, int32_t
   if (split) {
     drv::PairList pairs = ctx->pairs;
     if (ctx->tuning.pair_capacity) pairs.cap = std::min(pairs.cap, ctx->tuning.pair_capacity);
-    return cuda_check(ctx, drv::launch_light_split(ctx->s(), ctx->cfg, *vol, ll, ctx->counter, ctx->entries,
-                                                   ctx->entry_stride, ctx->voxels(), pairs,
-                                                   surrogate ? ctx->sur_weights : nullptr,
-                                                   ctx->tuning.cone_ctas_per_sm, ctx->tuning.gather_ctas_per_sm,
-                                                   ctx->num_sms),
-                      "light_caches");
+    cudaEvent_t* events = nullptr;
+    if (ctx->tuning.time_kernels) {
+      cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+      DRV_TRY_CUDA(ctx, cudaStreamIsCapturing(ctx->s(), &cs));
+      if (cs == cudaStreamCaptureStatusNone) {
+        for (cudaEvent_t& e : ctx->lk_events)
+          if (!e) DRV_TRY_CUDA(ctx, cudaEventCreate(&e));
+        events = ctx->lk_events;
+      }
+    }
+    drv_status st = cuda_check(ctx, drv::launch_light_split(ctx->s(), ctx->cfg, *vol, ll, ctx->counter, ctx->entries,
+                                                            ctx->entry_stride, ctx->voxels(), pairs,
+                                                            surrogate ? ctx->sur_weights : nullptr,
+                                                            ctx->tuning.cone_ctas_per_sm,
+                                                            ctx->tuning.gather_ctas_per_sm, ctx->num_sms, events),
+                               "light_caches");
+    if (events) ctx->lk_recorded = st == DRV_OK;
+    return st;
   }
   if (surrogate && ctx->tuning.light_path == DRV_LIGHT_PATH_SINGLE)
     return fail(ctx, DRV_ERR_INVALID_ARG, "surrogate visibility runs on the split light stage");
@@ -494,6 +508,24 @@ drv_status drv_set_tuning(DrvContext* ctx, const DrvTuning* t) {
       t->gather_ctas_per_sm < 0 || t->cone_ctas_per_sm > 32 || t->gather_ctas_per_sm > 32)
     return fail(ctx, DRV_ERR_INVALID_ARG, "bad tuning");
   ctx->tuning = *t;
+  return DRV_OK;
+}
+
+drv_status drv_get_light_pairs(DrvContext* ctx, uint32_t* pairs) {
+  if (!ctx || !pairs) return DRV_ERR_INVALID_ARG;
+  uint32_t n = 0;
+  DRV_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->s()));
+  DRV_TRY_CUDA(ctx, cudaMemcpy(&n, ctx->pairs.counters, 4, cudaMemcpyDeviceToHost));
+  *pairs = std::min(n, ctx->pairs.cap);
+  return DRV_OK;
+}
+
+drv_status drv_get_light_kernel_ms(DrvContext* ctx, float ms[DRV_LK_COUNT]) {
+  if (!ctx || !ms) return DRV_ERR_INVALID_ARG;
+  if (!ctx->lk_recorded) return fail(ctx, DRV_ERR_INVALID_ARG, "no split light stage ran with time_kernels");
+  DRV_TRY_CUDA(ctx, cudaEventSynchronize(ctx->lk_events[DRV_LK_COUNT]));
+  for (int k = 0; k < DRV_LK_COUNT; ++k)
+    DRV_TRY_CUDA(ctx, cudaEventElapsedTime(&ms[k], ctx->lk_events[k], ctx->lk_events[k + 1]));
   return DRV_OK;
 }
 

@@ -135,6 +135,9 @@ struct Context {
   void* pair_mem = nullptr;
   PairList pairs{};
   DrvTuning tuning{};
+  // Events between the split light stage's kernels (DrvTuning.time_kernels).
+  cudaEvent_t lk_events[DRV_LK_COUNT + 1] = {};
+  bool lk_recorded = false;
   // Visibility surrogate: packed BF16 inference weights.
   void* sur_weights = nullptr;
   bool sur_ready = false;
@@ -170,7 +173,8 @@ bool light_split_supported(const DrvConfig& cfg, const LightLaunch& ll);
 cudaError_t launch_light_split(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const LightLaunch& ll,
                                const DrvCacheCounter* counter, void* entries, uint32_t entry_stride,
                                const VoxelInputs& vox, const PairList& pairs, const void* weights,
-                               int cone_ctas_per_sm, int gather_ctas_per_sm, int num_sms);
+                               int cone_ctas_per_sm, int gather_ctas_per_sm, int num_sms,
+                               cudaEvent_t* events = nullptr);
 cudaError_t launch_apply(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const DrvPerFrame& f,
                          const DrvGBufferView& g, const uint32_t* atlas, const void* entries, uint32_t entry_stride,
                          const DrvCacheCounter* counter, float* out_rgb);

@@ -237,6 +237,19 @@ class Pipeline:
         self._c(self.lib.drv_set_tuning(self.ctx, C.byref(t)))
         return t
 
+    def light_pairs(self) -> int:
+        """Pairs the last split light stage listed (each traced or evaluated once)."""
+        n = C.c_uint32()
+        self._c(self.lib.drv_get_light_pairs(self.ctx, C.byref(n)))
+        return n.value
+
+    def light_kernel_ms(self) -> dict:
+        """Per-kernel milliseconds of the last split light stage run with
+        time_kernels set (see set_tuning)."""
+        ms = (C.c_float * len(abi.LIGHT_KERNELS))()
+        self._c(self.lib.drv_get_light_kernel_ms(self.ctx, ms))
+        return dict(zip(abi.LIGHT_KERNELS, list(ms)))
+
     def surrogate_stats(self) -> tuple[int, int]:
         """(pairs the MLP evaluated, pairs re-traced) of the last light stage."""
         ev, rt = C.c_uint32(), C.c_uint32()

@@ -434,11 +434,27 @@ typedef struct DrvTuning {
                               not fit are traced by the gather itself. 0: the whole allocation */
   int32_t cone_ctas_per_sm;   /* split stage: CTAs of the cone pass per SM (0: as many as fit) */
   int32_t gather_ctas_per_sm; /* split stage: CTAs of the gather pass per SM (0: as many as fit) */
-  int32_t reserved[4];
+  int32_t time_kernels;       /* nonzero: the split light stage records CUDA events between its
+                                 kernels (not while the stream is being captured) */
+  int32_t reserved[3];
 } DrvTuning;
 enum { DRV_LIGHT_PATH_AUTO = 0, DRV_LIGHT_PATH_SINGLE = 1, DRV_LIGHT_PATH_SPLIT = 2 };
 drv_status drv_set_tuning(DrvContext* ctx, const DrvTuning* tuning);
 drv_status drv_get_tuning(DrvContext* ctx, DrvTuning* tuning);
+
+/* (cache, shadow block) pairs the last split light stage listed as able to
+ * contribute (each traced or evaluated once). Synchronises. */
+drv_status drv_get_light_pairs(DrvContext* ctx, uint32_t* pairs);
+
+/* Kernels of the split light stage, in launch order (DrvTuning.time_kernels). */
+enum {
+  DRV_LK_CULL = 0, DRV_LK_CLASSIFY = 1, DRV_LK_SCATTER = 2, DRV_LK_MLP = 3, DRV_LK_CONE = 4, DRV_LK_GATHER = 5,
+  DRV_LK_COUNT = 6
+};
+/* Milliseconds of each kernel of the last split light stage launched with
+ * time_kernels set (0 for kernels that stage did not run). Synchronises.
+ * DRV_ERR_INVALID_ARG when no such stage ran. */
+drv_status drv_get_light_kernel_ms(DrvContext* ctx, float ms[DRV_LK_COUNT]);
 
 /* ---- allocation-free light stage ------------------------------------------
  * No counterpart in the reference: the reference renderer always owns its GL

@@ -77,3 +77,15 @@ def test_cta_knobs_keep_results(cuda, lib):
     assert np.array_equal(sh1, sh2)  # the gather's order is fixed per cache
     p1.close()
     p2.close()
+
+
+def test_kernel_timing_keeps_results_and_reports_each_kernel(cuda, lib):
+    p1, _, sh1 = _lit(REDUCED, 8)
+    p2, _, sh2 = _lit(REDUCED, 8, time_kernels=1)
+    assert np.array_equal(sh1, sh2)
+    ms = p2.light_kernel_ms()
+    assert set(ms) == set(abi.LIGHT_KERNELS)
+    assert ms["cull"] > 0 and ms["cone"] > 0 and ms["gather"] > 0 and ms["classify"] > 0
+    assert ms["mlp"] == pytest.approx(0.0, abs=0.05)  # no surrogate: the slot is empty
+    p1.close()
+    p2.close()
