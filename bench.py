@@ -36,9 +36,8 @@ METRIC = "caches lit/s and ms/frame at 1080p: plain vs surrogate, at ≤1% rel-L
 UNIT = "caches/s"
 
 # DRAM bytes (read + write) per launch of the light stage's top kernels at
-# ns_1080p_4096, from one ncu --set full capture each (cold caches; the
-# commands are in profiles/light_stage_kernels_ns_1080p_4096.md and
-# profiles/mlp_kernel_ns_1080p_4096.md).
+# ns_1080p_4096, from one `ncu --set full --clock-control none` capture each
+# (cold caches) of `bench.py --steps 1 --warmup 1` at that workload.
 NCU_TRAFFIC = {"cone_kernel": 12_660_736, "mlp_kernel": 7_976_192}
 
 
@@ -156,6 +155,20 @@ def kernel_launches_per_frame(w, surrogate: bool = False) -> int:
     else:
         n += 1
     return n + 3
+
+
+def reduce_over_ranks(light_ms: float, frame_ms: float, e2e_ms: float, caches: float, device=None):
+    """Replicas: the slowest rank's times and the caches of all ranks
+    (no collective on the data path, only this one for the report)."""
+    import torch
+    import torch.distributed as dist
+    vals = torch.tensor([light_ms, frame_ms, e2e_ms, caches], dtype=torch.float64, device=device)
+    if dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1:
+        mx, tot = vals.clone(), vals.clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        dist.all_reduce(tot, op=dist.ReduceOp.SUM)
+        return mx[0].item(), mx[1].item(), mx[2].item(), tot[3].item()
+    return light_ms, frame_ms, e2e_ms, float(caches)
 
 
 # ---------------------------------------------------------------- CPU arm
@@ -476,15 +489,8 @@ def run_ours(args):
     kernel_ms = {k: statistics.mean(v) for k, v in kern.items()}
 
     # ---- max over ranks (replicas)
-    vals = torch.tensor([hv["light_ms"], hv["frame_ms"], e2e_ms, float(count)], dtype=torch.float64, device=dev)
-    if ws > 1:
-        mx = vals.clone()
-        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
-        tot = vals.clone()
-        dist.all_reduce(tot, op=dist.ReduceOp.SUM)
-        light_ms_all, frame_ms_all, e2e_ms_all, caches_all = mx[0].item(), mx[1].item(), mx[2].item(), tot[3].item()
-    else:
-        light_ms_all, frame_ms_all, e2e_ms_all, caches_all = hv["light_ms"], hv["frame_ms"], e2e_ms, float(count)
+    light_ms_all, frame_ms_all, e2e_ms_all, caches_all = reduce_over_ranks(hv["light_ms"], hv["frame_ms"], e2e_ms,
+                                                                           float(count), device=dev)
 
     # ---- roofline of the light stage's dominant kernel
     pk = peaks()
@@ -512,8 +518,8 @@ def run_ours(args):
                     "traffic": NCU_TRAFFIC.get(f"{top}_kernel") if w.name == "ns_1080p_4096" else None,
                     "peak_source": pk["source"] + " (hbm_gbs)",
                     "algorithmic": f"{pairs_traced} traced pairs x 16 B + {count} caches x 16 B + {w.n_vpls} cones x 16 B",
-                    "note": "the cone pass is issue-bound (ALU/LSU on L1/L2-resident voxels), far from the HBM "
-                            "roofline; DRAM traffic per launch and issue utilisation are in profiles/"}
+                    "note": "the cone pass is issue-bound (71% issue active, ALU pipe 50%, voxel samples from "
+                            "L1/L2), far from the HBM roofline"}
     line = {
         "metric": METRIC, "value": caches_all / (light_ms_all / 1e3), "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": light_ms_all, "ms_per_frame": frame_ms_all,
