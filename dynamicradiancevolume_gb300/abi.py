@@ -128,6 +128,12 @@ class DrvTuning(C.Structure):
 LIGHT_KERNELS = ("cull", "classify", "scatter", "mlp", "cone", "gather")
 
 
+class DrvBatchScene(C.Structure):
+    _fields_ = [("ctx", C.c_void_p), ("scene", C.c_void_p), ("gbuffer", C.c_void_p), ("frame", C.c_void_p),
+                ("volume", C.c_void_p), ("lights", C.c_void_p), ("rsms", C.c_void_p), ("n_lights", C.c_int32),
+                ("out_rgb", C.c_void_p)]
+
+
 LIGHT_PATH_AUTO, LIGHT_PATH_SINGLE, LIGHT_PATH_SPLIT = 0, 1, 2
 
 STRUCT_ORDER = [DrvConfig, DrvCascade, DrvVolumeInfo, DrvPerFrame, DrvSpotLight, DrvLightDesc, DrvCamera, DrvBox,
@@ -181,6 +187,10 @@ PROTOTYPES = {
     "drv_get_tuning": (C.c_int, [VP, P(DrvTuning)]),
     "drv_get_light_kernel_ms": (C.c_int, [VP, P(C.c_float)]),
     "drv_get_light_pairs": (C.c_int, [VP, P(C.c_uint32)]),
+    "drv_batch_create": (C.c_int, [P(DrvBatchScene), C.c_int32, C.c_int32, VP, P(VP)]),
+    "drv_batch_launch": (C.c_int, [VP, VP]),
+    "drv_batch_times": (C.c_int, [VP, P(C.c_float), P(C.c_float)]),
+    "drv_batch_destroy": (C.c_int, [VP]),
     "drv_light_caches_static_scratch": (C.c_int, [P(DrvConfig), P(DrvVolumeInfo), P(VP), P(VP), P(C.c_int32),
                                                   P(C.c_int32), C.c_int32, VP, VP, VP, VP, VP]),
 }

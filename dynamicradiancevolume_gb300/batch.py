@@ -1,0 +1,227 @@
+"""Batched multi-scene frames: many independent seeded scenes of uneven sizes
+rendered by one CUDA-graph launch (drv_batch_*), against the same scenes run
+one by one; plus the autotuner that picks the batch's stream count and the
+light stage's grid knobs.
+
+    python -m dynamicradiancevolume_gb300.batch --scenes 64 --reps 10
+
+prints one JSON line: batch and one-by-one totals, scenes/s and caches lit/s,
+per-scene latency p50/p99, the tuned knobs.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import statistics
+import sys
+import time
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import abi, check, load, pipeline, surrogate
+
+# Size menus of the batch (log-spaced where the range is wide).
+RESOLUTIONS = (256, 384, 512, 768, 1024)
+VOXELS = (64, 128, 256)
+LIGHTS_LOD = ((2, 5), (1, 4), (2, 4), (1, 3), (2, 3))  # (lights, RSM read lod of 512^2): 512 ... 8192 VPLs
+CAV_RES = (32, 64)
+
+
+def batch_workloads(n: int, seed0: int = 0, precision: int = abi.PRECISION_BF16,
+                    visibility: int = abi.VISIBILITY_SURROGATE) -> list[tuple[pipeline.Workload, int]]:
+    """n scenes with sizes drawn from the menus by the scene's seed."""
+    out = []
+    for i in range(n):
+        seed = seed0 + i
+        r = np.random.default_rng(1000 + seed)
+        res = int(r.choice(RESOLUTIONS))
+        lights, lod = LIGHTS_LOD[int(r.integers(len(LIGHTS_LOD)))]
+        w = pipeline.Workload(f"batch_{seed}", res, res, int(r.integers(16, 65)), int(r.choice(VOXELS)), lights, 512,
+                              lod, 0, 4, 0.25, int(r.choice(CAV_RES)), 2, 32, 65536, precision=precision,
+                              visibility=visibility)
+        out.append((w, seed))
+    return out
+
+
+@dataclass
+class Scene:
+    pipe: pipeline.Pipeline
+    caches: int
+    vpls: int
+
+
+def make_scenes(specs, threshold: float = 0.5, params=None, device: str = "cuda") -> list[Scene]:
+    """Contexts, inputs (ray-cast once) and one ordinary frame per scene, so
+    that every scene's boxes are resident before a capture."""
+    scenes = []
+    for w, seed in specs:
+        hf = pipeline.host_frame(w, seed)
+        hf.config.surrogate_conf_threshold = threshold
+        p = pipeline.Pipeline(hf, device=device)
+        if w.visibility == abi.VISIBILITY_SURROGATE:
+            surrogate.upload(p, params if params is not None else surrogate.load_params())
+        p.raycast_inputs()
+        p.frame()
+        p.sync()
+        scenes.append(Scene(p, p.cache_count(), w.n_vpls))
+    return scenes
+
+
+def _batch_table(scenes: list[Scene]):
+    tab = (abi.DrvBatchScene * len(scenes))()
+    for i, s in enumerate(scenes):
+        p = s.pipe
+        tab[i] = abi.DrvBatchScene(p.ctx.value, C.addressof(p.hf.scene), C.addressof(p.gview),
+                                   C.addressof(p.hf.frame), C.addressof(p.hf.volume), C.addressof(p.hf.lights),
+                                   C.addressof(p.rsm_views), p.hf.workload.n_lights, p.out.data_ptr())
+    return tab
+
+
+class Batch:
+    """One captured graph over `scenes`, dealt over `streams` branches. A
+    launch waits for nothing: inputs written on other streams must be
+    complete (synchronised) first."""
+
+    def __init__(self, scenes: list[Scene], streams: int, stream=None):
+        self.lib = load()
+        self.scenes = scenes
+        self.table = _batch_table(scenes)
+        self.handle = C.c_void_p()
+        self.stream = stream
+        check(self.lib.drv_batch_create(self.table, len(scenes), streams,
+                                        C.c_void_p(stream.cuda_stream) if stream is not None else None,
+                                        C.byref(self.handle)))
+
+    def run(self) -> tuple[float, np.ndarray]:
+        """One launch; (total ms, per-scene completion ms from the start)."""
+        check(self.lib.drv_batch_launch(self.handle, None))
+        ms = (C.c_float * len(self.scenes))()
+        total = C.c_float()
+        check(self.lib.drv_batch_times(self.handle, ms, C.byref(total)))
+        return total.value, np.array(ms, dtype=np.float64)
+
+    def close(self):
+        if self.handle:
+            self.lib.drv_batch_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def set_knobs(scenes: list[Scene], cone_ctas: int, gather_ctas: int) -> None:
+    for s in scenes:
+        s.pipe.set_tuning(cone_ctas_per_sm=cone_ctas, gather_ctas_per_sm=gather_ctas)
+
+
+def time_batch(scenes, streams: int, reps: int, warmup: int = 2):
+    b = Batch(scenes, streams)
+    for _ in range(warmup):
+        b.run()
+    totals, per = [], []
+    for _ in range(reps):
+        t, ms = b.run()
+        totals.append(t)
+        per.append(ms)
+    b.close()
+    return statistics.median(totals), np.median(np.stack(per), axis=0)
+
+
+def time_one_by_one(scenes, reps: int, warmup: int = 2):
+    """Each scene alone (its frame as a one-scene graph), one after the other:
+    per-scene latency = its own frame time; total = their sum."""
+    lat = []
+    for s in scenes:
+        b = Batch([s], 1)
+        for _ in range(warmup):
+            b.run()
+        lat.append(statistics.median(b.run()[0] for _ in range(reps)))
+        b.close()
+    lat = np.array(lat)
+    return float(lat.sum()), lat
+
+
+def autotune(scenes, reps: int = 3, streams_menu=(1, 2, 4, 8, 16, 32), knob_menu=((0, 0), (4, 0), (2, 0), (0, 2),
+                                                                                   (2, 1), (1, 1)), log=print):
+    """Stream count first (default knobs), then the light stage's CTAs per SM
+    of the cone and gather passes at that stream count; returns the best
+    (streams, cone_ctas, gather_ctas) and the trials."""
+    trials = []
+    set_knobs(scenes, 0, 0)
+    best = None
+    for s in streams_menu:
+        if s > len(scenes):
+            continue
+        t, _ = time_batch(scenes, s, reps, warmup=1)
+        trials.append({"streams": s, "cone_ctas_per_sm": 0, "gather_ctas_per_sm": 0, "ms": t})
+        log(f"  streams {s:2d}: {t:.3f} ms")
+        if best is None or t < best[0]:
+            best = (t, s, 0, 0)
+    for cone, gather in knob_menu:
+        if (cone, gather) == (0, 0):
+            continue
+        set_knobs(scenes, cone, gather)
+        t, _ = time_batch(scenes, best[1], reps, warmup=1)
+        trials.append({"streams": best[1], "cone_ctas_per_sm": cone, "gather_ctas_per_sm": gather, "ms": t})
+        log(f"  streams {best[1]:2d} cone {cone} gather {gather}: {t:.3f} ms")
+        if t < best[0]:
+            best = (t, best[1], cone, gather)
+    set_knobs(scenes, best[2], best[3])
+    return {"streams": best[1], "cone_ctas_per_sm": best[2], "gather_ctas_per_sm": best[3], "ms": best[0]}, trials
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--scenes", type=int, default=64)
+    ap.add_argument("--reps", type=int, default=10)
+    ap.add_argument("--threshold", type=float, default=0.5)
+    ap.add_argument("--fp32-cone", action="store_true", help="FP32 storage and cone visibility instead")
+    args = ap.parse_args(argv)
+    prec = abi.PRECISION_FP32 if args.fp32_cone else abi.PRECISION_BF16
+    vis = abi.VISIBILITY_CONE if args.fp32_cone else abi.VISIBILITY_SURROGATE
+    t0 = time.time()
+    specs = batch_workloads(args.scenes, precision=prec, visibility=vis)
+    scenes = make_scenes(specs, args.threshold)
+    setup_s = time.time() - t0
+    log = lambda s: print(s, file=sys.stderr, flush=True)
+    tuned, trials = autotune(scenes, log=log)
+    batch_ms, batch_lat = time_batch(scenes, tuned["streams"], args.reps)
+    seq_ms, seq_lat = time_one_by_one(scenes, args.reps)
+    caches = np.array([s.caches for s in scenes])
+    px = np.array([s.pipe.hf.workload.width * s.pipe.hf.workload.height for s in scenes])
+    line = {
+        "scenes": args.scenes, "precision": "bf16" if prec == abi.PRECISION_BF16 else "f32",
+        "visibility": "surrogate" if vis == abi.VISIBILITY_SURROGATE else "cone",
+        "threshold": args.threshold if vis == abi.VISIBILITY_SURROGATE else None,
+        "sizes": {"pixels": [int(px.min()), int(px.max())], "caches": [int(caches.min()), int(caches.max())],
+                  "vpls": [int(min(s.vpls for s in scenes)), int(max(s.vpls for s in scenes))],
+                  "voxels": sorted({s.pipe.hf.workload.voxel_res for s in scenes})},
+        "tuned": tuned,
+        "batch": {"ms": batch_ms, "scenes_per_s": args.scenes / (batch_ms / 1e3),
+                  "caches_per_s": float(caches.sum()) / (batch_ms / 1e3),
+                  "latency_ms_p50": float(np.percentile(batch_lat, 50)),
+                  "latency_ms_p99": float(np.percentile(batch_lat, 99))},
+        "one_by_one": {"ms": seq_ms, "scenes_per_s": args.scenes / (seq_ms / 1e3),
+                       "caches_per_s": float(caches.sum()) / (seq_ms / 1e3),
+                       "latency_ms_p50": float(np.percentile(seq_lat, 50)),
+                       "latency_ms_p99": float(np.percentile(seq_lat, 99))},
+        "speedup": seq_ms / batch_ms,
+        "per_scene": [{"pixels": int(px[i]), "voxels": s.pipe.hf.workload.voxel_res, "vpls": s.vpls,
+                       "caches": s.caches, "cav_res": s.pipe.hf.workload.cav_res, "alone_ms": float(seq_lat[i]),
+                       "batch_done_ms": float(batch_lat[i])} for i, s in enumerate(scenes)],
+        "trials": trials,
+        "setup_s": setup_s,
+    }
+    print(json.dumps(line), flush=True)
+    for s in scenes:
+        s.pipe.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -13,8 +13,6 @@
 
 using drv::Context;
 
-struct DrvContext : Context {};
-
 namespace {
 
 drv_status fail(DrvContext* ctx, drv_status st, const std::string& msg) {
@@ -95,6 +93,19 @@ drv_status validate_config(const DrvConfig* c, std::string& why) {
 
 // Texel arrays must be aligned to their texel's scalar (the RG16I normal is
 // read as one 32-bit word per pixel).
+// Chunk partials of the single-launch light stage, a ticket per cache and
+// the two words of its unit counter (tickets and counter are reset by the
+// kernel that consumes them, so they are zeroed once here). About 3.5 KB per
+// cache with SH2, so contexts that only run the split stage never hold it.
+cudaError_t ensure_single_scratch(Context* c) {
+  if (c->light_scratch) return cudaSuccess;
+  const size_t n = c->cfg.max_caches;
+  cudaError_t e = cudaMalloc(&c->light_scratch, n * drv::kMaxLightChunks * (c->cfg.sh_order == 2 ? 27 : 12) * 4);
+  if (e != cudaSuccess) return e;
+  if ((e = cudaMalloc(&c->light_tickets, (n + 2) * 4)) != cudaSuccess) return e;
+  return cudaMemset(c->light_tickets, 0, (n + 2) * 4);
+}
+
 bool views_ok(const DrvGBufferView* g, const DrvConfig& c) {
   return g && g->depth && g->normal && g->albedo && g->width == c.width && g->height == c.height &&
          (g->normal_format == DRV_NORMAL_RG16I || g->normal_format == DRV_NORMAL_F32X3) &&
@@ -162,14 +173,9 @@ drv_status drv_create(const DrvConfig* cfg, DrvContext** out) {
   if ((e = cudaMalloc(&c->mips, off * 4)) != cudaSuccess) return bail(e);
   if ((e = cudaMalloc(&c->vox_corners, (size_t)N * N * N)) != cudaSuccess) return bail(e);
 
-  // Light-stage chunk partials and per-cache tickets (tickets are reset by the
-  // kernel that consumes them, so they are zeroed once here).
-  if ((e = cudaMalloc(&c->light_scratch, (size_t)cfg->max_caches * drv::kMaxLightChunks * (cfg->sh_order == 2 ? 27 : 12) * 4)) !=
-      cudaSuccess)
-    return bail(e);
-  // Tickets, then the two words of the dynamic unit counter.
-  if ((e = cudaMalloc(&c->light_tickets, ((size_t)cfg->max_caches + 2) * 4)) != cudaSuccess) return bail(e);
-  if ((e = cudaMemset(c->light_tickets, 0, ((size_t)cfg->max_caches + 2) * 4)) != cudaSuccess) return bail(e);
+  // The single-launch light stage's scratch, where frames need it from the
+  // start (no indirect shadow); otherwise on first use (ensure_single_scratch).
+  if (!cfg->indirect_shadow && (e = ensure_single_scratch(c)) != cudaSuccess) return bail(e);
   // RSM chains (levels below the caller's render-resolution level) and VPLs.
   const int R = cfg->max_rsm_resolution;
   for (int l = 0; l < cfg->max_lights; ++l) {
@@ -183,11 +189,13 @@ drv_status drv_create(const DrvConfig* cfg, DrvContext** out) {
     if ((e = cudaMalloc(&c->cones[l], (size_t)R * R * sizeof(DrvShadowCone))) != cudaSuccess) return bail(e);
   }
   if ((e = cudaMalloc(&c->sur_weights, drv::surrogate_weights_bytes())) != cudaSuccess) return bail(e);
-  // Pair list of the split light stage: room for 64 contributing shadow
-  // blocks per cache on average (clamped to [2^20, 2^25] pairs, 21 B each);
-  // caches beyond a full list are traced by the gather itself.
+  // Pair list of the split light stage: room for 256 contributing shadow
+  // blocks per cache on average (clamped to [2^22, 2^26] pairs, 21 B each:
+  // 88 MB .. 1.4 GB); caches beyond a full list are traced by the gather
+  // itself, with exact cones also when the surrogate is on.
   {
-    const uint64_t cap = std::min<uint64_t>(std::max<uint64_t>((uint64_t)cfg->max_caches * 64u, 1u << 20), 1u << 25);
+    const uint64_t cap =
+        std::min<uint64_t>(std::max<uint64_t>((uint64_t)cfg->max_caches * 256u, 1ull << 22), 1ull << 26);
     const size_t bytes = (size_t)cap * 21 + (size_t)cfg->max_caches * 8 + drv::kPairCounters * 4;
     if ((e = cudaMalloc(&c->pair_mem, bytes)) != cudaSuccess) return bail(e);
     if ((e = cudaMemset(c->pair_mem, 0, bytes)) != cudaSuccess) return bail(e);
@@ -409,8 +417,6 @@ drv_status drv_light_caches(DrvContext* ctx, const DrvSpotLight* lights, int32_t
     ll.lights[l].n_vpls = ctx->n_vpls[l];
     ll.lights[l].interval = ctx->interval[l];
   }
-  const drv::LightScratch scratch{ctx->light_scratch, ctx->light_tickets, ctx->light_tickets + ctx->cfg.max_caches,
-                                  drv::kMaxLightChunks};
   const bool surrogate = ctx->cfg.visibility == DRV_VISIBILITY_SURROGATE && ctx->cfg.indirect_shadow;
   if (surrogate && !ctx->sur_ready)
     return fail(ctx, DRV_ERR_INVALID_ARG, "surrogate visibility needs drv_set_surrogate_params");
@@ -443,6 +449,15 @@ drv_status drv_light_caches(DrvContext* ctx, const DrvSpotLight* lights, int32_t
   for (int l = 0; l < ll.n_lights; ++l) blocks += ll.lights[l].n_vpls / ll.lights[l].interval;
   if (surrogate && blocks > drv::kMaxSplitBlocks)
     return fail(ctx, DRV_ERR_INVALID_ARG, "surrogate visibility supports at most 65536 shadow blocks per frame");
+  if (!ctx->light_scratch) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    DRV_TRY_CUDA(ctx, cudaStreamIsCapturing(ctx->s(), &cs));
+    if (cs != cudaStreamCaptureStatusNone)
+      return fail(ctx, DRV_ERR_INVALID_ARG, "first single-launch light stage while the stream is being captured");
+    DRV_TRY_CUDA(ctx, ensure_single_scratch(ctx));
+  }
+  const drv::LightScratch scratch{ctx->light_scratch, ctx->light_tickets, ctx->light_tickets + ctx->cfg.max_caches,
+                                  drv::kMaxLightChunks};
   return cuda_check(ctx, drv::launch_light_caches(ctx->s(), ctx->cfg, *vol, ll, ctx->counter, ctx->entries,
                                                   ctx->entry_stride, ctx->voxels(), scratch, ctx->num_sms),
                     "light_caches");
@@ -507,6 +522,7 @@ drv_status drv_set_tuning(DrvContext* ctx, const DrvTuning* t) {
   if (t->light_path < DRV_LIGHT_PATH_AUTO || t->light_path > DRV_LIGHT_PATH_SPLIT || t->cone_ctas_per_sm < 0 ||
       t->gather_ctas_per_sm < 0 || t->cone_ctas_per_sm > 32 || t->gather_ctas_per_sm > 32)
     return fail(ctx, DRV_ERR_INVALID_ARG, "bad tuning");
+  if (t->light_path == DRV_LIGHT_PATH_SINGLE) DRV_TRY_CUDA(ctx, ensure_single_scratch(ctx));
   ctx->tuning = *t;
   return DRV_OK;
 }

@@ -193,3 +193,7 @@ cudaError_t launch_surrogate_train_step(cudaStream_t s, const float* X, const fl
 
 
 }  // namespace drv
+
+// The opaque handle of the C ABI is the context itself.
+struct DrvContext : drv::Context {};
+

@@ -330,6 +330,8 @@ template <int NK, bool BF16>
 __global__ void __launch_bounds__(kGatherThreads) gather_kernel(StageParams p, PairList L) {
   constexpr bool KAHAN = BF16;  // FP32 accumulation of BF16-stored results, compensated
   __shared__ float s_red[kGatherWarps][NK * 3];
+  __shared__ uint32_t s_count[kGatherWarps];  // list-full path: contributing blocks per warp
+  __shared__ int s_block[kGatherThreads];     // list-full path: this chunk's contributing blocks
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t n_caches = cache_count(p);
   for (uint32_t c = blockIdx.x; c < n_caches; c += gridDim.x) {
@@ -345,9 +347,33 @@ __global__ void __launch_bounds__(kGatherThreads) gather_kernel(StageParams p, P
         gather_block<NK, BF16, KAHAN>(p, acc, comp, (int)L.block[i], cx, cy, cz, L.shadow[i]);
       }
     } else {
-      for (int b = threadIdx.x; b < p.total_blocks; b += kGatherThreads)
-        if (block_live<BF16>(p, b, cx, cy, cz))
-          gather_block<NK, BF16, KAHAN>(p, acc, comp, b, cx, cy, cz, block_cone(p, b, cx, cy, cz));
+      // The list was full: trace this cache's cones here. The k-th
+      // contributing block goes to thread k mod kGatherThreads, as the k-th
+      // listed pair does above, so every thread sums the same pairs in the
+      // same order and the result is bitwise the same either way.
+      uint32_t before = 0;  // contributing blocks in earlier chunks
+      for (int b0 = 0; b0 < p.total_blocks; b0 += kGatherThreads) {
+        const int b = b0 + threadIdx.x;
+        const bool live = b < p.total_blocks && block_live<BF16>(p, b, cx, cy, cz);
+        const uint32_t m = __ballot_sync(0xffffffffu, live);
+        if (lane == 0) s_count[warp] = __popc(m);
+        __syncthreads();
+        uint32_t rank = __popc(m & ((1u << lane) - 1u)), n = 0;
+#pragma unroll
+        for (int w = 0; w < kGatherWarps; ++w) {
+          if (w < warp) rank += s_count[w];
+          n += s_count[w];
+        }
+        if (live) s_block[rank] = b;
+        __syncthreads();
+        const uint32_t i = (uint32_t)(threadIdx.x + kGatherThreads - before % kGatherThreads) % kGatherThreads;
+        if (i < n) {
+          const int bb = s_block[i];
+          gather_block<NK, BF16, KAHAN>(p, acc, comp, bb, cx, cy, cz, block_cone(p, bb, cx, cy, cz));
+        }
+        before += n;
+        __syncthreads();
+      }
     }
 #pragma unroll
     for (int k = 0; k < NK * 3; ++k) {

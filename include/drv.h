@@ -456,6 +456,38 @@ enum {
  * DRV_ERR_INVALID_ARG when no such stage ran. */
 drv_status drv_get_light_kernel_ms(DrvContext* ctx, float ms[DRV_LK_COUNT]);
 
+/* ---- batched frames ---------------------------------------------------------
+ * No counterpart in the reference (one scene per renderer). Many scenes'
+ * frames -- each its own context, inputs and sizes -- captured once into one
+ * CUDA graph, the scenes dealt round-robin over n_streams concurrent branches,
+ * and replayed with one launch. Every scene's drv_frame arguments are copied
+ * into the graph at capture (kernel parameters by value): new cameras,
+ * lights or buffers need a new batch. The scenes' contexts must not be used
+ * on other streams while a batch of theirs runs. */
+typedef struct DrvBatchScene {
+  DrvContext* ctx;
+  const DrvScene* scene;
+  const DrvGBufferView* gbuffer;
+  const DrvPerFrame* frame;
+  const DrvVolumeInfo* volume;
+  const DrvSpotLight* lights;
+  const DrvRSMView* rsms;
+  int32_t n_lights;
+  float* out_rgb;                   /* device, width*height*3 */
+} DrvBatchScene;
+typedef struct DrvBatch DrvBatch;
+/* cuda_stream: the stream the capture starts from and joins back to (not the
+ * legacy default stream; NULL: an internal one). Each context's stream
+ * setting is restored after the capture. */
+drv_status drv_batch_create(const DrvBatchScene* scenes, int32_t n_scenes, int32_t n_streams, void* cuda_stream,
+                            DrvBatch** out);
+/* One launch of the whole batch on cuda_stream (NULL: the capture stream). */
+drv_status drv_batch_launch(DrvBatch* batch, void* cuda_stream);
+/* After a launch: per scene, milliseconds from the batch's start to the end
+ * of that scene's frame, and the batch's total. Synchronises. */
+drv_status drv_batch_times(DrvBatch* batch, float* scene_ms, float* total_ms);
+drv_status drv_batch_destroy(DrvBatch* batch);
+
 /* ---- allocation-free light stage ------------------------------------------
  * No counterpart in the reference: the reference renderer always owns its GL
  * buffers. This is the cache-lighting stage (the kernel behind
