@@ -65,6 +65,12 @@ def make_scenes(specs, threshold: float = 0.5, params=None, device: str = "cuda"
         p.raycast_inputs()
         p.frame()
         p.sync()
+        # The pair list sized to this scene's contributing pairs (+25%): grown
+        # where the default is too small, so that no cache falls back to the
+        # gather's own cones.
+        p.set_tuning(pair_capacity=min(int(p.light_pairs() * 1.25) + 4096, 1 << 28))
+        p.frame()
+        p.sync()
         scenes.append(Scene(p, p.cache_count(), w.n_vpls))
     return scenes
 

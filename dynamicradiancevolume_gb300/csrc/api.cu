@@ -106,6 +106,32 @@ cudaError_t ensure_single_scratch(Context* c) {
   return cudaMemset(c->light_tickets, 0, (n + 2) * 4);
 }
 
+// (Re)allocates the pair list for `cap` pairs (one allocation, carved up).
+cudaError_t alloc_pairs(Context* c, uint64_t cap) {
+  if (cap > 0xFFFFFFF0ull) return cudaErrorInvalidValue;
+  if (c->pair_mem) {
+    cudaError_t e = cudaStreamSynchronize(c->s());
+    if (e != cudaSuccess) return e;
+    cudaFree(c->pair_mem);
+    c->pair_mem = nullptr;
+  }
+  const size_t bytes = (size_t)cap * 21 + (size_t)c->cfg.max_caches * 8 + drv::kPairCounters * 4;
+  cudaError_t e = cudaMalloc(&c->pair_mem, bytes);
+  if (e != cudaSuccess) return e;
+  if ((e = cudaMemset(c->pair_mem, 0, bytes)) != cudaSuccess) return e;
+  uint32_t* w = static_cast<uint32_t*>(c->pair_mem);
+  c->pairs.cache = w;
+  c->pairs.block = w + cap;
+  c->pairs.shadow = reinterpret_cast<float*>(w + 2 * cap);
+  c->pairs.order = w + 3 * cap;
+  c->pairs.retrace = w + 4 * cap;
+  c->pairs.info = w + 5 * cap;
+  c->pairs.counters = w + 5 * cap + 2 * (size_t)c->cfg.max_caches;
+  c->pairs.cls = reinterpret_cast<uint8_t*>(c->pairs.counters + drv::kPairCounters);
+  c->pairs.cap = (uint32_t)cap;
+  return cudaSuccess;
+}
+
 bool views_ok(const DrvGBufferView* g, const DrvConfig& c) {
   return g && g->depth && g->normal && g->albedo && g->width == c.width && g->height == c.height &&
          (g->normal_format == DRV_NORMAL_RG16I || g->normal_format == DRV_NORMAL_F32X3) &&
@@ -191,25 +217,12 @@ drv_status drv_create(const DrvConfig* cfg, DrvContext** out) {
   if ((e = cudaMalloc(&c->sur_weights, drv::surrogate_weights_bytes())) != cudaSuccess) return bail(e);
   // Pair list of the split light stage: room for 256 contributing shadow
   // blocks per cache on average (clamped to [2^22, 2^26] pairs, 21 B each:
-  // 88 MB .. 1.4 GB); caches beyond a full list are traced by the gather
-  // itself, with exact cones also when the surrogate is on.
-  {
-    const uint64_t cap =
-        std::min<uint64_t>(std::max<uint64_t>((uint64_t)cfg->max_caches * 256u, 1ull << 22), 1ull << 26);
-    const size_t bytes = (size_t)cap * 21 + (size_t)cfg->max_caches * 8 + drv::kPairCounters * 4;
-    if ((e = cudaMalloc(&c->pair_mem, bytes)) != cudaSuccess) return bail(e);
-    if ((e = cudaMemset(c->pair_mem, 0, bytes)) != cudaSuccess) return bail(e);
-    uint32_t* w = static_cast<uint32_t*>(c->pair_mem);
-    c->pairs.cache = w;
-    c->pairs.block = w + cap;
-    c->pairs.shadow = reinterpret_cast<float*>(w + 2 * cap);
-    c->pairs.order = w + 3 * cap;
-    c->pairs.retrace = w + 4 * cap;
-    c->pairs.info = w + 5 * cap;
-    c->pairs.counters = w + 5 * cap + 2 * (size_t)cfg->max_caches;
-    c->pairs.cls = reinterpret_cast<uint8_t*>(c->pairs.counters + drv::kPairCounters);
-    c->pairs.cap = (uint32_t)cap;
-  }
+  // 88 MB .. 1.4 GB; DrvTuning.pair_capacity grows it); caches beyond a full
+  // list are traced by the gather itself, with exact cones also when the
+  // surrogate is on.
+  if ((e = alloc_pairs(c, std::min<uint64_t>(std::max<uint64_t>((uint64_t)cfg->max_caches * 256u, 1ull << 22),
+                                             1ull << 26))) != cudaSuccess)
+    return bail(e);
   c->box_capacity = 512;
   if ((e = cudaMallocHost(&c->h_boxes, c->box_capacity * sizeof(DrvBox))) != cudaSuccess) return bail(e);
   if ((e = cudaMalloc(&c->d_boxes, c->box_capacity * sizeof(DrvBox))) != cudaSuccess) return bail(e);
@@ -523,6 +536,13 @@ drv_status drv_set_tuning(DrvContext* ctx, const DrvTuning* t) {
       t->gather_ctas_per_sm < 0 || t->cone_ctas_per_sm > 32 || t->gather_ctas_per_sm > 32)
     return fail(ctx, DRV_ERR_INVALID_ARG, "bad tuning");
   if (t->light_path == DRV_LIGHT_PATH_SINGLE) DRV_TRY_CUDA(ctx, ensure_single_scratch(ctx));
+  if (t->pair_capacity > ctx->pairs.cap) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    DRV_TRY_CUDA(ctx, cudaStreamIsCapturing(ctx->s(), &cs));
+    if (cs != cudaStreamCaptureStatusNone)
+      return fail(ctx, DRV_ERR_INVALID_ARG, "the pair list cannot grow while the stream is being captured");
+    DRV_TRY_CUDA(ctx, alloc_pairs(ctx, t->pair_capacity));
+  }
   ctx->tuning = *t;
   return DRV_OK;
 }
@@ -532,7 +552,7 @@ drv_status drv_get_light_pairs(DrvContext* ctx, uint32_t* pairs) {
   uint32_t n = 0;
   DRV_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->s()));
   DRV_TRY_CUDA(ctx, cudaMemcpy(&n, ctx->pairs.counters, 4, cudaMemcpyDeviceToHost));
-  *pairs = std::min(n, ctx->pairs.cap);
+  *pairs = n;
   return DRV_OK;
 }
 

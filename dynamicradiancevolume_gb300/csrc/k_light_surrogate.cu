@@ -58,31 +58,27 @@ __device__ __forceinline__ void ldmatrix_x4(uint32_t (&r)[4], const void* smem_r
                : "r"(addr));
 }
 
-// One hidden layer for both 16-row m-tiles: in = A fragments [2][KSTEPS][4],
-// out = A fragments of the next layer [2][4][4] after bias + GELU. The
-// accumulators start at the bias (D = A B + C with C = bias).
+// One hidden layer for one 16-row m-tile: in = A fragments [KSTEPS][4], out
+// = A fragments of the next layer [4][4] after bias + GELU. The accumulators
+// start at the bias (D = A B + C with C = bias).
 template <int KSTEPS, int LD>
-__device__ __forceinline__ void hidden_layer(const uint32_t (&in)[2][KSTEPS][4], const uint16_t* w, const float* bias,
-                                             uint32_t (&out)[2][4][4], int g, int tig) {
+__device__ __forceinline__ void hidden_layer(const uint32_t (&in)[KSTEPS][4], const uint16_t* w, const float* bias,
+                                             uint32_t (&out)[4][4], int g, int tig) {
 #pragma unroll
   for (int j = 0; j < kMlpHidden / 8; ++j) {
     const float bl = bias[8 * j + 2 * tig], bh = bias[8 * j + 2 * tig + 1];
-    float acc[2][4] = {{bl, bh, bl, bh}, {bl, bh, bl, bh}};
+    float acc[4] = {bl, bh, bl, bh};
     const uint16_t* wr = w + (8 * j + g) * LD + 2 * tig;
 #pragma unroll
     for (int kk = 0; kk < KSTEPS; ++kk) {
       const uint32_t b0 = *reinterpret_cast<const uint32_t*>(wr + 16 * kk);
       const uint32_t b1 = *reinterpret_cast<const uint32_t*>(wr + 16 * kk + 8);
-      mma_bf16(acc[0], in[0][kk], b0, b1);
-      mma_bf16(acc[1], in[1][kk], b0, b1);
+      mma_bf16(acc, in[kk], b0, b1);
     }
-#pragma unroll
-    for (int m = 0; m < 2; ++m) {
-      // n-tile j feeds k-step j/2 of the next layer: even tiles are its low
-      // k half (regs 0,1), odd tiles its high half (regs 2,3).
-      out[m][j >> 1][(j & 1) * 2 + 0] = gelu_bf16x2(pack_bf16x2(acc[m][0], acc[m][1]));
-      out[m][j >> 1][(j & 1) * 2 + 1] = gelu_bf16x2(pack_bf16x2(acc[m][2], acc[m][3]));
-    }
+    // n-tile j feeds k-step j/2 of the next layer: even tiles are its low k
+    // half (regs 0,1), odd tiles its high half (regs 2,3).
+    out[j >> 1][(j & 1) * 2 + 0] = gelu_bf16x2(pack_bf16x2(acc[0], acc[1]));
+    out[j >> 1][(j & 1) * 2 + 1] = gelu_bf16x2(pack_bf16x2(acc[2], acc[3]));
   }
 }
 
@@ -136,38 +132,37 @@ __global__ void __launch_bounds__(kThreads) mlp_kernel(StageParams p, PairList L
 #pragma unroll
     for (int k = 0; k < kMlpIn / 2; ++k) row[k] = pack_bf16x2(f[2 * k], f[2 * k + 1]);
     __syncwarp();
-    uint32_t a1[2][2][4];
+    // The two 16-row m-tiles one after the other: one tile's fragments are
+    // live at a time, which keeps the kernel near 64 registers.
+    float o[2][4];
 #pragma unroll
-    for (int m = 0; m < 2; ++m)
+    for (int m = 0; m < 2; ++m) {
+      uint32_t a1[2][4];
 #pragma unroll
       for (int kk = 0; kk < 2; ++kk)
-        ldmatrix_x4(a1[m][kk],
-                    xt + (16 * m + (lane & 7) + ((lane >> 3) & 1) * 8) * kLd1 + 16 * kk + ((lane >> 4) & 1) * 8);
-    __syncwarp();
-    uint32_t h1[2][4][4], h2[2][4][4];
-    hidden_layer<2, kLd1>(a1, s_w.w1, s_w.b1, h1, g, tig);
-    // Layers 2 and 3 have one shape: one copy of their code (instruction cache).
+        ldmatrix_x4(a1[kk], xt + (16 * m + (lane & 7) + ((lane >> 3) & 1) * 8) * kLd1 + 16 * kk +
+                                ((lane >> 4) & 1) * 8);
+      uint32_t h1[4][4], h2[4][4];
+      hidden_layer<2, kLd1>(a1, s_w.w1, s_w.b1, h1, g, tig);
+      // Layers 2 and 3 have one shape: one copy of their code (instruction cache).
 #pragma unroll 1
-    for (int layer = 0; layer < 2; ++layer) {
-      hidden_layer<4, kLdH>(h1, layer ? s_w.w3 : s_w.w2, layer ? s_w.b3 : s_w.b2, h2, g, tig);
-#pragma unroll
-      for (int m = 0; m < 2; ++m)
+      for (int layer = 0; layer < 2; ++layer) {
+        hidden_layer<4, kLdH>(h1, layer ? s_w.w3 : s_w.w2, layer ? s_w.b3 : s_w.b2, h2, g, tig);
 #pragma unroll
         for (int kk = 0; kk < 4; ++kk)
 #pragma unroll
-          for (int r = 0; r < 4; ++r) h1[m][kk][r] = h2[m][kk][r];
-    }
-    float o[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
-    {
+          for (int r = 0; r < 4; ++r) h1[kk][r] = h2[kk][r];
+      }
+      o[m][0] = o[m][1] = o[m][2] = o[m][3] = 0.0f;
       const uint16_t* wr = s_w.w4 + g * kLdH + 2 * tig;
 #pragma unroll
       for (int kk = 0; kk < 4; ++kk) {
         const uint32_t bb0 = *reinterpret_cast<const uint32_t*>(wr + 16 * kk);
         const uint32_t bb1 = *reinterpret_cast<const uint32_t*>(wr + 16 * kk + 8);
-        mma_bf16(o[0], h1[0][kk], bb0, bb1);
-        mma_bf16(o[1], h1[1][kk], bb0, bb1);
+        mma_bf16(o[m], h1[kk], bb0, bb1);
       }
     }
+    __syncwarp();
     // (visibility, confidence) of row `lane`: held by lane 4*(row&7),
     // registers 0,1 (rows 0-7 of an m-tile) or 2,3 (rows 8-15).
     const int src = 4 * (lane & 7);

@@ -238,7 +238,7 @@ class Pipeline:
         return t
 
     def light_pairs(self) -> int:
-        """Pairs the last split light stage listed (each traced or evaluated once)."""
+        """Contributing (cache, block) pairs of the last split light stage."""
         n = C.c_uint32()
         self._c(self.lib.drv_get_light_pairs(self.ctx, C.byref(n)))
         return n.value

@@ -430,8 +430,9 @@ drv_status drv_get_surrogate_stats(DrvContext* ctx, uint32_t* evaluated, uint32_
  * same up to the order of FP32 summation. Zero fields keep the default. */
 typedef struct DrvTuning {
   int32_t light_path;      /* DRV_LIGHT_PATH_*: light stage as one launch or as cull, cone, gather */
-  uint32_t pair_capacity;  /* split stage: pairs the list may hold (<= its allocation); caches that do
-                              not fit are traced by the gather itself. 0: the whole allocation */
+  uint32_t pair_capacity;  /* split stage: pairs the list may hold; caches that do not fit are traced
+                              by the gather itself (exact cones). 0: the whole allocation; above the
+                              allocation: the list grows to it (synchronises; not while capturing) */
   int32_t cone_ctas_per_sm;   /* split stage: CTAs of the cone pass per SM (0: as many as fit) */
   int32_t gather_ctas_per_sm; /* split stage: CTAs of the gather pass per SM (0: as many as fit) */
   int32_t time_kernels;       /* nonzero: the split light stage records CUDA events between its
@@ -442,8 +443,9 @@ enum { DRV_LIGHT_PATH_AUTO = 0, DRV_LIGHT_PATH_SINGLE = 1, DRV_LIGHT_PATH_SPLIT 
 drv_status drv_set_tuning(DrvContext* ctx, const DrvTuning* tuning);
 drv_status drv_get_tuning(DrvContext* ctx, DrvTuning* tuning);
 
-/* (cache, shadow block) pairs the last split light stage listed as able to
- * contribute (each traced or evaluated once). Synchronises. */
+/* (cache, shadow block) pairs the last split light stage found able to
+ * contribute (each traced or evaluated once; those beyond the list's
+ * capacity traced by the gather). Synchronises. */
 drv_status drv_get_light_pairs(DrvContext* ctx, uint32_t* pairs);
 
 /* Kernels of the split light stage, in launch order (DrvTuning.time_kernels). */
