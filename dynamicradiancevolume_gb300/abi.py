@@ -187,6 +187,9 @@ PROTOTYPES = {
     "drv_get_tuning": (C.c_int, [VP, P(DrvTuning)]),
     "drv_get_light_kernel_ms": (C.c_int, [VP, P(C.c_float)]),
     "drv_get_light_pairs": (C.c_int, [VP, P(C.c_uint32)]),
+    "drv_bruteforce_rsm": (C.c_int, [VP, P(DrvGBufferView), VP, P(DrvPerFrame), C.c_int32, VP]),
+    "drv_write_pfm": (C.c_int, [C.c_char_p, P(C.c_float), C.c_int32, C.c_int32, C.c_int32]),
+    "drv_read_pfm": (C.c_int, [C.c_char_p, P(C.c_float), C.c_int64, P(C.c_int32), P(C.c_int32)]),
     "drv_batch_create": (C.c_int, [P(DrvBatchScene), C.c_int32, C.c_int32, VP, P(VP)]),
     "drv_batch_launch": (C.c_int, [VP, VP]),
     "drv_batch_times": (C.c_int, [VP, P(C.c_float), P(C.c_float)]),

@@ -530,6 +530,23 @@ drv_status drv_get_surrogate_fallbacks(DrvContext* ctx, uint32_t* out) {
   return DRV_OK;
 }
 
+drv_status drv_bruteforce_rsm(DrvContext* ctx, const DrvGBufferView* g, const float* rough_metal,
+                              const DrvPerFrame* f, int32_t n_lights, float* out_rgb) {
+  if (!ctx || !f || !out_rgb || n_lights < 0 || n_lights > ctx->cfg.max_lights) return DRV_ERR_INVALID_ARG;
+  if (!views_ok(g, ctx->cfg)) return fail(ctx, DRV_ERR_INVALID_ARG, "G-buffer view does not match the config");
+  drv::LightLaunch ll{};
+  ll.n_lights = n_lights;
+  for (int l = 0; l < n_lights; ++l) {
+    if (ctx->n_vpls[l] < 1) return fail(ctx, DRV_ERR_INVALID_ARG, "drv_extract_vpls must run for every light first");
+    ll.lights[l].vpls = ctx->vpls[l];
+    ll.lights[l].n_vpls = ctx->n_vpls[l];
+    ll.lights[l].interval = 1;
+  }
+  return cuda_check(ctx, drv::launch_bruteforce_rsm(ctx->s(), *f, *g, rough_metal, ll,
+                                                    ctx->cfg.precision == DRV_PRECISION_BF16, out_rgb),
+                    "bruteforce_rsm");
+}
+
 drv_status drv_set_tuning(DrvContext* ctx, const DrvTuning* t) {
   if (!ctx || !t) return DRV_ERR_INVALID_ARG;
   if (t->light_path < DRV_LIGHT_PATH_AUTO || t->light_path > DRV_LIGHT_PATH_SPLIT || t->cone_ctas_per_sm < 0 ||

@@ -161,6 +161,9 @@ class Pipeline:
         for l in range(w.n_lights):
             self.rsm_views[l] = abi.DrvRSMView(R, self.rsm_flux[l].data_ptr(), self.rsm_normal[l].data_ptr(),
                                                self.rsm_dls[l].data_ptr())
+        # torch's pooled streams do not wait for its current stream, where the
+        # buffers above were zeroed: finish that before any stage runs.
+        torch.cuda.current_stream(self.device).synchronize()
 
     def set_frame(self, hf: HostFrame) -> None:
         """Switches to another frame of the same workload (scene, camera,
@@ -218,6 +221,20 @@ class Pipeline:
         out = self.out if out is None else out
         self._c(self.lib.drv_apply(self.ctx, C.byref(self.gview), C.byref(self.hf.frame), C.byref(self.hf.volume),
                                    C.c_void_p(out.data_ptr())))
+
+    def bruteforce(self, out=None, rough_metal=None):
+        """Unshadowed per-pixel gather over every VPL (no caches) into `out`
+        (a new tensor when None); rough_metal: (H, W, 2) device tensor for the
+        reference BRDF, None for its diffuse term."""
+        out = self.torch.zeros_like(self.out) if out is None else out
+        # the caller's tensors were written on torch's current stream
+        self.stream.wait_stream(self.torch.cuda.current_stream(self.device))
+        rm = C.c_void_p(rough_metal.data_ptr()) if rough_metal is not None else None
+        self._c(self.lib.drv_bruteforce_rsm(self.ctx, C.byref(self.gview), rm, C.byref(self.hf.frame),
+                                            self.hf.workload.n_lights, C.c_void_p(out.data_ptr())))
+        # `out` is handed back to work on torch's current stream
+        self.torch.cuda.current_stream(self.device).wait_stream(self.stream)
+        return out
 
     def frame(self, out=None):
         out = self.out if out is None else out

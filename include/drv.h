@@ -458,6 +458,24 @@ enum {
  * DRV_ERR_INVALID_ARG when no such stage ran. */
 drv_status drv_get_light_kernel_ms(DrvContext* ctx, float ms[DRV_LK_COUNT]);
 
+/* ---- brute-force RSM gather and image dumps --------------------------------
+ * Renderer::ApplyRSMsBruteForce (renderer.cpp:851-871, bruteforcersm.frag):
+ * per pixel, the unshadowed sum over every VAL (the context's extracted
+ * VPLs of lights 0..n_lights-1; drv_extract_vpls must have run for each)
+ * without caches: the ground truth the cache volume interpolates. out_rgb:
+ * device, width*height*3. rough_metal: device RG F32 per pixel for the
+ * reference BRDF (normalized Blinn-Phong + metallic, lightingfunctions.glsl),
+ * or NULL for its diffuse term albedo/pi (the cache path's). Pixels with
+ * depth below 1e-5 are 0. */
+drv_status drv_bruteforce_rsm(DrvContext* ctx, const DrvGBufferView* gbuffer, const float* rough_metal,
+                              const DrvPerFrame* frame, int32_t n_lights, float* out_rgb);
+/* The reference's PFM dump (rendering/hdrimage.cpp:6-66): host RGB floats
+ * (channels 3, or 4 with the 4th skipped), row 0 first. */
+drv_status drv_write_pfm(const char* path, const float* rgb, int32_t width, int32_t height, int32_t channels);
+/* Reads an RGB PFM written that way: width/height always, the pixels when rgb
+ * is non-NULL (DRV_ERR_CAPACITY when more than capacity_pixels). */
+drv_status drv_read_pfm(const char* path, float* rgb, int64_t capacity_pixels, int32_t* width, int32_t* height);
+
 /* ---- batched frames ---------------------------------------------------------
  * No counterpart in the reference (one scene per renderer). Many scenes'
  * frames -- each its own context, inputs and sizes -- captured once into one

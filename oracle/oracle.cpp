@@ -984,4 +984,72 @@ void orc_apply(const DrvConfig* cfg, const DrvVolumeInfo* vol, const DrvPerFrame
     }
 }
 
+// bruteforcersm.frag:15-82 (see oracle.h).
+void orc_bruteforce_rsm(const DrvPerFrame* f, int W, int H, const float* depth, const int16_t* normal16,
+                        const float* albedo, const float* rough_metal, int n_lights, const double* const* vpls,
+                        const int* n_vpls, double* out, int n_threads) {
+  set_threads(n_threads);
+  const d3 cam = mk(f->camera_position[0], f->camera_position[1], f->camera_position[2]);
+#pragma omp parallel for schedule(dynamic, 4)
+  for (int y = 0; y < H; ++y)
+    for (int x = 0; x < W; ++x) {
+      const size_t i = (size_t)y * W + x;
+      double* o = out + 3 * i;
+      o[0] = o[1] = o[2] = 0.0;
+      const float d = depth[i];
+      if (d < 0.00001f) continue;
+      float pf[3];
+      reconstruct_world_f32(f, x, y, W, H, d, pf);
+      const d3 p = mk(pf[0], pf[1], pf[2]);
+      double nn[3];
+      orc_unpack_normal16i(normal16 + 2 * i, nn);
+      const d3 n = mk(nn[0], nn[1], nn[2]);
+      const d3 base = mk(albedo[3 * i], albedo[3 * i + 1], albedo[3 * i + 2]);
+      // BRDF parameters, lightingfunctions.glsl:27-50.
+      d3 diffuse = base, specular = mk(0, 0, 0);
+      double blinn_exp = 0.0, blinn_norm = 0.0;
+      d3 to_cam = mk(0, 0, 0);
+      if (rough_metal) {
+        const double r = rough_metal[2 * i], m = rough_metal[2 * i + 1];
+        const double rsq = r * r;
+        blinn_exp = 2.0 / (rsq * rsq + 0.0005);
+        blinn_norm = (blinn_exp + 8.0) / (8.0 * kShaderPi);
+        diffuse = base * (1.0 - m) + mk(0.02, 0.02, 0.02) * m;
+        specular = mk(0.04, 0.04, 0.04) * (1.0 - m) + base * m;
+        d3 tc = cam - p;
+        to_cam = tc * (1.0 / std::sqrt(dot(tc, tc)));
+      }
+      double acc[3] = {0, 0, 0};
+      for (int l = 0; l < n_lights; ++l) {
+        const double* V = vpls[l];
+        for (int j = 0; j < n_vpls[l]; ++j) {
+          const double* v = V + 10 * j;
+          d3 to = mk(v[4], v[5], v[6]) - p;
+          const double d2 = dot(to, to);
+          to = to * (1.0 / std::sqrt(d2));
+          const double cos_theta = saturate(dot(to, n));
+          const double flux_to_intensity = saturate(dot(mk(v[7], v[8], v[9]), to * -1.0));
+          const double g = flux_to_intensity * cos_theta / (d2 + v[3]);
+          double brdf[3];
+          if (rough_metal) {
+            d3 h = to_cam + to;
+            h = h * (1.0 / std::sqrt(dot(h, h)));
+            const double bp = blinn_norm * std::pow(saturate(dot(n, h)), blinn_exp);
+            brdf[0] = diffuse.x / kShaderPi + bp * specular.x;
+            brdf[1] = diffuse.y / kShaderPi + bp * specular.y;
+            brdf[2] = diffuse.z / kShaderPi + bp * specular.z;
+          } else {
+            brdf[0] = diffuse.x / kShaderPi;
+            brdf[1] = diffuse.y / kShaderPi;
+            brdf[2] = diffuse.z / kShaderPi;
+          }
+          for (int ch = 0; ch < 3; ++ch) acc[ch] += brdf[ch] * v[ch] * g;
+        }
+      }
+      o[0] = acc[0];
+      o[1] = acc[1];
+      o[2] = acc[2];
+    }
+}
+
 }  // extern "C"

@@ -93,6 +93,17 @@ void orc_light_caches(const DrvConfig* cfg, const DrvVolumeInfo* vol, int n_cach
 void orc_light_caches_shadowed(const DrvConfig* cfg, int n_caches, const float* positions, int n_lights,
                                const DrvSpotLight* lights, const double* const* vpls, const int* n_vpls,
                                const double* shadow, int total_blocks, double* sh_out, int n_threads);
+/* Renderer::ApplyRSMsBruteForce (renderer.cpp:851-871) / bruteforcersm.frag:15-82:
+ * per pixel the unshadowed sum over every VAL of every light
+ * (bruteforcersm.frag:44-81), VALs as orc_extract_vpls makes them (the same
+ * position / normal / flux / disc-area formulas, bruteforcersm.frag:51-73).
+ * rough_metal (RG per pixel, may be NULL) selects the reference BRDF
+ * (lightingfunctions.glsl:27-66: normalized Blinn-Phong + metallic mix);
+ * NULL: the diffuse term albedo / pi of the cache path. Pixels with depth
+ * below 1e-5 (no geometry) are 0. normal: RG16I. */
+void orc_bruteforce_rsm(const DrvPerFrame* frame, int width, int height, const float* depth, const int16_t* normal16,
+                        const float* albedo, const float* rough_metal, int n_lights, const double* const* vpls,
+                        const int* n_vpls, double* out_rgb, int n_threads);
 /* cacheApply.frag per pixel; normal is RG16I (normal_format 0) or F32x3. */
 void orc_apply(const DrvConfig* cfg, const DrvVolumeInfo* vol, const DrvPerFrame* frame, int width, int height,
                const float* depth, const void* normal, int normal_format, const float* albedo, const uint32_t* atlas,

@@ -67,6 +67,7 @@ def load():
                                              I]),
         "orc_apply": (None, [P(abi.DrvConfig), P(abi.DrvVolumeInfo), P(abi.DrvPerFrame), I, I, VP, VP, I, VP, VP, I,
                              VP, VP, I]),
+        "orc_bruteforce_rsm": (None, [P(abi.DrvPerFrame), I, I, VP, VP, VP, VP, I, P(VP), P(I), VP, I]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -268,3 +269,20 @@ def apply(cfg, vol, frame, depth, normal, normal_format, albedo, atlas, sh, n_th
                      _p(np.ascontiguousarray(normal)), normal_format, _p(np.ascontiguousarray(albedo)),
                      _p(np.ascontiguousarray(atlas, dtype=np.uint32)), sh.shape[0], _p(sh), _p(out), n_threads)
     return out
+
+
+def bruteforce_rsm(frame, depth, normal16, albedo, vpls, rough_metal=None, n_threads=0):
+    """Unshadowed per-pixel gather over every VAL (bruteforcersm.frag)."""
+    H, W = depth.shape
+    out = np.zeros((H, W, 3), np.float64)
+    L = len(vpls)
+    keep = [np.ascontiguousarray(v, dtype=np.float64) for v in vpls]
+    vp = (C.c_void_p * L)(*[v.ctypes.data for v in keep])
+    nv = (C.c_int * L)(*[v.shape[0] for v in keep])
+    rm = None if rough_metal is None else np.ascontiguousarray(rough_metal, dtype=np.float32)
+    load().orc_bruteforce_rsm(C.byref(frame), W, H, _p(np.ascontiguousarray(depth, dtype=np.float32)),
+                              _p(np.ascontiguousarray(normal16, dtype=np.int16)),
+                              _p(np.ascontiguousarray(albedo, dtype=np.float32)), None if rm is None else _p(rm), L,
+                              vp, nv, _p(out), n_threads)
+    return out
+

@@ -117,3 +117,22 @@ def test_invalid_arguments_are_rejected_without_a_gpu(lib):
     L = abi.DrvSpotLight()
     assert lib.drv_prepare_light(C.byref(d), C.byref(L)) == abi.ERR_INVALID_ARG
     assert lib.drv_sync(None) == abi.ERR_INVALID_ARG
+
+
+@pytest.mark.parametrize("channels", [3, 4])
+def test_pfm_round_trip_and_header(lib, tmp_path, channels):
+    # rendering/hdrimage.cpp: "PF\n<w> <h>\n-1.000000\n" then RGB floats, row 0 first
+    import ctypes as C
+    w, h = 5, 3
+    img = np.random.default_rng(channels).random((h, w, channels)).astype(np.float32)
+    path = str(tmp_path / "x.pfm").encode()
+    assert lib.drv_write_pfm(path, img.ctypes.data_as(C.POINTER(C.c_float)), w, h, channels) == 0
+    raw = open(path, "rb").read()
+    header = b"PF\n5 3\n-1.000000\n"
+    assert raw.startswith(header) and len(raw) == len(header) + w * h * 12
+    ww, hh = C.c_int32(), C.c_int32()
+    assert lib.drv_read_pfm(path, None, 0, C.byref(ww), C.byref(hh)) == 0 and (ww.value, hh.value) == (w, h)
+    back = np.zeros((h, w, 3), np.float32)
+    assert lib.drv_read_pfm(path, back.ctypes.data_as(C.POINTER(C.c_float)), 2, C.byref(ww), C.byref(hh)) == 2
+    assert lib.drv_read_pfm(path, back.ctypes.data_as(C.POINTER(C.c_float)), w * h, C.byref(ww), C.byref(hh)) == 0
+    assert np.array_equal(back, img[..., :3])

@@ -5,6 +5,10 @@ import math
 import numpy as np
 import pytest
 
+from dynamicradiancevolume_gb300 import abi
+
+KSHADER_PI = 3.14159265358979  # the shaders' PI (globalubos.glsl)
+
 
 def test_morton_decode_matches_bitwise_definition(oracle):
     # cacheLightingRSM.comp:46-62: x takes the even bits, y the odd bits.
@@ -209,3 +213,42 @@ def test_allocation_flat_wall_predictable(oracle):
     for z, y, x in zip(zs, ys, xs):
         p = pos[atlas[z, y, x] - 1]
         assert np.allclose(p, np.array([x, y, z]) * 0.25 - 0.5)
+
+
+def _unit_frame(oracle, cam_pos=(0.0, 0.0, 2.5)):
+    f = abi.DrvPerFrame()
+    for k in range(4):
+        f.inverse_view_projection[5 * k] = 1.0  # identity: world = (ndc.x, ndc.y, depth)
+        f.view_projection[5 * k] = 1.0
+    f.camera_position[:] = cam_pos
+    return f
+
+
+def test_bruteforce_single_val_facing_the_pixel(oracle):
+    # 1x1 image: the pixel sits at world (0, 0, 0.5) with normal +z; one VAL
+    # straight above at distance 1, facing down, unit flux, zero area.
+    f = _unit_frame(oracle)
+    depth = np.array([[0.5]], np.float32)
+    n16 = np.array([oracle.pack_normal16i((0.0, 0.0, 1.0))], np.int16).reshape(1, 1, 2)
+    alb = np.array([[[0.5, 0.25, 1.0]]], np.float32)
+    a64 = alb[0, 0].astype(np.float64)
+    v = np.zeros((1, 10))
+    v[0, 0:3] = 1.0          # flux
+    v[0, 3] = 0.0            # disc area
+    v[0, 4:7] = (0, 0, 1.5)  # position
+    v[0, 7:10] = (0, 0, -1)  # normal
+    nz = oracle.unpack_normal16i(n16[0, 0])[2]  # +z packs to within 2^-15 of the axis
+    out = oracle.bruteforce_rsm(f, depth, n16, alb, [v])
+    assert np.allclose(out[0, 0], a64 / KSHADER_PI * nz, rtol=1e-12)
+    # reference BRDF, roughness 1, metallic 0, camera straight above: the
+    # half vector is +z, so Blinn-Phong is (e + 8) / (8 pi) * (n.z)^e
+    rm = np.array([[[1.0, 0.0]]], np.float32)
+    e = 2.0 / (1.0 + 0.0005)
+    spec = (e + 8.0) / (8.0 * KSHADER_PI) * nz ** e * 0.04
+    out = oracle.bruteforce_rsm(f, depth, n16, alb, [v], rough_metal=rm)
+    assert np.allclose(out[0, 0], (a64 / KSHADER_PI + spec) * nz, rtol=1e-6)
+    # a VAL facing away (or below the surface) adds nothing; no geometry -> 0
+    v2 = v.copy()
+    v2[0, 7:10] = (0, 0, 1)
+    assert np.all(oracle.bruteforce_rsm(f, depth, n16, alb, [v2]) == 0.0)
+    assert np.all(oracle.bruteforce_rsm(f, np.zeros((1, 1), np.float32), n16, alb, [v]) == 0.0)
