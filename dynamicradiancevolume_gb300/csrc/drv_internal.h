@@ -68,7 +68,7 @@ struct LightScratch {
 constexpr uint32_t kNoPair = 0xFFFFFFFFu;
 constexpr uint32_t kPairOverflow = 0xFFFFFFFFu;
 constexpr int kMaxSplitBlocks = 65536;  // shadow blocks per frame the split stage handles
-constexpr int kConeClasses = 16;
+constexpr int kConeClasses = 32;
 constexpr int kPairCounters = 8 + 2 * kConeClasses;
 struct PairList {
   uint32_t* cache;

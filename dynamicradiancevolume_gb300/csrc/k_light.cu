@@ -207,30 +207,26 @@ __global__ void __launch_bounds__(kCullThreads) cull_kernel(StageParams p, PairL
 }
 
 // Cone class of a pair: about how many steps its cone marches when nothing
-// occludes it, in buckets of 4, and whether its radius passes one voxel (mip
-// samples) on the way. cone_shadow steps by max(1, g * dist) with
+// occludes it, in buckets of 4, and at which step, if any, its radius passes
+// one voxel (its samples move to mip levels): never, after step 16, after
+// step 8, or earlier. cone_shadow steps by max(1, g * dist) with
 // g = 2 dsr / (1 - dsr): unit steps up to dist = 1 / g, then the distance
 // grows by the factor 1 + g per step, until it reaches the goal. Classes
 // only order the cones; results do not depend on them.
+__device__ __forceinline__ float cone_steps_to(float dist, float g, float m) {
+  // steps until the marched distance reaches `dist`
+  return dist <= m ? ceilf(dist) : m + ceilf(__log2f(dist / m) / __log2f(1.0f + g));
+}
+
 __device__ __forceinline__ int cone_class(float light_dist, float voxel_size, float dsr, int max_steps) {
   const float goal = fmaxf(light_dist / voxel_size - 2.0f, 1.0f);
   const float g = 2.0f * dsr / (1.0f - dsr);
   const float m = g > 0.0f ? fmaxf(1.0f, floorf(1.0f / g)) : 3.0e38f;  // last unit step
-  float n, dist;
-  if (goal <= m) {
-    n = ceilf(goal);
-    dist = n;
-  } else {
-    const float r = __log2f(1.0f + g);
-    n = m + ceilf(__log2f(goal / m) / r);
-    dist = goal;
-  }
-  if (n > (float)max_steps) {
-    n = (float)max_steps;
-    dist = n <= m ? n : m * exp2f((n - m) * __log2f(1.0f + g));
-  }
-  const int len = min(max((int)n - 1, 0) >> 2, kConeClasses / 2 - 1);
-  return (dist * dsr > 1.0f ? kConeClasses / 2 : 0) + len;
+  const float n = fminf(cone_steps_to(goal, g, m), (float)max_steps);
+  const float n_mip = dsr > 0.0f ? cone_steps_to(1.0f / dsr, g, m) : 3.0e38f;  // first step with radius > 1
+  const int len = min(max((int)n - 1, 0) >> 2, 7);
+  const int mip = n_mip > n ? 0 : (n_mip > 16.0f ? 1 : (n_mip > 8.0f ? 2 : 3));
+  return mip * 8 + len;
 }
 
 constexpr int kClassThreads = 256;
