@@ -89,16 +89,15 @@ __device__ __forceinline__ void add_to_entry(float* entry, int k, float v) {
   }
 }
 
-// True when some VPL of shadow block b can contribute to the cache.
+// True when some VPL of shadow block b may contribute to the cache (a
+// superset of the blocks the gather's exact test keeps, see may_contribute).
 template <bool BF16>
 __device__ __forceinline__ bool block_live(const StageParams& p, int b, float cx, float cy, float cz) {
   const int l = block_light(p, b);
   const LightArgs& la = p.ll.lights[l];
   const int lb = b - p.block_base[l];
-  for (int j = 0; j < la.interval; ++j) {
-    const VplData v = load_vpl<BF16>(la.vpls, lb * la.interval + j);
-    if (contributes(v, transfer(v, cx, cy, cz))) return true;
-  }
+  for (int j = 0; j < la.interval; ++j)
+    if (may_contribute(load_vpl<BF16>(la.vpls, lb * la.interval + j), cx, cy, cz)) return true;
   return false;
 }
 

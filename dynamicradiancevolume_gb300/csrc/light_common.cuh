@@ -195,6 +195,18 @@ __device__ __forceinline__ void retire_cta(uint32_t* work) {
   }
 }
 
+// A superset of `contributes` that needs no normalisation or division:
+// positive flux and -(n . t) > -1e-6 max|t_i| with t = VPL - cache. The exact
+// test's sign of -(n . t / |t|) can differ from the sign of -(n . t) only
+// within a few roundings of zero, far inside that margin; a pair that passes
+// here but not there is gathered with weight 0.
+__device__ __forceinline__ bool may_contribute(const VplData& v, float cx, float cy, float cz) {
+  const float tx = v.px - cx, ty = v.py - cy, tz = v.pz - cz;
+  const float facing = -(v.nx * tx + v.ny * ty + v.nz * tz);
+  const float scale = fmaxf(fmaxf(fabsf(tx), fabsf(ty)), fabsf(tz));
+  return facing > -1e-6f * scale && (v.fr > 0.0f || v.fg > 0.0f || v.fb > 0.0f);
+}
+
 // SH gather of one VPL, cacheLightingRSM.comp:255-278. acc (and comp with
 // KAHAN) point at this thread's column of a [NK*3][stride] shared array.
 template <int NK, bool KAHAN>
