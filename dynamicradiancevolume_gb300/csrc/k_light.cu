@@ -345,7 +345,8 @@ __global__ void __launch_bounds__(kGatherThreads) gather_kernel(StageParams p, P
       // The list was full: trace this cache's cones here. The k-th
       // contributing block goes to thread k mod kGatherThreads, as the k-th
       // listed pair does above, so every thread sums the same pairs in the
-      // same order and the result is bitwise the same either way.
+      // same order and the result is the same either way (to FP32 rounding:
+      // the cone is inlined here and in cone_kernel).
       uint32_t before = 0;  // contributing blocks in earlier chunks
       for (int b0 = 0; b0 < p.total_blocks; b0 += kGatherThreads) {
         const int b = b0 + threadIdx.x;

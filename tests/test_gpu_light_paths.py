@@ -1,8 +1,8 @@
 """The light stage's two execution forms — one launch (warp per cache chunk)
 and cull -> cone -> gather over a compacted pair list — give the same SH up
 to FP32 summation order; a pair list too small for the frame makes the gather
-trace the caches that did not fit, with bitwise the same result; the split
-form is deterministic run to run."""
+trace the caches that did not fit, with the same result to FP32 rounding; the
+split form is deterministic run to run."""
 import ctypes as C
 
 import numpy as np
@@ -51,10 +51,12 @@ def test_split_is_deterministic(cuda, lib):
 @pytest.mark.parametrize("cap", [1, 777, 20000])
 def test_full_pair_list_is_traced_by_the_gather(cap, cuda, lib):
     # caches that do not fit are traced by the gather with the same pair-to-
-    # thread assignment, so the SH are bitwise those of the listed path
+    # thread assignment and summation order; the cone code is inlined into
+    # two kernels, whose FMA contraction may differ, so the SH agree to FP32
+    # rounding
     p1, _, sh1 = _lit(REDUCED, 4)
     p2, _, sh2 = _lit(REDUCED, 4, pair_capacity=cap)
-    assert np.array_equal(sh2, sh1)
+    assert rel_l2(sh2, sh1) < 1e-6
     p1.close()
     p2.close()
 
