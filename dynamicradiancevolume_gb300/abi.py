@@ -117,12 +117,14 @@ class DrvBuffers(C.Structure):
                 ("counter", C.c_void_p), ("voxel_bits", C.c_void_p), ("voxel_corners", C.c_void_p),
                 ("voxel_mips", C.c_void_p * 16),
                 ("n_voxel_levels", C.c_int32), ("vpls", C.c_void_p * MAX_LIGHTS),
-                ("cones", C.c_void_p * MAX_LIGHTS), ("n_vpls", C.c_int32 * MAX_LIGHTS), ("n_lights", C.c_int32)]
+                ("cones", C.c_void_p * MAX_LIGHTS), ("n_vpls", C.c_int32 * MAX_LIGHTS), ("n_lights", C.c_int32),
+                ("voxel_mip_records", C.c_void_p * 16), ("n_record_levels", C.c_int32)]
 
 
 class DrvTuning(C.Structure):
     _fields_ = [("light_path", C.c_int32), ("pair_capacity", C.c_uint32), ("cone_ctas_per_sm", C.c_int32),
-                ("gather_ctas_per_sm", C.c_int32), ("time_kernels", C.c_int32), ("reserved", C.c_int32 * 3)]
+                ("gather_ctas_per_sm", C.c_int32), ("time_kernels", C.c_int32),
+                ("plain_voxel_reads", C.c_int32), ("reserved", C.c_int32 * 2)]
 
 
 LIGHT_KERNELS = ("cull", "classify", "scatter", "mlp", "cone", "gather")

@@ -46,6 +46,7 @@ void release(Context* c) {
   cudaFree(c->voxel_bits);
   cudaFree(c->mips);
   cudaFree(c->vox_corners);
+  cudaFree(c->vox_records);
 
   cudaFree(c->light_scratch);
   cudaFree(c->light_tickets);
@@ -64,6 +65,12 @@ void release(Context* c) {
   }
   cudaFree(c->d_boxes);
   cudaFreeHost(c->h_boxes);
+  for (int i = 0; i < 3; ++i) {
+    if (c->side[i]) cudaStreamDestroy(c->side[i]);
+    if (c->join_ev[i]) cudaEventDestroy(c->join_ev[i]);
+  }
+  if (c->fork_ev) cudaEventDestroy(c->fork_ev);
+  if (c->vox_fork_ev) cudaEventDestroy(c->vox_fork_ev);
   if (c->stream) cudaStreamDestroy(c->stream);
 }
 
@@ -175,6 +182,17 @@ drv_status drv_create(const DrvConfig* cfg, DrvContext** out) {
   if ((e = cudaGetDevice(&c->device)) != cudaSuccess) return bail(e);
   if ((e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device)) != cudaSuccess) return bail(e);
   if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) return bail(e);
+  // The side streams carry the frame's longest dependency chains (voxels,
+  // RSM): highest priority, so their small launches are not queued behind
+  // the allocation's CTAs.
+  int least = 0, greatest = 0;
+  if ((e = cudaDeviceGetStreamPriorityRange(&least, &greatest)) != cudaSuccess) return bail(e);
+  for (int i = 0; i < 3; ++i) {
+    if ((e = cudaStreamCreateWithPriority(&c->side[i], cudaStreamNonBlocking, greatest)) != cudaSuccess) return bail(e);
+    if ((e = cudaEventCreateWithFlags(&c->join_ev[i], cudaEventDisableTiming)) != cudaSuccess) return bail(e);
+  }
+  if ((e = cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming)) != cudaSuccess) return bail(e);
+  if ((e = cudaEventCreateWithFlags(&c->vox_fork_ev, cudaEventDisableTiming)) != cudaSuccess) return bail(e);
   // LightCacheBuffer: 64 B (SH1) or 128 B (SH2) entries (lightcache.glsl:33-76);
   // DrvCacheEntryBF16 (64 B) in BF16 precision.
   c->entry_stride = cfg->precision == DRV_PRECISION_BF16 ? 64u : (cfg->sh_order == 2 ? 128u : 64u);
@@ -198,6 +216,15 @@ drv_status drv_create(const DrvConfig* cfg, DrvContext** out) {
   }
   if ((e = cudaMalloc(&c->mips, off * 4)) != cudaSuccess) return bail(e);
   if ((e = cudaMalloc(&c->vox_corners, (size_t)N * N * N)) != cudaSuccess) return bail(e);
+  c->record_levels = drv::record_levels_for(cfg->precision, c->n_voxel_levels);
+  uint32_t records = 0;
+  for (int l = 1; l <= c->record_levels; ++l) {
+    c->record_offset[l] = records;
+    const uint32_t n = (uint32_t)(N >> l);
+    records += n * n * n;
+  }
+  c->record_offset[c->record_levels + 1] = records;
+  if (records && (e = cudaMalloc(&c->vox_records, (size_t)records * 16)) != cudaSuccess) return bail(e);
 
   // The single-launch light stage's scratch, where frames need it from the
   // start (no indirect shadow); otherwise on first use (ensure_single_scratch).
@@ -276,6 +303,9 @@ drv_status drv_get_buffers(DrvContext* ctx, DrvBuffers* o) {
   o->counter = ctx->counter;
   o->voxel_bits = ctx->voxel_bits;
   o->voxel_corners = ctx->vox_corners;
+  for (int l = 0; l < 16; ++l)
+    o->voxel_mip_records[l] = l >= 1 && l <= ctx->record_levels ? (void*)(ctx->vox_records + ctx->record_offset[l]) : nullptr;
+  o->n_record_levels = ctx->record_levels;
   const size_t texel = ctx->cfg.precision == DRV_PRECISION_BF16 ? 2 : 4;
   for (int l = 1; l < ctx->n_voxel_levels && l < 16; ++l)
     o->voxel_mips[l] = static_cast<char*>(ctx->mips) + ctx->mip_offset[l] * texel;
@@ -396,10 +426,26 @@ drv_status drv_voxelize(DrvContext* ctx, const DrvScene* scene, const DrvVolumeI
 
 drv_status drv_build_opacity_mips(DrvContext* ctx) {
   if (!ctx) return DRV_ERR_INVALID_ARG;
-  DRV_TRY_CUDA(ctx, drv::launch_build_mips(ctx->s(), ctx->cfg.voxel_res, ctx->voxel_bits, ctx->mips, ctx->mip_offset,
-                                            ctx->n_voxel_levels, ctx->cfg.precision));
-  return cuda_check(ctx, drv::launch_build_corners(ctx->s(), ctx->cfg.voxel_res, ctx->voxel_bits, ctx->vox_corners),
-                    "build_corners");
+  // The corner grid (side stream 2) and the mip chain + records (this
+  // stream) both read only the level-0 bits: built concurrently, joined here.
+  const cudaStream_t s = ctx->s();
+  DRV_TRY_CUDA(ctx, cudaEventRecord(ctx->vox_fork_ev, s));
+  DRV_TRY_CUDA(ctx, cudaStreamWaitEvent(ctx->side[2], ctx->vox_fork_ev, 0));
+  const drv_status corners =
+      cuda_check(ctx, drv::launch_build_corners(ctx->side[2], ctx->cfg.voxel_res, ctx->voxel_bits, ctx->vox_corners),
+                 "build_corners");
+  drv_status st = cuda_check(ctx,
+                             drv::launch_build_mips(s, ctx->cfg.voxel_res, ctx->voxel_bits, ctx->mips, ctx->mip_offset,
+                                                    ctx->n_voxel_levels, ctx->cfg.precision),
+                             "build_mips");
+  if (st == DRV_OK)
+    st = cuda_check(ctx,
+                    drv::launch_build_records(s, ctx->cfg.voxel_res, ctx->mips, ctx->mip_offset, ctx->cfg.precision,
+                                              ctx->vox_records, ctx->record_offset, ctx->record_levels),
+                    "build_records");
+  DRV_TRY_CUDA(ctx, cudaEventRecord(ctx->join_ev[2], ctx->side[2]));
+  DRV_TRY_CUDA(ctx, cudaStreamWaitEvent(s, ctx->join_ev[2], 0));
+  return st != DRV_OK ? st : corners;
 }
 
 // Renderer::AllocateCaches: clear counter and atlas (renderer.cpp:968-970),
@@ -448,7 +494,7 @@ drv_status drv_light_caches(DrvContext* ctx, const DrvSpotLight* lights, int32_t
       }
     }
     drv_status st = cuda_check(ctx, drv::launch_light_split(ctx->s(), ctx->cfg, *vol, ll, ctx->counter, ctx->entries,
-                                                            ctx->entry_stride, ctx->voxels(), pairs,
+                                                            ctx->entry_stride, ctx->light_voxels(), pairs,
                                                             surrogate ? ctx->sur_weights : nullptr,
                                                             ctx->tuning.cone_ctas_per_sm,
                                                             ctx->tuning.gather_ctas_per_sm, ctx->num_sms, events),
@@ -472,7 +518,7 @@ drv_status drv_light_caches(DrvContext* ctx, const DrvSpotLight* lights, int32_t
   const drv::LightScratch scratch{ctx->light_scratch, ctx->light_tickets, ctx->light_tickets + ctx->cfg.max_caches,
                                   drv::kMaxLightChunks};
   return cuda_check(ctx, drv::launch_light_caches(ctx->s(), ctx->cfg, *vol, ll, ctx->counter, ctx->entries,
-                                                  ctx->entry_stride, ctx->voxels(), scratch, ctx->num_sms),
+                                                  ctx->entry_stride, ctx->light_voxels(), scratch, ctx->num_sms),
                     "light_caches");
 }
 
@@ -492,16 +538,36 @@ drv_status drv_frame(DrvContext* ctx, const DrvScene* scene, const DrvGBufferVie
                      float* out_rgb) {
   if (!ctx || !scene || !g || !f || !vol || (n_lights > 0 && (!lights || !rsms)) || !out_rgb)
     return DRV_ERR_INVALID_ARG;
+  if (ctx->cur) return fail(ctx, DRV_ERR_INVALID_ARG, "drv_frame re-entered");
   drv_status st;
-  for (int l = 0; l < n_lights; ++l) {
-    if ((st = drv_prepare_rsm(ctx, l, &lights[l], &rsms[l])) != DRV_OK) return st;
-    if ((st = drv_extract_vpls(ctx, l, &lights[l])) != DRV_OK) return st;
+  // The box upload synchronises when the scene changed: do it on the
+  // context's stream, before the fork.
+  if (ctx->cfg.indirect_shadow && (st = drv_set_scene(ctx, scene)) != DRV_OK) return st;
+  // Renderer::Draw's first three stages are independent: RSM/VPLs on side
+  // stream 0, voxels on side stream 1, the cache allocation on the context's
+  // stream; the light stage waits for all three.
+  const cudaStream_t main = ctx->s();
+  DRV_TRY_CUDA(ctx, cudaEventRecord(ctx->fork_ev, main));
+  for (int i = 0; i < 2; ++i) DRV_TRY_CUDA(ctx, cudaStreamWaitEvent(ctx->side[i], ctx->fork_ev, 0));
+  st = DRV_OK;
+  ctx->cur = ctx->side[0];
+  for (int l = 0; l < n_lights && st == DRV_OK; ++l) {
+    st = drv_prepare_rsm(ctx, l, &lights[l], &rsms[l]);
+    if (st == DRV_OK) st = drv_extract_vpls(ctx, l, &lights[l]);
   }
-  if (ctx->cfg.indirect_shadow) {
-    if ((st = drv_voxelize(ctx, scene, vol)) != DRV_OK) return st;
-    if ((st = drv_build_opacity_mips(ctx)) != DRV_OK) return st;
+  ctx->cur = ctx->side[1];
+  if (st == DRV_OK && ctx->cfg.indirect_shadow) {
+    st = drv_voxelize(ctx, scene, vol);
+    if (st == DRV_OK) st = drv_build_opacity_mips(ctx);
   }
-  if ((st = drv_allocate_caches(ctx, g, f, vol)) != DRV_OK) return st;
+  ctx->cur = nullptr;
+  if (st == DRV_OK) st = drv_allocate_caches(ctx, g, f, vol);
+  // Join even after an error, so that no later call races the side streams.
+  for (int i = 0; i < 2; ++i) {
+    DRV_TRY_CUDA(ctx, cudaEventRecord(ctx->join_ev[i], ctx->side[i]));
+    DRV_TRY_CUDA(ctx, cudaStreamWaitEvent(main, ctx->join_ev[i], 0));
+  }
+  if (st != DRV_OK) return st;
   if ((st = drv_light_caches(ctx, lights, n_lights, vol, f)) != DRV_OK) return st;
   return drv_apply(ctx, g, f, vol, out_rgb);
 }

@@ -41,7 +41,18 @@ struct VoxelInputs {
   const uint8_t* corners = nullptr;     // level 0, corner-packed bytes in 4^3 bricks
   const void* mips = nullptr;           // levels 1..L concatenated (float, or half with BF16 precision)
   const size_t* mip_offsets = nullptr;  // texel offset of each level in mips
+  const uint4* records = nullptr;       // corner-packed mip records of levels 1..record_levels (optional)
+  const uint32_t* record_offsets = nullptr;  // record offset of each level (index 1..record_levels + 1)
+  int record_levels = 0;
 };
+
+// Levels that get corner-packed FP16 mip records: every level with BF16
+// precision (FP16 texels); levels 1..3 with FP32 precision, whose texels
+// k / 8^l (8^l <= 512) are exact in FP16.
+inline int record_levels_for(int precision, int n_levels) {
+  const int L = n_levels - 1;
+  return precision == DRV_PRECISION_BF16 ? L : (L < 3 ? L : 3);
+}
 
 // Device scratch of the light stage. partials: [max_caches * max_chunks][27]
 // chunk sums; tickets: one per cache; work: {next unit, retired CTAs}. Tickets
@@ -95,7 +106,15 @@ struct Context {
   cudaStream_t stream = nullptr;       // owned
   cudaStream_t user_stream = nullptr;  // set by drv_set_stream, borrowed (may be the legacy stream 0)
   bool has_user_stream = false;
-  cudaStream_t s() const { return has_user_stream ? user_stream : stream; }
+  // drv_frame runs the RSM/VPL stage and the voxel stage on two side streams,
+  // concurrently with the cache allocation on the context's stream (fork and
+  // join by events, so the frame stays one capturable DAG); while a stage is
+  // issued there, `cur` redirects s() to its side stream.
+  // Side stream 2 builds the corner grid while the mips are built.
+  cudaStream_t side[3] = {};
+  cudaEvent_t fork_ev = nullptr, join_ev[3] = {}, vox_fork_ev = nullptr;
+  cudaStream_t cur = nullptr;
+  cudaStream_t s() const { return cur ? cur : (has_user_stream ? user_stream : stream); }
   int device = 0;
   int num_sms = 0;
   std::string last_error;
@@ -113,7 +132,22 @@ struct Context {
   uint8_t* vox_corners = nullptr;  // level 0, corner-packed bytes in 4^3 bricks
   void* mips = nullptr;  // levels 1..L concatenated: float (FP32 precision) or half (BF16 precision)
   size_t mip_offset[kMaxVoxelLevels] = {};
-  VoxelInputs voxels() const { return VoxelInputs{vox_corners, mips, mip_offset}; }
+  uint4* vox_records = nullptr;  // corner-packed mip records (voxel_sample.cuh)
+  uint32_t record_offset[kMaxVoxelLevels + 1] = {};
+  int record_levels = 0;
+  // The voxel inputs of the light stage: without the mip records when
+  // DrvTuning.plain_voxel_reads asks for it.
+  VoxelInputs light_voxels() const {
+    VoxelInputs v = voxels();
+    if (tuning.plain_voxel_reads) {
+      v.records = nullptr;
+      v.record_levels = 0;
+    }
+    return v;
+  }
+  VoxelInputs voxels() const {
+    return VoxelInputs{vox_corners, mips, mip_offset, vox_records, record_offset, record_levels};
+  }
   int n_voxel_levels = 0;
   // RSM + VPLs per light.
   RsmChain rsm[DRV_MAX_LIGHTS];
@@ -161,6 +195,8 @@ cudaError_t launch_voxelize(cudaStream_t s, const DrvBox* boxes, int n_boxes, co
 cudaError_t launch_build_mips(cudaStream_t s, int n, const uint32_t* bits, void* mips, const size_t* offsets,
                               int n_levels, int precision);
 cudaError_t launch_build_corners(cudaStream_t s, int n, const uint32_t* bits, uint8_t* corners);
+cudaError_t launch_build_records(cudaStream_t s, int n, const void* mips, const size_t* mip_offsets, int precision,
+                                 uint4* records, const uint32_t* record_offsets, int record_levels);
 cudaError_t launch_allocate(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const DrvPerFrame& f,
                             const float* depth, int w, int h, uint32_t* atlas, void* entries, uint32_t entry_stride,
                             DrvCacheCounter* counter, uint32_t* ticket, uint32_t* err);

@@ -92,6 +92,18 @@ struct MipOffsets {
   size_t off[kMaxVoxelLevels];
 };
 
+// a[i] for a runtime i by an unrolled select over constant indices: a
+// runtime index into a by-value kernel argument makes the compiler copy the
+// whole array to the local-memory stack of every thread.
+template <typename T, int K>
+__device__ __forceinline__ T pick(const T (&a)[K], int i) {
+  T r = a[0];
+#pragma unroll
+  for (int k = 1; k < K; ++k)
+    if (k == i) r = a[k];
+  return r;
+}
+
 // Fused mips over one B^3 level-0 block (B = min(32, N)): levels 1..log2(B)
 // computed in shared memory from one read of the block's bits.
 template <typename T>
@@ -155,7 +167,7 @@ __global__ void __launch_bounds__(256) mips_kernel(int N, int B, const uint32_t*
       lv[cur ^ 1][i] = v;
       int gn = N >> level;
       size_t g = ((size_t)(bz * m + z) * gn + (by * m + y)) * gn + (bx * m + x);
-      store_mip(mips + mo.off[level] + g, v);
+      store_mip(mips + pick(mo.off, level) + g, v);
     }
     __syncthreads();
     cur ^= 1;
@@ -170,8 +182,8 @@ __global__ void __launch_bounds__(256) mips_tail_kernel(int N, int first_level, 
                                                         MipOffsets mo) {
   for (int level = first_level; level <= last_level; ++level) {
     int m = N >> level, p = m * 2;
-    const T* src = mips + mo.off[level - 1];
-    T* dst = mips + mo.off[level];
+    const T* src = mips + pick(mo.off, level - 1);
+    T* dst = mips + pick(mo.off, level);
     for (int i = threadIdx.x; i < m * m * m; i += blockDim.x) {
       int x = i % m, y = (i / m) % m, z = i / (m * m);
       float s = 0.0f;
@@ -236,7 +248,90 @@ __global__ void __launch_bounds__(256) corners_kernel(int N, int log2n, const ui
   for (int q = 0; q < 4; ++q) dst[q] = make_uint4(words[4 * q], words[4 * q + 1], words[4 * q + 2], words[4 * q + 3]);
 }
 
+// Corner-packed mip records (voxel_sample.cuh): one thread per 2x2x2 brick
+// of records of one level (blockIdx.y = level - 1). It reads the 3x3x3
+// texels its 8 records cover (+1 clamped) once and writes the brick's 128
+// bytes. Records hold FP16 texels: a copy with BF16 precision; with FP32
+// precision the records cover levels 1..3, whose texels k / 8^l (8^l <= 512)
+// FP16 holds exactly.
+struct RecordLevels {
+  uint32_t off[kMaxVoxelLevels + 1];  // record offset of level l
+  int levels;                         // K
+  int log2n;
+};
+
+__device__ __forceinline__ uint32_t half_bits(float v) { return (uint32_t)__half_as_ushort(__float2half_rn(v)); }
+__device__ __forceinline__ uint32_t half_bits(__half v) { return (uint32_t)__half_as_ushort(v); }
+
+template <typename T>
+__global__ void __launch_bounds__(256) records_kernel(const T* __restrict__ mips, MipOffsets mo, RecordLevels rl,
+                                                      uint4* __restrict__ out) {
+  // A thread's 8 records go through shared memory (slot r of thread t at
+  // t * 8 + (r ^ (t & 7)), spreading the writes over the banks) so that each
+  // warp stores its 32 bricks' 4 KB as 8 fully coalesced 512-byte rows.
+  __shared__ uint4 s_rec[256 * 8];
+  const int level = (int)blockIdx.y + 1;
+  const int ln = rl.log2n - level, n = 1 << ln, lb = ln > 0 ? ln - 1 : 0, nb = 1 << lb;
+  const uint32_t n_bricks = (uint32_t)nb * nb * nb;
+  const uint32_t brick = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = (int)threadIdx.x, lane = t & 31, warp0 = t & ~31;
+  if (blockIdx.x * blockDim.x + warp0 >= n_bricks) return;  // the whole warp is past the level
+  if (brick < n_bricks) {
+    const int x0 = (int)(brick & (nb - 1)) << 1, y0 = (int)((brick >> lb) & (nb - 1)) << 1,
+              z0 = (int)(brick >> (2 * lb)) << 1;
+    const T* src = mips + pick(mo.off, level);
+    uint32_t h[3][3][3];
+#pragma unroll
+    for (int dz = 0; dz < 3; ++dz)
+#pragma unroll
+      for (int dy = 0; dy < 3; ++dy) {
+        const T* row = src + ((size_t)min(z0 + dz, n - 1) * n + min(y0 + dy, n - 1)) * n;
+#pragma unroll
+        for (int dx = 0; dx < 3; ++dx) h[dz][dy][dx] = half_bits(row[min(x0 + dx, n - 1)]);
+      }
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      const int rx = r & 1, ry = (r >> 1) & 1, rz = r >> 2;
+      uint32_t w[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int j0 = 2 * q, j1 = 2 * q + 1;  // slot j = dx | dy << 1 | dz << 2
+        w[q] = h[rz + (j0 >> 2)][ry + ((j0 >> 1) & 1)][rx + (j0 & 1)] |
+               h[rz + (j1 >> 2)][ry + ((j1 >> 1) & 1)][rx + (j1 & 1)] << 16;
+      }
+      s_rec[t * 8 + (r ^ (t & 7))] = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+  }
+  __syncwarp();
+  uint4* dst = out + pick(rl.off, level) + (size_t)(blockIdx.x * blockDim.x + warp0) * 8;
+  const uint32_t left = (n > 1 ? n_bricks * 8u : 1u) - (blockIdx.x * blockDim.x + warp0) * 8u;  // a 1-texel level has one record
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const int m = k * 32 + lane;  // record of the warp's 256
+    const int src_t = warp0 + (m >> 3), r = m & 7;
+    if ((uint32_t)m < left) dst[m] = s_rec[src_t * 8 + (r ^ (src_t & 7))];
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_build_records(cudaStream_t s, int n, const void* mips, const size_t* mip_offsets, int precision,
+                                 uint4* records, const uint32_t* record_offsets, int record_levels) {
+  if (record_levels <= 0) return cudaSuccess;
+  MipOffsets mo{};
+  RecordLevels rl{};
+  for (int i = 0; i < kMaxVoxelLevels; ++i) mo.off[i] = mip_offsets[i];
+  for (int i = 0; i <= record_levels && i <= kMaxVoxelLevels; ++i) rl.off[i] = record_offsets[i];
+  rl.levels = record_levels;
+  while ((1 << (rl.log2n + 1)) <= n) ++rl.log2n;
+  const uint32_t nb = (uint32_t)(n >> 2) > 0 ? (uint32_t)(n >> 2) : 1u;  // bricks per axis at level 1
+  const dim3 grid((nb * nb * nb + 255) / 256, record_levels);
+  if (precision == DRV_PRECISION_BF16)
+    records_kernel<__half><<<grid, 256, 0, s>>>((const __half*)mips, mo, rl, records);
+  else
+    records_kernel<float><<<grid, 256, 0, s>>>((const float*)mips, mo, rl, records);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_build_corners(cudaStream_t s, int n, const uint32_t* bits, uint8_t* corners) {
   int l = 0;

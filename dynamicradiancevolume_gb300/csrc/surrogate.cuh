@@ -143,7 +143,7 @@ __device__ __forceinline__ void surrogate_features(const VoxelView& v, float inv
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
     const float t = (i + 0.5f) * 0.125f * reach_norm;
-    f[9 + i] = level_n(v, level, px + (qx - px) * t, py + (qy - py) * t, pz + (qz - pz) * t);
+    f[9 + i] = level_any(v, level, px + (qx - px) * t, py + (qy - py) * t, pz + (qz - pz) * t);
   }
   f[17] = dsr * 8.0f;
   f[18] = len_vox * (1.0f / 64.0f);

@@ -8,7 +8,15 @@
 // Level 0 is read from the corner-packed byte grid: byte (x, y, z) holds the
 // 8 voxels (x + dx, y + dy, z + dz), dx,dy,dz in {0,1}, with +1 clamped to the
 // last voxel, stored in 4x4x4 bricks of 64 bytes, so one trilinear level-0
-// sample is one byte load. Levels >= 1 are FP32 arrays (x fastest).
+// sample is one byte load. Levels >= 1 are FP32 arrays (x fastest) and, where
+// the context built them, corner-packed records of the same values: record
+// (x, y, z) of level l holds the 8 texels (x + dx, y + dy, z + dz), +1 clamped,
+// slot dx | dy << 1 | dz << 2, as FP16, 16 bytes, in 2x2x2 bricks (one
+// 128-byte line), so one trilinear mip sample is one 16-byte load instead of
+// eight. With BF16 precision the texels are FP16 anyway and every level has
+// records; with FP32 precision levels 1..3 have them: a level-l texel is
+// k / 8^l (a mean of means of binary voxels) and FP16 holds it exactly for
+// 8^l <= 512, so the sample is the same FP32 value bit for bit.
 #pragma once
 
 #include <cuda_fp16.h>
@@ -25,7 +33,15 @@ struct VoxelView {
   int log2n;
   int max_level;           // L = log2(N)
   int half_mips;
+  const uint4* records;    // corner-packed mip records (nullptr: none)
+  uint32_t roff[16];       // offset (records) of level l in `records`
+  int record_levels;       // levels 1..record_levels have records
 };
+
+// The arithmetic of the sampler and the cone is written with explicit
+// rounding intrinsics (no contraction left to the compiler), so every kernel
+// that inlines it computes the same bits.
+__device__ __forceinline__ float lerp(float a, float b, float t) { return __fmaf_rn(b - a, t, a); }
 
 __device__ __forceinline__ float mip_texel(const VoxelView& v, uint32_t i) {
   return v.half_mips ? __half2float(__ldg(static_cast<const __half*>(v.mips) + i))
@@ -39,20 +55,36 @@ __device__ __forceinline__ uint32_t corner_index(int x, int y, int z, int log2n)
   return (brick << 6) | (uint32_t)((z & 3) << 4 | (y & 3) << 2 | (x & 3));
 }
 
-__device__ __forceinline__ float level0(const VoxelView& v, float sx, float sy, float sz) {
-  const int n = v.N;
-  float ux = sx * n - 0.5f, uy = sy * n - 0.5f, uz = sz * n - 0.5f;
-  float fx = floorf(ux), fy = floorf(uy), fz = floorf(uz);
-  float ax = ux - fx, ay = uy - fy, az = uz - fz;
-  int x = (int)fx, y = (int)fy, z = (int)fz;
-  // Below 0 both taps clamp to voxel 0: keep the (0) corner only. At or above
-  // n-1 both taps clamp to voxel n-1, which the packed byte already repeats.
-  if (x < 0) { x = 0; ax = 0.0f; }
-  if (y < 0) { y = 0; ay = 0.0f; }
-  if (z < 0) { z = 0; az = 0.0f; }
-  x = min(x, n - 1);
-  y = min(y, n - 1);
-  z = min(z, n - 1);
+// Texel coordinates of a sample: u = s * n - 0.5 per axis for a level of n
+// texels. u0 (level 0) is computed from s; level l derives from it exactly,
+// u_l = (u0 + 0.5) * 2^-l - 0.5 (every step is exact in FP32 for |u0| < 2^22),
+// so all levels see the same point and a coarse texel footprint contains the
+// finer one.
+struct Coord {
+  float x, y, z;
+};
+
+__device__ __forceinline__ Coord level_coord(const Coord& u0, int level) {
+  const float sc = __uint_as_float((uint32_t)(127 - level) << 23);  // 2^-level
+  return Coord{__fmaf_rn(u0.x + 0.5f, sc, -0.5f), __fmaf_rn(u0.y + 0.5f, sc, -0.5f),
+               __fmaf_rn(u0.z + 0.5f, sc, -0.5f)};
+}
+
+// Base texel and weights of coordinate u in a level of n texels: below 0 both
+// taps clamp to texel 0 (keep the first tap only); at or above n - 1 both
+// clamp to n - 1, which the corner-packed byte / record repeats.
+__device__ __forceinline__ int tap(float u, int n, float& a) {
+  const float f = floorf(u);
+  a = u - f;
+  int i = (int)f;
+  if (i < 0) {
+    i = 0;
+    a = 0.0f;
+  }
+  return min(i, n - 1);
+}
+
+__device__ __forceinline__ float level0_taps(const VoxelView& v, int x, int y, int z, float ax, float ay, float az) {
   const uint32_t b = __ldg(v.corners + corner_index(x, y, z, v.log2n));
   // Trilinear weights sum to one, so eight equal corners give that value
   // exactly: empty space (the common case) costs no interpolation.
@@ -61,18 +93,22 @@ __device__ __forceinline__ float level0(const VoxelView& v, float sx, float sy, 
   const float t0 = (float)(b & 1u), t1 = (float)((b >> 1) & 1u), t2 = (float)((b >> 2) & 1u),
               t3 = (float)((b >> 3) & 1u), t4 = (float)((b >> 4) & 1u), t5 = (float)((b >> 5) & 1u),
               t6 = (float)((b >> 6) & 1u), t7 = (float)((b >> 7) & 1u);
-  float c00 = t0 + (t1 - t0) * ax, c10 = t2 + (t3 - t2) * ax;
-  float c01 = t4 + (t5 - t4) * ax, c11 = t6 + (t7 - t6) * ax;
-  float c0 = c00 + (c10 - c00) * ay, c1 = c01 + (c11 - c01) * ay;
-  return c0 + (c1 - c0) * az;
+  const float c00 = lerp(t0, t1, ax), c10 = lerp(t2, t3, ax);
+  const float c01 = lerp(t4, t5, ax), c11 = lerp(t6, t7, ax);
+  const float c0 = lerp(c00, c10, ay), c1 = lerp(c01, c11, ay);
+  return lerp(c0, c1, az);
 }
 
-__device__ __forceinline__ float level_n(const VoxelView& v, int level, float sx, float sy, float sz) {
+__device__ __forceinline__ float level0_at(const VoxelView& v, const Coord& u) {
+  float ax, ay, az;
+  const int x = tap(u.x, v.N, ax), y = tap(u.y, v.N, ay), z = tap(u.z, v.N, az);
+  return level0_taps(v, x, y, z, ax, ay, az);
+}
+
+__device__ __forceinline__ float level_n_at(const VoxelView& v, int level, const Coord& u) {
   const int ln = v.log2n - level, n = 1 << ln;
-  float ux = sx * n - 0.5f, uy = sy * n - 0.5f, uz = sz * n - 0.5f;
-  float fx = floorf(ux), fy = floorf(uy), fz = floorf(uz);
-  float ax = ux - fx, ay = uy - fy, az = uz - fz;
-  int x0 = (int)fx, y0 = (int)fy, z0 = (int)fz;
+  const float ax = u.x - floorf(u.x), ay = u.y - floorf(u.y), az = u.z - floorf(u.z);
+  const int x0 = (int)floorf(u.x), y0 = (int)floorf(u.y), z0 = (int)floorf(u.z);
   const int xa = min(max(x0, 0), n - 1), xb = min(max(x0 + 1, 0), n - 1);
   const int ya = min(max(y0, 0), n - 1) << ln, yb = min(max(y0 + 1, 0), n - 1) << ln;
   const int za = min(max(z0, 0), n - 1) << (2 * ln), zb = min(max(z0 + 1, 0), n - 1) << (2 * ln);
@@ -81,22 +117,78 @@ __device__ __forceinline__ float level_n(const VoxelView& v, int level, float sx
   float t2 = mip_texel(v, m + (za | yb | xa)), t3 = mip_texel(v, m + (za | yb | xb));
   float t4 = mip_texel(v, m + (zb | ya | xa)), t5 = mip_texel(v, m + (zb | ya | xb));
   float t6 = mip_texel(v, m + (zb | yb | xa)), t7 = mip_texel(v, m + (zb | yb | xb));
-  float c00 = t0 + (t1 - t0) * ax, c10 = t2 + (t3 - t2) * ax;
-  float c01 = t4 + (t5 - t4) * ax, c11 = t6 + (t7 - t6) * ax;
-  float c0 = c00 + (c10 - c00) * ay, c1 = c01 + (c11 - c01) * ay;
-  return c0 + (c1 - c0) * az;
+  const float c00 = lerp(t0, t1, ax), c10 = lerp(t2, t3, ax);
+  const float c01 = lerp(t4, t5, ax), c11 = lerp(t6, t7, ax);
+  const float c0 = lerp(c00, c10, ay), c1 = lerp(c01, c11, ay);
+  return lerp(c0, c1, az);
 }
 
+// Record index of texel (x, y, z) in a level of 2^ln texels per axis:
+// 2x2x2 bricks of 8 records, bricks x fastest.
+__device__ __forceinline__ uint32_t record_index(int x, int y, int z, int ln) {
+  const int lb = max(ln - 1, 0);  // bricks per axis = 2^(ln-1); a 1-texel level has x = y = z = 0
+  const uint32_t brick = ((uint32_t)((z >> 1) << lb | (y >> 1)) << lb) | (uint32_t)(x >> 1);
+  return brick << 3 | (uint32_t)((z & 1) << 2 | (y & 1) << 1 | (x & 1));
+}
+
+__device__ __forceinline__ __half2 u32_as_half2(uint32_t w) {
+  __half2 h;
+  memcpy(&h, &w, 4);
+  return h;
+}
+
+// level_n_at from the level's corner-packed record; `zero` reports a record
+// whose 8 texels are all 0 (the sample is then 0).
+__device__ __forceinline__ float level_record_at(const VoxelView& v, int level, const Coord& u, bool& zero) {
+  const int n = 1 << (v.log2n - level);
+  float ax, ay, az;
+  const int x = tap(u.x, n, ax), y = tap(u.y, n, ay), z = tap(u.z, n, az);
+  const uint4 r = __ldg(v.records + v.roff[level] + record_index(x, y, z, v.log2n - level));
+  zero = (r.x | r.y | r.z | r.w) == 0u;  // FP16 +0 is the all-zero pattern; texels are >= 0
+  if (zero) return 0.0f;
+  const float t0 = __low2float(u32_as_half2(r.x)), t1 = __high2float(u32_as_half2(r.x));
+  const float t2 = __low2float(u32_as_half2(r.y)), t3 = __high2float(u32_as_half2(r.y));
+  const float t4 = __low2float(u32_as_half2(r.z)), t5 = __high2float(u32_as_half2(r.z));
+  const float t6 = __low2float(u32_as_half2(r.w)), t7 = __high2float(u32_as_half2(r.w));
+  const float c00 = lerp(t0, t1, ax), c10 = lerp(t2, t3, ax);
+  const float c01 = lerp(t4, t5, ax), c11 = lerp(t6, t7, ax);
+  const float c0 = lerp(c00, c10, ay), c1 = lerp(c01, c11, ay);
+  return lerp(c0, c1, az);
+}
+
+// Trilinear sample of mip level >= 1 (from its records where they exist);
+// `zero` is set only from a record.
+__device__ __forceinline__ float level_any_at(const VoxelView& v, int level, const Coord& u, bool& zero) {
+  zero = false;
+  return level <= v.record_levels ? level_record_at(v, level, u, zero) : level_n_at(v, level, u);
+}
+
+// Trilinear sample of one mip level at s (no lod blend).
+__device__ __forceinline__ float level_any(const VoxelView& v, int level, float sx, float sy, float sz) {
+  const float fn = (float)(1 << (v.log2n - level));
+  const Coord u{__fmaf_rn(sx, fn, -0.5f), __fmaf_rn(sy, fn, -0.5f), __fmaf_rn(sz, fn, -0.5f)};
+  bool zero;
+  return level_any_at(v, level, u, zero);
+}
+
+// textureLod at s. For a blended lod the coarser level is read first: its
+// footprint contains the finer level's (the finer taps floor(u_f), floor(u_f)
+// + 1 lie within the fine texels of coarse taps floor(u_c), floor(u_c) + 1,
+// also where both clamp), so an all-zero coarse record makes both levels 0.
 __device__ __forceinline__ float sample_voxels(const VoxelView& v, float sx, float sy, float sz, float lod) {
-  if (!(lod > 0.0f)) return level0(v, sx, sy, sz);
-  if (lod >= (float)v.max_level) return level_n(v, v.max_level, sx, sy, sz);
+  const float fn = (float)v.N;
+  const Coord u0{__fmaf_rn(sx, fn, -0.5f), __fmaf_rn(sy, fn, -0.5f), __fmaf_rn(sz, fn, -0.5f)};
+  if (!(lod > 0.0f)) return level0_at(v, u0);
+  bool zero;
+  if (lod >= (float)v.max_level) return level_any_at(v, v.max_level, level_coord(u0, v.max_level), zero);
   const float fl = floorf(lod);
   const int d1 = (int)fl;
   const float fr = lod - fl;
-  const float t1 = d1 == 0 ? level0(v, sx, sy, sz) : level_n(v, d1, sx, sy, sz);
+  const float t2 = level_any_at(v, d1 + 1, level_coord(u0, d1 + 1), zero);
+  if (zero) return 0.0f;
+  const float t1 = d1 == 0 ? level0_at(v, u0) : level_any_at(v, d1, level_coord(u0, d1), zero);
   if (fr == 0.0f) return t1;
-  const float t2 = level_n(v, d1 + 1, sx, sy, sz);
-  return (1.0f - fr) * t1 + fr * t2;
+  return __fmaf_rn(fr, t2, __fmul_rn(1.0f - fr, t1));
 }
 
 // Indirect-shadow cone, cacheLightingRSM.comp:195-230: march from the cache
@@ -109,23 +201,24 @@ __device__ __forceinline__ float cone_shadow(const VoxelView& v, float voxel_siz
                                              float cz, float px, float py, float pz, float ax, float ay, float az,
                                              float dsr) {
   float tx = ax - cx, ty = ay - cy, tz = az - cz;
-  const float light_dist = sqrtf(tx * tx + ty * ty + tz * tz);
+  const float light_dist = sqrtf(__fmaf_rn(tz, tz, __fmaf_rn(ty, ty, __fmul_rn(tx, tx))));
   const float inv = 1.0f / light_dist;
   const float inv_n = 1.0f / (float)v.N;
-  const float dx = tx * inv * inv_n, dy = ty * inv * inv_n, dz = tz * inv * inv_n;
-  float qx = px + dx * 2.0f, qy = py + dy * 2.0f, qz = pz + dz * 2.0f;
+  const float dx = __fmul_rn(__fmul_rn(tx, inv), inv_n), dy = __fmul_rn(__fmul_rn(ty, inv), inv_n),
+              dz = __fmul_rn(__fmul_rn(tz, inv), inv_n);
+  float qx = __fmaf_rn(dx, 2.0f, px), qy = __fmaf_rn(dy, 2.0f, py), qz = __fmaf_rn(dz, 2.0f, pz);
   float occlusion = 0.0f, step = 1.0f, dist = 0.0f;
   const float goal = light_dist / voxel_size - 2.0f;
   const float k = 2.0f / (1.0f - dsr);
   for (int s = 0; s < max_steps; ++s) {
-    qx += dx * step;
-    qy += dy * step;
-    qz += dz * step;
+    qx = __fmaf_rn(dx, step, qx);
+    qy = __fmaf_rn(dy, step, qy);
+    qz = __fmaf_rn(dz, step, qz);
     dist += step;
-    const float radius = dist * dsr;
-    occlusion += (1.0f - occlusion) * sample_voxels(v, qx, qy, qz, __log2f(radius));
+    const float radius = __fmul_rn(dist, dsr);
+    occlusion = __fmaf_rn(1.0f - occlusion, sample_voxels(v, qx, qy, qz, __log2f(radius)), occlusion);
     if (dist >= goal || occlusion >= 1.0f) break;
-    step = fmaxf(1.0f, radius * k);
+    step = fmaxf(1.0f, __fmul_rn(radius, k));
   }
   return fminf(fmaxf(1.0f - occlusion, 0.0f), 1.0f);
 }

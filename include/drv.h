@@ -288,6 +288,11 @@ typedef struct DrvBuffers {
   DrvShadowCone* cones[DRV_MAX_LIGHTS];
   int32_t n_vpls[DRV_MAX_LIGHTS];
   int32_t n_lights;
+  void* voxel_mip_records[16];      /* levels 1..n_record_levels (index 1..): corner-packed 16-byte records, record
+                                       (x,y,z) = texels (x+dx,y+dy,z+dz) of the level, +1 clamped, slot dx|dy<<1|dz<<2,
+                                       2x2x2 bricks of 8 records; FP32 precision: u16 k = texel * 8^l (levels 1..5),
+                                       BF16 precision: the FP16 texels (every level) */
+  int32_t n_record_levels;
 } DrvBuffers;
 
 typedef struct DrvContext DrvContext;
@@ -437,7 +442,9 @@ typedef struct DrvTuning {
   int32_t gather_ctas_per_sm; /* split stage: CTAs of the gather pass per SM (0: as many as fit) */
   int32_t time_kernels;       /* nonzero: the split light stage records CUDA events between its
                                  kernels (not while the stream is being captured) */
-  int32_t reserved[3];
+  int32_t plain_voxel_reads;  /* nonzero: the cone tracer reads the plain mip arrays instead of the
+                                 corner-packed mip records; the result is the same bit for bit */
+  int32_t reserved[2];
 } DrvTuning;
 enum { DRV_LIGHT_PATH_AUTO = 0, DRV_LIGHT_PATH_SINGLE = 1, DRV_LIGHT_PATH_SPLIT = 2 };
 drv_status drv_set_tuning(DrvContext* ctx, const DrvTuning* tuning);

@@ -2,7 +2,8 @@
 and cull -> cone -> gather over a compacted pair list — give the same SH up
 to FP32 summation order; a pair list too small for the frame makes the gather
 trace the caches that did not fit, with the same result to FP32 rounding; the
-split form is deterministic run to run."""
+split form is deterministic run to run; reading the corner-packed mip records
+instead of the plain mip arrays leaves the result unchanged bit for bit."""
 import ctypes as C
 
 import numpy as np
@@ -56,7 +57,20 @@ def test_full_pair_list_is_traced_by_the_gather(cap, cuda, lib):
     # rounding
     p1, _, sh1 = _lit(REDUCED, 4)
     p2, _, sh2 = _lit(REDUCED, 4, pair_capacity=cap)
+    print("overflow cap %d: bitwise %s, rel-L2 %.3e" % (cap, np.array_equal(sh1, sh2), rel_l2(sh2, sh1)))
     assert rel_l2(sh2, sh1) < 1e-6
+    p1.close()
+    p2.close()
+
+
+@pytest.mark.parametrize("w", [pipeline.WORKLOADS["ns_1080p_4096"], REDUCED,
+                               pipeline.scaled(REDUCED, precision=abi.PRECISION_BF16)], ids=["ns", "c2r", "c2r_bf16"])
+@pytest.mark.parametrize("path", [abi.LIGHT_PATH_SPLIT, abi.LIGHT_PATH_SINGLE], ids=["split", "single"])
+def test_plain_voxel_reads_give_the_same_sh(w, path, cuda, lib):
+    p1, pos1, sh1 = _lit(w, 3, light_path=path)
+    p2, pos2, sh2 = _lit(w, 3, light_path=path, plain_voxel_reads=1)
+    assert np.array_equal(pos1, pos2)
+    assert np.array_equal(sh1, sh2)
     p1.close()
     p2.close()
 

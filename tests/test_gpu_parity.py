@@ -180,6 +180,44 @@ def test_corner_grid_matches_bits(case, request):
     assert np.array_equal(g, exp)
 
 
+def expected_records(level_texels, n):
+    """Corner-packed mip records of one level (n texels per axis, x fastest
+    input): 8 FP16 slots per record, slot dx | dy << 1 | dz << 2 = texel
+    (x + dx, y + dy, z + dz), +1 clamped; records in 2x2x2 bricks."""
+    t = np.asarray(level_texels).reshape(n, n, n)  # [z][y][x]
+    i = np.arange(n ** 3)
+    inn, brick = i & 7, i >> 3
+    nb = max(n // 2, 1)
+    x = (brick % nb) * 2 + (inn & 1)
+    y = ((brick // nb) % nb) * 2 + ((inn >> 1) & 1)
+    z = (brick // (nb * nb)) * 2 + (inn >> 2)
+    out = np.zeros((n ** 3, 8), np.uint16)
+    for j in range(8):
+        v = t[np.minimum(z + (j >> 2), n - 1), np.minimum(y + ((j >> 1) & 1), n - 1), np.minimum(x + (j & 1), n - 1)]
+        out[:, j] = v.astype(np.float16).view(np.uint16)
+    return out
+
+
+def device_records(r, level):
+    b = r.pipe.buffers()
+    n = r.w.voxel_res >> level
+    g = r.pipe._dev_tensor(b.voxel_mip_records[level], n ** 3 * 8, r.torch.int16).cpu().numpy()
+    return g.view(np.uint16).reshape(n ** 3, 8), n
+
+
+@pytest.mark.parametrize("case", ["c1", "c2r"])
+def test_mip_records_match_mips(case, request, oracle):
+    """FP32 precision: levels 1..3 get corner-packed FP16 records, exact
+    (their texels are k / 8^l with 8^l <= 512)."""
+    r = request.getfixturevalue(case)
+    b = r.pipe.buffers()
+    assert b.n_record_levels == min(3, len(r.mips))
+    for l in range(1, b.n_record_levels + 1):
+        g, n = device_records(r, l)
+        assert np.array_equal(r.mips[l - 1].astype(np.float16).astype(np.float32), r.mips[l - 1])
+        assert np.array_equal(g, expected_records(r.mips[l - 1], n))
+
+
 def _key_set(positions):
     return set(map(tuple, np.asarray(positions, np.float32).tolist()))
 

@@ -61,6 +61,19 @@ def test_mips_are_fp16(case, request, oracle):
             assert np.array_equal(g.astype(np.float64), ref)
 
 
+@pytest.mark.parametrize("case", ["c3"])
+def test_mip_records_are_fp16_texels(case, request):
+    """BF16 precision: every mip level gets corner-packed records of its FP16
+    texels."""
+    from test_gpu_parity import device_records, expected_records
+    r = request.getfixturevalue(case)
+    b = r.pipe.buffers()
+    assert b.n_record_levels == len(r.mips)
+    for l in range(1, b.n_record_levels + 1):
+        g, n = device_records(r, l)
+        assert np.array_equal(g, expected_records(r.mips[l - 1], n))
+
+
 @pytest.mark.parametrize("case", ["c3", "c3_sh2"])
 def test_light_sh_error_is_storage_rounding(case, request, oracle):
     """With Kahan-compensated FP32 accumulation the SH error against FP64 (on
