@@ -146,11 +146,11 @@ def light_stage_launches(w, surrogate: bool = False) -> int:
 
 def kernel_launches_per_frame(w, surrogate: bool = False) -> int:
     # per light: (read_lod + shadow_lod) downsample passes + 1 extraction;
-    # voxelize 1 + mips (1, +1 tail above 32^3) + corner grid 1; allocate 2
-    # (allocation, dispatch size); the light stage; apply 1.
+    # voxelize 1 + mips (1, +1 tail above 32^3) + mip records 1 + corner grid
+    # 1; allocate 2 (allocation, dispatch size); the light stage; apply 1.
     n = w.n_lights * (w.rsm_read_lod + w.shadow_lod + 1)
     if w.indirect_shadow:
-        n += 1 + (2 if w.voxel_res > 32 else 1) + 1
+        n += 1 + (2 if w.voxel_res > 32 else 1) + 1 + 1
         n += light_stage_launches(w, surrogate)
     else:
         n += 1

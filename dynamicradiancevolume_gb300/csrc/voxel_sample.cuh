@@ -55,34 +55,33 @@ __device__ __forceinline__ uint32_t corner_index(int x, int y, int z, int log2n)
   return (brick << 6) | (uint32_t)((z & 3) << 4 | (y & 3) << 2 | (x & 3));
 }
 
-// Texel coordinates of a sample: u = s * n - 0.5 per axis for a level of n
-// texels. u0 (level 0) is computed from s; level l derives from it exactly,
-// u_l = (u0 + 0.5) * 2^-l - 0.5 (every step is exact in FP32 for |u0| < 2^22),
+// A sample position U in level-0 voxel units (U = s * N for texture
+// coordinate s; exact, N is a power of two). Level l reads texel coordinate
+// u_l = U * 2^-l - 0.5 = s * n_l - 0.5, one rounding (exact for |U| < 2^22),
 // so all levels see the same point and a coarse texel footprint contains the
 // finer one.
 struct Coord {
   float x, y, z;
 };
 
-__device__ __forceinline__ Coord level_coord(const Coord& u0, int level) {
+__device__ __forceinline__ Coord level_coord(const Coord& U, int level) {
   const float sc = __uint_as_float((uint32_t)(127 - level) << 23);  // 2^-level
-  return Coord{__fmaf_rn(u0.x + 0.5f, sc, -0.5f), __fmaf_rn(u0.y + 0.5f, sc, -0.5f),
-               __fmaf_rn(u0.z + 0.5f, sc, -0.5f)};
+  return Coord{__fmaf_rn(U.x, sc, -0.5f), __fmaf_rn(U.y, sc, -0.5f), __fmaf_rn(U.z, sc, -0.5f)};
 }
 
-// Base texel and weights of coordinate u in a level of n texels: below 0 both
-// taps clamp to texel 0 (keep the first tap only); at or above n - 1 both
-// clamp to n - 1, which the corner-packed byte / record repeats.
-__device__ __forceinline__ int tap(float u, int n, float& a) {
-  const float f = floorf(u);
-  a = u - f;
-  int i = (int)f;
-  if (i < 0) {
-    i = 0;
-    a = 0.0f;
-  }
-  return min(i, n - 1);
+// Base texel and weight of coordinate u in a level of n texels (nm1 = n - 1):
+// below 0 both taps clamp to texel 0, at or above n - 1 both clamp to n - 1;
+// clamping u itself to [0, n - 1] gives the same sample, because the
+// corner-packed byte / record at n - 1 repeats texel n - 1 for the +1 tap.
+__device__ __forceinline__ int tap(float u, float nm1, float& a) {
+  const float c = fminf(fmaxf(u, 0.0f), nm1);
+  const float f = floorf(c);
+  a = c - f;
+  return (int)f;
 }
+
+// n - 1 as a float for a level of n = 2^ln texels.
+__device__ __forceinline__ float last_texel(int ln) { return __uint_as_float((uint32_t)(127 + ln) << 23) - 1.0f; }
 
 __device__ __forceinline__ float level0_taps(const VoxelView& v, int x, int y, int z, float ax, float ay, float az) {
   const uint32_t b = __ldg(v.corners + corner_index(x, y, z, v.log2n));
@@ -99,9 +98,11 @@ __device__ __forceinline__ float level0_taps(const VoxelView& v, int x, int y, i
   return lerp(c0, c1, az);
 }
 
-__device__ __forceinline__ float level0_at(const VoxelView& v, const Coord& u) {
+// Level 0 at position U (texel coordinate U - 0.5, exact).
+__device__ __forceinline__ float level0_at(const VoxelView& v, const Coord& U) {
+  const float nm1 = last_texel(v.log2n);
   float ax, ay, az;
-  const int x = tap(u.x, v.N, ax), y = tap(u.y, v.N, ay), z = tap(u.z, v.N, az);
+  const int x = tap(U.x - 0.5f, nm1, ax), y = tap(U.y - 0.5f, nm1, ay), z = tap(U.z - 0.5f, nm1, az);
   return level0_taps(v, x, y, z, ax, ay, az);
 }
 
@@ -140,9 +141,9 @@ __device__ __forceinline__ __half2 u32_as_half2(uint32_t w) {
 // level_n_at from the level's corner-packed record; `zero` reports a record
 // whose 8 texels are all 0 (the sample is then 0).
 __device__ __forceinline__ float level_record_at(const VoxelView& v, int level, const Coord& u, bool& zero) {
-  const int n = 1 << (v.log2n - level);
+  const float nm1 = last_texel(v.log2n - level);
   float ax, ay, az;
-  const int x = tap(u.x, n, ax), y = tap(u.y, n, ay), z = tap(u.z, n, az);
+  const int x = tap(u.x, nm1, ax), y = tap(u.y, nm1, ay), z = tap(u.z, nm1, az);
   const uint4 r = __ldg(v.records + v.roff[level] + record_index(x, y, z, v.log2n - level));
   zero = (r.x | r.y | r.z | r.w) == 0u;  // FP16 +0 is the all-zero pattern; texels are >= 0
   if (zero) return 0.0f;
@@ -163,32 +164,40 @@ __device__ __forceinline__ float level_any_at(const VoxelView& v, int level, con
   return level <= v.record_levels ? level_record_at(v, level, u, zero) : level_n_at(v, level, u);
 }
 
-// Trilinear sample of one mip level at s (no lod blend).
-__device__ __forceinline__ float level_any(const VoxelView& v, int level, float sx, float sy, float sz) {
-  const float fn = (float)(1 << (v.log2n - level));
-  const Coord u{__fmaf_rn(sx, fn, -0.5f), __fmaf_rn(sy, fn, -0.5f), __fmaf_rn(sz, fn, -0.5f)};
-  bool zero;
-  return level_any_at(v, level, u, zero);
+// Position U (level-0 voxel units) of texture coordinate s.
+__device__ __forceinline__ Coord voxel_pos(const VoxelView& v, float sx, float sy, float sz) {
+  const float fn = (float)v.N;
+  return Coord{__fmul_rn(sx, fn), __fmul_rn(sy, fn), __fmul_rn(sz, fn)};
 }
 
-// textureLod at s. For a blended lod the coarser level is read first: its
-// footprint contains the finer level's (the finer taps floor(u_f), floor(u_f)
-// + 1 lie within the fine texels of coarse taps floor(u_c), floor(u_c) + 1,
-// also where both clamp), so an all-zero coarse record makes both levels 0.
-__device__ __forceinline__ float sample_voxels(const VoxelView& v, float sx, float sy, float sz, float lod) {
-  const float fn = (float)v.N;
-  const Coord u0{__fmaf_rn(sx, fn, -0.5f), __fmaf_rn(sy, fn, -0.5f), __fmaf_rn(sz, fn, -0.5f)};
-  if (!(lod > 0.0f)) return level0_at(v, u0);
+// Trilinear sample of one mip level at s (no lod blend).
+__device__ __forceinline__ float level_any(const VoxelView& v, int level, float sx, float sy, float sz) {
   bool zero;
-  if (lod >= (float)v.max_level) return level_any_at(v, v.max_level, level_coord(u0, v.max_level), zero);
+  return level_any_at(v, level, level_coord(voxel_pos(v, sx, sy, sz), level), zero);
+}
+
+// textureLod at position U. For a blended lod the coarser level is read
+// first: its footprint contains the finer level's (the finer taps
+// floor(u_f), floor(u_f) + 1 lie within the fine texels of coarse taps
+// floor(u_c), floor(u_c) + 1, also where both clamp), so an all-zero coarse
+// record makes both levels 0.
+__device__ __forceinline__ float sample_voxels_at(const VoxelView& v, const Coord& U, float lod) {
+  if (!(lod > 0.0f)) return level0_at(v, U);
+  bool zero;
+  if (lod >= (float)v.max_level) return level_any_at(v, v.max_level, level_coord(U, v.max_level), zero);
   const float fl = floorf(lod);
   const int d1 = (int)fl;
   const float fr = lod - fl;
-  const float t2 = level_any_at(v, d1 + 1, level_coord(u0, d1 + 1), zero);
+  const float t2 = level_any_at(v, d1 + 1, level_coord(U, d1 + 1), zero);
   if (zero) return 0.0f;
-  const float t1 = d1 == 0 ? level0_at(v, u0) : level_any_at(v, d1, level_coord(u0, d1), zero);
+  const float t1 = d1 == 0 ? level0_at(v, U) : level_any_at(v, d1, level_coord(U, d1), zero);
   if (fr == 0.0f) return t1;
   return __fmaf_rn(fr, t2, __fmul_rn(1.0f - fr, t1));
+}
+
+// textureLod at texture coordinate s.
+__device__ __forceinline__ float sample_voxels(const VoxelView& v, float sx, float sy, float sz, float lod) {
+  return sample_voxels_at(v, voxel_pos(v, sx, sy, sz), lod);
 }
 
 // Indirect-shadow cone, cacheLightingRSM.comp:195-230: march from the cache
@@ -203,20 +212,22 @@ __device__ __forceinline__ float cone_shadow(const VoxelView& v, float voxel_siz
   float tx = ax - cx, ty = ay - cy, tz = az - cz;
   const float light_dist = sqrtf(__fmaf_rn(tz, tz, __fmaf_rn(ty, ty, __fmul_rn(tx, tx))));
   const float inv = 1.0f / light_dist;
-  const float inv_n = 1.0f / (float)v.N;
-  const float dx = __fmul_rn(__fmul_rn(tx, inv), inv_n), dy = __fmul_rn(__fmul_rn(ty, inv), inv_n),
-              dz = __fmul_rn(__fmul_rn(tz, inv), inv_n);
-  float qx = __fmaf_rn(dx, 2.0f, px), qy = __fmaf_rn(dy, 2.0f, py), qz = __fmaf_rn(dz, 2.0f, pz);
+  // The march in level-0 voxel units: direction D = (t / |t|) = (t / |t| / N) * N
+  // and position U = q * N, both exact scalings of the texture-space march
+  // q += d * step (rounding commutes with a power-of-two scale).
+  const float Dx = __fmul_rn(tx, inv), Dy = __fmul_rn(ty, inv), Dz = __fmul_rn(tz, inv);
+  const Coord P = voxel_pos(v, px, py, pz);
+  Coord U{__fmaf_rn(Dx, 2.0f, P.x), __fmaf_rn(Dy, 2.0f, P.y), __fmaf_rn(Dz, 2.0f, P.z)};
   float occlusion = 0.0f, step = 1.0f, dist = 0.0f;
   const float goal = light_dist / voxel_size - 2.0f;
   const float k = 2.0f / (1.0f - dsr);
   for (int s = 0; s < max_steps; ++s) {
-    qx = __fmaf_rn(dx, step, qx);
-    qy = __fmaf_rn(dy, step, qy);
-    qz = __fmaf_rn(dz, step, qz);
+    U.x = __fmaf_rn(Dx, step, U.x);
+    U.y = __fmaf_rn(Dy, step, U.y);
+    U.z = __fmaf_rn(Dz, step, U.z);
     dist += step;
     const float radius = __fmul_rn(dist, dsr);
-    occlusion = __fmaf_rn(1.0f - occlusion, sample_voxels(v, qx, qy, qz, __log2f(radius)), occlusion);
+    occlusion = __fmaf_rn(1.0f - occlusion, sample_voxels_at(v, U, __log2f(radius)), occlusion);
     if (dist >= goal || occlusion >= 1.0f) break;
     step = fmaxf(1.0f, __fmul_rn(radius, k));
   }
