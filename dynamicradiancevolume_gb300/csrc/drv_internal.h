@@ -74,7 +74,8 @@ struct LightScratch {
 // is not confident about, narrow cones (every sample on voxel level 0) from
 // its front, wide ones from its back.
 // counters (zeroed before each light stage): [0] pairs claimed, [3] narrow
-// and [4] wide cones in retrace, [5] pairs the surrogate evaluated,
+// and [4] wide cones in retrace, [5] pairs the surrogate evaluated, [6] the
+// cone pass's work cursor,
 // [8 + c] pairs of class c, [8 + kConeClasses + c] class c's scatter cursor.
 constexpr uint32_t kNoPair = 0xFFFFFFFFu;
 constexpr uint32_t kPairOverflow = 0xFFFFFFFFu;

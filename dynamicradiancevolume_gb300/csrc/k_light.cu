@@ -307,6 +307,26 @@ __global__ void __launch_bounds__(128) cone_kernel(StageParams p, PairList L) {
   }
   const uint32_t* ord = RETRACE ? L.retrace : L.order;
   const uint32_t n = min(nf + nb, L.cap);
+  if (!RETRACE) {
+    // Warps take 32 cones at a time from counters[6], from the end of the
+    // class order (the longest cones) to its start, so the short cones fill
+    // the tail of the pass.
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+      uint32_t base = 0;
+      if (lane == 0) base = atomicAdd(L.counters + 6, 32u);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (base >= n) break;
+      if (base + lane >= n) continue;
+      const uint32_t i = ord[n - 1u - (base + lane)];
+      const uint32_t b = L.block[i];
+      if (b == kNoPair) continue;
+      float cx, cy, cz;
+      cache_position<BF16>(p, L.cache[i], cx, cy, cz);
+      L.shadow[i] = block_cone(p, (int)b, cx, cy, cz);
+    }
+    return;
+  }
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     const uint32_t i = k < nf ? ord[k] : ord[L.cap - 1u - (k - nf)];
     const uint32_t b = L.block[i];
