@@ -100,6 +100,11 @@ class Batch:
                                         C.c_void_p(stream.cuda_stream) if stream is not None else None,
                                         C.byref(self.handle)))
 
+    def launch(self, stream=None) -> None:
+        """One launch on `stream` (default: the stream it was captured from);
+        returns without waiting."""
+        check(self.lib.drv_batch_launch(self.handle, C.c_void_p(stream.cuda_stream) if stream is not None else None))
+
     def run(self) -> tuple[float, np.ndarray]:
         """One launch; (total ms, per-scene completion ms from the start)."""
         check(self.lib.drv_batch_launch(self.handle, None))

@@ -462,8 +462,12 @@ drv_status drv_allocate_caches(DrvContext* ctx, const DrvGBufferView* g, const D
                     "allocate_caches");
 }
 
-drv_status drv_light_caches(DrvContext* ctx, const DrvSpotLight* lights, int32_t n_lights, const DrvVolumeInfo* vol,
-                            const DrvPerFrame* frame) {
+namespace {
+
+// The light stage. voxels_ready (drv_frame): an event the voxel build records
+// on another stream; only the kernels that read the voxels wait for it.
+drv_status light_caches(DrvContext* ctx, const DrvSpotLight* lights, int32_t n_lights, const DrvVolumeInfo* vol,
+                        const DrvPerFrame* frame, cudaEvent_t voxels_ready) {
   if (!ctx || !lights || !vol || !frame) return DRV_ERR_INVALID_ARG;
   if (n_lights < 0 || n_lights > ctx->cfg.max_lights) return fail(ctx, DRV_ERR_INVALID_ARG, "bad light count");
   drv::LightLaunch ll{};
@@ -497,11 +501,13 @@ drv_status drv_light_caches(DrvContext* ctx, const DrvSpotLight* lights, int32_t
                                                             ctx->entry_stride, ctx->light_voxels(), pairs,
                                                             surrogate ? ctx->sur_weights : nullptr,
                                                             ctx->tuning.cone_ctas_per_sm,
-                                                            ctx->tuning.gather_ctas_per_sm, ctx->num_sms, events),
+                                                            ctx->tuning.gather_ctas_per_sm, ctx->num_sms, events,
+                                                            voxels_ready),
                                "light_caches");
     if (events) ctx->lk_recorded = st == DRV_OK;
     return st;
   }
+  if (voxels_ready) DRV_TRY_CUDA(ctx, cudaStreamWaitEvent(ctx->s(), voxels_ready, 0));
   if (surrogate && ctx->tuning.light_path == DRV_LIGHT_PATH_SINGLE)
     return fail(ctx, DRV_ERR_INVALID_ARG, "surrogate visibility runs on the split light stage");
   long blocks = 0;
@@ -520,6 +526,13 @@ drv_status drv_light_caches(DrvContext* ctx, const DrvSpotLight* lights, int32_t
   return cuda_check(ctx, drv::launch_light_caches(ctx->s(), ctx->cfg, *vol, ll, ctx->counter, ctx->entries,
                                                   ctx->entry_stride, ctx->light_voxels(), scratch, ctx->num_sms),
                     "light_caches");
+}
+
+}  // namespace
+
+drv_status drv_light_caches(DrvContext* ctx, const DrvSpotLight* lights, int32_t n_lights, const DrvVolumeInfo* vol,
+                            const DrvPerFrame* frame) {
+  return light_caches(ctx, lights, n_lights, vol, frame, nullptr);
 }
 
 drv_status drv_apply(DrvContext* ctx, const DrvGBufferView* g, const DrvPerFrame* f, const DrvVolumeInfo* vol,
@@ -562,13 +575,16 @@ drv_status drv_frame(DrvContext* ctx, const DrvScene* scene, const DrvGBufferVie
   }
   ctx->cur = nullptr;
   if (st == DRV_OK) st = drv_allocate_caches(ctx, g, f, vol);
-  // Join even after an error, so that no later call races the side streams.
-  for (int i = 0; i < 2; ++i) {
-    DRV_TRY_CUDA(ctx, cudaEventRecord(ctx->join_ev[i], ctx->side[i]));
-    DRV_TRY_CUDA(ctx, cudaStreamWaitEvent(main, ctx->join_ev[i], 0));
-  }
+  // The light stage's cull and ordering need the VPLs and the caches; the
+  // voxels are waited for only by the kernels that read them. After an error
+  // both side streams are joined, so that no later call races them.
+  for (int i = 0; i < 2; ++i) DRV_TRY_CUDA(ctx, cudaEventRecord(ctx->join_ev[i], ctx->side[i]));
+  DRV_TRY_CUDA(ctx, cudaStreamWaitEvent(main, ctx->join_ev[0], 0));
+  if (st == DRV_OK) st = light_caches(ctx, lights, n_lights, vol, f, ctx->join_ev[1]);
+  // Joined by now on success (the voxel readers waited); this also covers an
+  // error or a stage that skipped the wait.
+  DRV_TRY_CUDA(ctx, cudaStreamWaitEvent(main, ctx->join_ev[1], 0));
   if (st != DRV_OK) return st;
-  if ((st = drv_light_caches(ctx, lights, n_lights, vol, f)) != DRV_OK) return st;
   return drv_apply(ctx, g, f, vol, out_rgb);
 }
 

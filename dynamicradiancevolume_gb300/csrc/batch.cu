@@ -99,7 +99,9 @@ extern "C" drv_status drv_batch_create(const DrvBatchScene* scenes, int32_t n_sc
   const cudaError_t ce = cudaStreamEndCapture(b->origin, &b->graph);
   if (st != DRV_OK) return bail(st);
   if (!ok || ce != cudaSuccess) return bail(DRV_ERR_CUDA);
-  if (cudaGraphInstantiate(&b->exec, b->graph, 0) != cudaSuccess) return bail(DRV_ERR_CUDA);
+  // Node priorities: the frames' high-priority side streams (RSM, voxels) keep theirs.
+  if (cudaGraphInstantiate(&b->exec, b->graph, cudaGraphInstantiateFlagUseNodePriority) != cudaSuccess)
+    return bail(DRV_ERR_CUDA);
   *out = b;
   return DRV_OK;
 }

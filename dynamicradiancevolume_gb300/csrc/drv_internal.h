@@ -211,7 +211,7 @@ cudaError_t launch_light_split(cudaStream_t s, const DrvConfig& cfg, const DrvVo
                                const DrvCacheCounter* counter, void* entries, uint32_t entry_stride,
                                const VoxelInputs& vox, const PairList& pairs, const void* weights,
                                int cone_ctas_per_sm, int gather_ctas_per_sm, int num_sms,
-                               cudaEvent_t* events = nullptr);
+                               cudaEvent_t* events = nullptr, cudaEvent_t voxels_ready = nullptr);
 cudaError_t launch_bruteforce_rsm(cudaStream_t s, const DrvPerFrame& f, const DrvGBufferView& g,
                                   const float* rough_metal, const LightLaunch& ll, int bf16, float* out_rgb);
 cudaError_t launch_apply(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const DrvPerFrame& f,
