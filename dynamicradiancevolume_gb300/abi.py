@@ -170,6 +170,7 @@ PROTOTYPES = {
     "drv_extract_vpls": (C.c_int, [VP, C.c_int32, P(DrvSpotLight)]),
     "drv_set_scene": (C.c_int, [VP, P(DrvScene)]),
     "drv_voxelize": (C.c_int, [VP, P(DrvScene), P(DrvVolumeInfo)]),
+    "drv_voxelize_triangles": (C.c_int, [VP, VP, C.c_int32, VP, C.c_int32, P(DrvVolumeInfo)]),
     "drv_build_opacity_mips": (C.c_int, [VP]),
     "drv_allocate_caches": (C.c_int, [VP, P(DrvGBufferView), P(DrvPerFrame), P(DrvVolumeInfo)]),
     "drv_light_caches": (C.c_int, [VP, P(DrvSpotLight), C.c_int32, P(DrvVolumeInfo), P(DrvPerFrame)]),

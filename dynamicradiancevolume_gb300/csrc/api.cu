@@ -8,6 +8,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "drv_internal.h"
 
@@ -47,6 +48,7 @@ void release(Context* c) {
   cudaFree(c->mips);
   cudaFree(c->vox_corners);
   cudaFree(c->vox_records);
+  cudaFree(c->ndc);
 
   cudaFree(c->light_scratch);
   cudaFree(c->light_tickets);
@@ -216,6 +218,23 @@ drv_status drv_create(const DrvConfig* cfg, DrvContext** out) {
   }
   if ((e = cudaMalloc(&c->mips, off * 4)) != cudaSuccess) return bail(e);
   if ((e = cudaMalloc(&c->vox_corners, (size_t)N * N * N)) != cudaSuccess) return bail(e);
+  {
+    // NDC of every pixel column and row, computed as the kernels would
+    // (2 * ((p + 0.5) / size) - 1 in binary32, no contraction): a table read
+    // replaces two IEEE divisions per pixel in the allocation.
+    std::vector<float> ndc((size_t)cfg->width + cfg->height);
+    for (int x = 0; x < cfg->width; ++x) {
+      const float t = ((float)x + 0.5f) / (float)cfg->width;
+      ndc[x] = t * 2.0f - 1.0f;
+    }
+    for (int y = 0; y < cfg->height; ++y) {
+      const float t = ((float)y + 0.5f) / (float)cfg->height;
+      ndc[cfg->width + y] = t * 2.0f - 1.0f;
+    }
+    if ((e = cudaMalloc(&c->ndc, ndc.size() * sizeof(float))) != cudaSuccess) return bail(e);
+    if ((e = cudaMemcpy(c->ndc, ndc.data(), ndc.size() * sizeof(float), cudaMemcpyHostToDevice)) != cudaSuccess)
+      return bail(e);
+  }
   c->record_levels = drv::record_levels_for(cfg->precision, c->n_voxel_levels);
   uint32_t records = 0;
   for (int l = 1; l <= c->record_levels; ++l) {
@@ -424,6 +443,19 @@ drv_status drv_voxelize(DrvContext* ctx, const DrvScene* scene, const DrvVolumeI
                     "voxelize");
 }
 
+drv_status drv_voxelize_triangles(DrvContext* ctx, const float* positions, int32_t n_vertices, const uint32_t* indices,
+                                  int32_t n_triangles, const DrvVolumeInfo* vol) {
+  if (!ctx || !vol || n_triangles < 0 || n_vertices < 0 || (n_triangles > 0 && (!positions || n_vertices < 1)))
+    return DRV_ERR_INVALID_ARG;
+  if (!indices && (int64_t)n_triangles * 3 > n_vertices)
+    return fail(ctx, DRV_ERR_INVALID_ARG, "without indices the triangles take 3 consecutive vertices each");
+  if (reinterpret_cast<uintptr_t>(positions) % 4 || reinterpret_cast<uintptr_t>(indices) % 4)
+    return fail(ctx, DRV_ERR_INVALID_ARG, "positions and indices must be 4-byte aligned");
+  return cuda_check(ctx, drv::launch_voxelize_triangles(ctx->s(), positions, n_vertices, indices, n_triangles, *vol,
+                                                        ctx->cfg.voxel_res, ctx->voxel_bits, ctx->num_sms),
+                    "voxelize_triangles");
+}
+
 drv_status drv_build_opacity_mips(DrvContext* ctx) {
   if (!ctx) return DRV_ERR_INVALID_ARG;
   // The corner grid (side stream 2) and the mip chain + records (this
@@ -458,7 +490,7 @@ drv_status drv_allocate_caches(DrvContext* ctx, const DrvGBufferView* g, const D
   DRV_TRY_CUDA(ctx, cudaMemsetAsync(ctx->atlas, 0, ctx->atlas_words * 4, ctx->s()));
   return cuda_check(ctx, drv::launch_allocate(ctx->s(), ctx->cfg, *vol, *f, g->depth, g->width, g->height, ctx->atlas,
                                               ctx->entries, ctx->entry_stride, ctx->counter, ctx->scratch_words,
-                                              ctx->scratch_words + 1),
+                                              ctx->scratch_words + 1, ctx->ndc),
                     "allocate_caches");
 }
 

@@ -7,6 +7,8 @@
 // contract of the allocation and voxelization stages.
 #pragma once
 
+#include <cmath>
+
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -40,6 +42,19 @@ __device__ __forceinline__ float mrow(const float* r, float x, float y, float z)
   float c = __fmul_rn(r[2], z);
   s = __fadd_rn(s, c);
   return __fadd_rn(s, r[3]);
+}
+
+// World position of the pixel at NDC (nx, ny) from its depth.
+__device__ __forceinline__ void reconstruct_world_ndc(const DrvPerFrame& f, float nx, float ny, float depth,
+                                                      float out[3]) {
+  const float* M = f.inverse_view_projection;
+  float X = mrow(M + 0, nx, ny, depth);
+  float Y = mrow(M + 4, nx, ny, depth);
+  float Z = mrow(M + 8, nx, ny, depth);
+  float W = mrow(M + 12, nx, ny, depth);
+  out[0] = __fdiv_rn(X, W);
+  out[1] = __fdiv_rn(Y, W);
+  out[2] = __fdiv_rn(Z, W);
 }
 
 // World position of pixel (px, py) from its depth (cacheGather.comp:113-119,
@@ -100,6 +115,60 @@ __device__ __forceinline__ int cache_1d_coord(const DrvVolumeInfo& v, int res, i
   int ix = trunc_clamp(__fdiv_rn(__fsub_rn(p[0], k.min[0]), k.world_voxel_size), res);
   int iy = trunc_clamp(__fdiv_rn(__fsub_rn(p[1], k.min[1]), k.world_voxel_size), res);
   int iz = trunc_clamp(__fdiv_rn(__fsub_rn(p[2], k.min[2]), k.world_voxel_size), res);
+  return ix + iy * res + iz * res * res + c * res * res * res;
+}
+
+// Exact reciprocals of the divisors of the cascade arithmetic: where a
+// cascade's cell size (or cell size x transition zone) is a power of two,
+// x / d = x * (1 / d) exactly in binary32 (both are exact scalings), so the
+// IEEE division can become one product; 0 marks a divisor that is not.
+struct CellRecip {
+  float inv_cell[DRV_MAX_CASCADES];
+  float inv_zone[DRV_MAX_CASCADES];
+};
+
+// Host: 1 / d when d is a normal power of two (then exact), else 0.
+inline float exact_reciprocal(float d) {
+  int e = 0;
+  const float m = frexpf(d, &e);
+  return (m == 0.5f && e > -125 && e < 127) ? ldexpf(1.0f, 1 - e) : 0.0f;
+}
+
+inline CellRecip make_cell_recip(const DrvVolumeInfo& v) {
+  CellRecip r{};
+  for (int c = 0; c < DRV_MAX_CASCADES; ++c) {
+    const float d = v.cascades[c].world_voxel_size;
+    r.inv_cell[c] = exact_reciprocal(d);
+    const float zone = d * v.cav_transition_zone_size;  // the kernels' __fmul_rn of the same floats
+    r.inv_zone[c] = exact_reciprocal(zone);
+  }
+  return r;
+}
+
+__device__ __forceinline__ float div_exact(float x, float d, float inv) {
+  return inv != 0.0f ? __fmul_rn(x, inv) : __fdiv_rn(x, d);
+}
+
+__device__ __forceinline__ float cascade_transition(const DrvVolumeInfo& v, const CellRecip& r, int c,
+                                                   const float p[3]) {
+  const DrvCascade& k = v.cascades[c];
+  float a0 = __fsub_rn(k.decision_max[0], p[0]), a1 = __fsub_rn(k.decision_max[1], p[1]),
+        a2 = __fsub_rn(k.decision_max[2], p[2]);
+  float b0 = __fsub_rn(p[0], k.decision_min[0]), b1 = __fsub_rn(p[1], k.decision_min[1]),
+        b2 = __fsub_rn(p[2], k.decision_min[2]);
+  float m = fminf(fminf(fminf(a0, a1), a2), fminf(fminf(b0, b1), b2));
+  float denom = __fmul_rn(k.world_voxel_size, v.cav_transition_zone_size);
+  float t = __fsub_rn(1.0f, div_exact(m, denom, r.inv_zone[c]));
+  return fminf(fmaxf(t, 0.0f), 1.0f);
+}
+
+__device__ __forceinline__ int cache_1d_coord(const DrvVolumeInfo& v, const CellRecip& r, int res, int c,
+                                              const float p[3]) {
+  const DrvCascade& k = v.cascades[c];
+  const float inv = r.inv_cell[c];
+  int ix = trunc_clamp(div_exact(__fsub_rn(p[0], k.min[0]), k.world_voxel_size, inv), res);
+  int iy = trunc_clamp(div_exact(__fsub_rn(p[1], k.min[1]), k.world_voxel_size, inv), res);
+  int iz = trunc_clamp(div_exact(__fsub_rn(p[2], k.min[2]), k.world_voxel_size, inv), res);
   return ix + iy * res + iz * res * res + c * res * res * res;
 }
 

@@ -130,6 +130,7 @@ struct Context {
   // Voxels.
   uint32_t* voxel_bits = nullptr;
   size_t voxel_words = 0;
+  float* ndc = nullptr;  // NDC x of each pixel column (width), then y of each row (height): allocation
   uint8_t* vox_corners = nullptr;  // level 0, corner-packed bytes in 4^3 bricks
   void* mips = nullptr;  // levels 1..L concatenated: float (FP32 precision) or half (BF16 precision)
   size_t mip_offset[kMaxVoxelLevels] = {};
@@ -193,6 +194,8 @@ cudaError_t launch_extract_vpls(cudaStream_t s, const DrvSpotLight& L, int res, 
                                 const float* dls, const float* dls_shadow, void* vpls, DrvShadowCone* cones, int precision);
 cudaError_t launch_voxelize(cudaStream_t s, const DrvBox* boxes, int n_boxes, const DrvVolumeInfo& vol, int n,
                             uint32_t* bits);
+cudaError_t launch_voxelize_triangles(cudaStream_t s, const float* positions, int n_vertices, const uint32_t* indices,
+                                      int n_triangles, const DrvVolumeInfo& vol, int n, uint32_t* bits, int num_sms);
 cudaError_t launch_build_mips(cudaStream_t s, int n, const uint32_t* bits, void* mips, const size_t* offsets,
                               int n_levels, int precision);
 cudaError_t launch_build_corners(cudaStream_t s, int n, const uint32_t* bits, uint8_t* corners);
@@ -200,7 +203,7 @@ cudaError_t launch_build_records(cudaStream_t s, int n, const void* mips, const 
                                  uint4* records, const uint32_t* record_offsets, int record_levels);
 cudaError_t launch_allocate(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const DrvPerFrame& f,
                             const float* depth, int w, int h, uint32_t* atlas, void* entries, uint32_t entry_stride,
-                            DrvCacheCounter* counter, uint32_t* ticket, uint32_t* err);
+                            DrvCacheCounter* counter, uint32_t* ticket, uint32_t* err, const float* ndc = nullptr);
 cudaError_t launch_light_caches(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const LightLaunch& ll,
                                 const DrvCacheCounter* counter, void* entries, uint32_t entry_stride,
                                 const VoxelInputs& vox, const LightScratch& scratch, int num_sms);

@@ -25,6 +25,9 @@ struct AllocParams {
   int bf16;        // DrvCacheEntryBF16 entries (cell key + BF16 SH) instead of LightCacheEntry
   DrvCacheCounter* counter;
   uint32_t* err;
+  CellRecip rc;
+  const float* ndc_x;  // NDC x of every pixel column, y of every row (or nullptr: computed)
+  const float* ndc_y;
 };
 
 // AllocateCaches, cacheGather.comp:32-91. Corners outside the atlas are
@@ -87,14 +90,17 @@ __global__ void __launch_bounds__(kTile* kTile) allocate_kernel(AllocParams p) {
     float d = __ldcs(p.depth + (size_t)py * p.w + px);  // read once: streaming
     if (d > 0.0001f) {
       float wp[3];
-      reconstruct_world(p.frame, px, py, p.w, p.h, d, wp);
+      if (p.ndc_x)
+        reconstruct_world_ndc(p.frame, __ldg(p.ndc_x + px), __ldg(p.ndc_y + py), d, wp);
+      else
+        reconstruct_world(p.frame, px, py, p.w, p.h, d, wp);
       cascade = select_cascade(p.vol, p.n_cascades, wp);
-      own = cache_1d_coord(p.vol, p.res, cascade, wp);
+      own = cache_1d_coord(p.vol, p.rc, p.res, cascade, wp);
       list1[lx][ly] = own;
       if (p.transitions) {
-        float t = cascade_transition(p.vol, cascade, wp);
+        float t = cascade_transition(p.vol, p.rc, cascade, wp);
         if (t > 0.0f && cascade < p.n_cascades - 1) {
-          own2 = cache_1d_coord(p.vol, p.res, cascade + 1, wp);
+          own2 = cache_1d_coord(p.vol, p.rc, p.res, cascade + 1, wp);
           list2[lx][ly] = own2;
         }
       }
@@ -132,8 +138,11 @@ __global__ void prepare_lighting_kernel(DrvCacheCounter* counter, uint32_t max_c
 
 cudaError_t launch_allocate(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const DrvPerFrame& f,
                             const float* depth, int w, int h, uint32_t* atlas, void* entries, uint32_t entry_stride,
-                            DrvCacheCounter* counter, uint32_t* /*ticket: unused*/, uint32_t* err) {
+                            DrvCacheCounter* counter, uint32_t* /*ticket: unused*/, uint32_t* err, const float* ndc) {
   AllocParams p;
+  p.rc = make_cell_recip(vol);
+  p.ndc_x = ndc;
+  p.ndc_y = ndc ? ndc + w : nullptr;
   p.vol = vol;
   p.frame = f;
   p.depth = depth;

@@ -32,6 +32,7 @@ struct ApplyParams {
   uint32_t max_caches;
   float cl[5];  // ShCosLobeFactor0, 1, 2n2_p1_n1, 20, 2p2
   float* out;
+  CellRecip rc;
 };
 
 // Irradiance of cascade c at wp for normal n: the 8 corner caches weighted
@@ -45,7 +46,7 @@ __device__ __forceinline__ f3 lighting(const ApplyParams& p, const float wp[3], 
   int a0[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
-    const float a = __fdiv_rn(__fsub_rn(wp[i], k.min[i]), k.world_voxel_size);
+    const float a = div_exact(__fsub_rn(wp[i], k.min[i]), k.world_voxel_size, p.rc.inv_cell[c]);
     a0[i] = __float2int_rz(fminf(fmaxf(a, -1e9f), 1e9f));
     const float t = a - (float)a0[i];
     wgt[i][0] = 1.0f - t;
@@ -153,7 +154,7 @@ __global__ void __launch_bounds__(256) apply_kernel(ApplyParams p) {
   f3 irr = lighting<BF16, SH2>(p, wp, c, n, n_caches);
   f3 col = mkf3(irr.x * alb.x, irr.y * alb.y, irr.z * alb.z);
   if (p.transitions) {
-    const float t = cascade_transition(p.vol, c, wp);
+    const float t = cascade_transition(p.vol, p.rc, c, wp);
     if (t > 0.0f && c < p.n_cascades - 1) {
       f3 irr2 = lighting<BF16, SH2>(p, wp, c + 1, n, n_caches);
       f3 col2 = mkf3(irr2.x * alb.x, irr2.y * alb.y, irr2.z * alb.z);
@@ -171,6 +172,7 @@ cudaError_t launch_apply(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeIn
                          const DrvGBufferView& g, const uint32_t* atlas, const void* entries, uint32_t entry_stride,
                          const DrvCacheCounter* counter, float* out_rgb) {
   ApplyParams p;
+  p.rc = make_cell_recip(vol);
   p.vol = vol;
   p.frame = f;
   p.depth = g.depth;

@@ -88,6 +88,160 @@ __global__ void __launch_bounds__(256) voxelize_kernel(const DrvBox* __restrict_
   }
 }
 
+// ---- triangle meshes ----------------------------------------------------
+// voxelize.{vert,geom,frag} for a triangle mesh, in binary32 with every
+// operation rounded as written (the oracle restates the same sequence):
+// positions in voxel units w = (p - VolumeWorldMin) / VoxelSizeInWorld (the
+// window coordinates of the reference's VoxelResolution^2 viewport); the
+// dominant axis of the normal picks the projection (voxelize.geom:24-51, ties
+// as there); each edge line moves outward by half a voxel in the L1 sense
+// (voxelize.geom:70-86); a pixel centre inside the three moved lines and
+// inside the triangle's AABB grown by half a voxel (voxelize.geom:59-62,
+// voxelize.frag:22-26), both inclusive, is a fragment; its depth is the
+// plane through the moved vertices carrying the original vertices' depths
+// (voxelize.geom:89-107); voxel z = int(depth), plus z - 1 / z + 1 where
+// int(depth -+ 1.414 |grad depth|) differs (voxelize.frag:39-55); depth
+// outside [0, N] is clipped and stores outside the grid are dropped.
+struct TriSetup {
+  int side;
+  float r[3][3];      // swizzled vertices: raster x, raster y, depth
+  float plane[3][3];  // moved edge lines a x + b y + c, inside <= 0
+  float aabb[4];      // x0, y0, x1, y1
+  float zA, zB, zC;   // depth plane
+  float max_change;
+  bool ok;
+};
+
+__device__ __forceinline__ float dmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float dsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float dadd(float a, float b) { return __fadd_rn(a, b); }
+
+__device__ __forceinline__ TriSetup tri_setup(const float* P0, const float* P1, const float* P2, const float* vm,
+                                              float vs) {
+  TriSetup t;
+  t.ok = false;
+  float w[3][3];
+  const float* P[3] = {P0, P1, P2};
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int a = 0; a < 3; ++a) w[i][a] = __fdiv_rn(dsub(P[i][a], vm[a]), vs);
+  const float e0[3] = {dsub(w[1][0], w[0][0]), dsub(w[1][1], w[0][1]), dsub(w[1][2], w[0][2])};
+  const float e1[3] = {dsub(w[2][0], w[0][0]), dsub(w[2][1], w[0][1]), dsub(w[2][2], w[0][2])};
+  const float n[3] = {fabsf(dsub(dmul(e0[1], e1[2]), dmul(e0[2], e1[1]))),
+                      fabsf(dsub(dmul(e0[2], e1[0]), dmul(e0[0], e1[2]))),
+                      fabsf(dsub(dmul(e0[0], e1[1]), dmul(e0[1], e1[0])))};
+  int side = n[0] > n[1] ? 0 : 1;
+  side = (side == 0 ? n[0] : n[1]) > n[2] ? side : 2;
+  t.side = side;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const float x = w[i][0], y = w[i][1], z = w[i][2];
+    t.r[i][0] = side == 0 ? z : x;
+    t.r[i][1] = side == 1 ? z : y;
+    t.r[i][2] = side == 0 ? x : (side == 1 ? y : z);
+  }
+  t.aabb[0] = dsub(fminf(fminf(t.r[0][0], t.r[1][0]), t.r[2][0]), 0.5f);
+  t.aabb[1] = dsub(fminf(fminf(t.r[0][1], t.r[1][1]), t.r[2][1]), 0.5f);
+  t.aabb[2] = dadd(fmaxf(fmaxf(t.r[0][0], t.r[1][0]), t.r[2][0]), 0.5f);
+  t.aabb[3] = dadd(fmaxf(fmaxf(t.r[0][1], t.r[1][1]), t.r[2][1]), 0.5f);
+  const float ax = dsub(t.r[0][0], t.r[2][0]), ay = dsub(t.r[0][1], t.r[2][1]);
+  const float bx = dsub(t.r[1][0], t.r[0][0]), by = dsub(t.r[1][1], t.r[0][1]);
+  const float area = dsub(dmul(ax, by), dmul(bx, ay));
+  if (!(area != 0.0f)) return t;
+  const float wind = area > 0.0f ? 1.0f : -1.0f;
+  // Edge i runs from vertex (i + 2) % 3 to vertex i (voxelize.geom:66-71).
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const int f = (i + 2) % 3;
+    const float dx = dsub(t.r[i][0], t.r[f][0]), dy = dsub(t.r[i][1], t.r[f][1]);
+    const float px = t.r[f][0], py = t.r[f][1];
+    const float a = dmul(dy, wind), b = dmul(-dx, wind), c = dmul(dsub(dmul(dx, py), dmul(dy, px)), wind);
+    t.plane[i][0] = a;
+    t.plane[i][1] = b;
+    t.plane[i][2] = dsub(c, dmul(0.5f, dadd(fabsf(a), fabsf(b))));
+  }
+  // Moved vertex i: moved line i meets moved line i + 1.
+  float V[3][2];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const float* L0 = t.plane[i];
+    const float* L1 = t.plane[(i + 1) % 3];
+    const float hx = dsub(dmul(L0[1], L1[2]), dmul(L0[2], L1[1]));
+    const float hy = dsub(dmul(L0[2], L1[0]), dmul(L0[0], L1[2]));
+    const float hw = dsub(dmul(L0[0], L1[1]), dmul(L0[1], L1[0]));
+    if (!(hw != 0.0f)) return t;
+    V[i][0] = __fdiv_rn(hx, hw);
+    V[i][1] = __fdiv_rn(hy, hw);
+  }
+  const float x10 = dsub(V[1][0], V[0][0]), y10 = dsub(V[1][1], V[0][1]);
+  const float x20 = dsub(V[2][0], V[0][0]), y20 = dsub(V[2][1], V[0][1]);
+  const float z10 = dsub(t.r[1][2], t.r[0][2]), z20 = dsub(t.r[2][2], t.r[0][2]);
+  const float det = dsub(dmul(x10, y20), dmul(x20, y10));
+  if (!(det != 0.0f)) return t;
+  t.zA = __fdiv_rn(dsub(dmul(z10, y20), dmul(z20, y10)), det);
+  t.zB = __fdiv_rn(dsub(dmul(x10, z20), dmul(x20, z10)), det);
+  t.zC = dsub(dsub(t.r[0][2], dmul(t.zA, V[0][0])), dmul(t.zB, V[0][1]));
+  t.max_change = dmul(__fsqrt_rn(dadd(dmul(t.zA, t.zA), dmul(t.zB, t.zB))), 1.414f);
+  t.ok = true;
+  return t;
+}
+
+__device__ __forceinline__ void set_voxel_swizzled(uint32_t* bits, int N, int side, int x, int y, int z) {
+  if (x < 0 || y < 0 || z < 0 || x >= N || y >= N || z >= N) return;
+  const int cx = side == 0 ? z : x, cy = side == 1 ? z : y, cz = side == 0 ? x : (side == 1 ? y : z);
+  const size_t i = ((size_t)cz * N + cy) * N + cx;
+  atomicOr(bits + (i >> 5), 1u << (i & 31));
+}
+
+struct TriVolume {
+  float vm[3];
+  float vs;
+};
+
+// A warp per triangle (grid-stride): every lane forms the same setup, the
+// lanes share the pixels of the grown AABB.
+__global__ void __launch_bounds__(256) triangles_kernel(const float* __restrict__ pos, int n_vertices,
+                                                        const uint32_t* __restrict__ idx, int n_tris, TriVolume tv,
+                                                        int N, uint32_t* __restrict__ bits) {
+  const int lane = threadIdx.x & 31;
+  const int n_warps = (int)((gridDim.x * blockDim.x) >> 5);
+  for (int k = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); k < n_tris; k += n_warps) {
+    const uint32_t i0 = idx ? __ldg(idx + 3 * k) : 3u * k, i1 = idx ? __ldg(idx + 3 * k + 1) : 3u * k + 1,
+                   i2 = idx ? __ldg(idx + 3 * k + 2) : 3u * k + 2;
+    if (i0 >= (uint32_t)n_vertices || i1 >= (uint32_t)n_vertices || i2 >= (uint32_t)n_vertices) continue;
+    float P[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      P[0][a] = __ldg(pos + 3 * (size_t)i0 + a);
+      P[1][a] = __ldg(pos + 3 * (size_t)i1 + a);
+      P[2][a] = __ldg(pos + 3 * (size_t)i2 + a);
+    }
+    const TriSetup t = tri_setup(P[0], P[1], P[2], tv.vm, tv.vs);
+    if (!t.ok) continue;
+    const int x0 = max(0, (int)floorf(t.aabb[0])), y0 = max(0, (int)floorf(t.aabb[1]));
+    const int x1 = min(N - 1, (int)floorf(t.aabb[2])), y1 = min(N - 1, (int)floorf(t.aabb[3]));
+    if (x1 < x0 || y1 < y0) continue;
+    const int W = x1 - x0 + 1, total = W * (y1 - y0 + 1);
+    for (int q = lane; q < total; q += 32) {
+      const int px = x0 + q % W, py = y0 + q / W;
+      const float cx = dadd((float)px, 0.5f), cy = dadd((float)py, 0.5f);
+      if (cx < t.aabb[0] || cy < t.aabb[1] || cx > t.aabb[2] || cy > t.aabb[3]) continue;
+      bool in = true;
+#pragma unroll
+      for (int e = 0; e < 3; ++e)
+        in = in && dadd(dadd(dmul(t.plane[e][0], cx), dmul(t.plane[e][1], cy)), t.plane[e][2]) <= 0.0f;
+      if (!in) continue;
+      const float z = dadd(dadd(dmul(t.zA, cx), dmul(t.zB, cy)), t.zC);
+      if (!(z >= 0.0f && z <= (float)N)) continue;
+      const int zi = (int)z;
+      set_voxel_swizzled(bits, N, t.side, px, py, zi);
+      if ((int)dsub(z, t.max_change) != zi) set_voxel_swizzled(bits, N, t.side, px, py, zi - 1);
+      if ((int)dadd(z, t.max_change) != zi) set_voxel_swizzled(bits, N, t.side, px, py, zi + 1);
+    }
+  }
+}
+
 struct MipOffsets {
   size_t off[kMaxVoxelLevels];
 };
@@ -347,6 +501,17 @@ cudaError_t launch_voxelize(cudaStream_t s, const DrvBox* boxes, int n_boxes, co
   cudaError_t e = cudaMemsetAsync(bits, 0, (size_t)n * n * (n / 32) * sizeof(uint32_t), s);
   if (e != cudaSuccess || n_boxes == 0) return e;
   voxelize_kernel<<<dim3(n_boxes * 6, kVoxelSplit), 256, 0, s>>>(boxes, vol, n, bits);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_voxelize_triangles(cudaStream_t s, const float* positions, int n_vertices, const uint32_t* indices,
+                                      int n_triangles, const DrvVolumeInfo& vol, int n, uint32_t* bits, int num_sms) {
+  if (n < 32 || (n & 31)) return cudaErrorInvalidValue;
+  cudaError_t e = cudaMemsetAsync(bits, 0, (size_t)n * n * (n / 32) * sizeof(uint32_t), s);
+  if (e != cudaSuccess || n_triangles <= 0) return e;
+  TriVolume tv{{vol.volume_world_min[0], vol.volume_world_min[1], vol.volume_world_min[2]}, vol.voxel_size_in_world};
+  const int warps = (n_triangles + 0) < num_sms * 64 ? n_triangles : num_sms * 64;  // <= 64 warps per SM in flight
+  triangles_kernel<<<(warps + 7) / 8, 256, 0, s>>>(positions, n_vertices, indices, n_triangles, tv, n, bits);
   return cudaGetLastError();
 }
 

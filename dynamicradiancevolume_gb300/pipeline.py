@@ -209,6 +209,23 @@ class Pipeline:
         self._c(self.lib.drv_voxelize(self.ctx, C.byref(self.hf.scene), C.byref(self.hf.volume)))
         self._c(self.lib.drv_build_opacity_mips(self.ctx))
 
+    def voxelize_triangles(self, positions, indices=None, mips: bool = True):
+        """Voxelizes a triangle mesh instead of the box scene: positions is a
+        device float32 tensor [V, 3] (world space), indices a device int32 /
+        uint32 tensor [T, 3] or None (consecutive triples)."""
+        torch = self.torch
+        pos = positions.contiguous()
+        assert pos.dtype == torch.float32 and pos.is_cuda
+        idx = None if indices is None else indices.contiguous()
+        n_tris = (pos.shape[0] // 3) if idx is None else idx.shape[0]
+        cur = torch.cuda.current_stream(self.device)
+        self.stream.wait_stream(cur)  # the mesh may have been written on the current stream
+        self._c(self.lib.drv_voxelize_triangles(self.ctx, C.c_void_p(pos.data_ptr()), pos.shape[0],
+                                                None if idx is None else C.c_void_p(idx.data_ptr()), n_tris,
+                                                C.byref(self.hf.volume)))
+        if mips:
+            self._c(self.lib.drv_build_opacity_mips(self.ctx))
+
     def allocate(self):
         self._c(self.lib.drv_allocate_caches(self.ctx, C.byref(self.gview), C.byref(self.hf.frame),
                                              C.byref(self.hf.volume)))

@@ -362,6 +362,16 @@ drv_status drv_set_scene(DrvContext* ctx, const DrvScene* scene);
 /* Voxelization::VoxelizeScene (voxelization.cpp:90-142): surface voxels of the
  * scene into the level-0 bitmask. */
 drv_status drv_voxelize(DrvContext* ctx, const DrvScene* scene, const DrvVolumeInfo* vol);
+/* Voxelization::VoxelizeScene for a triangle mesh (voxelize.vert/.geom/.frag:
+ * dominant-axis projection, half-voxel conservative raster, +-1 voxel depth
+ * conservativeness): the level-0 bitmask is cleared and the triangles'
+ * surface voxels set. positions: device, xyz per vertex in world space
+ * (n_vertices); indices: device, 3 per triangle, or NULL for consecutive
+ * vertex triples; triangles naming a vertex >= n_vertices are skipped. The
+ * opacity mips follow with drv_build_opacity_mips; drv_frame voxelizes the
+ * box scene it is given, so a mesh frame runs its stages one by one. */
+drv_status drv_voxelize_triangles(DrvContext* ctx, const float* positions, int32_t n_vertices, const uint32_t* indices,
+                                  int32_t n_triangles, const DrvVolumeInfo* vol);
 /* voxelmipmap.comp + voxelization.cpp:155-172: the full opacity mip chain. */
 drv_status drv_build_opacity_mips(DrvContext* ctx);
 /* Renderer::AllocateCaches (renderer.cpp:951-992): clear counter + atlas,

@@ -709,6 +709,130 @@ void orc_voxelize(const DrvBox* boxes, int n, const DrvVolumeInfo* vol, int N, u
       }
 }
 
+// voxelize.{vert,geom,frag} for a triangle mesh (binary32, no contraction):
+// positions in voxel units w = (p - VolumeWorldMin) / VoxelSizeInWorld
+// (window coordinates of the reference's VoxelResolution^2 viewport); the
+// dominant axis of the normal picks the projection (voxelize.geom:24-51,
+// ties as there); each edge line is moved outward by half a voxel in the L1
+// sense (voxelize.geom:70-86) and the pixel centres inside all three moved
+// lines (inclusive) and inside the triangle's AABB grown by half a voxel
+// (voxelize.geom:59-62, voxelize.frag:22-26; inclusive) are covered; the
+// depth is the plane through the moved vertices with the original vertices'
+// depths (voxelize.geom:89-107), voxel z = int(depth), plus z - 1 / z + 1 where
+// int(depth -+ 1.414 |grad depth|) differs (voxelize.frag:39-55); fragments
+// with depth outside [0, N] are clipped, stores outside the grid ignored.
+namespace {
+struct TriSetup {
+  int side;
+  float r[3][3];       // swizzled vertices (raster x, raster y, depth)
+  float plane[3][3];   // moved edge lines a x + b y + c (inside: <= 0)
+  float aabb[4];       // x0, y0, x1, y1
+  float zA, zB, zC;    // depth plane z = zA x + zB y + zC
+  float max_change;
+  bool ok;
+};
+
+TriSetup tri_setup(const float* p0, const float* p1, const float* p2, const float* vm, float vs) {
+  TriSetup t{};
+  float w[3][3];
+  const float* P[3] = {p0, p1, p2};
+  for (int i = 0; i < 3; ++i)
+    for (int a = 0; a < 3; ++a) w[i][a] = (P[i][a] - vm[a]) / vs;
+  const float e0[3] = {w[1][0] - w[0][0], w[1][1] - w[0][1], w[1][2] - w[0][2]};
+  const float e1[3] = {w[2][0] - w[0][0], w[2][1] - w[0][1], w[2][2] - w[0][2]};
+  const float n[3] = {std::fabs(e0[1] * e1[2] - e0[2] * e1[1]), std::fabs(e0[2] * e1[0] - e0[0] * e1[2]),
+                      std::fabs(e0[0] * e1[1] - e0[1] * e1[0])};
+  int side = n[0] > n[1] ? 0 : 1;
+  side = n[side] > n[2] ? side : 2;
+  t.side = side;
+  for (int i = 0; i < 3; ++i) {
+    const float x = w[i][0], y = w[i][1], z = w[i][2];
+    if (side == 0) { t.r[i][0] = z; t.r[i][1] = y; t.r[i][2] = x; }
+    else if (side == 1) { t.r[i][0] = x; t.r[i][1] = z; t.r[i][2] = y; }
+    else { t.r[i][0] = x; t.r[i][1] = y; t.r[i][2] = z; }
+  }
+  t.aabb[0] = std::min(std::min(t.r[0][0], t.r[1][0]), t.r[2][0]) - 0.5f;
+  t.aabb[1] = std::min(std::min(t.r[0][1], t.r[1][1]), t.r[2][1]) - 0.5f;
+  t.aabb[2] = std::max(std::max(t.r[0][0], t.r[1][0]), t.r[2][0]) + 0.5f;
+  t.aabb[3] = std::max(std::max(t.r[0][1], t.r[1][1]), t.r[2][1]) + 0.5f;
+  // Edge i runs from vertex from[i] to vertex to[i] (voxelize.geom:66-71).
+  const int from[3] = {2, 0, 1}, to[3] = {0, 1, 2};
+  const float ax = t.r[0][0] - t.r[2][0], ay = t.r[0][1] - t.r[2][1];
+  const float bx = t.r[1][0] - t.r[0][0], by = t.r[1][1] - t.r[0][1];
+  const float area = ax * by - bx * ay;
+  if (!(area != 0.0f)) return t;  // degenerate in its own projection: nothing rasterised
+  const float wind = area > 0.0f ? 1.0f : -1.0f;
+  for (int i = 0; i < 3; ++i) {
+    const float dx = t.r[to[i]][0] - t.r[from[i]][0], dy = t.r[to[i]][1] - t.r[from[i]][1];
+    const float px = t.r[from[i]][0], py = t.r[from[i]][1];
+    const float a = dy * wind, b = -dx * wind, c = (dx * py - dy * px) * wind;
+    t.plane[i][0] = a;
+    t.plane[i][1] = b;
+    t.plane[i][2] = c - 0.5f * (std::fabs(a) + std::fabs(b));
+  }
+  // Moved vertices: vertex i = moved line i intersected with moved line i+1
+  // (voxelize.geom:95-107), with vertex i's depth.
+  float V[3][2];
+  for (int i = 0; i < 3; ++i) {
+    const float* L0 = t.plane[i];
+    const float* L1 = t.plane[(i + 1) % 3];
+    const float hx = L0[1] * L1[2] - L0[2] * L1[1], hy = L0[2] * L1[0] - L0[0] * L1[2],
+                hw = L0[0] * L1[1] - L0[1] * L1[0];
+    if (!(hw != 0.0f)) return t;
+    V[i][0] = hx / hw;
+    V[i][1] = hy / hw;
+  }
+  const float x10 = V[1][0] - V[0][0], y10 = V[1][1] - V[0][1], x20 = V[2][0] - V[0][0], y20 = V[2][1] - V[0][1];
+  const float z10 = t.r[1][2] - t.r[0][2], z20 = t.r[2][2] - t.r[0][2];
+  const float det = x10 * y20 - x20 * y10;
+  if (!(det != 0.0f)) return t;
+  t.zA = (z10 * y20 - z20 * y10) / det;
+  t.zB = (x10 * z20 - x20 * z10) / det;
+  t.zC = t.r[0][2] - t.zA * V[0][0] - t.zB * V[0][1];
+  t.max_change = std::sqrt(t.zA * t.zA + t.zB * t.zB) * 1.414f;
+  t.ok = true;
+  return t;
+}
+
+inline void set_voxel_swz(uint32_t* bits, int N, int side, int x, int y, int z) {
+  if (x < 0 || y < 0 || z < 0 || x >= N || y >= N || z >= N) return;
+  int c[3];
+  if (side == 0) { c[0] = z; c[1] = y; c[2] = x; }
+  else if (side == 1) { c[0] = x; c[1] = z; c[2] = y; }
+  else { c[0] = x; c[1] = y; c[2] = z; }
+  const size_t i = ((size_t)c[2] * N + c[1]) * N + c[0];
+  bits[i >> 5] |= 1u << (i & 31);
+}
+}  // namespace
+
+void orc_voxelize_triangles(const float* positions, const uint32_t* indices, int n_tris, const DrvVolumeInfo* vol,
+                            int N, uint32_t* bits) {
+  std::memset(bits, 0, (((size_t)N * N * N + 31) / 32) * 4);
+  for (int k = 0; k < n_tris; ++k) {
+    const uint32_t i0 = indices ? indices[3 * k] : 3u * k, i1 = indices ? indices[3 * k + 1] : 3u * k + 1,
+                   i2 = indices ? indices[3 * k + 2] : 3u * k + 2;
+    const TriSetup t = tri_setup(positions + 3 * i0, positions + 3 * i1, positions + 3 * i2,
+                                 vol->volume_world_min, vol->voxel_size_in_world);
+    if (!t.ok) continue;
+    const int x0 = std::max(0, (int)std::floor(t.aabb[0])), y0 = std::max(0, (int)std::floor(t.aabb[1]));
+    const int x1 = std::min(N - 1, (int)std::floor(t.aabb[2])), y1 = std::min(N - 1, (int)std::floor(t.aabb[3]));
+    for (int py = y0; py <= y1; ++py)
+      for (int px = x0; px <= x1; ++px) {
+        const float cx = (float)px + 0.5f, cy = (float)py + 0.5f;
+        if (cx < t.aabb[0] || cy < t.aabb[1] || cx > t.aabb[2] || cy > t.aabb[3]) continue;
+        bool in = true;
+        for (int e = 0; e < 3; ++e) in = in && (t.plane[e][0] * cx + t.plane[e][1] * cy + t.plane[e][2] <= 0.0f);
+        if (!in) continue;
+        const float z = t.zA * cx + t.zB * cy + t.zC;
+        if (!(z >= 0.0f && z <= (float)N)) continue;
+        const int zi = (int)z;
+        set_voxel_swz(bits, N, t.side, px, py, zi);
+        if ((int)(z - t.max_change) != zi) set_voxel_swz(bits, N, t.side, px, py, zi - 1);
+        if ((int)(z + t.max_change) != zi) set_voxel_swz(bits, N, t.side, px, py, zi + 1);
+      }
+  }
+}
+
 // voxelmipmap.comp:8-13: a linear sample at the corner shared by 8 children
 // is their mean (stored as R8 in the reference; kept exact here).
 void orc_build_mips(int N, const uint32_t* bits, double* mips) {

@@ -71,6 +71,9 @@ void orc_extract_vpls(const DrvSpotLight* light, int res, const float* flux, con
                       const float* dls_shadow, double* vpl_out, double* cone_out);
 /* Surface voxelization of the box scene into the level-0 bitmask. */
 void orc_voxelize(const DrvBox* boxes, int n_boxes, const DrvVolumeInfo* vol, int voxel_res, uint32_t* bits);
+// Triangle mesh (positions xyz per vertex; indices: 3 per triangle, or NULL for consecutive triples).
+void orc_voxelize_triangles(const float* positions, const uint32_t* indices, int n_tris, const DrvVolumeInfo* vol,
+                            int voxel_res, uint32_t* bits);
 /* Opacity mips 1..L concatenated (level l has (N>>l)^3 doubles, x fastest). */
 void orc_build_mips(int voxel_res, const uint32_t* bits, double* mips);
 /* cacheGather.comp over the whole screen, tiles in row-major order, threads

@@ -58,6 +58,7 @@ def load():
         "orc_downsample_rsm": (None, [I, VP, VP, VP, VP, VP, VP]),
         "orc_extract_vpls": (None, [P(abi.DrvSpotLight), I, VP, VP, VP, VP, VP, VP]),
         "orc_voxelize": (None, [P(abi.DrvBox), I, P(abi.DrvVolumeInfo), I, VP]),
+        "orc_voxelize_triangles": (None, [VP, VP, I, P(abi.DrvVolumeInfo), I, VP]),
         "orc_build_mips": (None, [I, VP, VP]),
         "orc_allocate_caches": (I, [P(abi.DrvConfig), P(abi.DrvVolumeInfo), P(abi.DrvPerFrame), I, I, VP, VP, VP,
                                     P(C.c_uint32)]),
@@ -204,6 +205,17 @@ def extract_vpls(light, flux, n16, dls, dls_shadow):
 def voxelize(boxes, n_boxes, vol, N):
     bits = np.zeros(N ** 3 // 32, np.uint32)
     load().orc_voxelize(boxes, n_boxes, C.byref(vol), N, _p(bits))
+    return bits
+
+
+def voxelize_triangles(positions, indices, vol, N):
+    """positions: float32 [V, 3] world space; indices: uint32 [T, 3] or None
+    (consecutive triples). Returns the level-0 bitmask (uint32 words)."""
+    pos = np.ascontiguousarray(positions, dtype=np.float32).reshape(-1, 3)
+    idx = None if indices is None else np.ascontiguousarray(indices, dtype=np.uint32).reshape(-1, 3)
+    n = len(pos) // 3 if idx is None else len(idx)
+    bits = np.zeros(N ** 3 // 32, np.uint32)
+    load().orc_voxelize_triangles(_p(pos), None if idx is None else _p(idx), n, C.byref(vol), N, _p(bits))
     return bits
 
 

@@ -252,3 +252,62 @@ def test_bruteforce_single_val_facing_the_pixel(oracle):
     v2[0, 7:10] = (0, 0, 1)
     assert np.all(oracle.bruteforce_rsm(f, depth, n16, alb, [v2]) == 0.0)
     assert np.all(oracle.bruteforce_rsm(f, np.zeros((1, 1), np.float32), n16, alb, [v]) == 0.0)
+
+
+def _box_triangles(lo, hi):
+    """The 12 triangles of an axis-aligned box (float32 [36, 3])."""
+    c = np.array([[hi[0] if i & 1 else lo[0], hi[1] if i & 2 else lo[1], hi[2] if i & 4 else lo[2]] for i in range(8)],
+                 np.float32)
+    faces = [(0, 2, 6, 4), (1, 5, 7, 3), (0, 4, 5, 1), (2, 3, 7, 6), (0, 1, 3, 2), (4, 6, 7, 5)]
+    return np.array([c[k] for a, b, cc, d in faces for k in (a, b, cc, a, cc, d)], np.float32)
+
+
+def test_triangle_voxelization_of_box_faces_equals_the_box_rule(oracle):
+    """Axis-aligned faces as triangles: the conservative raster (half-voxel
+    L1 dilation, grown AABB) covers exactly the voxels whose square touches
+    the face, the box voxelizer's closed rule; the depth gradient is 0."""
+    from dynamicradiancevolume_gb300 import pipeline
+    w = pipeline.WORKLOADS["c1_small"]
+    hf = pipeline.host_frame(w, 3)
+    tris = np.concatenate([_box_triangles(hf.boxes[i].min[:3], hf.boxes[i].max[:3]) for i in range(hf.scene.n_boxes)])
+    a = oracle.voxelize_triangles(tris, None, hf.volume, w.voxel_res)
+    b = oracle.voxelize(hf.boxes, hf.scene.n_boxes, hf.volume, w.voxel_res)
+    assert np.array_equal(a, b)
+    # indexed: shared vertices give the same voxels
+    verts = tris.reshape(-1, 3)
+    uniq, inv = np.unique(verts, axis=0, return_inverse=True)
+    c = oracle.voxelize_triangles(uniq, inv.reshape(-1, 3).astype(np.uint32), hf.volume, w.voxel_res)
+    assert np.array_equal(c, b)
+
+
+def test_triangle_voxelization_known_answer(oracle):
+    """A triangle in the plane z = 10.25 voxels with corners at voxel
+    coordinates (4, 4), (12, 4), (4, 12): the pixel centres within half a
+    voxel (L1) of it — voxel columns x, y in [3, 12], x + y <= 16 + 1 — at
+    voxel z = 10."""
+    N = 32
+    vol = _volume(abi, N)
+    vs, vm = vol.voxel_size_in_world, np.array(vol.volume_world_min[:3])
+    tri = (np.array([[4, 4, 10.25], [12, 4, 10.25], [4, 12, 10.25]]) * vs + vm).astype(np.float32)
+    bits = oracle.voxelize_triangles(tri, None, vol, N)
+    v = np.unpackbits(bits.view(np.uint8), bitorder="little").reshape(N, N, N)  # [z][y][x]
+    zs, ys, xs = np.nonzero(v)
+    assert set(zs.tolist()) == {10}
+    exp = {(x, y) for x in range(N) for y in range(N)
+           if x + 0.5 >= 3.5 and y + 0.5 >= 3.5 and x + 0.5 <= 12.5 and y + 0.5 <= 12.5 and (x + 0.5) + (y + 0.5) <= 17.0}
+    assert set(zip(xs.tolist(), ys.tolist())) == exp
+
+
+def test_triangle_voxelization_depth_conservative(oracle):
+    """A steep triangle (depth slope 1 voxel per voxel): each covered column
+    also gets the voxels above and below the centre depth where the depth
+    changes by a voxel within the pixel (voxelize.frag:39-55)."""
+    N = 32
+    vol = _volume(abi, N)
+    vs, vm = vol.voxel_size_in_world, np.array(vol.volume_world_min[:3])
+    # plane z = 8 + 0.9 x (dominant axis z: |n_z| > |n_x|)
+    pts = np.array([[4, 4, 8 + 0.9 * 4], [20, 4, 8 + 0.9 * 20], [4, 20, 8 + 0.9 * 4]])
+    bits = oracle.voxelize_triangles((pts * vs + vm).astype(np.float32), None, vol, N)
+    v = np.unpackbits(bits.view(np.uint8), bitorder="little").reshape(N, N, N)
+    col = v[:, 10, 10]  # column at x = 10, y = 10
+    assert col.sum() >= 2  # more than the single voxel of the centre depth
