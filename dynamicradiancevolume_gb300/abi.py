@@ -20,6 +20,7 @@ SH2_SIGN_REFERENCE, SH2_SIGN_FIXED = 0, 1
 PRECISION_FP32, PRECISION_BF16 = 0, 1
 VISIBILITY_CONE, VISIBILITY_SURROGATE = 0, 1
 NORMAL_RG16I, NORMAL_F32X3 = 0, 1
+ALBEDO_F32X3, ALBEDO_SRGB8 = 0, 1
 
 f3 = C.c_float * 3
 f16 = C.c_float * 16
@@ -81,7 +82,7 @@ class DrvScene(C.Structure):
 
 class DrvGBufferView(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("depth", C.c_void_p), ("normal", C.c_void_p),
-                ("normal_format", C.c_int32), ("albedo", C.c_void_p)]
+                ("normal_format", C.c_int32), ("albedo", C.c_void_p), ("albedo_format", C.c_int32)]
 
 
 class DrvGBufferOut(C.Structure):

@@ -49,6 +49,7 @@ void release(Context* c) {
   cudaFree(c->vox_corners);
   cudaFree(c->vox_records);
   cudaFree(c->ndc);
+  cudaFree(c->srgb);
 
   cudaFree(c->light_scratch);
   cudaFree(c->light_tickets);
@@ -144,8 +145,18 @@ cudaError_t alloc_pairs(Context* c, uint64_t cap) {
 bool views_ok(const DrvGBufferView* g, const DrvConfig& c) {
   return g && g->depth && g->normal && g->albedo && g->width == c.width && g->height == c.height &&
          (g->normal_format == DRV_NORMAL_RG16I || g->normal_format == DRV_NORMAL_F32X3) &&
+         (g->albedo_format == DRV_ALBEDO_F32X3 || g->albedo_format == DRV_ALBEDO_SRGB8) &&
          reinterpret_cast<uintptr_t>(g->depth) % 4 == 0 && reinterpret_cast<uintptr_t>(g->normal) % 4 == 0 &&
-         reinterpret_cast<uintptr_t>(g->albedo) % 4 == 0;
+         (g->albedo_format == DRV_ALBEDO_SRGB8 || reinterpret_cast<uintptr_t>(g->albedo) % 4 == 0);
+}
+
+// The GL 4.5 sRGB decode (section 8.24) of the 256 byte values, evaluated in
+// double and rounded to float.
+void srgb_decode_table(float out[256]) {
+  for (int b = 0; b < 256; ++b) {
+    const double cs = b / 255.0;
+    out[b] = (float)(cs <= 0.04045 ? cs / 12.92 : std::pow((cs + 0.055) / 1.055, 2.4));
+  }
 }
 
 }  // namespace
@@ -234,6 +245,10 @@ drv_status drv_create(const DrvConfig* cfg, DrvContext** out) {
     if ((e = cudaMalloc(&c->ndc, ndc.size() * sizeof(float))) != cudaSuccess) return bail(e);
     if ((e = cudaMemcpy(c->ndc, ndc.data(), ndc.size() * sizeof(float), cudaMemcpyHostToDevice)) != cudaSuccess)
       return bail(e);
+    float srgb[256];
+    srgb_decode_table(srgb);
+    if ((e = cudaMalloc(&c->srgb, sizeof(srgb))) != cudaSuccess) return bail(e);
+    if ((e = cudaMemcpy(c->srgb, srgb, sizeof(srgb), cudaMemcpyHostToDevice)) != cudaSuccess) return bail(e);
   }
   c->record_levels = drv::record_levels_for(cfg->precision, c->n_voxel_levels);
   uint32_t records = 0;
@@ -572,7 +587,7 @@ drv_status drv_apply(DrvContext* ctx, const DrvGBufferView* g, const DrvPerFrame
   if (!ctx || !f || !vol || !out_rgb) return DRV_ERR_INVALID_ARG;
   if (!views_ok(g, ctx->cfg)) return fail(ctx, DRV_ERR_INVALID_ARG, "G-buffer view does not match the config");
   return cuda_check(ctx, drv::launch_apply(ctx->s(), ctx->cfg, *vol, *f, *g, ctx->atlas, ctx->entries,
-                                           ctx->entry_stride, ctx->counter, out_rgb),
+                                           ctx->entry_stride, ctx->counter, out_rgb, ctx->srgb),
                     "apply");
 }
 
@@ -657,7 +672,7 @@ drv_status drv_bruteforce_rsm(DrvContext* ctx, const DrvGBufferView* g, const fl
     ll.lights[l].interval = 1;
   }
   return cuda_check(ctx, drv::launch_bruteforce_rsm(ctx->s(), *f, *g, rough_metal, ll,
-                                                    ctx->cfg.precision == DRV_PRECISION_BF16, out_rgb),
+                                                    ctx->cfg.precision == DRV_PRECISION_BF16, out_rgb, ctx->srgb),
                     "bruteforce_rsm");
 }
 

@@ -172,6 +172,17 @@ __device__ __forceinline__ int cache_1d_coord(const DrvVolumeInfo& v, const Cell
   return ix + iy * res + iz * res * res + c * res * res * res;
 }
 
+// G-buffer diffuse of pixel i (drv_albedo_format): linear F32 RGB, or SRGB8
+// bytes decoded through `srgb` (the GL decode of the 256 byte values).
+__device__ __forceinline__ f3 load_albedo(const void* albedo, int format, const float* srgb, size_t i) {
+  if (format == DRV_ALBEDO_SRGB8) {
+    const uint8_t* a = static_cast<const uint8_t*>(albedo) + 3 * i;
+    return mkf3(__ldg(srgb + __ldcs(a)), __ldg(srgb + __ldcs(a + 1)), __ldg(srgb + __ldcs(a + 2)));
+  }
+  const float* a = static_cast<const float*>(albedo) + 3 * i;
+  return mkf3(__ldcs(a), __ldcs(a + 1), __ldcs(a + 2));
+}
+
 // ---- normal packing (utils.glsl:44-89) ----------------------------------
 // Saturating conversion to int16 (GL leaves out-of-range integer writes
 // undefined); the scale is applied as (x / PI) * 32768 so axis-aligned

@@ -131,6 +131,7 @@ struct Context {
   uint32_t* voxel_bits = nullptr;
   size_t voxel_words = 0;
   float* ndc = nullptr;  // NDC x of each pixel column (width), then y of each row (height): allocation
+  float* srgb = nullptr;  // the GL sRGB decode of the 256 byte values (DRV_ALBEDO_SRGB8)
   uint8_t* vox_corners = nullptr;  // level 0, corner-packed bytes in 4^3 bricks
   void* mips = nullptr;  // levels 1..L concatenated: float (FP32 precision) or half (BF16 precision)
   size_t mip_offset[kMaxVoxelLevels] = {};
@@ -216,10 +217,11 @@ cudaError_t launch_light_split(cudaStream_t s, const DrvConfig& cfg, const DrvVo
                                int cone_ctas_per_sm, int gather_ctas_per_sm, int num_sms,
                                cudaEvent_t* events = nullptr, cudaEvent_t voxels_ready = nullptr);
 cudaError_t launch_bruteforce_rsm(cudaStream_t s, const DrvPerFrame& f, const DrvGBufferView& g,
-                                  const float* rough_metal, const LightLaunch& ll, int bf16, float* out_rgb);
+                                  const float* rough_metal, const LightLaunch& ll, int bf16, float* out_rgb,
+                                  const float* srgb);
 cudaError_t launch_apply(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const DrvPerFrame& f,
                          const DrvGBufferView& g, const uint32_t* atlas, const void* entries, uint32_t entry_stride,
-                         const DrvCacheCounter* counter, float* out_rgb);
+                         const DrvCacheCounter* counter, float* out_rgb, const float* srgb);
 
 size_t surrogate_weights_bytes();
 size_t surrogate_train_scratch_floats(int n);

@@ -21,7 +21,9 @@ struct ApplyParams {
   const float* depth;
   const void* normal;
   int normal_format;
-  const float* albedo;
+  const void* albedo;
+  int albedo_format;
+  const float* srgb;
   int w, h;
   int res, n_cascades, transitions, sh2;
   int bf16;  // DrvCacheEntryBF16 entries
@@ -145,8 +147,8 @@ __global__ void __launch_bounds__(256) apply_kernel(ApplyParams p) {
     n = mkf3(__ldcs(q), __ldcs(q + 1), __ldcs(q + 2));
   }
   const float inv_pi = 1.0f / DRV_SHADER_PI;
-  const f3 alb = mkf3(__ldcs(p.albedo + 3 * i) * inv_pi, __ldcs(p.albedo + 3 * i + 1) * inv_pi,
-                      __ldcs(p.albedo + 3 * i + 2) * inv_pi);
+  const f3 a = load_albedo(p.albedo, p.albedo_format, p.srgb, i);
+  const f3 alb = mkf3(a.x * inv_pi, a.y * inv_pi, a.z * inv_pi);
   const uint32_t n_caches = min((uint32_t)max(p.counter->total_light_cache_count, 0), p.max_caches);
   float wp[3];
   reconstruct_world(p.frame, x, y, p.w, p.h, d, wp);
@@ -170,7 +172,7 @@ __global__ void __launch_bounds__(256) apply_kernel(ApplyParams p) {
 
 cudaError_t launch_apply(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const DrvPerFrame& f,
                          const DrvGBufferView& g, const uint32_t* atlas, const void* entries, uint32_t entry_stride,
-                         const DrvCacheCounter* counter, float* out_rgb) {
+                         const DrvCacheCounter* counter, float* out_rgb, const float* srgb) {
   ApplyParams p;
   p.rc = make_cell_recip(vol);
   p.vol = vol;
@@ -179,6 +181,8 @@ cudaError_t launch_apply(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeIn
   p.normal = g.normal;
   p.normal_format = g.normal_format;
   p.albedo = g.albedo;
+  p.albedo_format = g.albedo_format;
+  p.srgb = srgb;
   p.w = g.width;
   p.h = g.height;
   p.res = cfg.cav_res;

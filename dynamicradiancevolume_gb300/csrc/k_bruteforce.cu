@@ -25,7 +25,9 @@ struct BruteParams {
   const float* depth;
   const void* normal;
   int normal_format;
-  const float* albedo;
+  const void* albedo;
+  int albedo_format;
+  const float* srgb;
   const float* rough_metal;  // RG per pixel, or null: diffuse BRDF
   int w, h;
   LightLaunch ll;
@@ -58,7 +60,7 @@ __global__ void __launch_bounds__(kThreads) brute_kernel(BruteParams p) {
       const float* q = reinterpret_cast<const float*>(p.normal) + 3 * i;
       n = mkf3(q[0], q[1], q[2]);
     }
-    base = mkf3(p.albedo[3 * i], p.albedo[3 * i + 1], p.albedo[3 * i + 2]);
+    base = load_albedo(p.albedo, p.albedo_format, p.srgb, i);
     diffuse = base;
     if (SPECULAR) {
       // lightingfunctions.glsl:27-50
@@ -132,13 +134,16 @@ __global__ void __launch_bounds__(kThreads) brute_kernel(BruteParams p) {
 }  // namespace
 
 cudaError_t launch_bruteforce_rsm(cudaStream_t s, const DrvPerFrame& f, const DrvGBufferView& g,
-                                  const float* rough_metal, const LightLaunch& ll, int bf16, float* out_rgb) {
+                                  const float* rough_metal, const LightLaunch& ll, int bf16, float* out_rgb,
+                                  const float* srgb) {
   BruteParams p;
   p.frame = f;
   p.depth = g.depth;
   p.normal = g.normal;
   p.normal_format = g.normal_format;
   p.albedo = g.albedo;
+  p.albedo_format = g.albedo_format;
+  p.srgb = srgb;
   p.rough_metal = rough_metal;
   p.w = g.width;
   p.h = g.height;

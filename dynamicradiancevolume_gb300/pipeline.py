@@ -156,7 +156,7 @@ class Pipeline:
         self.normal_format = normal_format
         self.gview = abi.DrvGBufferView(W, H, self.depth.data_ptr(),
                                         (self.normal16 if normal_format == abi.NORMAL_RG16I else self.normal32).data_ptr(),
-                                        normal_format, self.albedo.data_ptr())
+                                        normal_format, self.albedo.data_ptr(), abi.ALBEDO_F32X3)
         self.rsm_views = (abi.DrvRSMView * w.n_lights)()
         for l in range(w.n_lights):
             self.rsm_views[l] = abi.DrvRSMView(R, self.rsm_flux[l].data_ptr(), self.rsm_normal[l].data_ptr(),

@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define DRV_ABI_VERSION 1
+#define DRV_ABI_VERSION 2
 #define DRV_MAX_CASCADES 4   /* MAX_NUM_ADDRESS_VOLUME_CASCADES, globalubos.glsl:43 */
 #define DRV_MAX_LIGHTS 16    /* maxExpectedLights, renderer.cpp:80 */
 #define DRV_LIGHTING_THREADS_PER_GROUP 64 /* lightcache.glsl:95 */
@@ -77,6 +77,15 @@ typedef enum drv_normal_format {
   DRV_NORMAL_RG16I = 0,   /* PackNormal16I, utils.glsl:83-89 (reference layout) */
   DRV_NORMAL_F32X3 = 1
 } drv_normal_format;
+
+/* G-buffer diffuse: linear RGB F32, or the reference's SRGB8 target
+ * (renderer.cpp:468, written with FRAMEBUFFER_SRGB on, renderer.cpp:507):
+ * 3 bytes per pixel, sRGB-encoded, read back as linear through the GL sRGB
+ * decode (GL 4.5 section 8.24). */
+typedef enum drv_albedo_format {
+  DRV_ALBEDO_F32X3 = 0,
+  DRV_ALBEDO_SRGB8 = 1
+} drv_albedo_format;
 
 /* Compile-time specialisations and setters of the reference's Renderer
  * (renderer.hpp:63-142, renderer.cpp:197-246). */
@@ -199,7 +208,8 @@ typedef struct DrvGBufferView {
   const float* depth;               /* D32F reversed-Z */
   const void* normal;               /* drv_normal_format */
   int32_t normal_format;
-  const float* albedo;              /* RGB F32 (linear) */
+  const void* albedo;               /* drv_albedo_format */
+  int32_t albedo_format;
 } DrvGBufferView;
 
 /* Writable G-buffer for the ray-cast producer. */
