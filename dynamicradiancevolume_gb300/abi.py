@@ -21,6 +21,7 @@ PRECISION_FP32, PRECISION_BF16 = 0, 1
 VISIBILITY_CONE, VISIBILITY_SURROGATE = 0, 1
 NORMAL_RG16I, NORMAL_F32X3 = 0, 1
 ALBEDO_F32X3, ALBEDO_SRGB8 = 0, 1
+RSM_F32, RSM_F16 = 0, 1
 
 f3 = C.c_float * 3
 f16 = C.c_float * 16
@@ -92,7 +93,7 @@ class DrvGBufferOut(C.Structure):
 
 class DrvRSMView(C.Structure):
     _fields_ = [("resolution", C.c_int32), ("flux", C.c_void_p), ("normal", C.c_void_p),
-                ("depth_lin_sq", C.c_void_p)]
+                ("depth_lin_sq", C.c_void_p), ("format", C.c_int32)]
 
 
 class DrvRSMOut(C.Structure):

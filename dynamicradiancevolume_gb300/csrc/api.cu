@@ -419,12 +419,19 @@ drv_status drv_prepare_rsm(DrvContext* ctx, int32_t li, const DrvSpotLight* L, c
   drv::RsmChain& ch = ctx->rsm[li];
   ch.res0 = R;
   ch.n_levels = deepest + 1;
-  ch.flux[0] = const_cast<float*>(v->flux);
+  if (v->format != DRV_RSM_F32 && v->format != DRV_RSM_F16) return fail(ctx, DRV_ERR_INVALID_ARG, "bad RSM format");
+  const size_t align = v->format == DRV_RSM_F16 ? 2 : 4;
+  if (reinterpret_cast<uintptr_t>(v->flux) % align || reinterpret_cast<uintptr_t>(v->depth_lin_sq) % align ||
+      reinterpret_cast<uintptr_t>(v->normal) % 2)
+    return fail(ctx, DRV_ERR_INVALID_ARG, "misaligned RSM view");
+  ch.flux[0] = const_cast<void*>(v->flux);
   ch.normal[0] = const_cast<int16_t*>(v->normal);
-  ch.dls[0] = const_cast<float*>(v->depth_lin_sq);
+  ch.dls[0] = const_cast<void*>(v->depth_lin_sq);
+  ch.half0 = v->format == DRV_RSM_F16;
   for (int k = 0; k < deepest; ++k) {
-    DRV_TRY_CUDA(ctx, drv::launch_downsample_rsm(ctx->s(), R >> k, ch.flux[k], ch.normal[k], ch.dls[k], ch.flux[k + 1],
-                                                 ch.normal[k + 1], ch.dls[k + 1]));
+    DRV_TRY_CUDA(ctx, drv::launch_downsample_rsm(ctx->s(), R >> k, ch.flux[k], ch.normal[k], ch.dls[k], ch.half(k),
+                                                 static_cast<float*>(ch.flux[k + 1]), ch.normal[k + 1],
+                                                 static_cast<float*>(ch.dls[k + 1])));
   }
   return DRV_OK;
 }
@@ -441,7 +448,8 @@ drv_status drv_extract_vpls(DrvContext* ctx, int32_t li, const DrvSpotLight* L) 
   if (shadow_level >= ch.n_levels) return fail(ctx, DRV_ERR_INVALID_ARG, "RSM chain too short for the shadow lod");
   if (L->indirect_shadow_sample_interval < 1) return DRV_ERR_INVALID_ARG;
   DRV_TRY_CUDA(ctx, drv::launch_extract_vpls(ctx->s(), *L, R, ch.flux[read_lod], ch.normal[read_lod], ch.dls[read_lod],
-                                             ch.dls[shadow_level], ctx->vpls[li], ctx->cones[li], ctx->cfg.precision));
+                                             ch.half(read_lod), ch.dls[shadow_level], ch.half(shadow_level),
+                                             ctx->vpls[li], ctx->cones[li], ctx->cfg.precision));
   ctx->n_vpls[li] = R * R;
   ctx->interval[li] = L->indirect_shadow_sample_interval;
   ctx->n_cones[li] = (R * R + L->indirect_shadow_sample_interval - 1) / L->indirect_shadow_sample_interval;

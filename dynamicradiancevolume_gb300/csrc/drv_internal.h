@@ -18,9 +18,11 @@ constexpr int kLightChunkMinBlocks = 128;  // shadow blocks per chunk, at least
 struct RsmChain {
   int res0 = 0;      // render resolution
   int n_levels = 0;  // levels res0, res0/2, ..., 1
-  float* flux[kMaxRsmLevels] = {};
+  void* flux[kMaxRsmLevels] = {};  // level 0 (the caller's): F32 or F16 per half0; below: F32
   int16_t* normal[kMaxRsmLevels] = {};
-  float* dls[kMaxRsmLevels] = {};
+  void* dls[kMaxRsmLevels] = {};
+  int half0 = 0;  // level 0's flux and (d, d^2) are F16 (DRV_RSM_F16)
+  bool half(int level) const { return level == 0 && half0; }
 };
 
 // Per-light arguments of the light stage.
@@ -189,10 +191,11 @@ RayFrame make_ray_frame(const float pos[3], const float dir[3], const float up[3
 cudaError_t launch_raycast_gbuffer(cudaStream_t s, const DrvBox* boxes, int n_boxes, RayFrame rf,
                                    const float* view_proj, int w, int h, DrvGBufferOut out);
 cudaError_t launch_raycast_rsm(cudaStream_t s, const DrvBox* boxes, int n_boxes, const DrvSpotLight& L, DrvRSMOut out);
-cudaError_t launch_downsample_rsm(cudaStream_t s, int res, const float* flux, const int16_t* nrm, const float* dls,
-                                  float* fo, int16_t* no, float* dlo);
-cudaError_t launch_extract_vpls(cudaStream_t s, const DrvSpotLight& L, int res, const float* flux, const int16_t* nrm,
-                                const float* dls, const float* dls_shadow, void* vpls, DrvShadowCone* cones, int precision);
+cudaError_t launch_downsample_rsm(cudaStream_t s, int res, const void* flux, const int16_t* nrm, const void* dls,
+                                  int src_half, float* fo, int16_t* no, float* dlo);
+cudaError_t launch_extract_vpls(cudaStream_t s, const DrvSpotLight& L, int res, const void* flux, const int16_t* nrm,
+                                const void* dls, int read_half, const void* dls_shadow, int shadow_half, void* vpls,
+                                DrvShadowCone* cones, int precision);
 cudaError_t launch_voxelize(cudaStream_t s, const DrvBox* boxes, int n_boxes, const DrvVolumeInfo& vol, int n,
                             uint32_t* bits);
 cudaError_t launch_voxelize_triangles(cudaStream_t s, const float* positions, int n_vertices, const uint32_t* indices,

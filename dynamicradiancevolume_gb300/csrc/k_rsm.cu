@@ -11,13 +11,18 @@
 namespace drv {
 namespace {
 
+// Element i of an F32 or F16 RSM array.
+__device__ __forceinline__ float rsm_at(const void* a, int half, size_t i) {
+  return half ? __half2float(static_cast<const __half*>(a)[i]) : static_cast<const float*>(a)[i];
+}
+
 // One downsample pass res -> res/2: flux = sum of the 2x2 children
 // (textureGather), normal = PackNormal16I(normalize(sum of unpacked normals)),
 // (d, d^2) = mean (linear sample at the shared corner).
-__global__ void __launch_bounds__(256) downsample_kernel(int res, const float* __restrict__ flux,
-                                                         const int16_t* __restrict__ nrm, const float* __restrict__ dls,
-                                                         float* __restrict__ fo, int16_t* __restrict__ no,
-                                                         float* __restrict__ dlo) {
+__global__ void __launch_bounds__(256) downsample_kernel(int res, const void* __restrict__ flux,
+                                                         const int16_t* __restrict__ nrm, const void* __restrict__ dls,
+                                                         int src_half, float* __restrict__ fo,
+                                                         int16_t* __restrict__ no, float* __restrict__ dlo) {
   int h = res >> 1;
   int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
   if (x >= h || y >= h) return;
@@ -28,12 +33,12 @@ __global__ void __launch_bounds__(256) downsample_kernel(int res, const float* _
 #pragma unroll
     for (int dx = 0; dx < 2; ++dx) {
       size_t j = (size_t)(2 * y + dy) * res + (2 * x + dx);
-      fs[0] += flux[3 * j];
-      fs[1] += flux[3 * j + 1];
-      fs[2] += flux[3 * j + 2];
+      fs[0] += rsm_at(flux, src_half, 3 * j);
+      fs[1] += rsm_at(flux, src_half, 3 * j + 1);
+      fs[2] += rsm_at(flux, src_half, 3 * j + 2);
       ns = ns + unpack_normal16i(nrm[2 * j], nrm[2 * j + 1]);
-      d0 += dls[2 * j];
-      d1 += dls[2 * j + 1];
+      d0 += rsm_at(dls, src_half, 2 * j);
+      d1 += rsm_at(dls, src_half, 2 * j + 1);
     }
   size_t i = (size_t)y * h + x;
   fo[3 * i] = fs[0];
@@ -59,9 +64,10 @@ __device__ __forceinline__ f3 unproject_dir(const DrvSpotLight& L, float u, floa
 }
 
 template <bool BF16>
-__global__ void __launch_bounds__(256) extract_kernel(DrvSpotLight L, int R, const float* __restrict__ flux,
-                                                      const int16_t* __restrict__ nrm, const float* __restrict__ dls,
-                                                      const float* __restrict__ dls_shadow, void* __restrict__ vpls_out,
+__global__ void __launch_bounds__(256) extract_kernel(DrvSpotLight L, int R, const void* __restrict__ flux,
+                                                      const int16_t* __restrict__ nrm, const void* __restrict__ dls,
+                                                      int read_half, const void* __restrict__ dls_shadow,
+                                                      int shadow_half, void* __restrict__ vpls_out,
                                                       DrvShadowCone* __restrict__ cones) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   int n = R * R;
@@ -72,7 +78,7 @@ __global__ void __launch_bounds__(256) extract_kernel(DrvSpotLight L, int R, con
     morton_decode((uint32_t)i, x, y);
     size_t t = (size_t)y * R + x;
     float u = (x + 0.5f) / R, v = (y + 0.5f) / R;
-    float d = dls[2 * t];
+    float d = rsm_at(dls, read_half, 2 * t);
     const f3 p = lp + unproject_dir(L, u, v) * d;
     const f3 nn = unpack_normal16i(nrm[2 * t], nrm[2 * t + 1]);
     const float area = d * d * L.val_area_factor;
@@ -82,7 +88,7 @@ __global__ void __launch_bounds__(256) extract_kernel(DrvSpotLight L, int R, con
       o.position[1] = p.y;
       o.position[2] = p.z;
       o.disc_area = area;
-      for (int c = 0; c < 3; ++c) o.flux_bf16[c] = to_bf16(flux[3 * t + c]);
+      for (int c = 0; c < 3; ++c) o.flux_bf16[c] = to_bf16(rsm_at(flux, read_half, 3 * t + c));
       o.normal_bf16[0] = to_bf16(nn.x);
       o.normal_bf16[1] = to_bf16(nn.y);
       o.normal_bf16[2] = to_bf16(nn.z);
@@ -90,9 +96,9 @@ __global__ void __launch_bounds__(256) extract_kernel(DrvSpotLight L, int R, con
       reinterpret_cast<DrvVPLBF16*>(vpls_out)[i] = o;
     } else {
       DrvVPL o;
-      o.flux[0] = flux[3 * t];
-      o.flux[1] = flux[3 * t + 1];
-      o.flux[2] = flux[3 * t + 2];
+      o.flux[0] = rsm_at(flux, read_half, 3 * t);
+      o.flux[1] = rsm_at(flux, read_half, 3 * t + 1);
+      o.flux[2] = rsm_at(flux, read_half, 3 * t + 2);
       o.disc_area = area;
       o.position[0] = p.x;
       o.position[1] = p.y;
@@ -125,8 +131,8 @@ __global__ void __launch_bounds__(256) extract_kernel(DrvSpotLight L, int R, con
       for (int dx = 0; dx < 2; ++dx) {
         float w = (dx ? ax : 1.0f - ax) * (dy ? ay : 1.0f - ay);
         int xx = min(max(x0 + dx, 0), rs - 1), yy = min(max(y0 + dy, 0), rs - 1);
-        dd0 += w * dls_shadow[((size_t)yy * rs + xx) * 2];
-        dd1 += w * dls_shadow[((size_t)yy * rs + xx) * 2 + 1];
+        dd0 += w * rsm_at(dls_shadow, shadow_half, ((size_t)yy * rs + xx) * 2);
+        dd1 += w * rsm_at(dls_shadow, shadow_half, ((size_t)yy * rs + xx) * 2 + 1);
       }
     f3 avg = lp + unproject_dir(L, u, v) * dd0;
     float var = fmaxf(0.0f, dd1 - dd0 * dd0);  // clamped: rounding can push it below 0
@@ -137,22 +143,24 @@ __global__ void __launch_bounds__(256) extract_kernel(DrvSpotLight L, int R, con
 
 }  // namespace
 
-cudaError_t launch_downsample_rsm(cudaStream_t s, int res, const float* flux, const int16_t* nrm, const float* dls,
-                                  float* fo, int16_t* no, float* dlo) {
+cudaError_t launch_downsample_rsm(cudaStream_t s, int res, const void* flux, const int16_t* nrm, const void* dls,
+                                  int src_half, float* fo, int16_t* no, float* dlo) {
   int h = res / 2;
   dim3 block(16, 16), grid((h + 15) / 16, (h + 15) / 16);
-  downsample_kernel<<<grid, block, 0, s>>>(res, flux, nrm, dls, fo, no, dlo);
+  downsample_kernel<<<grid, block, 0, s>>>(res, flux, nrm, dls, src_half, fo, no, dlo);
   return cudaGetLastError();
 }
 
-cudaError_t launch_extract_vpls(cudaStream_t s, const DrvSpotLight& L, int res, const float* flux, const int16_t* nrm,
-                                const float* dls, const float* dls_shadow, void* vpls, DrvShadowCone* cones,
-                                int precision) {
+cudaError_t launch_extract_vpls(cudaStream_t s, const DrvSpotLight& L, int res, const void* flux, const int16_t* nrm,
+                                const void* dls, int read_half, const void* dls_shadow, int shadow_half, void* vpls,
+                                DrvShadowCone* cones, int precision) {
   int n = res * res;
   if (precision == DRV_PRECISION_BF16)
-    extract_kernel<true><<<(n + 255) / 256, 256, 0, s>>>(L, res, flux, nrm, dls, dls_shadow, vpls, cones);
+    extract_kernel<true><<<(n + 255) / 256, 256, 0, s>>>(L, res, flux, nrm, dls, read_half, dls_shadow, shadow_half,
+                                                         vpls, cones);
   else
-    extract_kernel<false><<<(n + 255) / 256, 256, 0, s>>>(L, res, flux, nrm, dls, dls_shadow, vpls, cones);
+    extract_kernel<false><<<(n + 255) / 256, 256, 0, s>>>(L, res, flux, nrm, dls, read_half, dls_shadow, shadow_half,
+                                                          vpls, cones);
   return cudaGetLastError();
 }
 

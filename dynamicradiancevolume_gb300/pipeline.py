@@ -160,7 +160,7 @@ class Pipeline:
         self.rsm_views = (abi.DrvRSMView * w.n_lights)()
         for l in range(w.n_lights):
             self.rsm_views[l] = abi.DrvRSMView(R, self.rsm_flux[l].data_ptr(), self.rsm_normal[l].data_ptr(),
-                                               self.rsm_dls[l].data_ptr())
+                                               self.rsm_dls[l].data_ptr(), abi.RSM_F32)
         # torch's pooled streams do not wait for its current stream, where the
         # buffers above were zeroed: finish that before any stage runs.
         torch.cuda.current_stream(self.device).synchronize()

@@ -82,6 +82,14 @@ typedef enum drv_normal_format {
  * (renderer.cpp:468, written with FRAMEBUFFER_SRGB on, renderer.cpp:507):
  * 3 bytes per pixel, sRGB-encoded, read back as linear through the GL sRGB
  * decode (GL 4.5 section 8.24). */
+/* RSM flux and (d, d^2): F32, or F16 as the reference's RGB16F / RG16F
+ * targets (renderer.cpp:1288-1297); the context's mip chain below the caller's
+ * level is F32 either way. */
+typedef enum drv_rsm_format {
+  DRV_RSM_F32 = 0,
+  DRV_RSM_F16 = 1
+} drv_rsm_format;
+
 typedef enum drv_albedo_format {
   DRV_ALBEDO_F32X3 = 0,
   DRV_ALBEDO_SRGB8 = 1
@@ -225,9 +233,10 @@ typedef struct DrvGBufferOut {
  * normal RG16I, (distance, distance^2). */
 typedef struct DrvRSMView {
   int32_t resolution;
-  const float* flux;
-  const int16_t* normal;
-  const float* depth_lin_sq;
+  const void* flux;                 /* RGB, drv_rsm_format */
+  const int16_t* normal;            /* RG16I PackNormal16I */
+  const void* depth_lin_sq;         /* (d, d^2), drv_rsm_format */
+  int32_t format;                   /* drv_rsm_format */
 } DrvRSMView;
 
 typedef struct DrvRSMOut {

@@ -67,3 +67,38 @@ def test_srgb8_albedo_equals_its_linear_decode(w, lib, cuda):
     assert lib.drv_apply(p.ctx, C.byref(bad), C.byref(p.hf.frame), C.byref(p.hf.volume),
                          C.c_void_p(out8.data_ptr())) == abi.ERR_INVALID_ARG
     p.close()
+
+
+@pytest.mark.parametrize("w", [pipeline.WORKLOADS["c1_small"], REDUCED], ids=["c1", "c2r"])
+def test_f16_rsm_equals_its_f32_widening(w, lib, cuda):
+    """RGB16F flux and RG16F (d, d^2), the reference's RSM targets: the VPLs
+    and shadow-cone sources equal those of an F32 RSM holding the same
+    values, bit for bit (the chain below the caller's level is F32)."""
+    torch = pytest.importorskip("torch")
+    p = pipeline.Pipeline(pipeline.host_frame(w, 6))
+    p.raycast_inputs()
+    p.sync()
+    n = w.n_lights
+    halves = [(p.rsm_flux[l].half().contiguous(), p.rsm_dls[l].half().contiguous()) for l in range(n)]
+    for l in range(n):  # the F32 RSM now holds the F16-rounded values
+        p.rsm_flux[l].copy_(halves[l][0].float())
+        p.rsm_dls[l].copy_(halves[l][1].float())
+    torch.cuda.synchronize()
+    p.prepare_and_extract()
+    p.sync()
+    nc = [p.buffers().n_vpls[l] // p.hf.lights[l].indirect_shadow_sample_interval for l in range(n)]
+    ref = [(p.read_vpls(l).cpu().clone(), p.read_cones(l, nc[l]).cpu().clone()) for l in range(n)]
+    R = w.rsm_resolution
+    views = (abi.DrvRSMView * n)()
+    for l in range(n):
+        views[l] = abi.DrvRSMView(R, halves[l][0].data_ptr(), p.rsm_normal[l].data_ptr(), halves[l][1].data_ptr(),
+                                  abi.RSM_F16)
+        assert lib.drv_prepare_rsm(p.ctx, l, C.byref(p.hf.lights[l]), C.byref(views[l])) == abi.OK
+        assert lib.drv_extract_vpls(p.ctx, l, C.byref(p.hf.lights[l])) == abi.OK
+    p.sync()
+    for l in range(n):
+        assert torch.equal(p.read_vpls(l).cpu(), ref[l][0])
+        assert torch.equal(p.read_cones(l, nc[l]).cpu(), ref[l][1])
+    bad = abi.DrvRSMView(R, halves[0][0].data_ptr(), p.rsm_normal[0].data_ptr(), halves[0][1].data_ptr(), 5)
+    assert lib.drv_prepare_rsm(p.ctx, 0, C.byref(p.hf.lights[0]), C.byref(bad)) == abi.ERR_INVALID_ARG
+    p.close()
