@@ -22,6 +22,8 @@ VISIBILITY_CONE, VISIBILITY_SURROGATE = 0, 1
 NORMAL_RG16I, NORMAL_F32X3 = 0, 1
 ALBEDO_F32X3, ALBEDO_SRGB8 = 0, 1
 RSM_F32, RSM_F16 = 0, 1
+OUTPUT_RGB32F, OUTPUT_RGBA16F = 0, 1
+OUTPUT_WRITE, OUTPUT_ADD = 0, 1
 
 f3 = C.c_float * 3
 f16 = C.c_float * 16
@@ -34,7 +36,7 @@ class DrvConfig(C.Structure):
                 ("cascade_world_size", C.c_float * MAX_CASCADES), ("voxel_res", C.c_int32),
                 ("max_caches", C.c_uint32), ("precision", C.c_int32), ("visibility", C.c_int32),
                 ("surrogate_conf_threshold", C.c_float), ("sh2_sign", C.c_int32), ("max_lights", C.c_int32),
-                ("max_rsm_resolution", C.c_int32)]
+                ("max_rsm_resolution", C.c_int32), ("output_format", C.c_int32), ("output_blend", C.c_int32)]
 
 
 class DrvCascade(C.Structure):

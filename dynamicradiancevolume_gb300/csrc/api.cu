@@ -98,6 +98,10 @@ drv_status validate_config(const DrvConfig* c, std::string& why) {
            DRV_ERR_INVALID_ARG;
   if (c->sh2_sign != DRV_SH2_SIGN_REFERENCE && c->sh2_sign != DRV_SH2_SIGN_FIXED)
     return why = "sh2_sign must be 0 or 1", DRV_ERR_INVALID_ARG;
+  if (c->output_format != DRV_OUTPUT_RGB32F && c->output_format != DRV_OUTPUT_RGBA16F)
+    return why = "output_format must be DRV_OUTPUT_RGB32F or DRV_OUTPUT_RGBA16F", DRV_ERR_INVALID_ARG;
+  if (c->output_blend != DRV_OUTPUT_WRITE && c->output_blend != DRV_OUTPUT_ADD)
+    return why = "output_blend must be DRV_OUTPUT_WRITE or DRV_OUTPUT_ADD", DRV_ERR_INVALID_ARG;
   return DRV_OK;
 }
 
@@ -594,6 +598,8 @@ drv_status drv_apply(DrvContext* ctx, const DrvGBufferView* g, const DrvPerFrame
                      float* out_rgb) {
   if (!ctx || !f || !vol || !out_rgb) return DRV_ERR_INVALID_ARG;
   if (!views_ok(g, ctx->cfg)) return fail(ctx, DRV_ERR_INVALID_ARG, "G-buffer view does not match the config");
+  if (reinterpret_cast<uintptr_t>(out_rgb) % (ctx->cfg.output_format == DRV_OUTPUT_RGBA16F ? 8 : 4))
+    return fail(ctx, DRV_ERR_INVALID_ARG, "misaligned output");
   return cuda_check(ctx, drv::launch_apply(ctx->s(), ctx->cfg, *vol, *f, *g, ctx->atlas, ctx->entries,
                                            ctx->entry_stride, ctx->counter, out_rgb, ctx->srgb),
                     "apply");

@@ -33,7 +33,8 @@ struct ApplyParams {
   const DrvCacheCounter* counter;
   uint32_t max_caches;
   float cl[5];  // ShCosLobeFactor0, 1, 2n2_p1_n1, 20, 2p2
-  float* out;
+  float* out;  // RGB F32, or RGBA16F (out_half)
+  int out_half, out_add;
   CellRecip rc;
 };
 
@@ -123,19 +124,45 @@ __device__ __forceinline__ f3 lighting(const ApplyParams& p, const float wp[3], 
   return irr;
 }
 
+// The pixel's radiance into the target: RGB F32 or RGBA16F, written (alpha
+// 1) or added (alpha kept; the sum in FP32, one rounding to FP16).
+__device__ __forceinline__ void store_output(const ApplyParams& p, size_t i, f3 c) {
+  if (p.out_half) {
+    uint2* o = reinterpret_cast<uint2*>(p.out) + i;
+    uint2 v = p.out_add ? *o : make_uint2(0u, 0u);
+    if (p.out_add) {
+      c.x += __half2float(__ushort_as_half((unsigned short)(v.x & 0xFFFFu)));
+      c.y += __half2float(__ushort_as_half((unsigned short)(v.x >> 16)));
+      c.z += __half2float(__ushort_as_half((unsigned short)(v.y & 0xFFFFu)));
+    }
+    const uint32_t hx = __half_as_ushort(__float2half_rn(c.x)), hy = __half_as_ushort(__float2half_rn(c.y)),
+                   hz = __half_as_ushort(__float2half_rn(c.z));
+    const uint32_t alpha = p.out_add ? (v.y >> 16) : 0x3C00u;  // written: alpha 1
+    *o = make_uint2(hx | hy << 16, hz | alpha << 16);
+    return;
+  }
+  float* o = p.out + 3 * i;
+  if (p.out_add) {
+    o[0] += c.x;
+    o[1] += c.y;
+    o[2] += c.z;
+  } else {
+    __stcs(o, c.x);
+    __stcs(o + 1, c.y);
+    __stcs(o + 2, c.z);
+  }
+}
+
 template <bool BF16, bool SH2>
 __global__ void __launch_bounds__(256) apply_kernel(ApplyParams p) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
   if (x >= p.w || y >= p.h) return;
   const size_t i = (size_t)y * p.w + x;
-  float* o = p.out + 3 * i;
   // G-buffer texels are read once and the output written once: streaming
   // (evict-first) accesses keep L1/L2 for the atlas and the cache entries.
   const float d = __ldcs(p.depth + i);
   if (d < 0.00001f) {  // cacheApply.frag:304-307 (discard)
-    __stcs(o, 0.0f);
-    __stcs(o + 1, 0.0f);
-    __stcs(o + 2, 0.0f);
+    if (!p.out_add) store_output(p, i, mkf3(0.0f, 0.0f, 0.0f));
     return;
   }
   f3 n;
@@ -163,9 +190,7 @@ __global__ void __launch_bounds__(256) apply_kernel(ApplyParams p) {
       col = col * (1.0f - t) + col2 * t;  // mix(), cacheApply.frag:359
     }
   }
-  __stcs(o, col.x);
-  __stcs(o + 1, col.y);
-  __stcs(o + 2, col.z);
+  store_output(p, i, col);
 }
 
 }  // namespace
@@ -202,6 +227,8 @@ cudaError_t launch_apply(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeIn
   p.cl[3] = (float)(std::sqrt(5.0 * kPi) / 16.0);
   p.cl[4] = (float)(std::sqrt(15.0 * kPi) / 16.0);
   p.out = out_rgb;
+  p.out_half = cfg.output_format == DRV_OUTPUT_RGBA16F;
+  p.out_add = cfg.output_blend == DRV_OUTPUT_ADD;
   dim3 block(16, 16), grid((g.width + 15) / 16, (g.height + 15) / 16);
   if (p.bf16)
     p.sh2 ? apply_kernel<true, true><<<grid, block, 0, s>>>(p) : apply_kernel<true, false><<<grid, block, 0, s>>>(p);

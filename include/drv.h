@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define DRV_ABI_VERSION 2
+#define DRV_ABI_VERSION 3
 #define DRV_MAX_CASCADES 4   /* MAX_NUM_ADDRESS_VOLUME_CASCADES, globalubos.glsl:43 */
 #define DRV_MAX_LIGHTS 16    /* maxExpectedLights, renderer.cpp:80 */
 #define DRV_LIGHTING_THREADS_PER_GROUP 64 /* lightcache.glsl:95 */
@@ -114,7 +114,26 @@ typedef struct DrvConfig {
   int32_t sh2_sign;                 /* drv_sh2_sign */
   int32_t max_lights;               /* lights per frame, <= DRV_MAX_LIGHTS */
   int32_t max_rsm_resolution;       /* largest RSMRenderResolution any light will use */
+  int32_t output_format;            /* drv_output_format of drv_apply / drv_frame's out_rgb */
+  int32_t output_blend;             /* drv_output_blend */
 } DrvConfig;
+
+/* The apply's target: RGB F32 (width*height*3 floats), or the reference's
+ * RGBA16F HDR back buffer (renderer.cpp:477; width*height*4 halves; alpha 1
+ * when written, kept when added). */
+typedef enum drv_output_format {
+  DRV_OUTPUT_RGB32F = 0,
+  DRV_OUTPUT_RGBA16F = 1
+} drv_output_format;
+
+/* Written, or added to what the target holds (the reference's blending,
+ * glBlendFunc(GL_ONE, GL_ONE) renderer.cpp:119 with BLEND on in
+ * ApplyCaches, renderer.cpp:1053: indirect light on top of the direct light;
+ * an RGBA16F sum is formed in FP32 and rounded once). */
+typedef enum drv_output_blend {
+  DRV_OUTPUT_WRITE = 0,
+  DRV_OUTPUT_ADD = 1
+} drv_output_blend;
 
 /* CAVCascade, globalubos.glsl:48-58 (std140, 64 B). */
 typedef struct DrvCascade {
@@ -402,8 +421,10 @@ drv_status drv_allocate_caches(DrvContext* ctx, const DrvGBufferView* gbuffer, c
 drv_status drv_light_caches(DrvContext* ctx, const DrvSpotLight* lights, int32_t n_lights,
                             const DrvVolumeInfo* vol, const DrvPerFrame* frame);
 /* Renderer::ApplyCaches (renderer.cpp:1047-1079, cacheApply.frag): indirect
- * diffuse radiance per pixel into out_rgb (device, width*height*3 floats,
- * written, not blended; pixels with depth < 1e-5 get 0). */
+ * diffuse radiance per pixel into out_rgb (device; DrvConfig.output_format:
+ * width*height*3 floats, or width*height*4 halves; DrvConfig.output_blend:
+ * written, or added; pixels with depth < 1e-5 get 0, or are left as they are
+ * when adding). */
 drv_status drv_apply(DrvContext* ctx, const DrvGBufferView* gbuffer, const DrvPerFrame* frame,
                      const DrvVolumeInfo* vol, float* out_rgb);
 /* All stages of one frame on the context stream (Renderer::Draw,

@@ -102,3 +102,45 @@ def test_f16_rsm_equals_its_f32_widening(w, lib, cuda):
     bad = abi.DrvRSMView(R, halves[0][0].data_ptr(), p.rsm_normal[0].data_ptr(), halves[0][1].data_ptr(), 5)
     assert lib.drv_prepare_rsm(p.ctx, 0, C.byref(p.hf.lights[0]), C.byref(bad)) == abi.ERR_INVALID_ARG
     p.close()
+
+
+@pytest.mark.parametrize("fmt,blend", [(abi.OUTPUT_RGB32F, abi.OUTPUT_ADD), (abi.OUTPUT_RGBA16F, abi.OUTPUT_WRITE),
+                                       (abi.OUTPUT_RGBA16F, abi.OUTPUT_ADD)])
+def test_output_targets(fmt, blend, lib, cuda):
+    """RGBA16F target and additive blending (the reference's HDR back buffer
+    with glBlendFunc(ONE, ONE)) against the RGB F32 written result: the same
+    FP32 radiance, added in FP32 and rounded once to FP16."""
+    torch = pytest.importorskip("torch")
+    w = pipeline.WORKLOADS["c1_small"]
+    hf = pipeline.host_frame(w, 8)
+    p = pipeline.Pipeline(hf)  # RGB32F, written
+    p.raycast_inputs()
+    p.frame()
+    p.sync()
+    ref = p.out.clone()
+    p.close()
+    hf2 = pipeline.host_frame(w, 8)
+    hf2.config.output_format, hf2.config.output_blend = fmt, blend
+    q = pipeline.Pipeline(hf2)
+    q.raycast_inputs()
+    H, W = w.height, w.width
+    g = torch.Generator(device="cpu").manual_seed(3)
+    if fmt == abi.OUTPUT_RGBA16F:
+        base = (torch.rand((H, W, 4), generator=g) * 4).half().to(q.device)
+    else:
+        base = (torch.rand((H, W, 3), generator=g) * 4).to(q.device)
+    out = base.clone() if blend == abi.OUTPUT_ADD else torch.full_like(base, 7.0)
+    torch.cuda.synchronize()
+    q.frame(out)
+    q.sync()
+    r = ref.cpu().numpy()
+    o = out.cpu().numpy()
+    b = base.cpu().numpy()
+    if fmt == abi.OUTPUT_RGB32F:
+        assert np.array_equal(o, b + r)
+    else:
+        exp_rgb = ((b[..., :3].astype(np.float32) + r) if blend == abi.OUTPUT_ADD else r).astype(np.float16)
+        assert np.array_equal(o[..., :3], exp_rgb)
+        exp_a = b[..., 3] if blend == abi.OUTPUT_ADD else np.ones((H, W), np.float16)
+        assert np.array_equal(o[..., 3], exp_a)
+    q.close()
