@@ -18,6 +18,7 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libdrv_gb300.so"
+CLI = PKG / "drv_frame_cli"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -53,6 +54,7 @@ def build(verbose: bool = False) -> Path:
     with ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
         objs = list(ex.map(_compile, srcs))
     if LIB.exists() and LIB.stat().st_mtime >= max(o.stat().st_mtime for o in objs):
+        build_cli()
         return LIB
     tmp = LIB.with_suffix(".so.tmp")
     cmd = [nvcc(), "-shared", "-o", str(tmp), *map(str, objs), *ARCH, "-cudart", "static",
@@ -61,9 +63,26 @@ def build(verbose: bool = False) -> Path:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_cli()
     if verbose:
         print(f"built {LIB}")
     return LIB
+
+
+def build_cli() -> Path:
+    """drv_frame_cli: the C++ caller of the C ABI (cpp/drv_frame_cli.cpp),
+    linked against libdrv_gb300.so next to it."""
+    src = PKG / "cpp" / "drv_frame_cli.cpp"
+    if CLI.exists() and CLI.stat().st_mtime >= max(src.stat().st_mtime, LIB.stat().st_mtime):
+        return CLI
+    tmp = CLI.with_suffix(".tmp")
+    cmd = [nvcc(), "-O2", "-std=c++17", str(src), "-o", str(tmp), "-I", str(PKG.parent / "include"), "-L", str(PKG),
+           "-ldrv_gb300", "-Xlinker", "-rpath,$ORIGIN", "-cudart", "static"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"drv_frame_cli build failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, CLI)
+    return CLI
 
 
 if __name__ == "__main__":
