@@ -93,6 +93,11 @@ class DrvGBufferOut(C.Structure):
                 ("albedo", C.c_void_p)]
 
 
+class DrvMesh(C.Structure):
+    _fields_ = [("positions", C.c_void_p), ("normals", C.c_void_p), ("albedo", C.c_void_p), ("indices", C.c_void_p),
+                ("n_vertices", C.c_int32), ("n_triangles", C.c_int32)]
+
+
 class DrvRSMView(C.Structure):
     _fields_ = [("resolution", C.c_int32), ("flux", C.c_void_p), ("normal", C.c_void_p),
                 ("depth_lin_sq", C.c_void_p), ("format", C.c_int32)]
@@ -144,7 +149,7 @@ LIGHT_PATH_AUTO, LIGHT_PATH_SINGLE, LIGHT_PATH_SPLIT = 0, 1, 2
 
 STRUCT_ORDER = [DrvConfig, DrvCascade, DrvVolumeInfo, DrvPerFrame, DrvSpotLight, DrvLightDesc, DrvCamera, DrvBox,
                 DrvScene, DrvGBufferView, DrvGBufferOut, DrvRSMView, DrvRSMOut, DrvVPL, DrvShadowCone,
-                DrvCacheCounter, DrvBuffers, DrvTuning]
+                DrvCacheCounter, DrvBuffers, DrvTuning, DrvMesh]
 
 P = C.POINTER
 VP = C.c_void_p
@@ -170,6 +175,9 @@ PROTOTYPES = {
     "drv_raycast_gbuffer": (C.c_int, [VP, P(DrvScene), P(DrvCamera), P(DrvPerFrame), C.c_int32, C.c_int32,
                                       P(DrvGBufferOut)]),
     "drv_raycast_rsm": (C.c_int, [VP, P(DrvScene), P(DrvSpotLight), P(DrvRSMOut)]),
+    "drv_raster_gbuffer": (C.c_int, [VP, P(DrvMesh), P(DrvCamera), P(DrvPerFrame), C.c_int32, C.c_int32,
+                                     P(DrvGBufferOut)]),
+    "drv_raster_rsm": (C.c_int, [VP, P(DrvMesh), P(DrvSpotLight), P(DrvRSMOut)]),
     "drv_prepare_rsm": (C.c_int, [VP, C.c_int32, P(DrvSpotLight), P(DrvRSMView)]),
     "drv_extract_vpls": (C.c_int, [VP, C.c_int32, P(DrvSpotLight)]),
     "drv_set_scene": (C.c_int, [VP, P(DrvScene)]),

@@ -50,6 +50,7 @@ void release(Context* c) {
   cudaFree(c->vox_records);
   cudaFree(c->ndc);
   cudaFree(c->srgb);
+  cudaFree(c->raster_keys);
 
   cudaFree(c->light_scratch);
   cudaFree(c->light_tickets);
@@ -172,7 +173,7 @@ int drv_struct_sizes(uint32_t* out, int capacity) {
                         sizeof(DrvSpotLight),  sizeof(DrvLightDesc),  sizeof(DrvCamera),     sizeof(DrvBox),
                         sizeof(DrvScene),      sizeof(DrvGBufferView), sizeof(DrvGBufferOut), sizeof(DrvRSMView),
                         sizeof(DrvRSMOut),     sizeof(DrvVPL),        sizeof(DrvShadowCone), sizeof(DrvCacheCounter),
-                        sizeof(DrvBuffers),    sizeof(DrvTuning)};
+                        sizeof(DrvBuffers),    sizeof(DrvTuning),     sizeof(DrvMesh)};
   int n = (int)(sizeof(s) / sizeof(s[0]));
   if (!out) return n;
   int k = capacity < n ? capacity : n;
@@ -404,6 +405,61 @@ drv_status drv_raycast_rsm(DrvContext* ctx, const DrvScene* scene, const DrvSpot
   drv_status st = drv_set_scene(ctx, scene);
   if (st != DRV_OK) return st;
   return cuda_check(ctx, drv::launch_raycast_rsm(ctx->s(), ctx->d_boxes, scene->n_boxes, *light, *out), "raycast_rsm");
+}
+
+namespace {
+
+bool mesh_ok(const DrvMesh* m) {
+  if (!m || m->n_triangles < 0 || m->n_vertices < 0) return false;
+  if (m->n_triangles > 0 && (!m->positions || m->n_vertices < 1)) return false;
+  if (!m->indices && (int64_t)m->n_triangles * 3 > m->n_vertices) return false;
+  for (const void* p : {(const void*)m->positions, (const void*)m->normals, (const void*)m->albedo,
+                        (const void*)m->indices})
+    if (reinterpret_cast<uintptr_t>(p) % 4) return false;
+  return true;
+}
+
+// The visibility buffer of the mesh producers, grown to `pixels`.
+drv_status ensure_raster_keys(DrvContext* ctx, size_t pixels) {
+  if (ctx->raster_keys_cap >= pixels) return DRV_OK;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  DRV_TRY_CUDA(ctx, cudaStreamIsCapturing(ctx->s(), &cs));
+  if (cs != cudaStreamCaptureStatusNone)
+    return fail(ctx, DRV_ERR_INVALID_ARG, "first mesh raster at this size while the stream is being captured");
+  DRV_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->s()));
+  cudaFree(ctx->raster_keys);
+  ctx->raster_keys = nullptr;
+  ctx->raster_keys_cap = 0;
+  DRV_TRY_CUDA(ctx, cudaMalloc(&ctx->raster_keys, pixels * sizeof(unsigned long long)));
+  ctx->raster_keys_cap = pixels;
+  return DRV_OK;
+}
+
+}  // namespace
+
+drv_status drv_raster_gbuffer(DrvContext* ctx, const DrvMesh* mesh, const DrvCamera* cam, const DrvPerFrame* frame,
+                              int32_t w, int32_t h, const DrvGBufferOut* out) {
+  if (!ctx || !cam || !frame || !out || !out->depth || !out->albedo || w < 1 || h < 1) return DRV_ERR_INVALID_ARG;
+  if (!mesh_ok(mesh)) return fail(ctx, DRV_ERR_INVALID_ARG, "bad mesh");
+  drv_status st = ensure_raster_keys(ctx, (size_t)w * h);
+  if (st != DRV_OK) return st;
+  const double ty = std::tan(cam->fov_y_deg * (3.14159265358979323846 / 180.0) * 0.5);
+  const drv::RayFrame rf = drv::make_ray_frame(cam->position, cam->direction, cam->up, ty * cam->aspect, ty);
+  return cuda_check(ctx,
+                    drv::launch_raster_gbuffer(ctx->s(), *mesh, rf, frame->view_projection, w, h, ctx->raster_keys,
+                                               *out, ctx->num_sms),
+                    "raster_gbuffer");
+}
+
+drv_status drv_raster_rsm(DrvContext* ctx, const DrvMesh* mesh, const DrvSpotLight* light, const DrvRSMOut* out) {
+  if (!ctx || !light || !out || !out->flux || !out->normal || !out->depth_lin_sq) return DRV_ERR_INVALID_ARG;
+  if (light->rsm_render_resolution < 1) return DRV_ERR_INVALID_ARG;
+  if (!mesh_ok(mesh)) return fail(ctx, DRV_ERR_INVALID_ARG, "bad mesh");
+  const size_t R = (size_t)light->rsm_render_resolution;
+  drv_status st = ensure_raster_keys(ctx, R * R);
+  if (st != DRV_OK) return st;
+  return cuda_check(ctx, drv::launch_raster_rsm(ctx->s(), *mesh, *light, ctx->raster_keys, *out, ctx->num_sms),
+                    "raster_rsm");
 }
 
 // ShadowMap::PrepareRSM (renderer.cpp:1300-1339): successive 2x2 reductions,

@@ -134,6 +134,8 @@ struct Context {
   size_t voxel_words = 0;
   float* ndc = nullptr;  // NDC x of each pixel column (width), then y of each row (height): allocation
   float* srgb = nullptr;  // the GL sRGB decode of the 256 byte values (DRV_ALBEDO_SRGB8)
+  unsigned long long* raster_keys = nullptr;  // mesh producers' per-pixel visibility (drv_raster_*)
+  size_t raster_keys_cap = 0;
   uint8_t* vox_corners = nullptr;  // level 0, corner-packed bytes in 4^3 bricks
   void* mips = nullptr;  // levels 1..L concatenated: float (FP32 precision) or half (BF16 precision)
   size_t mip_offset[kMaxVoxelLevels] = {};
@@ -191,6 +193,10 @@ RayFrame make_ray_frame(const float pos[3], const float dir[3], const float up[3
 cudaError_t launch_raycast_gbuffer(cudaStream_t s, const DrvBox* boxes, int n_boxes, RayFrame rf,
                                    const float* view_proj, int w, int h, DrvGBufferOut out);
 cudaError_t launch_raycast_rsm(cudaStream_t s, const DrvBox* boxes, int n_boxes, const DrvSpotLight& L, DrvRSMOut out);
+cudaError_t launch_raster_gbuffer(cudaStream_t s, const DrvMesh& mesh, RayFrame rf, const float* view_proj, int w,
+                                  int h, unsigned long long* keys, DrvGBufferOut out, int num_sms);
+cudaError_t launch_raster_rsm(cudaStream_t s, const DrvMesh& mesh, const DrvSpotLight& L, unsigned long long* keys,
+                              DrvRSMOut out, int num_sms);
 cudaError_t launch_downsample_rsm(cudaStream_t s, int res, const void* flux, const int16_t* nrm, const void* dls,
                                   int src_half, float* fo, int16_t* no, float* dlo);
 cudaError_t launch_extract_vpls(cudaStream_t s, const DrvSpotLight& L, int res, const void* flux, const int16_t* nrm,

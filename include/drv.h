@@ -382,6 +382,29 @@ drv_status drv_raycast_gbuffer(DrvContext* ctx, const DrvScene* scene, const Drv
 drv_status drv_raycast_rsm(DrvContext* ctx, const DrvScene* scene, const DrvSpotLight* light,
                            const DrvRSMOut* out);
 
+/* A triangle mesh (device buffers): world-space positions (xyz per vertex),
+ * optional vertex normals (xyz per vertex; NULL: face normals), optional
+ * linear RGB albedo per triangle (NULL: 1), indices (3 per triangle; NULL:
+ * consecutive vertex triples). Untextured: the reference's base-colour and
+ * normal maps are not read. */
+typedef struct DrvMesh {
+  const float* positions;
+  const float* normals;
+  const float* albedo;
+  const uint32_t* indices;
+  int32_t n_vertices, n_triangles;
+} DrvMesh;
+
+/* The G-buffer fill (fillgbuffer.frag) and the RSM fill (fillrsm.frag:24-62)
+ * of a triangle mesh: visibility by rasterising the mesh (near-plane clip,
+ * pixel centres, reversed-Z nearest), then the pixel's ray against the
+ * visible triangle, shaded as the box producers above (normals turned to the
+ * viewer). The first call at a size allocates a 64-bit per-pixel visibility
+ * buffer (not while the stream is being captured). */
+drv_status drv_raster_gbuffer(DrvContext* ctx, const DrvMesh* mesh, const DrvCamera* camera,
+                              const DrvPerFrame* frame, int32_t width, int32_t height, const DrvGBufferOut* out);
+drv_status drv_raster_rsm(DrvContext* ctx, const DrvMesh* mesh, const DrvSpotLight* light, const DrvRSMOut* out);
+
 /* ---- the per-frame stages ----------------------------------------------- */
 /* ShadowMap::PrepareRSM + downsamplersm.frag (renderer.cpp:1300-1339): build
  * the RSM mip chain of light `light_index` from its render-resolution level

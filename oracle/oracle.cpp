@@ -596,6 +596,160 @@ void orc_raycast_rsm(const DrvBox* boxes, int n, const DrvSpotLight* L, float* f
     }
 }
 
+// The same producers for a triangle mesh (positions xyz per vertex, optional
+// vertex normals, optional RGB albedo per triangle, optional indices): the
+// nearest triangle along each ray (either face, inside the depth range),
+// normal = face normal or the barycentric blend of the vertex normals, turned
+// towards the ray.
+namespace {
+struct MeshIn {
+  const float* pos;
+  const float* nrm;
+  const float* alb;
+  const uint32_t* idx;
+  int nt;
+};
+
+d3 mesh_vertex(const MeshIn& m, uint32_t i) { return {m.pos[3 * i], m.pos[3 * i + 1], m.pos[3 * i + 2]}; }
+
+void mesh_tri(const MeshIn& m, int k, uint32_t v[3]) {
+  for (int j = 0; j < 3; ++j) v[j] = m.idx ? m.idx[3 * k + j] : 3u * k + j;
+}
+
+// Clip-space depth z/w of p under the row-major view-projection M, and
+// whether it lies in the rasteriser's depth range [0, 1] (near and far
+// planes; reversed-Z, so nearer is larger).
+bool in_depth_range(const float* M, d3 p) {
+  const double cz = M[8] * p.x + M[9] * p.y + M[10] * p.z + M[11];
+  const double cw = M[12] * p.x + M[13] * p.y + M[14] * p.z + M[15];
+  if (!(cw > 0.0)) return false;
+  const double z = cz / cw;
+  return z >= 0.0 && z <= 1.0;
+}
+
+// Nearest hit (Moller-Trumbore, both faces, t > 1e-6) inside the target's
+// depth range, as a rasteriser clips against the near and far planes:
+// triangle or -1.
+int mesh_trace(const MeshIn& m, const float* M, d3 o, d3 d, double& t_hit, double& l1, double& l2) {
+  int best = -1;
+  t_hit = 1e300;
+  for (int k = 0; k < m.nt; ++k) {
+    uint32_t v[3];
+    mesh_tri(m, k, v);
+    const d3 v0 = mesh_vertex(m, v[0]), e1 = mesh_vertex(m, v[1]) - v0, e2 = mesh_vertex(m, v[2]) - v0;
+    const d3 pv = cross(d, e2);
+    const double det = dot(e1, pv);
+    if (std::fabs(det) < 1e-300) continue;
+    const double inv = 1.0 / det;
+    const d3 tv = o - v0;
+    const double a = dot(tv, pv) * inv;
+    if (a < 0.0 || a > 1.0) continue;
+    const d3 qv = cross(tv, e1);
+    const double b = dot(d, qv) * inv;
+    if (b < 0.0 || a + b > 1.0) continue;
+    const double t = dot(e2, qv) * inv;
+    if (t > 1e-6 && t < t_hit && in_depth_range(M, o + d * t)) {
+      t_hit = t;
+      best = k;
+      l1 = a;
+      l2 = b;
+    }
+  }
+  return best;
+}
+
+d3 mesh_normal(const MeshIn& m, int k, double l1, double l2, d3 d) {
+  uint32_t v[3];
+  mesh_tri(m, k, v);
+  d3 n;
+  if (m.nrm) {
+    auto vn = [&](uint32_t i) { return d3{m.nrm[3 * i], m.nrm[3 * i + 1], m.nrm[3 * i + 2]}; };
+    n = vn(v[0]) * (1.0 - l1 - l2) + vn(v[1]) * l1 + vn(v[2]) * l2;
+  } else {
+    const d3 v0 = mesh_vertex(m, v[0]);
+    n = cross(mesh_vertex(m, v[1]) - v0, mesh_vertex(m, v[2]) - v0);
+  }
+  n = normalize(n);
+  if (dot(n, d) > 0.0) n = n * -1.0;
+  return d3{n.x + 0.0, n.y + 0.0, n.z + 0.0};  // no negative zeros (they pack to the other end of the atan2 range)
+}
+}  // namespace
+
+void orc_raycast_gbuffer_mesh(const float* pos, const float* nrm, const float* alb, const uint32_t* idx, int n_tris,
+                              const DrvPerFrame* f, const DrvCamera* cam, int W, int H, float* depth, int16_t* n16,
+                              float* n32, float* albedo) {
+  const MeshIn m{pos, nrm, alb, idx, n_tris};
+  d3 r, u, fw;
+  basis(ld3(cam->direction), ld3(cam->up), r, u, fw);
+  double ty = std::tan(cam->fov_y_deg * (kPi / 180.0) * 0.5), tx = ty * cam->aspect;
+  d3 o = ld3(cam->position);
+#pragma omp parallel for schedule(dynamic, 4)
+  for (int y = 0; y < H; ++y)
+    for (int x = 0; x < W; ++x) {
+      size_t i = (size_t)y * W + x;
+      double nx = ((x + 0.5) / W) * 2.0 - 1.0, ny = ((y + 0.5) / H) * 2.0 - 1.0;
+      d3 d = normalize(fw + r * (nx * tx) + u * (ny * ty));
+      double t, l1 = 0, l2 = 0;
+      const int k = mesh_trace(m, f->view_projection, o, d, t, l1, l2);
+      if (k < 0) {
+        depth[i] = 0.0f;
+        if (n16) n16[2 * i] = n16[2 * i + 1] = 0;
+        if (n32) n32[3 * i] = n32[3 * i + 1] = n32[3 * i + 2] = 0.0f;
+        for (int c = 0; c < 3; ++c) albedo[3 * i + c] = 0.0f;
+        continue;
+      }
+      d3 p = o + d * t;
+      const float* M = f->view_projection;
+      double cz = M[8] * p.x + M[9] * p.y + M[10] * p.z + M[11];
+      double cw = M[12] * p.x + M[13] * p.y + M[14] * p.z + M[15];
+      depth[i] = (float)(cz / cw);
+      const d3 n = mesh_normal(m, k, l1, l2, d);
+      double nn[3] = {n.x, n.y, n.z};
+      if (n16) orc_pack_normal16i(nn, n16 + 2 * i);
+      if (n32)
+        for (int c = 0; c < 3; ++c) n32[3 * i + c] = (float)nn[c];
+      for (int c = 0; c < 3; ++c) albedo[3 * i + c] = alb ? alb[3 * k + c] : 1.0f;
+    }
+}
+
+void orc_raycast_rsm_mesh(const float* pos, const float* nrm, const float* alb, const uint32_t* idx, int n_tris,
+                          const DrvSpotLight* L, float* flux, int16_t* n16, float* dls) {
+  const MeshIn m{pos, nrm, alb, idx, n_tris};
+  int R = L->rsm_render_resolution;
+  d3 o = ld3(L->position);
+  d3 ldir = ld3(L->direction);
+  double cos_half = L->cos_half_angle;
+#pragma omp parallel for schedule(dynamic, 4)
+  for (int y = 0; y < R; ++y)
+    for (int x = 0; x < R; ++x) {
+      size_t i = (size_t)y * R + x;
+      d3 d = unproject_dir(L->inverse_view_projection, (x + 0.5) / R, (y + 0.5) / R, o);
+      double th, l1 = 0, l2 = 0;
+      const int k = mesh_trace(m, L->view_projection, o, d, th, l1, l2);
+      if (k < 0) {
+        flux[3 * i] = flux[3 * i + 1] = flux[3 * i + 2] = 0.0f;
+        n16[2 * i] = n16[2 * i + 1] = 0;
+        dls[2 * i] = dls[2 * i + 1] = 0.0f;
+        continue;
+      }
+      d3 p = o + d * th;
+      d3 to_light = o - p;
+      double dist = length(to_light);
+      to_light = to_light * (1.0 / dist);
+      double cos_to_light = saturate(dot(to_light * -1.0, ldir));
+      double total_sr = 2.0 * kShaderPi * (1.0 - cos_half);
+      double pixel_sr = total_sr * cos_to_light / R / R;
+      double falloff = saturate(cos_to_light - cos_half) / (1.0 - cos_half);
+      for (int c = 0; c < 3; ++c)
+        flux[3 * i + c] = (float)((alb ? alb[3 * k + c] : 1.0f) * L->intensity[c] * (falloff * pixel_sr / kShaderPi));
+      dls[2 * i] = (float)dist;
+      dls[2 * i + 1] = (float)(dist * dist);
+      const d3 n = mesh_normal(m, k, l1, l2, d);
+      double nn[3] = {n.x, n.y, n.z};
+      orc_pack_normal16i(nn, n16 + 2 * i);
+    }
+}
+
 // downsamplersm.frag:15-33: flux = sum of the 2x2 children (textureGather),
 // normal = PackNormal16I(normalize(sum of unpacked)), (d, d^2) = bilinear at
 // the shared corner = mean of the 4 children.

@@ -71,6 +71,12 @@ void orc_extract_vpls(const DrvSpotLight* light, int res, const float* flux, con
                       const float* dls_shadow, double* vpl_out, double* cone_out);
 /* Surface voxelization of the box scene into the level-0 bitmask. */
 void orc_voxelize(const DrvBox* boxes, int n_boxes, const DrvVolumeInfo* vol, int voxel_res, uint32_t* bits);
+// Mesh producers (nrm, alb, idx may be NULL).
+void orc_raycast_gbuffer_mesh(const float* pos, const float* nrm, const float* alb, const uint32_t* idx, int n_tris,
+                              const DrvPerFrame* f, const DrvCamera* cam, int W, int H, float* depth, int16_t* n16,
+                              float* n32, float* albedo);
+void orc_raycast_rsm_mesh(const float* pos, const float* nrm, const float* alb, const uint32_t* idx, int n_tris,
+                          const DrvSpotLight* L, float* flux, int16_t* n16, float* dls);
 // Triangle mesh (positions xyz per vertex; indices: 3 per triangle, or NULL for consecutive triples).
 void orc_voxelize_triangles(const float* positions, const uint32_t* indices, int n_tris, const DrvVolumeInfo* vol,
                             int voxel_res, uint32_t* bits);

@@ -59,6 +59,9 @@ def load():
         "orc_extract_vpls": (None, [P(abi.DrvSpotLight), I, VP, VP, VP, VP, VP, VP]),
         "orc_voxelize": (None, [P(abi.DrvBox), I, P(abi.DrvVolumeInfo), I, VP]),
         "orc_voxelize_triangles": (None, [VP, VP, I, P(abi.DrvVolumeInfo), I, VP]),
+        "orc_raycast_gbuffer_mesh": (None, [VP, VP, VP, VP, I, P(abi.DrvPerFrame), P(abi.DrvCamera), I, I, VP, VP,
+                                            VP, VP]),
+        "orc_raycast_rsm_mesh": (None, [VP, VP, VP, VP, I, P(abi.DrvSpotLight), VP, VP, VP]),
         "orc_build_mips": (None, [I, VP, VP]),
         "orc_allocate_caches": (I, [P(abi.DrvConfig), P(abi.DrvVolumeInfo), P(abi.DrvPerFrame), I, I, VP, VP, VP,
                                     P(C.c_uint32)]),
@@ -217,6 +220,37 @@ def voxelize_triangles(positions, indices, vol, N):
     bits = np.zeros(N ** 3 // 32, np.uint32)
     load().orc_voxelize_triangles(_p(pos), None if idx is None else _p(idx), n, C.byref(vol), N, _p(bits))
     return bits
+
+
+def _mesh_args(positions, normals, albedo, indices):
+    pos = np.ascontiguousarray(positions, dtype=np.float32).reshape(-1, 3)
+    nrm = None if normals is None else np.ascontiguousarray(normals, dtype=np.float32).reshape(-1, 3)
+    alb = None if albedo is None else np.ascontiguousarray(albedo, dtype=np.float32).reshape(-1, 3)
+    idx = None if indices is None else np.ascontiguousarray(indices, dtype=np.uint32).reshape(-1, 3)
+    n = len(pos) // 3 if idx is None else len(idx)
+    keep = (pos, nrm, alb, idx)
+    return keep, [_p(pos), None if nrm is None else _p(nrm), None if alb is None else _p(alb),
+                  None if idx is None else _p(idx), n]
+
+
+def raycast_gbuffer_mesh(positions, normals, albedo, indices, frame, cam, W, H):
+    keep, args = _mesh_args(positions, normals, albedo, indices)
+    depth = np.zeros((H, W), np.float32)
+    n16 = np.zeros((H, W, 2), np.int16)
+    n32 = np.zeros((H, W, 3), np.float32)
+    alb = np.zeros((H, W, 3), np.float32)
+    load().orc_raycast_gbuffer_mesh(*args, C.byref(frame), C.byref(cam), W, H, _p(depth), _p(n16), _p(n32), _p(alb))
+    return depth, n16, n32, alb
+
+
+def raycast_rsm_mesh(positions, normals, albedo, indices, light):
+    keep, args = _mesh_args(positions, normals, albedo, indices)
+    R = light.rsm_render_resolution
+    flux = np.zeros((R, R, 3), np.float32)
+    n16 = np.zeros((R, R, 2), np.int16)
+    dls = np.zeros((R, R, 2), np.float32)
+    load().orc_raycast_rsm_mesh(*args, C.byref(light), _p(flux), _p(n16), _p(dls))
+    return flux, n16, dls
 
 
 def build_mips(N, bits):
