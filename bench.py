@@ -427,6 +427,25 @@ def run_ours(args):
                 info["rel_l2_vs_fp64"] = rel_l2(out, reference)
             variants[name] = info
             pipes[name] = pipe
+        # INDIRECT_SPECULAR with the reference's 16x16 per-cache envmaps on the
+        # BF16 frame: its cost (the envmap pass inside the light stage, the
+        # mips and the specular apply inside the frame). Not a headline
+        # candidate: the specular frame is another image.
+        import numpy as np
+        hf = pipeline.host_frame(pipeline.scaled(w, precision=abi.PRECISION_BF16, specular_envmap_size=16))
+        sp = pipeline.Pipeline(hf, device=str(dev))
+        rm = np.random.default_rng(11).integers(0, 256, (w.height, w.width, 2), dtype=np.uint8)
+        sp.rough_metal.copy_(torch.from_numpy(rm).to(dev))
+        torch.cuda.synchronize(dev)
+        sp.raycast_inputs()
+        sp.frame()
+        sp.sync()
+        specular = {"envmap_size": 16, "precision": "bf16", "caches": sp.cache_count(),
+                    "light_ms": measure_light_graph(sp, args.steps, args.warmup, flush),
+                    "frame_ms": measure_graph(sp, args.steps, args.warmup, flush),
+                    "light_ms_without": variants["precision_bf16"]["light_ms"],
+                    "frame_ms_without": variants["precision_bf16"]["frame_ms"]}
+        sp.close()
     clocks = clk.summary()
     ok = {n: v for n, v in variants.items() if v.get("rel_l2_vs_fp64", 1.0) <= 0.01}
     head = max(ok, key=lambda n: ok[n]["caches_lit_per_s"]) if ok else "plain_fp32"
@@ -598,6 +617,7 @@ def run_ours(args):
         "stage_ms": hv["stage_ms"],
         "light_kernel_ms": kernel_ms,
         "variants": variants,
+        "specular": specular,
         "roofline": roofline,
         "e2e": {"value": caches_all / (e2e_ms_all / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms_all, "ms_per_step_drv_frame": e2e_frame_ms,

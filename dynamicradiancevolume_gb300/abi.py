@@ -21,6 +21,7 @@ PRECISION_FP32, PRECISION_BF16 = 0, 1
 VISIBILITY_CONE, VISIBILITY_SURROGATE = 0, 1
 NORMAL_RG16I, NORMAL_F32X3 = 0, 1
 ALBEDO_F32X3, ALBEDO_SRGB8 = 0, 1
+ROUGH_METAL_RG8, ROUGH_METAL_F32 = 0, 1
 RSM_F32, RSM_F16 = 0, 1
 OUTPUT_RGB32F, OUTPUT_RGBA16F = 0, 1
 OUTPUT_WRITE, OUTPUT_ADD = 0, 1
@@ -36,7 +37,8 @@ class DrvConfig(C.Structure):
                 ("cascade_world_size", C.c_float * MAX_CASCADES), ("voxel_res", C.c_int32),
                 ("max_caches", C.c_uint32), ("precision", C.c_int32), ("visibility", C.c_int32),
                 ("surrogate_conf_threshold", C.c_float), ("sh2_sign", C.c_int32), ("max_lights", C.c_int32),
-                ("max_rsm_resolution", C.c_int32), ("output_format", C.c_int32), ("output_blend", C.c_int32)]
+                ("max_rsm_resolution", C.c_int32), ("output_format", C.c_int32), ("output_blend", C.c_int32),
+                ("specular_envmap_size", C.c_int32), ("specular_fill_level", C.c_int32)]
 
 
 class DrvCascade(C.Structure):
@@ -85,7 +87,8 @@ class DrvScene(C.Structure):
 
 class DrvGBufferView(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("depth", C.c_void_p), ("normal", C.c_void_p),
-                ("normal_format", C.c_int32), ("albedo", C.c_void_p), ("albedo_format", C.c_int32)]
+                ("normal_format", C.c_int32), ("albedo", C.c_void_p), ("albedo_format", C.c_int32),
+                ("rough_metal", C.c_void_p), ("rough_metal_format", C.c_int32)]
 
 
 class DrvGBufferOut(C.Structure):
@@ -127,7 +130,9 @@ class DrvBuffers(C.Structure):
                 ("voxel_mips", C.c_void_p * 16),
                 ("n_voxel_levels", C.c_int32), ("vpls", C.c_void_p * MAX_LIGHTS),
                 ("cones", C.c_void_p * MAX_LIGHTS), ("n_vpls", C.c_int32 * MAX_LIGHTS), ("n_lights", C.c_int32),
-                ("voxel_mip_records", C.c_void_p * 16), ("n_record_levels", C.c_int32)]
+                ("voxel_mip_records", C.c_void_p * 16), ("n_record_levels", C.c_int32),
+                ("specular_envmap", C.c_void_p * 8), ("specular_atlas_size", C.c_int32),
+                ("n_specular_levels", C.c_int32)]
 
 
 class DrvTuning(C.Structure):
@@ -203,6 +208,7 @@ PROTOTYPES = {
     "drv_get_light_kernel_ms": (C.c_int, [VP, P(C.c_float)]),
     "drv_get_light_pairs": (C.c_int, [VP, P(C.c_uint32)]),
     "drv_bruteforce_rsm": (C.c_int, [VP, P(DrvGBufferView), VP, P(DrvPerFrame), C.c_int32, VP]),
+    "drv_prepare_specular_envmaps": (C.c_int, [VP]),
     "drv_write_pfm": (C.c_int, [C.c_char_p, P(C.c_float), C.c_int32, C.c_int32, C.c_int32]),
     "drv_read_pfm": (C.c_int, [C.c_char_p, P(C.c_float), C.c_int64, P(C.c_int32), P(C.c_int32)]),
     "drv_batch_create": (C.c_int, [P(DrvBatchScene), C.c_int32, C.c_int32, VP, P(VP)]),

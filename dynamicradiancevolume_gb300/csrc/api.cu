@@ -51,6 +51,8 @@ void release(Context* c) {
   cudaFree(c->ndc);
   cudaFree(c->srgb);
   cudaFree(c->raster_keys);
+  cudaFree(c->spec_env);
+  cudaFree(c->spec_half);
 
   cudaFree(c->light_scratch);
   cudaFree(c->light_tickets);
@@ -103,6 +105,12 @@ drv_status validate_config(const DrvConfig* c, std::string& why) {
     return why = "output_format must be DRV_OUTPUT_RGB32F or DRV_OUTPUT_RGBA16F", DRV_ERR_INVALID_ARG;
   if (c->output_blend != DRV_OUTPUT_WRITE && c->output_blend != DRV_OUTPUT_ADD)
     return why = "output_blend must be DRV_OUTPUT_WRITE or DRV_OUTPUT_ADD", DRV_ERR_INVALID_ARG;
+  if (c->specular_envmap_size != 0 &&
+      (!is_pow2(c->specular_envmap_size) || c->specular_envmap_size < 4 || c->specular_envmap_size > 64))
+    return why = "specular_envmap_size must be 0 or a power of two in 4..64", DRV_ERR_INVALID_ARG;
+  if (c->specular_fill_level < 0 || (c->specular_fill_level > 0 && (c->specular_envmap_size == 0 ||
+                                     (1 << c->specular_fill_level) > c->specular_envmap_size)))
+    return why = "specular_fill_level must be 0..log2(specular_envmap_size)", DRV_ERR_INVALID_ARG;
   return DRV_OK;
 }
 
@@ -153,6 +161,14 @@ bool views_ok(const DrvGBufferView* g, const DrvConfig& c) {
          (g->albedo_format == DRV_ALBEDO_F32X3 || g->albedo_format == DRV_ALBEDO_SRGB8) &&
          reinterpret_cast<uintptr_t>(g->depth) % 4 == 0 && reinterpret_cast<uintptr_t>(g->normal) % 4 == 0 &&
          (g->albedo_format == DRV_ALBEDO_SRGB8 || reinterpret_cast<uintptr_t>(g->albedo) % 4 == 0);
+}
+
+// The apply's roughness / metallic input: needed only with specular on.
+bool rough_metal_ok(const DrvGBufferView* g, const DrvConfig& c) {
+  if (c.specular_envmap_size == 0) return true;
+  if (!g->rough_metal) return false;
+  if (g->rough_metal_format == DRV_ROUGH_METAL_RG8) return reinterpret_cast<uintptr_t>(g->rough_metal) % 2 == 0;
+  return g->rough_metal_format == DRV_ROUGH_METAL_F32 && reinterpret_cast<uintptr_t>(g->rough_metal) % 8 == 0;
 }
 
 // The GL 4.5 sRGB decode (section 8.24) of the 256 byte values, evaluated in
@@ -289,6 +305,27 @@ drv_status drv_create(const DrvConfig* cfg, DrvContext** out) {
   if ((e = alloc_pairs(c, std::min<uint64_t>(std::max<uint64_t>((uint64_t)cfg->max_caches * 256u, 1ull << 22),
                                              1ull << 26))) != cudaSuccess)
     return bail(e);
+  if (cfg->specular_envmap_size > 0) {
+    // AllocateCacheData (renderer.cpp:253, 279-287): an atlas of side
+    // 2^ceil(log2(ceil(sqrt(max_caches)) * size)) with log2(size) + 1 levels.
+    const int S = cfg->specular_envmap_size;
+    const uint64_t per_side = (uint64_t)std::ceil(std::sqrt((double)cfg->max_caches));
+    uint64_t side = 1;
+    while (side < per_side * (uint64_t)S) side <<= 1;
+    if (side > 65536) return bail(cudaErrorInvalidValue);
+    c->spec_atlas = (int)side;
+    c->spec_levels = ilog2(S) + 1;
+    uint64_t words = 0;
+    for (int l = 0; l < c->spec_levels; ++l) {
+      c->spec_off[l] = (uint32_t)words;
+      words += (side >> l) * (side >> l);
+    }
+    if (words > 0xFFFFFFFFull) return bail(cudaErrorInvalidValue);
+    if ((e = cudaMalloc(&c->spec_env, words * 4)) != cudaSuccess) return bail(e);
+    uint64_t per_cache = 0;  // the apply's FP16 copy: every level of each cache, 8 bytes a texel
+    for (int l = 0; l < c->spec_levels; ++l) per_cache += (uint64_t)(S >> l) * (S >> l);
+    if ((e = cudaMalloc(&c->spec_half, (size_t)cfg->max_caches * per_cache * 8)) != cudaSuccess) return bail(e);
+  }
   c->box_capacity = 512;
   if ((e = cudaMallocHost(&c->h_boxes, c->box_capacity * sizeof(DrvBox))) != cudaSuccess) return bail(e);
   if ((e = cudaMalloc(&c->d_boxes, c->box_capacity * sizeof(DrvBox))) != cudaSuccess) return bail(e);
@@ -355,6 +392,9 @@ drv_status drv_get_buffers(DrvContext* ctx, DrvBuffers* o) {
     o->n_vpls[l] = ctx->n_vpls[l];
   }
   o->n_lights = ctx->n_lights;
+  for (int l = 0; l < ctx->spec_levels; ++l) o->specular_envmap[l] = ctx->spec_env + ctx->spec_off[l];
+  o->specular_atlas_size = ctx->spec_atlas;
+  o->n_specular_levels = ctx->spec_levels;
   return DRV_OK;
 }
 
@@ -579,6 +619,21 @@ drv_status drv_allocate_caches(DrvContext* ctx, const DrvGBufferView* g, const D
 
 namespace {
 
+// The level-0 specular envmaps of the light stage just issued (pairs: its
+// pair list, or nullptr after the single-launch form).
+drv_status specular_gather(DrvContext* ctx, const drv::LightLaunch& ll, const DrvVolumeInfo* vol,
+                           const DrvPerFrame* frame, const drv::PairList* pairs) {
+  const drv::SpecView sv =
+      drv::make_spec_view(ctx->cfg, ctx->spec_env, ctx->spec_off, ctx->spec_atlas, ctx->spec_half, *frame);
+  ctx->spec_ready = false;  // the mips and the apply's copy are stale until drv_prepare_specular_envmaps
+  drv_status st = cuda_check(ctx, drv::launch_specular_gather(ctx->s(), ctx->cfg, *vol, ll, ctx->counter, ctx->entries,
+                                                              ctx->entry_stride, ctx->light_voxels(), pairs, sv,
+                                                              ctx->num_sms),
+                             "specular envmaps");
+  if (st == DRV_OK) ctx->spec_lit = true;
+  return st;
+}
+
 // The light stage. voxels_ready (drv_frame): an event the voxel build records
 // on another stream; only the kernels that read the voxels wait for it.
 drv_status light_caches(DrvContext* ctx, const DrvSpotLight* lights, int32_t n_lights, const DrvVolumeInfo* vol,
@@ -620,6 +675,7 @@ drv_status light_caches(DrvContext* ctx, const DrvSpotLight* lights, int32_t n_l
                                                             voxels_ready),
                                "light_caches");
     if (events) ctx->lk_recorded = st == DRV_OK;
+    if (st == DRV_OK && ctx->spec_env) st = specular_gather(ctx, ll, vol, frame, &pairs);
     return st;
   }
   if (voxels_ready) DRV_TRY_CUDA(ctx, cudaStreamWaitEvent(ctx->s(), voxels_ready, 0));
@@ -638,9 +694,12 @@ drv_status light_caches(DrvContext* ctx, const DrvSpotLight* lights, int32_t n_l
   }
   const drv::LightScratch scratch{ctx->light_scratch, ctx->light_tickets, ctx->light_tickets + ctx->cfg.max_caches,
                                   drv::kMaxLightChunks};
-  return cuda_check(ctx, drv::launch_light_caches(ctx->s(), ctx->cfg, *vol, ll, ctx->counter, ctx->entries,
-                                                  ctx->entry_stride, ctx->light_voxels(), scratch, ctx->num_sms),
-                    "light_caches");
+  drv_status st = cuda_check(ctx, drv::launch_light_caches(ctx->s(), ctx->cfg, *vol, ll, ctx->counter, ctx->entries,
+                                                           ctx->entry_stride, ctx->light_voxels(), scratch,
+                                                           ctx->num_sms),
+                             "light_caches");
+  if (st == DRV_OK && ctx->spec_env) st = specular_gather(ctx, ll, vol, frame, nullptr);
+  return st;
 }
 
 }  // namespace
@@ -654,11 +713,34 @@ drv_status drv_apply(DrvContext* ctx, const DrvGBufferView* g, const DrvPerFrame
                      float* out_rgb) {
   if (!ctx || !f || !vol || !out_rgb) return DRV_ERR_INVALID_ARG;
   if (!views_ok(g, ctx->cfg)) return fail(ctx, DRV_ERR_INVALID_ARG, "G-buffer view does not match the config");
+  if (!rough_metal_ok(g, ctx->cfg))
+    return fail(ctx, DRV_ERR_INVALID_ARG, "specular needs the G-buffer's roughness / metallic (aligned, known format)");
   if (reinterpret_cast<uintptr_t>(out_rgb) % (ctx->cfg.output_format == DRV_OUTPUT_RGBA16F ? 8 : 4))
     return fail(ctx, DRV_ERR_INVALID_ARG, "misaligned output");
+  drv::SpecView sv{};
+  if (ctx->spec_env) {
+    if (!ctx->spec_ready)
+      return fail(ctx, DRV_ERR_INVALID_ARG, "specular apply needs drv_prepare_specular_envmaps after the light stage");
+    sv = drv::make_spec_view(ctx->cfg, ctx->spec_env, ctx->spec_off, ctx->spec_atlas, ctx->spec_half, *f);
+  }
   return cuda_check(ctx, drv::launch_apply(ctx->s(), ctx->cfg, *vol, *f, *g, ctx->atlas, ctx->entries,
-                                           ctx->entry_stride, ctx->counter, out_rgb, ctx->srgb),
+                                           ctx->entry_stride, ctx->counter, out_rgb, ctx->srgb,
+                                           ctx->spec_env ? &sv : nullptr),
                     "apply");
+}
+
+drv_status drv_prepare_specular_envmaps(DrvContext* ctx) {
+  if (!ctx) return DRV_ERR_INVALID_ARG;
+  if (!ctx->spec_env) return fail(ctx, DRV_ERR_INVALID_ARG, "specular is off (specular_envmap_size 0)");
+  if (!ctx->spec_lit) return fail(ctx, DRV_ERR_INVALID_ARG, "drv_light_caches must run first");
+  const DrvPerFrame none{};
+  const drv::SpecView sv =
+      drv::make_spec_view(ctx->cfg, ctx->spec_env, ctx->spec_off, ctx->spec_atlas, ctx->spec_half, none);
+  drv_status st = cuda_check(ctx, drv::launch_envmap_prepare(ctx->s(), sv, ctx->counter, ctx->cfg.max_caches,
+                                                             ctx->cfg.specular_fill_level, ctx->num_sms),
+                             "specular envmap mips");
+  if (st == DRV_OK) ctx->spec_ready = true;
+  return st;
 }
 
 // Renderer::Draw, DYN_RADIANCE_VOLUME branch (renderer.cpp:539-594), plus the
@@ -669,6 +751,8 @@ drv_status drv_frame(DrvContext* ctx, const DrvScene* scene, const DrvGBufferVie
   if (!ctx || !scene || !g || !f || !vol || (n_lights > 0 && (!lights || !rsms)) || !out_rgb)
     return DRV_ERR_INVALID_ARG;
   if (ctx->cur) return fail(ctx, DRV_ERR_INVALID_ARG, "drv_frame re-entered");
+  if (!views_ok(g, ctx->cfg) || !rough_metal_ok(g, ctx->cfg))
+    return fail(ctx, DRV_ERR_INVALID_ARG, "G-buffer view does not match the config");
   drv_status st;
   // The box upload synchronises when the scene changed: do it on the
   // context's stream, before the fork.
@@ -701,6 +785,7 @@ drv_status drv_frame(DrvContext* ctx, const DrvScene* scene, const DrvGBufferVie
   // Joined by now on success (the voxel readers waited); this also covers an
   // error or a stage that skipped the wait.
   DRV_TRY_CUDA(ctx, cudaStreamWaitEvent(main, ctx->join_ev[1], 0));
+  if (st == DRV_OK && ctx->spec_env) st = drv_prepare_specular_envmaps(ctx);  // renderer.cpp:556-558
   if (st != DRV_OK) return st;
   return drv_apply(ctx, g, f, vol, out_rgb);
 }

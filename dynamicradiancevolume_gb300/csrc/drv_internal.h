@@ -25,6 +25,26 @@ struct RsmChain {
   bool half(int level) const { return level == 0 && half0; }
 };
 
+// The per-cache specular envmap atlas (INDIRECT_SPECULAR) and the scalars of
+// its path.
+struct SpecView {
+  uint32_t* levels;  // all levels, level l at levels + off[l] (R11F_G11F_B10F words)
+  uint32_t off[8];
+  int size;          // SPECULARENVMAP_PERCACHESIZE (power of two)
+  int log2size;
+  int n_levels;      // log2size + 1
+  int atlas;         // atlas side at level 0 (power of two)
+  int per_row;       // caches per atlas row: atlas / size
+  float norm;        // BlinnNormalization(GetBlinnPhongExponentForHemispherePixel(size))
+  float cam[3];      // CameraPosition
+  // The apply's copy of every level, per cache and in FP16 (RGB + 0, 8 bytes
+  // a texel; exact: R11/G11/B10 values are FP16 values): cache c's level l
+  // texel (x, y) at half[c * words + loff[l] + y * (size >> l) + x].
+  uint2* half;
+  uint32_t words;
+  uint32_t loff[8];
+};
+
 // Per-light arguments of the light stage.
 struct LightArgs {
   const void* vpls;  // DrvVPL (FP32 precision) or DrvVPLBF16
@@ -183,6 +203,14 @@ struct Context {
   void* sur_weights = nullptr;
   bool sur_ready = false;
   DrvVolumeInfo last_volume{};  // volume of the last drv_allocate_caches (cache positions refer to it)
+  // Indirect specular: the envmap atlas, all levels in one allocation.
+  uint32_t* spec_env = nullptr;
+  uint32_t spec_off[8] = {};
+  int spec_atlas = 0;
+  int spec_levels = 0;
+  uint2* spec_half = nullptr;  // the apply's per-cache FP16 copy (SpecView::half)
+  bool spec_lit = false;       // a light stage has written the level-0 envmaps
+  bool spec_ready = false;     // the envmaps were prepared after the last light stage
 };
 
 int light_chunks(int total_blocks, int max_chunks);
@@ -228,9 +256,22 @@ cudaError_t launch_light_split(cudaStream_t s, const DrvConfig& cfg, const DrvVo
 cudaError_t launch_bruteforce_rsm(cudaStream_t s, const DrvPerFrame& f, const DrvGBufferView& g,
                                   const float* rough_metal, const LightLaunch& ll, int bf16, float* out_rgb,
                                   const float* srgb);
+// spec: the envmap atlas when specular is on, else nullptr.
 cudaError_t launch_apply(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const DrvPerFrame& f,
                          const DrvGBufferView& g, const uint32_t* atlas, const void* entries, uint32_t entry_stride,
-                         const DrvCacheCounter* counter, float* out_rgb, const float* srgb);
+                         const DrvCacheCounter* counter, float* out_rgb, const float* srgb,
+                         const SpecView* spec = nullptr);
+// Indirect specular (k_specular.cu): the level-0 envmaps of the allocated
+// caches (pairs: the split stage's pair list with its shadowing; nullptr:
+// every shadow block, cones traced here), then their mips and hole fill.
+SpecView make_spec_view(const DrvConfig& cfg, uint32_t* levels, const uint32_t off[8], int atlas, uint2* half,
+                        const DrvPerFrame& f);
+cudaError_t launch_specular_gather(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol,
+                                   const LightLaunch& ll, const DrvCacheCounter* counter, void* entries,
+                                   uint32_t entry_stride, const VoxelInputs& vox, const PairList* pairs,
+                                   const SpecView& sv, int num_sms);
+cudaError_t launch_envmap_prepare(cudaStream_t s, const SpecView& sv, const DrvCacheCounter* counter,
+                                  uint32_t max_caches, int fill, int num_sms);
 
 size_t surrogate_weights_bytes();
 size_t surrogate_train_scratch_floats(int n);

@@ -7,10 +7,19 @@
 // (cacheApply.frag:264-284); here a corner outside the atlas, or whose slot is
 // 0 (never allocated) or 0xFFFFFFFF (locked by a capacity overflow),
 // contributes zero irradiance and its weight is not redistributed.
+//
+// With INDIRECT_SPECULAR (cacheApply.frag:76-116, 145-158) each corner cache
+// also contributes its specular envmap, fetched trilinearly (the sampler is
+// LINEAR/LINEAR/LINEAR, renderer.cpp:1070) at the concentric projection of
+// the cache-local normal and the lod of the pixel's Blinn exponent, and the
+// material splits into diffuse and specular colours by metallic.
 #include <cmath>
+
+#include <cuda_fp16.h>
 
 #include "drv_device.cuh"
 #include "drv_internal.h"
+#include "specular.cuh"
 
 namespace drv {
 namespace {
@@ -36,14 +45,75 @@ struct ApplyParams {
   float* out;  // RGB F32, or RGBA16F (out_half)
   int out_half, out_add;
   CellRecip rc;
+  SpecView spec;             // INDIRECT_SPECULAR only
+  const void* rough_metal;   // drv_rough_metal_format
+  int rm_f32;
 };
 
-// Irradiance of cascade c at wp for normal n: the 8 corner caches weighted
-// trilinearly (SampleCacheIrradiance). Per-axis weights, bounds and atlas
-// offsets are formed once; the 8 atlas words are loaded before any entry so
-// their latencies overlap.
-template <bool BF16, bool SH2>
-__device__ __forceinline__ f3 lighting(const ApplyParams& p, const float wp[3], int c, f3 n, uint32_t n_caches) {
+// Where a pixel reads the corner caches' envmaps. The lookup coordinate and
+// the lod are the pixel's, so the bilinear taps of each level — four texel
+// offsets within a cache's region and their weights (GL 4.5 section 8.14.2,
+// indices clamped to the region: the lookup is clamped half a texel of the
+// coarser level inside it, so the clamp only meets zero weights) — are the
+// same for all eight corner caches and are formed once.
+struct EnvTaps {
+  uint32_t at[4];  // (x0,y0), (x1,y0), (x0,y1), (x1,y1) within a cache's FP16 copy
+  float w[4];
+};
+
+struct EnvLookup {
+  EnvTaps t[2];  // level l0, level l1
+  int l0, l1;
+  float f;       // weight of level l1 (LINEAR mip filtering)
+};
+
+__device__ __forceinline__ EnvTaps env_taps(const SpecView& sv, int l, float u, float v) {
+  const int side = sv.size >> l;
+  const uint32_t stride = (uint32_t)side, base = sv.loff[l];
+  const float x = u * (float)side - 0.5f, y = v * (float)side - 0.5f;
+  const float fx = floorf(x), fy = floorf(y);
+  const float a = x - fx, b = y - fy;
+  const uint32_t x0 = (uint32_t)min(max((int)fx, 0), side - 1), x1 = (uint32_t)min(max((int)fx + 1, 0), side - 1);
+  const uint32_t y0 = (uint32_t)min(max((int)fy, 0), side - 1), y1 = (uint32_t)min(max((int)fy + 1, 0), side - 1);
+  EnvTaps t;
+  t.at[0] = base + y0 * stride + x0;
+  t.at[1] = base + y0 * stride + x1;
+  t.at[2] = base + y1 * stride + x0;
+  t.at[3] = base + y1 * stride + x1;
+  t.w[0] = (1.0f - a) * (1.0f - b);
+  t.w[1] = a * (1.0f - b);
+  t.w[2] = (1.0f - a) * b;
+  t.w[3] = a * b;
+  return t;
+}
+
+// Reads the prepared FP16 copy of cache c (the atlas's values exactly).
+__device__ __forceinline__ f3 env_bilinear(const uint2* half, const EnvTaps& t) {
+  f3 r = mkf3(0.0f, 0.0f, 0.0f);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const uint2 q = __ldg(half + t.at[k]);
+    const float2 rg = __half22float2(*reinterpret_cast<const __half2*>(&q.x));
+    const float b = __low2float(*reinterpret_cast<const __half2*>(&q.y));
+    r = mkf3(r.x + t.w[k] * rg.x, r.y + t.w[k] * rg.y, r.z + t.w[k] * b);
+  }
+  return r;
+}
+
+// textureLod with LINEAR mip filtering: the two levels around the lod.
+__device__ __forceinline__ f3 env_sample(const SpecView& sv, uint32_t c, const EnvLookup& q) {
+  const uint2* half = sv.half + (size_t)c * sv.words;
+  f3 r = env_bilinear(half, q.t[0]);
+  if (q.f > 0.0f) {
+    const f3 r1 = env_bilinear(half, q.t[1]);
+    r = mkf3(r.x + (r1.x - r.x) * q.f, r.y + (r1.y - r.y) * q.f, r.z + (r1.z - r.z) * q.f);
+  }
+  return r;
+}
+
+template <bool BF16, bool SH2, bool SPEC>
+__device__ __forceinline__ f3 lighting(const ApplyParams& p, const float wp[3], int c, f3 n, uint32_t n_caches,
+                                       const EnvLookup& q, f3& spec) {
   const DrvCascade& k = p.vol.cascades[c];
   float wgt[3][2];
   int a0[3];
@@ -120,6 +190,12 @@ __device__ __forceinline__ f3 lighting(const ApplyParams& p, const float wp[3], 
     irr.x += fmaxf(er, 0.0f) * w;
     irr.y += fmaxf(eg, 0.0f) * w;
     irr.z += fmaxf(eb, 0.0f) * w;
+    if (SPEC && live) {
+      const f3 e = env_sample(p.spec, addr - 1u, q);
+      spec.x += e.x * w;
+      spec.y += e.y * w;
+      spec.z += e.z * w;
+    }
   }
   return irr;
 }
@@ -153,7 +229,7 @@ __device__ __forceinline__ void store_output(const ApplyParams& p, size_t i, f3 
   }
 }
 
-template <bool BF16, bool SH2>
+template <bool BF16, bool SH2, bool SPEC>
 __global__ void __launch_bounds__(256) apply_kernel(ApplyParams p) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
   if (x >= p.w || y >= p.h) return;
@@ -175,18 +251,60 @@ __global__ void __launch_bounds__(256) apply_kernel(ApplyParams p) {
   }
   const float inv_pi = 1.0f / DRV_SHADER_PI;
   const f3 a = load_albedo(p.albedo, p.albedo_format, p.srgb, i);
-  const f3 alb = mkf3(a.x * inv_pi, a.y * inv_pi, a.z * inv_pi);
+  f3 alb = mkf3(a.x * inv_pi, a.y * inv_pi, a.z * inv_pi);
   const uint32_t n_caches = min((uint32_t)max(p.counter->total_light_cache_count, 0), p.max_caches);
   float wp[3];
   reconstruct_world(p.frame, x, y, p.w, p.h, d, wp);
   const int c = select_cascade(p.vol, p.n_cascades, wp);
-  f3 irr = lighting<BF16, SH2>(p, wp, c, n, n_caches);
+  EnvLookup q{};
+  f3 spec_col = mkf3(0.0f, 0.0f, 0.0f);
+  if (SPEC) {
+    float rough, metal;
+    if (p.rm_f32) {
+      const float2 rm = __ldcs(reinterpret_cast<const float2*>(p.rough_metal) + i);
+      rough = rm.x;
+      metal = rm.y;
+    } else {
+      const unsigned short rm = __ldcs(reinterpret_cast<const unsigned short*>(p.rough_metal) + i);
+      rough = (float)(rm & 0xFFu) / 255.0f;
+      metal = (float)(rm >> 8) / 255.0f;
+    }
+    // ComputeMaterialColors (lightingfunctions.glsl:41-49): mix(x, y, a) = x (1 - a) + y a.
+    alb = mkf3((a.x * (1.0f - metal) + 0.02f * metal) * inv_pi, (a.y * (1.0f - metal) + 0.02f * metal) * inv_pi,
+               (a.z * (1.0f - metal) + 0.02f * metal) * inv_pi);
+    spec_col = mkf3(0.04f * (1.0f - metal) + a.x * metal, 0.04f * (1.0f - metal) + a.y * metal,
+                    0.04f * (1.0f - metal) + a.z * metal);
+    // RoughnessToBlinnExponent, GetHemisphereLodForBlinnPhongExponent and
+    // the lookup clamp of cacheApply.frag:150-157.
+    const float rsq = rough * rough;
+    const float blinn = 2.0f / (rsq * rsq + 0.0005f);
+    const float S = (float)p.spec.size;
+    const float lod = fmaxf(0.0f, log2f(S * S / (1.0f + blinn)) * 0.5f);
+    const float half_px = 0.5f / (exp2f(-ceilf(lod)) * S);
+    const LocalFrame fr = local_view_space(p.frame.camera_position, wp[0], wp[1], wp[2]);
+    float u, v;
+    hemi_projection(to_local(fr, n), u, v);
+    u = fminf(fmaxf(u, half_px), 1.0f - half_px);
+    v = fminf(fmaxf(v, half_px), 1.0f - half_px);
+    const float fl = fminf(floorf(lod), (float)(p.spec.n_levels - 1));
+    q.l0 = (int)fl;
+    q.l1 = min(q.l0 + 1, p.spec.n_levels - 1);
+    q.f = q.l1 > q.l0 ? lod - fl : 0.0f;
+    q.t[0] = env_taps(p.spec, q.l0, u, v);
+    if (q.f > 0.0f) q.t[1] = env_taps(p.spec, q.l1, u, v);
+  }
+  f3 spec = mkf3(0.0f, 0.0f, 0.0f);
+  f3 irr = lighting<BF16, SH2, SPEC>(p, wp, c, n, n_caches, q, spec);
   f3 col = mkf3(irr.x * alb.x, irr.y * alb.y, irr.z * alb.z);
+  if (SPEC) col = mkf3(col.x + spec.x * spec_col.x, col.y + spec.y * spec_col.y, col.z + spec.z * spec_col.z);
   if (p.transitions) {
     const float t = cascade_transition(p.vol, p.rc, c, wp);
     if (t > 0.0f && c < p.n_cascades - 1) {
-      f3 irr2 = lighting<BF16, SH2>(p, wp, c + 1, n, n_caches);
+      f3 spec2 = mkf3(0.0f, 0.0f, 0.0f);
+      f3 irr2 = lighting<BF16, SH2, SPEC>(p, wp, c + 1, n, n_caches, q, spec2);
       f3 col2 = mkf3(irr2.x * alb.x, irr2.y * alb.y, irr2.z * alb.z);
+      if (SPEC)
+        col2 = mkf3(col2.x + spec2.x * spec_col.x, col2.y + spec2.y * spec_col.y, col2.z + spec2.z * spec_col.z);
       col = col * (1.0f - t) + col2 * t;  // mix(), cacheApply.frag:359
     }
   }
@@ -197,8 +315,8 @@ __global__ void __launch_bounds__(256) apply_kernel(ApplyParams p) {
 
 cudaError_t launch_apply(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const DrvPerFrame& f,
                          const DrvGBufferView& g, const uint32_t* atlas, const void* entries, uint32_t entry_stride,
-                         const DrvCacheCounter* counter, float* out_rgb, const float* srgb) {
-  ApplyParams p;
+                         const DrvCacheCounter* counter, float* out_rgb, const float* srgb, const SpecView* spec) {
+  ApplyParams p{};
   p.rc = make_cell_recip(vol);
   p.vol = vol;
   p.frame = f;
@@ -230,10 +348,24 @@ cudaError_t launch_apply(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeIn
   p.out_half = cfg.output_format == DRV_OUTPUT_RGBA16F;
   p.out_add = cfg.output_blend == DRV_OUTPUT_ADD;
   dim3 block(16, 16), grid((g.width + 15) / 16, (g.height + 15) / 16);
+  if (spec) {
+    p.spec = *spec;
+    p.rough_metal = g.rough_metal;
+    p.rm_f32 = g.rough_metal_format == DRV_ROUGH_METAL_F32;
+    if (p.bf16)
+      p.sh2 ? apply_kernel<true, true, true><<<grid, block, 0, s>>>(p)
+            : apply_kernel<true, false, true><<<grid, block, 0, s>>>(p);
+    else
+      p.sh2 ? apply_kernel<false, true, true><<<grid, block, 0, s>>>(p)
+            : apply_kernel<false, false, true><<<grid, block, 0, s>>>(p);
+    return cudaGetLastError();
+  }
   if (p.bf16)
-    p.sh2 ? apply_kernel<true, true><<<grid, block, 0, s>>>(p) : apply_kernel<true, false><<<grid, block, 0, s>>>(p);
+    p.sh2 ? apply_kernel<true, true, false><<<grid, block, 0, s>>>(p)
+          : apply_kernel<true, false, false><<<grid, block, 0, s>>>(p);
   else
-    p.sh2 ? apply_kernel<false, true><<<grid, block, 0, s>>>(p) : apply_kernel<false, false><<<grid, block, 0, s>>>(p);
+    p.sh2 ? apply_kernel<false, true, false><<<grid, block, 0, s>>>(p)
+          : apply_kernel<false, false, false><<<grid, block, 0, s>>>(p);
   return cudaGetLastError();
 }
 

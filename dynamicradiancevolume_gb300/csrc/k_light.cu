@@ -73,6 +73,7 @@ StageParams make_stage_params(const DrvConfig& cfg, const DrvVolumeInfo& vol, co
   p.ev[2] = (float)std::sqrt(15.0 / (4.0 * kPi));
   p.ev[3] = (float)std::sqrt(5.0 / (16.0 * kPi));
   p.ev[4] = (float)std::sqrt(15.0 / (16.0 * kPi));
+  p.spec = cfg.specular_envmap_size > 0;
   return p;
 }
 
@@ -89,27 +90,6 @@ __device__ __forceinline__ void add_to_entry(float* entry, int k, float v) {
   }
 }
 
-// True when some VPL of shadow block b may contribute to the cache (a
-// superset of the blocks the gather's exact test keeps, see may_contribute).
-template <bool BF16>
-__device__ __forceinline__ bool block_live(const StageParams& p, int b, float cx, float cy, float cz) {
-  const int l = block_light(p, b);
-  const LightArgs& la = p.ll.lights[l];
-  const int lb = b - p.block_base[l];
-  for (int j = 0; j < la.interval; ++j)
-    if (may_contribute(load_vpl<BF16>(la.vpls, lb * la.interval + j), cx, cy, cz)) return true;
-  return false;
-}
-
-// Shadowing of block b seen from the cache (the reference's cone).
-__device__ __forceinline__ float block_cone(const StageParams& p, int b, float cx, float cy, float cz) {
-  const int l = block_light(p, b);
-  const float4 c = __ldg(reinterpret_cast<const float4*>(p.ll.lights[l].cones) + (b - p.block_base[l]));
-  const float vx = (cx - p.vol_min[0]) * p.inv_extent, vy = (cy - p.vol_min[1]) * p.inv_extent,
-              vz = (cz - p.vol_min[2]) * p.inv_extent;
-  return cone_shadow(p.vox, p.voxel_size, p.max_steps, cx, cy, cz, vx, vy, vz, c.x, c.y, c.z, c.w);
-}
-
 // SH gather of the contributing VPLs of block b with the given shadowing
 // into acc/comp (stride 1: register arrays once inlined).
 template <int NK, bool BF16, bool KAHAN>
@@ -121,7 +101,7 @@ __device__ __forceinline__ void gather_block(const StageParams& p, float* acc, f
   for (int j = 0; j < la.interval; ++j) {
     const VplData v = load_vpl<BF16>(la.vpls, lb * la.interval + j);
     const Transfer t = transfer(v, cx, cy, cz);
-    if (contributes(v, t)) accumulate<NK, KAHAN>(p.ev, acc, comp, 1, v, t, shadowing);
+    if (contributes(v, t) && flux_ok(p, v)) accumulate<NK, KAHAN>(p.ev, acc, comp, 1, v, t, shadowing);
   }
 }
 
@@ -456,7 +436,7 @@ __global__ void __launch_bounds__(kThreads, 8) light_kernel(FusedParams fp) {
       for (int j = 0; j < la.interval; ++j) {
         const VplData v = load_vpl<BF16>(la.vpls, lb * la.interval + j);
         const Transfer t = transfer(v, cx, cy, cz);
-        if (contributes(v, t)) accumulate<NK, KAHAN>(p.ev, acc, comp, kThreads, v, t, s);
+        if (contributes(v, t) && flux_ok(p, v)) accumulate<NK, KAHAN>(p.ev, acc, comp, kThreads, v, t, s);
       }
     };
     const int b0 = chunk * fp.chunk_blocks, b1 = min(b0 + fp.chunk_blocks, p.total_blocks);
@@ -471,7 +451,7 @@ __global__ void __launch_bounds__(kThreads, 8) light_kernel(FusedParams fp) {
           const int l = block_light(p, b);
           const VplData v = load_vpl<BF16>(p.ll.lights[l].vpls, b - p.block_base[l]);
           const Transfer t = transfer(v, cx, cy, cz);
-          if (contributes(v, t)) accumulate<NK, KAHAN>(p.ev, acc, comp, kThreads, v, t, 1.0f);
+          if (contributes(v, t) && flux_ok(p, v)) accumulate<NK, KAHAN>(p.ev, acc, comp, kThreads, v, t, 1.0f);
         }
       }
       const uint32_t mask = __ballot_sync(0xffffffffu, live);

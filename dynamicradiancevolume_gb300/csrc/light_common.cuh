@@ -32,6 +32,7 @@ struct StageParams {
   float* entries;
   int stride_floats;
   float ev[5];  // ShEvaFactor0, 1, 2n2_p1_n1, 20, 2p2 (renderer.cpp:302-306)
+  int spec;     // INDIRECT_SPECULAR: VPLs with a flux sum below 0.001 are skipped
 };
 
 // Host: the device view of a voxel pyramid of resolution cfg.voxel_res.
@@ -199,6 +200,12 @@ __device__ __forceinline__ void retire_cta(uint32_t* work) {
   }
 }
 
+// With INDIRECT_SPECULAR the reference skips a VPL whose flux sum is below
+// 0.001 (cacheLightingRSM.comp:240-241), for the SH as well.
+__device__ __forceinline__ bool flux_ok(const StageParams& p, const VplData& v) {
+  return !p.spec || !(__fadd_rn(__fadd_rn(v.fr, v.fg), v.fb) < 0.001f);
+}
+
 // A superset of `contributes` that needs no normalisation or division:
 // positive flux and -(n . t) > -1e-6 max|t_i| with t = VPL - cache. The exact
 // test's sign of -(n . t / |t|) can differ from the sign of -(n . t) only
@@ -209,6 +216,27 @@ __device__ __forceinline__ bool may_contribute(const VplData& v, float cx, float
   const float facing = -(v.nx * tx + v.ny * ty + v.nz * tz);
   const float scale = fmaxf(fmaxf(fabsf(tx), fabsf(ty)), fabsf(tz));
   return facing > -1e-6f * scale && (v.fr > 0.0f || v.fg > 0.0f || v.fb > 0.0f);
+}
+
+// True when some VPL of shadow block b may contribute to the cache (a
+// superset of the blocks the gather's exact test keeps, see may_contribute).
+template <bool BF16>
+__device__ __forceinline__ bool block_live(const StageParams& p, int b, float cx, float cy, float cz) {
+  const int l = block_light(p, b);
+  const LightArgs& la = p.ll.lights[l];
+  const int lb = b - p.block_base[l];
+  for (int j = 0; j < la.interval; ++j)
+    if (may_contribute(load_vpl<BF16>(la.vpls, lb * la.interval + j), cx, cy, cz)) return true;
+  return false;
+}
+
+// Shadowing of block b seen from the cache (the reference's cone).
+__device__ __forceinline__ float block_cone(const StageParams& p, int b, float cx, float cy, float cz) {
+  const int l = block_light(p, b);
+  const float4 c = __ldg(reinterpret_cast<const float4*>(p.ll.lights[l].cones) + (b - p.block_base[l]));
+  const float vx = (cx - p.vol_min[0]) * p.inv_extent, vy = (cy - p.vol_min[1]) * p.inv_extent,
+              vz = (cz - p.vol_min[2]) * p.inv_extent;
+  return cone_shadow(p.vox, p.voxel_size, p.max_steps, cx, cy, cz, vx, vy, vz, c.x, c.y, c.z, c.w);
 }
 
 // SH gather of one VPL, cacheLightingRSM.comp:255-278. acc (and comp with

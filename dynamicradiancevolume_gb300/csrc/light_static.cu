@@ -72,6 +72,7 @@ extern "C" drv_status drv_light_caches_static_scratch(const DrvConfig* cfg, cons
   if (n_lights > 0 && (!vpls || !n_vpls || !intervals)) return DRV_ERR_INVALID_ARG;
   if (cfg->indirect_shadow && (!cones || !voxel_corners || !voxel_mips)) return DRV_ERR_INVALID_ARG;
   if (cfg->sh_order != 1 && cfg->sh_order != 2) return DRV_ERR_INVALID_ARG;
+  if (cfg->specular_envmap_size != 0) return DRV_ERR_INVALID_ARG;  // the envmap atlas belongs to a context
   if (cfg->voxel_res < 32 || cfg->voxel_res > 1024 || (cfg->voxel_res & (cfg->voxel_res - 1)))
     return DRV_ERR_INVALID_ARG;
   if (cfg->max_caches > DRV_STATIC_SCRATCH_MAX_CACHES) return DRV_ERR_CAPACITY;

@@ -40,6 +40,8 @@ class Workload:
     albedo: tuple = (0.2, 0.9)
     precision: int = abi.PRECISION_FP32
     visibility: int = abi.VISIBILITY_CONE
+    specular_envmap_size: int = 0  # INDIRECT_SPECULAR off; else the per-cache envmap side (16 in the reference)
+    specular_fill_level: int = 0
 
     @property
     def n_vpls(self) -> int:
@@ -84,6 +86,8 @@ def make_config(w: Workload) -> abi.DrvConfig:
     cfg.max_rsm_resolution = w.rsm_resolution
     cfg.precision = w.precision
     cfg.visibility = w.visibility
+    cfg.specular_envmap_size = w.specular_envmap_size
+    cfg.specular_fill_level = w.specular_fill_level
     return cfg
 
 
@@ -153,10 +157,13 @@ class Pipeline:
         self.rsm_flux = [torch.zeros((R, R, 3), dtype=torch.float32, device=dev) for _ in range(w.n_lights)]
         self.rsm_normal = [torch.zeros((R, R, 2), dtype=torch.int16, device=dev) for _ in range(w.n_lights)]
         self.rsm_dls = [torch.zeros((R, R, 2), dtype=torch.float32, device=dev) for _ in range(w.n_lights)]
+        # GBuffer_RoughnessMetalic (RG8 unorm), read by the specular apply.
+        self.rough_metal = torch.zeros((H, W, 2), dtype=torch.uint8, device=dev)
         self.normal_format = normal_format
         self.gview = abi.DrvGBufferView(W, H, self.depth.data_ptr(),
                                         (self.normal16 if normal_format == abi.NORMAL_RG16I else self.normal32).data_ptr(),
-                                        normal_format, self.albedo.data_ptr(), abi.ALBEDO_F32X3)
+                                        normal_format, self.albedo.data_ptr(), abi.ALBEDO_F32X3,
+                                        self.rough_metal.data_ptr(), abi.ROUGH_METAL_RG8)
         self.rsm_views = (abi.DrvRSMView * w.n_lights)()
         for l in range(w.n_lights):
             self.rsm_views[l] = abi.DrvRSMView(R, self.rsm_flux[l].data_ptr(), self.rsm_normal[l].data_ptr(),
@@ -347,6 +354,26 @@ class Pipeline:
         b = self.buffers()
         n = w.n_cascades * w.cav_res ** 3
         return self._dev_tensor(b.cav_atlas, n, self.torch.int32).view(w.cav_res, w.cav_res, w.n_cascades * w.cav_res)
+
+    def prepare_specular(self):
+        self._c(self.lib.drv_prepare_specular_envmaps(self.ctx))
+
+    def read_specular(self, n_caches: int):
+        """The allocated caches' specular envmaps as numpy uint32 words
+        [n_caches, sum of levels], each cache's levels row-major one after the
+        other (the oracle's per-cache layout), gathered from the atlas."""
+        import numpy as np
+        b = self.buffers()
+        S, T, L = self.hf.config.specular_envmap_size, b.specular_atlas_size, b.n_specular_levels
+        per_row = T // S
+        out = []
+        for l in range(L):
+            side, t = S >> l, T >> l
+            lv = self._dev_tensor(b.specular_envmap[l], t * t, self.torch.int32).cpu().numpy().view(np.uint32)
+            lv = lv.reshape(t // side, side, t // side, side).transpose(0, 2, 1, 3).reshape(-1, side * side)
+            out.append(lv[:n_caches])  # atlas cell (row, col) = cache row * per_row + col
+        assert per_row == T // S
+        return np.concatenate(out, axis=1)
 
     def read_voxel_bits(self):
         N = self.hf.workload.voxel_res

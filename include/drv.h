@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define DRV_ABI_VERSION 3
+#define DRV_ABI_VERSION 4
 #define DRV_MAX_CASCADES 4   /* MAX_NUM_ADDRESS_VOLUME_CASCADES, globalubos.glsl:43 */
 #define DRV_MAX_LIGHTS 16    /* maxExpectedLights, renderer.cpp:80 */
 #define DRV_LIGHTING_THREADS_PER_GROUP 64 /* lightcache.glsl:95 */
@@ -95,6 +95,14 @@ typedef enum drv_albedo_format {
   DRV_ALBEDO_SRGB8 = 1
 } drv_albedo_format;
 
+/* Roughness / metallic per pixel (GBuffer_RoughnessMetalic): the
+ * reference's RG8 unorm target (renderer.cpp:469, 2 bytes per pixel, read as
+ * byte / 255) or RG F32. */
+typedef enum drv_rough_metal_format {
+  DRV_ROUGH_METAL_RG8 = 0,
+  DRV_ROUGH_METAL_F32 = 1
+} drv_rough_metal_format;
+
 /* Compile-time specialisations and setters of the reference's Renderer
  * (renderer.hpp:63-142, renderer.cpp:197-246). */
 typedef struct DrvConfig {
@@ -116,6 +124,15 @@ typedef struct DrvConfig {
   int32_t max_rsm_resolution;       /* largest RSMRenderResolution any light will use */
   int32_t output_format;            /* drv_output_format of drv_apply / drv_frame's out_rgb */
   int32_t output_blend;             /* drv_output_blend */
+  /* INDIRECT_SPECULAR (renderer.cpp:200-206): 0 = off (the reference's
+   * default, m_indirectSpecular false); otherwise SPECULARENVMAP_PERCACHESIZE,
+   * the per-cache envmap resolution, a power of two in 4..64 (16 in the
+   * reference). With it on, the light stage also fills a per-cache specular
+   * envmap, skips VPLs whose flux sum is below 0.001 (for the SH too, as
+   * cacheLightingRSM.comp:240-241 does), and the apply adds the specular
+   * term with the G-buffer's roughness / metallic. */
+  int32_t specular_envmap_size;
+  int32_t specular_fill_level;      /* m_specularEnvmapMaxFillHolesLevel, 0..log2(size) (0 in the reference) */
 } DrvConfig;
 
 /* The apply's target: RGB F32 (width*height*3 floats), or the reference's
@@ -237,6 +254,8 @@ typedef struct DrvGBufferView {
   int32_t normal_format;
   const void* albedo;               /* drv_albedo_format */
   int32_t albedo_format;
+  const void* rough_metal;          /* drv_rough_metal_format; read only with specular_envmap_size > 0 */
+  int32_t rough_metal_format;
 } DrvGBufferView;
 
 /* Writable G-buffer for the ray-cast producer. */
@@ -331,6 +350,16 @@ typedef struct DrvBuffers {
                                        2x2x2 bricks of 8 records; FP32 precision: u16 k = texel * 8^l (levels 1..5),
                                        BF16 precision: the FP16 texels (every level) */
   int32_t n_record_levels;
+  /* The per-cache specular envmap atlas (m_specularEnvmap, renderer.cpp:253-
+   * 287): n_specular_levels levels of specular_atlas_size >> level texels
+   * square, R11F_G11F_B10F packed in 32 bits (R bits 0-10, G 11-21, B 22-31),
+   * rows contiguous; cache i's region at each level is the square of side
+   * specular_envmap_size >> level at column i % n, row i / n (n =
+   * specular_atlas_size / specular_envmap_size). Only allocated caches'
+   * regions are written; NULL when specular is off. */
+  uint32_t* specular_envmap[8];
+  int32_t specular_atlas_size;
+  int32_t n_specular_levels;
 } DrvBuffers;
 
 typedef struct DrvContext DrvContext;
@@ -538,6 +567,15 @@ enum {
  * DRV_ERR_INVALID_ARG when no such stage ran. */
 drv_status drv_get_light_kernel_ms(DrvContext* ctx, float ms[DRV_LK_COUNT]);
 
+/* ---- indirect specular ---------------------------------------------------
+ * Renderer::PrepareSpecularEnvmaps (renderer.cpp:994-1043): the mip levels
+ * of every allocated cache's envmap (specularenvmap_mipmap.frag: each texel
+ * the mean of the 2x2 texels below) and, with specular_fill_level > 0, the
+ * hole fill from that level down to 1 (specularenvmap_fillholes.frag). Runs
+ * after drv_light_caches (drv_frame calls it); DRV_ERR_INVALID_ARG when
+ * specular is off. */
+drv_status drv_prepare_specular_envmaps(DrvContext* ctx);
+
 /* ---- brute-force RSM gather and image dumps --------------------------------
  * Renderer::ApplyRSMsBruteForce (renderer.cpp:851-871, bruteforcersm.frag):
  * per pixel, the unshadowed sum over every VAL (the context's extracted
@@ -602,6 +640,8 @@ drv_status drv_batch_destroy(DrvBatch* batch);
  * and the output (the cache entries: positions read, SH accumulated with +=)
  * as device pointers, and the stream to run on.
  *  - max_caches above DRV_STATIC_SCRATCH_MAX_CACHES returns DRV_ERR_CAPACITY;
+ *  - specular_envmap_size > 0 returns DRV_ERR_INVALID_ARG (the envmap atlas
+ *    belongs to a context);
  *  - the first call on a device looks the array up on that device; make it
  *    before any stream capture;
  *  - all calls share the array (it keeps the last call's contents; each call

@@ -1096,16 +1096,112 @@ void orc_light_caches(const DrvConfig* cfg, const DrvVolumeInfo* vol, int n_cach
                       int n_lights, const DrvSpotLight* lights, const double* const* vpls,
                       const double* const* cones, const int* n_vpls, const uint32_t* bits, const double* mips,
                       double* sh_out, int n_threads) {
+  orc_light_caches_specular(cfg, vol, n_caches, positions, nullptr, n_lights, lights, vpls, cones, n_vpls, bits, mips,
+                            sh_out, nullptr, n_threads);
+}
+
+namespace {
+// ComputeLocalViewSpace (lightcache.glsl:98-106).
+void local_view_space(d3 cam, d3 p, d3& x, d3& y, d3& z) {
+  z = normalize(cam - p);
+  x = normalize(mk(z.z, 0.0, -z.x));
+  y = cross(z, x);
+}
+
+// HemisphericalProjection, concentric square map (utils.glsl:103-170).
+void hemi_projection(d3 d, double& u, double& v) {
+  const double r = std::sqrt(std::max(1.0 - d.z, 0.0)) * 0.5;
+  double phi = std::atan2(d.y, d.x) * (4.0 / kShaderPi);
+  if (phi < -1.0) phi += 8.0;
+  double px, py;
+  if (phi < 3.0) {
+    if (phi < 1.0) {
+      px = r;
+      py = phi * r;
+    } else {
+      px = -(phi - 2.0) * r;
+      py = r;
+    }
+  } else if (phi < 5.0) {
+    px = -r;
+    py = -(phi - 4.0) * r;
+  } else {
+    px = (phi - 6.0) * r;
+    py = -r;
+  }
+  u = px + 0.5;
+  v = py + 0.5;
+}
+
+// GL unsigned 11/10-bit float (5-bit exponent, bias 15, mbits of mantissa)
+// from a double: negative -> 0, NaN -> NaN, +inf -> inf, above the largest
+// finite value -> that value, else the nearest value (ties to even).
+uint32_t encode_ufloat(double x, int mbits) {
+  const uint32_t mmask = (1u << mbits) - 1u;
+  if (std::isnan(x)) return (31u << mbits) | 1u;
+  if (!(x > 0.0)) return 0u;
+  if (std::isinf(x)) return 31u << mbits;
+  int e;
+  std::frexp(x, &e);  // x = m 2^e, m in [0.5, 1)
+  int E = e + 14;     // biased exponent of a normal result
+  if (E < 1) return (uint32_t)std::nearbyint(std::ldexp(x, 14 + mbits));  // subnormal (2^mbits: smallest normal)
+  double q = std::nearbyint(std::ldexp(x, mbits - (e - 1)));               // in [2^mbits, 2^(mbits+1)]
+  if (q >= (double)(2u << mbits)) {
+    q = (double)(1u << mbits);
+    ++E;
+  }
+  if (E > 30) return (30u << mbits) | mmask;
+  return ((uint32_t)E << mbits) | ((uint32_t)q - (1u << mbits));
+}
+
+double decode_ufloat(uint32_t v, int mbits) {
+  const uint32_t e = v >> mbits, m = v & ((1u << mbits) - 1u);
+  if (e == 0) return std::ldexp((double)m, -14 - mbits);
+  if (e == 31) return m ? std::nan("") : INFINITY;
+  return std::ldexp(1.0 + (double)m / (double)(1u << mbits), (int)e - 15);
+}
+}  // namespace
+
+uint32_t orc_encode_r11g11b10(const double rgb[3]) {
+  return encode_ufloat(rgb[0], 6) | encode_ufloat(rgb[1], 6) << 11 | encode_ufloat(rgb[2], 5) << 22;
+}
+
+void orc_encode_r11g11b10_n(const double* rgb, int64_t n, uint32_t* out) {
+  for (int64_t i = 0; i < n; ++i) out[i] = orc_encode_r11g11b10(rgb + 3 * i);
+}
+
+void orc_decode_r11g11b10(uint32_t v, double rgb[3]) {
+  rgb[0] = decode_ufloat(v & 0x7FFu, 6);
+  rgb[1] = decode_ufloat((v >> 11) & 0x7FFu, 6);
+  rgb[2] = decode_ufloat(v >> 22, 5);
+}
+
+void orc_light_caches_specular(const DrvConfig* cfg, const DrvVolumeInfo* vol, int n_caches, const float* positions,
+                               const float* cam, int n_lights, const DrvSpotLight* lights,
+                               const double* const* vpls, const double* const* cones, const int* n_vpls,
+                               const uint32_t* bits, const double* mips, double* sh_out, double* env_out,
+                               int n_threads) {
   set_threads(n_threads);
   double cl[5], ev[5];
   orc_sh_constants(DRV_SH2_SIGN_REFERENCE, cl, ev);
   const bool sh2 = cfg->sh_order == 2;
+  const int S = cfg->specular_envmap_size;
+  const bool spec = S > 0;
+  const bool env = spec && env_out && cam;
+  // BlinnNormalization(GetBlinnPhongExponentForHemispherePixel(S)) (utils.glsl:180-190,
+  // lightingfunctions.glsl:37-40).
+  const double norm = ((double)S * S - 1.0 + 8.0) / (8.0 * kShaderPi);
 #pragma omp parallel for schedule(dynamic, 16)
   for (int c = 0; c < n_caches; ++c) {
     double acc[27];
     for (int k = 0; k < 27; ++k) acc[k] = 0.0;
     d3 wp = ld3(positions + 3 * c);
     double cp[3] = {wp.x, wp.y, wp.z};
+    double* E = env ? env_out + (size_t)c * S * S * 3 : nullptr;
+    if (E)
+      for (int k = 0; k < S * S * 3; ++k) E[k] = 0.0;
+    d3 fx{}, fy{}, fz{};
+    if (env) local_view_space(ld3(cam), wp, fx, fy, fz);
     for (int l = 0; l < n_lights; ++l) {
       const double* V = vpls[l];
       const double* C = cones[l];
@@ -1117,11 +1213,29 @@ void orc_light_caches(const DrvConfig* cfg, const DrvVolumeInfo* vol, int n_cach
           shadowing = orc_cone_shadow(vol, cfg->voxel_res, bits, mips, cp, cone, cone[3], cfg->max_cone_steps);
         }
         const double* v = V + 10 * j;
+        // INDIRECT_SPECULAR skips VPLs of little flux (cacheLightingRSM.comp:240-241)
+        if (spec && v[0] + v[1] + v[2] < 0.001) continue;
         d3 to = mk(v[4], v[5], v[6]) - wp;
         double d2 = dot(to, to);
         to = to * (1.0 / std::sqrt(d2));
         double f = saturate(-dot(mk(v[7], v[8], v[9]), to)) * shadowing;
         double s = f / (d2 + v[3]);
+        if (E && s > 0.0) {
+          // cacheLightingRSM.comp:310-335: the reflected radiance into the
+          // texel of the cache-local half vector (texel clamped to S - 1).
+          const d3 tl = mk(dot(to, fx), dot(to, fy), dot(to, fz));
+          d3 h = mk(tl.x, tl.y, tl.z + 1.0);
+          const double hl = length(h);
+          if (hl > 0.0) {
+            h = h * (1.0 / hl);
+            double pu, pv;
+            hemi_projection(h, pu, pv);
+            const int tx = std::min(std::max((int)(pu * S + 0.5), 0), S - 1);
+            const int ty = std::min(std::max((int)(pv * S + 0.5), 0), S - 1);
+            const double k = s * saturate(dot(h, tl));
+            for (int ch = 0; ch < 3; ++ch) E[3 * (ty * S + tx) + ch] += v[ch] * k;
+          }
+        }
         for (int ch = 0; ch < 3; ++ch) {
           double L = v[ch] * s;
           acc[0 * 3 + ch] += ev[0] * L;
@@ -1139,6 +1253,63 @@ void orc_light_caches(const DrvConfig* cfg, const DrvVolumeInfo* vol, int n_cach
       }
     }
     for (int k = 0; k < 27; ++k) sh_out[(size_t)c * 27 + k] = acc[k];
+    if (E)
+      for (int k = 0; k < S * S * 3; ++k) E[k] *= norm;
+  }
+}
+
+// Renderer::PrepareSpecularEnvmaps (renderer.cpp:994-1043) on per-cache
+// envmaps (cache c's levels at c * words, level l at the sum of the sizes of
+// the levels above it, (S >> l)^2 texels row-major): mips
+// (specularenvmap_mipmap.frag, the mean of the 2x2 texels below), then the
+// hole fill from `fill` down to 1 (specularenvmap_fillholes.frag); every
+// texel stored rounded to R11F_G11F_B10F.
+void orc_specular_prepare(int S, int fill, int n_caches, uint32_t* env, int n_threads) {
+  set_threads(n_threads);
+  int L = 0;
+  while ((1 << L) <= S) ++L;  // log2(S) + 1 levels
+  std::vector<int> off(L + 1, 0);
+  for (int l = 1; l <= L; ++l) off[l] = off[l - 1] + (S >> (l - 1)) * (S >> (l - 1));
+  const int words = off[L];
+#pragma omp parallel for schedule(static)
+  for (int c = 0; c < n_caches; ++c) {
+    uint32_t* e = env + (size_t)c * words;
+    for (int l = 1; l < L; ++l) {
+      const int side = S >> l, below = 2 * side;
+      for (int y = 0; y < side; ++y)
+        for (int x = 0; x < side; ++x) {
+          double a[3], b[3], cc[3], d[3], m[3];
+          orc_decode_r11g11b10(e[off[l - 1] + (2 * y) * below + 2 * x], a);
+          orc_decode_r11g11b10(e[off[l - 1] + (2 * y) * below + 2 * x + 1], b);
+          orc_decode_r11g11b10(e[off[l - 1] + (2 * y + 1) * below + 2 * x], cc);
+          orc_decode_r11g11b10(e[off[l - 1] + (2 * y + 1) * below + 2 * x + 1], d);
+          for (int ch = 0; ch < 3; ++ch) m[ch] = 0.25 * ((a[ch] + b[ch]) + (cc[ch] + d[ch]));
+          e[off[l] + y * side + x] = orc_encode_r11g11b10(m);
+        }
+    }
+    for (int i = fill; i > 0; --i) {
+      const int side = S >> i, below = 2 * side;
+      for (int y = 0; y < side; ++y)
+        for (int x = 0; x < side; ++x) {
+          double sc[3];
+          orc_decode_r11g11b10(e[off[i] + y * side + x], sc);
+          if (sc[0] + sc[1] + sc[2] < 0.0001) continue;
+          const int at[4] = {(2 * y) * below + 2 * x, (2 * y) * below + 2 * x + 1, (2 * y + 1) * below + 2 * x,
+                             (2 * y + 1) * below + 2 * x + 1};
+          double dc[4][3], sum[3] = {0, 0, 0};
+          for (int k = 0; k < 4; ++k) {
+            orc_decode_r11g11b10(e[off[i - 1] + at[k]], dc[k]);
+            if (dc[k][0] + dc[k][1] + dc[k][2] == 0.0)
+              for (int ch = 0; ch < 3; ++ch) dc[k][ch] = sc[ch];
+            for (int ch = 0; ch < 3; ++ch) sum[ch] += dc[k][ch];
+          }
+          for (int k = 0; k < 4; ++k) {
+            double o[3];
+            for (int ch = 0; ch < 3; ++ch) o[ch] = dc[k][ch] * (4.0 * sc[ch] / (sum[ch] + 0.00001));
+            e[off[i - 1] + at[k]] = orc_encode_r11g11b10(o);
+          }
+        }
+    }
   }
 }
 
@@ -1197,10 +1368,61 @@ void orc_light_caches_shadowed(const DrvConfig* cfg, int n_caches, const float* 
 void orc_apply(const DrvConfig* cfg, const DrvVolumeInfo* vol, const DrvPerFrame* f, int W, int H, const float* depth,
                const void* normal, int normal_format, const float* albedo, const uint32_t* atlas, int n_caches,
                const double* sh, double* out, int n_threads) {
+  orc_apply_specular(cfg, vol, f, W, H, depth, normal, normal_format, albedo, nullptr, atlas, n_caches, sh, nullptr,
+                     out, n_threads);
+}
+
+namespace {
+// Bilinear fetch of one level of a per-cache envmap (GL 4.5 section 8.14.2),
+// texel indices clamped to the level.
+void env_bilinear(const uint32_t* lv, int side, double u, double v, double out[3]) {
+  const double x = u * side - 0.5, y = v * side - 0.5;
+  const double fx = std::floor(x), fy = std::floor(y), a = x - fx, b = y - fy;
+  auto cl = [&](double q) { return std::min(std::max((int)q, 0), side - 1); };
+  const int x0 = cl(fx), x1 = cl(fx + 1), y0 = cl(fy), y1 = cl(fy + 1);
+  double t00[3], t10[3], t01[3], t11[3];
+  orc_decode_r11g11b10(lv[y0 * side + x0], t00);
+  orc_decode_r11g11b10(lv[y0 * side + x1], t10);
+  orc_decode_r11g11b10(lv[y1 * side + x0], t01);
+  orc_decode_r11g11b10(lv[y1 * side + x1], t11);
+  for (int ch = 0; ch < 3; ++ch)
+    out[ch] = (1 - a) * (1 - b) * t00[ch] + a * (1 - b) * t10[ch] + (1 - a) * b * t01[ch] + a * b * t11[ch];
+}
+}  // namespace
+
+// cacheApply.frag with INDIRECT_SPECULAR (:76-116, 145-158) when
+// cfg->specular_envmap_size > 0: rough_metal (RG F32 per pixel) and env (the
+// per-cache envmaps as orc_specular_prepare lays them out) give each corner
+// cache's trilinear envmap sample, and the material splits by metallic.
+void orc_apply_specular(const DrvConfig* cfg, const DrvVolumeInfo* vol, const DrvPerFrame* f, int W, int H,
+                        const float* depth, const void* normal, int normal_format, const float* albedo,
+                        const float* rough_metal, const uint32_t* atlas, int n_caches, const double* sh,
+                        const uint32_t* env, double* out, int n_threads) {
   set_threads(n_threads);
   const int res = cfg->cav_res, nC = cfg->n_cascades, AW = nC * res;
   const bool transitions = cfg->cascade_transition > 0.0f;
-  auto lighting = [&](const float p[3], int c, const double n[3], const double alb[3], double col[3]) {
+  const int S = cfg->specular_envmap_size;
+  const bool spec = S > 0 && rough_metal && env;
+  int L = 0;
+  while (spec && (1 << L) <= S) ++L;
+  std::vector<int> eoff(L + 1, 0);
+  for (int l = 1; l <= L; ++l) eoff[l] = eoff[l - 1] + (S >> (l - 1)) * (S >> (l - 1));
+  const int ewords = spec ? eoff[L] : 0;
+  struct Lookup {
+    double u, v, f;
+    int l0, l1;
+  };
+  auto env_sample = [&](uint32_t cache, const Lookup& q, double o[3]) {
+    const uint32_t* e = env + (size_t)cache * ewords;
+    env_bilinear(e + eoff[q.l0], S >> q.l0, q.u, q.v, o);
+    if (q.f > 0.0) {
+      double o1[3];
+      env_bilinear(e + eoff[q.l1], S >> q.l1, q.u, q.v, o1);
+      for (int ch = 0; ch < 3; ++ch) o[ch] = o[ch] * (1.0 - q.f) + o1[ch] * q.f;
+    }
+  };
+  auto lighting = [&](const float p[3], int c, const double n[3], const double alb[3], const Lookup* q,
+                      const double* spec_col, double col[3]) {
     static const int off[8][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {1, 1, 0}, {0, 0, 1}, {1, 0, 1}, {0, 1, 1}, {1, 1, 1}};
     const DrvCascade& k = vol->cascades[c];
     float a[3];
@@ -1211,7 +1433,7 @@ void orc_apply(const DrvConfig* cfg, const DrvVolumeInfo* vol, const DrvPerFrame
       a0[i] = (int)std::trunc(std::max(-1e9f, std::min(1e9f, a[i])));
       t[i] = (double)a[i] - (double)a0[i];
     }
-    double irr[3] = {0, 0, 0};
+    double irr[3] = {0, 0, 0}, sp[3] = {0, 0, 0};
     for (int i = 0; i < 8; ++i) {
       double w = (off[i][0] ? t[0] : 1 - t[0]) * (off[i][1] ? t[1] : 1 - t[1]) * (off[i][2] ? t[2] : 1 - t[2]);
       int x = a0[0] + off[i][0], y = a0[1] + off[i][1], z = a0[2] + off[i][2];
@@ -1222,8 +1444,13 @@ void orc_apply(const DrvConfig* cfg, const DrvVolumeInfo* vol, const DrvPerFrame
       double e[3];
       orc_sh_irradiance(cfg->sh_order, cfg->sh2_sign, sh + (size_t)(addr - 1) * 27, n, e);
       for (int ch = 0; ch < 3; ++ch) irr[ch] += e[ch] * w;
+      if (q) {
+        double es[3];
+        env_sample(addr - 1, *q, es);
+        for (int ch = 0; ch < 3; ++ch) sp[ch] += es[ch] * w;
+      }
     }
-    for (int ch = 0; ch < 3; ++ch) col[ch] = irr[ch] * alb[ch] / kShaderPi;
+    for (int ch = 0; ch < 3; ++ch) col[ch] = irr[ch] * alb[ch] / kShaderPi + (q ? sp[ch] * spec_col[ch] : 0.0);
   };
 #pragma omp parallel for schedule(static)
   for (int y = 0; y < H; ++y)
@@ -1246,13 +1473,38 @@ void orc_apply(const DrvConfig* cfg, const DrvVolumeInfo* vol, const DrvPerFrame
         n[2] = nf[2];
       }
       double alb[3] = {albedo[3 * i], albedo[3 * i + 1], albedo[3 * i + 2]};
+      Lookup q{};
+      double spec_col[3] = {0, 0, 0};
+      if (spec) {
+        // ComputeMaterialColors, RoughnessToBlinnExponent,
+        // GetHemisphereLodForBlinnPhongExponent and the lookup clamp
+        // (lightingfunctions.glsl:27-49, utils.glsl:193-200, cacheApply.frag:150-157).
+        const double rough = rough_metal[2 * i], metal = rough_metal[2 * i + 1];
+        for (int ch = 0; ch < 3; ++ch) {
+          spec_col[ch] = 0.04 * (1.0 - metal) + alb[ch] * metal;
+          alb[ch] = alb[ch] * (1.0 - metal) + 0.02 * metal;
+        }
+        const double rsq = rough * rough, blinn = 2.0 / (rsq * rsq + 0.0005);
+        const double lod = std::max(0.0, std::log2((double)S * S / (1.0 + blinn)) * 0.5);
+        const double half_px = 0.5 / (std::exp2(-std::ceil(lod)) * S);
+        d3 fx, fy, fz;
+        local_view_space(ld3(f->camera_position), mk(p[0], p[1], p[2]), fx, fy, fz);
+        const d3 nv = mk(n[0], n[1], n[2]);
+        hemi_projection(mk(dot(nv, fx), dot(nv, fy), dot(nv, fz)), q.u, q.v);
+        q.u = std::min(std::max(q.u, half_px), 1.0 - half_px);
+        q.v = std::min(std::max(q.v, half_px), 1.0 - half_px);
+        const double fl = std::min(std::floor(lod), (double)(L - 1));
+        q.l0 = (int)fl;
+        q.l1 = std::min(q.l0 + 1, L - 1);
+        q.f = q.l1 > q.l0 ? lod - fl : 0.0;
+      }
       double col[3];
-      lighting(p, c, n, alb, col);
+      lighting(p, c, n, alb, spec ? &q : nullptr, spec_col, col);
       if (transitions) {
         float t = cascade_transition_f32(vol, c, p);
         if (t > 0.0f && c < nC - 1) {
           double col2[3];
-          lighting(p, c + 1, n, alb, col2);
+          lighting(p, c + 1, n, alb, spec ? &q : nullptr, spec_col, col2);
           for (int ch = 0; ch < 3; ++ch) col[ch] = col[ch] * (1.0 - t) + col2[ch] * t;
         }
       }

@@ -97,6 +97,25 @@ int orc_allocate_caches(const DrvConfig* cfg, const DrvVolumeInfo* vol, const Dr
 void orc_light_caches(const DrvConfig* cfg, const DrvVolumeInfo* vol, int n_caches, const float* positions,
                       int n_lights, const DrvSpotLight* lights, const double* const* vpls, const double* const* cones,
                       const int* n_vpls, const uint32_t* bits, const double* mips, double* sh_out, int n_threads);
+/* orc_light_caches with INDIRECT_SPECULAR (cfg->specular_envmap_size S > 0):
+ * VPLs whose flux sum is below 0.001 are skipped (cacheLightingRSM.comp:240),
+ * and with cam and env_out each cache's level-0 specular envmap is written,
+ * S*S texels RGB row-major per cache, FP64 before rounding
+ * (cacheLightingRSM.comp:87-98, 310-335: reflected radiance into the texel of
+ * the cache-local half vector, times the base level's Blinn normalisation). */
+void orc_light_caches_specular(const DrvConfig* cfg, const DrvVolumeInfo* vol, int n_caches, const float* positions,
+                               const float* cam, int n_lights, const DrvSpotLight* lights,
+                               const double* const* vpls, const double* const* cones, const int* n_vpls,
+                               const uint32_t* bits, const double* mips, double* sh_out, double* env_out,
+                               int n_threads);
+/* R11F_G11F_B10F (GL packed float: R bits 0-10, G 11-21, B 22-31). */
+uint32_t orc_encode_r11g11b10(const double rgb[3]);
+void orc_encode_r11g11b10_n(const double* rgb, int64_t n, uint32_t* out);
+void orc_decode_r11g11b10(uint32_t v, double rgb[3]);
+/* Renderer::PrepareSpecularEnvmaps on per-cache envmaps in place (level 0
+ * given, encoded): mips and the hole fill from level `fill` down to 1. Cache
+ * c's levels start at c * sum_l (S >> l)^2 words. */
+void orc_specular_prepare(int S, int fill, int n_caches, uint32_t* env, int n_threads);
 /* The same gather with given shadowing per (cache, shadow block) pair:
  * shadow[c * total_blocks + b], blocks of all lights in light order. */
 void orc_light_caches_shadowed(const DrvConfig* cfg, int n_caches, const float* positions, int n_lights,
@@ -117,6 +136,13 @@ void orc_bruteforce_rsm(const DrvPerFrame* frame, int width, int height, const f
 void orc_apply(const DrvConfig* cfg, const DrvVolumeInfo* vol, const DrvPerFrame* frame, int width, int height,
                const float* depth, const void* normal, int normal_format, const float* albedo, const uint32_t* atlas,
                int n_caches, const double* sh, double* out_rgb, int n_threads);
+/* orc_apply plus the INDIRECT_SPECULAR term (cfg->specular_envmap_size > 0,
+ * rough_metal RG F32 per pixel and env as orc_specular_prepare lays it out;
+ * either NULL: the diffuse apply). */
+void orc_apply_specular(const DrvConfig* cfg, const DrvVolumeInfo* vol, const DrvPerFrame* frame, int width,
+                        int height, const float* depth, const void* normal, int normal_format, const float* albedo,
+                        const float* rough_metal, const uint32_t* atlas, int n_caches, const double* sh,
+                        const uint32_t* env, double* out_rgb, int n_threads);
 #ifdef __cplusplus
 }
 #endif

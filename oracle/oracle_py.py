@@ -72,6 +72,14 @@ def load():
         "orc_apply": (None, [P(abi.DrvConfig), P(abi.DrvVolumeInfo), P(abi.DrvPerFrame), I, I, VP, VP, I, VP, VP, I,
                              VP, VP, I]),
         "orc_bruteforce_rsm": (None, [P(abi.DrvPerFrame), I, I, VP, VP, VP, VP, I, P(VP), P(I), VP, I]),
+        "orc_light_caches_specular": (None, [P(abi.DrvConfig), P(abi.DrvVolumeInfo), I, VP, VP, I,
+                                             P(abi.DrvSpotLight), P(VP), P(VP), P(I), VP, VP, VP, VP, I]),
+        "orc_encode_r11g11b10": (C.c_uint32, [P(D)]),
+        "orc_encode_r11g11b10_n": (None, [VP, C.c_int64, VP]),
+        "orc_decode_r11g11b10": (None, [C.c_uint32, P(D)]),
+        "orc_specular_prepare": (None, [I, I, I, VP, I]),
+        "orc_apply_specular": (None, [P(abi.DrvConfig), P(abi.DrvVolumeInfo), P(abi.DrvPerFrame), I, I, VP, VP, I,
+                                      VP, VP, VP, I, VP, VP, VP, I]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -291,6 +299,76 @@ def light_caches(cfg, vol, positions, lights, vpls, cones, bits, mips, n_threads
     load().orc_light_caches(C.byref(cfg), C.byref(vol), n, _p(positions), L, lights, vp, cp, nv, _p(bits), _p(mips),
                             _p(sh), n_threads)
     return sh
+
+
+def light_caches_specular(cfg, vol, positions, cam, lights, vpls, cones, bits, mips, n_threads=0):
+    """SH [n, 27] and level-0 specular envmaps [n, S, S, 3] (FP64, not rounded)."""
+    positions = np.ascontiguousarray(positions, dtype=np.float32)
+    n = positions.shape[0]
+    L = len(vpls)
+    S = cfg.specular_envmap_size
+    sh = np.zeros((n, 27), np.float64)
+    env = np.zeros((n, S, S, 3), np.float64)
+    vp = (C.c_void_p * L)(*[v.ctypes.data for v in vpls])
+    cp = (C.c_void_p * L)(*[c.ctypes.data for c in cones])
+    nv = (C.c_int * L)(*[v.shape[0] for v in vpls])
+    cam = np.ascontiguousarray(cam, dtype=np.float32)
+    load().orc_light_caches_specular(C.byref(cfg), C.byref(vol), n, _p(positions), _p(cam), L, lights, vp, cp, nv,
+                                     _p(bits), _p(mips), _p(sh), _p(env), n_threads)
+    return sh, env
+
+
+def encode_r11g11b10(rgb) -> np.ndarray:
+    """[..., 3] float64 -> uint32 R11F_G11F_B10F words (the GL rules, nearest)."""
+    a = np.ascontiguousarray(rgb, dtype=np.float64).reshape(-1, 3)
+    out = np.zeros(a.shape[0], np.uint32)
+    load().orc_encode_r11g11b10_n(_p(a), a.shape[0], _p(out))
+    return out.reshape(np.shape(rgb)[:-1])
+
+
+def decode_r11g11b10(words) -> np.ndarray:
+    """uint32 R11F_G11F_B10F words -> [..., 3] float64 (vectorised)."""
+    w = np.asarray(words, dtype=np.uint32)
+
+    def uf(v, mb):
+        e = (v >> mb).astype(np.int64)
+        m = (v & ((1 << mb) - 1)).astype(np.float64)
+        normal = np.ldexp(1.0 + m / (1 << mb), e - 15)
+        sub = np.ldexp(m, -14 - mb)
+        out = np.where(e == 0, sub, normal)
+        return np.where(e == 31, np.where(m > 0, np.nan, np.inf), out)
+
+    return np.stack([uf(w & 0x7FF, 6), uf((w >> 11) & 0x7FF, 6), uf(w >> 22, 5)], -1)
+
+
+def specular_levels(S: int) -> list:
+    """Word offsets of the levels of one per-cache envmap, and the total."""
+    off, o, l = [], 0, 0
+    while (S >> l) >= 1:
+        off.append(o)
+        o += (S >> l) ** 2
+        l += 1
+    return off + [o]
+
+
+def specular_prepare(S: int, fill: int, env_words, n_threads=0) -> np.ndarray:
+    """Mips + hole fill of per-cache envmaps [n, words] (level 0 given) in a copy."""
+    e = np.ascontiguousarray(env_words, dtype=np.uint32).copy()
+    load().orc_specular_prepare(S, fill, e.shape[0], _p(e), n_threads)
+    return e
+
+
+def apply_specular(cfg, vol, frame, depth, normal, normal_format, albedo, rough_metal, atlas, sh, env, n_threads=0):
+    H, W = depth.shape
+    out = np.zeros((H, W, 3), np.float64)
+    sh = np.ascontiguousarray(sh, dtype=np.float64)
+    rm = np.ascontiguousarray(rough_metal, dtype=np.float32)
+    env = np.ascontiguousarray(env, dtype=np.uint32)
+    load().orc_apply_specular(C.byref(cfg), C.byref(vol), C.byref(frame), W, H, _p(np.ascontiguousarray(depth)),
+                              _p(np.ascontiguousarray(normal)), normal_format, _p(np.ascontiguousarray(albedo)),
+                              _p(rm), _p(np.ascontiguousarray(atlas, dtype=np.uint32)), sh.shape[0], _p(sh), _p(env),
+                              _p(out), n_threads)
+    return out
 
 
 def light_caches_shadowed(cfg, positions, lights, vpls, shadow, n_threads=0):

@@ -23,7 +23,7 @@ def rel_l2(a, b):
 class Run:
     """Runs the GPU stages of one workload and the oracle on the same inputs."""
 
-    def __init__(self, w, oracle, seed=None, normal_format=abi.NORMAL_RG16I, sh2_sign=None):
+    def __init__(self, w, oracle, seed=None, normal_format=abi.NORMAL_RG16I, sh2_sign=None, tuning=None):
         import torch
         self.torch = torch
         self.w = w
@@ -32,12 +32,27 @@ class Run:
         if sh2_sign is not None:
             self.hf.config.sh2_sign = sh2_sign
         self.pipe = pipeline.Pipeline(self.hf, normal_format=normal_format)
+        self.spec = w.specular_envmap_size > 0
+        if self.spec:
+            # seeded roughness / metallic (RG8 unorm), as the G-buffer pass writes them
+            rng = np.random.default_rng(11)
+            self.rough_metal_u8 = rng.integers(0, 256, (w.height, w.width, 2), dtype=np.uint8)
+            self.pipe.rough_metal.copy_(torch.from_numpy(self.rough_metal_u8))
+            torch.cuda.synchronize()
+            # the apply reads byte / 255 in binary32
+            self.rough_metal = self.rough_metal_u8.astype(np.float32) / np.float32(255.0)
+        if tuning:
+            self.pipe.set_tuning(**tuning)
         self.pipe.raycast_inputs()
         self.pipe.prepare_and_extract()
         if w.indirect_shadow:
             self.pipe.voxelize()
         self.pipe.allocate()
         self.pipe.light()
+        if self.spec:
+            # the level-0 envmaps as the light stage leaves them (the hole fill rewrites level 0)
+            self.env_lit = self.pipe.read_specular(min(self.pipe.cache_count(), w.max_caches))
+            self.pipe.prepare_specular()
         self.pipe.apply()
         self.pipe.sync()
         torch.cuda.synchronize()
@@ -60,6 +75,8 @@ class Run:
         if w.indirect_shadow:
             self.bits = p.read_voxel_bits().cpu().numpy().view(np.uint32)
             self.mips = [p.read_mip(l).cpu().numpy() for l in range(1, int(np.log2(w.voxel_res)) + 1)]
+        if self.spec:
+            self.env = p.read_specular(n)  # [n, words] per-cache envmap levels
 
     # oracle views of the GPU's own inputs
     def oracle_vpls(self):

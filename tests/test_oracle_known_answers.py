@@ -311,3 +311,52 @@ def test_triangle_voxelization_depth_conservative(oracle):
     v = np.unpackbits(bits.view(np.uint8), bitorder="little").reshape(N, N, N)
     col = v[:, 10, 10]  # column at x = 10, y = 10
     assert col.sum() >= 2  # more than the single voxel of the centre depth
+
+
+def test_r11g11b10_codec_known_answers(oracle):
+    """The GL packed-float texel of the specular envmaps (GL 4.5 sections
+    2.3.4.3-4): 5-bit exponent with bias 15, 6 (blue 5) mantissa bits, round
+    to nearest, negatives to 0, large values to the largest finite one."""
+    one = (15 << 6) | ((15 << 6) << 11) | ((15 << 5) << 22)
+    assert int(oracle.encode_r11g11b10(np.array([1.0, 1.0, 1.0]))) == one
+    w = oracle.encode_r11g11b10(np.array([[65024.0, 1e9, 64512.0], [-1.0, 0.0, -np.inf], [np.inf, 2.0 ** -20, 0.5]]))
+    assert list(oracle.decode_r11g11b10(w[0])) == [65024.0, 65024.0, 64512.0]
+    assert list(oracle.decode_r11g11b10(w[1])) == [0.0, 0.0, 0.0]
+    r, g, b = oracle.decode_r11g11b10(w[2])
+    assert np.isinf(r) and g == 2.0 ** -20 and b == 0.5  # 2^-20 is the smallest red/green subnormal
+    # ties go to the even mantissa: 1 + 1/128 -> 1, 1 + 3/128 -> 1 + 2/64
+    t = oracle.decode_r11g11b10(oracle.encode_r11g11b10(np.array([[1 + 1 / 128, 1 + 3 / 128, 1 + 1 / 64]])))[0]
+    assert list(t) == [1.0, 1.0 + 2 / 64, 1.0]  # blue: 1 + 1/64 is a tie at 5 bits
+    # every finite code of each channel decodes and encodes back to itself
+    for shift, mb in ((0, 6), (11, 6), (22, 5)):
+        codes = np.arange(0, 31 << mb, dtype=np.uint32)
+        vals = oracle.decode_r11g11b10(codes << shift)
+        assert np.array_equal(oracle.encode_r11g11b10(vals), codes << shift)
+
+
+def test_specular_prepare_known_answer(oracle):
+    """Mips are the 2x2 means (exact here); the hole fill gives zero texels
+    their parent's colour and rescales the four so that their mean keeps the
+    parent's value (up to the 1e-5 guard and the texel rounding)."""
+    S = 8
+    off = oracle.specular_levels(S)
+    rng = np.random.default_rng(5)
+    lvl0 = np.zeros((S, S, 3))
+    lvl0[rng.random((S, S)) < 0.3] = rng.choice([0.25, 0.5, 1.0, 2.0, 4.0], size=(1, 3))
+    e = np.zeros((1, off[-1]), np.uint32)
+    e[0, :S * S] = oracle.encode_r11g11b10(lvl0.reshape(-1, 3))
+    m = oracle.specular_prepare(S, 0, e)
+    for l in range(1, len(off) - 1):
+        side = S >> l
+        below = oracle.decode_r11g11b10(m[0, off[l - 1]:off[l]]).reshape(2 * side, 2 * side, 3)
+        mean = below.reshape(side, 2, side, 2, 3).mean(axis=(1, 3))
+        assert np.array_equal(oracle.encode_r11g11b10(mean.reshape(-1, 3)), m[0, off[l]:off[l + 1]])
+    f = oracle.specular_prepare(S, 2, e)
+    assert np.array_equal(f[0, off[2]:], m[0, off[2]:])  # the fill leaves levels 2.. as the mips made them
+    for l in (1, 0):  # levels the fill wrote (from level 2 down)
+        side = S >> (l + 1)
+        parent = oracle.decode_r11g11b10(f[0, off[l + 1]:off[l + 2]]).reshape(side, side, 3)
+        kids = oracle.decode_r11g11b10(f[0, off[l]:off[l + 1]]).reshape(side, 2, side, 2, 3)
+        live = parent.sum(-1) >= 1e-4
+        assert np.all(kids.sum(-1).min(axis=(1, 3))[live] > 0)  # no holes under a lit parent
+        np.testing.assert_allclose(kids.mean(axis=(1, 3))[live], parent[live], rtol=2e-2)
