@@ -39,6 +39,11 @@ UNIT = "caches/s"
 # ns_1080p_4096, from one `ncu --set full --clock-control none` capture each
 # (cold caches) of `bench.py --steps 1 --warmup 1` at that workload.
 NCU_TRAFFIC = {"cone_kernel": 12_660_736, "mlp_kernel": 7_976_192}
+# Cache-level bytes of one cone pass of ns_1080p_4096 (BF16) and their share
+# of the L1/TEX and L2 throughput peaks, from one ncu capture: the cone march
+# reads its voxels from L1/L2, so these, not HBM, are its memory roofline.
+NCU_CONE_CACHE = {"l1_bytes": 261_125_792, "l2_bytes": 129_594_048, "l1_pct_of_peak": 17.78,
+                  "l2_pct_of_peak": 6.58, "ncu_us": 104.9}
 
 
 def parse():
@@ -598,8 +603,16 @@ def run_ours(args):
                     "traffic": NCU_TRAFFIC.get(f"{top}_kernel") if w.name == "ns_1080p_4096" else None,
                     "peak_source": pk["source"] + " (hbm_gbs)",
                     "algorithmic": f"{pairs_traced} traced pairs x 16 B + {count} caches x 16 B + {w.n_vpls} cones x 16 B",
-                    "note": "the cone pass is issue-bound (71% issue active, ALU pipe 50%, voxel samples from "
+                    "note": "the cone pass is issue-bound (75% issue active, ALU pipe 55%, voxel samples from "
                             "L1/L2), far from the HBM roofline"}
+        if top == "cone" and w.name == "ns_1080p_4096":
+            c = NCU_CONE_CACHE
+            roofline["cache_levels"] = {
+                "l1_gbs": c["l1_bytes"] / (top_ms / 1e3) / 1e9, "l2_gbs": c["l2_bytes"] / (top_ms / 1e3) / 1e9,
+                "l1_pct_of_peak": c["l1_pct_of_peak"], "l2_pct_of_peak": c["l2_pct_of_peak"],
+                "bytes_per_launch": {"l1": c["l1_bytes"], "l2": c["l2_bytes"]},
+                "note": "bytes and % of peak from one ncu capture of the BF16 cone pass (%.1f us there); "
+                        "GB/s = those bytes over this run's live kernel time" % c["ncu_us"]}
     line = {
         "metric": METRIC, "value": caches_all / (light_ms_all / 1e3), "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": light_ms_all, "ms_per_frame": frame_ms_all,

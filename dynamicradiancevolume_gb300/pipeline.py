@@ -411,3 +411,29 @@ class Pipeline:
 
 def scaled(w: Workload, **kw) -> Workload:
     return replace(w, **kw)
+
+
+def main(argv=None) -> int:
+    """Runs whole frames (drv_frame) of a named workload on cuda:0: ray-cast
+    inputs once, then --frames frames; prints the cache and pair counts.
+    `python -m dynamicradiancevolume_gb300.pipeline ns_1080p_4096 --precision bf16 --frames 4`."""
+    import argparse
+    ap = argparse.ArgumentParser(description=main.__doc__)
+    ap.add_argument("workload", choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", choices=["fp32", "bf16"], default="fp32")
+    ap.add_argument("--frames", type=int, default=4)
+    ap.add_argument("--seed", type=int, default=None)
+    a = ap.parse_args(argv)
+    w = scaled(WORKLOADS[a.workload], precision=abi.PRECISION_BF16 if a.precision == "bf16" else abi.PRECISION_FP32)
+    p = Pipeline(host_frame(w, a.seed))
+    p.raycast_inputs()
+    for _ in range(a.frames):
+        p.frame()
+    p.sync()
+    print("workload %s (%s): %d caches, %d lit pairs" % (w.name, a.precision, p.cache_count(), p.light_pairs()))
+    p.close()
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())
