@@ -262,7 +262,26 @@ def oracle_frame_from(pipe):
     cfg.precision, cfg.visibility = 0, 0
     st, atlas, pos, count = O.allocate_caches(cfg, hf.volume, hf.frame, depth)
     sh = O.light_caches(cfg, hf.volume, pos, hf.lights, vp, cones, bits, mips)
-    return O.apply(cfg, hf.volume, hf.frame, depth, n16, 0, alb, atlas, sh)  # 0: RG16I normals
+    out = O.apply(cfg, hf.volume, hf.frame, depth, n16, 0, alb, atlas, sh)  # 0: RG16I normals
+    return out, pos[:count], sh[:count]
+
+
+def errors_vs_fp64(pipe, count, out, reference) -> dict:
+    """Per-result errors against the FP64 oracle frame: the caches' SH
+    (matched by position: the allocation is bit-exact, its order is the
+    atomics') and the final radiance, rel-L2 and max |difference|."""
+    import numpy as np
+    ref_out, ref_pos, ref_sh = reference
+    e = {"rel_l2_vs_fp64": rel_l2(out, ref_out), "radiance_max_abs_vs_fp64": float(np.max(np.abs(out - ref_out)))}
+    pos, sh = pipe.read_entries_decoded(count)
+    if pos.shape == ref_pos.shape:
+        a, b = np.lexsort(pos.T[::-1]), np.lexsort(ref_pos.T[::-1])
+        if np.array_equal(pos[a], ref_pos[b]):
+            nk = 27 if pipe.hf.workload.sh_order == 2 else 12
+            g, r = sh[a][:, :nk], ref_sh[b][:, :nk]
+            e["sh_rel_l2_vs_fp64"] = rel_l2(g, r)
+            e["sh_max_abs_vs_fp64"] = float(np.max(np.abs(g - r)))
+    return e
 
 
 def rel_l2(a, b) -> float:
@@ -409,7 +428,13 @@ def run_ours(args):
             light_ms = measure_light_graph(pipe, args.steps, args.warmup, flush)
             pipe.frame()
             pipe.sync()
-            pipe.light()
+            # errors of this frame's SH and radiance (read before the extra
+            # light stage below, whose SH would add onto the frame's)
+            out = pipe.out.cpu().numpy()
+            if reference is None and rank == 0:
+                reference = oracle_frame_from(pipe)
+            errors = errors_vs_fp64(pipe, count, out, reference) if rank == 0 else {}
+            pipe.light()  # one eager light stage: its pair count and surrogate statistics
             info = {"caches_lit_per_s": count / (light_ms / 1e3), "light_ms": light_ms, "frame_ms": graph_ms,
                     "live_pairs": pipe.light_pairs(),
                     "frame_ms_stream": frame_ms, "stage_ms": stage_ms, "caches": count,
@@ -425,11 +450,7 @@ def run_ours(args):
                 info["retraced_pairs"] = fb.value
                 info["evaluated_share_of_pairs"] = ev.value / max(count * blocks, 1)
                 info["retraced_share_of_evaluated"] = fb.value / max(ev.value, 1)
-            out = pipe.out.cpu().numpy()
-            if reference is None and rank == 0:
-                reference = oracle_frame_from(pipe)
-            if rank == 0:
-                info["rel_l2_vs_fp64"] = rel_l2(out, reference)
+            info.update(errors)
             variants[name] = info
             pipes[name] = pipe
         # INDIRECT_SPECULAR with the reference's 16x16 per-cache envmaps on the
@@ -461,103 +482,120 @@ def run_ours(args):
         if n != head:
             p.close()
 
-    # ---- e2e through drv_frame with host buffers (pinned), H2D + D2H inside the region.
+    # ---- e2e through the C ABI with host buffers (pinned), H2D + D2H inside the region.
     # Two contexts on two streams take the steps in turn (double buffering, as
     # a renderer uploads frame k+1 while frame k renders): every step copies
-    # its G-buffer and RSM from pinned host memory, runs drv_frame and copies
+    # its G-buffer and RSM from pinned host memory, runs the frame and copies
     # its radiance back; the copies of one step overlap the kernels of the
     # other. Both contexts' working sets together exceed L2 (~2 x 120 MB).
+    # The headline uses the reference's own render targets (D32F depth, RG16I
+    # normal, SRGB8 diffuse, RGB16F / RG16I / RG16F RSM, RGBA16F output with
+    # additive blending, renderer.cpp:119, 468-480, 1288-1290); the same steps
+    # over F32 targets are reported beside it.
     wv_head = next(wv for name, wv, thr in plan if name == head)
-    hf2 = pipeline.host_frame(wv_head)
-    if head.startswith("surrogate"):
-        hf2.config.surrogate_conf_threshold = hv["threshold"]
-    pipe2 = pipeline.Pipeline(hf2, device=str(dev))
-    if head.startswith("surrogate"):
-        surrogate.upload(pipe2, weights)
-    pipes = [pipe, pipe2]
-    host_in = [t.cpu().pin_memory() for t in (pipe.depth, pipe.normal16, pipe.albedo)]
-    host_rsm = [[t.cpu().pin_memory() for t in (pipe.rsm_flux[l], pipe.rsm_normal[l], pipe.rsm_dls[l])]
-                for l in range(w.n_lights)]
-    host_out = [torch.empty(pipe.out.shape, dtype=torch.float32).pin_memory() for _ in pipes]
-    h2d = sum(t.numel() * t.element_size() for t in host_in) + sum(
-        t.numel() * t.element_size() for r in host_rsm for t in r)
-    d2h = host_out[0].numel() * 4
+    g_ref, rsm_ref = pipeline.reference_format_inputs(pipe)
 
-    def e2e_step(k):
-        p = pipes[k % 2]
-        dev_in = [p.depth, p.normal16, p.albedo]
-        with torch.cuda.stream(p.stream):
-            for d, h in zip(dev_in, host_in):
-                d.copy_(h, non_blocking=True)
-            for l in range(w.n_lights):
-                for d, h in zip((p.rsm_flux[l], p.rsm_normal[l], p.rsm_dls[l]), host_rsm[l]):
+    def e2e_pipes(formats):
+        out = []
+        for _ in range(2):
+            hf2 = pipeline.host_frame(wv_head)
+            if head.startswith("surrogate"):
+                hf2.config.surrogate_conf_threshold = hv["threshold"]
+            if formats == "reference":
+                hf2.config.output_format, hf2.config.output_blend = abi.OUTPUT_RGBA16F, abi.OUTPUT_ADD
+                q = pipeline.Pipeline(hf2, device=str(dev), albedo_format=abi.ALBEDO_SRGB8, rsm_format=abi.RSM_F16)
+            else:
+                q = pipeline.Pipeline(hf2, device=str(dev))
+            if head.startswith("surrogate"):
+                surrogate.upload(q, weights)
+            out.append(q)
+        return out
+
+    def run_e2e(formats, graph, two_contexts=True):
+        """Mean ms per step; (h2d, d2h) bytes per step."""
+        qs = e2e_pipes(formats)
+        if formats == "reference":
+            host_in = [torch.from_numpy(a).pin_memory() for a in g_ref]
+            host_rsm = [[torch.from_numpy(a).pin_memory() for a in r] for r in rsm_ref]
+            dev_in = lambda q: [q.depth, q.normal16, q.albedo8]
+            dev_rsm = lambda q, l: (q.rsm_flux16[l], q.rsm_normal[l], q.rsm_dls16[l])
+        else:
+            host_in = [t.cpu().pin_memory() for t in (pipe.depth, pipe.normal16, pipe.albedo)]
+            host_rsm = [[t.cpu().pin_memory() for t in (pipe.rsm_flux[l], pipe.rsm_normal[l], pipe.rsm_dls[l])]
+                        for l in range(w.n_lights)]
+            dev_in = lambda q: [q.depth, q.normal16, q.albedo]
+            dev_rsm = lambda q, l: (q.rsm_flux[l], q.rsm_normal[l], q.rsm_dls[l])
+        host_out = [torch.empty(q.out.shape, dtype=q.out.dtype).pin_memory() for q in qs]
+        h2d = sum(t.numel() * t.element_size() for t in host_in) + sum(
+            t.numel() * t.element_size() for r in host_rsm for t in r)
+        d2h = host_out[0].numel() * host_out[0].element_size()
+        # one eager frame per context first (the scene's boxes become resident:
+        # a capture cannot include their upload)
+        for q in qs:
+            with torch.cuda.stream(q.stream):
+                for d, h in zip(dev_in(q), host_in):
                     d.copy_(h, non_blocking=True)
-        p.frame()
-        with torch.cuda.stream(p.stream):
-            host_out[k % 2].copy_(p.out, non_blocking=True)
+                for l in range(w.n_lights):
+                    for d, h in zip(dev_rsm(q, l), host_rsm[l]):
+                        d.copy_(h, non_blocking=True)
+            q.frame()
+            q.sync()
+        graphs = [batch_mod.Batch([batch_mod.Scene(q, 0, 0)], 1, stream=q.stream) for q in qs] if graph else None
 
-    for k in range(max(args.warmup, 2)):
-        e2e_step(k)
-    torch.cuda.synchronize(dev)
-    with torch.cuda.stream(pipe.stream):
-        flush.zero_()
-    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    start.record(pipe.stream)
-    pipe2.stream.wait_event(start)
-    for k in range(args.steps):
-        e2e_step(k)
-    pipe.stream.wait_stream(pipe2.stream)
-    end.record(pipe.stream)
-    end.synchronize()
-    e2e_ms = start.elapsed_time(end) / args.steps
-    # the same steps one at a time on one context, for comparison
-    serial = []
-    for k in range(args.steps):
-        with torch.cuda.stream(pipe.stream):
+        def step(k):
+            i = k % 2 if two_contexts else 0
+            q = qs[i]
+            with torch.cuda.stream(q.stream):
+                for d, h in zip(dev_in(q), host_in):
+                    d.copy_(h, non_blocking=True)
+                for l in range(w.n_lights):
+                    for d, h in zip(dev_rsm(q, l), host_rsm[l]):
+                        d.copy_(h, non_blocking=True)
+            if graph:
+                graphs[i].launch(q.stream)
+            else:
+                q.frame()
+            with torch.cuda.stream(q.stream):
+                host_out[i].copy_(q.out, non_blocking=True)
+
+        for k in range(max(args.warmup, 2)):
+            step(k)
+        torch.cuda.synchronize(dev)
+        a, b = qs[0], qs[1]
+        with torch.cuda.stream(a.stream):
             flush.zero_()
-        a, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(pipe.stream)
-        e2e_step(0)
-        b_.record(pipe.stream)
-        b_.synchronize()
-        serial.append(a.elapsed_time(b_))
-    e2e_serial_ms = statistics.mean(serial)
-    torch.cuda.synchronize(dev)
-    e2e_frame_ms = e2e_ms
-    # The same double-buffered steps with each context's frame captured once
-    # as a CUDA graph (drv_batch of one scene) and replayed per step; the
-    # inputs still come from host memory and the radiance goes back every step.
-    graphs = [batch_mod.Batch([batch_mod.Scene(q, 0, 0)], 1, stream=q.stream) for q in pipes]
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if two_contexts:
+            start.record(a.stream)
+            b.stream.wait_event(start)
+            for k in range(args.steps):
+                step(k)
+            a.stream.wait_stream(b.stream)
+            end.record(a.stream)
+            end.synchronize()
+            ms = start.elapsed_time(end) / args.steps
+        else:
+            serial = []
+            for k in range(args.steps):
+                with torch.cuda.stream(a.stream):
+                    flush.zero_()
+                start.record(a.stream)
+                step(0)
+                end.record(a.stream)
+                end.synchronize()
+                serial.append(start.elapsed_time(end))
+            ms = statistics.mean(serial)
+        torch.cuda.synchronize(dev)
+        for g in graphs or []:
+            g.close()
+        for q in qs:
+            q.close()
+        return ms, h2d, d2h
 
-    def e2e_graph_step(k):
-        p = pipes[k % 2]
-        with torch.cuda.stream(p.stream):
-            for d, h in zip((p.depth, p.normal16, p.albedo), host_in):
-                d.copy_(h, non_blocking=True)
-            for l in range(w.n_lights):
-                for d, h in zip((p.rsm_flux[l], p.rsm_normal[l], p.rsm_dls[l]), host_rsm[l]):
-                    d.copy_(h, non_blocking=True)
-        graphs[k % 2].launch(p.stream)
-        with torch.cuda.stream(p.stream):
-            host_out[k % 2].copy_(p.out, non_blocking=True)
-
-    for k in range(max(args.warmup, 2)):
-        e2e_graph_step(k)
-    torch.cuda.synchronize(dev)
-    with torch.cuda.stream(pipe.stream):
-        flush.zero_()
-    start.record(pipe.stream)
-    pipe2.stream.wait_event(start)
-    for k in range(args.steps):
-        e2e_graph_step(k)
-    pipe.stream.wait_stream(pipe2.stream)
-    end.record(pipe.stream)
-    end.synchronize()
-    e2e_ms = start.elapsed_time(end) / args.steps
-    for g in graphs:
-        g.close()
-    torch.cuda.synchronize(dev)
-    pipe2.close()
+    e2e_ms, h2d, d2h = run_e2e("reference", graph=True)
+    e2e_frame_ms, _, _ = run_e2e("reference", graph=False)
+    e2e_serial_ms, _, _ = run_e2e("reference", graph=False, two_contexts=False)
+    e2e_f32_ms, h2d_f32, d2h_f32 = run_e2e("f32", graph=True)
     count = hv["caches"]
 
     # ---- per-kernel times of the headline light stage (non-graph, events between its kernels)
@@ -611,7 +649,7 @@ def run_ours(args):
                 "l1_gbs": c["l1_bytes"] / (top_ms / 1e3) / 1e9, "l2_gbs": c["l2_bytes"] / (top_ms / 1e3) / 1e9,
                 "l1_pct_of_peak": c["l1_pct_of_peak"], "l2_pct_of_peak": c["l2_pct_of_peak"],
                 "bytes_per_launch": {"l1": c["l1_bytes"], "l2": c["l2_bytes"]},
-                "note": "bytes and % of peak from one ncu capture of the BF16 cone pass (%.1f us there); "
+                "note": "bytes and share of peak from one ncu capture of the BF16 cone pass (%.1f us there); "
                         "GB/s = those bytes over this run's live kernel time" % c["ncu_us"]}
     line = {
         "metric": METRIC, "value": caches_all / (light_ms_all / 1e3), "unit": UNIT, "n_gpus": ws,
@@ -627,6 +665,8 @@ def run_ours(args):
                            "(drv_frame) replayed the same way",
                    "l2": "flushed between steps (256 MiB write)"},
         "rel_l2_vs_fp64": hv.get("rel_l2_vs_fp64"),
+        "errors_vs_fp64": {k: hv.get(k) for k in ("rel_l2_vs_fp64", "radiance_max_abs_vs_fp64", "sh_rel_l2_vs_fp64",
+                                                  "sh_max_abs_vs_fp64")},
         "stage_ms": hv["stage_ms"],
         "light_kernel_ms": kernel_ms,
         "variants": variants,
@@ -635,12 +675,18 @@ def run_ours(args):
         "e2e": {"value": caches_all / (e2e_ms_all / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms_all, "ms_per_step_drv_frame": e2e_frame_ms,
                 "ms_per_step_one_context": e2e_serial_ms,
+                "formats": "the reference's render targets: D32F depth, RG16I normal, SRGB8 diffuse; RSM RGB16F "
+                           "flux, RG16I normal, RG16F (d, d^2); radiance added into an RGBA16F HDR buffer",
+                "f32_formats": {"ms_per_step": e2e_f32_ms, "h2d_bytes_per_step": h2d_f32,
+                                "d2h_bytes_per_step": d2h_f32,
+                                "value": caches_all / (e2e_f32_ms / 1e3)},
                 "scope": "whole frame per step: G-buffer and RSM copied from pinned host memory, the frame "
                          "replayed as a CUDA graph (drv_batch_launch of a one-scene batch captured once per "
                          "context), radiance copied back, all inside the timed region; two contexts on two "
                          "streams take the steps in turn (double buffering). ms_per_step_drv_frame: the same "
                          "steps calling drv_frame (kernels launched one by one); ms_per_step_one_context: "
-                         "drv_frame steps on one context, one at a time"},
+                         "drv_frame steps on one context, one at a time; f32_formats: the graph steps with "
+                         "F32 diffuse, F32 RSM and an RGB F32 output"},
         "gpu_launches": light_stage_launches(w, head.startswith("surrogate")) * args.steps,
         "clocks": clocks,
     }

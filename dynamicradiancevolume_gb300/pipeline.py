@@ -133,7 +133,14 @@ def host_frame(w: Workload, seed: int | None = None) -> HostFrame:
 class Pipeline:
     """One DrvContext + device buffers for one frame of a workload."""
 
-    def __init__(self, hf: HostFrame, device: str = "cuda", normal_format: int = abi.NORMAL_RG16I):
+    def __init__(self, hf: HostFrame, device: str = "cuda", normal_format: int = abi.NORMAL_RG16I,
+                 albedo_format: int = abi.ALBEDO_F32X3, rsm_format: int = abi.RSM_F32):
+        """albedo_format / rsm_format: the G-buffer view's diffuse target and
+        the RSM views' flux and (d, d^2) targets (F32, or the reference's
+        SRGB8 / RGB16F + RG16F: then `albedo8`, `rsm_flux16` and `rsm_dls16`
+        are the buffers the views read, and the ray casters' F32 buffers are
+        only their sources). The output's shape follows the config's
+        output_format (RGB F32, or RGBA16F)."""
         import torch
         self.torch = torch
         self.lib = load()
@@ -152,7 +159,10 @@ class Pipeline:
         self.normal16 = torch.zeros((H, W, 2), dtype=torch.int16, device=dev)
         self.normal32 = torch.zeros((H, W, 3), dtype=torch.float32, device=dev)
         self.albedo = torch.zeros((H, W, 3), dtype=torch.float32, device=dev)
-        self.out = torch.zeros((H, W, 3), dtype=torch.float32, device=dev)
+        if hf.config.output_format == abi.OUTPUT_RGBA16F:
+            self.out = torch.zeros((H, W, 4), dtype=torch.float16, device=dev)
+        else:
+            self.out = torch.zeros((H, W, 3), dtype=torch.float32, device=dev)
         R = w.rsm_resolution
         self.rsm_flux = [torch.zeros((R, R, 3), dtype=torch.float32, device=dev) for _ in range(w.n_lights)]
         self.rsm_normal = [torch.zeros((R, R, 2), dtype=torch.int16, device=dev) for _ in range(w.n_lights)]
@@ -160,14 +170,23 @@ class Pipeline:
         # GBuffer_RoughnessMetalic (RG8 unorm), read by the specular apply.
         self.rough_metal = torch.zeros((H, W, 2), dtype=torch.uint8, device=dev)
         self.normal_format = normal_format
+        self.albedo8 = torch.zeros((H, W, 3), dtype=torch.uint8, device=dev) if albedo_format == abi.ALBEDO_SRGB8 \
+            else None
         self.gview = abi.DrvGBufferView(W, H, self.depth.data_ptr(),
                                         (self.normal16 if normal_format == abi.NORMAL_RG16I else self.normal32).data_ptr(),
-                                        normal_format, self.albedo.data_ptr(), abi.ALBEDO_F32X3,
-                                        self.rough_metal.data_ptr(), abi.ROUGH_METAL_RG8)
+                                        normal_format, (self.albedo8 if self.albedo8 is not None else self.albedo).data_ptr(),
+                                        albedo_format, self.rough_metal.data_ptr(), abi.ROUGH_METAL_RG8)
+        half = rsm_format == abi.RSM_F16
+        self.rsm_flux16 = [torch.zeros((R, R, 3), dtype=torch.float16, device=dev) for _ in range(w.n_lights)] \
+            if half else None
+        self.rsm_dls16 = [torch.zeros((R, R, 2), dtype=torch.float16, device=dev) for _ in range(w.n_lights)] \
+            if half else None
         self.rsm_views = (abi.DrvRSMView * w.n_lights)()
         for l in range(w.n_lights):
-            self.rsm_views[l] = abi.DrvRSMView(R, self.rsm_flux[l].data_ptr(), self.rsm_normal[l].data_ptr(),
-                                               self.rsm_dls[l].data_ptr(), abi.RSM_F32)
+            flux = self.rsm_flux16[l] if half else self.rsm_flux[l]
+            dls = self.rsm_dls16[l] if half else self.rsm_dls[l]
+            self.rsm_views[l] = abi.DrvRSMView(R, flux.data_ptr(), self.rsm_normal[l].data_ptr(), dls.data_ptr(),
+                                               rsm_format)
         # torch's pooled streams do not wait for its current stream, where the
         # buffers above were zeroed: finish that before any stage runs.
         torch.cuda.current_stream(self.device).synchronize()
@@ -411,6 +430,26 @@ class Pipeline:
 
 def scaled(w: Workload, **kw) -> Workload:
     return replace(w, **kw)
+
+
+def srgb_encode(lin):
+    """Linear [0, 1] -> SRGB8 bytes, the GL sRGB encoding (GL 4.5 section
+    17.3.9) rounded to the nearest byte: what an SRGB8 render target stores."""
+    import numpy as np
+    lin = np.clip(np.asarray(lin, np.float64), 0.0, 1.0)
+    cs = np.where(lin <= 0.0031308, lin * 12.92, 1.055 * lin ** (1 / 2.4) - 0.055)
+    return np.clip(np.rint(cs * 255.0), 0, 255).astype(np.uint8)
+
+
+def reference_format_inputs(p: "Pipeline"):
+    """A pipeline's ray-cast inputs (F32 buffers) as the reference's render
+    targets hold them: depth D32F, normal RG16I, diffuse SRGB8, and per light
+    the RSM's RGB16F flux, RG16I normal and RG16F (d, d^2) (numpy arrays)."""
+    import numpy as np
+    g = (p.depth.cpu().numpy(), p.normal16.cpu().numpy(), srgb_encode(p.albedo.cpu().numpy()))
+    rsm = [(p.rsm_flux[l].cpu().numpy().astype(np.float16), p.rsm_normal[l].cpu().numpy(),
+            p.rsm_dls[l].cpu().numpy().astype(np.float16)) for l in range(p.hf.workload.n_lights)]
+    return g, rsm
 
 
 def main(argv=None) -> int:

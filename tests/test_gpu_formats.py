@@ -19,10 +19,7 @@ def srgb_decode(b):
     return np.where(cs <= 0.04045, cs / 12.92, ((cs + 0.055) / 1.055) ** 2.4).astype(np.float32)
 
 
-def srgb_encode(lin):
-    lin = np.clip(np.asarray(lin, np.float64), 0.0, 1.0)
-    cs = np.where(lin <= 0.0031308, lin * 12.92, 1.055 * lin ** (1 / 2.4) - 0.055)
-    return np.clip(np.rint(cs * 255.0), 0, 255).astype(np.uint8)
+srgb_encode = pipeline.srgb_encode
 
 
 def test_decode_table_known_values():
