@@ -112,6 +112,7 @@ constexpr int kCullWarps = kCullThreads / 32;
 // CTA per cache: contributing blocks -> a contiguous run of the pair list.
 template <bool BF16>
 __global__ void __launch_bounds__(kCullThreads) cull_kernel(StageParams p, PairList L) {
+  pdl_wait_and_release();
   extern __shared__ uint32_t s_dyn[];  // [W] ballot words, [W] exclusive prefix of their popcounts
   __shared__ uint32_t s_warp[kCullWarps];
   __shared__ uint32_t s_base, s_count;
@@ -213,6 +214,7 @@ constexpr int kClassThreads = 256;
 // Thread per listed pair: its cone class; class totals in counters[8 + c].
 template <bool BF16>
 __global__ void __launch_bounds__(kClassThreads) classify_kernel(StageParams p, PairList L) {
+  pdl_wait_and_release();
   __shared__ uint32_t s_hist[kConeClasses];
   if (threadIdx.x < kConeClasses) s_hist[threadIdx.x] = 0u;
   __syncthreads();
@@ -241,6 +243,7 @@ constexpr int kScatterTile = 4 * kClassThreads;
 // to its class's region of L.order (regions in class order); a CTA reserves
 // its share of each region with one atomic per class.
 __global__ void __launch_bounds__(kClassThreads) scatter_kernel(PairList L) {
+  pdl_wait_and_release();
   __shared__ uint32_t s_region[kConeClasses], s_hist[kConeClasses], s_pos[kConeClasses];
   const uint32_t n = min(L.counters[0], L.cap);
   if (threadIdx.x < kConeClasses) {
@@ -277,6 +280,7 @@ __global__ void __launch_bounds__(kClassThreads) scatter_kernel(PairList L) {
 // L.order, every listed pair in class order.
 template <bool BF16, bool RETRACE>
 __global__ void __launch_bounds__(128) cone_kernel(StageParams p, PairList L) {
+  pdl_wait_and_release();
   uint32_t nf = 0, nb = 0;
   if (RETRACE) {
     nf = min(L.counters[3], L.cap);
@@ -323,6 +327,7 @@ constexpr int kGatherWarps = kGatherThreads / 32;
 // CTA per cache: SH gather of the cache's pairs with their shadowing.
 template <int NK, bool BF16>
 __global__ void __launch_bounds__(kGatherThreads) gather_kernel(StageParams p, PairList L) {
+  pdl_wait_and_release();
   constexpr bool KAHAN = BF16;  // FP32 accumulation of BF16-stored results, compensated
   __shared__ float s_red[kGatherWarps][NK * 3];
   __shared__ uint32_t s_count[kGatherWarps];  // list-full path: contributing blocks per warp
@@ -500,14 +505,25 @@ __global__ void __launch_bounds__(kThreads, 8) light_kernel(FusedParams fp) {
 }
 
 // Launch of CTAs_PER_SM x SMs CTAs (at most what fits), or a full persistent grid.
+// after: launched with programmatic stream serialisation (launch_after).
 template <typename... KArgs, typename... Args>
 cudaError_t launch_grid(void (*kernel)(KArgs...), int threads, size_t smem, cudaStream_t s, int num_sms,
-                        int ctas_per_sm, const Args&... args) {
+                        int ctas_per_sm, bool after, const Args&... args) {
   int per_sm = resident_ctas(reinterpret_cast<const void*>(kernel), threads, smem);
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
   if (ctas_per_sm > 0 && ctas_per_sm < per_sm) per_sm = ctas_per_sm;
+  if (after) return launch_after(kernel, num_sms * per_sm, threads, smem, s, args...);
   kernel<<<num_sms * per_sm, threads, smem, s>>>(args...);
   return cudaGetLastError();
+}
+
+// launch_persistent with programmatic stream serialisation.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_persistent_after(void (*kernel)(KArgs...), int threads, size_t smem, cudaStream_t s, int num_sms,
+                                    const Args&... args) {
+  const int per_sm = resident_ctas(reinterpret_cast<const void*>(kernel), threads, smem);
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  return launch_after(kernel, num_sms * per_sm, threads, smem, s, args...);
 }
 
 // events (optional, DRV_LK_COUNT + 1): recorded before the first kernel and
@@ -527,23 +543,25 @@ cudaError_t split_variant(cudaStream_t s, const StageParams& p, const PairList& 
   if ((e = launch_persistent(cull_kernel<BF16>, kCullThreads, cull_smem, s, num_sms, p, L)) != cudaSuccess) return e;
   if ((e = mark(DRV_LK_CLASSIFY)) != cudaSuccess) return e;
   if (!weights) {
-    if ((e = launch_persistent(classify_kernel<BF16>, kClassThreads, 0, s, num_sms, p, L)) != cudaSuccess) return e;
+    if ((e = launch_persistent_after(classify_kernel<BF16>, kClassThreads, 0, s, num_sms, p, L)) != cudaSuccess)
+      return e;
     if ((e = mark(DRV_LK_SCATTER)) != cudaSuccess) return e;
-    if ((e = launch_persistent(scatter_kernel, kClassThreads, 0, s, num_sms, L)) != cudaSuccess) return e;
+    if ((e = launch_persistent_after(scatter_kernel, kClassThreads, 0, s, num_sms, L)) != cudaSuccess) return e;
     if ((e = mark(DRV_LK_MLP)) != cudaSuccess || (e = wait_voxels()) != cudaSuccess ||
         (e = mark(DRV_LK_CONE)) != cudaSuccess)
       return e;
-    e = launch_grid(cone_kernel<BF16, false>, 128, 0, s, num_sms, cone_ctas, p, L);
+    e = launch_grid(cone_kernel<BF16, false>, 128, 0, s, num_sms, cone_ctas, true, p, L);
   } else {
     if ((e = mark(DRV_LK_SCATTER)) != cudaSuccess || (e = wait_voxels()) != cudaSuccess ||
         (e = mark(DRV_LK_MLP)) != cudaSuccess)
       return e;
     if ((e = launch_surrogate_mlp(s, p, L, weights, conf_threshold, BF16, num_sms)) != cudaSuccess) return e;
     if ((e = mark(DRV_LK_CONE)) != cudaSuccess) return e;
-    e = launch_grid(cone_kernel<BF16, true>, 128, 0, s, num_sms, cone_ctas, p, L);
+    e = launch_grid(cone_kernel<BF16, true>, 128, 0, s, num_sms, cone_ctas, true, p, L);
   }
   if (e != cudaSuccess || (e = mark(DRV_LK_GATHER)) != cudaSuccess) return e;
-  if ((e = launch_grid(gather_kernel<NK, BF16>, kGatherThreads, 0, s, num_sms, gather_ctas, p, L)) != cudaSuccess)
+  if ((e = launch_grid(gather_kernel<NK, BF16>, kGatherThreads, 0, s, num_sms, gather_ctas, true, p, L)) !=
+      cudaSuccess)
     return e;
   return mark(DRV_LK_COUNT);
 }

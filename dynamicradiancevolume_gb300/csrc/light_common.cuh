@@ -79,6 +79,35 @@ cudaError_t launch_persistent(void (*kernel)(KArgs...), int threads, size_t smem
   return cudaGetLastError();
 }
 
+// Programmatic dependent launch within the split light stage: a grid waits
+// here until the previous grid of the stream has completed and its writes
+// are visible (a no-op when it was launched without the attribute), then
+// lets the next grid of the stream launch, so that the next grid's launch and
+// CTA placement overlap this grid's tail.
+__device__ __forceinline__ void pdl_wait_and_release() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// Host: a launch that may start before the previous kernel of the stream
+// has finished (it must call pdl_wait_and_release before reading that
+// kernel's output).
+template <typename... KArgs, typename... Args>
+cudaError_t launch_after(void (*kernel)(KArgs...), int blocks, int threads, size_t smem, cudaStream_t s,
+                         const Args&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)blocks);
+  cfg.blockDim = dim3((unsigned)threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 __device__ __forceinline__ uint32_t cache_count(const StageParams& p) {
   return min((uint32_t)max(p.counter->total_light_cache_count, 0), p.max_caches);
 }
