@@ -325,8 +325,11 @@ constexpr int kGatherThreads = 256;
 constexpr int kGatherWarps = kGatherThreads / 32;
 
 // CTA per cache: SH gather of the cache's pairs with their shadowing.
+// Three CTAs per SM fit the FP32 instances without spilling (30.7 -> 26.6 us
+// at 1080p / 4096 VPLs); the BF16 instances, with Kahan sums, spill there
+// and keep two (32.8 us against 36.3).
 template <int NK, bool BF16>
-__global__ void __launch_bounds__(kGatherThreads) gather_kernel(StageParams p, PairList L) {
+__global__ void __launch_bounds__(kGatherThreads, BF16 ? 2 : 3) gather_kernel(StageParams p, PairList L) {
   pdl_wait_and_release();
   constexpr bool KAHAN = BF16;  // FP32 accumulation of BF16-stored results, compensated
   __shared__ float s_red[kGatherWarps][NK * 3];
