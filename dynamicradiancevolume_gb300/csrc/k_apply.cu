@@ -231,9 +231,9 @@ __device__ __forceinline__ void store_output(const ApplyParams& p, size_t i, f3 
 
 // Five CTAs per SM (48 registers, a few bytes spilled) hide more of the
 // corner loads' latency than four: 0.1215 -> 0.1152 ms (FP32) and 0.1052 ->
-// 0.1013 ms (BF16) at 1080p. The specular instances keep their registers.
+// 0.1013 ms (BF16) at 1080p; the specular instances at three (80 registers).
 template <bool BF16, bool SH2, bool SPEC>
-__global__ void __launch_bounds__(256, SPEC ? 2 : 5) apply_kernel(ApplyParams p) {
+__global__ void __launch_bounds__(256, SPEC ? 3 : 5) apply_kernel(ApplyParams p) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
   if (x >= p.w || y >= p.h) return;
   const size_t i = (size_t)y * p.w + x;
