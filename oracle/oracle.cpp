@@ -669,7 +669,10 @@ d3 mesh_normal(const MeshIn& m, int k, double l1, double l2, d3 d) {
     const d3 v0 = mesh_vertex(m, v[0]);
     n = cross(mesh_vertex(m, v[1]) - v0, mesh_vertex(m, v[2]) - v0);
   }
-  n = normalize(n);
+  // Normalised through the largest component first, so that an axis-aligned
+  // normal comes out exactly (+-1 on its axis, as the box casters give it).
+  const double big = std::max(std::max(std::fabs(n.x), std::fabs(n.y)), std::fabs(n.z));
+  n = big > 0.0 ? normalize(d3{n.x / big, n.y / big, n.z / big}) : d3{0.0, 0.0, 1.0};
   if (dot(n, d) > 0.0) n = n * -1.0;
   return d3{n.x + 0.0, n.y + 0.0, n.z + 0.0};  // no negative zeros (they pack to the other end of the atan2 range)
 }

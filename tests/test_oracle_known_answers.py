@@ -360,3 +360,43 @@ def test_specular_prepare_known_answer(oracle):
         live = parent.sum(-1) >= 1e-4
         assert np.all(kids.sum(-1).min(axis=(1, 3))[live] > 0)  # no holes under a lit parent
         np.testing.assert_allclose(kids.mean(axis=(1, 3))[live], parent[live], rtol=2e-2)
+
+
+def test_mesh_ray_caster_equals_box_caster_on_box_scenes(oracle):
+    """The box scene given as triangles (12 per box): the FP64 mesh ray
+    caster reproduces the box ray caster exactly, G-buffer and RSM, when no
+    surface is closer to the light than its near plane."""
+    from dynamicradiancevolume_gb300 import pipeline
+    w = pipeline.scaled(pipeline.WORKLOADS["c1_small"], width=96, height=64, rsm_resolution=32)
+    hf = pipeline.host_frame(w, 5)
+    boxes = [hf.boxes[i] for i in range(hf.scene.n_boxes)]
+    tris = np.concatenate([_box_triangles(b.min[:3], b.max[:3]) for b in boxes])
+    alb = np.repeat(np.array([b.albedo[:3] for b in boxes], np.float32), 12, axis=0)
+    d0, n0, m0, a0 = oracle.raycast_gbuffer(hf.boxes, hf.scene.n_boxes, hf.frame, hf.camera, w.width, w.height)
+    d1, n1, m1, a1 = oracle.raycast_gbuffer_mesh(tris, None, alb, None, hf.frame, hf.camera, w.width, w.height)
+    assert np.array_equal(n0, n1) and np.array_equal(a0, a1)
+    np.testing.assert_allclose(d1, d0, rtol=1e-6, atol=0)
+    f0, r0, l0 = oracle.raycast_rsm(hf.boxes, hf.scene.n_boxes, hf.lights[0])
+    f1, r1, l1 = oracle.raycast_rsm_mesh(tris, None, alb, None, hf.lights[0])
+    assert l0[..., 0].min() > hf.light_descs[0].near_plane
+    assert np.array_equal(r0, r1)
+    np.testing.assert_allclose(l1, l0, rtol=1e-6, atol=0)
+    np.testing.assert_allclose(f1, f0, rtol=1e-5, atol=1e-12)
+
+
+def test_mesh_ray_caster_clips_at_the_near_plane(oracle):
+    """A light with a box inside its near plane: the rasteriser (and the mesh
+    caster) clip that surface and see what lies behind it, the box caster
+    (no near plane) sees the box."""
+    from dynamicradiancevolume_gb300 import pipeline
+    w = pipeline.scaled(pipeline.WORKLOADS["c1_small"], rsm_resolution=32)
+    hf = pipeline.host_frame(w, 9)
+    near = hf.light_descs[0].near_plane
+    boxes = [hf.boxes[i] for i in range(hf.scene.n_boxes)]
+    tris = np.concatenate([_box_triangles(b.min[:3], b.max[:3]) for b in boxes])
+    _, _, l0 = oracle.raycast_rsm(hf.boxes, hf.scene.n_boxes, hf.lights[0])
+    _, _, l1 = oracle.raycast_rsm_mesh(tris, None, None, None, hf.lights[0])
+    assert l0[..., 0].min() < near  # the box caster sees a surface inside the near plane
+    assert l1[..., 0][l1[..., 0] > 0].min() >= near  # the mesh caster never does
+    closer = l0[..., 0] < near
+    assert np.all(l1[..., 0][closer] > l0[..., 0][closer])  # it sees what lies behind instead
