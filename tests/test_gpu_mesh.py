@@ -143,3 +143,29 @@ def test_frame_from_a_mesh(lib, cuda, oracle):
     assert np.linalg.norm(out - ref) / np.linalg.norm(ref) < 0.05
     p.close()
     q.close()
+
+
+def test_indexed_mesh_equals_triangle_soup(lib, cuda, oracle):
+    """The same triangles given once as a soup and once as shared vertices +
+    indices rasterise to the same G-buffer and RSM, bit for bit; the F32
+    normal target holds the normal the RG16I target packs."""
+    torch = pytest.importorskip("torch")
+    oracle_unpack = oracle.unpack_normal16i
+    w = pipeline.scaled(pipeline.WORKLOADS["c1_small"], rsm_resolution=64)
+    p = pipeline.Pipeline(pipeline.host_frame(w, 3))
+    tris, alb = _box_mesh(p.hf)
+    _raster_inputs(p, lib, Mesh(torch, p.device, tris, None, alb))
+    g0, r0 = _snapshot(p)
+    n32 = p.normal32.cpu().numpy()
+    uniq, inv = np.unique(tris.reshape(-1, 3), axis=0, return_inverse=True)
+    _raster_inputs(p, lib, Mesh(torch, p.device, uniq, None, alb, indices=inv.reshape(-1, 3)))
+    g1, r1 = _snapshot(p)
+    for k in g0:
+        assert np.array_equal(g0[k], g1[k]), k
+    for a, b in zip(r0, r1):
+        assert all(np.array_equal(x, y) for x, y in zip(a, b))
+    live = g0["depth"] != 0
+    np.testing.assert_allclose(np.linalg.norm(n32[live], axis=-1), 1.0, atol=1e-6)
+    un = np.stack([oracle_unpack(v) for v in g0["normal16"][live][::53]])
+    assert np.all(np.sum(un * n32[live][::53], -1) > 0.9999)
+    p.close()

@@ -179,3 +179,43 @@ def test_specular_config_and_inputs_are_checked(lib, cuda):
     q.apply()
     q.sync()
     q.close()
+
+
+def test_rough_metal_f32_equals_rg8(lib, oracle, cuda):
+    """The roughness / metallic target as RG F32 holding byte / 255 gives the
+    frame the reference's RG8 target gives, bit for bit."""
+    torch = pytest.importorskip("torch")
+    r = Run(SPEC_C1, oracle, seed=2)
+    q = r.pipe
+    rm32 = torch.from_numpy(r.rough_metal.copy()).to(q.device)
+    torch.cuda.synchronize()
+    g = abi.DrvGBufferView.from_buffer_copy(q.gview)
+    g.rough_metal, g.rough_metal_format = rm32.data_ptr(), abi.ROUGH_METAL_F32
+    out = torch.zeros_like(q.out)
+    assert lib.drv_apply(q.ctx, C.byref(g), C.byref(q.hf.frame), C.byref(q.hf.volume),
+                         C.c_void_p(out.data_ptr())) == abi.OK
+    q.sync()
+    assert np.array_equal(out.cpu().numpy(), r.out)
+
+
+def test_bf16_specular_frame_within_one_percent_of_fp64(lib, oracle, cuda):
+    """BF16 storage with the specular path: the frame against the FP64 chain."""
+    r = Run(pipeline.scaled(SPEC_C1, precision=abi.PRECISION_BF16), oracle, seed=5)
+    cfg = r.hf.config
+    vp = r.oracle_vpls()
+    bits = oracle.voxelize(r.hf.boxes, r.hf.scene.n_boxes, r.hf.volume, r.w.voxel_res)
+    mips = oracle.build_mips(r.w.voxel_res, bits)
+    c32 = abi.DrvConfig.from_buffer_copy(cfg)
+    c32.precision = abi.PRECISION_FP32
+    st, atlas, pos, count = oracle.allocate_caches(c32, r.hf.volume, r.hf.frame, r.depth)
+    sh, env = oracle.light_caches_specular(c32, r.hf.volume, pos, r.hf.frame.camera_position[:], r.hf.lights,
+                                           [v for v, _ in vp], [c for _, c in vp], bits, mips)
+    S = r.w.specular_envmap_size
+    e = np.zeros((env.shape[0], oracle.specular_levels(S)[-1]), np.uint32)
+    e[:, :S * S] = oracle.encode_r11g11b10(env).reshape(env.shape[0], S * S)
+    e = oracle.specular_prepare(S, r.w.specular_fill_level, e)
+    ref = oracle.apply_specular(c32, r.hf.volume, r.hf.frame, r.depth, r.n16, abi.NORMAL_RG16I, r.albedo,
+                                r.rough_metal, atlas, sh, e)
+    err = rel_l2(r.out, ref)
+    print("bf16 specular frame rel-L2 %.3e" % err)
+    assert err < 1e-2
