@@ -11,7 +11,10 @@
 //    shadow).
 //  * envmap_prepare_kernel (a CTA per cache) computes the mip levels
 //    (specularenvmap_mipmap.frag) and the optional hole fill
-//    (specularenvmap_fillholes.frag) of each allocated cache's envmap.
+//    (specularenvmap_fillholes.frag) of each allocated cache's envmap, and
+//    writes the apply's per-cache FP16 copy of every level (R11/G11/B10
+//    values are FP16 values, so the copy is exact and the apply reads its
+//    texels without unpacking).
 //
 // Differences from the reference, each exact to FP32 rounding or documented:
 //  - the sum is formed in FP32 and rounded to R11F_G11F_B10F once (the
