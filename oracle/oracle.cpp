@@ -1165,6 +1165,8 @@ double decode_ufloat(uint32_t v, int mbits) {
 }
 }  // namespace
 
+void orc_hemi_projection(const double d[3], double uv[2]) { hemi_projection(d3{d[0], d[1], d[2]}, uv[0], uv[1]); }
+
 uint32_t orc_encode_r11g11b10(const double rgb[3]) {
   return encode_ufloat(rgb[0], 6) | encode_ufloat(rgb[1], 6) << 11 | encode_ufloat(rgb[2], 5) << 22;
 }

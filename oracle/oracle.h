@@ -108,6 +108,9 @@ void orc_light_caches_specular(const DrvConfig* cfg, const DrvVolumeInfo* vol, i
                                const double* const* vpls, const double* const* cones, const int* n_vpls,
                                const uint32_t* bits, const double* mips, double* sh_out, double* env_out,
                                int n_threads);
+/* HemisphericalProjection (utils.glsl:103-170, concentric square map) of a
+ * direction of the z+ hemisphere to [0, 1]^2. */
+void orc_hemi_projection(const double d[3], double uv[2]);
 /* R11F_G11F_B10F (GL packed float: R bits 0-10, G 11-21, B 22-31). */
 uint32_t orc_encode_r11g11b10(const double rgb[3]);
 void orc_encode_r11g11b10_n(const double* rgb, int64_t n, uint32_t* out);

@@ -74,6 +74,7 @@ def load():
         "orc_bruteforce_rsm": (None, [P(abi.DrvPerFrame), I, I, VP, VP, VP, VP, I, P(VP), P(I), VP, I]),
         "orc_light_caches_specular": (None, [P(abi.DrvConfig), P(abi.DrvVolumeInfo), I, VP, VP, I,
                                              P(abi.DrvSpotLight), P(VP), P(VP), P(I), VP, VP, VP, VP, I]),
+        "orc_hemi_projection": (None, [P(D), P(D)]),
         "orc_encode_r11g11b10": (C.c_uint32, [P(D)]),
         "orc_encode_r11g11b10_n": (None, [VP, C.c_int64, VP]),
         "orc_decode_r11g11b10": (None, [C.c_uint32, P(D)]),
@@ -316,6 +317,12 @@ def light_caches_specular(cfg, vol, positions, cam, lights, vpls, cones, bits, m
     load().orc_light_caches_specular(C.byref(cfg), C.byref(vol), n, _p(positions), _p(cam), L, lights, vp, cp, nv,
                                      _p(bits), _p(mips), _p(sh), _p(env), n_threads)
     return sh, env
+
+
+def hemi_projection(d) -> tuple:
+    out = (C.c_double * 2)()
+    load().orc_hemi_projection((C.c_double * 3)(*d), out)
+    return out[0], out[1]
 
 
 def encode_r11g11b10(rgb) -> np.ndarray:

@@ -400,3 +400,87 @@ def test_mesh_ray_caster_clips_at_the_near_plane(oracle):
     assert l1[..., 0][l1[..., 0] > 0].min() >= near  # the mesh caster never does
     closer = l0[..., 0] < near
     assert np.all(l1[..., 0][closer] > l0[..., 0][closer])  # it sees what lies behind instead
+
+
+def test_hemispherical_projection_known_answers(oracle):
+    """The concentric square map (utils.glsl:103-170): the pole to the centre,
+    the horizon's axis directions to the edge midpoints, the diagonal to the
+    corner's direction; a direction and its mirror image are mirrored."""
+    pts = {(0, 0, 1): (0.5, 0.5), (1, 0, 0): (1.0, 0.5), (0, 1, 0): (0.5, 1.0), (-1, 0, 0): (0.0, 0.5),
+           (0, -1, 0): (0.5, 0.0)}
+    for d, uv in pts.items():
+        assert np.allclose(oracle.hemi_projection(d), uv, atol=1e-12), d
+    s = math.sqrt(0.5)
+    u, v = oracle.hemi_projection((s, s, 0.0))  # phi = 1: the corner of the square's right edge
+    assert np.allclose((u, v), (1.0, 1.0), atol=1e-12)
+    rng = np.random.default_rng(1)
+    for _ in range(50):
+        d = rng.normal(size=3)
+        d[2] = abs(d[2])
+        d /= np.linalg.norm(d)
+        u, v = oracle.hemi_projection(d)
+        um, vm = oracle.hemi_projection((-d[0], d[1], d[2]))
+        assert 0.0 <= u <= 1.0 and 0.0 <= v <= 1.0
+        assert abs(um - (1.0 - u)) < 1e-9 and abs(vm - v) < 1e-9
+
+
+def test_specular_envmap_of_one_vpl_known_answer(oracle):
+    """One cache, one VPL, no shadow: the level-0 envmap holds one texel, at
+    the concentric projection of the cache-local half vector, with
+    flux * saturate(n . -l) / (d^2 + area) * saturate(h . l) * (S^2 + 7) / (8 pi)
+    (cacheLightingRSM.comp:234-335); the SH are unchanged by the specular
+    path when the flux passes its 0.001 threshold."""
+    S = 16
+    cfg = abi.DrvConfig()
+    cfg.sh_order, cfg.indirect_shadow, cfg.voxel_res, cfg.max_cone_steps = 2, 0, 32, 4
+    cfg.specular_envmap_size = S
+    vol = _volume(abi, 32)
+    L = (abi.DrvSpotLight * 1)()
+    L[0].indirect_shadow_sample_interval = 1
+    c = np.array([[0.3, 0.4, 0.5]], np.float32)
+    cam = np.array([0.9, 0.7, 0.1], np.float32)
+    p, n = np.array([0.6, 0.2, 0.9]), np.array([-0.6, 0.3, -0.74])
+    n = n / np.linalg.norm(n)
+    vpl = np.array([[0.5, 0.25, 0.125, 0.01, *p, *n]])
+    bits = np.zeros(32 ** 3 // 32, np.uint32)
+    mips = np.zeros(oracle.n_mip_values(32))
+    sh, env = oracle.light_caches_specular(cfg, vol, c, cam, L, [vpl], [np.zeros((1, 4))], bits, mips)
+    # independent restatement
+    cc, camd = c[0].astype(np.float64), cam.astype(np.float64)
+    z = (camd - cc) / np.linalg.norm(camd - cc)
+    x = np.array([z[2], 0.0, -z[0]]) / np.linalg.norm([z[2], 0.0, -z[0]])
+    y = np.cross(z, x)
+    t = p - cc
+    d2 = t @ t
+    l = t / math.sqrt(d2)
+    g = max(0.0, min(1.0, -(n @ l))) / (d2 + 0.01)
+    ll = np.array([l @ x, l @ y, l @ z])
+    h = ll + np.array([0.0, 0.0, 1.0])
+    h /= np.linalg.norm(h)
+    r = math.sqrt(max(0.0, 1.0 - h[2])) * 0.5
+    phi = math.atan2(h[1], h[0]) * 4.0 / 3.14159265358979
+    if phi < -1:
+        phi += 8
+    if phi < 1:
+        uv = (r, phi * r)
+    elif phi < 3:
+        uv = (-(phi - 2) * r, r)
+    elif phi < 5:
+        uv = (-r, -(phi - 4) * r)
+    else:
+        uv = ((phi - 6) * r, -r)
+    tx, ty = (min(max(int((q + 0.5) * S + 0.5), 0), S - 1) for q in uv)
+    k = g * max(0.0, min(1.0, h @ ll)) * (S * S + 7) / (8 * 3.14159265358979)
+    nz = np.argwhere(env[0].sum(-1) > 0)
+    assert nz.tolist() == [[ty, tx]]
+    np.testing.assert_allclose(env[0, ty, tx], vpl[0, :3] * k, rtol=1e-12)
+    # the SH of the same VPL without the specular path are the same (flux sum 0.875 >= 0.001)
+    cfg0 = abi.DrvConfig.from_buffer_copy(cfg)
+    cfg0.specular_envmap_size = 0
+    sh0 = oracle.light_caches(cfg0, vol, c, L, [vpl], [np.zeros((1, 4))], bits, mips)
+    np.testing.assert_allclose(sh, sh0, rtol=0, atol=0)
+    # a VPL below the threshold adds nothing with specular on
+    dim = vpl.copy()
+    dim[0, :3] = 0.0003
+    sh_dim, env_dim = oracle.light_caches_specular(cfg, vol, c, cam, L, [dim], [np.zeros((1, 4))], bits, mips)
+    assert not sh_dim.any() and not env_dim.any()
