@@ -49,8 +49,8 @@ __device__ __forceinline__ float decode_ufloat(uint32_t v, int mbits) {
 // The same decode in three instructions for a finite code: its exponent and
 // mantissa fields moved into a binary32 give (1 + m 2^-mbits) 2^(e - 127), or
 // the denormal m 2^-(mbits + 126) when e = 0, and the product with 2^112 is
-// the code's value, exactly (denormals are not flushed in this build). The
-// all-ones exponent (infinity, NaN) takes the general path.
+// the code's value, exactly (the library is compiled without flushing
+// denormals). The all-ones exponent (infinity, NaN) takes the general path.
 __device__ __forceinline__ float decode_ufloat_fast(uint32_t v, int mbits) {
   const float x = __fmul_rn(__uint_as_float(v << (23 - mbits)), 0x1p112f);
   return (v >> mbits) == 31u ? decode_ufloat(v, mbits) : x;

@@ -4,7 +4,7 @@
  *
  * TEST INFRASTRUCTURE ONLY. Nothing in the product links, imports or calls
  * this library; only the tests, the smoke check and the CPU-baseline leg of
- * the benchmark do, and only as the checker.
+ * the benchmark do, and only to check results against.
  *
  * The reference is GLSL inside a Windows/OpenGL 4.5 application; it cannot
  * run without a graphics stack, so parity is anchored on this restatement.

@@ -1,7 +1,7 @@
 """ctypes binding of the FP64 oracle (oracle/_build/liboracle.so).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, the smoke check and the
-CPU-baseline leg of bench.py, as the checker. Arrays are numpy; layouts are
+CPU-baseline leg of bench.py, to check results against. Arrays are numpy; layouts are
 those of include/drv.h.
 """
 from __future__ import annotations
