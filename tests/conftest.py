@@ -12,6 +12,15 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
 
 
+@pytest.fixture(scope="session", autouse=True)
+def _product_built():
+    """Builds libdrv_gb300.so (incremental: nothing to do when it is up to
+    date), so that the suite also runs from a fresh checkout; a build that
+    fails fails the session."""
+    from dynamicradiancevolume_gb300 import build
+    build.build()
+
+
 @pytest.fixture(scope="session")
 def oracle():
     import oracle_py
@@ -22,8 +31,8 @@ def oracle():
 
 @pytest.fixture(scope="session")
 def lib():
-    """The product library; building it is the build step's job, so a missing
-    library is an error here, not a skip."""
+    """The product library (built by `_product_built`); a library that does
+    not load is an error here, not a skip."""
     import dynamicradiancevolume_gb300 as drv
     return drv.load()
 
