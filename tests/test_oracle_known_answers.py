@@ -484,3 +484,40 @@ def test_specular_envmap_of_one_vpl_known_answer(oracle):
     dim[0, :3] = 0.0003
     sh_dim, env_dim = oracle.light_caches_specular(cfg, vol, c, cam, L, [dim], [np.zeros((1, 4))], bits, mips)
     assert not sh_dim.any() and not env_dim.any()
+
+
+def test_specular_apply_of_a_constant_envmap(oracle):
+    """Zero SH and the same constant envmap in every cache (all levels): every
+    lit pixel's radiance is that constant times the specular colour,
+    0.04 (1 - metallic) + albedo * metallic (lightingfunctions.glsl:41-49),
+    times the weight of its live corners, whatever its lookup and lod. The
+    weight (1 where all 8 corners are allocated; less where the reference's
+    tile dedupe or the atlas edge left some out; blended across a cascade
+    transition) is the diffuse apply's output for unit irradiance and an
+    albedo of pi."""
+    from dynamicradiancevolume_gb300 import pipeline
+    w = pipeline.scaled(pipeline.WORKLOADS["c1_small"], width=64, height=48, specular_envmap_size=8)
+    hf = pipeline.host_frame(w, 5)
+    depth, n16, _, albedo = oracle.raycast_gbuffer(hf.boxes, hf.scene.n_boxes, hf.frame, hf.camera, w.width,
+                                                   w.height)
+    st, atlas, pos, count = oracle.allocate_caches(hf.config, hf.volume, hf.frame, depth)
+    E = np.array([0.75, 0.5, 0.25])
+    words = oracle.specular_levels(8)[-1]
+    env = np.full((count, words), int(oracle.encode_r11g11b10(E)), np.uint32)
+    sh = np.zeros((count, 27))
+    rng = np.random.default_rng(3)
+    rm = (rng.integers(0, 256, (w.height, w.width, 2)).astype(np.float32) / np.float32(255.0))
+    out = oracle.apply_specular(hf.config, hf.volume, hf.frame, depth, n16, abi.NORMAL_RG16I, albedo, rm, atlas, sh,
+                                env)
+    lit = depth >= 1e-5
+    # corner weights: unit irradiance (SH00 = 1 / its cosine-lobe response), albedo pi
+    f0 = oracle.sh_irradiance(2, 0, np.eye(1, 27).ravel(), (0.0, 0.0, 1.0))[0]
+    unit = np.zeros((count, 27))
+    unit[:, 0:3] = 1.0 / f0
+    wsum = oracle.apply(hf.config, hf.volume, hf.frame, depth, n16, abi.NORMAL_RG16I,
+                        np.full_like(albedo, np.float32(3.14159265358979)), atlas, unit)[..., 0:1]
+    m = rm[..., 1:2].astype(np.float64)
+    expect = wsum * E * (0.04 * (1.0 - m) + albedo.astype(np.float64) * m)
+    np.testing.assert_allclose(out[lit], expect[lit], rtol=1e-6, atol=1e-12)
+    assert np.mean(np.abs(wsum[lit] - 1.0) < 1e-6) > 0.9  # most pixels have all 8 corners (pi passed in binary32)
+    assert not out[~lit].any()
