@@ -229,7 +229,7 @@ drv_status drv_create(const DrvConfig* cfg, DrvContext** out) {
   if ((e = cudaEventCreateWithFlags(&c->vox_fork_ev, cudaEventDisableTiming)) != cudaSuccess) return bail(e);
   // LightCacheBuffer: 64 B (SH1) or 128 B (SH2) entries (lightcache.glsl:33-76);
   // DrvCacheEntryBF16 (64 B) in BF16 precision.
-  c->entry_stride = cfg->precision == DRV_PRECISION_BF16 ? 64u : (cfg->sh_order == 2 ? 128u : 64u);
+  c->entry_stride = drv::entry_stride_for(*cfg);
   if ((e = cudaMalloc(&c->entries, (size_t)cfg->max_caches * c->entry_stride)) != cudaSuccess) return bail(e);
   c->atlas_words = (size_t)cfg->n_cascades * cfg->cav_res * cfg->cav_res * cfg->cav_res;
   if ((e = cudaMalloc(&c->atlas, c->atlas_words * 4)) != cudaSuccess) return bail(e);

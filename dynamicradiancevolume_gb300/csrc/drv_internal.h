@@ -76,6 +76,13 @@ inline int record_levels_for(int precision, int n_levels) {
   return precision == DRV_PRECISION_BF16 ? L : (L < 3 ? L : 3);
 }
 
+// Bytes between consecutive cache entries: DrvCacheEntryBF16 (64 B) with BF16
+// precision, else LightCacheEntry std430 (lightcache.glsl:33-76): 64 B for
+// SH1, 128 B for SH2. Every path that addresses entries takes it from here.
+inline uint32_t entry_stride_for(const DrvConfig& cfg) {
+  return cfg.precision == DRV_PRECISION_BF16 ? 64u : (cfg.sh_order == 2 ? 128u : 64u);
+}
+
 // Device scratch of the light stage. partials: [max_caches * max_chunks][27]
 // chunk sums; tickets: one per cache; work: {next unit, retired CTAs}. Tickets
 // and work are zero between launches (each launch leaves them zero).

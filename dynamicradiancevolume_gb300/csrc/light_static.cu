@@ -20,7 +20,13 @@
 //    kernel runs, and calls that overlap on the GPU (different streams, no
 //    ordering) race on it;
 //  - at most DRV_STATIC_SCRATCH_MAX_CACHES caches; a config with a larger
-//    max_caches is rejected with DRV_ERR_CAPACITY.
+//    max_caches is rejected with DRV_ERR_CAPACITY;
+//  - FP32 precision only: the inputs are DrvVPL arrays and FP32 mips, the
+//    entries LightCacheEntry std430 (64 B for SH1, 128 B for SH2). A BF16
+//    config is rejected with DRV_ERR_INVALID_ARG before anything is launched;
+//  - the array's device address is looked up once per device ordinal, in the
+//    context current at that first call: callers use the device's primary
+//    context (the runtime API's, as torch and most engines do).
 #include <mutex>
 
 #include "drv_internal.h"
@@ -72,6 +78,10 @@ extern "C" drv_status drv_light_caches_static_scratch(const DrvConfig* cfg, cons
   if (n_lights > 0 && (!vpls || !n_vpls || !intervals)) return DRV_ERR_INVALID_ARG;
   if (cfg->indirect_shadow && (!cones || !voxel_corners || !voxel_mips)) return DRV_ERR_INVALID_ARG;
   if (cfg->sh_order != 1 && cfg->sh_order != 2) return DRV_ERR_INVALID_ARG;
+  // The declared inputs are FP32 (DrvVPL, float mips) and so are the entries:
+  // a BF16 config would make the kernel read DrvVPLBF16 / half mips and
+  // address entries with another stride than the caller's buffer.
+  if (cfg->precision != DRV_PRECISION_FP32) return DRV_ERR_INVALID_ARG;
   if (cfg->specular_envmap_size != 0) return DRV_ERR_INVALID_ARG;  // the envmap atlas belongs to a context
   if (cfg->voxel_res < 32 || cfg->voxel_res > 1024 || (cfg->voxel_res & (cfg->voxel_res - 1)))
     return DRV_ERR_INVALID_ARG;
@@ -102,7 +112,7 @@ extern "C" drv_status drv_light_caches_static_scratch(const DrvConfig* cfg, cons
     const size_t n = (size_t)(cfg->voxel_res >> l);
     off += n * n * n;
   }
-  const uint32_t stride = cfg->sh_order == 2 ? 128u : 64u;
+  const uint32_t stride = drv::entry_stride_for(*cfg);
   const drv::VoxelInputs vox{voxel_corners, voxel_mips, offsets};
   cudaError_t e = drv::launch_light_caches(s, *cfg, *vol, ll, counter, cache_entries, stride, vox, ls, num_sms);
   return e == cudaSuccess ? DRV_OK : DRV_ERR_CUDA;

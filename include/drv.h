@@ -642,8 +642,12 @@ drv_status drv_batch_destroy(DrvBatch* batch);
  *  - max_caches above DRV_STATIC_SCRATCH_MAX_CACHES returns DRV_ERR_CAPACITY;
  *  - specular_envmap_size > 0 returns DRV_ERR_INVALID_ARG (the envmap atlas
  *    belongs to a context);
- *  - the first call on a device looks the array up on that device; make it
- *    before any stream capture;
+ *  - FP32 precision only (DrvVPL inputs, FP32 mips, LightCacheEntry std430
+ *    entries of 64 B for SH1 and 128 B for SH2): precision BF16 returns
+ *    DRV_ERR_INVALID_ARG and launches nothing;
+ *  - the first call on a device looks the array up on that device, in the
+ *    context current then (use the device's primary context, as the CUDA
+ *    runtime does); make it before any stream capture;
  *  - all calls share the array (it keeps the last call's contents; each call
  *    clears the tickets first): calls that overlap on the GPU race. */
 #define DRV_STATIC_SCRATCH_MAX_CACHES 4096

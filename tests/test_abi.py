@@ -136,3 +136,17 @@ def test_pfm_round_trip_and_header(lib, tmp_path, channels):
     assert lib.drv_read_pfm(path, back.ctypes.data_as(C.POINTER(C.c_float)), 2, C.byref(ww), C.byref(hh)) == 2
     assert lib.drv_read_pfm(path, back.ctypes.data_as(C.POINTER(C.c_float)), w * h, C.byref(ww), C.byref(hh)) == 0
     assert np.array_equal(back, img[..., :3])
+
+
+def test_static_scratch_refuses_bf16_before_any_device_call(lib):
+    """No GPU needed: the precision check comes before any CUDA call, so the
+    dummy (never dereferenced) pointers below are not touched."""
+    hf = pipeline.host_frame(pipeline.scaled(pipeline.WORKLOADS["c1_small"], sh_order=2, max_caches=1024,
+                                             precision=abi.PRECISION_BF16))
+    dummy = C.c_void_p(16)
+    ptrs = (C.c_void_p * 1)(16)
+    n_vpls = (C.c_int32 * 1)(1024)
+    intervals = (C.c_int32 * 1)(1)
+    st = lib.drv_light_caches_static_scratch(C.byref(hf.config), C.byref(hf.volume), ptrs, ptrs, n_vpls, intervals,
+                                             1, dummy, dummy, dummy, dummy, None)
+    assert st == abi.ERR_INVALID_ARG

@@ -81,3 +81,35 @@ def test_static_scratch_light_matches_regular_light(sh_order, lib, cuda):
                                              C.c_void_p(p.stream.cuda_stream))
     assert st == abi.ERR_CAPACITY
     p.close()
+
+
+def test_static_scratch_refuses_bf16_and_launches_nothing(lib, cuda):
+    """The entry point's inputs are FP32 (DrvVPL, FP32 mips, std430 entries):
+    a BF16 config, whose entries are 64 B even with SH2, is refused before
+    anything runs, so the caller's entries stay as they were."""
+    import torch
+    w = pipeline.scaled(pipeline.WORKLOADS["c1_small"], sh_order=2, max_caches=abi.STATIC_SCRATCH_MAX_CACHES,
+                        precision=abi.PRECISION_BF16)
+    hf = pipeline.host_frame(w)
+    p = pipeline.Pipeline(hf)
+    p.raycast_inputs()
+    p.prepare_and_extract()
+    p.voxelize()
+    p.allocate()
+    p.sync()
+    count = p.cache_count()
+    b = p.buffers()
+    assert b.entry_stride == 64
+    entries = _device_floats(torch, b.cache_entries, count * (b.entry_stride // 4), p.device)
+    before = entries.clone().cpu().numpy()
+    vpls = (C.c_void_p * 1)(b.vpls[0])
+    cones = (C.c_void_p * 1)(b.cones[0])
+    n_vpls = (C.c_int32 * 1)(b.n_vpls[0])
+    intervals = (C.c_int32 * 1)(hf.lights[0].indirect_shadow_sample_interval)
+    st = lib.drv_light_caches_static_scratch(C.byref(hf.config), C.byref(hf.volume), vpls, cones, n_vpls, intervals,
+                                             1, b.voxel_corners, b.voxel_mips[1], b.counter, b.cache_entries,
+                                             C.c_void_p(p.stream.cuda_stream))
+    assert st == abi.ERR_INVALID_ARG
+    p.stream.synchronize()
+    assert np.array_equal(entries.clone().cpu().numpy(), before)
+    p.close()
