@@ -177,14 +177,39 @@ def reduce_over_ranks(light_ms: float, frame_ms: float, e2e_ms: float, caches: f
 
 
 # ---------------------------------------------------------------- CPU arm
-def cpu_frame(w, hf, n_threads: int, cache_sample: int | None):
-    """One FP64 oracle frame on the host (inputs ray-cast by the oracle, not
-    timed). Returns (caches, seconds, sample_note)."""
+def workload_config(w) -> dict:
+    """The `config` object of both arms' JSON lines: the workload alone."""
+    return {"workload": w.name, "width": w.width, "height": w.height, "n_vpls": w.n_vpls, "n_lights": w.n_lights,
+            "voxel_res": w.voxel_res, "cascades": f"{w.n_cascades}x{w.cav_res}^3", "sh_order": w.sh_order,
+            "cone_steps": w.max_cone_steps,
+            "l2": "GPU arm: flushed between steps (256 MiB write); CPU arm: host caches, not flushed"}
+
+
+def product_library_mapped() -> bool:
+    """True when this process has mapped libdrv_gb300.so (Linux /proc)."""
+    try:
+        return "libdrv_gb300.so" in Path("/proc/self/maps").read_text()
+    except OSError:
+        return False
+
+
+def oracle_inputs(hf, w):
+    """The frame's G-buffer and RSMs, ray-cast by the oracle (not timed)."""
     sys.path.insert(0, str(ROOT / "oracle"))
-    import numpy as np
     import oracle_py as O
     depth, n16, n32, alb = O.raycast_gbuffer(hf.boxes, hf.scene.n_boxes, hf.frame, hf.camera, w.width, w.height)
     rsms = [O.raycast_rsm(hf.boxes, hf.scene.n_boxes, hf.lights[l]) for l in range(w.n_lights)]
+    return depth, n16, alb, rsms
+
+
+def cpu_frame(w, hf, inputs, n_threads: int, cache_sample: int | None = None):
+    """One FP64 oracle frame on the host over ray-cast inputs. Every cache is
+    lit unless cache_sample is given (then a spread sample, extrapolated
+    linearly and labelled so). Returns (caches, frame s, light s, note)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import numpy as np
+    import oracle_py as O
+    depth, n16, alb, rsms = inputs
     t0 = time.perf_counter()
     vp, cones = [], []
     for l in range(w.n_lights):
@@ -208,21 +233,26 @@ def cpu_frame(w, hf, n_threads: int, cache_sample: int | None):
     O.apply(hf.config, hf.volume, hf.frame, depth, n16, 0, alb, atlas, sh, n_threads=n_threads)
     t_apply = time.perf_counter() - t2
     note = (f"FP64 oracle frame on {n_threads} host threads; light stage on {sample} of {n} caches"
-            + (" (extrapolated linearly)" if sample < n else " (all caches)"))
+            + (" (extrapolated linearly)" if sample < n else " (all caches, every step)"))
     return n, t_fixed + t_light + t_apply, t_light, note
 
 
 def run_reference(args):
+    """The CPU arm: the FP64 oracle alone (scene, inputs, every stage), on all
+    host cores; the product library is never loaded in this process."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
-    from dynamicradiancevolume_gb300 import pipeline
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle_py as O
+    from dynamicradiancevolume_gb300 import pipeline  # workload table only (pure Python)
     w = pipeline.WORKLOADS[args.workload]
-    hf = pipeline.host_frame(w)
+    hf = O.host_frame(w)
+    inputs = oracle_inputs(hf, w)
     threads = os.cpu_count() or 1
     frames, lights, caches, note = [], [], 0, ""
     for i in range(args.warmup + args.steps):
-        caches, t_frame, t_light, note = cpu_frame(w, hf, threads, cache_sample=256)
+        caches, t_frame, t_light, note = cpu_frame(w, hf, inputs, threads)
         if i >= args.warmup:
             frames.append(t_frame)
             lights.append(t_light)
@@ -232,12 +262,11 @@ def run_reference(args):
             "warmup": args.warmup, "ms_per_step": t * 1e3, "ms_per_frame": tf * 1e3, "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded procedural box room)",
-            "config": {"workload": w.name, "width": w.width, "height": w.height, "n_vpls": w.n_vpls,
-                       "voxel_res": w.voxel_res, "cascades": f"{w.n_cascades}x{w.cav_res}^3", "sh_order": w.sh_order,
-                       "caches": caches},
+            "config": workload_config(w), "caches": caches, "variant": "fp64_oracle",
             "impl": "reference",
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": note},
-            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "product_library_loaded": product_library_mapped()}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -657,13 +686,9 @@ def run_ours(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "bf16" if head != "plain_fp32" else "f32",
         "data": "synthetic (seeded procedural box room)",
-        "config": {"workload": w.name, "variant": head, "width": w.width, "height": w.height, "n_vpls": w.n_vpls,
-                   "n_lights": w.n_lights, "voxel_res": w.voxel_res, "cascades": f"{w.n_cascades}x{w.cav_res}^3",
-                   "sh_order": w.sh_order, "cone_steps": w.max_cone_steps, "caches": count,
-                   "step": "the light stage (drv_light_caches) over the frame's VPLs, voxels and caches, "
-                           "captured once as a CUDA graph and replayed; ms_per_frame = the whole frame "
-                           "(drv_frame) replayed the same way",
-                   "l2": "flushed between steps (256 MiB write)"},
+        "config": workload_config(w), "variant": head, "caches": count,
+        "step": "the light stage (drv_light_caches) over the frame's VPLs, voxels and caches, captured once as "
+                "a CUDA graph and replayed; ms_per_frame = the whole frame (drv_frame) replayed the same way",
         "rel_l2_vs_fp64": hv.get("rel_l2_vs_fp64"),
         "errors_vs_fp64": {k: hv.get(k) for k in ("rel_l2_vs_fp64", "radiance_max_abs_vs_fp64", "sh_rel_l2_vs_fp64",
                                                   "sh_max_abs_vs_fp64")},
@@ -691,10 +716,13 @@ def run_ours(args):
         "clocks": clocks,
     }
     if rank == 0 and not args.no_cpu_baseline:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import oracle_py as O
         threads = os.cpu_count() or 1
-        caches, t_frame, t_light, note = cpu_frame(w, pipeline.host_frame(w), threads, cache_sample=256)
+        hf_cpu = O.host_frame(w)
+        caches, t_frame, t_light, note = cpu_frame(w, hf_cpu, oracle_inputs(hf_cpu, w), threads)
         line["cpu_baseline"] = {"value": caches / t_light, "unit": UNIT, "cores": threads, "kind": "port",
-                                "sample": note, "ms_per_frame": t_frame * 1e3}
+                                "sample": note + " (one frame)", "ms_per_frame": t_frame * 1e3}
     if rank == 0:
         print(json.dumps(line), flush=True)
     pipe.close()

@@ -1587,4 +1587,122 @@ void orc_bruteforce_rsm(const DrvPerFrame* f, int W, int H, const float* depth, 
     }
 }
 
+// ---------------------------------------------------------------- scenes
+// The seeded box rooms of the benchmark workloads: splitmix64 draws, an
+// inward unit-cube room (box 0) and n_boxes boxes inside it; camera and spot
+// light rejection-sampled clear of the boxes. Same draws in the same order as
+// the product's generator, so both give the same floats.
+namespace {
+struct SplitMix {
+  uint64_t s;
+  uint64_t next() {
+    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+  }
+  double u01() { return (double)(next() >> 11) * (1.0 / 9007199254740992.0); }
+  double u(double a, double b) { return a + (b - a) * u01(); }
+};
+
+// Signed distance from p to the nearest non-room box (negative inside).
+double box_clearance(const DrvScene* scene, const double p[3]) {
+  double best = 1e30;
+  for (int b = 0; b < scene->n_boxes; ++b) {
+    const DrvBox& x = scene->boxes[b];
+    if (x.inward) continue;
+    double outside2 = 0.0, depth = 1e30;
+    bool inside = true;
+    for (int i = 0; i < 3; ++i) {
+      const double e = std::max((double)x.min[i] - p[i], p[i] - (double)x.max[i]);
+      if (e > 0) {
+        outside2 += e * e;
+        inside = false;
+      } else {
+        depth = std::min(depth, -e);
+      }
+    }
+    best = std::min(best, inside ? -depth : std::sqrt(outside2));
+  }
+  return best;
+}
+
+void clear_sample(SplitMix& r, const DrvScene* scene, const double lo[3], const double hi[3], double margin,
+                  double p[3]) {
+  for (int tries = 0; tries < 4096; ++tries) {
+    for (int i = 0; i < 3; ++i) p[i] = r.u(lo[i], hi[i]);
+    if (!scene || box_clearance(scene, p) >= margin) return;
+  }
+}
+
+void unit_towards(const double from[3], const double to[3], float out[3]) {
+  const double d[3] = {to[0] - from[0], to[1] - from[1], to[2] - from[2]};
+  const double inv = 1.0 / std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+  for (int i = 0; i < 3; ++i) out[i] = (float)(d[i] * inv);
+}
+}  // namespace
+
+void orc_generate_scene(uint64_t seed, int n_boxes, float size_min, float size_max, float albedo_min,
+                        float albedo_max, DrvBox* boxes, DrvScene* scene) {
+  SplitMix r{seed * 0x2545F4914F6CDD1Dull + 1};
+  std::memset(boxes, 0, sizeof(DrvBox) * (size_t)(n_boxes + 1));
+  for (int i = 0; i < 3; ++i) {
+    boxes[0].max[i] = 1.0f;
+    boxes[0].albedo[i] = (float)r.u(albedo_min, albedo_max);
+  }
+  boxes[0].inward = 1;
+  for (int b = 1; b <= n_boxes; ++b) {
+    for (int i = 0; i < 3; ++i) {
+      const float size = (float)r.u(size_min, size_max);
+      const float lo = (float)r.u(0.0, 1.0 - size);
+      boxes[b].min[i] = lo;
+      boxes[b].max[i] = lo + size;
+    }
+    for (int i = 0; i < 3; ++i) boxes[b].albedo[i] = (float)r.u(albedo_min, albedo_max);
+  }
+  scene->n_boxes = n_boxes + 1;
+  scene->boxes = boxes;
+  for (int i = 0; i < 3; ++i) {
+    scene->aabb_min[i] = 0.0f;
+    scene->aabb_max[i] = 1.0f;
+  }
+}
+
+void orc_generate_camera(uint64_t seed, const DrvScene* scene, float aspect, DrvCamera* c) {
+  SplitMix r{seed * 0x9E3779B97F4A7C15ull + 7};
+  std::memset(c, 0, sizeof(*c));
+  const double lo[3] = {0.15, 0.35, 0.05}, hi[3] = {0.85, 0.8, 0.25};
+  double p[3];
+  clear_sample(r, scene, lo, hi, 0.08, p);
+  const double t[3] = {r.u(0.3, 0.7), r.u(0.15, 0.45), r.u(0.7, 0.95)};
+  for (int i = 0; i < 3; ++i) c->position[i] = (float)p[i];
+  unit_towards(p, t, c->direction);
+  c->up[1] = 1.0f;
+  c->fov_y_deg = 60.0f;
+  c->aspect = aspect;
+  c->near_plane = 0.01f;
+  c->far_plane = 1000.0f;
+}
+
+void orc_generate_light(uint64_t seed, const DrvScene* scene, uint32_t rsm_resolution, uint32_t rsm_read_lod,
+                        uint32_t indirect_shadow_lod, DrvLightDesc* L) {
+  SplitMix r{seed * 0xD1B54A32D192ED03ull + 13};
+  std::memset(L, 0, sizeof(*L));
+  const double lo[3] = {0.2, 0.75, 0.2}, hi[3] = {0.8, 0.95, 0.8};
+  double p[3];
+  clear_sample(r, scene, lo, hi, 0.05, p);
+  const double t[3] = {r.u(0.25, 0.75), r.u(0.0, 0.2), r.u(0.25, 0.75)};
+  for (int i = 0; i < 3; ++i) {
+    L->intensity[i] = 10.0f;
+    L->position[i] = (float)p[i];
+  }
+  unit_towards(p, t, L->direction);
+  L->half_angle = (float)(30.0 * kPi / 180.0);
+  L->rsm_resolution = rsm_resolution;
+  L->rsm_read_lod = rsm_read_lod;
+  L->indirect_shadow_lod = indirect_shadow_lod;
+  L->near_plane = 0.1f;
+  L->far_plane = 10000.0f;
+}
+
 }  // extern "C"

@@ -51,6 +51,18 @@ void orc_prepare_camera(const DrvCamera* cam, DrvPerFrame* out);
 void orc_compute_volume_info(const DrvConfig* cfg, const float aabb_min[3], const float aabb_max[3],
                              const float camera_position[3], DrvVolumeInfo* out);
 
+/* -- the benchmark's seeded procedural scenes (host-side, no reference
+ *    counterpart: they replace the reference's assimp meshes). The same
+ *    generator as the product's drv_generate_scene / drv_generate_camera /
+ *    drv_generate_light, restated so that the CPU arm of the benchmark
+ *    builds its frame without the product library; a CPU test requires both
+ *    to produce identical scenes. */
+void orc_generate_scene(uint64_t seed, int n_boxes, float size_min, float size_max, float albedo_min,
+                        float albedo_max, DrvBox* boxes /* n_boxes + 1 */, DrvScene* scene);
+void orc_generate_camera(uint64_t seed, const DrvScene* scene, float aspect, DrvCamera* out);
+void orc_generate_light(uint64_t seed, const DrvScene* scene, uint32_t rsm_resolution, uint32_t rsm_read_lod,
+                        uint32_t indirect_shadow_lod, DrvLightDesc* out);
+
 /* -- input producers ---------------------------------------------------- */
 void orc_raycast_gbuffer(const DrvBox* boxes, int n_boxes, const DrvPerFrame* frame, const DrvCamera* cam,
                          int width, int height, float* depth, int16_t* normal16, float* normal32, float* albedo);

@@ -81,6 +81,11 @@ def load():
         "orc_specular_prepare": (None, [I, I, I, VP, I]),
         "orc_apply_specular": (None, [P(abi.DrvConfig), P(abi.DrvVolumeInfo), P(abi.DrvPerFrame), I, I, VP, VP, I,
                                       VP, VP, VP, I, VP, VP, VP, I]),
+        "orc_generate_scene": (None, [C.c_uint64, I, C.c_float, C.c_float, C.c_float, C.c_float, P(abi.DrvBox),
+                                      P(abi.DrvScene)]),
+        "orc_generate_camera": (None, [C.c_uint64, P(abi.DrvScene), C.c_float, P(abi.DrvCamera)]),
+        "orc_generate_light": (None, [C.c_uint64, P(abi.DrvScene), C.c_uint32, C.c_uint32, C.c_uint32,
+                                      P(abi.DrvLightDesc)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -417,3 +422,65 @@ def bruteforce_rsm(frame, depth, normal16, albedo, vpls, rough_metal=None, n_thr
                               vp, nv, _p(out), n_threads)
     return out
 
+
+
+# ---------------------------------------------------------------- host frames
+def make_config(w):
+    """DrvConfig of a workload (a `pipeline.Workload`), field by field as the
+    product's drv_default_config + pipeline.make_config set it, without the
+    product library."""
+    abi = _abi()
+    cfg = abi.DrvConfig()
+    cfg.width, cfg.height = w.width, w.height
+    cfg.sh_order = w.sh_order
+    cfg.indirect_shadow = w.indirect_shadow
+    cfg.max_cone_steps = w.max_cone_steps
+    cfg.cascade_transition = w.cascade_transition
+    cfg.n_cascades = w.n_cascades
+    cfg.cav_res = w.cav_res
+    for c in range(abi.MAX_CASCADES):
+        cfg.cascade_world_size[c] = w.cascade_world_size0 * (2.0 ** c)
+    cfg.voxel_res = w.voxel_res
+    cfg.max_caches = w.max_caches
+    cfg.precision = w.precision
+    cfg.visibility = w.visibility
+    cfg.surrogate_conf_threshold = 0.5
+    cfg.sh2_sign = 0
+    cfg.max_lights = w.n_lights
+    cfg.max_rsm_resolution = w.rsm_resolution
+    cfg.output_format = 0
+    cfg.output_blend = 0
+    cfg.specular_envmap_size = w.specular_envmap_size
+    cfg.specular_fill_level = w.specular_fill_level
+    return cfg
+
+
+def host_frame(w, seed=None):
+    """The seeded frame description of a workload (scene, camera, lights,
+    UBO mirrors) built by the oracle alone: the same values the product's
+    pipeline.host_frame produces, for the benchmark's CPU arm."""
+    from types import SimpleNamespace
+    abi = _abi()
+    lib = load()
+    seed = w.seed if seed is None else seed
+    cfg = make_config(w)
+    boxes = (abi.DrvBox * (w.n_boxes + 1))()
+    scene = abi.DrvScene()
+    lib.orc_generate_scene(seed, w.n_boxes, w.box_size[0], w.box_size[1], w.albedo[0], w.albedo[1], boxes,
+                           C.byref(scene))
+    cam = abi.DrvCamera()
+    lib.orc_generate_camera(seed, C.byref(scene), w.width / w.height, C.byref(cam))
+    frame = abi.DrvPerFrame()
+    lib.orc_prepare_camera(C.byref(cam), C.byref(frame))
+    descs = []
+    lights = (abi.DrvSpotLight * w.n_lights)()
+    for l in range(w.n_lights):
+        d = abi.DrvLightDesc()
+        lib.orc_generate_light(seed * 31 + l, C.byref(scene), w.rsm_resolution, w.rsm_read_lod, w.shadow_lod,
+                               C.byref(d))
+        lib.orc_prepare_light(C.byref(d), C.byref(lights[l]))
+        descs.append(d)
+    vol = abi.DrvVolumeInfo()
+    lib.orc_compute_volume_info(C.byref(cfg), scene.aabb_min, scene.aabb_max, cam.position, C.byref(vol))
+    return SimpleNamespace(workload=w, config=cfg, boxes=boxes, scene=scene, camera=cam, frame=frame,
+                           light_descs=descs, lights=lights, volume=vol)

@@ -150,3 +150,19 @@ def test_static_scratch_refuses_bf16_before_any_device_call(lib):
     st = lib.drv_light_caches_static_scratch(C.byref(hf.config), C.byref(hf.volume), ptrs, ptrs, n_vpls, intervals,
                                              1, dummy, dummy, dummy, dummy, None)
     assert st == abi.ERR_INVALID_ARG
+
+
+@pytest.mark.parametrize("name", list(pipeline.WORKLOADS))
+def test_oracle_host_frame_equals_product_host_frame(lib, oracle, name):
+    """The benchmark's CPU arm builds its frame with the oracle alone; it must
+    be the frame the GPU arm renders: same config, boxes, camera, lights and
+    volume, byte for byte."""
+    w = pipeline.WORKLOADS[name]
+    a, b = pipeline.host_frame(w), oracle.host_frame(w)
+    assert bytes(a.config) == bytes(b.config)
+    assert bytes(a.boxes) == bytes(b.boxes)
+    assert bytes(a.camera) == bytes(b.camera)
+    assert bytes(a.frame) == bytes(b.frame)
+    assert bytes(a.lights) == bytes(b.lights)
+    assert all(bytes(x) == bytes(y) for x, y in zip(a.light_descs, b.light_descs))
+    assert bytes(a.volume) == bytes(b.volume)

@@ -417,3 +417,95 @@ def test_ns_output_properties(ns):
     # pixels without geometry get exactly zero (cacheApply.frag:304-307)
     assert np.all(out[ns.depth < 1e-5] == 0)
     assert ns.count > 500
+
+
+# The headline frame, whole: final indirect radiance of every pixel against
+# the FP64 oracle frame from the same G-buffer and RSM (the 1% relative L2
+# bar is the one the benchmark's metric states), in FP32 and in the BF16
+# precision variant (BF16 VPLs and SH, FP16 mips, Kahan FP32 sums).
+def test_ns_frame_within_one_percent_of_fp64(ns, oracle):
+    ref = oracle_frame(ns, oracle)
+    err = rel_l2(ns.out, ref)
+    assert err < 1e-2, err
+    assert err < 1e-4, err  # measured ~1e-5: FP32 everywhere, one rounding order apart
+    assert np.abs(ns.out).max() > 0
+
+
+@pytest.fixture(scope="module")
+def ns_bf16(lib, oracle, cuda):
+    w = pipeline.scaled(pipeline.WORKLOADS["ns_1080p_4096"], name="ns_1080p_4096_bf16", precision=abi.PRECISION_BF16)
+    return Run(w, oracle)
+
+
+def test_ns_bf16_frame_within_one_percent_of_fp64(ns_bf16, oracle):
+    ref = oracle_frame(ns_bf16, oracle)
+    err = rel_l2(ns_bf16.out, ref)
+    assert err < 1e-2, err
+
+
+# Config 2 at its full size: 1920x1080, 64 boxes, 256^3 voxels with 8 mips,
+# three spot lights each with a 512^2 RSM read at 64^2 (12288 VPLs), four
+# 32^3 cascades with transitions, SH2, 32-step cones. The three lights' SH
+# accumulate into each entry as the reference's per-light dispatches do
+# (renderer.cpp:924-932, cacheLightingRSM.comp:357-373).
+@pytest.fixture(scope="module")
+def c2(lib, oracle, cuda):
+    return Run(pipeline.WORKLOADS["c2_production"], oracle)
+
+
+def test_c2_production_allocation_bit_exact(c2, oracle):
+    st, atlas, pos, count = oracle.allocate_caches(c2.hf.config, c2.hf.volume, c2.hf.frame, c2.depth)
+    assert c2.count == count
+    assert _key_set(c2.positions) == _key_set(pos)
+    assert np.array_equal(c2.atlas != 0, atlas != 0)
+    assert c2.w.n_vpls == 12288 and len(c2.vpls) == 3
+
+
+def test_c2_production_voxels_exact(c2, oracle):
+    bits = oracle.voxelize(c2.hf.boxes, c2.hf.scene.n_boxes, c2.hf.volume, c2.w.voxel_res)
+    assert np.array_equal(c2.bits, bits)
+
+
+def test_c2_production_vpls_match_oracle(c2):
+    # the bars of test_vpl_extraction_matches_oracle, for each of the three lights
+    for (ov, oc), gv, gc in zip(c2.oracle_vpls(), c2.gpu_vpls_f64(), c2.cones):
+        assert gv.shape == ov.shape == (4096, 10)
+        assert np.allclose(gv[:, 0:3], ov[:, 0:3], rtol=1e-5, atol=1e-12)
+        assert np.allclose(gv[:, 3], ov[:, 3], rtol=1e-4)
+        assert np.allclose(gv[:, 4:7], ov[:, 4:7], rtol=0, atol=1e-5)
+        assert np.max(np.abs(gv[:, 7:10] - ov[:, 7:10])) < 2e-3
+        assert np.allclose(gc[:, 0:3], oc[:, 0:3], atol=1e-5)
+        assert np.allclose(gc[:, 3], oc[:, 3], rtol=1e-3, atol=1e-6)
+
+
+def test_c2_production_light_sample_matches_fp64(c2, oracle):
+    """Three lights' SH summed per cache: a seeded sample of 96 caches against
+    the FP64 gather of all 12288 VPLs with 32-step cones."""
+    rng = np.random.default_rng(1)
+    idx = rng.choice(c2.entries.shape[0], size=min(96, c2.entries.shape[0]), replace=False)
+    mips = oracle.build_mips(c2.w.voxel_res, c2.bits)
+    sh = oracle.light_caches(c2.hf.config, c2.hf.volume, c2.positions[idx].copy(), c2.hf.lights, c2.gpu_vpls_f64(),
+                             [c.astype(np.float64) for c in c2.cones], c2.bits, mips)
+    assert rel_l2(c2.gpu_sh()[idx], sh) < 1e-3
+
+
+def test_c2_production_lights_accumulate(c2, oracle):
+    """Each light adds its share: the SH of the three lights equals the sum of
+    the FP64 gathers of each light alone (same sample of caches)."""
+    rng = np.random.default_rng(2)
+    idx = rng.choice(c2.entries.shape[0], size=min(32, c2.entries.shape[0]), replace=False)
+    mips = oracle.build_mips(c2.w.voxel_res, c2.bits)
+    vp, cones = c2.gpu_vpls_f64(), [c.astype(np.float64) for c in c2.cones]
+    single = [oracle.light_caches(c2.hf.config, c2.hf.volume, c2.positions[idx].copy(),
+                                  (abi.DrvSpotLight * 1)(c2.hf.lights[l]), vp[l:l + 1], cones[l:l + 1], c2.bits, mips)
+              for l in range(3)]
+    assert rel_l2(c2.gpu_sh()[idx], single[0] + single[1] + single[2]) < 1e-3
+    # every light contributes something to this view
+    assert min(np.abs(s).sum() for s in single) > 0
+
+
+def test_c2_production_frame_within_one_percent_of_fp64(c2, oracle):
+    ref = oracle_frame(c2, oracle)
+    err = rel_l2(c2.out, ref)
+    assert err < 1e-2, err
+    assert np.isfinite(c2.out).all() and (c2.out >= 0).all()
