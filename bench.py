@@ -433,7 +433,12 @@ def run_ours(args):
 
     # ---- variants: plain FP32 cone, BF16 precision, surrogate visibility
     variants = {}
-    weights = surrogate.load_params() if surrogate.DEFAULT_WEIGHTS.with_suffix(".bin").exists() else None
+    weights, features, surrogate_note = None, "segment8", None
+    if surrogate.DEFAULT_WEIGHTS.with_suffix(".bin").exists():
+        try:
+            weights, features = surrogate.load_params(), surrogate.load_features()
+        except ValueError as e:  # a checkpoint of another model layout: no surrogate variants
+            surrogate_note = str(e)
     plan = [("plain_fp32", w, None), ("precision_bf16", pipeline.scaled(w, precision=abi.PRECISION_BF16), None)]
     if weights is not None:
         for thr in args.thresholds:
@@ -447,7 +452,7 @@ def run_ours(args):
                 hf.config.surrogate_conf_threshold = thr
             pipe = pipeline.Pipeline(hf, device=str(dev))
             if thr is not None:
-                surrogate.upload(pipe, weights)
+                surrogate.upload(pipe, weights, features)
             pipe.raycast_inputs()
             pipe.frame()
             pipe.sync()
@@ -536,7 +541,7 @@ def run_ours(args):
             else:
                 q = pipeline.Pipeline(hf2, device=str(dev))
             if head.startswith("surrogate"):
-                surrogate.upload(q, weights)
+                surrogate.upload(q, weights, features)
             out.append(q)
         return out
 

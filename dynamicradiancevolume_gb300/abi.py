@@ -138,7 +138,8 @@ class DrvBuffers(C.Structure):
 class DrvTuning(C.Structure):
     _fields_ = [("light_path", C.c_int32), ("pair_capacity", C.c_uint32), ("cone_ctas_per_sm", C.c_int32),
                 ("gather_ctas_per_sm", C.c_int32), ("time_kernels", C.c_int32),
-                ("plain_voxel_reads", C.c_int32), ("reserved", C.c_int32 * 2)]
+                ("plain_voxel_reads", C.c_int32), ("surrogate_wait_test", C.c_int32),
+                ("reserved", C.c_int32 * 1)]
 
 
 LIGHT_KERNELS = ("cull", "classify", "scatter", "mlp", "cone", "gather")
@@ -196,6 +197,7 @@ PROTOTYPES = {
                             P(DrvSpotLight), P(DrvRSMView), C.c_int32, VP]),
     "drv_get_cache_count": (C.c_int, [VP, P(C.c_uint32)]),
     "drv_set_surrogate_params": (C.c_int, [VP, VP]),
+    "drv_set_surrogate_features": (C.c_int, [VP, C.c_int32]),
     "drv_surrogate_make_pairs": (C.c_int, [VP, C.c_uint64, C.c_int32, VP, VP]),
     "drv_surrogate_train_scratch_floats": (C.c_size_t, [C.c_int32]),
     "drv_surrogate_train_step": (C.c_int, [VP, VP, C.c_int32, VP, VP, VP, VP, C.c_int32, C.c_float, C.c_float,
@@ -222,6 +224,9 @@ STATIC_SCRATCH_MAX_CACHES = 4096
 SURROGATE_INPUTS = 32
 SURROGATE_PARAMS = 10562
 SURROGATE_ENUMERATE = 0xFFFFFFFFFFFFFFFF
+SURROGATE_FEATURES_SEGMENT8 = 0  # the configuration's 17 inputs
+SURROGATE_FEATURES_CONE4 = 1     # 27 inputs with the cone's first four samples
+SURROGATE_FEATURE_NAMES = {"segment8": SURROGATE_FEATURES_SEGMENT8, "cone4": SURROGATE_FEATURES_CONE4}
 
 
 def header_functions(header: Path) -> list[str]:

@@ -61,7 +61,8 @@ def make_scenes(specs, threshold: float = 0.5, params=None, device: str = "cuda"
         hf.config.surrogate_conf_threshold = threshold
         p = pipeline.Pipeline(hf, device=device)
         if w.visibility == abi.VISIBILITY_SURROGATE:
-            surrogate.upload(p, params if params is not None else surrogate.load_params())
+            surrogate.upload(p, params if params is not None else surrogate.load_params(),
+                             "segment8" if params is not None else surrogate.load_features())
         p.raycast_inputs()
         p.frame()
         p.sync()

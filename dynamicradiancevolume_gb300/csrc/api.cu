@@ -667,9 +667,16 @@ drv_status light_caches(DrvContext* ctx, const DrvSpotLight* lights, int32_t n_l
         events = ctx->lk_events;
       }
     }
+    drv::SurrogateArgs sur;
+    if (surrogate) {
+      sur.weights = ctx->sur_weights;
+      sur.feature_set = ctx->sur_features;
+      sur.threshold = ctx->cfg.surrogate_conf_threshold;
+      sur.err = ctx->scratch_words + 1;
+      sur.hold_commit = ctx->tuning.surrogate_wait_test;
+    }
     drv_status st = cuda_check(ctx, drv::launch_light_split(ctx->s(), ctx->cfg, *vol, ll, ctx->counter, ctx->entries,
-                                                            ctx->entry_stride, ctx->light_voxels(), pairs,
-                                                            surrogate ? ctx->sur_weights : nullptr,
+                                                            ctx->entry_stride, ctx->light_voxels(), pairs, sur,
                                                             ctx->tuning.cone_ctas_per_sm,
                                                             ctx->tuning.gather_ctas_per_sm, ctx->num_sms, events,
                                                             voxels_ready),
@@ -802,7 +809,18 @@ drv_status drv_surrogate_eval(DrvContext* ctx, const float* features, int32_t n,
   if (!ctx || !features || !out || n < 0) return DRV_ERR_INVALID_ARG;
   if (!ctx->sur_ready) return fail(ctx, DRV_ERR_INVALID_ARG, "drv_set_surrogate_params first");
   if (n == 0) return DRV_OK;
-  return cuda_check(ctx, drv::launch_surrogate_eval(ctx->s(), ctx->sur_weights, features, n, out), "surrogate_eval");
+  if (((uintptr_t)features & 15u) != 0) return fail(ctx, DRV_ERR_INVALID_ARG, "features must be 16-byte aligned");
+  return cuda_check(ctx, drv::launch_surrogate_eval(ctx->s(), ctx->sur_weights, features, n, out,
+                                                    ctx->scratch_words + 1, ctx->num_sms),
+                    "surrogate_eval");
+}
+
+drv_status drv_set_surrogate_features(DrvContext* ctx, int32_t feature_set) {
+  if (!ctx) return DRV_ERR_INVALID_ARG;
+  if (feature_set != DRV_SURROGATE_FEATURES_SEGMENT8 && feature_set != DRV_SURROGATE_FEATURES_CONE4)
+    return fail(ctx, DRV_ERR_INVALID_ARG, "unknown surrogate feature set");
+  ctx->sur_features = feature_set;
+  return DRV_OK;
 }
 
 drv_status drv_get_surrogate_fallbacks(DrvContext* ctx, uint32_t* out) {
@@ -898,7 +916,7 @@ drv_status drv_surrogate_make_pairs(DrvContext* ctx, uint64_t seed, int32_t n_pa
   }
   return cuda_check(ctx, drv::launch_surrogate_pairs(ctx->s(), ctx->cfg, ctx->last_volume, ll, ctx->counter,
                                                      ctx->entries, ctx->entry_stride, ctx->voxels(), seed, n_pairs,
-                                                     features, targets),
+                                                     features, targets, ctx->sur_features),
                     "surrogate_make_pairs");
 }
 

@@ -206,9 +206,10 @@ struct Context {
   // Events between the split light stage's kernels (DrvTuning.time_kernels).
   cudaEvent_t lk_events[DRV_LK_COUNT + 1] = {};
   bool lk_recorded = false;
-  // Visibility surrogate: packed BF16 inference weights.
+  // Visibility surrogate: packed BF16 inference weights and their feature set.
   void* sur_weights = nullptr;
   bool sur_ready = false;
+  int sur_features = DRV_SURROGATE_FEATURES_SEGMENT8;
   DrvVolumeInfo last_volume{};  // volume of the last drv_allocate_caches (cache positions refer to it)
   // Indirect specular: the envmap atlas, all levels in one allocation.
   uint32_t* spec_env = nullptr;
@@ -252,12 +253,24 @@ cudaError_t launch_allocate(cudaStream_t s, const DrvConfig& cfg, const DrvVolum
 cudaError_t launch_light_caches(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const LightLaunch& ll,
                                 const DrvCacheCounter* counter, void* entries, uint32_t entry_stride,
                                 const VoxelInputs& vox, const LightScratch& scratch, int num_sms);
+// The learned visibility surrogate of a light stage: packed weights
+// (nullptr: plain cones), feature set (kFeature*), confidence threshold, the
+// device error word its bounded waits report to, and the timeout test hook
+// (DrvTuning.surrogate_wait_test).
+struct SurrogateArgs {
+  const void* weights = nullptr;
+  int feature_set = 0;
+  float threshold = 0.5f;
+  uint32_t* err = nullptr;
+  int hold_commit = 0;
+};
+
 // Split light stage: cull -> (cones | surrogate MLP + cones of the
-// unconfident pairs) -> gather. weights == nullptr: plain cones.
+// unconfident pairs) -> gather.
 bool light_split_supported(const DrvConfig& cfg, const LightLaunch& ll);
 cudaError_t launch_light_split(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const LightLaunch& ll,
                                const DrvCacheCounter* counter, void* entries, uint32_t entry_stride,
-                               const VoxelInputs& vox, const PairList& pairs, const void* weights,
+                               const VoxelInputs& vox, const PairList& pairs, const SurrogateArgs& sur,
                                int cone_ctas_per_sm, int gather_ctas_per_sm, int num_sms,
                                cudaEvent_t* events = nullptr, cudaEvent_t voxels_ready = nullptr);
 cudaError_t launch_bruteforce_rsm(cudaStream_t s, const DrvPerFrame& f, const DrvGBufferView& g,
@@ -283,11 +296,12 @@ cudaError_t launch_envmap_prepare(cudaStream_t s, const SpecView& sv, const DrvC
 size_t surrogate_weights_bytes();
 size_t surrogate_train_scratch_floats(int n);
 cudaError_t launch_pack_surrogate_weights(cudaStream_t s, const float* params, void* weights);
-cudaError_t launch_surrogate_eval(cudaStream_t s, const void* weights, const float* X, int n, float* out);
+cudaError_t launch_surrogate_eval(cudaStream_t s, const void* weights, const float* X, int n, float* out,
+                                  uint32_t* err, int num_sms);
 cudaError_t launch_surrogate_pairs(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol,
                                    const LightLaunch& ll, const DrvCacheCounter* counter, const void* entries,
                                    uint32_t entry_stride, const VoxelInputs& vox, uint64_t seed, int n_pairs,
-                                   float* features, float* targets);
+                                   float* features, float* targets, int feature_set);
 cudaError_t launch_surrogate_train_step(cudaStream_t s, const float* X, const float* Y, int n, float* params,
                                         float* m, float* v, float* scratch, int step, float lr, float conf_tau,
                                         float weight_decay, float* loss_out);

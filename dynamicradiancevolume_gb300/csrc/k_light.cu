@@ -533,9 +533,8 @@ cudaError_t launch_persistent_after(void (*kernel)(KArgs...), int threads, size_
 // after each kernel slot, skipped slots included, so slot k's time is
 // elapsed(events[k], events[k + 1]).
 template <int NK, bool BF16>
-cudaError_t split_variant(cudaStream_t s, const StageParams& p, const PairList& L, const void* weights,
-                          float conf_threshold, int cone_ctas, int gather_ctas, int num_sms, cudaEvent_t* ev,
-                          cudaEvent_t voxels_ready) {
+cudaError_t split_variant(cudaStream_t s, const StageParams& p, const PairList& L, const SurrogateArgs& sur,
+                          int cone_ctas, int gather_ctas, int num_sms, cudaEvent_t* ev, cudaEvent_t voxels_ready) {
   // Only the cone pass and the surrogate's features read the voxels: with
   // voxels_ready, the cull and the ordering passes overlap the voxel build.
   auto wait_voxels = [&]() { return voxels_ready ? cudaStreamWaitEvent(s, voxels_ready, 0) : cudaSuccess; };
@@ -545,7 +544,7 @@ cudaError_t split_variant(cudaStream_t s, const StageParams& p, const PairList& 
   const size_t cull_smem = (size_t)((p.total_blocks + 31) >> 5) * 2 * sizeof(uint32_t);
   if ((e = launch_persistent(cull_kernel<BF16>, kCullThreads, cull_smem, s, num_sms, p, L)) != cudaSuccess) return e;
   if ((e = mark(DRV_LK_CLASSIFY)) != cudaSuccess) return e;
-  if (!weights) {
+  if (!sur.weights) {
     if ((e = launch_persistent_after(classify_kernel<BF16>, kClassThreads, 0, s, num_sms, p, L)) != cudaSuccess)
       return e;
     if ((e = mark(DRV_LK_SCATTER)) != cudaSuccess) return e;
@@ -558,7 +557,7 @@ cudaError_t split_variant(cudaStream_t s, const StageParams& p, const PairList& 
     if ((e = mark(DRV_LK_SCATTER)) != cudaSuccess || (e = wait_voxels()) != cudaSuccess ||
         (e = mark(DRV_LK_MLP)) != cudaSuccess)
       return e;
-    if ((e = launch_surrogate_mlp(s, p, L, weights, conf_threshold, BF16, num_sms)) != cudaSuccess) return e;
+    if ((e = launch_surrogate_mlp(s, p, L, sur, BF16, num_sms)) != cudaSuccess) return e;
     if ((e = mark(DRV_LK_CONE)) != cudaSuccess) return e;
     e = launch_grid(cone_kernel<BF16, true>, 128, 0, s, num_sms, cone_ctas, true, p, L);
   }
@@ -623,17 +622,16 @@ bool light_split_supported(const DrvConfig& cfg, const LightLaunch& ll) {
 
 cudaError_t launch_light_split(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const LightLaunch& ll,
                                const DrvCacheCounter* counter, void* entries, uint32_t entry_stride,
-                               const VoxelInputs& vox, const PairList& pairs, const void* weights,
+                               const VoxelInputs& vox, const PairList& pairs, const SurrogateArgs& sur,
                                int cone_ctas_per_sm, int gather_ctas_per_sm, int num_sms, cudaEvent_t* events,
                                cudaEvent_t voxels_ready) {
   const StageParams p = make_stage_params(cfg, vol, ll, counter, entries, entry_stride, vox);
-  const float thr = cfg.surrogate_conf_threshold;
   const bool bf16 = cfg.precision == DRV_PRECISION_BF16;
   if (cfg.sh_order == 2)
-    return bf16 ? split_variant<9, true>(s, p, pairs, weights, thr, cone_ctas_per_sm, gather_ctas_per_sm, num_sms, events, voxels_ready)
-                : split_variant<9, false>(s, p, pairs, weights, thr, cone_ctas_per_sm, gather_ctas_per_sm, num_sms, events, voxels_ready);
-  return bf16 ? split_variant<4, true>(s, p, pairs, weights, thr, cone_ctas_per_sm, gather_ctas_per_sm, num_sms, events, voxels_ready)
-              : split_variant<4, false>(s, p, pairs, weights, thr, cone_ctas_per_sm, gather_ctas_per_sm, num_sms, events, voxels_ready);
+    return bf16 ? split_variant<9, true>(s, p, pairs, sur, cone_ctas_per_sm, gather_ctas_per_sm, num_sms, events, voxels_ready)
+                : split_variant<9, false>(s, p, pairs, sur, cone_ctas_per_sm, gather_ctas_per_sm, num_sms, events, voxels_ready);
+  return bf16 ? split_variant<4, true>(s, p, pairs, sur, cone_ctas_per_sm, gather_ctas_per_sm, num_sms, events, voxels_ready)
+              : split_variant<4, false>(s, p, pairs, sur, cone_ctas_per_sm, gather_ctas_per_sm, num_sms, events, voxels_ready);
 }
 
 }  // namespace drv

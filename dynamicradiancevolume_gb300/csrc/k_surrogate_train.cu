@@ -44,6 +44,7 @@ struct PairParams {
   int n_pairs;
   float* features;
   float* targets;
+  int feature_set;
 };
 
 __device__ __forceinline__ void vpl_normal(const void* vpls, int bf16, int i, float& nx, float& ny, float& nz) {
@@ -66,7 +67,7 @@ __global__ void __launch_bounds__(128) pairs_kernel(PairParams p) {
   const uint32_t count = min((uint32_t)max(p.counter->total_light_cache_count, 0), p.max_caches);
   float* f = p.features + (size_t)i * kMlpIn;
   if (count == 0 || p.total_blocks == 0) {
-    for (int k = 0; k < kMlpIn; ++k) f[k] = 0.0f;
+    for (int k = 0; k < kMlpIn; ++k) f[k] = k == kOneInput ? 1.0f : 0.0f;
     p.targets[i] = 1.0f;
     return;
   }
@@ -76,7 +77,7 @@ __global__ void __launch_bounds__(128) pairs_kernel(PairParams p) {
     cache = (uint32_t)(i / p.total_blocks);
     b = i % p.total_blocks;
     if (cache >= count) {
-      for (int k = 0; k < kMlpIn; ++k) f[k] = 0.0f;
+      for (int k = 0; k < kMlpIn; ++k) f[k] = k == kOneInput ? 1.0f : 0.0f;
       p.targets[i] = 1.0f;
       return;
     }
@@ -134,8 +135,12 @@ __global__ void __launch_bounds__(128) pairs_kernel(PairParams p) {
   float nx, ny, nz;
   vpl_normal(la.vpls, p.bf16, lb * la.interval, nx, ny, nz);
   const float inv_extent = 1.0f / (p.voxel_size * p.vox.N);
-  surrogate_features(p.vox, inv_extent, p.vol_min, p.voxel_size, p.max_steps, cx, cy, cz, cone.x, cone.y, cone.z, nx,
-                     ny, nz, cone.w, f);
+  if (p.feature_set == kFeatureCone4)
+    pair_features<kFeatureCone4>(p.vox, inv_extent, p.vol_min, p.voxel_size, p.max_steps, cx, cy, cz, cone.x, cone.y,
+                                 cone.z, nx, ny, nz, cone.w, f);
+  else
+    pair_features<kFeatureSegment8>(p.vox, inv_extent, p.vol_min, p.voxel_size, p.max_steps, cx, cy, cz, cone.x,
+                                    cone.y, cone.z, nx, ny, nz, cone.w, f);
   const float vx = (cx - p.vol_min[0]) * inv_extent, vy = (cy - p.vol_min[1]) * inv_extent,
               vz = (cz - p.vol_min[2]) * inv_extent;
   p.targets[i] = cone_shadow(p.vox, p.voxel_size, p.max_steps, cx, cy, cz, vx, vy, vz, cone.x, cone.y, cone.z, cone.w);
@@ -317,7 +322,7 @@ __global__ void __launch_bounds__(256) loss_sum_kernel(const float* __restrict__
 cudaError_t launch_surrogate_pairs(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol,
                                    const LightLaunch& ll, const DrvCacheCounter* counter, const void* entries,
                                    uint32_t entry_stride, const VoxelInputs& vox, uint64_t seed, int n_pairs,
-                                   float* features, float* targets) {
+                                   float* features, float* targets, int feature_set) {
   PairParams p;
   p.ll = ll;
   int base = 0;
@@ -344,6 +349,7 @@ cudaError_t launch_surrogate_pairs(cudaStream_t s, const DrvConfig& cfg, const D
   p.n_pairs = n_pairs;
   p.features = features;
   p.targets = targets;
+  p.feature_set = feature_set;
   pairs_kernel<<<(n_pairs + 127) / 128, 128, 0, s>>>(p);
   return cudaGetLastError();
 }

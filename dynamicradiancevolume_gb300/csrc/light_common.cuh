@@ -61,8 +61,8 @@ StageParams make_stage_params(const DrvConfig& cfg, const DrvVolumeInfo& vol, co
 
 // Host: the surrogate's pass over the pair list (k_light_surrogate.cu):
 // shadowing of the confident pairs, the others appended to L.retrace.
-cudaError_t launch_surrogate_mlp(cudaStream_t s, const StageParams& p, const PairList& L, const void* weights,
-                                 float conf_threshold, bool bf16, int num_sms);
+cudaError_t launch_surrogate_mlp(cudaStream_t s, const StageParams& p, const PairList& L, const SurrogateArgs& sa,
+                                 bool bf16, int num_sms);
 
 // Host: resident CTAs per SM of a kernel at this block size and dynamic
 // shared memory, queried once per (kernel, block, smem) and device.

@@ -3,10 +3,12 @@
 // parameter layout and activation, shared by the pair generator, the trainer
 // and the inference kernel.
 //
-// MLP: 32 inputs -> 64 -> 64 -> 64 -> 2, GELU (tanh form) between layers.
+// MLP: 32 inputs -> 64 -> 64 -> 64 -> 2, GELU between layers in its
+// sigmoid form x sigmoid(1.702 x) (Hendrycks & Gimpel 2016, section 2).
 // Output 0 is the visibility logit (visibility = sigmoid), output 1 the
 // confidence logit: pairs whose sigmoid(confidence) is below the threshold
-// are re-traced with the cone.
+// are re-traced with the cone. Input 31 is the constant 1 (it carries the
+// first layer's bias on the tensor cores).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -20,8 +22,14 @@ namespace drv {
 constexpr int kMlpIn = 32;
 constexpr int kMlpHidden = 64;
 constexpr int kMlpOut = 2;
-constexpr int kMlpOutPad = 8;  // layer-4 rows padded to one n8 MMA tile
-constexpr int kFeatures = 27;  // used inputs; the rest are zero
+constexpr int kOneInput = kMlpIn - 1;  // the constant-1 input
+
+// Feature sets (DRV_SURROGATE_FEATURES_*): the configuration's 17 inputs
+// (cache, VPL position and normal, eight mip-3 opacities along the segment),
+// or 27 inputs that add the cone's aperture, length, direction and its own
+// first four samples.
+constexpr int kFeatureSegment8 = 0;
+constexpr int kFeatureCone4 = 1;
 
 // Parameter offsets (floats) of the flat FP32 master copy; weights are
 // [out][in] row-major (in contiguous), biases follow each weight matrix.
@@ -35,57 +43,13 @@ constexpr int kOffW4 = kOffB3 + kMlpHidden;
 constexpr int kOffB4 = kOffW4 + kMlpOut * kMlpHidden;
 constexpr int kMlpParams = kOffB4 + kMlpOut;  // 10562
 
-// GELU, tanh approximation: 0.5 x (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3))).
-__device__ __forceinline__ float gelu(float x) {
-  const float u = 0.7978845608f * (x + 0.044715f * x * x * x);
-  return 0.5f * x * (1.0f + tanhf(u));
-}
-__device__ __forceinline__ float gelu_grad(float x) {
-  const float x2 = x * x;
-  const float u = 0.7978845608f * (x + 0.044715f * x2 * x);
-  const float t = tanhf(u);
-  return 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * 0.7978845608f * (1.0f + 3.0f * 0.044715f * x2);
-}
+// GELU, sigmoid form, and its derivative (training, FP32).
+constexpr float kGeluK = 1.702f;
 __device__ __forceinline__ float sigmoidf(float x) { return 1.0f / (1.0f + __expf(-x)); }
-
-// GELU for inference: the same tanh form with the hardware tanh
-// approximation (MUFU.TANH), as the BF16 activations it feeds tolerate.
-__device__ __forceinline__ float tanh_fast(float x) {
-  float y;
-  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
-__device__ __forceinline__ float gelu_fast(float x) {
-  const float u = 0.7978845608f * (x + 0.044715f * x * x * x);
-  return 0.5f * x * (1.0f + tanh_fast(u));
-}
-
-// Two FP32 values -> bf16x2 (lo in the low half), round to nearest even.
-__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
-  uint32_t r;
-  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
-  return r;
-}
-
-// GELU of the inference MLP on two BF16 values at once, in bf16x2
-// arithmetic with the hardware tanh: 0.5 x (1 + tanh(x (c0 + c1 x^2))) with
-// c0 = sqrt(2/pi), c1 = 0.044715 c0 rounded to BF16 (0x3F4C, 0x3D12). The
-// activations it produces are stored as BF16 anyway, and the error of BF16
-// arithmetic here is of the order of that rounding.
-__device__ __forceinline__ uint32_t gelu_bf16x2(uint32_t x) {
-  uint32_t y;
-  asm("{\n"
-      ".reg .b32 x2, u, t, h;\n"
-      "mul.rn.bf16x2 x2, %1, %1;\n"
-      "fma.rn.bf16x2 u, x2, %2, %3;\n"
-      "mul.rn.bf16x2 u, u, %1;\n"
-      "tanh.approx.bf16x2 t, u;\n"
-      "mul.rn.bf16x2 h, %1, %4;\n"
-      "fma.rn.bf16x2 %0, h, t, h;\n"
-      "}"
-      : "=r"(y)
-      : "r"(x), "r"(0x3D123D12u), "r"(0x3F4C3F4Cu), "r"(0x3F003F00u));
-  return y;
+__device__ __forceinline__ float gelu(float x) { return x * sigmoidf(kGeluK * x); }
+__device__ __forceinline__ float gelu_grad(float x) {
+  const float s = sigmoidf(kGeluK * x);
+  return s + kGeluK * x * s * (1.0f - s);
 }
 
 // Distance (in voxels) the cone of cacheLightingRSM.comp:195-228 reaches
@@ -172,7 +136,52 @@ __device__ __forceinline__ void surrogate_features(const VoxelView& v, float inv
     f[26] = 1.0f - transmit;
   }
 #pragma unroll
-  for (int i = kFeatures; i < kMlpIn; ++i) f[i] = 0.0f;
+  for (int i = 27; i < kOneInput; ++i) f[i] = 0.0f;
+  f[kOneInput] = 1.0f;
+}
+
+// The configuration's 17 inputs of one (cache, shadow block) pair: 0-2 the
+// cache and 3-5 the block's cone target (the VPL position) in normalised
+// volume coordinates, 6-8 the VPL normal, 9-16 eight trilinear opacity
+// samples of mip level 3 at the midpoints of eight equal parts of the
+// segment from the cache to the target; 31 the constant 1.
+__device__ __forceinline__ void segment_features(const VoxelView& v, float inv_extent, const float vol_min[3],
+                                                 float cx, float cy, float cz, float tx, float ty, float tz, float nx,
+                                                 float ny, float nz, float* f) {
+  const float px = (cx - vol_min[0]) * inv_extent, py = (cy - vol_min[1]) * inv_extent,
+              pz = (cz - vol_min[2]) * inv_extent;
+  const float qx = (tx - vol_min[0]) * inv_extent, qy = (ty - vol_min[1]) * inv_extent,
+              qz = (tz - vol_min[2]) * inv_extent;
+  f[0] = px;
+  f[1] = py;
+  f[2] = pz;
+  f[3] = qx;
+  f[4] = qy;
+  f[5] = qz;
+  f[6] = nx;
+  f[7] = ny;
+  f[8] = nz;
+  const int level = min(3, v.max_level);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const float t = (i + 0.5f) * 0.125f;
+    f[9 + i] = level_any(v, level, px + (qx - px) * t, py + (qy - py) * t, pz + (qz - pz) * t);
+  }
+#pragma unroll
+  for (int i = 17; i < kOneInput; ++i) f[i] = 0.0f;
+  f[kOneInput] = 1.0f;
+}
+
+// Features of a pair in feature set FS.
+template <int FS>
+__device__ __forceinline__ void pair_features(const VoxelView& v, float inv_extent, const float vol_min[3],
+                                              float voxel_size, int max_steps, float cx, float cy, float cz,
+                                              float tx, float ty, float tz, float nx, float ny, float nz, float dsr,
+                                              float* f) {
+  if (FS == kFeatureSegment8)
+    segment_features(v, inv_extent, vol_min, cx, cy, cz, tx, ty, tz, nx, ny, nz, f);
+  else
+    surrogate_features(v, inv_extent, vol_min, voxel_size, max_steps, cx, cy, cz, tx, ty, tz, nx, ny, nz, dsr, f);
 }
 
 }  // namespace drv

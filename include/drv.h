@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define DRV_ABI_VERSION 4
+#define DRV_ABI_VERSION 5
 #define DRV_MAX_CASCADES 4   /* MAX_NUM_ADDRESS_VOLUME_CASCADES, globalubos.glsl:43 */
 #define DRV_MAX_LIGHTS 16    /* maxExpectedLights, renderer.cpp:80 */
 #define DRV_LIGHTING_THREADS_PER_GROUP 64 /* lightcache.glsl:95 */
@@ -492,20 +492,32 @@ drv_status drv_get_cache_count(DrvContext* ctx, uint32_t* out_count);
 
 /* ---- learned visibility surrogate -----------------------------------------
  * No counterpart in the reference: an MLP (32 inputs -> 64 -> 64 -> 64 -> 2,
- * GELU; BF16 weights, FP32 accumulation on tensor cores) predicts the
- * indirect-shadow cone's visibility of a (cache, shadow block) pair plus a
- * confidence; with DrvConfig.visibility = DRV_VISIBILITY_SURROGATE,
- * drv_light_caches uses it and re-traces pairs whose confidence is below
- * DrvConfig.surrogate_conf_threshold with the cone. Parameters are a flat FP32
- * array of DRV_SURROGATE_PARAMS floats: W1[64][32], b1[64], W2[64][64], b2,
- * W3[64][64], b3, W4[2][64], b4[2] (weights [out][in]). */
+ * GELU in its sigmoid form x sigmoid(1.702 x); BF16 weights and activations,
+ * FP32 accumulation on the tcgen05 tensor cores) predicts the indirect-shadow
+ * cone's visibility of a (cache, shadow block) pair plus a confidence; with
+ * DrvConfig.visibility = DRV_VISIBILITY_SURROGATE, drv_light_caches uses it and
+ * re-traces pairs whose confidence is below DrvConfig.surrogate_conf_threshold
+ * with the cone. Parameters are a flat FP32 array of DRV_SURROGATE_PARAMS
+ * floats: W1[64][32], b1[64], W2[64][64], b2, W3[64][64], b3, W4[2][64], b4[2]
+ * (weights [out][in]). Input 31 is the constant 1. */
 #define DRV_SURROGATE_INPUTS 32
 #define DRV_SURROGATE_PARAMS 10562
 /* Uploads parameters (device FP32 array) as the context's BF16 inference weights. */
 drv_status drv_set_surrogate_params(DrvContext* ctx, const float* params_device);
+/* The inputs the uploaded parameters were trained on:
+ *  SEGMENT8 (default): the cache and the block's cone target in normalised
+ *    volume coordinates, the VPL normal, and eight trilinear opacity samples
+ *    of voxel mip 3 at the midpoints of eight equal parts of the segment
+ *    between them (inputs 0-16);
+ *  CONE4: 27 inputs, adding the cone's aperture and length, the direction,
+ *    and the cone's own first four samples and their composited occlusion
+ *    (mip-3 samples over the part of the segment the cone reaches). */
+enum { DRV_SURROGATE_FEATURES_SEGMENT8 = 0, DRV_SURROGATE_FEATURES_CONE4 = 1 };
+drv_status drv_set_surrogate_features(DrvContext* ctx, int32_t feature_set);
 /* Training pairs from the context's current frame (after drv_extract_vpls,
  * drv_build_opacity_mips and drv_allocate_caches): random (cache, shadow
- * block) pairs, features[n][32] and the cone-traced visibility targets[n].
+ * block) pairs, features[n][32] (the context's feature set) and the
+ * cone-traced visibility targets[n].
  * seed = DRV_SURROGATE_ENUMERATE lists the pairs in order instead (pair i =
  * cache i / n_blocks, block i % n_blocks, blocks of all lights in light
  * order). */
@@ -521,7 +533,8 @@ size_t drv_surrogate_train_scratch_floats(int32_t n);
 drv_status drv_surrogate_train_step(const float* features, const float* targets, int32_t n, float* params,
                                     float* adam_m, float* adam_v, float* scratch, int32_t step, float lr,
                                     float conf_tau, float weight_decay, float* loss_out, void* cuda_stream);
-/* Evaluates the context's inference weights on n feature rows:
+/* Evaluates the context's inference weights on n feature rows (the
+ * tensor-core kernel of the light stage; input 31 is taken as 1):
  * out[n][2] = (visibility, confidence). */
 drv_status drv_surrogate_eval(DrvContext* ctx, const float* features, int32_t n, float* out);
 /* Pairs re-traced with the cone by the last surrogate light stage. Synchronises. */
@@ -546,7 +559,10 @@ typedef struct DrvTuning {
                                  kernels (not while the stream is being captured) */
   int32_t plain_voxel_reads;  /* nonzero: the cone tracer reads the plain mip arrays instead of the
                                  corner-packed mip records; the result is the same bit for bit */
-  int32_t reserved[2];
+  int32_t surrogate_wait_test; /* test hook, nonzero: the surrogate pass withholds its first tensor-core
+                                  commit, so its bounded wait (~10 ms here) runs out; the stage then
+                                  reports DRV_ERR_TIMEOUT from drv_sync and leaves the shadowing unset */
+  int32_t reserved[1];
 } DrvTuning;
 enum { DRV_LIGHT_PATH_AUTO = 0, DRV_LIGHT_PATH_SINGLE = 1, DRV_LIGHT_PATH_SPLIT = 2 };
 drv_status drv_set_tuning(DrvContext* ctx, const DrvTuning* tuning);
