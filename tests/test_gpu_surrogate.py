@@ -85,10 +85,9 @@ def test_pairs_targets_are_cone_visibility(frame, lib):
     assert 0.05 < y.mean() < 0.999
     x = X.cpu().numpy()
     assert np.all(x[:, 17:31] == 0) and np.all(x[:, 31] == 1)  # padding, the constant input
-    # cone targets lie on surfaces inside the volume; caches sit on cascade
-    # corners, which may lie outside it
-    assert np.all((x[:, 3:6] >= -1e-3) & (x[:, 3:6] <= 1 + 1e-3))
-    assert np.all(np.isfinite(x[:, 0:3])) and np.all(np.abs(x[:, 0:3] - 0.5) < 2)
+    # normalised volume coordinates: caches sit on cascade corners and block
+    # cone targets on offset sample points, either may lie somewhat outside
+    assert np.all(np.isfinite(x[:, 0:6])) and np.all(np.abs(x[:, 0:6] - 0.5) < 2)
     assert np.allclose(np.linalg.norm(x[:, 6:9], axis=1), 1, atol=1e-3)  # VPL normal
     assert np.all((x[:, 9:17] >= 0) & (x[:, 9:17] <= 1))  # mip-3 opacity samples
     surrogate.set_features(frame.pipe, "cone4")
