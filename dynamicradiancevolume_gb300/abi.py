@@ -226,7 +226,9 @@ SURROGATE_PARAMS = 10562
 SURROGATE_ENUMERATE = 0xFFFFFFFFFFFFFFFF
 SURROGATE_FEATURES_SEGMENT8 = 0  # the configuration's 17 inputs
 SURROGATE_FEATURES_CONE4 = 1     # 27 inputs with the cone's first four samples
-SURROGATE_FEATURE_NAMES = {"segment8": SURROGATE_FEATURES_SEGMENT8, "cone4": SURROGATE_FEATURES_CONE4}
+SURROGATE_FEATURES_CONE8 = 2     # 23 inputs with eight samples of the cone's own sampler
+SURROGATE_FEATURE_NAMES = {"segment8": SURROGATE_FEATURES_SEGMENT8, "cone4": SURROGATE_FEATURES_CONE4,
+                           "cone8": SURROGATE_FEATURES_CONE8}
 
 
 def header_functions(header: Path) -> list[str]:

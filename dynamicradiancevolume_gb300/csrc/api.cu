@@ -817,7 +817,8 @@ drv_status drv_surrogate_eval(DrvContext* ctx, const float* features, int32_t n,
 
 drv_status drv_set_surrogate_features(DrvContext* ctx, int32_t feature_set) {
   if (!ctx) return DRV_ERR_INVALID_ARG;
-  if (feature_set != DRV_SURROGATE_FEATURES_SEGMENT8 && feature_set != DRV_SURROGATE_FEATURES_CONE4)
+  if (feature_set != DRV_SURROGATE_FEATURES_SEGMENT8 && feature_set != DRV_SURROGATE_FEATURES_CONE4 &&
+      feature_set != DRV_SURROGATE_FEATURES_CONE8)
     return fail(ctx, DRV_ERR_INVALID_ARG, "unknown surrogate feature set");
   ctx->sur_features = feature_set;
   return DRV_OK;

@@ -451,13 +451,16 @@ cudaError_t launch_tc(cudaStream_t s, const Rows& rows, uint32_t n_rows, const v
     if (dev >= 64 || !((done >> dev) & 1u)) {
       e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
+      // Four CTAs of ~47 KB per SM need the largest shared-memory carveout.
+      e = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               (int)cudaSharedmemCarveoutMaxShared);
+      if (e != cudaSuccess) return e;
       if (dev < 64) done |= 1ull << dev;
     }
   }
-  // At most four CTAs per SM: 4 x 64 tensor-memory columns of the SM's 512.
-  int per_sm = resident_ctas(reinterpret_cast<const void*>(kernel), kThreads, smem);
-  if (per_sm < 1) return cudaErrorInvalidConfiguration;
-  per_sm = per_sm > 4 ? 4 : per_sm;
+  // Four CTAs per SM (__launch_bounds__; 4 x 64 of the SM's 512 tensor-memory
+  // columns): the CTAs of one SM overlap each other's MMA round trips.
+  const int per_sm = 4;
   const uint32_t tiles = (n_rows + kThreads - 1) / kThreads;
   const uint32_t grid = tiles == 0 ? 1u : (tiles < (uint32_t)(num_sms * per_sm) ? tiles : (uint32_t)(num_sms * per_sm));
   kernel<<<grid, kThreads, smem, s>>>(rows, static_cast<const uint8_t*>(weights), err, hold_commit);
@@ -484,6 +487,12 @@ cudaError_t launch_surrogate_mlp(cudaStream_t s, const StageParams& p, const Pai
   // The row count is on the device (pairs the cull listed): the grid covers
   // the list's capacity and idle CTAs return after the first tile check.
   const uint32_t cap_rows = L.cap;
+  if (sa.feature_set == kFeatureCone8) {
+    if (bf16) return launch_tc(s, PairRows<true, kFeatureCone8>{p, L, sa.threshold}, cap_rows, sa.weights, sa.err,
+                               sa.hold_commit, num_sms);
+    return launch_tc(s, PairRows<false, kFeatureCone8>{p, L, sa.threshold}, cap_rows, sa.weights, sa.err,
+                     sa.hold_commit, num_sms);
+  }
   if (sa.feature_set == kFeatureCone4) {
     if (bf16) return launch_tc(s, PairRows<true, kFeatureCone4>{p, L, sa.threshold}, cap_rows, sa.weights, sa.err,
                                sa.hold_commit, num_sms);

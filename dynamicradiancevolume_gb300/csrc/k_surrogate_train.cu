@@ -135,7 +135,10 @@ __global__ void __launch_bounds__(128) pairs_kernel(PairParams p) {
   float nx, ny, nz;
   vpl_normal(la.vpls, p.bf16, lb * la.interval, nx, ny, nz);
   const float inv_extent = 1.0f / (p.voxel_size * p.vox.N);
-  if (p.feature_set == kFeatureCone4)
+  if (p.feature_set == kFeatureCone8)
+    pair_features<kFeatureCone8>(p.vox, inv_extent, p.vol_min, p.voxel_size, p.max_steps, cx, cy, cz, cone.x, cone.y,
+                                 cone.z, nx, ny, nz, cone.w, f);
+  else if (p.feature_set == kFeatureCone4)
     pair_features<kFeatureCone4>(p.vox, inv_extent, p.vol_min, p.voxel_size, p.max_steps, cx, cy, cz, cone.x, cone.y,
                                  cone.z, nx, ny, nz, cone.w, f);
   else

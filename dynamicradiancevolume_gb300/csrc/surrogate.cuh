@@ -30,6 +30,7 @@ constexpr int kOneInput = kMlpIn - 1;  // the constant-1 input
 // first four samples.
 constexpr int kFeatureSegment8 = 0;
 constexpr int kFeatureCone4 = 1;
+constexpr int kFeatureCone8 = 2;
 
 // Parameter offsets (floats) of the flat FP32 master copy; weights are
 // [out][in] row-major (in contiguous), biases follow each weight matrix.
@@ -172,6 +173,56 @@ __device__ __forceinline__ void segment_features(const VoxelView& v, float inv_e
   f[kOneInput] = 1.0f;
 }
 
+// Inputs 0-8 as segment_features, then eight samples of the cone's own
+// sampler (textureLod at the cone's level of detail, cacheLightingRSM.comp:
+// 216-221) at marched distances goal^((j + 1) / 8), j = 0..7 (geometric, as
+// the cone's steps grow), 17 their composited occlusion 1 - prod(1 - s),
+// 18 the aperture (x 8), 19 the march length in voxels (/ 64), 20-22 the
+// direction; 31 the constant 1.
+__device__ __forceinline__ void cone8_features(const VoxelView& v, float inv_extent, const float vol_min[3],
+                                               float voxel_size, float cx, float cy, float cz, float tx, float ty,
+                                               float tz, float nx, float ny, float nz, float dsr, float* f) {
+  const float px = (cx - vol_min[0]) * inv_extent, py = (cy - vol_min[1]) * inv_extent,
+              pz = (cz - vol_min[2]) * inv_extent;
+  const float qx = (tx - vol_min[0]) * inv_extent, qy = (ty - vol_min[1]) * inv_extent,
+              qz = (tz - vol_min[2]) * inv_extent;
+  f[0] = px;
+  f[1] = py;
+  f[2] = pz;
+  f[3] = qx;
+  f[4] = qy;
+  f[5] = qz;
+  f[6] = nx;
+  f[7] = ny;
+  f[8] = nz;
+  const float dx = tx - cx, dy = ty - cy, dz = tz - cz;
+  const float len = sqrtf(dx * dx + dy * dy + dz * dz);
+  const float inv_len = 1.0f / fmaxf(len, 1e-20f);
+  const float Dx = dx * inv_len, Dy = dy * inv_len, Dz = dz * inv_len;
+  const float goal = fmaxf(len / voxel_size - 2.0f, 1.0f);  // voxels the cone marches
+  const Coord P = voxel_pos(v, px, py, pz);
+  const float lg = __log2f(goal) * 0.125f;
+  float transmit = 1.0f;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const float d = exp2f(lg * (float)(j + 1));  // marched distance
+    const float at = 2.0f + d;                   // from the cache: the march starts 2 voxels out
+    const Coord U{P.x + Dx * at, P.y + Dy * at, P.z + Dz * at};
+    const float s = sample_voxels_at(v, U, __log2f(d * dsr));
+    f[9 + j] = s;
+    transmit *= 1.0f - s;
+  }
+  f[17] = 1.0f - transmit;
+  f[18] = dsr * 8.0f;
+  f[19] = goal * (1.0f / 64.0f);
+  f[20] = Dx;
+  f[21] = Dy;
+  f[22] = Dz;
+#pragma unroll
+  for (int i = 23; i < kOneInput; ++i) f[i] = 0.0f;
+  f[kOneInput] = 1.0f;
+}
+
 // Features of a pair in feature set FS.
 template <int FS>
 __device__ __forceinline__ void pair_features(const VoxelView& v, float inv_extent, const float vol_min[3],
@@ -180,6 +231,8 @@ __device__ __forceinline__ void pair_features(const VoxelView& v, float inv_exte
                                               float* f) {
   if (FS == kFeatureSegment8)
     segment_features(v, inv_extent, vol_min, cx, cy, cz, tx, ty, tz, nx, ny, nz, f);
+  else if (FS == kFeatureCone8)
+    cone8_features(v, inv_extent, vol_min, voxel_size, cx, cy, cz, tx, ty, tz, nx, ny, nz, dsr, f);
   else
     surrogate_features(v, inv_extent, vol_min, voxel_size, max_steps, cx, cy, cz, tx, ty, tz, nx, ny, nz, dsr, f);
 }

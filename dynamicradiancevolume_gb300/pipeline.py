@@ -462,14 +462,28 @@ def main(argv=None) -> int:
     ap.add_argument("--precision", choices=["fp32", "bf16"], default="fp32")
     ap.add_argument("--frames", type=int, default=4)
     ap.add_argument("--seed", type=int, default=None)
+    ap.add_argument("--max-caches", type=int, default=None, help="capacity (the pair list scales with it)")
+    ap.add_argument("--surrogate", default=None, help="surrogate visibility with this checkpoint (path stem)")
+    ap.add_argument("--threshold", type=float, default=0.5, help="surrogate confidence threshold")
     a = ap.parse_args(argv)
     w = scaled(WORKLOADS[a.workload], precision=abi.PRECISION_BF16 if a.precision == "bf16" else abi.PRECISION_FP32)
-    p = Pipeline(host_frame(w, a.seed))
+    if a.max_caches:
+        w = scaled(w, max_caches=a.max_caches)
+    if a.surrogate:
+        w = scaled(w, visibility=abi.VISIBILITY_SURROGATE)
+    hf = host_frame(w, a.seed)
+    hf.config.surrogate_conf_threshold = a.threshold
+    p = Pipeline(hf)
+    if a.surrogate:
+        from . import surrogate
+        surrogate.upload(p, surrogate.load_params(a.surrogate), surrogate.load_features(a.surrogate))
     p.raycast_inputs()
     for _ in range(a.frames):
         p.frame()
     p.sync()
     print("workload %s (%s): %d caches, %d lit pairs" % (w.name, a.precision, p.cache_count(), p.light_pairs()))
+    if a.surrogate:
+        print("surrogate: %d pairs evaluated, %d re-traced" % p.surrogate_stats())
     p.close()
     return 0
 

@@ -511,8 +511,12 @@ drv_status drv_set_surrogate_params(DrvContext* ctx, const float* params_device)
  *    between them (inputs 0-16);
  *  CONE4: 27 inputs, adding the cone's aperture and length, the direction,
  *    and the cone's own first four samples and their composited occlusion
- *    (mip-3 samples over the part of the segment the cone reaches). */
-enum { DRV_SURROGATE_FEATURES_SEGMENT8 = 0, DRV_SURROGATE_FEATURES_CONE4 = 1 };
+ *    (mip-3 samples over the part of the segment the cone reaches);
+ *  CONE8: inputs 0-8 as SEGMENT8, then eight samples of the cone's own
+ *    sampler at its level of detail at geometrically spaced marched
+ *    distances, their composited occlusion, the aperture, the march length
+ *    and the direction (23 inputs). */
+enum { DRV_SURROGATE_FEATURES_SEGMENT8 = 0, DRV_SURROGATE_FEATURES_CONE4 = 1, DRV_SURROGATE_FEATURES_CONE8 = 2 };
 drv_status drv_set_surrogate_features(DrvContext* ctx, int32_t feature_set);
 /* Training pairs from the context's current frame (after drv_extract_vpls,
  * drv_build_opacity_mips and drv_allocate_caches): random (cache, shadow
