@@ -186,6 +186,143 @@ __global__ void __launch_bounds__(kCullThreads) cull_kernel(StageParams p, PairL
   }
 }
 
+// ---- cull over VPL plane records in shared memory
+// The test of may_contribute, rewritten as a plane test: a VPL at p with
+// normal n faces the cache c when n . c - n . p > 0. Each VPL becomes one
+// 16-byte record {n, -n . p + eps (1 + |p|_inf)} (no-flux VPLs: -inf, never
+// live), staged once per CTA in shared memory; a cache passes when
+// n . c + w > -eps |c|_inf. The margin eps = 1e-5 covers the FP32 rounding of
+// both this sum and the gather's normalised test (a few u = 2^-24 relative to
+// |p| + |c|), so the cull stays a superset of the pairs the gather's exact
+// test keeps; the few extra near-tangent pairs are gathered with weight 0.
+// Each CTA tests kCullRecCaches caches per pass: one shared-memory load
+// serves that many tests of three FMAs each.
+constexpr int kCullRecThreads = 512;
+constexpr int kCullRecWarps = kCullRecThreads / 32;
+constexpr int kCullRecCaches = 4;
+constexpr float kCullRecEps = 1e-5f;
+constexpr size_t kCullRecMaxSmem = 220 * 1024;
+
+// Shared memory of cull_records_kernel: the records, then per cache of the
+// pass the ballot words and their exclusive prefix.
+inline size_t cull_records_smem(int total_vpls, int words) {
+  return (size_t)total_vpls * 16 + (size_t)2 * kCullRecCaches * words * 4;
+}
+
+template <bool BF16>
+__global__ void __launch_bounds__(kCullRecThreads) cull_records_kernel(StageParams p, PairList L, int total_vpls) {
+  pdl_wait_and_release();
+  extern __shared__ float4 s_rec[];
+  __shared__ uint32_t s_base[kCullRecCaches], s_count[kCullRecCaches];
+  const int W = (p.total_blocks + 31) >> 5;
+  uint32_t* s_mask = reinterpret_cast<uint32_t*>(s_rec + total_vpls);  // [K][W]
+  uint32_t* s_pre = s_mask + kCullRecCaches * W;                        // [K][W]
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // VPL records, in light order (light l's VPLs from vpl_base(l)).
+  for (int g = threadIdx.x; g < total_vpls; g += kCullRecThreads) {
+    int l = 0, base = 0;
+    while (g >= base + p.ll.lights[l].n_vpls) base += p.ll.lights[l].n_vpls, ++l;
+    const VplData v = load_vpl<BF16>(p.ll.lights[l].vpls, g - base);
+    float4 r;
+    r.x = v.nx;
+    r.y = v.ny;
+    r.z = v.nz;
+    const float pm = fmaxf(fmaxf(fabsf(v.px), fabsf(v.py)), fabsf(v.pz));
+    const bool flux = v.fr > 0.0f || v.fg > 0.0f || v.fb > 0.0f;
+    r.w = flux ? -(v.nx * v.px + v.ny * v.py + v.nz * v.pz) + kCullRecEps * (1.0f + pm) : -INFINITY;
+    s_rec[g] = r;
+  }
+  __syncthreads();
+  const uint32_t n_caches = cache_count(p);
+  for (uint32_t c0 = blockIdx.x * kCullRecCaches; c0 < n_caches; c0 += gridDim.x * kCullRecCaches) {
+    float cx[kCullRecCaches], cy[kCullRecCaches], cz[kCullRecCaches], lim[kCullRecCaches];
+#pragma unroll
+    for (int k = 0; k < kCullRecCaches; ++k) {
+      const uint32_t c = min(c0 + k, n_caches - 1u);  // past the end: a copy of the last cache, not written
+      cache_position<BF16>(p, c, cx[k], cy[k], cz[k]);
+      lim[k] = -kCullRecEps * fmaxf(fmaxf(fabsf(cx[k]), fabsf(cy[k])), fabsf(cz[k]));
+    }
+    for (int w = warp; w < W; w += kCullRecWarps) {
+      const int b = (w << 5) + lane;
+      bool live[kCullRecCaches];
+#pragma unroll
+      for (int k = 0; k < kCullRecCaches; ++k) live[k] = false;
+      if (b < p.total_blocks) {
+        int l = 0, vbase = 0;
+        while (b >= p.block_base[l + 1]) vbase += p.ll.lights[l].n_vpls, ++l;
+        const int interval = p.ll.lights[l].interval;
+        const int first = vbase + (b - p.block_base[l]) * interval;
+        for (int j = 0; j < interval; ++j) {
+          const float4 r = s_rec[first + j];
+#pragma unroll
+          for (int k = 0; k < kCullRecCaches; ++k)
+            live[k] |= fmaf(r.x, cx[k], fmaf(r.y, cy[k], fmaf(r.z, cz[k], r.w))) > lim[k];
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < kCullRecCaches; ++k) {
+        const uint32_t m = __ballot_sync(0xffffffffu, live[k]);
+        if (lane == 0) s_mask[k * W + w] = m;
+      }
+    }
+    __syncthreads();
+    // Warp k: exclusive prefix of cache k's word popcounts, then its run of
+    // the pair list (one atomic per cache).
+    if (warp < kCullRecCaches && c0 + warp < n_caches) {
+      const int k = warp;
+      const uint32_t c = c0 + k;
+      const int per = (W + 31) >> 5;
+      const int w0 = lane * per;
+      uint32_t local = 0;
+      for (int q = 0; q < per; ++q)
+        if (w0 + q < W) local += __popc(s_mask[k * W + w0 + q]);
+      uint32_t incl = local;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+      }
+      const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+      uint32_t run = incl - local;
+      for (int q = 0; q < per; ++q)
+        if (w0 + q < W) {
+          s_pre[k * W + w0 + q] = run;
+          run += __popc(s_mask[k * W + w0 + q]);
+        }
+      if (lane == 0) {
+        const uint32_t base = total ? atomicAdd(L.counters, total) : 0u;
+        const bool over = (uint64_t)base + total > (uint64_t)L.cap;
+        L.info[2 * c] = base;
+        L.info[2 * c + 1] = over ? kPairOverflow : total;
+        s_base[k] = base;
+        s_count[k] = over ? kPairOverflow : total;
+      }
+    }
+    __syncthreads();
+    const int nk = (int)min((uint32_t)kCullRecCaches, n_caches - c0);
+    for (int idx = warp; idx < nk * W; idx += kCullRecWarps) {
+      const int k = idx / W, w = idx - k * W;
+      const uint32_t base = s_base[k];
+      if (s_count[k] != kPairOverflow) {
+        const uint32_t m = s_mask[idx];
+        if ((m >> lane) & 1u) {
+          const uint32_t i = base + s_pre[idx] + __popc(m & ((1u << lane) - 1u));
+          L.cache[i] = c0 + k;
+          L.block[i] = (uint32_t)((w << 5) + lane);
+        }
+      } else if (w == 0) {
+        // The list is full: the gather traces this cache itself; the claimed
+        // slots below the capacity stay empty.
+        uint32_t total = 0;
+        for (int q = 0; q < W; ++q) total += __popc(s_mask[k * W + q]);
+        const uint32_t end = (uint32_t)min((uint64_t)base + total, (uint64_t)L.cap);
+        for (uint32_t i = base + lane; i < end; i += 32) L.block[i] = kNoPair;
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // Cone class of a pair: about how many steps its cone marches when nothing
 // occludes it, in buckets of 4, and at which step, if any, its radius passes
 // one voxel (its samples move to mip levels): never, after step 16, after
@@ -529,6 +666,23 @@ cudaError_t launch_persistent_after(void (*kernel)(KArgs...), int threads, size_
   return launch_after(kernel, num_sms * per_sm, threads, smem, s, args...);
 }
 
+// Raises a kernel's dynamic shared-memory limit, once per (kernel, device).
+template <typename... KArgs>
+cudaError_t set_max_smem(void (*kernel)(KArgs...), size_t bytes) {
+  static std::mutex mu;
+  static uint64_t done = 0;  // bit d: set on device d
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(mu);
+  if (dev < 64 && ((done >> dev) & 1u)) return cudaSuccess;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                                 (int)cudaSharedmemCarveoutMaxShared);
+  if (e == cudaSuccess && dev < 64) done |= 1ull << dev;
+  return e;
+}
+
 // events (optional, DRV_LK_COUNT + 1): recorded before the first kernel and
 // after each kernel slot, skipped slots included, so slot k's time is
 // elapsed(events[k], events[k + 1]).
@@ -541,8 +695,18 @@ cudaError_t split_variant(cudaStream_t s, const StageParams& p, const PairList& 
   auto mark = [&](int k) { return ev ? cudaEventRecord(ev[k], s) : cudaSuccess; };
   cudaError_t e = cudaMemsetAsync(L.counters, 0, kPairCounters * sizeof(uint32_t), s);
   if (e != cudaSuccess || (e = mark(DRV_LK_CULL)) != cudaSuccess) return e;
-  const size_t cull_smem = (size_t)((p.total_blocks + 31) >> 5) * 2 * sizeof(uint32_t);
-  if ((e = launch_persistent(cull_kernel<BF16>, kCullThreads, cull_smem, s, num_sms, p, L)) != cudaSuccess) return e;
+  int total_vpls = 0;
+  for (int l = 0; l < p.ll.n_lights; ++l) total_vpls += p.ll.lights[l].n_vpls;
+  const int words = (p.total_blocks + 31) >> 5;
+  const size_t rec_smem = cull_records_smem(total_vpls, words);
+  if (rec_smem <= kCullRecMaxSmem) {
+    if ((e = set_max_smem(cull_records_kernel<BF16>, kCullRecMaxSmem)) != cudaSuccess) return e;
+    e = launch_persistent(cull_records_kernel<BF16>, kCullRecThreads, rec_smem, s, num_sms, p, L, total_vpls);
+  } else {
+    const size_t cull_smem = (size_t)words * 2 * sizeof(uint32_t);
+    e = launch_persistent(cull_kernel<BF16>, kCullThreads, cull_smem, s, num_sms, p, L);
+  }
+  if (e != cudaSuccess) return e;
   if ((e = mark(DRV_LK_CLASSIFY)) != cudaSuccess) return e;
   if (!sur.weights) {
     if ((e = launch_persistent_after(classify_kernel<BF16>, kClassThreads, 0, s, num_sms, p, L)) != cudaSuccess)
