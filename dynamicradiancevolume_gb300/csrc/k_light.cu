@@ -667,19 +667,23 @@ cudaError_t launch_persistent_after(void (*kernel)(KArgs...), int threads, size_
 }
 
 // Raises a kernel's dynamic shared-memory limit, once per (kernel, device).
-template <typename... KArgs>
-cudaError_t set_max_smem(void (*kernel)(KArgs...), size_t bytes) {
+cudaError_t set_max_smem(const void* kernel, size_t bytes) {
+  struct Done {
+    const void* kernel;
+    int device;
+  };
   static std::mutex mu;
-  static uint64_t done = 0;  // bit d: set on device d
+  static std::vector<Done> done;
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   std::lock_guard<std::mutex> lock(mu);
-  if (dev < 64 && ((done >> dev) & 1u)) return cudaSuccess;
+  for (const Done& d : done)
+    if (d.kernel == kernel && d.device == dev) return cudaSuccess;
   e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
                                                  (int)cudaSharedmemCarveoutMaxShared);
-  if (e == cudaSuccess && dev < 64) done |= 1ull << dev;
+  if (e == cudaSuccess) done.push_back(Done{kernel, dev});
   return e;
 }
 
@@ -700,7 +704,8 @@ cudaError_t split_variant(cudaStream_t s, const StageParams& p, const PairList& 
   const int words = (p.total_blocks + 31) >> 5;
   const size_t rec_smem = cull_records_smem(total_vpls, words);
   if (rec_smem <= kCullRecMaxSmem) {
-    if ((e = set_max_smem(cull_records_kernel<BF16>, kCullRecMaxSmem)) != cudaSuccess) return e;
+    if ((e = set_max_smem(reinterpret_cast<const void*>(cull_records_kernel<BF16>), kCullRecMaxSmem)) != cudaSuccess)
+      return e;
     e = launch_persistent(cull_records_kernel<BF16>, kCullRecThreads, rec_smem, s, num_sms, p, L, total_vpls);
   } else {
     const size_t cull_smem = (size_t)words * 2 * sizeof(uint32_t);
