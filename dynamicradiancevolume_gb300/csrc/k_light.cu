@@ -209,7 +209,9 @@ inline size_t cull_records_smem(int total_vpls, int words) {
   return (size_t)total_vpls * 16 + (size_t)2 * kCullRecCaches * words * 4;
 }
 
-template <bool BF16>
+// UNIT: every light's shadow blocks are single VPLs, so block b's record is
+// record b.
+template <bool BF16, bool UNIT>
 __global__ void __launch_bounds__(kCullRecThreads) cull_records_kernel(StageParams p, PairList L, int total_vpls) {
   pdl_wait_and_release();
   extern __shared__ float4 s_rec[];
@@ -248,15 +250,22 @@ __global__ void __launch_bounds__(kCullRecThreads) cull_records_kernel(StagePara
 #pragma unroll
       for (int k = 0; k < kCullRecCaches; ++k) live[k] = false;
       if (b < p.total_blocks) {
-        int l = 0, vbase = 0;
-        while (b >= p.block_base[l + 1]) vbase += p.ll.lights[l].n_vpls, ++l;
-        const int interval = p.ll.lights[l].interval;
-        const int first = vbase + (b - p.block_base[l]) * interval;
-        for (int j = 0; j < interval; ++j) {
-          const float4 r = s_rec[first + j];
+        if (UNIT) {
+          const float4 r = s_rec[b];
 #pragma unroll
           for (int k = 0; k < kCullRecCaches; ++k)
-            live[k] |= fmaf(r.x, cx[k], fmaf(r.y, cy[k], fmaf(r.z, cz[k], r.w))) > lim[k];
+            live[k] = fmaf(r.x, cx[k], fmaf(r.y, cy[k], fmaf(r.z, cz[k], r.w))) > lim[k];
+        } else {
+          int l = 0, vbase = 0;
+          while (b >= p.block_base[l + 1]) vbase += p.ll.lights[l].n_vpls, ++l;
+          const int interval = p.ll.lights[l].interval;
+          const int first = vbase + (b - p.block_base[l]) * interval;
+          for (int j = 0; j < interval; ++j) {
+            const float4 r = s_rec[first + j];
+#pragma unroll
+            for (int k = 0; k < kCullRecCaches; ++k)
+              live[k] |= fmaf(r.x, cx[k], fmaf(r.y, cy[k], fmaf(r.z, cz[k], r.w))) > lim[k];
+          }
         }
       }
 #pragma unroll
@@ -300,17 +309,19 @@ __global__ void __launch_bounds__(kCullRecThreads) cull_records_kernel(StagePara
     }
     __syncthreads();
     const int nk = (int)min((uint32_t)kCullRecCaches, n_caches - c0);
-    for (int idx = warp; idx < nk * W; idx += kCullRecWarps) {
-      const int k = idx / W, w = idx - k * W;
-      const uint32_t base = s_base[k];
+    const uint32_t below = (1u << lane) - 1u;
+    for (int k = 0; k < nk; ++k) {
+      const uint32_t base = s_base[k], c = c0 + k;
       if (s_count[k] != kPairOverflow) {
-        const uint32_t m = s_mask[idx];
-        if ((m >> lane) & 1u) {
-          const uint32_t i = base + s_pre[idx] + __popc(m & ((1u << lane) - 1u));
-          L.cache[i] = c0 + k;
-          L.block[i] = (uint32_t)((w << 5) + lane);
+        for (int w = warp; w < W; w += kCullRecWarps) {
+          const uint32_t m = s_mask[k * W + w];
+          if ((m >> lane) & 1u) {
+            const uint32_t i = base + s_pre[k * W + w] + __popc(m & below);
+            L.cache[i] = c;
+            L.block[i] = (uint32_t)((w << 5) + lane);
+          }
         }
-      } else if (w == 0) {
+      } else if (warp == 0) {
         // The list is full: the gather traces this cache itself; the claimed
         // slots below the capacity stay empty.
         uint32_t total = 0;
@@ -458,6 +469,37 @@ __global__ void __launch_bounds__(128) cone_kernel(StageParams p, PairList L) {
   }
 }
 
+// Sum over the warp of each lane's v[0..N-1] (N = 16 or 32), returned in
+// lane k for value k (lanes >= N get nothing useful): at each step a lane
+// keeps the half of its values its own half of the warp will own, sends the
+// other half to the partner lane and adds what it receives, so the 32-value
+// case takes 16 + 8 + 4 + 2 + 1 = 31 shuffles instead of 32 x 5.
+template <int N>
+__device__ __forceinline__ float warp_transpose_reduce(float (&v)[32], int lane) {
+  // Values N..31 are unused: first fold lane halves when N = 16.
+  int n = N;
+#pragma unroll
+  for (int half = 16; half >= 1; half >>= 1) {
+    if (half >= n) {  // fewer values than lanes in this half: plain butterfly on each
+#pragma unroll
+      for (int i = 0; i < 32; ++i)
+        if (i < n) v[i] += __shfl_xor_sync(0xffffffffu, v[i], half);
+      continue;
+    }
+    const bool upper = (lane & half) != 0;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      if (i < n / 2) {
+        const float send = upper ? v[i] : v[i + n / 2];
+        const float keep = upper ? v[i + n / 2] : v[i];
+        v[i] = keep + __shfl_xor_sync(0xffffffffu, send, half);
+      }
+    }
+    n /= 2;
+  }
+  return v[0];
+}
+
 constexpr int kGatherThreads = 256;
 constexpr int kGatherWarps = kGatherThreads / 32;
 
@@ -516,12 +558,13 @@ __global__ void __launch_bounds__(kGatherThreads, BF16 ? 2 : 3) gather_kernel(St
         __syncthreads();
       }
     }
+    {
+      // Warp reduction of the NK*3 sums: lane k ends up with coefficient k.
+      float v[32];
 #pragma unroll
-    for (int k = 0; k < NK * 3; ++k) {
-      float v = KAHAN ? __fsub_rn(acc[k], comp[k]) : acc[k];
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-      if (lane == 0) s_red[warp][k] = v;
+      for (int k = 0; k < 32; ++k) v[k] = k < NK * 3 ? (KAHAN ? __fsub_rn(acc[k], comp[k]) : acc[k]) : 0.0f;
+      const float mine = warp_transpose_reduce<NK * 3 <= 16 ? 16 : 32>(v, lane);
+      if (lane < NK * 3) s_red[warp][lane] = mine;
     }
     __syncthreads();
     if (threadIdx.x < NK * 3) {
@@ -704,9 +747,11 @@ cudaError_t split_variant(cudaStream_t s, const StageParams& p, const PairList& 
   const int words = (p.total_blocks + 31) >> 5;
   const size_t rec_smem = cull_records_smem(total_vpls, words);
   if (rec_smem <= kCullRecMaxSmem) {
-    if ((e = set_max_smem(reinterpret_cast<const void*>(cull_records_kernel<BF16>), kCullRecMaxSmem)) != cudaSuccess)
-      return e;
-    e = launch_persistent(cull_records_kernel<BF16>, kCullRecThreads, rec_smem, s, num_sms, p, L, total_vpls);
+    bool unit = true;
+    for (int l = 0; l < p.ll.n_lights; ++l) unit = unit && p.ll.lights[l].interval == 1;
+    auto kernel = unit ? cull_records_kernel<BF16, true> : cull_records_kernel<BF16, false>;
+    if ((e = set_max_smem(reinterpret_cast<const void*>(kernel), kCullRecMaxSmem)) != cudaSuccess) return e;
+    e = launch_persistent(kernel, kCullRecThreads, rec_smem, s, num_sms, p, L, total_vpls);
   } else {
     const size_t cull_smem = (size_t)words * 2 * sizeof(uint32_t);
     e = launch_persistent(cull_kernel<BF16>, kCullThreads, cull_smem, s, num_sms, p, L);
