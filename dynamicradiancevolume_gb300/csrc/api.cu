@@ -68,6 +68,7 @@ void release(Context* c) {
     }
     cudaFree(c->vpls[l]);
     cudaFree(c->cones[l]);
+    cudaFree(c->vpl_records[l]);
   }
   cudaFree(c->d_boxes);
   cudaFreeHost(c->h_boxes);
@@ -295,6 +296,7 @@ drv_status drv_create(const DrvConfig* cfg, DrvContext** out) {
     }
     if ((e = cudaMalloc(&c->vpls[l], (size_t)R * R * sizeof(DrvVPL))) != cudaSuccess) return bail(e);
     if ((e = cudaMalloc(&c->cones[l], (size_t)R * R * sizeof(DrvShadowCone))) != cudaSuccess) return bail(e);
+    if ((e = cudaMalloc(&c->vpl_records[l], (size_t)R * R * sizeof(float4))) != cudaSuccess) return bail(e);
   }
   if ((e = cudaMalloc(&c->sur_weights, drv::surrogate_weights_bytes())) != cudaSuccess) return bail(e);
   // Pair list of the split light stage: room for 256 contributing shadow
@@ -549,7 +551,8 @@ drv_status drv_extract_vpls(DrvContext* ctx, int32_t li, const DrvSpotLight* L) 
   if (L->indirect_shadow_sample_interval < 1) return DRV_ERR_INVALID_ARG;
   DRV_TRY_CUDA(ctx, drv::launch_extract_vpls(ctx->s(), *L, R, ch.flux[read_lod], ch.normal[read_lod], ch.dls[read_lod],
                                              ch.half(read_lod), ch.dls[shadow_level], ch.half(shadow_level),
-                                             ctx->vpls[li], ctx->cones[li], ctx->cfg.precision));
+                                             ctx->vpls[li], ctx->cones[li], ctx->cfg.precision,
+                                             ctx->vpl_records[li]));
   ctx->n_vpls[li] = R * R;
   ctx->interval[li] = L->indirect_shadow_sample_interval;
   ctx->n_cones[li] = (R * R + L->indirect_shadow_sample_interval - 1) / L->indirect_shadow_sample_interval;
@@ -649,6 +652,7 @@ drv_status light_caches(DrvContext* ctx, const DrvSpotLight* lights, int32_t n_l
     ll.lights[l].cones = ctx->cones[l];
     ll.lights[l].n_vpls = ctx->n_vpls[l];
     ll.lights[l].interval = ctx->interval[l];
+    ll.lights[l].records = ctx->vpl_records[l];
   }
   const bool surrogate = ctx->cfg.visibility == DRV_VISIBILITY_SURROGATE && ctx->cfg.indirect_shadow;
   if (surrogate && !ctx->sur_ready)
@@ -677,6 +681,7 @@ drv_status light_caches(DrvContext* ctx, const DrvSpotLight* lights, int32_t n_l
     }
     drv_status st = cuda_check(ctx, drv::launch_light_split(ctx->s(), ctx->cfg, *vol, ll, ctx->counter, ctx->entries,
                                                             ctx->entry_stride, ctx->light_voxels(), pairs, sur,
+                                                            ctx->scratch_words + 1,
                                                             ctx->tuning.cone_ctas_per_sm,
                                                             ctx->tuning.gather_ctas_per_sm, ctx->num_sms, events,
                                                             voxels_ready),

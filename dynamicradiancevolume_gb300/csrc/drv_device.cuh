@@ -256,4 +256,15 @@ __device__ __forceinline__ uint32_t pack_cell(int x, int y, int z, int c) {
 // Atomic OR of device error bits.
 __device__ __forceinline__ void raise_error(uint32_t* err, uint32_t bits) { atomicOr(err, bits); }
 
+// Cull record of a VPL as the light stage stores it (normal n, position p,
+// flux positive or not): the plane {n, -n . p + eps (1 + |p|_inf)}, or -inf in
+// w when it has no flux (no cache can see it). A cache c passes when
+// n . c + w > -eps |c|_inf (k_light.cu, cull_records_kernel).
+constexpr float kCullRecordEps = 1e-5f;
+__device__ __forceinline__ float4 make_cull_record(float nx, float ny, float nz, float px, float py, float pz,
+                                                   bool flux) {
+  const float pm = fmaxf(fmaxf(fabsf(px), fabsf(py)), fabsf(pz));
+  return make_float4(nx, ny, nz, flux ? -(nx * px + ny * py + nz * pz) + kCullRecordEps * (1.0f + pm) : -INFINITY);
+}
+
 }  // namespace drv

@@ -51,6 +51,7 @@ struct LightArgs {
   const DrvShadowCone* cones;
   int n_vpls;
   int interval;  // IndirectShadowComputationSampleInterval
+  const float4* records = nullptr;  // the cull's VPL plane records (make_cull_record), or none
 };
 
 struct LightLaunch {
@@ -187,6 +188,7 @@ struct Context {
   RsmChain rsm[DRV_MAX_LIGHTS];
   void* vpls[DRV_MAX_LIGHTS] = {};  // DrvVPL or DrvVPLBF16 per cfg.precision
   DrvShadowCone* cones[DRV_MAX_LIGHTS] = {};
+  float4* vpl_records[DRV_MAX_LIGHTS] = {};  // the cull's plane record of every VPL (written by the extraction)
   int n_vpls[DRV_MAX_LIGHTS] = {};
   int n_cones[DRV_MAX_LIGHTS] = {};
   int interval[DRV_MAX_LIGHTS] = {};
@@ -237,7 +239,7 @@ cudaError_t launch_downsample_rsm(cudaStream_t s, int res, const void* flux, con
                                   int src_half, float* fo, int16_t* no, float* dlo);
 cudaError_t launch_extract_vpls(cudaStream_t s, const DrvSpotLight& L, int res, const void* flux, const int16_t* nrm,
                                 const void* dls, int read_half, const void* dls_shadow, int shadow_half, void* vpls,
-                                DrvShadowCone* cones, int precision);
+                                DrvShadowCone* cones, int precision, float4* records);
 cudaError_t launch_voxelize(cudaStream_t s, const DrvBox* boxes, int n_boxes, const DrvVolumeInfo& vol, int n,
                             uint32_t* bits);
 cudaError_t launch_voxelize_triangles(cudaStream_t s, const float* positions, int n_vertices, const uint32_t* indices,
@@ -271,7 +273,7 @@ bool light_split_supported(const DrvConfig& cfg, const LightLaunch& ll);
 cudaError_t launch_light_split(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const LightLaunch& ll,
                                const DrvCacheCounter* counter, void* entries, uint32_t entry_stride,
                                const VoxelInputs& vox, const PairList& pairs, const SurrogateArgs& sur,
-                               int cone_ctas_per_sm, int gather_ctas_per_sm, int num_sms,
+                               uint32_t* err, int cone_ctas_per_sm, int gather_ctas_per_sm, int num_sms,
                                cudaEvent_t* events = nullptr, cudaEvent_t voxels_ready = nullptr);
 cudaError_t launch_bruteforce_rsm(cudaStream_t s, const DrvPerFrame& f, const DrvGBufferView& g,
                                   const float* rough_metal, const LightLaunch& ll, int bf16, float* out_rgb,

@@ -74,6 +74,7 @@ StageParams make_stage_params(const DrvConfig& cfg, const DrvVolumeInfo& vol, co
   p.ev[3] = (float)std::sqrt(5.0 / (16.0 * kPi));
   p.ev[4] = (float)std::sqrt(15.0 / (16.0 * kPi));
   p.spec = cfg.specular_envmap_size > 0;
+  p.err = nullptr;
   return p;
 }
 
@@ -200,7 +201,6 @@ __global__ void __launch_bounds__(kCullThreads) cull_kernel(StageParams p, PairL
 constexpr int kCullRecThreads = 512;
 constexpr int kCullRecWarps = kCullRecThreads / 32;
 constexpr int kCullRecCaches = 4;
-constexpr float kCullRecEps = 1e-5f;
 constexpr size_t kCullRecMaxSmem = 220 * 1024;
 
 // Shared memory of cull_records_kernel: the records, then per cache of the
@@ -210,31 +210,78 @@ inline size_t cull_records_smem(int total_vpls, int words) {
 }
 
 // UNIT: every light's shadow blocks are single VPLs, so block b's record is
-// record b.
-template <bool BF16, bool UNIT>
+// record b. COPY: every light has its records in global memory (written by
+// the VPL extraction); one bulk asynchronous copy per light (TMA, completion
+// on an mbarrier, bounded wait) stages them, instead of computing them here
+// from the VPLs.
+template <bool BF16, bool UNIT, bool COPY>
 __global__ void __launch_bounds__(kCullRecThreads) cull_records_kernel(StageParams p, PairList L, int total_vpls) {
   pdl_wait_and_release();
   extern __shared__ float4 s_rec[];
   __shared__ uint32_t s_base[kCullRecCaches], s_count[kCullRecCaches];
+  __shared__ __align__(8) uint64_t s_bar;
   const int W = (p.total_blocks + 31) >> 5;
   uint32_t* s_mask = reinterpret_cast<uint32_t*>(s_rec + total_vpls);  // [K][W]
   uint32_t* s_pre = s_mask + kCullRecCaches * W;                        // [K][W]
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   // VPL records, in light order (light l's VPLs from vpl_base(l)).
-  for (int g = threadIdx.x; g < total_vpls; g += kCullRecThreads) {
-    int l = 0, base = 0;
-    while (g >= base + p.ll.lights[l].n_vpls) base += p.ll.lights[l].n_vpls, ++l;
-    const VplData v = load_vpl<BF16>(p.ll.lights[l].vpls, g - base);
-    float4 r;
-    r.x = v.nx;
-    r.y = v.ny;
-    r.z = v.nz;
-    const float pm = fmaxf(fmaxf(fabsf(v.px), fabsf(v.py)), fabsf(v.pz));
-    const bool flux = v.fr > 0.0f || v.fg > 0.0f || v.fb > 0.0f;
-    r.w = flux ? -(v.nx * v.px + v.ny * v.py + v.nz * v.pz) + kCullRecEps * (1.0f + pm) : -INFINITY;
-    s_rec[g] = r;
+  if (COPY) {
+    const uint32_t bar = (uint32_t)__cvta_generic_to_shared(&s_bar);
+    if (threadIdx.x == 0) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(total_vpls * 16)
+                   : "memory");
+      int base = 0;
+      for (int l = 0; l < p.ll.n_lights; ++l) {
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                         (uint32_t)__cvta_generic_to_shared(s_rec + base)),
+                     "l"(p.ll.lights[l].records), "r"(p.ll.lights[l].n_vpls * 16), "r"(bar)
+                     : "memory");
+        base += p.ll.lights[l].n_vpls;
+      }
+    }
+    __syncthreads();  // the barrier is initialised before anyone waits on it
+    bool ok = false;
+    const unsigned long long t0 = clock64();
+    for (;;) {
+      uint32_t done;
+      asm volatile(
+          "{\n.reg .pred q;\nmbarrier.try_wait.parity.shared::cta.b64 q, [%1], 0;\nselp.u32 %0, 1, 0, q;\n}\n"
+          : "=r"(done)
+          : "r"(bar)
+          : "memory");
+      if (done) {
+        ok = true;
+        break;
+      }
+      if ((unsigned long long)(clock64() - t0) > 2000000000ull) break;  // about a second
+    }
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0 && p.err) raise_error(p.err, DRV_DEVERR_TIMEOUT);
+      // the copies may still be in flight: wait for them once more (bounded)
+      // before this CTA's shared memory is released
+      const unsigned long long t1 = clock64();
+      for (;;) {
+        uint32_t done;
+        asm volatile(
+            "{\n.reg .pred q;\nmbarrier.try_wait.parity.shared::cta.b64 q, [%1], 0;\nselp.u32 %0, 1, 0, q;\n}\n"
+            : "=r"(done)
+            : "r"(bar)
+            : "memory");
+        if (done || (unsigned long long)(clock64() - t1) > 2000000000ull) break;
+      }
+      return;
+    }
+  } else {
+    for (int g = threadIdx.x; g < total_vpls; g += kCullRecThreads) {
+      int l = 0, base = 0;
+      while (g >= base + p.ll.lights[l].n_vpls) base += p.ll.lights[l].n_vpls, ++l;
+      const VplData v = load_vpl<BF16>(p.ll.lights[l].vpls, g - base);
+      s_rec[g] = make_cull_record(v.nx, v.ny, v.nz, v.px, v.py, v.pz, v.fr > 0.0f || v.fg > 0.0f || v.fb > 0.0f);
+    }
+    __syncthreads();
   }
-  __syncthreads();
   const uint32_t n_caches = cache_count(p);
   for (uint32_t c0 = blockIdx.x * kCullRecCaches; c0 < n_caches; c0 += gridDim.x * kCullRecCaches) {
     float cx[kCullRecCaches], cy[kCullRecCaches], cz[kCullRecCaches], lim[kCullRecCaches];
@@ -242,7 +289,7 @@ __global__ void __launch_bounds__(kCullRecThreads) cull_records_kernel(StagePara
     for (int k = 0; k < kCullRecCaches; ++k) {
       const uint32_t c = min(c0 + k, n_caches - 1u);  // past the end: a copy of the last cache, not written
       cache_position<BF16>(p, c, cx[k], cy[k], cz[k]);
-      lim[k] = -kCullRecEps * fmaxf(fmaxf(fabsf(cx[k]), fabsf(cy[k])), fabsf(cz[k]));
+      lim[k] = -kCullRecordEps * fmaxf(fmaxf(fabsf(cx[k]), fabsf(cy[k])), fabsf(cz[k]));
     }
     for (int w = warp; w < W; w += kCullRecWarps) {
       const int b = (w << 5) + lane;
@@ -747,9 +794,13 @@ cudaError_t split_variant(cudaStream_t s, const StageParams& p, const PairList& 
   const int words = (p.total_blocks + 31) >> 5;
   const size_t rec_smem = cull_records_smem(total_vpls, words);
   if (rec_smem <= kCullRecMaxSmem) {
-    bool unit = true;
-    for (int l = 0; l < p.ll.n_lights; ++l) unit = unit && p.ll.lights[l].interval == 1;
-    auto kernel = unit ? cull_records_kernel<BF16, true> : cull_records_kernel<BF16, false>;
+    bool unit = true, copy = true;
+    for (int l = 0; l < p.ll.n_lights; ++l) {
+      unit = unit && p.ll.lights[l].interval == 1;
+      copy = copy && p.ll.lights[l].records != nullptr;
+    }
+    auto kernel = unit ? (copy ? cull_records_kernel<BF16, true, true> : cull_records_kernel<BF16, true, false>)
+                       : (copy ? cull_records_kernel<BF16, false, true> : cull_records_kernel<BF16, false, false>);
     if ((e = set_max_smem(reinterpret_cast<const void*>(kernel), kCullRecMaxSmem)) != cudaSuccess) return e;
     e = launch_persistent(kernel, kCullRecThreads, rec_smem, s, num_sms, p, L, total_vpls);
   } else {
@@ -837,9 +888,10 @@ bool light_split_supported(const DrvConfig& cfg, const LightLaunch& ll) {
 cudaError_t launch_light_split(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const LightLaunch& ll,
                                const DrvCacheCounter* counter, void* entries, uint32_t entry_stride,
                                const VoxelInputs& vox, const PairList& pairs, const SurrogateArgs& sur,
-                               int cone_ctas_per_sm, int gather_ctas_per_sm, int num_sms, cudaEvent_t* events,
-                               cudaEvent_t voxels_ready) {
-  const StageParams p = make_stage_params(cfg, vol, ll, counter, entries, entry_stride, vox);
+                               uint32_t* err, int cone_ctas_per_sm, int gather_ctas_per_sm, int num_sms,
+                               cudaEvent_t* events, cudaEvent_t voxels_ready) {
+  StageParams p = make_stage_params(cfg, vol, ll, counter, entries, entry_stride, vox);
+  p.err = err;
   const bool bf16 = cfg.precision == DRV_PRECISION_BF16;
   if (cfg.sh_order == 2)
     return bf16 ? split_variant<9, true>(s, p, pairs, sur, cone_ctas_per_sm, gather_ctas_per_sm, num_sms, events, voxels_ready)

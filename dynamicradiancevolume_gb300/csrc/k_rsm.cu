@@ -68,7 +68,8 @@ __global__ void __launch_bounds__(256) extract_kernel(DrvSpotLight L, int R, con
                                                       const int16_t* __restrict__ nrm, const void* __restrict__ dls,
                                                       int read_half, const void* __restrict__ dls_shadow,
                                                       int shadow_half, void* __restrict__ vpls_out,
-                                                      DrvShadowCone* __restrict__ cones) {
+                                                      DrvShadowCone* __restrict__ cones,
+                                                      float4* __restrict__ records) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   int n = R * R;
   if (i >= n) return;
@@ -94,6 +95,12 @@ __global__ void __launch_bounds__(256) extract_kernel(DrvSpotLight L, int R, con
       o.normal_bf16[2] = to_bf16(nn.z);
       o._pad = 0u;
       reinterpret_cast<DrvVPLBF16*>(vpls_out)[i] = o;
+      // the cull's record of the stored (BF16) normal and flux
+      if (records)
+        records[i] = make_cull_record(from_bf16(o.normal_bf16[0]), from_bf16(o.normal_bf16[1]),
+                                      from_bf16(o.normal_bf16[2]), p.x, p.y, p.z,
+                                      from_bf16(o.flux_bf16[0]) > 0.0f || from_bf16(o.flux_bf16[1]) > 0.0f ||
+                                          from_bf16(o.flux_bf16[2]) > 0.0f);
     } else {
       DrvVPL o;
       o.flux[0] = rsm_at(flux, read_half, 3 * t);
@@ -109,6 +116,9 @@ __global__ void __launch_bounds__(256) extract_kernel(DrvSpotLight L, int R, con
       o.normal[2] = nn.z;
       o._pad1 = 0.0f;
       reinterpret_cast<DrvVPL*>(vpls_out)[i] = o;
+      if (records)
+        records[i] = make_cull_record(nn.x, nn.y, nn.z, p.x, p.y, p.z,
+                                      o.flux[0] > 0.0f || o.flux[1] > 0.0f || o.flux[2] > 0.0f);
     }
   }
   const int interval = L.indirect_shadow_sample_interval;
@@ -153,14 +163,14 @@ cudaError_t launch_downsample_rsm(cudaStream_t s, int res, const void* flux, con
 
 cudaError_t launch_extract_vpls(cudaStream_t s, const DrvSpotLight& L, int res, const void* flux, const int16_t* nrm,
                                 const void* dls, int read_half, const void* dls_shadow, int shadow_half, void* vpls,
-                                DrvShadowCone* cones, int precision) {
+                                DrvShadowCone* cones, int precision, float4* records) {
   int n = res * res;
   if (precision == DRV_PRECISION_BF16)
     extract_kernel<true><<<(n + 255) / 256, 256, 0, s>>>(L, res, flux, nrm, dls, read_half, dls_shadow, shadow_half,
-                                                         vpls, cones);
+                                                         vpls, cones, records);
   else
     extract_kernel<false><<<(n + 255) / 256, 256, 0, s>>>(L, res, flux, nrm, dls, read_half, dls_shadow, shadow_half,
-                                                          vpls, cones);
+                                                          vpls, cones, records);
   return cudaGetLastError();
 }
 

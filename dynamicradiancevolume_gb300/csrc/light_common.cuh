@@ -33,6 +33,7 @@ struct StageParams {
   int stride_floats;
   float ev[5];  // ShEvaFactor0, 1, 2n2_p1_n1, 20, 2p2 (renderer.cpp:302-306)
   int spec;     // INDIRECT_SPECULAR: VPLs with a flux sum below 0.001 are skipped
+  uint32_t* err;  // device error word for bounded waits (nullptr: none)
 };
 
 // Host: the device view of a voxel pyramid of resolution cfg.voxel_res.
