@@ -39,11 +39,6 @@ UNIT = "caches/s"
 # ns_1080p_4096, from one `ncu --set full --clock-control none` capture each
 # (cold caches) of `bench.py --steps 1 --warmup 1` at that workload.
 NCU_TRAFFIC = {"cone_kernel": 12_660_736, "mlp_kernel": 7_976_192}
-# Cache-level bytes of one cone pass of ns_1080p_4096 (BF16) and their share
-# of the L1/TEX and L2 throughput peaks, from one ncu capture: the cone march
-# reads its voxels from L1/L2, so these, not HBM, are its memory roofline.
-NCU_CONE_CACHE = {"l1_bytes": 261_125_792, "l2_bytes": 129_594_048, "l1_pct_of_peak": 17.78,
-                  "l2_pct_of_peak": 6.58, "ncu_us": 104.9}
 
 
 def parse():
@@ -54,6 +49,8 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="ns_1080p_4096")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extra-workloads", action="store_true",
+                    help="measure only --workload (by default the 1080p line also measures c2_production)")
     ap.add_argument("--thresholds", type=float, nargs="*", default=[0.5, 0.8],
                     help="surrogate confidence thresholds to measure")
     return ap.parse_args()
@@ -414,84 +411,88 @@ def measure_light_graph(pipe, steps, warmup, flush):
     return statistics.mean(a.elapsed_time(b) for a, b in ev)
 
 
-def run_ours(args):
+def measure_cache_peaks(dev) -> dict:
+    """L1 and L2 load throughput of this GPU (drv_measure_load_bandwidth),
+    GB/s: the denominators of the cone pass's memory roofline."""
     import ctypes as C
     import torch
-    import torch.distributed as dist
+    from dynamicradiancevolume_gb300 import load
+    lib = load()
+    buf = torch.randint(0, 2**31 - 1, (16 * 1024 * 1024,), dtype=torch.int32, device=dev)  # 64 MB < L2
+    stream = torch.cuda.current_stream(dev)
+    out = {}
+    for level, reps in ((1, 200), (2, 20)):
+        g = C.c_float()
+        st = lib.drv_measure_load_bandwidth(level, C.c_void_p(buf.data_ptr()), buf.numel() * 4, reps,
+                                            C.c_void_p(stream.cuda_stream), C.byref(g))
+        out[f"l{level}_gbs"] = g.value if st == 0 else None
+    out["method"] = ("drv_measure_load_bandwidth: 16-byte loads, L1 = every CTA re-reading its own 32 KB window "
+                     "(2 CTAs per SM), L2 = all SMs sweeping a 64 MB buffer with L1-bypassing loads")
+    return out
+
+
+def measure_workload(w, args, dev, flush, rank, weights, features, full: bool) -> dict:
+    """Everything the JSON line reports for one workload: its variants
+    (plain FP32 cone, BF16 precision, surrogate thresholds), the headline
+    variant (fastest within 1% rel-L2 of the FP64 oracle frame), its e2e
+    through the C ABI with host buffers, per-kernel light-stage times and the
+    voxel loads of its cone pass. `full`: also the specular cost, the
+    drv_frame / one-context / F32-target e2e forms."""
+    import ctypes as C
+    import numpy as np
+    import torch
     from dynamicradiancevolume_gb300 import abi, pipeline, surrogate
     from dynamicradiancevolume_gb300 import batch as batch_mod
 
-    ws, rank, local = dist_env()
-    if ws > 1:
-        dist.init_process_group("nccl")
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
-    w = pipeline.WORKLOADS[args.workload]
-    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MiB > 129 MB L2
-    if ws > 1:
-        dist.barrier()
-
-    # ---- variants: plain FP32 cone, BF16 precision, surrogate visibility
-    variants = {}
-    weights, features, surrogate_note = None, "segment8", None
-    if surrogate.DEFAULT_WEIGHTS.with_suffix(".bin").exists():
-        try:
-            weights, features = surrogate.load_params(), surrogate.load_features()
-        except ValueError as e:  # a checkpoint of another model layout: no surrogate variants
-            surrogate_note = str(e)
     plan = [("plain_fp32", w, None), ("precision_bf16", pipeline.scaled(w, precision=abi.PRECISION_BF16), None)]
     if weights is not None:
         for thr in args.thresholds:
             plan.append((f"surrogate_t{thr:g}", pipeline.scaled(w, visibility=abi.VISIBILITY_SURROGATE), thr))
-    reference = None
-    pipes = {}
-    with ClockSampler(local) as clk:
-        for name, wv, thr in plan:
-            hf = pipeline.host_frame(wv)
-            if thr is not None:
-                hf.config.surrogate_conf_threshold = thr
-            pipe = pipeline.Pipeline(hf, device=str(dev))
-            if thr is not None:
-                surrogate.upload(pipe, weights, features)
-            pipe.raycast_inputs()
-            pipe.frame()
-            pipe.sync()
-            count = pipe.cache_count()
-            frame_ms, stage_ms = measure(pipe, args.steps, args.warmup, flush)
-            graph_ms = measure_graph(pipe, args.steps, args.warmup, flush)
-            light_ms = measure_light_graph(pipe, args.steps, args.warmup, flush)
-            pipe.frame()
-            pipe.sync()
-            # errors of this frame's SH and radiance (read before the extra
-            # light stage below, whose SH would add onto the frame's)
-            out = pipe.out.cpu().numpy()
-            if reference is None and rank == 0:
-                reference = oracle_frame_from(pipe)
-            errors = errors_vs_fp64(pipe, count, out, reference) if rank == 0 else {}
-            pipe.light()  # one eager light stage: its pair count and surrogate statistics
-            info = {"caches_lit_per_s": count / (light_ms / 1e3), "light_ms": light_ms, "frame_ms": graph_ms,
-                    "live_pairs": pipe.light_pairs(),
-                    "frame_ms_stream": frame_ms, "stage_ms": stage_ms, "caches": count,
-                    "caches_per_s_of_frame": count / (graph_ms / 1e3)}
-            if thr is not None:
-                ev, fb = C.c_uint32(), C.c_uint32()
-                pipe.lib.drv_get_surrogate_stats(pipe.ctx, C.byref(ev), C.byref(fb))
-                blocks = sum(pipe.buffers().n_vpls[l] // hf.lights[l].indirect_shadow_sample_interval
-                             for l in range(w.n_lights))
-                info["threshold"] = thr
-                info["shadow_blocks"] = blocks
-                info["evaluated_pairs"] = ev.value
-                info["retraced_pairs"] = fb.value
-                info["evaluated_share_of_pairs"] = ev.value / max(count * blocks, 1)
-                info["retraced_share_of_evaluated"] = fb.value / max(ev.value, 1)
-            info.update(errors)
-            variants[name] = info
-            pipes[name] = pipe
-        # INDIRECT_SPECULAR with the reference's 16x16 per-cache envmaps on the
-        # BF16 frame: its cost (the envmap pass inside the light stage, the
-        # mips and the specular apply inside the frame). Not a headline
+    variants, pipes, reference = {}, {}, None
+    for name, wv, thr in plan:
+        hf = pipeline.host_frame(wv)
+        if thr is not None:
+            hf.config.surrogate_conf_threshold = thr
+        pipe = pipeline.Pipeline(hf, device=str(dev))
+        if thr is not None:
+            surrogate.upload(pipe, weights, features)
+        pipe.raycast_inputs()
+        pipe.frame()
+        pipe.sync()
+        count = pipe.cache_count()
+        frame_ms, stage_ms = measure(pipe, args.steps, args.warmup, flush)
+        graph_ms = measure_graph(pipe, args.steps, args.warmup, flush)
+        light_ms = measure_light_graph(pipe, args.steps, args.warmup, flush)
+        pipe.frame()
+        pipe.sync()
+        # errors of this frame's SH and radiance (read before the extra light
+        # stage below, whose SH would add onto the frame's)
+        out = pipe.out.cpu().numpy()
+        if reference is None and rank == 0:
+            reference = oracle_frame_from(pipe)
+        errors = errors_vs_fp64(pipe, count, out, reference) if rank == 0 else {}
+        pipe.light()  # one eager light stage: its pair count and surrogate statistics
+        info = {"caches_lit_per_s": count / (light_ms / 1e3), "light_ms": light_ms, "frame_ms": graph_ms,
+                "live_pairs": pipe.light_pairs(), "frame_ms_stream": frame_ms, "stage_ms": stage_ms,
+                "caches": count, "caches_per_s_of_frame": count / (graph_ms / 1e3)}
+        if thr is not None:
+            ev, fb = C.c_uint32(), C.c_uint32()
+            pipe.lib.drv_get_surrogate_stats(pipe.ctx, C.byref(ev), C.byref(fb))
+            blocks = sum(pipe.buffers().n_vpls[l] // hf.lights[l].indirect_shadow_sample_interval
+                         for l in range(w.n_lights))
+            info.update({"threshold": thr, "features": features, "shadow_blocks": blocks,
+                         "evaluated_pairs": ev.value, "retraced_pairs": fb.value,
+                         "evaluated_share_of_pairs": ev.value / max(count * blocks, 1),
+                         "retraced_share_of_evaluated": fb.value / max(ev.value, 1)})
+        info.update(errors)
+        variants[name] = info
+        pipes[name] = pipe
+    specular = None
+    if full:
+        # INDIRECT_SPECULAR with the reference's 16x16 per-cache envmaps on
+        # the BF16 frame: its cost (the envmap pass inside the light stage,
+        # the mips and the specular apply inside the frame). Not a headline
         # candidate: the specular frame is another image.
-        import numpy as np
         hf = pipeline.host_frame(pipeline.scaled(w, precision=abi.PRECISION_BF16, specular_envmap_size=16))
         sp = pipeline.Pipeline(hf, device=str(dev))
         rm = np.random.default_rng(11).integers(0, 256, (w.height, w.width, 2), dtype=np.uint8)
@@ -506,7 +507,6 @@ def run_ours(args):
                     "light_ms_without": variants["precision_bf16"]["light_ms"],
                     "frame_ms_without": variants["precision_bf16"]["frame_ms"]}
         sp.close()
-    clocks = clk.summary()
     ok = {n: v for n, v in variants.items() if v.get("rel_l2_vs_fp64", 1.0) <= 0.01}
     head = max(ok, key=lambda n: ok[n]["caches_lit_per_s"]) if ok else "plain_fp32"
     pipe = pipes[head]
@@ -521,11 +521,10 @@ def run_ours(args):
     # a renderer uploads frame k+1 while frame k renders): every step copies
     # its G-buffer and RSM from pinned host memory, runs the frame and copies
     # its radiance back; the copies of one step overlap the kernels of the
-    # other. Both contexts' working sets together exceed L2 (~2 x 120 MB).
-    # The headline uses the reference's own render targets (D32F depth, RG16I
-    # normal, SRGB8 diffuse, RGB16F / RG16I / RG16F RSM, RGBA16F output with
-    # additive blending, renderer.cpp:119, 468-480, 1288-1290); the same steps
-    # over F32 targets are reported beside it.
+    # other. The headline uses the reference's own render targets (D32F depth,
+    # RG16I normal, SRGB8 diffuse, RGB16F / RG16I / RG16F RSM, RGBA16F output
+    # with additive blending, renderer.cpp:119, 468-480, 1288-1290); the same
+    # steps over F32 targets are reported beside it.
     wv_head = next(wv for name, wv, thr in plan if name == head)
     g_ref, rsm_ref = pipeline.reference_format_inputs(pipe)
 
@@ -563,8 +562,8 @@ def run_ours(args):
         h2d = sum(t.numel() * t.element_size() for t in host_in) + sum(
             t.numel() * t.element_size() for r in host_rsm for t in r)
         d2h = host_out[0].numel() * host_out[0].element_size()
-        # one eager frame per context first (the scene's boxes become resident:
-        # a capture cannot include their upload)
+        # one eager frame per context first (the scene's boxes become
+        # resident: a capture cannot include their upload)
         for q in qs:
             with torch.cuda.stream(q.stream):
                 for d, h in zip(dev_in(q), host_in):
@@ -626,11 +625,25 @@ def run_ours(args):
             q.close()
         return ms, h2d, d2h
 
-    e2e_ms, h2d, d2h = run_e2e("reference", graph=True)
-    e2e_frame_ms, _, _ = run_e2e("reference", graph=False)
-    e2e_serial_ms, _, _ = run_e2e("reference", graph=False, two_contexts=False)
-    e2e_f32_ms, h2d_f32, d2h_f32 = run_e2e("f32", graph=True)
     count = hv["caches"]
+    e2e_ms, h2d, d2h = run_e2e("reference", graph=True)
+    e2e = {"value": count / (e2e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+           "ms_per_step": e2e_ms,
+           "formats": "the reference's render targets: D32F depth, RG16I normal, SRGB8 diffuse; RSM RGB16F flux, "
+                      "RG16I normal, RG16F (d, d^2); radiance added into an RGBA16F HDR buffer",
+           "scope": "whole frame per step: G-buffer and RSM copied from pinned host memory, the frame replayed as "
+                    "a CUDA graph (drv_batch_launch of a one-scene batch captured once per context), radiance "
+                    "copied back, all inside the timed region; two contexts on two streams take the steps in turn "
+                    "(double buffering)"}
+    if full:
+        e2e["ms_per_step_drv_frame"], _, _ = run_e2e("reference", graph=False)
+        e2e["ms_per_step_one_context"], _, _ = run_e2e("reference", graph=False, two_contexts=False)
+        f32_ms, h2d_f32, d2h_f32 = run_e2e("f32", graph=True)
+        e2e["f32_formats"] = {"ms_per_step": f32_ms, "h2d_bytes_per_step": h2d_f32, "d2h_bytes_per_step": d2h_f32,
+                              "value": count / (f32_ms / 1e3)}
+        e2e["scope"] += ("; ms_per_step_drv_frame: the same steps calling drv_frame (kernels launched one by one); "
+                         "ms_per_step_one_context: drv_frame steps on one context, one at a time; f32_formats: the "
+                         "graph steps with F32 diffuse, F32 RSM and an RGB F32 output")
 
     # ---- per-kernel times of the headline light stage (non-graph, events between its kernels)
     pipe.set_tuning(time_kernels=1)
@@ -644,47 +657,105 @@ def run_ours(args):
                 kern[k].append(v)
     pipe.set_tuning(time_kernels=0)
     kernel_ms = {k: statistics.mean(v) for k, v in kern.items()}
+    # ---- the voxel loads of one cone pass (its measuring instance, outside the timed regions)
+    pipe.set_tuning(count_voxel_reads=1)
+    pipe.light()
+    reads = (C.c_uint32 * 3)()
+    pipe._c(pipe.lib.drv_get_cone_voxel_reads(pipe.ctx, reads))
+    pipe.set_tuning(count_voxel_reads=0)
+    traced = hv.get("retraced_pairs") if head.startswith("surrogate") else hv["live_pairs"]
+    pipe.close()
+    return {"w": w, "head": head, "variants": variants, "specular": specular, "e2e": e2e, "kernel_ms": kernel_ms,
+            "voxel_reads": list(reads), "traced_pairs": traced, "hv": hv, "count": count}
 
-    # ---- max over ranks (replicas)
-    light_ms_all, frame_ms_all, e2e_ms_all, caches_all = reduce_over_ranks(hv["light_ms"], hv["frame_ms"], e2e_ms,
-                                                                           float(count), device=dev)
 
-    # ---- roofline of the light stage's dominant kernel
-    pk = peaks()
+def cone_roofline(r, cache_peaks, pk, w_name) -> dict:
+    """The light stage's dominant kernel against its bound. The cone pass
+    reads its voxel pyramid from L1/L2 (16 MiB corner grid + mip records,
+    L2-resident): algorithmic bytes = the counted voxel loads (level-0 corner
+    bytes x 1 B, FP16 mip records x 16 B, plain mip texels x 4 B FP32 / 2 B
+    BF16) + 16 B per traced pair (its order index, cache and block indices,
+    the shadowing written), over the kernel's live event time, against the
+    measured L2 load throughput; L1 and HBM figures beside it."""
+    kernel_ms, hv = r["kernel_ms"], r["hv"]
     top = max(kernel_ms, key=kernel_ms.get)
     top_ms = kernel_ms[top]
-    n_pairs = hv.get("evaluated_pairs") or 0
     if top == "mlp":
+        n_pairs = hv.get("evaluated_pairs") or 0
         flop = n_pairs * 20736  # 2 (32*64 + 64*64 + 64*64 + 64*2) per evaluated pair
         achieved = flop / (top_ms / 1e3) / 1e12
-        roofline = {"bound": "tensor", "kernel": "mlp_kernel", "achieved": achieved, "peak": pk["bf16_tflops"],
-                    "unit": "TFLOP/s", "frac": achieved / pk["bf16_tflops"],
-                    "traffic": NCU_TRAFFIC["mlp_kernel"] if w.name == "ns_1080p_4096" else None,
-                    "peak_source": pk["source"] + " (bf16_tflops, burst)",
-                    "algorithmic": f"{n_pairs} evaluated pairs x 20736 flop"}
-    else:
-        # Per traced pair: its order index, the pair (cache, block) and the
-        # shadow it writes = 16 B; cache positions and cones are per cache /
-        # per block and the voxel samples are L1/L2 hits (the cold-cache DRAM
-        # bytes, which include the bricks the cones touch, are `traffic`).
-        pairs_traced = variants[head]["live_pairs"]
-        nbytes = pairs_traced * 16 + count * 16 + w.n_vpls * 16
-        achieved = nbytes / (top_ms / 1e3) / 1e9
-        roofline = {"bound": "hbm", "kernel": f"{top}_kernel", "achieved": achieved, "peak": pk["hbm_gbs"],
-                    "unit": "GB/s", "frac": achieved / pk["hbm_gbs"],
-                    "traffic": NCU_TRAFFIC.get(f"{top}_kernel") if w.name == "ns_1080p_4096" else None,
+        return {"bound": "tensor", "kernel": "mlp_tc_kernel", "achieved": achieved, "peak": pk["bf16_tflops"],
+                "unit": "TFLOP/s", "frac": achieved / pk["bf16_tflops"], "traffic": None,
+                "peak_source": pk["source"] + " (bf16_tflops, burst)",
+                "algorithmic": f"{n_pairs} evaluated pairs x 20736 flop"}
+    l0, rec, tex = r["voxel_reads"]
+    tex_bytes = 2 if r["head"] in ("precision_bf16",) or r["head"].startswith("surrogate") else 4
+    traced = r["traced_pairs"] or 0
+    voxel_bytes = l0 * 1 + rec * 16 + tex * tex_bytes
+    nbytes = voxel_bytes + traced * 16
+    achieved = nbytes / (top_ms / 1e3) / 1e9
+    l2 = cache_peaks.get("l2_gbs") or float("nan")
+    l1 = cache_peaks.get("l1_gbs") or float("nan")
+    return {"bound": "l2", "kernel": f"{top}_kernel", "achieved": achieved, "peak": l2, "unit": "GB/s",
+            "frac": achieved / l2,
+            "traffic": NCU_TRAFFIC.get(f"{top}_kernel") if w_name == "ns_1080p_4096" else None,
+            "peak_source": "measured on this GPU by drv_measure_load_bandwidth (L2, 16-byte loads)",
+            "algorithmic": (f"{l0} level-0 corner bytes x 1 B + {rec} mip records x 16 B + {tex} mip texels x "
+                            f"{tex_bytes} B + {traced} traced pairs x 16 B = {nbytes} B per launch"),
+            "l1": {"peak_gbs": l1, "frac": achieved / l1},
+            "hbm": {"peak_gbs": pk["hbm_gbs"], "frac": achieved / pk["hbm_gbs"],
                     "peak_source": pk["source"] + " (hbm_gbs)",
-                    "algorithmic": f"{pairs_traced} traced pairs x 16 B + {count} caches x 16 B + {w.n_vpls} cones x 16 B",
-                    "note": "the cone pass is issue-bound (75% issue active, ALU pipe 55%, voxel samples from "
-                            "L1/L2), far from the HBM roofline"}
-        if top == "cone" and w.name == "ns_1080p_4096":
-            c = NCU_CONE_CACHE
-            roofline["cache_levels"] = {
-                "l1_gbs": c["l1_bytes"] / (top_ms / 1e3) / 1e9, "l2_gbs": c["l2_bytes"] / (top_ms / 1e3) / 1e9,
-                "l1_pct_of_peak": c["l1_pct_of_peak"], "l2_pct_of_peak": c["l2_pct_of_peak"],
-                "bytes_per_launch": {"l1": c["l1_bytes"], "l2": c["l2_bytes"]},
-                "note": "bytes and share of peak from one ncu capture of the BF16 cone pass (%.1f us there); "
-                        "GB/s = those bytes over this run's live kernel time" % c["ncu_us"]}
+                    "note": "the voxel pyramid is L2-resident; one ncu capture of this pass read about 13 MB "
+                            "from DRAM per launch (profiles/)"},
+            "note": "the cone pass is issue-bound (about 75% issue active, ALU pipe 55%, 21 of 32 lanes active): "
+                    "its loads are a small share of either cache's throughput"}
+
+
+def cpu_baseline_of(w, threads) -> dict:
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle_py as O
+    hf_cpu = O.host_frame(w)
+    caches, t_frame, t_light, note = cpu_frame(w, hf_cpu, oracle_inputs(hf_cpu, w), threads)
+    return {"value": caches / t_light, "unit": UNIT, "cores": threads, "kind": "port", "sample": note + " (one frame)",
+            "ms_per_frame": t_frame * 1e3}
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+    from dynamicradiancevolume_gb300 import abi, pipeline, surrogate
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    w = pipeline.WORKLOADS[args.workload]
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MiB > 129 MB L2
+    if ws > 1:
+        dist.barrier()
+    weights, features, surrogate_note = None, "segment8", None
+    if surrogate.DEFAULT_WEIGHTS.with_suffix(".bin").exists():
+        try:
+            weights, features = surrogate.load_params(), surrogate.load_features()
+        except ValueError as e:  # a checkpoint of another model layout: no surrogate variants
+            surrogate_note = str(e)
+    extra = [] if args.no_extra_workloads or args.workload != "ns_1080p_4096" else ["c2_production"]
+    with ClockSampler(local) as clk:
+        r = measure_workload(w, args, dev, flush, rank, weights, features, full=True)
+        others = {name: measure_workload(pipeline.WORKLOADS[name], args, dev, flush, rank, None, features,
+                                         full=False) for name in extra}
+        cache_peaks = measure_cache_peaks(dev)
+    clocks = clk.summary()
+    pk = peaks()
+    hv, head, count = r["hv"], r["head"], r["count"]
+
+    # ---- max over ranks (replicas)
+    light_ms_all, frame_ms_all, e2e_ms_all, caches_all = reduce_over_ranks(hv["light_ms"], hv["frame_ms"],
+                                                                           r["e2e"]["ms_per_step"], float(count),
+                                                                           device=dev)
+    e2e = dict(r["e2e"])
+    e2e.update({"value": caches_all / (e2e_ms_all / 1e3), "ms_per_step": e2e_ms_all})
     line = {
         "metric": METRIC, "value": caches_all / (light_ms_all / 1e3), "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": light_ms_all, "ms_per_frame": frame_ms_all,
@@ -698,39 +769,36 @@ def run_ours(args):
         "errors_vs_fp64": {k: hv.get(k) for k in ("rel_l2_vs_fp64", "radiance_max_abs_vs_fp64", "sh_rel_l2_vs_fp64",
                                                   "sh_max_abs_vs_fp64")},
         "stage_ms": hv["stage_ms"],
-        "light_kernel_ms": kernel_ms,
-        "variants": variants,
-        "specular": specular,
-        "roofline": roofline,
-        "e2e": {"value": caches_all / (e2e_ms_all / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms_all, "ms_per_step_drv_frame": e2e_frame_ms,
-                "ms_per_step_one_context": e2e_serial_ms,
-                "formats": "the reference's render targets: D32F depth, RG16I normal, SRGB8 diffuse; RSM RGB16F "
-                           "flux, RG16I normal, RG16F (d, d^2); radiance added into an RGBA16F HDR buffer",
-                "f32_formats": {"ms_per_step": e2e_f32_ms, "h2d_bytes_per_step": h2d_f32,
-                                "d2h_bytes_per_step": d2h_f32,
-                                "value": caches_all / (e2e_f32_ms / 1e3)},
-                "scope": "whole frame per step: G-buffer and RSM copied from pinned host memory, the frame "
-                         "replayed as a CUDA graph (drv_batch_launch of a one-scene batch captured once per "
-                         "context), radiance copied back, all inside the timed region; two contexts on two "
-                         "streams take the steps in turn (double buffering). ms_per_step_drv_frame: the same "
-                         "steps calling drv_frame (kernels launched one by one); ms_per_step_one_context: "
-                         "drv_frame steps on one context, one at a time; f32_formats: the graph steps with "
-                         "F32 diffuse, F32 RSM and an RGB F32 output"},
+        "light_kernel_ms": r["kernel_ms"],
+        "variants": r["variants"],
+        "specular": r["specular"],
+        "roofline": cone_roofline(r, cache_peaks, pk, w.name),
+        "cache_peaks": cache_peaks,
+        "e2e": e2e,
         "gpu_launches": light_stage_launches(w, head.startswith("surrogate")) * args.steps,
         "clocks": clocks,
     }
+    if surrogate_note:
+        line["surrogate_skipped"] = surrogate_note
+    threads = os.cpu_count() or 1
     if rank == 0 and not args.no_cpu_baseline:
-        sys.path.insert(0, str(ROOT / "oracle"))
-        import oracle_py as O
-        threads = os.cpu_count() or 1
-        hf_cpu = O.host_frame(w)
-        caches, t_frame, t_light, note = cpu_frame(w, hf_cpu, oracle_inputs(hf_cpu, w), threads)
-        line["cpu_baseline"] = {"value": caches / t_light, "unit": UNIT, "cores": threads, "kind": "port",
-                                "sample": note + " (one frame)", "ms_per_frame": t_frame * 1e3}
+        line["cpu_baseline"] = cpu_baseline_of(w, threads)
+    if others:
+        line["workloads"] = {}
+        for name, o in others.items():
+            ov = o["hv"]
+            entry = {"config": workload_config(o["w"]), "variant": o["head"], "caches": o["count"],
+                     "value": o["count"] / (ov["light_ms"] / 1e3), "unit": UNIT, "ms_per_step": ov["light_ms"],
+                     "ms_per_frame": ov["frame_ms"], "rel_l2_vs_fp64": ov.get("rel_l2_vs_fp64"),
+                     "errors_vs_fp64": {k: ov.get(k) for k in ("rel_l2_vs_fp64", "radiance_max_abs_vs_fp64",
+                                                               "sh_rel_l2_vs_fp64", "sh_max_abs_vs_fp64")},
+                     "light_kernel_ms": o["kernel_ms"], "variants": o["variants"],
+                     "roofline": cone_roofline(o, cache_peaks, pk, name), "e2e": o["e2e"]}
+            if rank == 0 and not args.no_cpu_baseline:
+                entry["cpu_baseline"] = cpu_baseline_of(o["w"], threads)
+            line["workloads"][name] = entry
     if rank == 0:
         print(json.dumps(line), flush=True)
-    pipe.close()
     if ws > 1:
         dist.destroy_process_group()
     return 0

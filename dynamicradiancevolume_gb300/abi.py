@@ -139,7 +139,7 @@ class DrvTuning(C.Structure):
     _fields_ = [("light_path", C.c_int32), ("pair_capacity", C.c_uint32), ("cone_ctas_per_sm", C.c_int32),
                 ("gather_ctas_per_sm", C.c_int32), ("time_kernels", C.c_int32),
                 ("plain_voxel_reads", C.c_int32), ("surrogate_wait_test", C.c_int32),
-                ("reserved", C.c_int32 * 1)]
+                ("count_voxel_reads", C.c_int32)]
 
 
 LIGHT_KERNELS = ("cull", "classify", "scatter", "mlp", "cone", "gather")
@@ -198,6 +198,8 @@ PROTOTYPES = {
     "drv_get_cache_count": (C.c_int, [VP, P(C.c_uint32)]),
     "drv_set_surrogate_params": (C.c_int, [VP, VP]),
     "drv_set_surrogate_features": (C.c_int, [VP, C.c_int32]),
+    "drv_get_cone_voxel_reads": (C.c_int, [VP, P(C.c_uint32)]),
+    "drv_measure_load_bandwidth": (C.c_int, [C.c_int32, VP, C.c_size_t, C.c_int32, VP, P(C.c_float)]),
     "drv_surrogate_make_pairs": (C.c_int, [VP, C.c_uint64, C.c_int32, VP, VP]),
     "drv_surrogate_train_scratch_floats": (C.c_size_t, [C.c_int32]),
     "drv_surrogate_train_step": (C.c_int, [VP, VP, C.c_int32, VP, VP, VP, VP, C.c_int32, C.c_float, C.c_float,

@@ -683,7 +683,8 @@ drv_status light_caches(DrvContext* ctx, const DrvSpotLight* lights, int32_t n_l
                                                             ctx->entry_stride, ctx->light_voxels(), pairs, sur,
                                                             ctx->scratch_words + 1,
                                                             ctx->tuning.cone_ctas_per_sm,
-                                                            ctx->tuning.gather_ctas_per_sm, ctx->num_sms, events,
+                                                            ctx->tuning.gather_ctas_per_sm, ctx->num_sms,
+                                                            ctx->tuning.count_voxel_reads != 0, events,
                                                             voxels_ready),
                                "light_caches");
     if (events) ctx->lk_recorded = st == DRV_OK;
@@ -869,6 +870,19 @@ drv_status drv_set_tuning(DrvContext* ctx, const DrvTuning* t) {
     DRV_TRY_CUDA(ctx, alloc_pairs(ctx, t->pair_capacity));
   }
   ctx->tuning = *t;
+  return DRV_OK;
+}
+
+drv_status drv_get_cone_voxel_reads(DrvContext* ctx, uint32_t reads[3]) {
+  if (!ctx || !reads) return DRV_ERR_INVALID_ARG;
+  if (!ctx->tuning.count_voxel_reads)
+    return fail(ctx, DRV_ERR_INVALID_ARG, "set DrvTuning.count_voxel_reads before the light stage");
+  uint32_t c[8];
+  DRV_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->s()));
+  DRV_TRY_CUDA(ctx, cudaMemcpy(c, ctx->pairs.counters, sizeof(c), cudaMemcpyDeviceToHost));
+  reads[0] = c[1];
+  reads[1] = c[2];
+  reads[2] = c[7];
   return DRV_OK;
 }
 

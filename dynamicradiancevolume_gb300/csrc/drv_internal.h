@@ -103,9 +103,10 @@ struct LightScratch {
 // length that take one sampling path; retrace lists the pairs the surrogate
 // is not confident about, narrow cones (every sample on voxel level 0) from
 // its front, wide ones from its back.
-// counters (zeroed before each light stage): [0] pairs claimed, [3] narrow
-// and [4] wide cones in retrace, [5] pairs the surrogate evaluated, [6] the
-// cone pass's work cursor,
+// counters (zeroed before each light stage): [0] pairs claimed, [1] level-0
+// corner bytes, [2] mip records and [7] plain mip texels the cone pass read
+// (its counting instance only), [3] narrow and [4] wide cones in retrace,
+// [5] pairs the surrogate evaluated, [6] the cone pass's work cursor,
 // [8 + c] pairs of class c, [8 + kConeClasses + c] class c's scatter cursor.
 constexpr uint32_t kNoPair = 0xFFFFFFFFu;
 constexpr uint32_t kPairOverflow = 0xFFFFFFFFu;
@@ -274,7 +275,8 @@ cudaError_t launch_light_split(cudaStream_t s, const DrvConfig& cfg, const DrvVo
                                const DrvCacheCounter* counter, void* entries, uint32_t entry_stride,
                                const VoxelInputs& vox, const PairList& pairs, const SurrogateArgs& sur,
                                uint32_t* err, int cone_ctas_per_sm, int gather_ctas_per_sm, int num_sms,
-                               cudaEvent_t* events = nullptr, cudaEvent_t voxels_ready = nullptr);
+                               bool count_voxel_reads = false, cudaEvent_t* events = nullptr,
+                               cudaEvent_t voxels_ready = nullptr);
 cudaError_t launch_bruteforce_rsm(cudaStream_t s, const DrvPerFrame& f, const DrvGBufferView& g,
                                   const float* rough_metal, const LightLaunch& ll, int bf16, float* out_rgb,
                                   const float* srgb);

@@ -32,6 +32,7 @@
 // without indirect shadow and the allocation-free entry point.
 #include <cmath>
 #include <mutex>
+#include <type_traits>
 #include <vector>
 
 #include "drv_device.cuh"
@@ -472,8 +473,11 @@ __global__ void __launch_bounds__(kClassThreads) scatter_kernel(PairList L) {
 
 // Thread per cone, over a cone-order list. RETRACE: L.retrace, its n_front
 // narrow cones from the front and n_back wide ones from the back; otherwise
-// L.order, every listed pair in class order.
-template <bool BF16, bool RETRACE>
+// L.order, every listed pair in class order. COUNT (a separate, measuring
+// instance): the voxel loads of all cones are summed into counters[1]
+// (level-0 corner bytes), [2] (16-byte mip records) and [7] (plain mip
+// texels).
+template <bool BF16, bool RETRACE, bool COUNT = false>
 __global__ void __launch_bounds__(128) cone_kernel(StageParams p, PairList L) {
   pdl_wait_and_release();
   uint32_t nf = 0, nb = 0;
@@ -486,6 +490,23 @@ __global__ void __launch_bounds__(128) cone_kernel(StageParams p, PairList L) {
   }
   const uint32_t* ord = RETRACE ? L.retrace : L.order;
   const uint32_t n = min(nf + nb, L.cap);
+  typename std::conditional<COUNT, VoxelReads, NoReads>::type reads;
+  auto flush_reads = [&]() {
+    if constexpr (COUNT) {
+      uint32_t a = reads.level0_bytes, b = reads.records, c = reads.texels;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+        c += __shfl_xor_sync(0xffffffffu, c, o);
+      }
+      if ((threadIdx.x & 31) == 0) {
+        atomicAdd(L.counters + 1, a);
+        atomicAdd(L.counters + 2, b);
+        atomicAdd(L.counters + 7, c);
+      }
+    }
+  };
   if (!RETRACE) {
     // Warps take 32 cones at a time from counters[6], from the end of the
     // class order (the longest cones) to its start, so the short cones fill
@@ -502,8 +523,9 @@ __global__ void __launch_bounds__(128) cone_kernel(StageParams p, PairList L) {
       if (b == kNoPair) continue;
       float cx, cy, cz;
       cache_position<BF16>(p, L.cache[i], cx, cy, cz);
-      L.shadow[i] = block_cone(p, (int)b, cx, cy, cz);
+      L.shadow[i] = block_cone(p, (int)b, cx, cy, cz, reads);
     }
+    flush_reads();
     return;
   }
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
@@ -512,8 +534,9 @@ __global__ void __launch_bounds__(128) cone_kernel(StageParams p, PairList L) {
     if (b == kNoPair) continue;
     float cx, cy, cz;
     cache_position<BF16>(p, L.cache[i], cx, cy, cz);
-    L.shadow[i] = block_cone(p, (int)b, cx, cy, cz);
+    L.shadow[i] = block_cone(p, (int)b, cx, cy, cz, reads);
   }
+  flush_reads();
 }
 
 // Sum over the warp of each lane's v[0..N-1] (N = 16 or 32), returned in
@@ -782,7 +805,8 @@ cudaError_t set_max_smem(const void* kernel, size_t bytes) {
 // elapsed(events[k], events[k + 1]).
 template <int NK, bool BF16>
 cudaError_t split_variant(cudaStream_t s, const StageParams& p, const PairList& L, const SurrogateArgs& sur,
-                          int cone_ctas, int gather_ctas, int num_sms, cudaEvent_t* ev, cudaEvent_t voxels_ready) {
+                          int cone_ctas, int gather_ctas, int num_sms, bool count_reads, cudaEvent_t* ev,
+                          cudaEvent_t voxels_ready) {
   // Only the cone pass and the surrogate's features read the voxels: with
   // voxels_ready, the cull and the ordering passes overlap the voxel build.
   auto wait_voxels = [&]() { return voxels_ready ? cudaStreamWaitEvent(s, voxels_ready, 0) : cudaSuccess; };
@@ -817,14 +841,16 @@ cudaError_t split_variant(cudaStream_t s, const StageParams& p, const PairList& 
     if ((e = mark(DRV_LK_MLP)) != cudaSuccess || (e = wait_voxels()) != cudaSuccess ||
         (e = mark(DRV_LK_CONE)) != cudaSuccess)
       return e;
-    e = launch_grid(cone_kernel<BF16, false>, 128, 0, s, num_sms, cone_ctas, true, p, L);
+    e = count_reads ? launch_grid(cone_kernel<BF16, false, true>, 128, 0, s, num_sms, cone_ctas, true, p, L)
+                    : launch_grid(cone_kernel<BF16, false>, 128, 0, s, num_sms, cone_ctas, true, p, L);
   } else {
     if ((e = mark(DRV_LK_SCATTER)) != cudaSuccess || (e = wait_voxels()) != cudaSuccess ||
         (e = mark(DRV_LK_MLP)) != cudaSuccess)
       return e;
     if ((e = launch_surrogate_mlp(s, p, L, sur, BF16, num_sms)) != cudaSuccess) return e;
     if ((e = mark(DRV_LK_CONE)) != cudaSuccess) return e;
-    e = launch_grid(cone_kernel<BF16, true>, 128, 0, s, num_sms, cone_ctas, true, p, L);
+    e = count_reads ? launch_grid(cone_kernel<BF16, true, true>, 128, 0, s, num_sms, cone_ctas, true, p, L)
+                    : launch_grid(cone_kernel<BF16, true>, 128, 0, s, num_sms, cone_ctas, true, p, L);
   }
   if (e != cudaSuccess || (e = mark(DRV_LK_GATHER)) != cudaSuccess) return e;
   if ((e = launch_grid(gather_kernel<NK, BF16>, kGatherThreads, 0, s, num_sms, gather_ctas, true, p, L)) !=
@@ -889,15 +915,16 @@ cudaError_t launch_light_split(cudaStream_t s, const DrvConfig& cfg, const DrvVo
                                const DrvCacheCounter* counter, void* entries, uint32_t entry_stride,
                                const VoxelInputs& vox, const PairList& pairs, const SurrogateArgs& sur,
                                uint32_t* err, int cone_ctas_per_sm, int gather_ctas_per_sm, int num_sms,
-                               cudaEvent_t* events, cudaEvent_t voxels_ready) {
+                               bool count_reads, cudaEvent_t* events, cudaEvent_t voxels_ready) {
   StageParams p = make_stage_params(cfg, vol, ll, counter, entries, entry_stride, vox);
   p.err = err;
   const bool bf16 = cfg.precision == DRV_PRECISION_BF16;
+  const int cc = cone_ctas_per_sm, gc = gather_ctas_per_sm;
   if (cfg.sh_order == 2)
-    return bf16 ? split_variant<9, true>(s, p, pairs, sur, cone_ctas_per_sm, gather_ctas_per_sm, num_sms, events, voxels_ready)
-                : split_variant<9, false>(s, p, pairs, sur, cone_ctas_per_sm, gather_ctas_per_sm, num_sms, events, voxels_ready);
-  return bf16 ? split_variant<4, true>(s, p, pairs, sur, cone_ctas_per_sm, gather_ctas_per_sm, num_sms, events, voxels_ready)
-              : split_variant<4, false>(s, p, pairs, sur, cone_ctas_per_sm, gather_ctas_per_sm, num_sms, events, voxels_ready);
+    return bf16 ? split_variant<9, true>(s, p, pairs, sur, cc, gc, num_sms, count_reads, events, voxels_ready)
+                : split_variant<9, false>(s, p, pairs, sur, cc, gc, num_sms, count_reads, events, voxels_ready);
+  return bf16 ? split_variant<4, true>(s, p, pairs, sur, cc, gc, num_sms, count_reads, events, voxels_ready)
+              : split_variant<4, false>(s, p, pairs, sur, cc, gc, num_sms, count_reads, events, voxels_ready);
 }
 
 }  // namespace drv

@@ -260,13 +260,19 @@ __device__ __forceinline__ bool block_live(const StageParams& p, int b, float cx
   return false;
 }
 
-// Shadowing of block b seen from the cache (the reference's cone).
-__device__ __forceinline__ float block_cone(const StageParams& p, int b, float cx, float cy, float cz) {
+// Shadowing of block b seen from the cache (the reference's cone); `reads`
+// counts the voxel loads (NoReads: nothing).
+template <class R>
+__device__ __forceinline__ float block_cone(const StageParams& p, int b, float cx, float cy, float cz, R& reads) {
   const int l = block_light(p, b);
   const float4 c = __ldg(reinterpret_cast<const float4*>(p.ll.lights[l].cones) + (b - p.block_base[l]));
   const float vx = (cx - p.vol_min[0]) * p.inv_extent, vy = (cy - p.vol_min[1]) * p.inv_extent,
               vz = (cz - p.vol_min[2]) * p.inv_extent;
-  return cone_shadow(p.vox, p.voxel_size, p.max_steps, cx, cy, cz, vx, vy, vz, c.x, c.y, c.z, c.w);
+  return cone_shadow(p.vox, p.voxel_size, p.max_steps, cx, cy, cz, vx, vy, vz, c.x, c.y, c.z, c.w, reads);
+}
+__device__ __forceinline__ float block_cone(const StageParams& p, int b, float cx, float cy, float cz) {
+  NoReads r;
+  return block_cone(p, b, cx, cy, cz, r);
 }
 
 // SH gather of one VPL, cacheLightingRSM.comp:255-278. acc (and comp with

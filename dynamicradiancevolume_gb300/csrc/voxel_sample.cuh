@@ -38,6 +38,22 @@ struct VoxelView {
   int record_levels;       // levels 1..record_levels have records
 };
 
+// Voxel loads of the sampler, for the cone pass's memory roofline: every
+// sampling function takes a reads object; NoReads (the default) compiles to
+// nothing, VoxelReads counts level-0 corner bytes (1 B each), mip records
+// (16 B each) and plain mip texels (2 or 4 B each).
+struct NoReads {
+  __device__ __forceinline__ void on_level0() {}
+  __device__ __forceinline__ void on_record() {}
+  __device__ __forceinline__ void on_texels(int) {}
+};
+struct VoxelReads {
+  uint32_t level0_bytes = 0, records = 0, texels = 0;
+  __device__ __forceinline__ void on_level0() { ++level0_bytes; }
+  __device__ __forceinline__ void on_record() { ++records; }
+  __device__ __forceinline__ void on_texels(int n) { texels += (uint32_t)n; }
+};
+
 // The arithmetic of the sampler and the cone is written with explicit
 // rounding intrinsics (no contraction left to the compiler), so every kernel
 // that inlines it computes the same bits.
@@ -83,7 +99,10 @@ __device__ __forceinline__ int tap(float u, float nm1, float& a) {
 // n - 1 as a float for a level of n = 2^ln texels.
 __device__ __forceinline__ float last_texel(int ln) { return __uint_as_float((uint32_t)(127 + ln) << 23) - 1.0f; }
 
-__device__ __forceinline__ float level0_taps(const VoxelView& v, int x, int y, int z, float ax, float ay, float az) {
+template <class R>
+__device__ __forceinline__ float level0_taps(const VoxelView& v, int x, int y, int z, float ax, float ay, float az,
+                                             R& reads) {
+  reads.on_level0();
   const uint32_t b = __ldg(v.corners + corner_index(x, y, z, v.log2n));
   // Trilinear weights sum to one, so eight equal corners give that value
   // exactly: empty space (the common case) costs no interpolation.
@@ -99,14 +118,17 @@ __device__ __forceinline__ float level0_taps(const VoxelView& v, int x, int y, i
 }
 
 // Level 0 at position U (texel coordinate U - 0.5, exact).
-__device__ __forceinline__ float level0_at(const VoxelView& v, const Coord& U) {
+template <class R>
+__device__ __forceinline__ float level0_at(const VoxelView& v, const Coord& U, R& reads) {
   const float nm1 = last_texel(v.log2n);
   float ax, ay, az;
   const int x = tap(U.x - 0.5f, nm1, ax), y = tap(U.y - 0.5f, nm1, ay), z = tap(U.z - 0.5f, nm1, az);
-  return level0_taps(v, x, y, z, ax, ay, az);
+  return level0_taps(v, x, y, z, ax, ay, az, reads);
 }
 
-__device__ __forceinline__ float level_n_at(const VoxelView& v, int level, const Coord& u) {
+template <class R>
+__device__ __forceinline__ float level_n_at(const VoxelView& v, int level, const Coord& u, R& reads) {
+  reads.on_texels(8);
   const int ln = v.log2n - level, n = 1 << ln;
   const float ax = u.x - floorf(u.x), ay = u.y - floorf(u.y), az = u.z - floorf(u.z);
   const int x0 = (int)floorf(u.x), y0 = (int)floorf(u.y), z0 = (int)floorf(u.z);
@@ -140,7 +162,10 @@ __device__ __forceinline__ __half2 u32_as_half2(uint32_t w) {
 
 // level_n_at from the level's corner-packed record; `zero` reports a record
 // whose 8 texels are all 0 (the sample is then 0).
-__device__ __forceinline__ float level_record_at(const VoxelView& v, int level, const Coord& u, bool& zero) {
+template <class R>
+__device__ __forceinline__ float level_record_at(const VoxelView& v, int level, const Coord& u, bool& zero,
+                                                 R& reads) {
+  reads.on_record();
   const float nm1 = last_texel(v.log2n - level);
   float ax, ay, az;
   const int x = tap(u.x, nm1, ax), y = tap(u.y, nm1, ay), z = tap(u.z, nm1, az);
@@ -159,9 +184,14 @@ __device__ __forceinline__ float level_record_at(const VoxelView& v, int level, 
 
 // Trilinear sample of mip level >= 1 (from its records where they exist);
 // `zero` is set only from a record.
-__device__ __forceinline__ float level_any_at(const VoxelView& v, int level, const Coord& u, bool& zero) {
+template <class R>
+__device__ __forceinline__ float level_any_at(const VoxelView& v, int level, const Coord& u, bool& zero, R& reads) {
   zero = false;
-  return level <= v.record_levels ? level_record_at(v, level, u, zero) : level_n_at(v, level, u);
+  return level <= v.record_levels ? level_record_at(v, level, u, zero, reads) : level_n_at(v, level, u, reads);
+}
+__device__ __forceinline__ float level_any_at(const VoxelView& v, int level, const Coord& u, bool& zero) {
+  NoReads r;
+  return level_any_at(v, level, u, zero, r);
 }
 
 // Position U (level-0 voxel units) of texture coordinate s.
@@ -181,18 +211,23 @@ __device__ __forceinline__ float level_any(const VoxelView& v, int level, float 
 // floor(u_f), floor(u_f) + 1 lie within the fine texels of coarse taps
 // floor(u_c), floor(u_c) + 1, also where both clamp), so an all-zero coarse
 // record makes both levels 0.
-__device__ __forceinline__ float sample_voxels_at(const VoxelView& v, const Coord& U, float lod) {
-  if (!(lod > 0.0f)) return level0_at(v, U);
+template <class R>
+__device__ __forceinline__ float sample_voxels_at(const VoxelView& v, const Coord& U, float lod, R& reads) {
+  if (!(lod > 0.0f)) return level0_at(v, U, reads);
   bool zero;
-  if (lod >= (float)v.max_level) return level_any_at(v, v.max_level, level_coord(U, v.max_level), zero);
+  if (lod >= (float)v.max_level) return level_any_at(v, v.max_level, level_coord(U, v.max_level), zero, reads);
   const float fl = floorf(lod);
   const int d1 = (int)fl;
   const float fr = lod - fl;
-  const float t2 = level_any_at(v, d1 + 1, level_coord(U, d1 + 1), zero);
+  const float t2 = level_any_at(v, d1 + 1, level_coord(U, d1 + 1), zero, reads);
   if (zero) return 0.0f;
-  const float t1 = d1 == 0 ? level0_at(v, U) : level_any_at(v, d1, level_coord(U, d1), zero);
+  const float t1 = d1 == 0 ? level0_at(v, U, reads) : level_any_at(v, d1, level_coord(U, d1), zero, reads);
   if (fr == 0.0f) return t1;
   return __fmaf_rn(fr, t2, __fmul_rn(1.0f - fr, t1));
+}
+__device__ __forceinline__ float sample_voxels_at(const VoxelView& v, const Coord& U, float lod) {
+  NoReads r;
+  return sample_voxels_at(v, U, lod, r);
 }
 
 // textureLod at texture coordinate s.
@@ -206,9 +241,10 @@ __device__ __forceinline__ float sample_voxels(const VoxelView& v, float sx, flo
 // occlusion reaches 1 a further step gives occlusion * (1 - s) + s >= 1 for
 // any sample s in [0, 1], so the clamped result is 0 (to within one rounding)
 // whatever is sampled: the march stops there (the reference marches on).
+template <class R>
 __device__ __forceinline__ float cone_shadow(const VoxelView& v, float voxel_size, int max_steps, float cx, float cy,
                                              float cz, float px, float py, float pz, float ax, float ay, float az,
-                                             float dsr) {
+                                             float dsr, R& reads) {
   float tx = ax - cx, ty = ay - cy, tz = az - cz;
   const float light_dist = sqrtf(__fmaf_rn(tz, tz, __fmaf_rn(ty, ty, __fmul_rn(tx, tx))));
   const float inv = 1.0f / light_dist;
@@ -227,11 +263,17 @@ __device__ __forceinline__ float cone_shadow(const VoxelView& v, float voxel_siz
     U.z = __fmaf_rn(Dz, step, U.z);
     dist += step;
     const float radius = __fmul_rn(dist, dsr);
-    occlusion = __fmaf_rn(1.0f - occlusion, sample_voxels_at(v, U, __log2f(radius)), occlusion);
+    occlusion = __fmaf_rn(1.0f - occlusion, sample_voxels_at(v, U, __log2f(radius), reads), occlusion);
     if (dist >= goal || occlusion >= 1.0f) break;
     step = fmaxf(1.0f, __fmul_rn(radius, k));
   }
   return fminf(fmaxf(1.0f - occlusion, 0.0f), 1.0f);
+}
+__device__ __forceinline__ float cone_shadow(const VoxelView& v, float voxel_size, int max_steps, float cx, float cy,
+                                             float cz, float px, float py, float pz, float ax, float ay, float az,
+                                             float dsr) {
+  NoReads r;
+  return cone_shadow(v, voxel_size, max_steps, cx, cy, cz, px, py, pz, ax, ay, az, dsr, r);
 }
 
 }  // namespace drv

@@ -566,7 +566,9 @@ typedef struct DrvTuning {
   int32_t surrogate_wait_test; /* test hook, nonzero: the surrogate pass withholds its first tensor-core
                                   commit, so its bounded wait (~10 ms here) runs out; the stage then
                                   reports DRV_ERR_TIMEOUT from drv_sync and leaves the shadowing unset */
-  int32_t reserved[1];
+  int32_t count_voxel_reads;   /* nonzero: the split stage's cone pass runs its measuring instance, which
+                                  also counts the voxel loads of its cones (drv_get_cone_voxel_reads);
+                                  results are the same bit for bit */
 } DrvTuning;
 enum { DRV_LIGHT_PATH_AUTO = 0, DRV_LIGHT_PATH_SINGLE = 1, DRV_LIGHT_PATH_SPLIT = 2 };
 drv_status drv_set_tuning(DrvContext* ctx, const DrvTuning* tuning);
@@ -576,6 +578,23 @@ drv_status drv_get_tuning(DrvContext* ctx, DrvTuning* tuning);
  * contribute (each traced or evaluated once; those beyond the list's
  * capacity traced by the gather). Synchronises. */
 drv_status drv_get_light_pairs(DrvContext* ctx, uint32_t* pairs);
+
+/* Voxel loads of the last split light stage's cone pass run with
+ * DrvTuning.count_voxel_reads: reads[0] level-0 corner-packed bytes (1 B each),
+ * reads[1] corner-packed FP16 mip records (16 B each), reads[2] plain mip
+ * texels (4 B with FP32 precision, 2 B with BF16). These are the algorithmic
+ * bytes of the cone march (its L1/L2 roofline). Synchronises. No counterpart in
+ * the reference. */
+drv_status drv_get_cone_voxel_reads(DrvContext* ctx, uint32_t reads[3]);
+
+/* Load throughput of this GPU from L1 (level 1: every CTA re-reads its own
+ * 32 KB window; buffer >= 64 KB x SMs) or from L2 (level 2: all SMs sweep
+ * `bytes` of the buffer with loads that bypass L1; a buffer below the L2 size
+ * stays resident), in GB/s: the peaks the cone pass's voxel loads are held
+ * against. buffer: device, 16-byte aligned, never written. Synchronises. No
+ * counterpart in the reference. */
+drv_status drv_measure_load_bandwidth(int32_t level, const void* buffer, size_t bytes, int32_t reps,
+                                      void* cuda_stream, float* out_gbs);
 
 /* Kernels of the split light stage, in launch order (DrvTuning.time_kernels). */
 enum {

@@ -107,3 +107,43 @@ def test_kernel_timing_keeps_results_and_reports_each_kernel(cuda, lib):
     assert ms["mlp"] == pytest.approx(0.0, abs=0.05)  # no surrogate: the slot is empty
     p1.close()
     p2.close()
+
+
+@pytest.mark.parametrize("w", [pipeline.WORKLOADS["c1_small"], REDUCED], ids=["c1", "c2r"])
+def test_counting_cone_pass_is_bitwise_the_same(w, cuda, lib):
+    """The cone pass's measuring instance (DrvTuning.count_voxel_reads) traces
+    the same cones: same SH bit for bit; it reads at least one voxel sample per
+    traced cone and no more than its step limit allows (each step reads at most
+    one level-0 byte, or two mip records / sixteen plain texels)."""
+    p1, pos1, sh1 = _lit(w, 9, light_path=abi.LIGHT_PATH_SPLIT)
+    p2, pos2, sh2 = _lit(w, 9, light_path=abi.LIGHT_PATH_SPLIT, count_voxel_reads=1)
+    assert np.array_equal(pos1, pos2) and np.array_equal(sh1, sh2)
+    reads = (C.c_uint32 * 3)()
+    assert lib.drv_get_cone_voxel_reads(p2.ctx, reads) == abi.OK
+    l0, rec, tex = list(reads)
+    pairs = p2.light_pairs()
+    assert pairs > 0
+    assert l0 + rec + tex // 8 >= pairs
+    assert l0 + rec / 2 + tex / 16 <= pairs * w.max_cone_steps
+    # without the knob the counts are not available
+    assert lib.drv_get_cone_voxel_reads(p1.ctx, reads) == abi.ERR_INVALID_ARG
+    p1.close()
+    p2.close()
+
+
+def test_load_bandwidth_probe(cuda, lib):
+    """L1- and L2-resident load throughput, in GB/s (the cone pass's roofline
+    denominators): positive and within what a GPU can do; bad arguments refused."""
+    import torch
+    buf = torch.zeros(16 * 1024 * 1024, dtype=torch.int32, device=cuda)  # 64 MB
+    s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    g = C.c_float()
+    for level in (1, 2):
+        assert lib.drv_measure_load_bandwidth(level, C.c_void_p(buf.data_ptr()), buf.numel() * 4, 10, s,
+                                              C.byref(g)) == abi.OK
+        assert 100.0 < g.value < 1e6
+    assert lib.drv_measure_load_bandwidth(3, C.c_void_p(buf.data_ptr()), buf.numel() * 4, 10, s,
+                                          C.byref(g)) == abi.ERR_INVALID_ARG
+    assert lib.drv_measure_load_bandwidth(1, C.c_void_p(buf.data_ptr()), 1024, 10, s,
+                                          C.byref(g)) == abi.ERR_INVALID_ARG
+    assert int(buf.abs().sum()) == 0  # never written
