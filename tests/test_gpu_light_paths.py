@@ -113,8 +113,8 @@ def test_kernel_timing_keeps_results_and_reports_each_kernel(cuda, lib):
 def test_counting_cone_pass_is_bitwise_the_same(w, cuda, lib):
     """The cone pass's measuring instance (DrvTuning.count_voxel_reads) traces
     the same cones: same SH bit for bit; it reads at least one voxel sample per
-    traced cone and no more than its step limit allows (each step reads at most
-    one level-0 byte, or two mip records / sixteen plain texels)."""
+    traced cone and no more than its step limit allows (a step reads at most
+    two samples: level-0 bytes, mip records, or eight plain texels each)."""
     p1, pos1, sh1 = _lit(w, 9, light_path=abi.LIGHT_PATH_SPLIT)
     p2, pos2, sh2 = _lit(w, 9, light_path=abi.LIGHT_PATH_SPLIT, count_voxel_reads=1)
     assert np.array_equal(pos1, pos2) and np.array_equal(sh1, sh2)
@@ -124,7 +124,7 @@ def test_counting_cone_pass_is_bitwise_the_same(w, cuda, lib):
     pairs = p2.light_pairs()
     assert pairs > 0
     assert l0 + rec + tex // 8 >= pairs
-    assert l0 + rec / 2 + tex / 16 <= pairs * w.max_cone_steps
+    assert l0 + rec + tex / 8 <= 2 * pairs * w.max_cone_steps
     # without the knob the counts are not available
     assert lib.drv_get_cone_voxel_reads(p1.ctx, reads) == abi.ERR_INVALID_ARG
     p1.close()
