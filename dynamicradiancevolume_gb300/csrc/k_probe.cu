@@ -21,12 +21,15 @@ __global__ void __launch_bounds__(kL1Threads) l1_sweep_kernel(const uint4* __res
   const uint4* w = buf + (size_t)blockIdx.x * kL1WindowVec;
   uint32_t acc = 0;
   for (int r = 0; r < reps; ++r) {
+    // each pass starts at another offset of the window (and depends on the
+    // previous pass), so no pass's loads can be reused for another
+    const int rot = (int)((acc & 1u) + (uint32_t)r * 97u) & (kL1WindowVec - 1);
 #pragma unroll 4
     for (int i = threadIdx.x; i < kL1WindowVec; i += kL1Threads) {
-      const uint4 q = __ldg(w + i);
+      const uint4 q = __ldg(w + ((i + rot) & (kL1WindowVec - 1)));
       acc ^= q.x ^ q.y ^ q.z ^ q.w;
     }
-    acc = acc * 2654435761u + (uint32_t)r;  // a loop-carried dependence: every pass is kept
+    acc = acc * 2654435761u + (uint32_t)r;
   }
   if (acc == 0x9E3779B9u) sink[blockIdx.x * kL1Threads + threadIdx.x] = acc;
 }
@@ -36,9 +39,12 @@ __global__ void __launch_bounds__(256) l2_sweep_kernel(const uint4* __restrict__
   uint32_t acc = 0;
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   for (int r = 0; r < reps; ++r) {
+    const size_t rot = ((size_t)(acc & 1u) + (size_t)r * 4099u) % n_vec;
 #pragma unroll 4
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_vec; i += stride) {
-      const uint4 q = __ldcg(buf + i);
+      size_t j = i + rot;
+      if (j >= n_vec) j -= n_vec;
+      const uint4 q = __ldcg(buf + j);
       acc ^= q.x ^ q.y ^ q.z ^ q.w;
     }
     acc = acc * 2654435761u + (uint32_t)r;
