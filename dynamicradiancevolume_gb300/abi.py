@@ -15,7 +15,7 @@ MAX_LIGHTS = 16
 OK, ERR_INVALID_ARG, ERR_CAPACITY, ERR_CUDA, ERR_TIMEOUT, ERR_NOT_SUPPORTED, ERR_NUMERIC = range(7)
 STATUS_NAMES = {0: "DRV_OK", 1: "DRV_ERR_INVALID_ARG", 2: "DRV_ERR_CAPACITY", 3: "DRV_ERR_CUDA",
                 4: "DRV_ERR_TIMEOUT", 5: "DRV_ERR_NOT_SUPPORTED", 6: "DRV_ERR_NUMERIC"}
-DEVERR_CAPACITY, DEVERR_TIMEOUT, DEVERR_BOUNDS = 0x1, 0x2, 0x4
+DEVERR_CAPACITY, DEVERR_TIMEOUT, DEVERR_BOUNDS, DEVERR_NUMERIC = 0x1, 0x2, 0x4, 0x8
 SH2_SIGN_REFERENCE, SH2_SIGN_FIXED = 0, 1
 PRECISION_FP32, PRECISION_BF16 = 0, 1
 VISIBILITY_CONE, VISIBILITY_SURROGATE = 0, 1
@@ -139,7 +139,7 @@ class DrvTuning(C.Structure):
     _fields_ = [("light_path", C.c_int32), ("pair_capacity", C.c_uint32), ("cone_ctas_per_sm", C.c_int32),
                 ("gather_ctas_per_sm", C.c_int32), ("time_kernels", C.c_int32),
                 ("plain_voxel_reads", C.c_int32), ("surrogate_wait_test", C.c_int32),
-                ("count_voxel_reads", C.c_int32)]
+                ("count_voxel_reads", C.c_int32), ("check_inputs", C.c_int32)]
 
 
 LIGHT_KERNELS = ("cull", "classify", "scatter", "mlp", "cone", "gather")

@@ -234,10 +234,12 @@ drv_status drv_create(const DrvConfig* cfg, DrvContext** out) {
   if ((e = cudaMalloc(&c->entries, (size_t)cfg->max_caches * c->entry_stride)) != cudaSuccess) return bail(e);
   c->atlas_words = (size_t)cfg->n_cascades * cfg->cav_res * cfg->cav_res * cfg->cav_res;
   if ((e = cudaMalloc(&c->atlas, c->atlas_words * 4)) != cudaSuccess) return bail(e);
-  // counter (16 B) + ticket + error word, one allocation.
-  if ((e = cudaMalloc(&c->counter, 32)) != cudaSuccess) return bail(e);
+  // counter (16 B) + ticket + error word (cleared by every allocation, 32 B in
+  // all), then the input-check word (read and cleared by drv_get_error), one
+  // allocation.
+  if ((e = cudaMalloc(&c->counter, 64)) != cudaSuccess) return bail(e);
   c->scratch_words = reinterpret_cast<uint32_t*>(c->counter + 1);
-  if ((e = cudaMemset(c->counter, 0, 32)) != cudaSuccess) return bail(e);
+  if ((e = cudaMemset(c->counter, 0, 64)) != cudaSuccess) return bail(e);
   // Voxel level 0 (bitmask) and FP32 mips.
   const int N = cfg->voxel_res;
   c->voxel_words = (size_t)N * N * N / 32;
@@ -357,7 +359,11 @@ const char* drv_last_error_string(DrvContext* ctx) { return ctx ? ctx->last_erro
 drv_status drv_get_error(DrvContext* ctx, uint32_t* bits) {
   if (!ctx || !bits) return DRV_ERR_INVALID_ARG;
   DRV_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->s()));
-  DRV_TRY_CUDA(ctx, cudaMemcpy(bits, ctx->scratch_words + 1, 4, cudaMemcpyDeviceToHost));
+  uint32_t w[4];
+  DRV_TRY_CUDA(ctx, cudaMemcpy(w, ctx->scratch_words + 1, 16, cudaMemcpyDeviceToHost));
+  *bits = w[0] | w[3];
+  // The input-check word is reported once: cleared once read.
+  if (w[3]) DRV_TRY_CUDA(ctx, cudaMemset(ctx->input_err(), 0, 4));
   return DRV_OK;
 }
 
@@ -368,7 +374,9 @@ drv_status drv_sync(DrvContext* ctx) {
   if (st != DRV_OK) return st;
   if (bits & DRV_DEVERR_CAPACITY) return fail(ctx, DRV_ERR_CAPACITY, "more light caches requested than max_caches");
   if (bits & DRV_DEVERR_TIMEOUT) return fail(ctx, DRV_ERR_TIMEOUT, "a bounded device-side wait gave up");
-  if (bits & DRV_DEVERR_BOUNDS) return fail(ctx, DRV_ERR_INVALID_ARG, "device-side bounds check failed");
+  if (bits & DRV_DEVERR_BOUNDS)
+    return fail(ctx, DRV_ERR_INVALID_ARG, "device-side bounds check failed: an atlas slot names a cache beyond the count");
+  if (bits & DRV_DEVERR_NUMERIC) return fail(ctx, DRV_ERR_NUMERIC, "non-finite value in an input (check_inputs)");
   return DRV_OK;
 }
 
@@ -530,6 +538,11 @@ drv_status drv_prepare_rsm(DrvContext* ctx, int32_t li, const DrvSpotLight* L, c
   ch.normal[0] = const_cast<int16_t*>(v->normal);
   ch.dls[0] = const_cast<void*>(v->depth_lin_sq);
   ch.half0 = v->format == DRV_RSM_F16;
+  if (ctx->tuning.check_inputs) {
+    const size_t n = (size_t)R * R;
+    DRV_TRY_CUDA(ctx, drv::launch_scan_finite(ctx->s(), v->flux, n * 3, ch.half0, ctx->input_err()));
+    DRV_TRY_CUDA(ctx, drv::launch_scan_finite(ctx->s(), v->depth_lin_sq, n * 2, ch.half0, ctx->input_err()));
+  }
   for (int k = 0; k < deepest; ++k) {
     DRV_TRY_CUDA(ctx, drv::launch_downsample_rsm(ctx->s(), R >> k, ch.flux[k], ch.normal[k], ch.dls[k], ch.half(k),
                                                  static_cast<float*>(ch.flux[k + 1]), ch.normal[k + 1],
@@ -612,6 +625,12 @@ drv_status drv_allocate_caches(DrvContext* ctx, const DrvGBufferView* g, const D
   if (!ctx || !f || !vol) return DRV_ERR_INVALID_ARG;
   if (!views_ok(g, ctx->cfg)) return fail(ctx, DRV_ERR_INVALID_ARG, "G-buffer view does not match the config");
   ctx->last_volume = *vol;
+  if (ctx->tuning.check_inputs) {
+    const size_t n = (size_t)g->width * g->height;
+    DRV_TRY_CUDA(ctx, drv::launch_scan_finite(ctx->s(), g->depth, n, 0, ctx->input_err()));
+    if (g->normal_format == DRV_NORMAL_F32X3)
+      DRV_TRY_CUDA(ctx, drv::launch_scan_finite(ctx->s(), g->normal, n * 3, 0, ctx->input_err()));
+  }
   DRV_TRY_CUDA(ctx, cudaMemsetAsync(ctx->counter, 0, 32, ctx->s()));
   DRV_TRY_CUDA(ctx, cudaMemsetAsync(ctx->atlas, 0, ctx->atlas_words * 4, ctx->s()));
   return cuda_check(ctx, drv::launch_allocate(ctx->s(), ctx->cfg, *vol, *f, g->depth, g->width, g->height, ctx->atlas,
@@ -736,9 +755,12 @@ drv_status drv_apply(DrvContext* ctx, const DrvGBufferView* g, const DrvPerFrame
       return fail(ctx, DRV_ERR_INVALID_ARG, "specular apply needs drv_prepare_specular_envmaps after the light stage");
     sv = drv::make_spec_view(ctx->cfg, ctx->spec_env, ctx->spec_off, ctx->spec_atlas, ctx->spec_half, *f);
   }
+  if (ctx->tuning.check_inputs && g->albedo_format == DRV_ALBEDO_F32X3)
+    DRV_TRY_CUDA(ctx, drv::launch_scan_finite(ctx->s(), g->albedo, (size_t)g->width * g->height * 3, 0,
+                                              ctx->input_err()));
   return cuda_check(ctx, drv::launch_apply(ctx->s(), ctx->cfg, *vol, *f, *g, ctx->atlas, ctx->entries,
                                            ctx->entry_stride, ctx->counter, out_rgb, ctx->srgb,
-                                           ctx->spec_env ? &sv : nullptr),
+                                           ctx->spec_env ? &sv : nullptr, ctx->scratch_words + 1),
                     "apply");
 }
 

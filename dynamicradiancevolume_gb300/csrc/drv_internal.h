@@ -157,7 +157,8 @@ struct Context {
   uint32_t* atlas = nullptr;
   size_t atlas_words = 0;
   DrvCacheCounter* counter = nullptr;
-  uint32_t* scratch_words = nullptr;  // [0] alloc ticket, [1] device error bits
+  uint32_t* scratch_words = nullptr;  // [0] alloc ticket, [1] device error bits, [4] input-check bits
+  uint32_t* input_err() const { return scratch_words + 4; }
   // Voxels.
   uint32_t* voxel_bits = nullptr;
   size_t voxel_words = 0;
@@ -281,10 +282,14 @@ cudaError_t launch_bruteforce_rsm(cudaStream_t s, const DrvPerFrame& f, const Dr
                                   const float* rough_metal, const LightLaunch& ll, int bf16, float* out_rgb,
                                   const float* srgb);
 // spec: the envmap atlas when specular is on, else nullptr.
+// err: device error word (DRV_DEVERR_BOUNDS for an atlas slot past the count).
 cudaError_t launch_apply(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const DrvPerFrame& f,
                          const DrvGBufferView& g, const uint32_t* atlas, const void* entries, uint32_t entry_stride,
                          const DrvCacheCounter* counter, float* out_rgb, const float* srgb,
-                         const SpecView* spec = nullptr);
+                         const SpecView* spec = nullptr, uint32_t* err = nullptr);
+// Sets DRV_DEVERR_NUMERIC in *word when any of n values (float, or half when
+// half is nonzero) is NaN or infinite.
+cudaError_t launch_scan_finite(cudaStream_t s, const void* data, size_t n, int half, uint32_t* word);
 // Indirect specular (k_specular.cu): the level-0 envmaps of the allocated
 // caches (pairs: the split stage's pair list with its shadowing; nullptr:
 // every shadow block, cones traced here), then their mips and hole fill.

@@ -48,6 +48,7 @@ struct ApplyParams {
   SpecView spec;             // INDIRECT_SPECULAR only
   const void* rough_metal;   // drv_rough_metal_format
   int rm_f32;
+  uint32_t* err;             // DRV_DEVERR_BOUNDS (nullptr: not reported)
 };
 
 // Where a pixel reads the corner caches' envmaps. The lookup coordinate and
@@ -150,8 +151,11 @@ __device__ __forceinline__ f3 lighting(const ApplyParams& p, const float wp[3], 
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
     const uint32_t addr = slot[i];
-    // unallocated, outside the atlas, or 0xFFFFFFFF (locked by an overflow)
+    // unallocated, outside the atlas, or 0xFFFFFFFF (locked by an overflow);
+    // any other index past the count is not read (the reference reads it
+    // unchecked, cacheApply.frag:88-100) and is reported
     const bool live = addr != 0u && addr <= n_caches;
+    if (addr > n_caches && addr != 0xFFFFFFFFu && p.err) raise_error(p.err, DRV_DEVERR_BOUNDS);
     const int ox = i & 1, oy = (i >> 1) & 1, oz = i >> 2;
     const float w = wgt[0][ox] * wgt[1][oy] * wgt[2][oz];
     float er = 0.0f, eg = 0.0f, eb = 0.0f;
@@ -318,8 +322,10 @@ __global__ void __launch_bounds__(256, SPEC ? 3 : 5) apply_kernel(ApplyParams p)
 
 cudaError_t launch_apply(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const DrvPerFrame& f,
                          const DrvGBufferView& g, const uint32_t* atlas, const void* entries, uint32_t entry_stride,
-                         const DrvCacheCounter* counter, float* out_rgb, const float* srgb, const SpecView* spec) {
+                         const DrvCacheCounter* counter, float* out_rgb, const float* srgb, const SpecView* spec,
+                         uint32_t* err) {
   ApplyParams p{};
+  p.err = err;
   p.rc = make_cell_recip(vol);
   p.vol = vol;
   p.frame = f;

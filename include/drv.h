@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define DRV_ABI_VERSION 5
+#define DRV_ABI_VERSION 6
 #define DRV_MAX_CASCADES 4   /* MAX_NUM_ADDRESS_VOLUME_CASCADES, globalubos.glsl:43 */
 #define DRV_MAX_LIGHTS 16    /* maxExpectedLights, renderer.cpp:80 */
 #define DRV_LIGHTING_THREADS_PER_GROUP 64 /* lightcache.glsl:95 */
@@ -53,7 +53,8 @@ typedef enum drv_status {
 /* Device error-word bits (drv_get_error). */
 #define DRV_DEVERR_CAPACITY 0x1u
 #define DRV_DEVERR_TIMEOUT 0x2u
-#define DRV_DEVERR_BOUNDS 0x4u
+#define DRV_DEVERR_BOUNDS 0x4u   /* an atlas slot named a cache beyond the frame's count (drv_apply) */
+#define DRV_DEVERR_NUMERIC 0x8u  /* a non-finite input value (DrvTuning.check_inputs) */
 
 typedef enum drv_sh2_sign {
   /* Host constants exactly as renderer.cpp:296-300 uploads them
@@ -569,6 +570,11 @@ typedef struct DrvTuning {
   int32_t count_voxel_reads;   /* nonzero: the split stage's cone pass runs its measuring instance, which
                                   also counts the voxel loads of its cones (drv_get_cone_voxel_reads);
                                   results are the same bit for bit */
+  int32_t check_inputs;        /* nonzero: drv_prepare_rsm, drv_allocate_caches and drv_apply (so also
+                                  drv_frame) scan their float inputs (RSM flux and (d, d^2), depth, F32
+                                  normals and albedo) for NaN / Inf; one found is reported once, as
+                                  DRV_ERR_NUMERIC, by the next drv_sync (DRV_DEVERR_NUMERIC). A debugging
+                                  aid: it reads every input once more */
 } DrvTuning;
 enum { DRV_LIGHT_PATH_AUTO = 0, DRV_LIGHT_PATH_SINGLE = 1, DRV_LIGHT_PATH_SPLIT = 2 };
 drv_status drv_set_tuning(DrvContext* ctx, const DrvTuning* tuning);

@@ -6,6 +6,8 @@ Bars (written per test):
   - final indirect radiance within 1% relative L2 of the FP64 oracle
     (the tolerance the benchmark spec's metric states).
 """
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -513,3 +515,83 @@ def test_c2_production_frame_within_one_percent_of_fp64(c2, oracle):
     err = rel_l2(c2.out, ref)
     assert err < 1e-2, err
     assert np.isfinite(c2.out).all() and (c2.out >= 0).all()
+
+
+# ---------------------------------------------------------------- error paths
+def _view_u32(torch, ptr, numel, device):
+    """A writable uint32 (as int32) view of `numel` words at a device address."""
+
+    class _View:
+        __cuda_array_interface__ = {"shape": (numel,), "typestr": "<i4", "data": (int(ptr), False), "version": 3,
+                                    "strides": None}
+
+    return torch.as_tensor(_View(), device=device)
+
+
+def test_non_finite_inputs_are_reported_with_check_inputs(lib, cuda):
+    """A NaN written into the G-buffer depth or the RSM flux (host-side
+    injection) is reported as DRV_ERR_NUMERIC by the next drv_sync when
+    check_inputs is on, once; without it the frame runs, nothing is reported
+    and the output stays finite (the NaN pixel has no geometry)."""
+    import math
+    import torch
+    import dynamicradiancevolume_gb300 as drv
+    hf = pipeline.host_frame(pipeline.WORKLOADS["c1_small"])
+    p = pipeline.Pipeline(hf)
+    p.raycast_inputs()
+    p.frame()
+    p.sync()
+    p.depth.view(-1)[1234] = math.nan
+    p.frame()
+    p.sync()  # not checked: no status
+    assert np.isfinite(p.out.cpu().numpy()).all()
+    p.set_tuning(check_inputs=1)
+    p.frame()
+    with pytest.raises(drv.DrvError) as e:
+        p.sync()
+    assert e.value.status == abi.ERR_NUMERIC
+    p.sync()  # reported once
+    p.depth.view(-1)[1234] = 0.5
+    p.frame()
+    p.sync()  # finite inputs: nothing to report
+    p.rsm_flux[0].view(-1)[77] = math.inf
+    p.frame()
+    with pytest.raises(drv.DrvError) as e:
+        p.sync()
+    assert e.value.status == abi.ERR_NUMERIC
+    p.close()
+
+
+def test_atlas_slot_past_the_count_is_reported_not_read(lib, cuda):
+    """A cache-address atlas whose slot names a cache beyond the frame's count
+    (host-side corruption between allocation and apply): the apply does not
+    read that entry (it contributes nothing), latches DRV_DEVERR_BOUNDS, and
+    drv_sync reports it; the rest of the frame is unchanged."""
+    import torch
+    import dynamicradiancevolume_gb300 as drv
+    hf = pipeline.host_frame(pipeline.WORKLOADS["c1_small"])
+    p = pipeline.Pipeline(hf)
+    p.raycast_inputs()
+    p.frame()
+    p.sync()
+    good = p.out.cpu().numpy().copy()
+    count = p.cache_count()
+    b = p.buffers()
+    atlas = _view_u32(torch, b.cav_atlas, hf.config.n_cascades * hf.config.cav_res ** 3, p.device)
+    live = torch.nonzero(atlas > 0).flatten()
+    slot = int(live[len(live) // 2])
+    atlas[slot] = count + 1000
+    torch.cuda.synchronize()
+    st = lib.drv_apply(p.ctx, C.byref(p.gview), C.byref(hf.frame), C.byref(hf.volume),
+                       C.c_void_p(p.out.data_ptr()))
+    assert st == abi.OK
+    bits = C.c_uint32()
+    assert lib.drv_get_error(p.ctx, C.byref(bits)) == abi.OK
+    assert bits.value & abi.DEVERR_BOUNDS
+    with pytest.raises(drv.DrvError):
+        p.sync()
+    out = p.out.cpu().numpy()
+    assert np.isfinite(out).all()
+    changed = np.any(out != good, axis=-1)
+    assert 0 < changed.mean() < 0.5  # only pixels around that one corner lose its contribution
+    p.close()
