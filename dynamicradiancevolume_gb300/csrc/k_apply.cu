@@ -244,7 +244,9 @@ __global__ void __launch_bounds__(256, SPEC ? 3 : 5) apply_kernel(ApplyParams p)
   // G-buffer texels are read once and the output written once: streaming
   // (evict-first) accesses keep L1/L2 for the atlas and the cache entries.
   const float d = __ldcs(p.depth + i);
-  if (d < 0.00001f) {  // cacheApply.frag:304-307 (discard)
+  // cacheApply.frag:304-307 (discard). A NaN depth counts as no geometry
+  // too (the reference's test passes it and shades NaN).
+  if (!(d >= 0.00001f)) {
     if (!p.out_add) store_output(p, i, mkf3(0.0f, 0.0f, 0.0f));
     return;
   }
