@@ -85,6 +85,25 @@ __device__ __forceinline__ void publish(const AllocParams& p, int coord, int cas
   }
 }
 
+// Warp-aggregated reservation of entries for the won corners (the reference
+// takes one atomicAdd per won corner, cacheGather.comp:63): a scan of the
+// lanes' counts and one atomicAdd per warp; returns this lane's first index.
+// Called by every lane of the warp.
+__device__ __forceinline__ uint32_t reserve_entries(const AllocParams& p, uint32_t won, int lane) {
+  const uint32_t mine = (uint32_t)__popc(won);
+  uint32_t incl = mine;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+  uint32_t base = 0;
+  if (lane == 31 && total) base = (uint32_t)atomicAdd(&p.counter->total_light_cache_count, (int)total);
+  base = __shfl_sync(0xffffffffu, base, 31);
+  return base + incl - mine;
+}
+
 // Eight CTAs per SM (32 registers): 0.054 -> 0.048 ms at 1080p,
 // the compare-and-swap chains' latency hidden by more resident tiles.
 __global__ void __launch_bounds__(kTile* kTile, 8) allocate_kernel(AllocParams p) {
@@ -121,38 +140,26 @@ __global__ void __launch_bounds__(kTile* kTile, 8) allocate_kernel(AllocParams p
   // neighbour registered the same cell; the vector equality of :146 holds
   // only for thread (0,0), so the other threads of row 0 / column 0 compare
   // against themselves and never allocate (kept as in the reference).
-  uint32_t won1 = 0, won2 = 0;
+  const int lane = (int)((threadIdx.y * kTile + threadIdx.x) & 31u);
   {
+    uint32_t won = 0;
     const int ux = max(0, lx - 1), uy = max(0, ly - 1);
     const bool self = (ux == lx && uy == ly);
     if (((list1[lx][uy] != own && list1[ux][ly] != own && list1[ux][uy] != own) || self) && own != -1)
-      won1 = lock_corners(p, own, cascade);
+      won = lock_corners(p, own, cascade);
+    const uint32_t first = reserve_entries(p, won, lane);
+    if (won) publish(p, own, cascade, won, first);
   }
   // cacheGather.comp:153-162: transition cells, looking down/right.
   if (p.transitions) {
+    uint32_t won = 0;
     const int dx = min(kTile - 1, lx + 1), dy = min(kTile - 1, ly + 1);
     const bool corner = (dx == kTile - 1 && dy == kTile - 1);
     if (((list2[lx][dy] != own2 && list2[dx][ly] != own2 && list2[dx][dy] != own2) || corner) && own2 != -1)
-      won2 = lock_corners(p, own2, cascade + 1);
+      won = lock_corners(p, own2, cascade + 1);
+    const uint32_t first = reserve_entries(p, won, lane);
+    if (won) publish(p, own2, cascade + 1, won, first);
   }
-  // Warp-aggregated reservation (the reference takes one atomicAdd per won
-  // corner, cacheGather.comp:63): a scan of the lanes' won-corner counts and
-  // one atomicAdd per warp.
-  const int lane = (int)((threadIdx.y * kTile + threadIdx.x) & 31u);
-  const uint32_t mine = (uint32_t)(__popc(won1) + __popc(won2));
-  uint32_t incl = mine;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += t;
-  }
-  const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-  uint32_t base = 0;
-  if (lane == 0 && total) base = (uint32_t)atomicAdd(&p.counter->total_light_cache_count, (int)total);
-  base = __shfl_sync(0xffffffffu, base, 0);
-  const uint32_t first = base + incl - mine;
-  if (won1) publish(p, own, cascade, won1, first);
-  if (won2) publish(p, own2, cascade + 1, won2, first + (uint32_t)__popc(won1));
 }
 
 // cachePrepareLighting.comp: dispatch size of the lighting pass.
