@@ -30,19 +30,18 @@ struct AllocParams {
   const float* ndc_y;
 };
 
-// AllocateCaches, cacheGather.comp:32-91, in two halves so that a warp can
-// reserve all its entries with one atomic: lock_corners tries the cell's 8
-// corners (compare-and-swap 0 -> 0xFFFFFFFF; all issued before any result is
-// used) and returns the won ones as a mask; publish writes the won corners'
-// entries from consecutive indices starting at `first`. Corners outside the
-// atlas are skipped (the reference performs an image atomic there, which GL
-// defines to do nothing and return 0, and then allocates an entry nobody can
-// address). Entry order is atomic order, as in the reference.
-__device__ __forceinline__ uint32_t lock_corners(const AllocParams& p, int coord, int cascade) {
+// AllocateCaches, cacheGather.comp:32-91. Corners outside the atlas are
+// skipped (the reference performs an image atomic there, which GL defines to
+// do nothing and return 0, and then allocates an entry nobody can address).
+// The 8 compare-and-swaps are independent, so all are issued before any
+// result is used, and the won corners take consecutive entries from one
+// atomicAdd (entry order is atomic order in the reference as well).
+__device__ void allocate_cell(const AllocParams& p, int coord, int cascade) {
   const int res = p.res, res2 = res * res, res3 = res2 * res;
   const int aw = p.n_cascades * res;
   const int base = coord - res3 * cascade;
   const int bz = base / res2, by = (base - bz * res2) / res, bx = base % res;
+  const DrvCascade& k = p.vol.cascades[cascade];
   uint32_t won = 0;
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
@@ -53,15 +52,8 @@ __device__ __forceinline__ uint32_t lock_corners(const AllocParams& p, int coord
         atomicCAS(p.atlas + ((size_t)lz * res + ly) * aw + ax, 0u, 0xFFFFFFFFu) == 0u)
       won |= 1u << i;
   }
-  return won;
-}
-
-__device__ __forceinline__ void publish(const AllocParams& p, int coord, int cascade, uint32_t won, uint32_t first) {
-  const int res = p.res, res2 = res * res, res3 = res2 * res;
-  const int aw = p.n_cascades * res;
-  const int base = coord - res3 * cascade;
-  const int bz = base / res2, by = (base - bz * res2) / res, bx = base % res;
-  const DrvCascade& k = p.vol.cascades[cascade];
+  if (!won) return;
+  const uint32_t first = (uint32_t)atomicAdd(&p.counter->total_light_cache_count, __popc(won));
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
     if (!((won >> i) & 1u)) continue;
@@ -85,26 +77,7 @@ __device__ __forceinline__ void publish(const AllocParams& p, int coord, int cas
   }
 }
 
-// Warp-aggregated reservation of entries for the won corners (the reference
-// takes one atomicAdd per won corner, cacheGather.comp:63): a scan of the
-// lanes' counts and one atomicAdd per warp; returns this lane's first index.
-// Called by every lane of the warp.
-__device__ __forceinline__ uint32_t reserve_entries(const AllocParams& p, uint32_t won, int lane) {
-  const uint32_t mine = (uint32_t)__popc(won);
-  uint32_t incl = mine;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += t;
-  }
-  const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-  uint32_t base = 0;
-  if (lane == 31 && total) base = (uint32_t)atomicAdd(&p.counter->total_light_cache_count, (int)total);
-  base = __shfl_sync(0xffffffffu, base, 31);
-  return base + incl - mine;
-}
-
-// Eight CTAs per SM (32 registers): 0.054 -> 0.048 ms at 1080p,
+// Eight CTAs per SM (32 registers, no spill): 0.054 -> 0.048 ms at 1080p,
 // the compare-and-swap chains' latency hidden by more resident tiles.
 __global__ void __launch_bounds__(kTile* kTile, 8) allocate_kernel(AllocParams p) {
   __shared__ int list1[kTile][kTile];
@@ -140,25 +113,18 @@ __global__ void __launch_bounds__(kTile* kTile, 8) allocate_kernel(AllocParams p
   // neighbour registered the same cell; the vector equality of :146 holds
   // only for thread (0,0), so the other threads of row 0 / column 0 compare
   // against themselves and never allocate (kept as in the reference).
-  const int lane = (int)((threadIdx.y * kTile + threadIdx.x) & 31u);
   {
-    uint32_t won = 0;
     const int ux = max(0, lx - 1), uy = max(0, ly - 1);
     const bool self = (ux == lx && uy == ly);
     if (((list1[lx][uy] != own && list1[ux][ly] != own && list1[ux][uy] != own) || self) && own != -1)
-      won = lock_corners(p, own, cascade);
-    const uint32_t first = reserve_entries(p, won, lane);
-    if (won) publish(p, own, cascade, won, first);
+      allocate_cell(p, own, cascade);
   }
   // cacheGather.comp:153-162: transition cells, looking down/right.
   if (p.transitions) {
-    uint32_t won = 0;
     const int dx = min(kTile - 1, lx + 1), dy = min(kTile - 1, ly + 1);
     const bool corner = (dx == kTile - 1 && dy == kTile - 1);
     if (((list2[lx][dy] != own2 && list2[dx][ly] != own2 && list2[dx][dy] != own2) || corner) && own2 != -1)
-      won = lock_corners(p, own2, cascade + 1);
-    const uint32_t first = reserve_entries(p, won, lane);
-    if (won) publish(p, own2, cascade + 1, won, first);
+      allocate_cell(p, own2, cascade + 1);
   }
 }
 
