@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extra-workloads", action="store_true",
                     help="measure only --workload (by default the 1080p line also measures c2_production)")
+    ap.add_argument("--batch-scenes", type=int, default=64,
+                    help="scenes of the batched multi-scene measurement (0: none)")
     ap.add_argument("--thresholds", type=float, nargs="*", default=[0.5, 0.8],
                     help="surrogate confidence thresholds to measure")
     return ap.parse_args()
@@ -746,6 +748,10 @@ def run_ours(args):
         others = {name: measure_workload(pipeline.WORKLOADS[name], args, dev, flush, rank, None, features,
                                          full=False) for name in extra}
         cache_peaks = measure_cache_peaks(dev)
+        batch = None
+        if args.batch_scenes > 0 and args.workload == "ns_1080p_4096" and rank == 0:
+            from dynamicradiancevolume_gb300 import batch as batch_mod
+            batch = batch_mod.run_batch(args.batch_scenes, reps=5, log=lambda m: None, tune_reps=2)
     clocks = clk.summary()
     pk = peaks()
     hv, head, count = r["hv"], r["head"], r["count"]
@@ -780,6 +786,13 @@ def run_ours(args):
     }
     if surrogate_note:
         line["surrogate_skipped"] = surrogate_note
+    if batch is not None:
+        # config 5: many seeded scenes of uneven sizes, BF16 storage, surrogate
+        # visibility; one CUDA-graph launch against the scenes one by one (each
+        # scene's frame alone, as the reference renders one scene per Renderer)
+        line["batch"] = {k: batch[k] for k in ("scenes", "precision", "visibility", "threshold", "sizes", "tuned",
+                                               "batch", "one_by_one", "speedup")}
+        line["batch"]["trials"] = len(batch["trials"])
     threads = os.cpu_count() or 1
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_of(w, threads)

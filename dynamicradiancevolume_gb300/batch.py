@@ -1,7 +1,7 @@
 """Batched multi-scene frames: many independent seeded scenes of uneven sizes
 rendered by one CUDA-graph launch (drv_batch_*), against the same scenes run
 one by one; plus the autotuner that picks the batch's stream count and the
-light stage's grid knobs.
+light stage's grid and tile knobs.
 
     python -m dynamicradiancevolume_gb300.batch --scenes 64 --reps 10
 
@@ -126,9 +126,17 @@ class Batch:
             pass
 
 
-def set_knobs(scenes: list[Scene], cone_ctas: int, gather_ctas: int) -> None:
+# The light stage's knobs the autotuner searches, each with its menu: the cone
+# and gather passes' CTAs per SM (0: as many as fit), the cull's tile (caches
+# tested per pass against the VPL records staged in shared memory) and the
+# gather's tile (threads per cache, i.e. pairs a thread sums).
+KNOB_MENUS = {"cone_ctas_per_sm": (0, 4, 2), "gather_ctas_per_sm": (0, 2, 1), "cull_caches_per_pass": (4, 2, 8),
+              "gather_threads": (256, 128)}
+
+
+def set_knobs(scenes: list[Scene], **knobs) -> None:
     for s in scenes:
-        s.pipe.set_tuning(cone_ctas_per_sm=cone_ctas, gather_ctas_per_sm=gather_ctas)
+        s.pipe.set_tuning(**knobs)
 
 
 def time_batch(scenes, streams: int, reps: int, warmup: int = 2):
@@ -158,67 +166,65 @@ def time_one_by_one(scenes, reps: int, warmup: int = 2):
     return float(lat.sum()), lat
 
 
-def autotune(scenes, reps: int = 3, streams_menu=(1, 2, 4, 8, 16, 32), knob_menu=((0, 0), (4, 0), (2, 0), (0, 2),
-                                                                                   (2, 1), (1, 1)), log=print):
-    """Stream count first (default knobs), then the light stage's CTAs per SM
-    of the cone and gather passes at that stream count; returns the best
-    (streams, cone_ctas, gather_ctas) and the trials."""
-    trials = []
-    set_knobs(scenes, 0, 0)
-    best = None
+def autotune(scenes, reps: int = 3, streams_menu=(1, 2, 4, 8, 16, 32), knob_menus=None, log=print):
+    """Stream count first (default knobs), then each light-stage knob in turn
+    over its menu with the others held at their best (coordinate descent);
+    returns the best setting and every trial."""
+    knob_menus = knob_menus or KNOB_MENUS
+    best_knobs = {k: menu[0] for k, menu in knob_menus.items()}
+    set_knobs(scenes, **best_knobs)
+    trials, best = [], None
     for s in streams_menu:
         if s > len(scenes):
             continue
         t, _ = time_batch(scenes, s, reps, warmup=1)
-        trials.append({"streams": s, "cone_ctas_per_sm": 0, "gather_ctas_per_sm": 0, "ms": t})
+        trials.append({"streams": s, **best_knobs, "ms": t})
         log(f"  streams {s:2d}: {t:.3f} ms")
         if best is None or t < best[0]:
-            best = (t, s, 0, 0)
-    for cone, gather in knob_menu:
-        if (cone, gather) == (0, 0):
-            continue
-        set_knobs(scenes, cone, gather)
-        t, _ = time_batch(scenes, best[1], reps, warmup=1)
-        trials.append({"streams": best[1], "cone_ctas_per_sm": cone, "gather_ctas_per_sm": gather, "ms": t})
-        log(f"  streams {best[1]:2d} cone {cone} gather {gather}: {t:.3f} ms")
-        if t < best[0]:
-            best = (t, best[1], cone, gather)
-    set_knobs(scenes, best[2], best[3])
-    return {"streams": best[1], "cone_ctas_per_sm": best[2], "gather_ctas_per_sm": best[3], "ms": best[0]}, trials
+            best = (t, s)
+    best_ms, streams = best
+    for name, menu in knob_menus.items():
+        for v in menu[1:]:
+            trial = dict(best_knobs, **{name: v})
+            set_knobs(scenes, **trial)
+            t, _ = time_batch(scenes, streams, reps, warmup=1)
+            trials.append({"streams": streams, **trial, "ms": t})
+            log(f"  streams {streams:2d} {name} {v}: {t:.3f} ms")
+            if t < best_ms:
+                best_ms, best_knobs = t, trial
+    set_knobs(scenes, **best_knobs)
+    return {"streams": streams, **best_knobs, "ms": best_ms}, trials
 
 
-def main(argv=None):
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--scenes", type=int, default=64)
-    ap.add_argument("--reps", type=int, default=10)
-    ap.add_argument("--threshold", type=float, default=0.5)
-    ap.add_argument("--fp32-cone", action="store_true", help="FP32 storage and cone visibility instead")
-    args = ap.parse_args(argv)
-    prec = abi.PRECISION_FP32 if args.fp32_cone else abi.PRECISION_BF16
-    vis = abi.VISIBILITY_CONE if args.fp32_cone else abi.VISIBILITY_SURROGATE
+def run_batch(n_scenes: int, reps: int, threshold: float = 0.5, fp32_cone: bool = False, log=None,
+              tune_reps: int = 3) -> dict:
+    """Builds n seeded scenes, autotunes, times the batch and the scenes one
+    by one; returns the report (scenes/s, caches lit/s, latency p50/p99)."""
+    prec = abi.PRECISION_FP32 if fp32_cone else abi.PRECISION_BF16
+    vis = abi.VISIBILITY_CONE if fp32_cone else abi.VISIBILITY_SURROGATE
+    log = log or (lambda s: print(s, file=sys.stderr, flush=True))
     t0 = time.time()
-    specs = batch_workloads(args.scenes, precision=prec, visibility=vis)
-    scenes = make_scenes(specs, args.threshold)
+    specs = batch_workloads(n_scenes, precision=prec, visibility=vis)
+    scenes = make_scenes(specs, threshold)
     setup_s = time.time() - t0
-    log = lambda s: print(s, file=sys.stderr, flush=True)
-    tuned, trials = autotune(scenes, log=log)
-    batch_ms, batch_lat = time_batch(scenes, tuned["streams"], args.reps)
-    seq_ms, seq_lat = time_one_by_one(scenes, args.reps)
+    tuned, trials = autotune(scenes, reps=tune_reps, log=log)
+    batch_ms, batch_lat = time_batch(scenes, tuned["streams"], reps)
+    seq_ms, seq_lat = time_one_by_one(scenes, reps)
     caches = np.array([s.caches for s in scenes])
     px = np.array([s.pipe.hf.workload.width * s.pipe.hf.workload.height for s in scenes])
     line = {
-        "scenes": args.scenes, "precision": "bf16" if prec == abi.PRECISION_BF16 else "f32",
+        "scenes": n_scenes, "precision": "bf16" if prec == abi.PRECISION_BF16 else "f32",
         "visibility": "surrogate" if vis == abi.VISIBILITY_SURROGATE else "cone",
-        "threshold": args.threshold if vis == abi.VISIBILITY_SURROGATE else None,
+        "threshold": threshold if vis == abi.VISIBILITY_SURROGATE else None,
         "sizes": {"pixels": [int(px.min()), int(px.max())], "caches": [int(caches.min()), int(caches.max())],
                   "vpls": [int(min(s.vpls for s in scenes)), int(max(s.vpls for s in scenes))],
                   "voxels": sorted({s.pipe.hf.workload.voxel_res for s in scenes})},
         "tuned": tuned,
-        "batch": {"ms": batch_ms, "scenes_per_s": args.scenes / (batch_ms / 1e3),
+        "batch": {"ms": batch_ms, "scenes_per_s": n_scenes / (batch_ms / 1e3),
                   "caches_per_s": float(caches.sum()) / (batch_ms / 1e3),
                   "latency_ms_p50": float(np.percentile(batch_lat, 50)),
                   "latency_ms_p99": float(np.percentile(batch_lat, 99))},
-        "one_by_one": {"ms": seq_ms, "scenes_per_s": args.scenes / (seq_ms / 1e3),
+        "one_by_one": {"ms": seq_ms, "scenes_per_s": n_scenes / (seq_ms / 1e3),
                        "caches_per_s": float(caches.sum()) / (seq_ms / 1e3),
                        "latency_ms_p50": float(np.percentile(seq_lat, 50)),
                        "latency_ms_p99": float(np.percentile(seq_lat, 99))},
@@ -229,9 +235,19 @@ def main(argv=None):
         "trials": trials,
         "setup_s": setup_s,
     }
-    print(json.dumps(line), flush=True)
     for s in scenes:
         s.pipe.close()
+    return line
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--scenes", type=int, default=64)
+    ap.add_argument("--reps", type=int, default=10)
+    ap.add_argument("--threshold", type=float, default=0.5)
+    ap.add_argument("--fp32-cone", action="store_true", help="FP32 storage and cone visibility instead")
+    args = ap.parse_args(argv)
+    print(json.dumps(run_batch(args.scenes, args.reps, args.threshold, args.fp32_cone)), flush=True)
     return 0
 
 

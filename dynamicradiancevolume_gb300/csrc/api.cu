@@ -690,6 +690,12 @@ drv_status light_caches(DrvContext* ctx, const DrvSpotLight* lights, int32_t n_l
         events = ctx->lk_events;
       }
     }
+    drv::SplitKnobs knobs;
+    knobs.cone_ctas_per_sm = ctx->tuning.cone_ctas_per_sm;
+    knobs.gather_ctas_per_sm = ctx->tuning.gather_ctas_per_sm;
+    if (ctx->tuning.cull_caches_per_pass) knobs.cull_caches_per_pass = ctx->tuning.cull_caches_per_pass;
+    if (ctx->tuning.gather_threads) knobs.gather_threads = ctx->tuning.gather_threads;
+    knobs.count_voxel_reads = ctx->tuning.count_voxel_reads != 0;
     drv::SurrogateArgs sur;
     if (surrogate) {
       sur.weights = ctx->sur_weights;
@@ -700,10 +706,7 @@ drv_status light_caches(DrvContext* ctx, const DrvSpotLight* lights, int32_t n_l
     }
     drv_status st = cuda_check(ctx, drv::launch_light_split(ctx->s(), ctx->cfg, *vol, ll, ctx->counter, ctx->entries,
                                                             ctx->entry_stride, ctx->light_voxels(), pairs, sur,
-                                                            ctx->scratch_words + 1,
-                                                            ctx->tuning.cone_ctas_per_sm,
-                                                            ctx->tuning.gather_ctas_per_sm, ctx->num_sms,
-                                                            ctx->tuning.count_voxel_reads != 0, events,
+                                                            ctx->scratch_words + 1, knobs, ctx->num_sms, events,
                                                             voxels_ready),
                                "light_caches");
     if (events) ctx->lk_recorded = st == DRV_OK;
@@ -883,6 +886,11 @@ drv_status drv_set_tuning(DrvContext* ctx, const DrvTuning* t) {
   if (t->light_path < DRV_LIGHT_PATH_AUTO || t->light_path > DRV_LIGHT_PATH_SPLIT || t->cone_ctas_per_sm < 0 ||
       t->gather_ctas_per_sm < 0 || t->cone_ctas_per_sm > 32 || t->gather_ctas_per_sm > 32)
     return fail(ctx, DRV_ERR_INVALID_ARG, "bad tuning");
+  if (t->cull_caches_per_pass != 0 && t->cull_caches_per_pass != 2 && t->cull_caches_per_pass != 4 &&
+      t->cull_caches_per_pass != 8)
+    return fail(ctx, DRV_ERR_INVALID_ARG, "cull_caches_per_pass must be 0, 2, 4 or 8");
+  if (t->gather_threads != 0 && t->gather_threads != 128 && t->gather_threads != 256)
+    return fail(ctx, DRV_ERR_INVALID_ARG, "gather_threads must be 0, 128 or 256");
   if (t->light_path == DRV_LIGHT_PATH_SINGLE) DRV_TRY_CUDA(ctx, ensure_single_scratch(ctx));
   if (t->pair_capacity > ctx->pairs.cap) {
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;

@@ -269,14 +269,25 @@ struct SurrogateArgs {
   int hold_commit = 0;
 };
 
+// Execution knobs of the split light stage (DrvTuning): CTAs per SM of the
+// cone and gather passes (0: as many as fit), the cull's caches per pass (2,
+// 4 or 8) and the gather's threads per cache (128 or 256), and the cone
+// pass's measuring instance.
+struct SplitKnobs {
+  int cone_ctas_per_sm = 0;
+  int gather_ctas_per_sm = 0;
+  int cull_caches_per_pass = 4;
+  int gather_threads = 256;
+  bool count_voxel_reads = false;
+};
+
 // Split light stage: cull -> (cones | surrogate MLP + cones of the
 // unconfident pairs) -> gather.
 bool light_split_supported(const DrvConfig& cfg, const LightLaunch& ll);
 cudaError_t launch_light_split(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const LightLaunch& ll,
                                const DrvCacheCounter* counter, void* entries, uint32_t entry_stride,
                                const VoxelInputs& vox, const PairList& pairs, const SurrogateArgs& sur,
-                               uint32_t* err, int cone_ctas_per_sm, int gather_ctas_per_sm, int num_sms,
-                               bool count_voxel_reads = false, cudaEvent_t* events = nullptr,
+                               uint32_t* err, const SplitKnobs& knobs, int num_sms, cudaEvent_t* events = nullptr,
                                cudaEvent_t voxels_ready = nullptr);
 cudaError_t launch_bruteforce_rsm(cudaStream_t s, const DrvPerFrame& f, const DrvGBufferView& g,
                                   const float* rough_metal, const LightLaunch& ll, int bf16, float* out_rgb,

@@ -197,17 +197,18 @@ __global__ void __launch_bounds__(kCullThreads) cull_kernel(StageParams p, PairL
 // both this sum and the gather's normalised test (a few u = 2^-24 relative to
 // |p| + |c|), so the cull stays a superset of the pairs the gather's exact
 // test keeps; the few extra near-tangent pairs are gathered with weight 0.
-// Each CTA tests kCullRecCaches caches per pass: one shared-memory load
-// serves that many tests of three FMAs each.
+// Each CTA tests K caches per pass (the tile: K caches x every record; 4 by
+// default, DrvTuning.cull_caches_per_pass): one shared-memory load serves K
+// tests of three FMAs each.
 constexpr int kCullRecThreads = 512;
 constexpr int kCullRecWarps = kCullRecThreads / 32;
-constexpr int kCullRecCaches = 4;
+constexpr int kCullRecCaches = 4;  // default K
 constexpr size_t kCullRecMaxSmem = 220 * 1024;
 
 // Shared memory of cull_records_kernel: the records, then per cache of the
 // pass the ballot words and their exclusive prefix.
-inline size_t cull_records_smem(int total_vpls, int words) {
-  return (size_t)total_vpls * 16 + (size_t)2 * kCullRecCaches * words * 4;
+inline size_t cull_records_smem(int total_vpls, int words, int K) {
+  return (size_t)total_vpls * 16 + (size_t)2 * K * words * 4;
 }
 
 // UNIT: every light's shadow blocks are single VPLs, so block b's record is
@@ -215,15 +216,15 @@ inline size_t cull_records_smem(int total_vpls, int words) {
 // the VPL extraction); one bulk asynchronous copy per light (TMA, completion
 // on an mbarrier, bounded wait) stages them, instead of computing them here
 // from the VPLs.
-template <bool BF16, bool UNIT, bool COPY>
+template <bool BF16, bool UNIT, bool COPY, int K>
 __global__ void __launch_bounds__(kCullRecThreads) cull_records_kernel(StageParams p, PairList L, int total_vpls) {
   pdl_wait_and_release();
   extern __shared__ float4 s_rec[];
-  __shared__ uint32_t s_base[kCullRecCaches], s_count[kCullRecCaches];
+  __shared__ uint32_t s_base[K], s_count[K];
   __shared__ __align__(8) uint64_t s_bar;
   const int W = (p.total_blocks + 31) >> 5;
   uint32_t* s_mask = reinterpret_cast<uint32_t*>(s_rec + total_vpls);  // [K][W]
-  uint32_t* s_pre = s_mask + kCullRecCaches * W;                        // [K][W]
+  uint32_t* s_pre = s_mask + K * W;                        // [K][W]
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   // VPL records, in light order (light l's VPLs from vpl_base(l)).
   if (COPY) {
@@ -284,24 +285,24 @@ __global__ void __launch_bounds__(kCullRecThreads) cull_records_kernel(StagePara
     __syncthreads();
   }
   const uint32_t n_caches = cache_count(p);
-  for (uint32_t c0 = blockIdx.x * kCullRecCaches; c0 < n_caches; c0 += gridDim.x * kCullRecCaches) {
-    float cx[kCullRecCaches], cy[kCullRecCaches], cz[kCullRecCaches], lim[kCullRecCaches];
+  for (uint32_t c0 = blockIdx.x * K; c0 < n_caches; c0 += gridDim.x * K) {
+    float cx[K], cy[K], cz[K], lim[K];
 #pragma unroll
-    for (int k = 0; k < kCullRecCaches; ++k) {
+    for (int k = 0; k < K; ++k) {
       const uint32_t c = min(c0 + k, n_caches - 1u);  // past the end: a copy of the last cache, not written
       cache_position<BF16>(p, c, cx[k], cy[k], cz[k]);
       lim[k] = -kCullRecordEps * fmaxf(fmaxf(fabsf(cx[k]), fabsf(cy[k])), fabsf(cz[k]));
     }
     for (int w = warp; w < W; w += kCullRecWarps) {
       const int b = (w << 5) + lane;
-      bool live[kCullRecCaches];
+      bool live[K];
 #pragma unroll
-      for (int k = 0; k < kCullRecCaches; ++k) live[k] = false;
+      for (int k = 0; k < K; ++k) live[k] = false;
       if (b < p.total_blocks) {
         if (UNIT) {
           const float4 r = s_rec[b];
 #pragma unroll
-          for (int k = 0; k < kCullRecCaches; ++k)
+          for (int k = 0; k < K; ++k)
             live[k] = fmaf(r.x, cx[k], fmaf(r.y, cy[k], fmaf(r.z, cz[k], r.w))) > lim[k];
         } else {
           int l = 0, vbase = 0;
@@ -311,13 +312,13 @@ __global__ void __launch_bounds__(kCullRecThreads) cull_records_kernel(StagePara
           for (int j = 0; j < interval; ++j) {
             const float4 r = s_rec[first + j];
 #pragma unroll
-            for (int k = 0; k < kCullRecCaches; ++k)
+            for (int k = 0; k < K; ++k)
               live[k] |= fmaf(r.x, cx[k], fmaf(r.y, cy[k], fmaf(r.z, cz[k], r.w))) > lim[k];
           }
         }
       }
 #pragma unroll
-      for (int k = 0; k < kCullRecCaches; ++k) {
+      for (int k = 0; k < K; ++k) {
         const uint32_t m = __ballot_sync(0xffffffffu, live[k]);
         if (lane == 0) s_mask[k * W + w] = m;
       }
@@ -325,7 +326,7 @@ __global__ void __launch_bounds__(kCullRecThreads) cull_records_kernel(StagePara
     __syncthreads();
     // Warp k: exclusive prefix of cache k's word popcounts, then its run of
     // the pair list (one atomic per cache).
-    if (warp < kCullRecCaches && c0 + warp < n_caches) {
+    if (warp < K && c0 + warp < n_caches) {
       const int k = warp;
       const uint32_t c = c0 + k;
       const int per = (W + 31) >> 5;
@@ -356,7 +357,7 @@ __global__ void __launch_bounds__(kCullRecThreads) cull_records_kernel(StagePara
       }
     }
     __syncthreads();
-    const int nk = (int)min((uint32_t)kCullRecCaches, n_caches - c0);
+    const int nk = (int)min((uint32_t)K, n_caches - c0);
     const uint32_t below = (1u << lane) - 1u;
     for (int k = 0; k < nk; ++k) {
       const uint32_t base = s_base[k], c = c0 + k;
@@ -570,20 +571,20 @@ __device__ __forceinline__ float warp_transpose_reduce(float (&v)[32], int lane)
   return v[0];
 }
 
-constexpr int kGatherThreads = 256;
-constexpr int kGatherWarps = kGatherThreads / 32;
+constexpr int kGatherThreads = 256;  // default threads per cache
 
 // CTA per cache: SH gather of the cache's pairs with their shadowing.
 // Three CTAs per SM fit the FP32 instances without spilling (30.7 -> 26.6 us
 // at 1080p / 4096 VPLs); the BF16 instances, with Kahan sums, spill there
 // and keep two (32.8 us against 36.3).
-template <int NK, bool BF16>
-__global__ void __launch_bounds__(kGatherThreads, BF16 ? 2 : 3) gather_kernel(StageParams p, PairList L) {
+template <int NK, bool BF16, int THREADS>
+__global__ void __launch_bounds__(THREADS, (BF16 ? 2 : 3) * 256 / THREADS) gather_kernel(StageParams p, PairList L) {
+  constexpr int kGatherWarps = THREADS / 32;
   pdl_wait_and_release();
   constexpr bool KAHAN = BF16;  // FP32 accumulation of BF16-stored results, compensated
   __shared__ float s_red[kGatherWarps][NK * 3];
   __shared__ uint32_t s_count[kGatherWarps];  // list-full path: contributing blocks per warp
-  __shared__ int s_block[kGatherThreads];     // list-full path: this chunk's contributing blocks
+  __shared__ int s_block[THREADS];     // list-full path: this chunk's contributing blocks
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t n_caches = cache_count(p);
   for (uint32_t c = blockIdx.x; c < n_caches; c += gridDim.x) {
@@ -594,18 +595,18 @@ __global__ void __launch_bounds__(kGatherThreads, BF16 ? 2 : 3) gather_kernel(St
     for (int k = 0; k < NK * 3; ++k) acc[k] = comp[k] = 0.0f;
     const uint32_t first = L.info[2 * c], count = L.info[2 * c + 1];
     if (count != kPairOverflow) {
-      for (uint32_t j = threadIdx.x; j < count; j += kGatherThreads) {
+      for (uint32_t j = threadIdx.x; j < count; j += THREADS) {
         const uint32_t i = first + j;
         gather_block<NK, BF16, KAHAN>(p, acc, comp, (int)L.block[i], cx, cy, cz, L.shadow[i]);
       }
     } else {
       // The list was full: trace this cache's cones here. The k-th
-      // contributing block goes to thread k mod kGatherThreads, as the k-th
+      // contributing block goes to thread k mod THREADS, as the k-th
       // listed pair does above, so every thread sums the same pairs in the
       // same order and the result is the same either way (to FP32 rounding:
       // the cone is inlined here and in cone_kernel).
       uint32_t before = 0;  // contributing blocks in earlier chunks
-      for (int b0 = 0; b0 < p.total_blocks; b0 += kGatherThreads) {
+      for (int b0 = 0; b0 < p.total_blocks; b0 += THREADS) {
         const int b = b0 + threadIdx.x;
         const bool live = b < p.total_blocks && block_live<BF16>(p, b, cx, cy, cz);
         const uint32_t m = __ballot_sync(0xffffffffu, live);
@@ -619,7 +620,7 @@ __global__ void __launch_bounds__(kGatherThreads, BF16 ? 2 : 3) gather_kernel(St
         }
         if (live) s_block[rank] = b;
         __syncthreads();
-        const uint32_t i = (uint32_t)(threadIdx.x + kGatherThreads - before % kGatherThreads) % kGatherThreads;
+        const uint32_t i = (uint32_t)(threadIdx.x + THREADS - before % THREADS) % THREADS;
         if (i < n) {
           const int bb = s_block[i];
           gather_block<NK, BF16, KAHAN>(p, acc, comp, bb, cx, cy, cz, block_cone(p, bb, cx, cy, cz));
@@ -779,6 +780,18 @@ cudaError_t launch_persistent_after(void (*kernel)(KArgs...), int threads, size_
   return launch_after(kernel, num_sms * per_sm, threads, smem, s, args...);
 }
 
+// The record cull's instance for one-VPL blocks (unit), records copied from
+// the extraction (copy) and K caches per pass (2, 4 or 8).
+template <bool BF16>
+void (*cull_kernel_for(bool unit, bool copy, int K))(StageParams, PairList, int) {
+#define DRV_CULL_K(U, CP)                                                   \
+  (K == 2 ? cull_records_kernel<BF16, U, CP, 2>                             \
+          : (K == 8 ? cull_records_kernel<BF16, U, CP, 8> : cull_records_kernel<BF16, U, CP, 4>))
+  if (unit) return copy ? DRV_CULL_K(true, true) : DRV_CULL_K(true, false);
+  return copy ? DRV_CULL_K(false, true) : DRV_CULL_K(false, false);
+#undef DRV_CULL_K
+}
+
 // Raises a kernel's dynamic shared-memory limit, once per (kernel, device).
 cudaError_t set_max_smem(const void* kernel, size_t bytes) {
   struct Done {
@@ -805,8 +818,9 @@ cudaError_t set_max_smem(const void* kernel, size_t bytes) {
 // elapsed(events[k], events[k + 1]).
 template <int NK, bool BF16>
 cudaError_t split_variant(cudaStream_t s, const StageParams& p, const PairList& L, const SurrogateArgs& sur,
-                          int cone_ctas, int gather_ctas, int num_sms, bool count_reads, cudaEvent_t* ev,
-                          cudaEvent_t voxels_ready) {
+                          const SplitKnobs& knobs, int num_sms, cudaEvent_t* ev, cudaEvent_t voxels_ready) {
+  const int cone_ctas = knobs.cone_ctas_per_sm;
+  const bool count_reads = knobs.count_voxel_reads;
   // Only the cone pass and the surrogate's features read the voxels: with
   // voxels_ready, the cull and the ordering passes overlap the voxel build.
   auto wait_voxels = [&]() { return voxels_ready ? cudaStreamWaitEvent(s, voxels_ready, 0) : cudaSuccess; };
@@ -816,15 +830,15 @@ cudaError_t split_variant(cudaStream_t s, const StageParams& p, const PairList& 
   int total_vpls = 0;
   for (int l = 0; l < p.ll.n_lights; ++l) total_vpls += p.ll.lights[l].n_vpls;
   const int words = (p.total_blocks + 31) >> 5;
-  const size_t rec_smem = cull_records_smem(total_vpls, words);
+  const int K = knobs.cull_caches_per_pass;
+  const size_t rec_smem = cull_records_smem(total_vpls, words, K);
   if (rec_smem <= kCullRecMaxSmem) {
     bool unit = true, copy = true;
     for (int l = 0; l < p.ll.n_lights; ++l) {
       unit = unit && p.ll.lights[l].interval == 1;
       copy = copy && p.ll.lights[l].records != nullptr;
     }
-    auto kernel = unit ? (copy ? cull_records_kernel<BF16, true, true> : cull_records_kernel<BF16, true, false>)
-                       : (copy ? cull_records_kernel<BF16, false, true> : cull_records_kernel<BF16, false, false>);
+    auto kernel = cull_kernel_for<BF16>(unit, copy, K);
     if ((e = set_max_smem(reinterpret_cast<const void*>(kernel), kCullRecMaxSmem)) != cudaSuccess) return e;
     e = launch_persistent(kernel, kCullRecThreads, rec_smem, s, num_sms, p, L, total_vpls);
   } else {
@@ -853,9 +867,11 @@ cudaError_t split_variant(cudaStream_t s, const StageParams& p, const PairList& 
                     : launch_grid(cone_kernel<BF16, true>, 128, 0, s, num_sms, cone_ctas, true, p, L);
   }
   if (e != cudaSuccess || (e = mark(DRV_LK_GATHER)) != cudaSuccess) return e;
-  if ((e = launch_grid(gather_kernel<NK, BF16>, kGatherThreads, 0, s, num_sms, gather_ctas, true, p, L)) !=
-      cudaSuccess)
-    return e;
+  if (knobs.gather_threads == 128)
+    e = launch_grid(gather_kernel<NK, BF16, 128>, 128, 0, s, num_sms, knobs.gather_ctas_per_sm, true, p, L);
+  else
+    e = launch_grid(gather_kernel<NK, BF16, 256>, 256, 0, s, num_sms, knobs.gather_ctas_per_sm, true, p, L);
+  if (e != cudaSuccess) return e;
   return mark(DRV_LK_COUNT);
 }
 
@@ -914,17 +930,16 @@ bool light_split_supported(const DrvConfig& cfg, const LightLaunch& ll) {
 cudaError_t launch_light_split(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const LightLaunch& ll,
                                const DrvCacheCounter* counter, void* entries, uint32_t entry_stride,
                                const VoxelInputs& vox, const PairList& pairs, const SurrogateArgs& sur,
-                               uint32_t* err, int cone_ctas_per_sm, int gather_ctas_per_sm, int num_sms,
-                               bool count_reads, cudaEvent_t* events, cudaEvent_t voxels_ready) {
+                               uint32_t* err, const SplitKnobs& knobs, int num_sms, cudaEvent_t* events,
+                               cudaEvent_t voxels_ready) {
   StageParams p = make_stage_params(cfg, vol, ll, counter, entries, entry_stride, vox);
   p.err = err;
   const bool bf16 = cfg.precision == DRV_PRECISION_BF16;
-  const int cc = cone_ctas_per_sm, gc = gather_ctas_per_sm;
   if (cfg.sh_order == 2)
-    return bf16 ? split_variant<9, true>(s, p, pairs, sur, cc, gc, num_sms, count_reads, events, voxels_ready)
-                : split_variant<9, false>(s, p, pairs, sur, cc, gc, num_sms, count_reads, events, voxels_ready);
-  return bf16 ? split_variant<4, true>(s, p, pairs, sur, cc, gc, num_sms, count_reads, events, voxels_ready)
-              : split_variant<4, false>(s, p, pairs, sur, cc, gc, num_sms, count_reads, events, voxels_ready);
+    return bf16 ? split_variant<9, true>(s, p, pairs, sur, knobs, num_sms, events, voxels_ready)
+                : split_variant<9, false>(s, p, pairs, sur, knobs, num_sms, events, voxels_ready);
+  return bf16 ? split_variant<4, true>(s, p, pairs, sur, knobs, num_sms, events, voxels_ready)
+              : split_variant<4, false>(s, p, pairs, sur, knobs, num_sms, events, voxels_ready);
 }
 
 }  // namespace drv

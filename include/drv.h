@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define DRV_ABI_VERSION 6
+#define DRV_ABI_VERSION 7
 #define DRV_MAX_CASCADES 4   /* MAX_NUM_ADDRESS_VOLUME_CASCADES, globalubos.glsl:43 */
 #define DRV_MAX_LIGHTS 16    /* maxExpectedLights, renderer.cpp:80 */
 #define DRV_LIGHTING_THREADS_PER_GROUP 64 /* lightcache.glsl:95 */
@@ -575,6 +575,9 @@ typedef struct DrvTuning {
                                   normals and albedo) for NaN / Inf; one found is reported once, as
                                   DRV_ERR_NUMERIC, by the next drv_sync (DRV_DEVERR_NUMERIC). A debugging
                                   aid: it reads every input once more */
+  int32_t cull_caches_per_pass; /* split stage: caches the cull tests per pass against the VPL records staged
+                                   in shared memory (the cull's tile: 2, 4 or 8; 0: 4) */
+  int32_t gather_threads;      /* split stage: threads per cache of the gather (128 or 256; 0: 256) */
 } DrvTuning;
 enum { DRV_LIGHT_PATH_AUTO = 0, DRV_LIGHT_PATH_SINGLE = 1, DRV_LIGHT_PATH_SPLIT = 2 };
 drv_status drv_set_tuning(DrvContext* ctx, const DrvTuning* tuning);

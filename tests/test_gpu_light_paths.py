@@ -147,3 +147,21 @@ def test_load_bandwidth_probe(cuda, lib):
     assert lib.drv_measure_load_bandwidth(1, C.c_void_p(buf.data_ptr()), 1024, 10, s,
                                           C.byref(g)) == abi.ERR_INVALID_ARG
     assert int(buf.abs().sum()) == 0  # never written
+
+
+@pytest.mark.parametrize("w", [pipeline.WORKLOADS["c1_small"], REDUCED], ids=["c1", "c2r"])
+def test_tile_knobs_keep_the_result(w, cuda, lib):
+    """The cull's caches per pass only change which caches share a pass (each
+    cache's pair run stays in block order): the SH are the same bit for bit.
+    A 128-thread gather sums each cache's pairs in another order: the same
+    to FP32 rounding."""
+    p0, pos0, sh0 = _lit(w, 13, light_path=abi.LIGHT_PATH_SPLIT)
+    for k in (2, 8):
+        p1, pos1, sh1 = _lit(w, 13, light_path=abi.LIGHT_PATH_SPLIT, cull_caches_per_pass=k)
+        assert np.array_equal(pos1, pos0) and np.array_equal(sh1, sh0)
+        p1.close()
+    p2, pos2, sh2 = _lit(w, 13, light_path=abi.LIGHT_PATH_SPLIT, gather_threads=128)
+    assert np.array_equal(pos2, pos0)
+    assert rel_l2(sh2, sh0) < 1e-6
+    p2.close()
+    p0.close()
