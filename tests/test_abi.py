@@ -166,3 +166,16 @@ def test_oracle_host_frame_equals_product_host_frame(lib, oracle, name):
     assert bytes(a.lights) == bytes(b.lights)
     assert all(bytes(x) == bytes(y) for x, y in zip(a.light_descs, b.light_descs))
     assert bytes(a.volume) == bytes(b.volume)
+
+
+def test_missing_library_is_not_supported_not_a_fallback(tmp_path):
+    """Without the built library every entry point raises DRV_ERR_NOT_SUPPORTED
+    (there is no CPU fallback)."""
+    import subprocess
+    import sys
+    code = ("import dynamicradiancevolume_gb300 as d, pathlib\n"
+            "d.LIB_PATH = pathlib.Path(r'%s') / 'libdrv_gb300.so'\n"
+            "try:\n    d.load()\nexcept d.DrvError as e:\n    print('status', e.status)\n" % tmp_path)
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True,
+                       cwd=str(drv.HEADER.parents[1]))
+    assert f"status {abi.ERR_NOT_SUPPORTED}" in r.stdout, r.stdout + r.stderr
