@@ -140,7 +140,8 @@ class DrvTuning(C.Structure):
                 ("gather_ctas_per_sm", C.c_int32), ("time_kernels", C.c_int32),
                 ("plain_voxel_reads", C.c_int32), ("surrogate_wait_test", C.c_int32),
                 ("count_voxel_reads", C.c_int32), ("check_inputs", C.c_int32),
-                ("cull_caches_per_pass", C.c_int32), ("gather_threads", C.c_int32)]
+                ("cull_caches_per_pass", C.c_int32), ("gather_threads", C.c_int32),
+                ("scalar_apply", C.c_int32)]
 
 
 LIGHT_KERNELS = ("cull", "classify", "scatter", "mlp", "cone", "gather")

@@ -763,7 +763,8 @@ drv_status drv_apply(DrvContext* ctx, const DrvGBufferView* g, const DrvPerFrame
                                               ctx->input_err()));
   return cuda_check(ctx, drv::launch_apply(ctx->s(), ctx->cfg, *vol, *f, *g, ctx->atlas, ctx->entries,
                                            ctx->entry_stride, ctx->counter, out_rgb, ctx->srgb,
-                                           ctx->spec_env ? &sv : nullptr, ctx->scratch_words + 1),
+                                           ctx->spec_env ? &sv : nullptr, ctx->scratch_words + 1,
+                                           ctx->tuning.scalar_apply != 0),
                     "apply");
 }
 

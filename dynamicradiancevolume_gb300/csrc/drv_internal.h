@@ -294,10 +294,12 @@ cudaError_t launch_bruteforce_rsm(cudaStream_t s, const DrvPerFrame& f, const Dr
                                   const float* srgb);
 // spec: the envmap atlas when specular is on, else nullptr.
 // err: device error word (DRV_DEVERR_BOUNDS for an atlas slot past the count).
+// scalar: BF16 entries evaluated per pixel on the FP32 pipes instead of on the
+// tensor cores (DrvTuning.scalar_apply).
 cudaError_t launch_apply(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const DrvPerFrame& f,
                          const DrvGBufferView& g, const uint32_t* atlas, const void* entries, uint32_t entry_stride,
                          const DrvCacheCounter* counter, float* out_rgb, const float* srgb,
-                         const SpecView* spec = nullptr, uint32_t* err = nullptr);
+                         const SpecView* spec = nullptr, uint32_t* err = nullptr, bool scalar = false);
 // Sets DRV_DEVERR_NUMERIC in *word when any of n values (float, or half when
 // half is nonzero) is NaN or infinite.
 cudaError_t launch_scan_finite(cudaStream_t s, const void* data, size_t n, int half, uint32_t* word);

@@ -320,12 +320,231 @@ __global__ void __launch_bounds__(256, SPEC ? 3 : 5) apply_kernel(ApplyParams p)
   store_output(p, i, col);
 }
 
+// ---------------------------------------------------------- tensor-core form
+// BF16 entries without specular: the 8 corners' irradiance of a whole warp of
+// pixels on the tensor cores. E_ch(pixel, corner) = sum_k F_k(n) SH_k,ch
+// (SampleCacheIrradiance, lightcache.glsl:137-179, with the signs of its terms
+// folded into F) is a product of a [pixels x 9] matrix of per-pixel factors and
+// a [9 x corners] matrix of one cell's SH per channel. The warp (a 16 x 2 pixel
+// tile) groups its pixels by cell (cascade and base corner; almost always one
+// or two groups); per group, lane (g, t) loads corner g's BF16 entry as the B
+// fragment, and mma.sync m16n8k16 (BF16 operands, FP32 accumulation) gives
+// every pixel's 8 corner irradiances for each channel. F is split into BF16
+// hi + lo parts (two MMAs), so the products keep about 16 bits of F; the SH
+// values are the stored BF16 ones exactly. The clamp at zero, the trilinear
+// weights and the sum over corners follow on the accumulators (quad shuffles).
+// The sum's order differs from the per-pixel form's (FP32 rounding).
+constexpr int kTcRow = 24;  // BF16 values per shared-memory row: 16 used + 8 pad (conflict-free ldmatrix)
+
+__device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], uint32_t addr) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(addr));
+}
+
+__device__ __forceinline__ void mma_bf16_16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+template <bool SH2>
+__global__ void __launch_bounds__(256, 3) apply_tc_kernel(ApplyParams p) {
+  constexpr int NK = SH2 ? 9 : 4;
+  __shared__ __align__(16) uint16_t s_f[8][2][32 * kTcRow];  // per warp: F hi rows, F lo rows
+  const int tid = threadIdx.y * 16 + threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int x = blockIdx.x * 16 + threadIdx.x, y = blockIdx.y * 16 + threadIdx.y;
+  const bool inside = x < p.w && y < p.h;
+  const size_t i = inside ? (size_t)y * p.w + x : 0;
+  const float d = inside ? __ldcs(p.depth + i) : 0.0f;
+  // cacheApply.frag:304-307 (discard); a NaN depth counts as no geometry.
+  const bool geom = inside && d >= 0.00001f;
+  f3 n = mkf3(0.0f, 0.0f, 1.0f), alb = mkf3(0.0f, 0.0f, 0.0f);
+  float wp[3] = {0.0f, 0.0f, 0.0f};
+  int c = 0;
+  if (geom) {
+    if (p.normal_format == DRV_NORMAL_RG16I) {
+      const int q = __ldcs(reinterpret_cast<const int*>(p.normal) + i);
+      n = unpack_normal16i((int16_t)(q & 0xFFFF), (int16_t)(q >> 16));
+    } else {
+      const float* q = reinterpret_cast<const float*>(p.normal) + 3 * i;
+      n = mkf3(__ldcs(q), __ldcs(q + 1), __ldcs(q + 2));
+    }
+    const float inv_pi = 1.0f / DRV_SHADER_PI;
+    const f3 a = load_albedo(p.albedo, p.albedo_format, p.srgb, i);
+    alb = mkf3(a.x * inv_pi, a.y * inv_pi, a.z * inv_pi);
+    reconstruct_world(p.frame, x, y, p.w, p.h, d, wp);
+    c = select_cascade(p.vol, p.n_cascades, wp);
+  }
+  // Per-normal factors of SampleCacheIrradiance, signs folded in (0 without geometry).
+  float F[16];
+  {
+    const float f1y = p.cl[1] * n.y, f1z = p.cl[1] * n.z, f1x = p.cl[1] * n.x;
+    F[0] = p.cl[0];
+    F[1] = -f1y;
+    F[2] = f1z;
+    F[3] = -f1x;
+    F[4] = -(p.cl[2] * n.x * n.y);
+    F[5] = p.cl[2] * n.y * n.z;
+    F[6] = p.cl[3] * (n.z * n.z * 3.0f - 1.0f);
+    F[7] = p.cl[2] * n.x * n.z;
+    F[8] = p.cl[4] * (n.x * n.x - n.y * n.y);
+#pragma unroll
+    for (int k = 0; k < 16; ++k)
+      if (k >= NK || !geom) F[k] = 0.0f;
+  }
+  {
+    uint32_t hi[8], lo[8];
+#pragma unroll
+    for (int k = 0; k < 16; k += 2) {
+      const uint16_t h0 = to_bf16(F[k]), h1 = to_bf16(F[k + 1]);
+      const uint16_t l0 = to_bf16(F[k] - from_bf16(h0)), l1 = to_bf16(F[k + 1] - from_bf16(h1));
+      hi[k / 2] = (uint32_t)h0 | (uint32_t)h1 << 16;
+      lo[k / 2] = (uint32_t)l0 | (uint32_t)l1 << 16;
+    }
+    uint4* rh = reinterpret_cast<uint4*>(s_f[warp][0] + lane * kTcRow);
+    uint4* rl = reinterpret_cast<uint4*>(s_f[warp][1] + lane * kTcRow);
+    rh[0] = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+    rh[1] = make_uint4(hi[4], hi[5], hi[6], hi[7]);
+    rl[0] = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+    rl[1] = make_uint4(lo[4], lo[5], lo[6], lo[7]);
+  }
+  __syncwarp();
+  // A fragments of the two 16-pixel halves of the warp, hi and lo.
+  uint32_t ah[2][4], al[2][4];
+#pragma unroll
+  for (int m = 0; m < 2; ++m) {
+    const int row = 16 * m + (lane & 7) + ((lane >> 3) & 1) * 8, col = ((lane >> 4) & 1) * 8;
+    ldsm_x4(ah[m], (uint32_t)__cvta_generic_to_shared(s_f[warp][0] + row * kTcRow + col));
+    ldsm_x4(al[m], (uint32_t)__cvta_generic_to_shared(s_f[warp][1] + row * kTcRow + col));
+  }
+  const uint32_t n_caches = min((uint32_t)max(p.counter->total_light_cache_count, 0), p.max_caches);
+  const int g = lane >> 2, t = lane & 3;
+  const int aw = p.n_cascades * p.res;
+  float tmix = 0.0f;
+  bool in_tr = false;
+  if (geom && p.transitions) {
+    tmix = cascade_transition(p.vol, p.rc, c, wp);
+    in_tr = tmix > 0.0f && c < p.n_cascades - 1;
+  }
+  f3 col = mkf3(0.0f, 0.0f, 0.0f);
+  for (int call = 0; call < 2; ++call) {
+    const bool part = geom && (call == 0 || in_tr);
+    if (call == 1 && !__any_sync(0xffffffffu, part)) break;
+    const int cc = c + call;
+    // The pixel's cell in cascade cc and its trilinear fractions.
+    int a0[3] = {0, 0, 0};
+    float fr[3] = {0.0f, 0.0f, 0.0f};
+    if (part) {
+      const DrvCascade& k = p.vol.cascades[cc];
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const float a = div_exact(__fsub_rn(wp[j], k.min[j]), k.world_voxel_size, p.rc.inv_cell[cc]);
+        a0[j] = __float2int_rz(fminf(fmaxf(a, -1e9f), 1e9f));
+        fr[j] = a - (float)a0[j];
+      }
+    }
+    const unsigned long long key =
+        part ? ((unsigned long long)(uint32_t)cc << 60) | ((unsigned long long)((uint32_t)a0[0] & 0xFFFFFu) << 40) |
+                   ((unsigned long long)((uint32_t)a0[1] & 0xFFFFFu) << 20) | (unsigned long long)((uint32_t)a0[2] & 0xFFFFFu)
+             : ~0ull;
+    f3 irr = mkf3(0.0f, 0.0f, 0.0f);
+    uint32_t remaining = __ballot_sync(0xffffffffu, part);
+    while (remaining) {
+      const int leader = __ffs(remaining) - 1;
+      const unsigned long long gk = __shfl_sync(0xffffffffu, key, leader);
+      const bool member = part && key == gk;
+      remaining &= ~__ballot_sync(0xffffffffu, member);
+      // Corner g of the group's cell (x fastest, cacheApply.frag:219-230).
+      const int gc = __shfl_sync(0xffffffffu, cc, leader);
+      const int gx = __shfl_sync(0xffffffffu, a0[0], leader) + (g & 1) + p.res * gc;
+      const int gy = __shfl_sync(0xffffffffu, a0[1], leader) + ((g >> 1) & 1);
+      const int gz = __shfl_sync(0xffffffffu, a0[2], leader) + (g >> 2);
+      const bool inside_atlas = gx >= 0 && gx < aw && gy >= 0 && gy < p.res && gz >= 0 && gz < p.res;
+      const uint32_t slot = inside_atlas ? __ldg(p.atlas + ((size_t)gz * p.res + gy) * aw + gx) : 0u;
+      const bool live = slot != 0u && slot <= n_caches;
+      if (slot > n_caches && slot != 0xFFFFFFFFu && p.err && t == 0) raise_error(p.err, DRV_DEVERR_BOUNDS);
+      // B fragments: rows k = 2t, 2t + 1 (and 8 for t = 0), column g.
+      uint32_t b0[3] = {0u, 0u, 0u}, b1[3] = {0u, 0u, 0u};
+      if (live) {
+        const uint16_t* sh = reinterpret_cast<const uint16_t*>(p.entries + (size_t)(slot - 1u) * p.stride_floats) + 2;
+        const int k0 = 2 * t, k1 = 2 * t + 1;
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) {
+          const uint32_t v0 = k0 < NK ? __ldg(sh + 3 * k0 + ch) : 0u, v1 = k1 < NK ? __ldg(sh + 3 * k1 + ch) : 0u;
+          b0[ch] = v0 | v1 << 16;
+          b1[ch] = (SH2 && t == 0) ? (uint32_t)__ldg(sh + 24 + ch) : 0u;
+        }
+      }
+      // Accumulators: lane (g, t) holds pixels 16m + g (+ 8) at corners 2t, 2t + 1.
+      float part_sum[2][2][3];
+#pragma unroll
+      for (int m = 0; m < 2; ++m) {
+        float dv[3][4];
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) {
+          dv[ch][0] = dv[ch][1] = dv[ch][2] = dv[ch][3] = 0.0f;
+          mma_bf16_16816(dv[ch], ah[m], b0[ch], b1[ch]);
+          mma_bf16_16816(dv[ch], al[m], b0[ch], b1[ch]);
+        }
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int r = 16 * m + g + 8 * h;
+          const float fx = __shfl_sync(0xffffffffu, fr[0], r), fy = __shfl_sync(0xffffffffu, fr[1], r),
+                      fz = __shfl_sync(0xffffffffu, fr[2], r);
+          const float wyz = ((t & 1) ? fy : 1.0f - fy) * ((t >> 1) ? fz : 1.0f - fz);
+          const float w0 = (1.0f - fx) * wyz, w1 = fx * wyz;
+#pragma unroll
+          for (int ch = 0; ch < 3; ++ch)
+            part_sum[m][h][ch] = fmaxf(dv[ch][2 * h], 0.0f) * w0 + fmaxf(dv[ch][2 * h + 1], 0.0f) * w1;
+        }
+      }
+      // Sum over the quad's corners, then each pixel takes its own sums.
+#pragma unroll
+      for (int m = 0; m < 2; ++m)
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+#pragma unroll
+          for (int ch = 0; ch < 3; ++ch) {
+            float v = part_sum[m][h][ch];
+            v += __shfl_xor_sync(0xffffffffu, v, 1);
+            v += __shfl_xor_sync(0xffffffffu, v, 2);
+            part_sum[m][h][ch] = v;
+          }
+      const int src = 4 * (lane & 7), mm = lane >> 4, hh = (lane >> 3) & 1;
+      float mine[3];
+#pragma unroll
+      for (int ch = 0; ch < 3; ++ch) {
+        const float v00 = __shfl_sync(0xffffffffu, part_sum[0][0][ch], src);
+        const float v01 = __shfl_sync(0xffffffffu, part_sum[0][1][ch], src);
+        const float v10 = __shfl_sync(0xffffffffu, part_sum[1][0][ch], src);
+        const float v11 = __shfl_sync(0xffffffffu, part_sum[1][1][ch], src);
+        mine[ch] = mm ? (hh ? v11 : v10) : (hh ? v01 : v00);
+      }
+      if (member) irr = mkf3(mine[0], mine[1], mine[2]);
+    }
+    const f3 cc_col = mkf3(irr.x * alb.x, irr.y * alb.y, irr.z * alb.z);
+    if (call == 0)
+      col = cc_col;
+    else if (in_tr)
+      col = col * (1.0f - tmix) + cc_col * tmix;  // mix(), cacheApply.frag:359
+  }
+  if (!inside) return;
+  if (!geom) {
+    if (!p.out_add) store_output(p, i, mkf3(0.0f, 0.0f, 0.0f));
+    return;
+  }
+  store_output(p, i, col);
+}
+
 }  // namespace
 
 cudaError_t launch_apply(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const DrvPerFrame& f,
                          const DrvGBufferView& g, const uint32_t* atlas, const void* entries, uint32_t entry_stride,
                          const DrvCacheCounter* counter, float* out_rgb, const float* srgb, const SpecView* spec,
-                         uint32_t* err) {
+                         uint32_t* err, bool scalar) {
   ApplyParams p{};
   p.err = err;
   p.rc = make_cell_recip(vol);
@@ -371,7 +590,9 @@ cudaError_t launch_apply(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeIn
             : apply_kernel<false, false, true><<<grid, block, 0, s>>>(p);
     return cudaGetLastError();
   }
-  if (p.bf16)
+  if (p.bf16 && !scalar)
+    p.sh2 ? apply_tc_kernel<true><<<grid, block, 0, s>>>(p) : apply_tc_kernel<false><<<grid, block, 0, s>>>(p);
+  else if (p.bf16)
     p.sh2 ? apply_kernel<true, true, false><<<grid, block, 0, s>>>(p)
           : apply_kernel<true, false, false><<<grid, block, 0, s>>>(p);
   else

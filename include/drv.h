@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define DRV_ABI_VERSION 7
+#define DRV_ABI_VERSION 8
 #define DRV_MAX_CASCADES 4   /* MAX_NUM_ADDRESS_VOLUME_CASCADES, globalubos.glsl:43 */
 #define DRV_MAX_LIGHTS 16    /* maxExpectedLights, renderer.cpp:80 */
 #define DRV_LIGHTING_THREADS_PER_GROUP 64 /* lightcache.glsl:95 */
@@ -578,6 +578,9 @@ typedef struct DrvTuning {
   int32_t cull_caches_per_pass; /* split stage: caches the cull tests per pass against the VPL records staged
                                    in shared memory (the cull's tile: 2, 4 or 8; 0: 4) */
   int32_t gather_threads;      /* split stage: threads per cache of the gather (128 or 256; 0: 256) */
+  int32_t scalar_apply;        /* nonzero: with BF16 entries (no specular) the apply evaluates each corner's
+                                  SH per pixel on the FP32 pipes instead of a warp's cells on the tensor
+                                  cores; the same result to FP32 rounding */
 } DrvTuning;
 enum { DRV_LIGHT_PATH_AUTO = 0, DRV_LIGHT_PATH_SINGLE = 1, DRV_LIGHT_PATH_SPLIT = 2 };
 drv_status drv_set_tuning(DrvContext* ctx, const DrvTuning* tuning);
