@@ -2,17 +2,19 @@
 """Benchmark: caches lit/s and ms/frame of the per-frame indirect-lighting
 path at 1080p with 4096 VPLs (the production workload with one spot light).
 
-A step is one frame of the path over inputs already resident in HBM
-(G-buffer + RSM): RSM mips + VPL extraction, voxelization + opacity mips,
-cache allocation, cache lighting (SH gather + cone-traced shadow), apply.
-`value` = caches lit per second of frame time (whole frame, all ranks);
-`e2e` = the same through the C-ABI call with host buffers, the H2D copy of
-the inputs and the D2H copy of the radiance inside the timed region.
+A step is the cache-lighting stage (SH gather of every VPL into every cache
+with a cone-traced shadow per pair) over one frame's VPLs, voxel pyramid and
+caches, resident in HBM; `value` = caches lit per second of that stage (all
+ranks) and `ms_per_frame` = the whole frame (RSM mips + VPL extraction,
+voxelization + opacity mips, cache allocation, cache lighting, apply).
+`e2e` = caches lit per second of whole frames through the C-ABI calls with
+host buffers in the reference's render-target formats, the H2D copy of the
+G-buffer and RSM and the D2H copy of the radiance inside the timed region.
 
 --impl reference times the reference's CPU implementation of the path: the
 reference itself is GLSL inside an OpenGL 4.5 Windows application that cannot
 run here (no graphics stack), so its CPU arm is the FP64 restatement of its
-shader math, on all host cores.
+shader math, on all host cores, with the product library never loaded.
 
 Multi-GPU: replicas only (each rank renders its own frame; no collective on
 the data path); `value` sums the ranks' caches over the max of their times.
@@ -35,10 +37,10 @@ sys.path.insert(0, str(ROOT))
 METRIC = "caches lit/s and ms/frame at 1080p: plain vs surrogate, at ≤1% rel-L2 vs FP64"
 UNIT = "caches/s"
 
-# DRAM bytes (read + write) per launch of the light stage's top kernels at
-# ns_1080p_4096, from one `ncu --set full --clock-control none` capture each
+# DRAM bytes (read + write) per launch of the light stage's top kernel at
+# ns_1080p_4096, from one `ncu --set full --clock-control none` capture
 # (cold caches) of `bench.py --steps 1 --warmup 1` at that workload.
-NCU_TRAFFIC = {"cone_kernel": 12_660_736, "mlp_kernel": 7_976_192}
+NCU_TRAFFIC = {"cone_kernel": 12_660_736}
 
 
 def parse():
@@ -477,6 +479,12 @@ def measure_workload(w, args, dev, flush, rank, weights, features, full: bool) -
         info = {"caches_lit_per_s": count / (light_ms / 1e3), "light_ms": light_ms, "frame_ms": graph_ms,
                 "live_pairs": pipe.light_pairs(), "frame_ms_stream": frame_ms, "stage_ms": stage_ms,
                 "caches": count, "caches_per_s_of_frame": count / (graph_ms / 1e3)}
+        if w.n_lights > 1:
+            # the reference's form: one lighting pass per light, each adding
+            # into the entries (renderer.cpp:924-932)
+            pipe.set_tuning(per_light_dispatch=1)
+            info["light_ms_per_light_dispatch"] = measure_light_graph(pipe, args.steps, args.warmup, flush)
+            pipe.set_tuning(per_light_dispatch=0)
         if thr is not None:
             ev, fb = C.c_uint32(), C.c_uint32()
             pipe.lib.drv_get_surrogate_stats(pipe.ctx, C.byref(ev), C.byref(fb))
@@ -789,9 +797,11 @@ def run_ours(args):
     if batch is not None:
         # config 5: many seeded scenes of uneven sizes, BF16 storage, surrogate
         # visibility; one CUDA-graph launch against the scenes one by one (each
-        # scene's frame alone, as the reference renders one scene per Renderer)
+        # scene's frame alone as a graph) and against the reference's form
+        # (each scene alone, host-issued kernels, one lighting pass per light)
         line["batch"] = {k: batch[k] for k in ("scenes", "precision", "visibility", "threshold", "sizes", "tuned",
-                                               "batch", "one_by_one", "speedup")}
+                                               "batch", "one_by_one", "reference_form", "speedup",
+                                               "speedup_vs_reference_form")}
         line["batch"]["trials"] = len(batch["trials"])
     threads = os.cpu_count() or 1
     if rank == 0 and not args.no_cpu_baseline:

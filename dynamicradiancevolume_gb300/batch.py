@@ -166,6 +166,32 @@ def time_one_by_one(scenes, reps: int, warmup: int = 2):
     return float(lat.sum()), lat
 
 
+def time_reference_form(scenes, reps: int, warmup: int = 2):
+    """The reference's unbatched form: each scene alone, its frame issued
+    kernel by kernel from the host (drv_frame, no graph) with one lighting
+    pass per light (renderer.cpp:899-933, DrvTuning.per_light_dispatch);
+    per-scene latency = its own frame time; total = their sum."""
+    import torch
+    lat = []
+    for s in scenes:
+        p = s.pipe
+        p.set_tuning(per_light_dispatch=1)
+        for _ in range(warmup):
+            p.frame()
+        times = []
+        for _ in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(p.stream)
+            p.frame()
+            b.record(p.stream)
+            b.synchronize()
+            times.append(a.elapsed_time(b))
+        p.set_tuning(per_light_dispatch=0)
+        lat.append(statistics.median(times))
+    lat = np.array(lat)
+    return float(lat.sum()), lat
+
+
 def autotune(scenes, reps: int = 3, streams_menu=(1, 2, 4, 8, 16, 32), knob_menus=None, log=print):
     """Stream count first (default knobs), then each light-stage knob in turn
     over its menu with the others held at their best (coordinate descent);
@@ -210,6 +236,7 @@ def run_batch(n_scenes: int, reps: int, threshold: float = 0.5, fp32_cone: bool 
     tuned, trials = autotune(scenes, reps=tune_reps, log=log)
     batch_ms, batch_lat = time_batch(scenes, tuned["streams"], reps)
     seq_ms, seq_lat = time_one_by_one(scenes, reps)
+    ref_ms, ref_lat = time_reference_form(scenes, reps)
     caches = np.array([s.caches for s in scenes])
     px = np.array([s.pipe.hf.workload.width * s.pipe.hf.workload.height for s in scenes])
     line = {
@@ -228,10 +255,17 @@ def run_batch(n_scenes: int, reps: int, threshold: float = 0.5, fp32_cone: bool 
                        "caches_per_s": float(caches.sum()) / (seq_ms / 1e3),
                        "latency_ms_p50": float(np.percentile(seq_lat, 50)),
                        "latency_ms_p99": float(np.percentile(seq_lat, 99))},
+        "reference_form": {"ms": ref_ms, "scenes_per_s": n_scenes / (ref_ms / 1e3),
+                           "caches_per_s": float(caches.sum()) / (ref_ms / 1e3),
+                           "latency_ms_p50": float(np.percentile(ref_lat, 50)),
+                           "latency_ms_p99": float(np.percentile(ref_lat, 99)),
+                           "form": "each scene alone, drv_frame issued from the host (no graph), "
+                                   "one lighting pass per light"},
         "speedup": seq_ms / batch_ms,
+        "speedup_vs_reference_form": ref_ms / batch_ms,
         "per_scene": [{"pixels": int(px[i]), "voxels": s.pipe.hf.workload.voxel_res, "vpls": s.vpls,
                        "caches": s.caches, "cav_res": s.pipe.hf.workload.cav_res, "alone_ms": float(seq_lat[i]),
-                       "batch_done_ms": float(batch_lat[i])} for i, s in enumerate(scenes)],
+                       "reference_form_ms": float(ref_lat[i]), "batch_done_ms": float(batch_lat[i])} for i, s in enumerate(scenes)],
         "trials": trials,
         "setup_s": setup_s,
     }

@@ -704,6 +704,24 @@ drv_status light_caches(DrvContext* ctx, const DrvSpotLight* lights, int32_t n_l
       sur.err = ctx->scratch_words + 1;
       sur.hold_commit = ctx->tuning.surrogate_wait_test;
     }
+    if (ctx->tuning.per_light_dispatch && ll.n_lights > 1) {
+      // One split stage per light, each adding its SH into the entries (the
+      // reference's dispatch loop); the voxel wait is taken once, up front.
+      if (voxels_ready) DRV_TRY_CUDA(ctx, cudaStreamWaitEvent(ctx->s(), voxels_ready, 0));
+      ctx->lk_recorded = false;
+      drv_status st = DRV_OK;
+      for (int l = 0; l < ll.n_lights && st == DRV_OK; ++l) {
+        drv::LightLaunch one{};
+        one.n_lights = 1;
+        one.lights[0] = ll.lights[l];
+        st = cuda_check(ctx, drv::launch_light_split(ctx->s(), ctx->cfg, *vol, one, ctx->counter, ctx->entries,
+                                                     ctx->entry_stride, ctx->light_voxels(), pairs, sur,
+                                                     ctx->scratch_words + 1, knobs, ctx->num_sms, nullptr, nullptr),
+                        "light_caches");
+      }
+      if (st == DRV_OK && ctx->spec_env) st = specular_gather(ctx, ll, vol, frame, nullptr);
+      return st;
+    }
     drv_status st = cuda_check(ctx, drv::launch_light_split(ctx->s(), ctx->cfg, *vol, ll, ctx->counter, ctx->entries,
                                                             ctx->entry_stride, ctx->light_voxels(), pairs, sur,
                                                             ctx->scratch_words + 1, knobs, ctx->num_sms, events,

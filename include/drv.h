@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define DRV_ABI_VERSION 8
+#define DRV_ABI_VERSION 9
 #define DRV_MAX_CASCADES 4   /* MAX_NUM_ADDRESS_VOLUME_CASCADES, globalubos.glsl:43 */
 #define DRV_MAX_LIGHTS 16    /* maxExpectedLights, renderer.cpp:80 */
 #define DRV_LIGHTING_THREADS_PER_GROUP 64 /* lightcache.glsl:95 */
@@ -581,6 +581,12 @@ typedef struct DrvTuning {
   int32_t scalar_apply;        /* nonzero: with BF16 entries (no specular) the apply evaluates each corner's
                                   SH per pixel on the FP32 pipes instead of a warp's cells on the tensor
                                   cores; the same result to FP32 rounding */
+  int32_t per_light_dispatch;  /* nonzero: the split light stage runs once per light, each light's SH added
+                                  into the entries in turn, as the reference dispatches one lighting pass
+                                  per light (renderer.cpp:924-932); the same result to FP32 rounding (BF16
+                                  entries are rounded once per light). Kernel timing is off, the pair and
+                                  surrogate counts are the last light's, and with indirect specular the
+                                  envmaps are gathered after the loop with their own cones */
 } DrvTuning;
 enum { DRV_LIGHT_PATH_AUTO = 0, DRV_LIGHT_PATH_SINGLE = 1, DRV_LIGHT_PATH_SPLIT = 2 };
 drv_status drv_set_tuning(DrvContext* ctx, const DrvTuning* tuning);

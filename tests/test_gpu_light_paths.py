@@ -165,3 +165,22 @@ def test_tile_knobs_keep_the_result(w, cuda, lib):
     assert rel_l2(sh2, sh0) < 1e-6
     p2.close()
     p0.close()
+
+
+@pytest.mark.parametrize("prec", [abi.PRECISION_FP32, abi.PRECISION_BF16], ids=["f32", "bf16"])
+def test_per_light_dispatch_equals_one_pass(prec, cuda, lib):
+    """The reference's dispatch loop (DrvTuning.per_light_dispatch: one split
+    stage per light, each adding into the entries) against one pass over every
+    light's pairs: the same SH to FP32 rounding; BF16 entries are rounded once
+    per light instead of once, so they agree to BF16 rounding."""
+    w = pipeline.scaled(REDUCED, precision=prec)
+    assert w.n_lights > 1
+    p1, pos1, sh1 = _lit(w, 7)
+    p2, pos2, sh2 = _lit(w, 7, per_light_dispatch=1)
+    assert np.array_equal(pos1, pos2)
+    err = rel_l2(sh2, sh1)
+    print("per-light dispatch: rel-L2 %.3e" % err)
+    assert err < (1e-5 if prec == abi.PRECISION_FP32 else 1e-2)
+    assert np.abs(sh1).max() > 0
+    p1.close()
+    p2.close()

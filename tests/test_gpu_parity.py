@@ -25,7 +25,8 @@ def rel_l2(a, b):
 class Run:
     """Runs the GPU stages of one workload and the oracle on the same inputs."""
 
-    def __init__(self, w, oracle, seed=None, normal_format=abi.NORMAL_RG16I, sh2_sign=None, tuning=None):
+    def __init__(self, w, oracle, seed=None, normal_format=abi.NORMAL_RG16I, sh2_sign=None, tuning=None,
+                 surrogate=None):
         import torch
         self.torch = torch
         self.w = w
@@ -33,7 +34,12 @@ class Run:
         self.hf = pipeline.host_frame(w, seed)
         if sh2_sign is not None:
             self.hf.config.sh2_sign = sh2_sign
+        if surrogate is not None:  # (params, feature set, confidence threshold)
+            self.hf.config.surrogate_conf_threshold = surrogate[2]
         self.pipe = pipeline.Pipeline(self.hf, normal_format=normal_format)
+        if surrogate is not None:
+            from dynamicradiancevolume_gb300 import surrogate as sur
+            sur.upload(self.pipe, surrogate[0], surrogate[1])
         self.spec = w.specular_envmap_size > 0
         if self.spec:
             # seeded roughness / metallic (RG8 unorm), as the G-buffer pass writes them

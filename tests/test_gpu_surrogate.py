@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 from dynamicradiancevolume_gb300 import abi, pipeline, surrogate
-from test_gpu_parity import Run, rel_l2
+from test_gpu_parity import Run, oracle_frame, rel_l2
 
 pytestmark = pytest.mark.gpu
 
@@ -277,3 +277,22 @@ def test_bounded_wait_timeout_is_reported_and_context_recovers(frame, oracle):
     assert np.array_equal(pos[a], frame.positions[b])
     assert rel_l2(sh[a], frame.gpu_sh()[b]) < 1e-5
     p.close()
+
+
+@pytest.mark.parametrize("threshold", [0.8, 0.95])
+@pytest.mark.parametrize("seed", [1000, 1001, 1002])
+def test_shipped_surrogate_frame_within_one_percent_of_fp64(seed, threshold, lib, oracle, cuda):
+    """The shipped checkpoint on held-out scenes (seeds no training scene
+    used) at 1080p / 4096 VPLs: the whole frame, the surrogate's visibilities
+    with the low-confidence pairs re-traced, against the FP64 oracle frame
+    with every pair cone-traced, within the 1% relative L2 the configuration
+    allows."""
+    w = pipeline.scaled(pipeline.WORKLOADS["ns_1080p_4096"], name="ns_surrogate",
+                        visibility=abi.VISIBILITY_SURROGATE)
+    r = Run(w, oracle, seed=seed,
+            surrogate=(surrogate.load_params(), surrogate.load_features(), threshold))
+    err = rel_l2(r.out, oracle_frame(r, oracle))
+    print("seed %d threshold %.1f: frame rel-L2 %.4f" % (seed, threshold, err))
+    assert np.isfinite(r.out).all()
+    assert err < 1e-2, err
+    r.pipe.close()
