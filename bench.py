@@ -125,6 +125,10 @@ def dist_env():
     return ws, rank, local
 
 
+# BF16 tensor flops of one surrogate MLP evaluation (32 -> 64 -> 64 -> 64 -> 2).
+MLP_FLOPS_PER_PAIR = 2 * (32 * 64 + 64 * 64 + 64 * 64 + 64 * 2)
+
+
 def peaks() -> dict:
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -486,8 +490,26 @@ def measure_workload(w, args, dev, flush, rank, weights, features, full: bool) -
             info["light_ms_per_light_dispatch"] = measure_light_graph(pipe, args.steps, args.warmup, flush)
             pipe.set_tuning(per_light_dispatch=0)
         if thr is not None:
+            # per-kernel times of this variant's light stage (events between its
+            # kernels, L2 flushed before each stage) and the MLP's tensor rate
+            pipe.set_tuning(time_kernels=1)
+            kern = {k: [] for k in abi.LIGHT_KERNELS}
+            for i in range(args.warmup + args.steps):
+                with torch.cuda.stream(pipe.stream):
+                    flush.zero_()
+                pipe.light()
+                if i >= args.warmup:
+                    for k, v in pipe.light_kernel_ms().items():
+                        kern[k].append(v)
+            pipe.set_tuning(time_kernels=0)
+            info["light_kernel_ms"] = {k: statistics.mean(v) for k, v in kern.items()}
             ev, fb = C.c_uint32(), C.c_uint32()
             pipe.lib.drv_get_surrogate_stats(pipe.ctx, C.byref(ev), C.byref(fb))
+            mlp_s = info["light_kernel_ms"]["mlp"] / 1e3
+            tf = ev.value * MLP_FLOPS_PER_PAIR / mlp_s / 1e12 if mlp_s > 0 else None
+            info["mlp_tensor"] = {"flops_per_pair": MLP_FLOPS_PER_PAIR, "tflops": tf,
+                                  "frac_of_bf16_peak": tf / peaks()["bf16_tflops"] if tf else None,
+                                  "peak_source": peaks()["source"] + " (bf16_tflops, burst)"}
             blocks = sum(pipe.buffers().n_vpls[l] // hf.lights[l].indirect_shadow_sample_interval
                          for l in range(w.n_lights))
             info.update({"threshold": thr, "features": features, "shadow_blocks": blocks,
@@ -801,8 +823,12 @@ def run_ours(args):
         # (each scene alone, host-issued kernels, one lighting pass per light)
         line["batch"] = {k: batch[k] for k in ("scenes", "precision", "visibility", "threshold", "sizes", "tuned",
                                                "batch", "one_by_one", "reference_form", "speedup",
-                                               "speedup_vs_reference_form")}
+                                               "speedup_vs_reference_form", "largest_tenth")}
         line["batch"]["trials"] = len(batch["trials"])
+        # the stream-count sweep at default knobs: 1 stream = the scenes back
+        # to back inside one graph (no host gaps, no concurrency)
+        line["batch"]["ms_by_streams"] = {str(t["streams"]): t["ms"] for t in batch["trials"]
+                                          if all(t.get(k) == m[0] for k, m in batch_mod.KNOB_MENUS.items())}
     threads = os.cpu_count() or 1
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_of(w, threads)

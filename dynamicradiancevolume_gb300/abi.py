@@ -141,7 +141,7 @@ class DrvTuning(C.Structure):
                 ("plain_voxel_reads", C.c_int32), ("surrogate_wait_test", C.c_int32),
                 ("count_voxel_reads", C.c_int32), ("check_inputs", C.c_int32),
                 ("cull_caches_per_pass", C.c_int32), ("gather_threads", C.c_int32),
-                ("scalar_apply", C.c_int32),
+                ("tensor_core_apply", C.c_int32),
                 ("per_light_dispatch", C.c_int32)]
 
 

@@ -131,7 +131,7 @@ class Batch:
 # tested per pass against the VPL records staged in shared memory) and the
 # gather's tile (threads per cache, i.e. pairs a thread sums).
 KNOB_MENUS = {"cone_ctas_per_sm": (0, 4, 2), "gather_ctas_per_sm": (0, 2, 1), "cull_caches_per_pass": (4, 2, 8),
-              "gather_threads": (256, 128)}
+              "gather_threads": (512, 256)}
 
 
 def set_knobs(scenes: list[Scene], **knobs) -> None:
@@ -263,6 +263,12 @@ def run_batch(n_scenes: int, reps: int, threshold: float = 0.5, fp32_cone: bool 
                                    "one lighting pass per light"},
         "speedup": seq_ms / batch_ms,
         "speedup_vs_reference_form": ref_ms / batch_ms,
+        # the tenth of the scenes with the longest frames alone: their share of
+        # the one-by-one total bounds what any schedule of the batch can save
+        "largest_tenth": {"scenes": max(1, n_scenes // 10),
+                          "alone_ms": float(np.sort(seq_lat)[::-1][:max(1, n_scenes // 10)].sum()),
+                          "share_of_one_by_one": float(np.sort(seq_lat)[::-1][:max(1, n_scenes // 10)].sum()
+                                                       / max(seq_ms, 1e-9))},
         "per_scene": [{"pixels": int(px[i]), "voxels": s.pipe.hf.workload.voxel_res, "vpls": s.vpls,
                        "caches": s.caches, "cav_res": s.pipe.hf.workload.cav_res, "alone_ms": float(seq_lat[i]),
                        "reference_form_ms": float(ref_lat[i]), "batch_done_ms": float(batch_lat[i])} for i, s in enumerate(scenes)],

@@ -139,19 +139,37 @@ cudaError_t alloc_pairs(Context* c, uint64_t cap) {
     cudaFree(c->pair_mem);
     c->pair_mem = nullptr;
   }
-  const size_t bytes = (size_t)cap * 21 + (size_t)c->cfg.max_caches * 8 + drv::kPairCounters * 4;
+  // Every array starts on a 16-byte boundary (the unit list is read and
+  // written as 8-byte vectors).
+  const size_t slots = drv::gather_partial_slots(cap, c->cfg.max_caches);
+  const size_t mc = c->cfg.max_caches;
+  size_t bytes = 0;
+  auto take = [&bytes](size_t n) {
+    const size_t at = bytes;
+    bytes = (bytes + n + 15) & ~(size_t)15;
+    return at;
+  };
+  const size_t o_cache = take(cap * 4), o_block = take(cap * 4), o_shadow = take(cap * 4),
+               o_order = take(cap * 4), o_retrace = take(cap * 4), o_info = take(mc * 8),
+               o_counters = take(drv::kPairCounters * 4), o_tickets = take(mc * 4),
+               o_partials = take(slots * drv::kGatherSlotFloats * 4), o_units = take(slots * sizeof(uint2)),
+               o_cls = take(cap);
   cudaError_t e = cudaMalloc(&c->pair_mem, bytes);
   if (e != cudaSuccess) return e;
   if ((e = cudaMemset(c->pair_mem, 0, bytes)) != cudaSuccess) return e;
-  uint32_t* w = static_cast<uint32_t*>(c->pair_mem);
-  c->pairs.cache = w;
-  c->pairs.block = w + cap;
-  c->pairs.shadow = reinterpret_cast<float*>(w + 2 * cap);
-  c->pairs.order = w + 3 * cap;
-  c->pairs.retrace = w + 4 * cap;
-  c->pairs.info = w + 5 * cap;
-  c->pairs.counters = w + 5 * cap + 2 * (size_t)c->cfg.max_caches;
-  c->pairs.cls = reinterpret_cast<uint8_t*>(c->pairs.counters + drv::kPairCounters);
+  char* m = static_cast<char*>(c->pair_mem);
+  c->pairs.cache = reinterpret_cast<uint32_t*>(m + o_cache);
+  c->pairs.block = reinterpret_cast<uint32_t*>(m + o_block);
+  c->pairs.shadow = reinterpret_cast<float*>(m + o_shadow);
+  c->pairs.order = reinterpret_cast<uint32_t*>(m + o_order);
+  c->pairs.retrace = reinterpret_cast<uint32_t*>(m + o_retrace);
+  c->pairs.info = reinterpret_cast<uint32_t*>(m + o_info);
+  c->pairs.counters = reinterpret_cast<uint32_t*>(m + o_counters);
+  c->pairs.tickets = reinterpret_cast<uint32_t*>(m + o_tickets);
+  c->pairs.partials = reinterpret_cast<float*>(m + o_partials);
+  c->pairs.partial_tail = (uint32_t)(cap / drv::kGatherChunk + 1);
+  c->pairs.units = reinterpret_cast<uint2*>(m + o_units);
+  c->pairs.cls = reinterpret_cast<uint8_t*>(m + o_cls);
   c->pairs.cap = (uint32_t)cap;
   return cudaSuccess;
 }
@@ -782,7 +800,7 @@ drv_status drv_apply(DrvContext* ctx, const DrvGBufferView* g, const DrvPerFrame
   return cuda_check(ctx, drv::launch_apply(ctx->s(), ctx->cfg, *vol, *f, *g, ctx->atlas, ctx->entries,
                                            ctx->entry_stride, ctx->counter, out_rgb, ctx->srgb,
                                            ctx->spec_env ? &sv : nullptr, ctx->scratch_words + 1,
-                                           ctx->tuning.scalar_apply != 0),
+                                           ctx->tuning.tensor_core_apply != 0),
                     "apply");
 }
 
@@ -908,8 +926,8 @@ drv_status drv_set_tuning(DrvContext* ctx, const DrvTuning* t) {
   if (t->cull_caches_per_pass != 0 && t->cull_caches_per_pass != 2 && t->cull_caches_per_pass != 4 &&
       t->cull_caches_per_pass != 8)
     return fail(ctx, DRV_ERR_INVALID_ARG, "cull_caches_per_pass must be 0, 2, 4 or 8");
-  if (t->gather_threads != 0 && t->gather_threads != 128 && t->gather_threads != 256)
-    return fail(ctx, DRV_ERR_INVALID_ARG, "gather_threads must be 0, 128 or 256");
+  if (t->gather_threads != 0 && t->gather_threads != 256 && t->gather_threads != 512)
+    return fail(ctx, DRV_ERR_INVALID_ARG, "gather_threads must be 0, 256 or 512");
   if (t->light_path == DRV_LIGHT_PATH_SINGLE) DRV_TRY_CUDA(ctx, ensure_single_scratch(ctx));
   if (t->pair_capacity > ctx->pairs.cap) {
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;

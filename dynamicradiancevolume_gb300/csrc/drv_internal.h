@@ -107,12 +107,22 @@ struct LightScratch {
 // corner bytes, [2] mip records and [7] plain mip texels the cone pass read
 // (its counting instance only), [3] narrow and [4] wide cones in retrace,
 // [5] pairs the surrogate evaluated, [6] the cone pass's work cursor,
-// [8 + c] pairs of class c, [8 + kConeClasses + c] class c's scatter cursor.
+// [8 + c] pairs of class c, [8 + kConeClasses + c] class c's scatter cursor,
+// [kGatherUnitsCounter] the gather units listed in units.
+// The gather takes a cache's run in units of kGatherChunk pairs (units[u] =
+// {cache, unit index}, listed by the cull), a warp per unit; a cache of
+// several units sums their partials (partials: a slot per
+// unit, full units at the index of the multiple of kGatherChunk they cover,
+// each cache's last unit at partial_tail + cache) in unit order, done by the
+// unit that finishes last (tickets: per cache, zero between stages).
 constexpr uint32_t kNoPair = 0xFFFFFFFFu;
 constexpr uint32_t kPairOverflow = 0xFFFFFFFFu;
 constexpr int kMaxSplitBlocks = 65536;  // shadow blocks per frame the split stage handles
 constexpr int kConeClasses = 32;
-constexpr int kPairCounters = 8 + 2 * kConeClasses;
+constexpr int kGatherUnitsCounter = 8 + 2 * kConeClasses;
+constexpr int kPairCounters = kGatherUnitsCounter + 8;
+constexpr uint32_t kGatherChunk = 512;  // pairs per gather unit (a multiple of 32)
+constexpr int kGatherSlotFloats = 27;   // partial sums per unit slot (NK * 3 <= 27)
 struct PairList {
   uint32_t* cache;
   uint32_t* block;
@@ -122,8 +132,17 @@ struct PairList {
   uint8_t* cls;
   uint32_t* info;
   uint32_t* counters;
+  uint32_t* tickets;    // [max_caches]
+  float* partials;      // [partial_tail + max_caches][kGatherSlotFloats]
+  uint2* units;         // [partial_tail + max_caches]
+  uint32_t partial_tail;
   uint32_t cap;
 };
+// Slots of the gather's partial sums (and bound on its units) a pair list of
+// `cap` pairs needs.
+inline size_t gather_partial_slots(uint64_t cap, uint32_t max_caches) {
+  return (size_t)(cap / kGatherChunk + 1) + max_caches;
+}
 
 // Ray frame of a pinhole camera: direction = normalize(fwd + nx*right + ny*up).
 struct RayFrame {
@@ -277,7 +296,7 @@ struct SplitKnobs {
   int cone_ctas_per_sm = 0;
   int gather_ctas_per_sm = 0;
   int cull_caches_per_pass = 4;
-  int gather_threads = 256;
+  int gather_threads = 512;
   bool count_voxel_reads = false;
 };
 
@@ -294,12 +313,12 @@ cudaError_t launch_bruteforce_rsm(cudaStream_t s, const DrvPerFrame& f, const Dr
                                   const float* srgb);
 // spec: the envmap atlas when specular is on, else nullptr.
 // err: device error word (DRV_DEVERR_BOUNDS for an atlas slot past the count).
-// scalar: BF16 entries evaluated per pixel on the FP32 pipes instead of on the
-// tensor cores (DrvTuning.scalar_apply).
+// tensor_core: BF16 entries evaluated a warp's cells at a time on the tensor
+// cores instead of per pixel on the FP32 pipes (DrvTuning.tensor_core_apply).
 cudaError_t launch_apply(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const DrvPerFrame& f,
                          const DrvGBufferView& g, const uint32_t* atlas, const void* entries, uint32_t entry_stride,
                          const DrvCacheCounter* counter, float* out_rgb, const float* srgb,
-                         const SpecView* spec = nullptr, uint32_t* err = nullptr, bool scalar = false);
+                         const SpecView* spec = nullptr, uint32_t* err = nullptr, bool tensor_core = false);
 // Sets DRV_DEVERR_NUMERIC in *word when any of n values (float, or half when
 // half is nonzero) is NaN or infinite.
 cudaError_t launch_scan_finite(cudaStream_t s, const void* data, size_t n, int half, uint32_t* word);

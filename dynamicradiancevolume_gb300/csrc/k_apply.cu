@@ -544,7 +544,7 @@ __global__ void __launch_bounds__(256, 3) apply_tc_kernel(ApplyParams p) {
 cudaError_t launch_apply(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeInfo& vol, const DrvPerFrame& f,
                          const DrvGBufferView& g, const uint32_t* atlas, const void* entries, uint32_t entry_stride,
                          const DrvCacheCounter* counter, float* out_rgb, const float* srgb, const SpecView* spec,
-                         uint32_t* err, bool scalar) {
+                         uint32_t* err, bool tensor_core) {
   ApplyParams p{};
   p.err = err;
   p.rc = make_cell_recip(vol);
@@ -590,7 +590,7 @@ cudaError_t launch_apply(cudaStream_t s, const DrvConfig& cfg, const DrvVolumeIn
             : apply_kernel<false, false, true><<<grid, block, 0, s>>>(p);
     return cudaGetLastError();
   }
-  if (p.bf16 && !scalar)
+  if (p.bf16 && tensor_core)
     p.sh2 ? apply_tc_kernel<true><<<grid, block, 0, s>>>(p) : apply_tc_kernel<false><<<grid, block, 0, s>>>(p);
   else if (p.bf16)
     p.sh2 ? apply_kernel<true, true, false><<<grid, block, 0, s>>>(p)

@@ -21,9 +21,10 @@
 //     march cones of one length along one sampling path; with the learned
 //     surrogate, the MLP (k_light_surrogate.cu) fills in the shadowing first
 //     and only the pairs it is not confident about are traced;
-//  3. gather_kernel (a CTA per cache): each thread gathers a fixed subset of
-//     the cache's pairs with their shadowing into SH partial sums in
-//     registers, reduced in a fixed order — the result does not depend on
+//  3. gather_kernel (a warp per unit of up to kGatherChunk pairs of one
+//     cache; one wave takes every cache at once): each lane gathers a fixed
+//     subset of the unit's pairs with their shadowing into SH partial sums
+//     in registers, reduced in a fixed order — the result does not depend on
 //     scheduling — and read-modify-written into the entry once (`+=`, as the
 //     reference's per-light dispatches accumulate).
 //
@@ -108,6 +109,15 @@ __device__ __forceinline__ void gather_block(const StageParams& p, float* acc, f
 }
 
 // ------------------------------------------------------------ split stage
+// Lists the gather units of cache c's run: one per kGatherChunk listed
+// pairs, one for a cache the list could not hold.
+__device__ __forceinline__ void note_gather_units(const PairList& L, uint32_t c, uint32_t total, bool over) {
+  const uint32_t n = over ? 1u : (total + kGatherChunk - 1) / kGatherChunk;
+  if (!n) return;
+  const uint32_t base = atomicAdd(L.counters + kGatherUnitsCounter, n);
+  for (uint32_t k = 0; k < n; ++k) L.units[base + k] = make_uint2(c, k);
+}
+
 constexpr int kCullThreads = 256;
 constexpr int kCullWarps = kCullThreads / 32;
 
@@ -164,6 +174,7 @@ __global__ void __launch_bounds__(kCullThreads) cull_kernel(StageParams p, PairL
       const bool over = (uint64_t)base + total > (uint64_t)L.cap;
       L.info[2 * c] = base;
       L.info[2 * c + 1] = over ? kPairOverflow : total;
+      note_gather_units(L, c, total, over);
       s_base = base;
       s_count = over ? kPairOverflow : total;
     }
@@ -352,6 +363,7 @@ __global__ void __launch_bounds__(kCullRecThreads) cull_records_kernel(StagePara
         const bool over = (uint64_t)base + total > (uint64_t)L.cap;
         L.info[2 * c] = base;
         L.info[2 * c + 1] = over ? kPairOverflow : total;
+        note_gather_units(L, c, total, over);
         s_base[k] = base;
         s_count[k] = over ? kPairOverflow : total;
       }
@@ -571,80 +583,193 @@ __device__ __forceinline__ float warp_transpose_reduce(float (&v)[32], int lane)
   return v[0];
 }
 
-constexpr int kGatherThreads = 256;  // default threads per cache
+// The gather's VPLs: as many as fit in kGatherStageBytes of shared memory
+// (VPL g of the lights' arrays back to back, in light order) are copied there
+// once per CTA; the rest are read from global memory.
+constexpr size_t kGatherStageBytes = 220 * 1024;
+template <bool BF16>
+__host__ __device__ constexpr uint32_t vpl_bytes() {
+  return BF16 ? (uint32_t)sizeof(DrvVPLBF16) : (uint32_t)sizeof(DrvVPL);
+}
+uint32_t gather_staged_vpls(const LightLaunch& ll, bool bf16) {
+  uint32_t total = 0;
+  for (int l = 0; l < ll.n_lights; ++l) total += (uint32_t)ll.lights[l].n_vpls;
+  const uint32_t fit = (uint32_t)(kGatherStageBytes / (bf16 ? vpl_bytes<true>() : vpl_bytes<false>()));
+  return total < fit ? total : fit;
+}
 
-// CTA per cache: SH gather of the cache's pairs with their shadowing.
-// Three CTAs per SM fit the FP32 instances without spilling (30.7 -> 26.6 us
-// at 1080p / 4096 VPLs); the BF16 instances, with Kahan sums, spill there
-// and keep two (32.8 us against 36.3).
+// SH gather of block b with the given shadowing, its VPLs from the staged
+// copy (g < staged) or from global memory.
+template <int NK, bool BF16, bool KAHAN>
+__device__ __forceinline__ void gather_block_staged(const StageParams& p, const unsigned char* s_vpl,
+                                                    const uint32_t* s_vbase, uint32_t staged, float* acc, float* comp,
+                                                    int b, float cx, float cy, float cz, float shadowing) {
+  const int l = block_light(p, b);
+  const LightArgs& la = p.ll.lights[l];
+  const int lb = b - p.block_base[l];
+  for (int j = 0; j < la.interval; ++j) {
+    const int i = lb * la.interval + j;
+    const uint32_t g = s_vbase[l] + (uint32_t)i;
+    const VplData v = g < staged ? load_vpl<BF16, true>(s_vpl, (int)g) : load_vpl<BF16>(la.vpls, i);
+    const Transfer t = transfer(v, cx, cy, cz);
+    if (contributes(v, t) && flux_ok(p, v)) accumulate<NK, KAHAN>(p.ev, acc, comp, 1, v, t, shadowing);
+  }
+}
+
+// Warp per gather unit: kGatherChunk pairs of one cache's run (lane j sums
+// the unit's pairs j, j + 32, ... in order), or the whole cache when the list
+// could not hold it (the warp tests every block and traces the live ones'
+// cones; the k-th live block goes to lane k mod 32, the lane its listed pair
+// would have had). The cull lists the units, so one wave of warps takes
+// every cache at once and a long run is spread over several warps. A cache
+// of one unit adds
+// its sums to the entry directly (`+=`, as the reference's per-light
+// dispatches accumulate); a longer one writes each unit's sums to its slot
+// and the unit that finishes last adds them in unit order: the result does
+// not depend on scheduling. One CTA per SM: its VPL copy (a bulk
+// asynchronous copy per light, issued before the wait on the previous
+// kernel, since the VPLs were written before the light stage began) is
+// shared by all its warps. THREADS only sets the warps per CTA.
 template <int NK, bool BF16, int THREADS>
-__global__ void __launch_bounds__(THREADS, (BF16 ? 2 : 3) * 256 / THREADS) gather_kernel(StageParams p, PairList L) {
-  constexpr int kGatherWarps = THREADS / 32;
-  pdl_wait_and_release();
+__global__ void __launch_bounds__(THREADS, 1) gather_kernel(StageParams p, PairList L, uint32_t staged) {
+  extern __shared__ __align__(16) unsigned char s_vpl[];
+  __shared__ uint32_t s_vbase[DRV_MAX_LIGHTS];
+  __shared__ __align__(8) uint64_t s_bar;
   constexpr bool KAHAN = BF16;  // FP32 accumulation of BF16-stored results, compensated
-  __shared__ float s_red[kGatherWarps][NK * 3];
-  __shared__ uint32_t s_count[kGatherWarps];  // list-full path: contributing blocks per warp
-  __shared__ int s_block[THREADS];     // list-full path: this chunk's contributing blocks
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint32_t n_caches = cache_count(p);
-  for (uint32_t c = blockIdx.x; c < n_caches; c += gridDim.x) {
+  constexpr int NV = NK * 3;
+  const int lane = threadIdx.x & 31;
+  const uint32_t bar = (uint32_t)__cvta_generic_to_shared(&s_bar);
+  if (threadIdx.x == 0) {
+    uint32_t base = 0;
+    for (int l = 0; l < p.ll.n_lights; ++l) {
+      s_vbase[l] = base;
+      base += (uint32_t)p.ll.lights[l].n_vpls;
+    }
+    if (staged) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(staged * vpl_bytes<BF16>())
+                   : "memory");
+      for (int l = 0; l < p.ll.n_lights; ++l) {
+        const uint32_t v0 = s_vbase[l];
+        if (v0 >= staged) break;
+        const uint32_t n = min((uint32_t)p.ll.lights[l].n_vpls, staged - v0);
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                         (uint32_t)__cvta_generic_to_shared(s_vpl + (size_t)v0 * vpl_bytes<BF16>())),
+                     "l"(p.ll.lights[l].vpls), "r"(n * vpl_bytes<BF16>()), "r"(bar)
+                     : "memory");
+      }
+    }
+  }
+  __syncthreads();  // offsets written, barrier initialised before anyone waits on it
+  pdl_wait_and_release();
+  if (staged) {
+    bool ok = false;
+    const unsigned long long t0 = clock64();
+    for (;;) {
+      uint32_t done;
+      asm volatile(
+          "{\n.reg .pred q;\nmbarrier.try_wait.parity.shared::cta.b64 q, [%1], 0;\nselp.u32 %0, 1, 0, q;\n}\n"
+          : "=r"(done)
+          : "r"(bar)
+          : "memory");
+      if (done) {
+        ok = true;
+        break;
+      }
+      if ((unsigned long long)(clock64() - t0) > 2000000000ull) break;  // about a second
+    }
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0 && p.err) raise_error(p.err, DRV_DEVERR_TIMEOUT);
+      // the copies may still be in flight: wait for them once more (bounded)
+      // before this CTA's shared memory is released
+      const unsigned long long t1 = clock64();
+      for (;;) {
+        uint32_t done;
+        asm volatile(
+            "{\n.reg .pred q;\nmbarrier.try_wait.parity.shared::cta.b64 q, [%1], 0;\nselp.u32 %0, 1, 0, q;\n}\n"
+            : "=r"(done)
+            : "r"(bar)
+            : "memory");
+        if (done || (unsigned long long)(clock64() - t1) > 2000000000ull) break;
+      }
+      return;
+    }
+  }
+  const uint32_t n_units = L.counters[kGatherUnitsCounter];
+  const uint32_t warps = gridDim.x * (THREADS / 32);
+  for (uint32_t u = blockIdx.x * (THREADS / 32) + (threadIdx.x >> 5); u < n_units; u += warps) {
+    const uint2 unit = L.units[u];
+    const uint32_t c = unit.x, k = unit.y;
+    const uint32_t first = L.info[2 * c], count = L.info[2 * c + 1];
+    const bool over = count == kPairOverflow;
+    const uint32_t units = over ? 1u : (count + kGatherChunk - 1) / kGatherChunk;
     float cx, cy, cz;
     cache_position<BF16>(p, c, cx, cy, cz);
-    float acc[NK * 3], comp[NK * 3];
+    float acc[NV], comp[NV];
 #pragma unroll
-    for (int k = 0; k < NK * 3; ++k) acc[k] = comp[k] = 0.0f;
-    const uint32_t first = L.info[2 * c], count = L.info[2 * c + 1];
-    if (count != kPairOverflow) {
-      for (uint32_t j = threadIdx.x; j < count; j += THREADS) {
-        const uint32_t i = first + j;
-        gather_block<NK, BF16, KAHAN>(p, acc, comp, (int)L.block[i], cx, cy, cz, L.shadow[i]);
+    for (int q = 0; q < NV; ++q) acc[q] = comp[q] = 0.0f;
+    const uint32_t lo = first + k * kGatherChunk;
+    if (!over) {
+      // the next pair's block and shadowing are loaded while this pair is summed
+      const uint32_t hi = first + min(count, (k + 1) * kGatherChunk);
+      uint32_t i = lo + lane;
+      uint32_t b_next = i < hi ? __ldg(L.block + i) : 0u;
+      float s_next = i < hi ? __ldg(L.shadow + i) : 0.0f;
+      for (; i < hi; i += 32) {
+        const uint32_t b = b_next;
+        const float shadowing = s_next;
+        if (i + 32 < hi) {
+          b_next = __ldg(L.block + i + 32);
+          s_next = __ldg(L.shadow + i + 32);
+        }
+        gather_block_staged<NK, BF16, KAHAN>(p, s_vpl, s_vbase, staged, acc, comp, (int)b, cx, cy, cz, shadowing);
       }
     } else {
-      // The list was full: trace this cache's cones here. The k-th
-      // contributing block goes to thread k mod THREADS, as the k-th
-      // listed pair does above, so every thread sums the same pairs in the
-      // same order and the result is the same either way (to FP32 rounding:
-      // the cone is inlined here and in cone_kernel).
-      uint32_t before = 0;  // contributing blocks in earlier chunks
-      for (int b0 = 0; b0 < p.total_blocks; b0 += THREADS) {
-        const int b = b0 + threadIdx.x;
+      uint32_t before = 0;  // live blocks in earlier rounds
+      for (int b0 = 0; b0 < p.total_blocks; b0 += 32) {
+        const int b = b0 + lane;
         const bool live = b < p.total_blocks && block_live<BF16>(p, b, cx, cy, cz);
         const uint32_t m = __ballot_sync(0xffffffffu, live);
-        if (lane == 0) s_count[warp] = __popc(m);
-        __syncthreads();
-        uint32_t rank = __popc(m & ((1u << lane) - 1u)), n = 0;
-#pragma unroll
-        for (int w = 0; w < kGatherWarps; ++w) {
-          if (w < warp) rank += s_count[w];
-          n += s_count[w];
-        }
-        if (live) s_block[rank] = b;
-        __syncthreads();
-        const uint32_t i = (uint32_t)(threadIdx.x + THREADS - before % THREADS) % THREADS;
-        if (i < n) {
-          const int bb = s_block[i];
-          gather_block<NK, BF16, KAHAN>(p, acc, comp, bb, cx, cy, cz, block_cone(p, bb, cx, cy, cz));
-        }
-        before += n;
-        __syncthreads();
+        const int n = __popc(m);
+        const int i = (lane - (int)(before & 31u)) & 31;  // this lane's live block of the round
+        const int src = i < n ? (int)__fns(m, 0u, i + 1) : 0;
+        const int bb = __shfl_sync(0xffffffffu, b, src);
+        if (i < n)
+          gather_block_staged<NK, BF16, KAHAN>(p, s_vpl, s_vbase, staged, acc, comp, bb, cx, cy, cz,
+                                               block_cone(p, bb, cx, cy, cz));
+        before += (uint32_t)n;
       }
     }
-    {
-      // Warp reduction of the NK*3 sums: lane k ends up with coefficient k.
-      float v[32];
+    // Warp reduction of the NV sums: lane q ends up with coefficient q.
+    float v[32];
 #pragma unroll
-      for (int k = 0; k < 32; ++k) v[k] = k < NK * 3 ? (KAHAN ? __fsub_rn(acc[k], comp[k]) : acc[k]) : 0.0f;
-      const float mine = warp_transpose_reduce<NK * 3 <= 16 ? 16 : 32>(v, lane);
-      if (lane < NK * 3) s_red[warp][lane] = mine;
+    for (int q = 0; q < 32; ++q) v[q] = q < NV ? (KAHAN ? __fsub_rn(acc[q], comp[q]) : acc[q]) : 0.0f;
+    const float mine = warp_transpose_reduce<NV <= 16 ? 16 : 32>(v, lane);
+    float* entry = p.entries + (size_t)c * p.stride_floats;
+    if (units == 1u) {
+      if (lane < NV) add_to_entry<BF16>(entry, lane, mine);
+      continue;
     }
-    __syncthreads();
-    if (threadIdx.x < NK * 3) {
-      float v = 0.0f;
-#pragma unroll
-      for (int w = 0; w < kGatherWarps; ++w) v += s_red[w][threadIdx.x];
-      add_to_entry<BF16>(p.entries + (size_t)c * p.stride_floats, threadIdx.x, v);
+    auto slot_of = [&](uint32_t j) -> size_t {
+      return j + 1 < units ? (first + j * kGatherChunk + kGatherChunk - 1) / kGatherChunk
+                           : (size_t)L.partial_tail + c;
+    };
+    if (lane < NV) L.partials[slot_of(k) * kGatherSlotFloats + lane] = mine;
+    __threadfence();
+    __syncwarp();
+    uint32_t ticket = 0;
+    if (lane == 0) ticket = atomicAdd(L.tickets + c, 1u);
+    ticket = __shfl_sync(0xffffffffu, ticket, 0);
+    if (ticket + 1u != units) continue;
+    __threadfence();
+    if (lane < NV) {
+      float sum = 0.0f;
+      for (uint32_t j = 0; j < units; ++j)
+        sum += j == k ? mine : __ldcg(L.partials + slot_of(j) * kGatherSlotFloats + lane);
+      add_to_entry<BF16>(entry, lane, sum);
     }
-    __syncthreads();
+    if (lane == 0) L.tickets[c] = 0u;  // ready for the next stage
   }
 }
 
@@ -867,10 +992,14 @@ cudaError_t split_variant(cudaStream_t s, const StageParams& p, const PairList& 
                     : launch_grid(cone_kernel<BF16, true>, 128, 0, s, num_sms, cone_ctas, true, p, L);
   }
   if (e != cudaSuccess || (e = mark(DRV_LK_GATHER)) != cudaSuccess) return e;
-  if (knobs.gather_threads == 128)
-    e = launch_grid(gather_kernel<NK, BF16, 128>, 128, 0, s, num_sms, knobs.gather_ctas_per_sm, true, p, L);
-  else
-    e = launch_grid(gather_kernel<NK, BF16, 256>, 256, 0, s, num_sms, knobs.gather_ctas_per_sm, true, p, L);
+  {
+    const uint32_t staged = gather_staged_vpls(p.ll, BF16);
+    const size_t smem = (size_t)staged * vpl_bytes<BF16>();
+    auto kernel = knobs.gather_threads == 256 ? gather_kernel<NK, BF16, 256> : gather_kernel<NK, BF16, 512>;
+    if ((e = set_max_smem(reinterpret_cast<const void*>(kernel), kGatherStageBytes)) != cudaSuccess) return e;
+    e = launch_grid(kernel, knobs.gather_threads == 256 ? 256 : 512, smem, s, num_sms, knobs.gather_ctas_per_sm,
+                    true, p, L, staged);
+  }
   if (e != cudaSuccess) return e;
   return mark(DRV_LK_COUNT);
 }

@@ -150,12 +150,22 @@ struct VplData {
   float px, py, pz, area, fr, fg, fb, nx, ny, nz;
 };
 
-template <bool BF16>
+// 16 bytes from global memory through the read-only path, or (SHARED) from
+// a copy in shared memory.
+template <bool SHARED, typename T>
+__device__ __forceinline__ T load16(const T* q) {
+  if constexpr (SHARED) return *q;
+  else return __ldg(q);
+}
+
+// VPL i of an array (DrvVPL, or DrvVPLBF16 with BF16 precision) in global
+// memory, or (SHARED) of its copy in shared memory.
+template <bool BF16, bool SHARED = false>
 __device__ __forceinline__ VplData load_vpl(const void* base, int i) {
   VplData d;
   if (BF16) {
     const uint4* q = reinterpret_cast<const uint4*>(static_cast<const DrvVPLBF16*>(base) + i);
-    const uint4 a = __ldg(q), b = __ldg(q + 1);
+    const uint4 a = load16<SHARED>(q), b = load16<SHARED>(q + 1);
     d.px = __uint_as_float(a.x);
     d.py = __uint_as_float(a.y);
     d.pz = __uint_as_float(a.z);
@@ -168,7 +178,7 @@ __device__ __forceinline__ VplData load_vpl(const void* base, int i) {
     d.nz = from_bf16((uint16_t)(b.z >> 16));
   } else {
     const float4* q = reinterpret_cast<const float4*>(static_cast<const DrvVPL*>(base) + i);
-    const float4 a = __ldg(q), b = __ldg(q + 1), n = __ldg(q + 2);  // {flux, area}, {position}, {normal}
+    const float4 a = load16<SHARED>(q), b = load16<SHARED>(q + 1), n = load16<SHARED>(q + 2);  // {flux, area}, {position}, {normal}
     d.fr = a.x;
     d.fg = a.y;
     d.fb = a.z;

@@ -577,10 +577,13 @@ typedef struct DrvTuning {
                                   aid: it reads every input once more */
   int32_t cull_caches_per_pass; /* split stage: caches the cull tests per pass against the VPL records staged
                                    in shared memory (the cull's tile: 2, 4 or 8; 0: 4) */
-  int32_t gather_threads;      /* split stage: threads per cache of the gather (128 or 256; 0: 256) */
-  int32_t scalar_apply;        /* nonzero: with BF16 entries (no specular) the apply evaluates each corner's
-                                  SH per pixel on the FP32 pipes instead of a warp's cells on the tensor
-                                  cores; the same result to FP32 rounding */
+  int32_t gather_threads;      /* split stage: threads per CTA of the gather, one CTA per SM sharing its
+                                  staged VPLs, a warp per unit of a cache's pairs (256 or 512; 0: 512) */
+  int32_t tensor_core_apply;   /* nonzero: with BF16 entries (no specular) the apply evaluates a warp's
+                                  cells on the tensor cores (mma.sync of per-pixel factors against a
+                                  cell's corner SH) instead of each corner's SH per pixel on the FP32
+                                  pipes; the same result to FP32 rounding (measured slower at 1080p:
+                                  107 against 101 us) */
   int32_t per_light_dispatch;  /* nonzero: the split light stage runs once per light, each light's SH added
                                   into the entries in turn, as the reference dispatches one lighting pass
                                   per light (renderer.cpp:924-932); the same result to FP32 rounding (BF16

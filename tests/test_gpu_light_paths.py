@@ -51,10 +51,11 @@ def test_split_is_deterministic(cuda, lib):
 
 @pytest.mark.parametrize("cap", [1, 777, 20000])
 def test_full_pair_list_is_traced_by_the_gather(cap, cuda, lib):
-    # caches that do not fit are traced by the gather with the same pair-to-
-    # thread assignment and summation order; the cone code is inlined into
-    # two kernels, whose FMA contraction may differ, so the SH agree to FP32
-    # rounding
+    # caches that do not fit are traced by the gather, the k-th live block on
+    # lane k mod 32 as its listed pair would be, in one unit (a listed cache
+    # of more than 512 pairs sums several units' partials); the cone code is
+    # inlined into two kernels, whose FMA contraction may differ, so the SH
+    # agree to FP32 rounding
     p1, _, sh1 = _lit(REDUCED, 4)
     p2, _, sh2 = _lit(REDUCED, 4, pair_capacity=cap)
     print("overflow cap %d: bitwise %s, rel-L2 %.3e" % (cap, np.array_equal(sh1, sh2), rel_l2(sh2, sh1)))
@@ -152,19 +153,44 @@ def test_load_bandwidth_probe(cuda, lib):
 @pytest.mark.parametrize("w", [pipeline.WORKLOADS["c1_small"], REDUCED], ids=["c1", "c2r"])
 def test_tile_knobs_keep_the_result(w, cuda, lib):
     """The cull's caches per pass only change which caches share a pass (each
-    cache's pair run stays in block order): the SH are the same bit for bit.
-    A 128-thread gather sums each cache's pairs in another order: the same
-    to FP32 rounding."""
+    cache's pair run stays in block order), and the gather's threads per CTA
+    only how many of its warp units share a CTA: the SH are the same bit for
+    bit."""
     p0, pos0, sh0 = _lit(w, 13, light_path=abi.LIGHT_PATH_SPLIT)
     for k in (2, 8):
         p1, pos1, sh1 = _lit(w, 13, light_path=abi.LIGHT_PATH_SPLIT, cull_caches_per_pass=k)
         assert np.array_equal(pos1, pos0) and np.array_equal(sh1, sh0)
         p1.close()
-    p2, pos2, sh2 = _lit(w, 13, light_path=abi.LIGHT_PATH_SPLIT, gather_threads=128)
-    assert np.array_equal(pos2, pos0)
-    assert rel_l2(sh2, sh0) < 1e-6
+    p2, pos2, sh2 = _lit(w, 13, light_path=abi.LIGHT_PATH_SPLIT, gather_threads=256)
+    assert np.array_equal(pos2, pos0) and np.array_equal(sh2, sh0)
     p2.close()
     p0.close()
+
+
+W_MULTI_UNIT = pipeline.scaled(pipeline.WORKLOADS["c1_small"], name="c1_4096_vpls", rsm_resolution=64)
+
+
+def test_multi_unit_caches_are_deterministic_and_match_single_launch(cuda, lib):
+    """With 4096 VPLs in one 2 m cascade the caches average more than one
+    gather unit (512 pairs) of contributing blocks: each unit's partial sums
+    are combined in unit order by whichever unit finishes last, so runs agree
+    bit for bit, whatever the CTA size or grid, and equal the single-launch
+    form to FP32 summation order."""
+    p1, pos1, sh1 = _lit(W_MULTI_UNIT, 2, light_path=abi.LIGHT_PATH_SPLIT)
+    assert p1.light_pairs() > 512 * p1.cache_count()  # so some cache has several units
+    p2, pos2, sh2 = _lit(W_MULTI_UNIT, 2, light_path=abi.LIGHT_PATH_SPLIT, gather_threads=256,
+                         gather_ctas_per_sm=1)
+    assert np.array_equal(pos1, pos2) and np.array_equal(sh1, sh2)
+    p3, pos3, sh3 = _lit(W_MULTI_UNIT, 2, light_path=abi.LIGHT_PATH_SINGLE)
+    assert np.array_equal(pos1, pos3)
+    assert rel_l2(sh3, sh1) < 1e-5
+    # twice on one context: the tickets are back at zero after each stage
+    p1.light()
+    p1.sync()
+    pos_b, sh_b = p1.read_entries_decoded(p1.cache_count())
+    assert rel_l2(sh_b[np.lexsort(pos_b.T[::-1])], 2 * sh1) < 1e-6
+    for p in (p1, p2, p3):
+        p.close()
 
 
 @pytest.mark.parametrize("prec", [abi.PRECISION_FP32, abi.PRECISION_BF16], ids=["f32", "bf16"])

@@ -99,21 +99,22 @@ def test_precision_frame_within_one_percent_of_fp64(case, request, oracle):
 
 @pytest.mark.parametrize("sh_order", [1, 2])
 def test_tensor_core_apply_equals_per_pixel_apply(sh_order, lib, cuda):
-    """With BF16 entries the apply evaluates a warp's cells on the tensor cores
-    (F split into BF16 hi + lo parts, FP32 accumulation); the per-pixel FP32
-    form (DrvTuning.scalar_apply) gives the same radiance to FP32 rounding, on
-    a production-shaped frame with four cascades and transitions."""
+    """With BF16 entries the apply's tensor-core form (DrvTuning.
+    tensor_core_apply: a warp's cells at a time, F split into BF16 hi + lo
+    parts, FP32 accumulation) gives the same radiance as the per-pixel FP32
+    form to FP32 rounding, on a production-shaped frame with four cascades and
+    transitions."""
     from test_gpu_parity import REDUCED
     w = pipeline.scaled(REDUCED, name=f"tc_apply_sh{sh_order}", sh_order=sh_order, precision=abi.PRECISION_BF16)
     p = pipeline.Pipeline(pipeline.host_frame(w, 4))
     p.raycast_inputs()
     p.frame()
     p.sync()
-    tc = p.out.cpu().numpy().copy()
-    p.set_tuning(scalar_apply=1)
+    scalar = p.out.cpu().numpy().copy()
+    p.set_tuning(tensor_core_apply=1)
     p.apply()
     p.sync()
-    scalar = p.out.cpu().numpy()
+    tc = p.out.cpu().numpy()
     assert np.abs(scalar).max() > 0
     assert rel_l2(tc, scalar) < 1e-5
     assert np.max(np.abs(tc - scalar)) <= 1e-4 * np.abs(scalar).max()

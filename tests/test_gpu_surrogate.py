@@ -292,7 +292,7 @@ def test_shipped_surrogate_frame_within_one_percent_of_fp64(seed, threshold, lib
     r = Run(w, oracle, seed=seed,
             surrogate=(surrogate.load_params(), surrogate.load_features(), threshold))
     err = rel_l2(r.out, oracle_frame(r, oracle))
-    print("seed %d threshold %.1f: frame rel-L2 %.4f" % (seed, threshold, err))
+    print("seed %d threshold %.2f: frame rel-L2 %.4f" % (seed, threshold, err))
     assert np.isfinite(r.out).all()
     assert err < 1e-2, err
     r.pipe.close()
