@@ -740,7 +740,26 @@ def cone_roofline(r, cache_peaks, pk, w_name) -> dict:
                     "note": "the voxel pyramid is L2-resident; one ncu capture of this pass read about 13 MB "
                             "from DRAM per launch (profiles/)"},
             "note": "the cone pass is issue-bound (about 75% issue active, ALU pipe 55%, 21 of 32 lanes active): "
-                    "its loads are a small share of either cache's throughput"}
+                    "its loads are a small share of either cache's throughput",
+            "gather": gather_roofline(r, pk)}
+
+
+def gather_roofline(r, pk) -> dict:
+    """The gather pass against the FP32 pipe: the algorithmic flops of the SH
+    sum per gathered pair (sh_flops_per_pair; the BF16 variant's Kahan
+    compensation is not counted) over its live event time, against the
+    nominal FP32 rate of this GPU (SMs x 128 FP32 lanes x 2 flop x max SM
+    clock)."""
+    import torch
+    g_ms = r["kernel_ms"].get("gather") or 0.0
+    pairs = r["hv"].get("live_pairs") or 0
+    per = sh_flops_per_pair(r["w"].sh_order)
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    peak = sms * 128 * 2 * pk["sm_max_mhz"] * 1e6 / 1e12
+    achieved = pairs * per / (g_ms / 1e3) / 1e12 if g_ms > 0 else None
+    return {"kernel": "gather_kernel", "bound": "fp32 pipe", "flops_per_pair": per, "pairs": pairs,
+            "achieved_tflops": achieved, "peak_tflops": peak, "frac": achieved / peak if achieved else None,
+            "peak_source": f"nominal: {sms} SMs x 128 FP32 lanes x 2 flop x {pk['sm_max_mhz']:.0f} MHz"}
 
 
 def cpu_baseline_of(w, threads) -> dict:

@@ -15,6 +15,7 @@
 #include <stdint.h>
 
 #include "../../include/drv.h"
+#include "f32x2.cuh"
 
 namespace drv {
 
@@ -35,6 +36,7 @@ __device__ __forceinline__ float dot3(f3 a, f3 b) { return a.x * b.x + a.y * b.y
 __device__ __forceinline__ f3 normalize3(f3 a) { return a * rsqrtf(dot3(a, a)); }
 __device__ __forceinline__ float sat(float x) { return fminf(fmaxf(x, 0.0f), 1.0f); }
 __device__ __forceinline__ f3 ldf3(const float* p) { return {p[0], p[1], p[2]}; }
+
 
 // ---- binary32 mirrors ------------------------------------------------------
 // M-row * (x, y, z, 1), left to right.

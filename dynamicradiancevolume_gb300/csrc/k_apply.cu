@@ -142,12 +142,16 @@ __device__ __forceinline__ f3 lighting(const ApplyParams& p, const float wp[3], 
     const bool v = (ox ? vx1 : vx0) && (oy ? vy1 : vy0) && (oz ? vz1 : vz0);
     slot[i] = v ? __ldg(p.atlas + (base + ox + oy * aw + oz * plane)) : 0u;
   }
-  // Per-normal factors of SampleCacheIrradiance.
+  // Per-normal factors of SampleCacheIrradiance, with the signs of its terms
+  // (SH1neg1, SH1pos1 and SH2neg2 enter negated) folded in.
   const float f0 = p.cl[0];
-  const float f1y = p.cl[1] * n.y, f1z = p.cl[1] * n.z, f1x = p.cl[1] * n.x;
-  const float f4 = p.cl[2] * n.x * n.y, f5 = p.cl[2] * n.y * n.z, f6 = p.cl[3] * (n.z * n.z * 3.0f - 1.0f);
+  const float f1y = -(p.cl[1] * n.y), f1z = p.cl[1] * n.z, f1x = -(p.cl[1] * n.x);
+  const float f4 = -(p.cl[2] * n.x * n.y), f5 = p.cl[2] * n.y * n.z, f6 = p.cl[3] * (n.z * n.z * 3.0f - 1.0f);
   const float f7 = p.cl[2] * n.x * n.z, f8 = p.cl[4] * (n.x * n.x - n.y * n.y);
-  f3 irr = mkf3(0.f, 0.f, 0.f);
+  // Red and green are summed as one packed pair, blue alone.
+  auto pair = [](float v) { return make_float2(v, v); };
+  float2 irr_rg = make_float2(0.f, 0.f);
+  float irr_b = 0.0f;
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
     const uint32_t addr = slot[i];
@@ -158,7 +162,8 @@ __device__ __forceinline__ f3 lighting(const ApplyParams& p, const float wp[3], 
     if (addr > n_caches && addr != 0xFFFFFFFFu && p.err) raise_error(p.err, DRV_DEVERR_BOUNDS);
     const int ox = i & 1, oy = (i >> 1) & 1, oz = i >> 2;
     const float w = wgt[0][ox] * wgt[1][oy] * wgt[2][oz];
-    float er = 0.0f, eg = 0.0f, eb = 0.0f;
+    float2 erg = make_float2(0.0f, 0.0f);
+    float eb = 0.0f;
     if (!live) {
     } else if (BF16) {
       // 27 BF16 values from byte 4 of the 64-byte entry, coefficient-major.
@@ -168,32 +173,44 @@ __device__ __forceinline__ f3 lighting(const ApplyParams& p, const float wp[3], 
       float sh[27];
 #pragma unroll
       for (int j = 0; j < 27; ++j) sh[j] = from_bf16((uint16_t)(q[1 + (j >> 1)] >> (16 * (j & 1))));
-      er = sh[0] * f0 - sh[3] * f1y + sh[6] * f1z - sh[9] * f1x;
-      eg = sh[1] * f0 - sh[4] * f1y + sh[7] * f1z - sh[10] * f1x;
-      eb = sh[2] * f0 - sh[5] * f1y + sh[8] * f1z - sh[11] * f1x;
+      auto rg = [&](int k) { return make_float2(sh[3 * k], sh[3 * k + 1]); };
+      erg = mul2(rg(0), pair(f0));
+      erg = fma2(rg(1), pair(f1y), erg);
+      erg = fma2(rg(2), pair(f1z), erg);
+      erg = fma2(rg(3), pair(f1x), erg);
+      eb = __fmaf_rn(sh[11], f1x, __fmaf_rn(sh[8], f1z, __fmaf_rn(sh[5], f1y, __fmul_rn(sh[2], f0))));
       if (SH2) {
-        er += -sh[12] * f4 + sh[15] * f5 + sh[18] * f6 + sh[21] * f7 + sh[24] * f8;
-        eg += -sh[13] * f4 + sh[16] * f5 + sh[19] * f6 + sh[22] * f7 + sh[25] * f8;
-        eb += -sh[14] * f4 + sh[17] * f5 + sh[20] * f6 + sh[23] * f7 + sh[26] * f8;
+        erg = fma2(rg(4), pair(f4), erg);
+        erg = fma2(rg(5), pair(f5), erg);
+        erg = fma2(rg(6), pair(f6), erg);
+        erg = fma2(rg(7), pair(f7), erg);
+        erg = fma2(rg(8), pair(f8), erg);
+        eb = __fmaf_rn(sh[26], f8, __fmaf_rn(sh[23], f7, __fmaf_rn(sh[20], f6, __fmaf_rn(sh[17], f5,
+                       __fmaf_rn(sh[14], f4, eb)))));
       }
     } else {
       const float4* e = reinterpret_cast<const float4*>(p.entries + (size_t)(addr - 1u) * p.stride_floats);
       const float4 q1 = __ldg(e + 1), q2 = __ldg(e + 2), q3 = __ldg(e + 3);
       // q1 = {SH1neg1, SH00_r}, q2 = {SH10, SH00_g}, q3 = {SH1pos1, SH00_b}
-      er = q1.w * f0 - q1.x * f1y + q2.x * f1z - q3.x * f1x;
-      eg = q2.w * f0 - q1.y * f1y + q2.y * f1z - q3.y * f1x;
-      eb = q3.w * f0 - q1.z * f1y + q2.z * f1z - q3.z * f1x;
+      erg = mul2(make_float2(q1.w, q2.w), pair(f0));
+      erg = fma2(make_float2(q1.x, q1.y), pair(f1y), erg);
+      erg = fma2(make_float2(q2.x, q2.y), pair(f1z), erg);
+      erg = fma2(make_float2(q3.x, q3.y), pair(f1x), erg);
+      eb = __fmaf_rn(q3.z, f1x, __fmaf_rn(q2.z, f1z, __fmaf_rn(q1.z, f1y, __fmul_rn(q3.w, f0))));
       if (SH2) {
         const float4 q4 = __ldg(e + 4), q5 = __ldg(e + 5), q6 = __ldg(e + 6), q7 = __ldg(e + 7);
         // q4 = {SH2neg2, SH20_r}, q5 = {SH2neg1, SH20_g}, q6 = {SH2pos1, SH20_b}, q7 = {SH2pos2, pad}
-        er += -q4.x * f4 + q5.x * f5 + q4.w * f6 + q6.x * f7 + q7.x * f8;
-        eg += -q4.y * f4 + q5.y * f5 + q5.w * f6 + q6.y * f7 + q7.y * f8;
-        eb += -q4.z * f4 + q5.z * f5 + q6.w * f6 + q6.z * f7 + q7.z * f8;
+        erg = fma2(make_float2(q4.x, q4.y), pair(f4), erg);
+        erg = fma2(make_float2(q5.x, q5.y), pair(f5), erg);
+        erg = fma2(make_float2(q4.w, q5.w), pair(f6), erg);
+        erg = fma2(make_float2(q6.x, q6.y), pair(f7), erg);
+        erg = fma2(make_float2(q7.x, q7.y), pair(f8), erg);
+        eb = __fmaf_rn(q7.z, f8, __fmaf_rn(q6.z, f7, __fmaf_rn(q6.w, f6, __fmaf_rn(q5.z, f5,
+                       __fmaf_rn(q4.z, f4, eb)))));
       }
     }
-    irr.x += fmaxf(er, 0.0f) * w;
-    irr.y += fmaxf(eg, 0.0f) * w;
-    irr.z += fmaxf(eb, 0.0f) * w;
+    irr_rg = fma2(make_float2(fmaxf(erg.x, 0.0f), fmaxf(erg.y, 0.0f)), pair(w), irr_rg);
+    irr_b = __fmaf_rn(fmaxf(eb, 0.0f), w, irr_b);
     if (SPEC && live) {
       const f3 e = env_sample(p.spec, addr - 1u, q);
       spec.x += e.x * w;
@@ -201,7 +218,7 @@ __device__ __forceinline__ f3 lighting(const ApplyParams& p, const float wp[3], 
       spec.z += e.z * w;
     }
   }
-  return irr;
+  return mkf3(irr_rg.x, irr_rg.y, irr_b);
 }
 
 // The pixel's radiance into the target: RGB F32 or RGBA16F, written (alpha

@@ -295,22 +295,35 @@ __device__ __forceinline__ void accumulate(const float ev[5], float* acc, float*
   const float tx = t.tx, ty = t.ty, tz = t.tz;
   const float bs[9] = {ev[0], -ev[1] * ty, ev[1] * tz, -ev[1] * tx, -ev[2] * tx * ty, ev[2] * ty * tz,
                        ev[3] * (tz * tz * 3.0f - 1.0f), ev[2] * tx * tz, ev[4] * (tx * tx - ty * ty)};
+  // Red and green as one packed pair, blue alone.
+  const float2 Lrg = make_float2(L[0], L[1]);
 #pragma unroll
-  for (int k = 0; k < NK; ++k)
-#pragma unroll
-    for (int ch = 0; ch < 3; ++ch) {
-      const int o = (3 * k + ch) * stride;
-      const float x = bs[k] * L[ch];
-      if (KAHAN) {
-        // Kahan-compensated running sum (FP32 accumulation, BF16 storage).
-        const float y = __fsub_rn(x, comp[o]);
-        const float tt = __fadd_rn(acc[o], y);
-        comp[o] = __fsub_rn(__fsub_rn(tt, acc[o]), y);
-        acc[o] = tt;
-      } else {
-        acc[o] += x;
-      }
+  for (int k = 0; k < NK; ++k) {
+    const int o = 3 * k * stride, ob = (3 * k + 2) * stride;
+    const float2 b2 = make_float2(bs[k], bs[k]);
+    float2 a2 = make_float2(acc[o], acc[o + stride]);
+    if (KAHAN) {
+      // Kahan-compensated running sums (FP32 accumulation, BF16 storage).
+      const float2 x2 = mul2(b2, Lrg);
+      const float2 c2 = make_float2(comp[o], comp[o + stride]);
+      const float2 y2 = sub2(x2, c2);
+      const float2 t2 = add2(a2, y2);
+      const float2 n2 = sub2(sub2(t2, a2), y2);
+      comp[o] = n2.x;
+      comp[o + stride] = n2.y;
+      a2 = t2;
+      const float xb = __fmul_rn(bs[k], L[2]);
+      const float yb = __fsub_rn(xb, comp[ob]);
+      const float tb = __fadd_rn(acc[ob], yb);
+      comp[ob] = __fsub_rn(__fsub_rn(tb, acc[ob]), yb);
+      acc[ob] = tb;
+    } else {
+      a2 = fma2(b2, Lrg, a2);
+      acc[ob] = __fmaf_rn(bs[k], L[2], acc[ob]);
     }
+    acc[o] = a2.x;
+    acc[o + stride] = a2.y;
+  }
 }
 
 }  // namespace drv

@@ -23,6 +23,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "f32x2.cuh"
+
 namespace drv {
 
 struct VoxelView {
@@ -58,6 +60,21 @@ struct VoxelReads {
 // rounding intrinsics (no contraction left to the compiler), so every kernel
 // that inlines it computes the same bits.
 __device__ __forceinline__ float lerp(float a, float b, float t) { return __fmaf_rn(b - a, t, a); }
+
+// Trilinear blend of corners t0..t7 (x fastest): the seven lerps of
+// lerp(lerp(lerp(t0, t1, ax), lerp(t2, t3, ax), ay), lerp(lerp(t4, t5, ax),
+// lerp(t6, t7, ax), ay), az), the x and y lerps two at a time in packed FP32
+// pairs: the same roundings, so the same bits, in fewer instructions.
+__device__ __forceinline__ float trilerp(float t0, float t1, float t2, float t3, float t4, float t5, float t6,
+                                         float t7, float ax, float ay, float az) {
+  const float2 axx = make_float2(ax, ax);
+  const float2 lo0 = make_float2(t0, t2), lo1 = make_float2(t4, t6);
+  const float2 c0 = fma2(sub2(make_float2(t1, t3), lo0), axx, lo0);  // (c00, c10)
+  const float2 c1 = fma2(sub2(make_float2(t5, t7), lo1), axx, lo1);  // (c01, c11)
+  const float2 lo = make_float2(c0.x, c1.x);
+  const float2 cz = fma2(sub2(make_float2(c0.y, c1.y), lo), make_float2(ay, ay), lo);  // (lerp in y) at z0, z1
+  return lerp(cz.x, cz.y, az);
+}
 
 __device__ __forceinline__ float mip_texel(const VoxelView& v, uint32_t i) {
   return v.half_mips ? __half2float(__ldg(static_cast<const __half*>(v.mips) + i))
@@ -108,13 +125,8 @@ __device__ __forceinline__ float level0_taps(const VoxelView& v, int x, int y, i
   // exactly: empty space (the common case) costs no interpolation.
   if (b == 0u) return 0.0f;
   if (b == 0xFFu) return 1.0f;
-  const float t0 = (float)(b & 1u), t1 = (float)((b >> 1) & 1u), t2 = (float)((b >> 2) & 1u),
-              t3 = (float)((b >> 3) & 1u), t4 = (float)((b >> 4) & 1u), t5 = (float)((b >> 5) & 1u),
-              t6 = (float)((b >> 6) & 1u), t7 = (float)((b >> 7) & 1u);
-  const float c00 = lerp(t0, t1, ax), c10 = lerp(t2, t3, ax);
-  const float c01 = lerp(t4, t5, ax), c11 = lerp(t6, t7, ax);
-  const float c0 = lerp(c00, c10, ay), c1 = lerp(c01, c11, ay);
-  return lerp(c0, c1, az);
+  auto bit = [b](int k) { return (b >> k) & 1u ? 1.0f : 0.0f; };
+  return trilerp(bit(0), bit(1), bit(2), bit(3), bit(4), bit(5), bit(6), bit(7), ax, ay, az);
 }
 
 // Level 0 at position U (texel coordinate U - 0.5, exact).
@@ -140,10 +152,7 @@ __device__ __forceinline__ float level_n_at(const VoxelView& v, int level, const
   float t2 = mip_texel(v, m + (za | yb | xa)), t3 = mip_texel(v, m + (za | yb | xb));
   float t4 = mip_texel(v, m + (zb | ya | xa)), t5 = mip_texel(v, m + (zb | ya | xb));
   float t6 = mip_texel(v, m + (zb | yb | xa)), t7 = mip_texel(v, m + (zb | yb | xb));
-  const float c00 = lerp(t0, t1, ax), c10 = lerp(t2, t3, ax);
-  const float c01 = lerp(t4, t5, ax), c11 = lerp(t6, t7, ax);
-  const float c0 = lerp(c00, c10, ay), c1 = lerp(c01, c11, ay);
-  return lerp(c0, c1, az);
+  return trilerp(t0, t1, t2, t3, t4, t5, t6, t7, ax, ay, az);
 }
 
 // Record index of texel (x, y, z) in a level of 2^ln texels per axis:
@@ -176,10 +185,7 @@ __device__ __forceinline__ float level_record_at(const VoxelView& v, int level, 
   const float t2 = __low2float(u32_as_half2(r.y)), t3 = __high2float(u32_as_half2(r.y));
   const float t4 = __low2float(u32_as_half2(r.z)), t5 = __high2float(u32_as_half2(r.z));
   const float t6 = __low2float(u32_as_half2(r.w)), t7 = __high2float(u32_as_half2(r.w));
-  const float c00 = lerp(t0, t1, ax), c10 = lerp(t2, t3, ax);
-  const float c01 = lerp(t4, t5, ax), c11 = lerp(t6, t7, ax);
-  const float c0 = lerp(c00, c10, ay), c1 = lerp(c01, c11, ay);
-  return lerp(c0, c1, az);
+  return trilerp(t0, t1, t2, t3, t4, t5, t6, t7, ax, ay, az);
 }
 
 // Trilinear sample of mip level >= 1 (from its records where they exist);
