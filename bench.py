@@ -40,7 +40,7 @@ UNIT = "caches/s"
 # DRAM bytes (read + write) per launch of the light stage's top kernel at
 # ns_1080p_4096, from one `ncu --set full --clock-control none` capture
 # (cold caches) of `bench.py --steps 1 --warmup 1` at that workload.
-NCU_TRAFFIC = {"cone_kernel": 12_660_736}
+NCU_TRAFFIC = {"cone_kernel": 13_395_200}
 
 
 def parse():
@@ -737,9 +737,9 @@ def cone_roofline(r, cache_peaks, pk, w_name) -> dict:
             "l1": {"peak_gbs": l1, "frac": achieved / l1},
             "hbm": {"peak_gbs": pk["hbm_gbs"], "frac": achieved / pk["hbm_gbs"],
                     "peak_source": pk["source"] + " (hbm_gbs)",
-                    "note": "the voxel pyramid is L2-resident; one ncu capture of this pass read about 13 MB "
+                    "note": "the voxel pyramid is L2-resident; one ncu capture of this pass read 13.4 MB "
                             "from DRAM per launch (profiles/)"},
-            "note": "the cone pass is issue-bound (about 75% issue active, ALU pipe 55%, 21 of 32 lanes active): "
+            "note": "the cone pass is issue-bound (73% issue active, ALU pipe 55%, 23.5 of 32 lanes active): "
                     "its loads are a small share of either cache's throughput",
             "gather": gather_roofline(r, pk)}
 
