@@ -744,6 +744,45 @@ def cone_roofline(r, cache_peaks, pk, w_name) -> dict:
             "gather": gather_roofline(r, pk)}
 
 
+def stage_rooflines(w, bf16: bool, caches: int, stage_ms: dict, pk) -> dict:
+    """The HBM-bound stages against the measured copy bandwidth: algorithmic
+    bytes of one frame's stage (every input read once, every output written
+    once, gathered per-cache data counted once per cache) over the stage's
+    stream-timed duration. RSM texels: RGB F32 flux + RG16I normal + RG F32
+    (d, d^2) = 24 B; G-buffer: F32 depth, RG16I normal, RGB F32 albedo; output
+    RGB F32."""
+    px = w.width * w.height
+    R, K = w.rsm_resolution, w.rsm_read_lod + w.shadow_lod
+    levels = [(R >> k) ** 2 * 24 for k in range(K + 1)]
+    n_vpl = (R >> w.rsm_read_lod) ** 2
+    vpl_out = n_vpl * ((32 if bf16 else 48) + 16 + 16)  # VPL, shadow cone, cull record
+    rsm = w.n_lights * (sum(levels[:-1]) + levels[-1] + sum(levels[1:]) + vpl_out)
+    N = w.voxel_res
+    L = N.bit_length() - 1
+    mip_texels = sum((N >> l) ** 3 for l in range(1, L + 1))
+    rec_levels = L if bf16 else min(L, 3)
+    rec_texels = sum((N >> l) ** 3 for l in range(1, rec_levels + 1))
+    vox = (N ** 3 // 8 * 3  # bit grid written once, read by the mip and corner passes
+           + mip_texels * (2 if bf16 else 4) * 2  # mip texels written, read back for the records
+           + N ** 3  # corner-packed level 0 written
+           + rec_texels * 16)  # mip records written
+    entry = 64 if bf16 else (128 if w.sh_order == 2 else 64)
+    atlas = w.n_cascades * w.cav_res ** 3 * 4
+    alloc = px * 4 + atlas + caches * entry
+    apply = px * (4 + 4 + 12 + 12) + atlas + caches * entry
+    out = {}
+    for name, nbytes in (("rsm+vpl", rsm), ("voxelize+mips", vox), ("allocate", alloc), ("apply", apply)):
+        ms = stage_ms.get(name) or 0.0
+        gbs = nbytes / (ms / 1e3) / 1e9 if ms > 0 else None
+        out[name] = {"bytes": int(nbytes), "ms": ms, "achieved_gbs": gbs,
+                     "frac_of_hbm": gbs / pk["hbm_gbs"] if gbs else None}
+    out["peak_gbs"] = pk["hbm_gbs"]
+    out["peak_source"] = pk["source"] + " (hbm_gbs)"
+    out["note"] = ("stream-timed stages of one frame, L2 flushed before the frame; these stages are latency- or "
+                   "issue-bound (profiles/): their HBM fractions are low by that measure")
+    return out
+
+
 def gather_roofline(r, pk) -> dict:
     """The gather pass against the FP32 pipe: the algorithmic flops of the SH
     sum per gathered pair (sh_flops_per_pair; the BF16 variant's Kahan
@@ -829,6 +868,7 @@ def run_ours(args):
         "specular": r["specular"],
         "roofline": cone_roofline(r, cache_peaks, pk, w.name),
         "cache_peaks": cache_peaks,
+        "stage_roofline": stage_rooflines(w, head != "plain_fp32", count, hv["stage_ms"], pk),
         "e2e": e2e,
         "gpu_launches": light_stage_launches(w, head.startswith("surrogate")) * args.steps,
         "clocks": clocks,

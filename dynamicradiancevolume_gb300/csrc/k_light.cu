@@ -227,6 +227,23 @@ inline size_t cull_records_smem(int total_vpls, int words, int K) {
 // the VPL extraction); one bulk asynchronous copy per light (TMA, completion
 // on an mbarrier, bounded wait) stages them, instead of computing them here
 // from the VPLs.
+// One VPL plane record against K caches, ORed into live[]: n.c + w > lim,
+// the three multiply-adds of two caches at a time in packed FP32 pairs (the
+// same roundings as fmaf).
+template <int K>
+__device__ __forceinline__ void plane_tests(const float4 r, const float (&cx)[K], const float (&cy)[K],
+                                            const float (&cz)[K], const float (&lim)[K], bool (&live)[K]) {
+  const float2 rx = make_float2(r.x, r.x), ry = make_float2(r.y, r.y), rz = make_float2(r.z, r.z),
+               rw = make_float2(r.w, r.w);
+#pragma unroll
+  for (int k = 0; k < K; k += 2) {
+    const float2 d = fma2(rx, make_float2(cx[k], cx[k + 1]),
+                          fma2(ry, make_float2(cy[k], cy[k + 1]), fma2(rz, make_float2(cz[k], cz[k + 1]), rw)));
+    live[k] |= d.x > lim[k];
+    live[k + 1] |= d.y > lim[k + 1];
+  }
+}
+
 template <bool BF16, bool UNIT, bool COPY, int K>
 __global__ void __launch_bounds__(kCullRecThreads) cull_records_kernel(StageParams p, PairList L, int total_vpls) {
   pdl_wait_and_release();
@@ -311,21 +328,13 @@ __global__ void __launch_bounds__(kCullRecThreads) cull_records_kernel(StagePara
       for (int k = 0; k < K; ++k) live[k] = false;
       if (b < p.total_blocks) {
         if (UNIT) {
-          const float4 r = s_rec[b];
-#pragma unroll
-          for (int k = 0; k < K; ++k)
-            live[k] = fmaf(r.x, cx[k], fmaf(r.y, cy[k], fmaf(r.z, cz[k], r.w))) > lim[k];
+          plane_tests<K>(s_rec[b], cx, cy, cz, lim, live);
         } else {
           int l = 0, vbase = 0;
           while (b >= p.block_base[l + 1]) vbase += p.ll.lights[l].n_vpls, ++l;
           const int interval = p.ll.lights[l].interval;
           const int first = vbase + (b - p.block_base[l]) * interval;
-          for (int j = 0; j < interval; ++j) {
-            const float4 r = s_rec[first + j];
-#pragma unroll
-            for (int k = 0; k < K; ++k)
-              live[k] |= fmaf(r.x, cx[k], fmaf(r.y, cy[k], fmaf(r.z, cz[k], r.w))) > lim[k];
-          }
+          for (int j = 0; j < interval; ++j) plane_tests<K>(s_rec[first + j], cx, cy, cz, lim, live);
         }
       }
 #pragma unroll

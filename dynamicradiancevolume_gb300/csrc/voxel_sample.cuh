@@ -99,7 +99,8 @@ struct Coord {
 
 __device__ __forceinline__ Coord level_coord(const Coord& U, int level) {
   const float sc = __uint_as_float((uint32_t)(127 - level) << 23);  // 2^-level
-  return Coord{__fmaf_rn(U.x, sc, -0.5f), __fmaf_rn(U.y, sc, -0.5f), __fmaf_rn(U.z, sc, -0.5f)};
+  const float2 xy = fma2(make_float2(U.x, U.y), make_float2(sc, sc), make_float2(-0.5f, -0.5f));
+  return Coord{xy.x, xy.y, __fmaf_rn(U.z, sc, -0.5f)};
 }
 
 // Base texel and weight of coordinate u in a level of n texels (nm1 = n - 1):
@@ -264,8 +265,9 @@ __device__ __forceinline__ float cone_shadow(const VoxelView& v, float voxel_siz
   const float goal = light_dist / voxel_size - 2.0f;
   const float k = 2.0f / (1.0f - dsr);
   for (int s = 0; s < max_steps; ++s) {
-    U.x = __fmaf_rn(Dx, step, U.x);
-    U.y = __fmaf_rn(Dy, step, U.y);
+    const float2 xy = fma2(make_float2(Dx, Dy), make_float2(step, step), make_float2(U.x, U.y));
+    U.x = xy.x;
+    U.y = xy.y;
     U.z = __fmaf_rn(Dz, step, U.z);
     dist += step;
     const float radius = __fmul_rn(dist, dsr);
