@@ -271,7 +271,10 @@ __device__ __forceinline__ float cone_shadow(const VoxelView& v, float voxel_siz
     U.z = __fmaf_rn(Dz, step, U.z);
     dist += step;
     const float radius = __fmul_rn(dist, dsr);
-    occlusion = __fmaf_rn(1.0f - occlusion, sample_voxels_at(v, U, __log2f(radius), reads), occlusion);
+    // A sphere of radius <= 1 voxel samples level 0 (its lod log2(radius) is
+    // <= 0): the logarithm is taken only on the mip branch.
+    const float s_vox = radius > 1.0f ? sample_voxels_at(v, U, __log2f(radius), reads) : level0_at(v, U, reads);
+    occlusion = __fmaf_rn(1.0f - occlusion, s_vox, occlusion);
     if (dist >= goal || occlusion >= 1.0f) break;
     step = fmaxf(1.0f, __fmul_rn(radius, k));
   }
