@@ -125,6 +125,11 @@ def dist_env():
     return ws, rank, local
 
 
+# Frames in flight of the end-to-end measurement: contexts taking the steps
+# in turn, each step's copies overlapping the other frames' kernels (a
+# renderer's triple-buffered swap chain).
+E2E_FRAMES_IN_FLIGHT = 3
+
 # BF16 tensor flops of one surrogate MLP evaluation (32 -> 64 -> 64 -> 64 -> 2).
 MLP_FLOPS_PER_PAIR = 2 * (32 * 64 + 64 * 64 + 64 * 64 + 64 * 2)
 
@@ -549,20 +554,20 @@ def measure_workload(w, args, dev, flush, rank, weights, features, full: bool) -
             p.close()
 
     # ---- e2e through the C ABI with host buffers (pinned), H2D + D2H inside the region.
-    # Two contexts on two streams take the steps in turn (double buffering, as
-    # a renderer uploads frame k+1 while frame k renders): every step copies
-    # its G-buffer and RSM from pinned host memory, runs the frame and copies
-    # its radiance back; the copies of one step overlap the kernels of the
-    # other. The headline uses the reference's own render targets (D32F depth,
+    # E2E_FRAMES_IN_FLIGHT contexts on their own streams take the steps in
+    # turn (a renderer's swap chain: frame k+1 uploads while frame k renders):
+    # every step copies its G-buffer and RSM from pinned host memory, runs the
+    # frame and copies its radiance back; the copies of one step overlap the
+    # kernels of the others, and frames overlap where one leaves SMs idle. The headline uses the reference's own render targets (D32F depth,
     # RG16I normal, SRGB8 diffuse, RGB16F / RG16I / RG16F RSM, RGBA16F output
     # with additive blending, renderer.cpp:119, 468-480, 1288-1290); the same
     # steps over F32 targets are reported beside it.
     wv_head = next(wv for name, wv, thr in plan if name == head)
     g_ref, rsm_ref = pipeline.reference_format_inputs(pipe)
 
-    def e2e_pipes(formats):
+    def e2e_pipes(formats, n):
         out = []
-        for _ in range(2):
+        for _ in range(n):
             hf2 = pipeline.host_frame(wv_head)
             if head.startswith("surrogate"):
                 hf2.config.surrogate_conf_threshold = hv["threshold"]
@@ -576,9 +581,11 @@ def measure_workload(w, args, dev, flush, rank, weights, features, full: bool) -
             out.append(q)
         return out
 
-    def run_e2e(formats, graph, two_contexts=True):
-        """Mean ms per step; (h2d, d2h) bytes per step."""
-        qs = e2e_pipes(formats)
+    def run_e2e(formats, graph, n_ctx=E2E_FRAMES_IN_FLIGHT):
+        """Mean ms per step with n_ctx contexts taking the steps in turn, each
+        on its own stream (n_ctx frames in flight; 1: one step at a time);
+        (h2d, d2h) bytes per step."""
+        qs = e2e_pipes(formats, n_ctx)
         if formats == "reference":
             host_in = [torch.from_numpy(a).pin_memory() for a in g_ref]
             host_rsm = [[torch.from_numpy(a).pin_memory() for a in r] for r in rsm_ref]
@@ -608,7 +615,7 @@ def measure_workload(w, args, dev, flush, rank, weights, features, full: bool) -
         graphs = [batch_mod.Batch([batch_mod.Scene(q, 0, 0)], 1, stream=q.stream) for q in qs] if graph else None
 
         def step(k):
-            i = k % 2 if two_contexts else 0
+            i = k % n_ctx
             q = qs[i]
             with torch.cuda.stream(q.stream):
                 for d, h in zip(dev_in(q), host_in):
@@ -623,19 +630,21 @@ def measure_workload(w, args, dev, flush, rank, weights, features, full: bool) -
             with torch.cuda.stream(q.stream):
                 host_out[i].copy_(q.out, non_blocking=True)
 
-        for k in range(max(args.warmup, 2)):
+        for k in range(max(args.warmup, n_ctx)):  # every context's graph warmed
             step(k)
         torch.cuda.synchronize(dev)
-        a, b = qs[0], qs[1]
+        a = qs[0]
         with torch.cuda.stream(a.stream):
             flush.zero_()
         start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        if two_contexts:
+        if n_ctx > 1:
             start.record(a.stream)
-            b.stream.wait_event(start)
+            for q in qs[1:]:
+                q.stream.wait_event(start)
             for k in range(args.steps):
                 step(k)
-            a.stream.wait_stream(b.stream)
+            for q in qs[1:]:
+                a.stream.wait_stream(q.stream)
             end.record(a.stream)
             end.synchronize()
             ms = start.elapsed_time(end) / args.steps
@@ -665,15 +674,20 @@ def measure_workload(w, args, dev, flush, rank, weights, features, full: bool) -
                       "RG16I normal, RG16F (d, d^2); radiance added into an RGBA16F HDR buffer",
            "scope": "whole frame per step: G-buffer and RSM copied from pinned host memory, the frame replayed as "
                     "a CUDA graph (drv_batch_launch of a one-scene batch captured once per context), radiance "
-                    "copied back, all inside the timed region; two contexts on two streams take the steps in turn "
-                    "(double buffering)"}
+                    f"copied back, all inside the timed region; {E2E_FRAMES_IN_FLIGHT} contexts on their own "
+                    "streams take the steps in turn (frames in flight, as a renderer's swap chain)",
+           "frames_in_flight": E2E_FRAMES_IN_FLIGHT}
     if full:
+        e2e["ms_per_step_by_frames_in_flight"] = {
+            str(n): (e2e_ms if n == E2E_FRAMES_IN_FLIGHT else run_e2e("reference", graph=True, n_ctx=n)[0])
+            for n in (1, 2, 3, 4)}
         e2e["ms_per_step_drv_frame"], _, _ = run_e2e("reference", graph=False)
-        e2e["ms_per_step_one_context"], _, _ = run_e2e("reference", graph=False, two_contexts=False)
+        e2e["ms_per_step_one_context"], _, _ = run_e2e("reference", graph=False, n_ctx=1)
         f32_ms, h2d_f32, d2h_f32 = run_e2e("f32", graph=True)
         e2e["f32_formats"] = {"ms_per_step": f32_ms, "h2d_bytes_per_step": h2d_f32, "d2h_bytes_per_step": d2h_f32,
                               "value": count / (f32_ms / 1e3)}
-        e2e["scope"] += ("; ms_per_step_drv_frame: the same steps calling drv_frame (kernels launched one by one); "
+        e2e["scope"] += ("; ms_per_step_by_frames_in_flight: the graph steps with 1-4 contexts in turn; "
+                         "ms_per_step_drv_frame: the same steps calling drv_frame (kernels launched one by one); "
                          "ms_per_step_one_context: drv_frame steps on one context, one at a time; f32_formats: the "
                          "graph steps with F32 diffuse, F32 RSM and an RGB F32 output")
 
