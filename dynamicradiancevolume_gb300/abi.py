@@ -142,7 +142,7 @@ class DrvTuning(C.Structure):
                 ("count_voxel_reads", C.c_int32), ("check_inputs", C.c_int32),
                 ("cull_caches_per_pass", C.c_int32), ("gather_threads", C.c_int32),
                 ("tensor_core_apply", C.c_int32),
-                ("per_light_dispatch", C.c_int32)]
+                ("per_light_dispatch", C.c_int32), ("gather_wait_test", C.c_int32)]
 
 
 LIGHT_KERNELS = ("cull", "classify", "scatter", "mlp", "cone", "gather")

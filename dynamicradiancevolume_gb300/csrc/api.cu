@@ -714,6 +714,7 @@ drv_status light_caches(DrvContext* ctx, const DrvSpotLight* lights, int32_t n_l
     if (ctx->tuning.cull_caches_per_pass) knobs.cull_caches_per_pass = ctx->tuning.cull_caches_per_pass;
     if (ctx->tuning.gather_threads) knobs.gather_threads = ctx->tuning.gather_threads;
     knobs.count_voxel_reads = ctx->tuning.count_voxel_reads != 0;
+    knobs.gather_wait_test = ctx->tuning.gather_wait_test;
     drv::SurrogateArgs sur;
     if (surrogate) {
       sur.weights = ctx->sur_weights;

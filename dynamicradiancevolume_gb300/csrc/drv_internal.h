@@ -114,7 +114,7 @@ struct LightScratch {
 // several units sums their partials (partials: a slot per
 // unit, full units at the index of the multiple of kGatherChunk they cover,
 // each cache's last unit at partial_tail + cache) in unit order, done by the
-// unit that finishes last (tickets: per cache, zero between stages).
+// unit that finishes last (tickets: per cache, zeroed by the cull).
 constexpr uint32_t kNoPair = 0xFFFFFFFFu;
 constexpr uint32_t kPairOverflow = 0xFFFFFFFFu;
 constexpr int kMaxSplitBlocks = 65536;  // shadow blocks per frame the split stage handles
@@ -297,6 +297,7 @@ struct SplitKnobs {
   int gather_ctas_per_sm = 0;
   int cull_caches_per_pass = 4;
   int gather_threads = 512;
+  int gather_wait_test = 0;  // test hook: the gather's VPL copies are withheld (its bounded wait runs out)
   bool count_voxel_reads = false;
 };
 

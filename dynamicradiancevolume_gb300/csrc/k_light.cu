@@ -110,8 +110,11 @@ __device__ __forceinline__ void gather_block(const StageParams& p, float* acc, f
 
 // ------------------------------------------------------------ split stage
 // Lists the gather units of cache c's run: one per kGatherChunk listed
-// pairs, one for a cache the list could not hold.
+// pairs, one for a cache the list could not hold; and zeroes the cache's
+// ticket, so that a gather that stopped early (a timed-out copy) leaves no
+// count behind for the next stage.
 __device__ __forceinline__ void note_gather_units(const PairList& L, uint32_t c, uint32_t total, bool over) {
+  L.tickets[c] = 0u;
   const uint32_t n = over ? 1u : (total + kGatherChunk - 1) / kGatherChunk;
   if (!n) return;
   const uint32_t base = atomicAdd(L.counters + kGatherUnitsCounter, n);
@@ -639,8 +642,13 @@ __device__ __forceinline__ void gather_block_staged(const StageParams& p, const 
 // asynchronous copy per light, issued before the wait on the previous
 // kernel, since the VPLs were written before the light stage began) is
 // shared by all its warps. THREADS only sets the warps per CTA.
+// hold_copy (test hook): the copies are not issued, so the wait runs out
+// after kGatherTestWaitCycles (~10 ms) and the timeout path is taken.
+constexpr unsigned long long kGatherWaitCycles = 2000000000ull;  // about a second
+constexpr unsigned long long kGatherTestWaitCycles = 20000000ull;
 template <int NK, bool BF16, int THREADS>
-__global__ void __launch_bounds__(THREADS, 1) gather_kernel(StageParams p, PairList L, uint32_t staged) {
+__global__ void __launch_bounds__(THREADS, 1) gather_kernel(StageParams p, PairList L, uint32_t staged,
+                                                            int hold_copy) {
   extern __shared__ __align__(16) unsigned char s_vpl[];
   __shared__ uint32_t s_vbase[DRV_MAX_LIGHTS];
   __shared__ __align__(8) uint64_t s_bar;
@@ -659,7 +667,7 @@ __global__ void __launch_bounds__(THREADS, 1) gather_kernel(StageParams p, PairL
       asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
       asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(staged * vpl_bytes<BF16>())
                    : "memory");
-      for (int l = 0; l < p.ll.n_lights; ++l) {
+      for (int l = 0; l < p.ll.n_lights && !hold_copy; ++l) {
         const uint32_t v0 = s_vbase[l];
         if (v0 >= staged) break;
         const uint32_t n = min((uint32_t)p.ll.lights[l].n_vpls, staged - v0);
@@ -673,6 +681,7 @@ __global__ void __launch_bounds__(THREADS, 1) gather_kernel(StageParams p, PairL
   __syncthreads();  // offsets written, barrier initialised before anyone waits on it
   pdl_wait_and_release();
   if (staged) {
+    const unsigned long long limit = hold_copy ? kGatherTestWaitCycles : kGatherWaitCycles;
     bool ok = false;
     const unsigned long long t0 = clock64();
     for (;;) {
@@ -686,7 +695,7 @@ __global__ void __launch_bounds__(THREADS, 1) gather_kernel(StageParams p, PairL
         ok = true;
         break;
       }
-      if ((unsigned long long)(clock64() - t0) > 2000000000ull) break;  // about a second
+      if ((unsigned long long)(clock64() - t0) > limit) break;
     }
     if (__syncthreads_or(!ok)) {
       if (threadIdx.x == 0 && p.err) raise_error(p.err, DRV_DEVERR_TIMEOUT);
@@ -700,7 +709,7 @@ __global__ void __launch_bounds__(THREADS, 1) gather_kernel(StageParams p, PairL
             : "=r"(done)
             : "r"(bar)
             : "memory");
-        if (done || (unsigned long long)(clock64() - t1) > 2000000000ull) break;
+        if (done || (unsigned long long)(clock64() - t1) > limit) break;
       }
       return;
     }
@@ -778,7 +787,6 @@ __global__ void __launch_bounds__(THREADS, 1) gather_kernel(StageParams p, PairL
         sum += j == k ? mine : __ldcg(L.partials + slot_of(j) * kGatherSlotFloats + lane);
       add_to_entry<BF16>(entry, lane, sum);
     }
-    if (lane == 0) L.tickets[c] = 0u;  // ready for the next stage
   }
 }
 
@@ -1007,7 +1015,7 @@ cudaError_t split_variant(cudaStream_t s, const StageParams& p, const PairList& 
     auto kernel = knobs.gather_threads == 256 ? gather_kernel<NK, BF16, 256> : gather_kernel<NK, BF16, 512>;
     if ((e = set_max_smem(reinterpret_cast<const void*>(kernel), kGatherStageBytes)) != cudaSuccess) return e;
     e = launch_grid(kernel, knobs.gather_threads == 256 ? 256 : 512, smem, s, num_sms, knobs.gather_ctas_per_sm,
-                    true, p, L, staged);
+                    true, p, L, staged, knobs.gather_wait_test);
   }
   if (e != cudaSuccess) return e;
   return mark(DRV_LK_COUNT);

@@ -590,6 +590,9 @@ typedef struct DrvTuning {
                                   entries are rounded once per light). Kernel timing is off, the pair and
                                   surrogate counts are the last light's, and with indirect specular the
                                   envmaps are gathered after the loop with their own cones */
+  int32_t gather_wait_test;    /* test hook, nonzero: the split stage's gather waits for VPL copies it never
+                                  issues, so its bounded wait (~10 ms here) runs out; the stage reports
+                                  DRV_ERR_TIMEOUT from drv_sync and its caches miss their SH */
 } DrvTuning;
 enum { DRV_LIGHT_PATH_AUTO = 0, DRV_LIGHT_PATH_SINGLE = 1, DRV_LIGHT_PATH_SPLIT = 2 };
 drv_status drv_set_tuning(DrvContext* ctx, const DrvTuning* tuning);

@@ -184,7 +184,7 @@ def test_multi_unit_caches_are_deterministic_and_match_single_launch(cuda, lib):
     p3, pos3, sh3 = _lit(W_MULTI_UNIT, 2, light_path=abi.LIGHT_PATH_SINGLE)
     assert np.array_equal(pos1, pos3)
     assert rel_l2(sh3, sh1) < 1e-5
-    # twice on one context: the tickets are back at zero after each stage
+    # twice on one context: each stage starts from zeroed tickets
     p1.light()
     p1.sync()
     pos_b, sh_b = p1.read_entries_decoded(p1.cache_count())
@@ -210,3 +210,35 @@ def test_per_light_dispatch_equals_one_pass(prec, cuda, lib):
     assert np.abs(sh1).max() > 0
     p1.close()
     p2.close()
+
+
+def test_gather_copy_timeout_is_reported_and_context_recovers(cuda, lib):
+    """The gather's wait for its staged VPLs is bounded: with the test hook
+    the copies are withheld, every CTA's wait runs out (about 10 ms), the
+    stage latches DRV_DEVERR_TIMEOUT and drv_sync reports DRV_ERR_TIMEOUT.
+    The same context, allocated and lit again without the hook, gives the
+    SH of a context that never timed out, bit for bit: no cache is left
+    with a count of finished units from the stage that stopped."""
+    import dynamicradiancevolume_gb300 as drv
+    ref_p, ref_pos, ref_sh = _lit(W_MULTI_UNIT, 2, light_path=abi.LIGHT_PATH_SPLIT)
+    p = pipeline.Pipeline(pipeline.host_frame(W_MULTI_UNIT, 2))
+    p.set_tuning(light_path=abi.LIGHT_PATH_SPLIT)
+    p.raycast_inputs()
+    p.prepare_and_extract()
+    p.voxelize()
+    p.allocate()
+    p.set_tuning(gather_wait_test=1)
+    p.light()
+    with pytest.raises(drv.DrvError) as e:
+        p.sync()
+    assert e.value.status == abi.ERR_TIMEOUT
+    p.set_tuning(gather_wait_test=0)
+    p.allocate()
+    p.light()
+    p.sync()
+    pos, sh = p.read_entries_decoded(p.cache_count())
+    order = np.lexsort(pos.T[::-1])
+    assert np.array_equal(pos[order], ref_pos)
+    assert np.array_equal(sh[order], ref_sh)
+    p.close()
+    ref_p.close()
