@@ -467,10 +467,17 @@ __global__ void __launch_bounds__(kClassThreads) scatter_kernel(PairList L) {
   pdl_wait_and_release();
   __shared__ uint32_t s_region[kConeClasses], s_hist[kConeClasses], s_pos[kConeClasses];
   const uint32_t n = min(L.counters[0], L.cap);
-  if (threadIdx.x < kConeClasses) {
-    uint32_t region = 0;
-    for (int k = 0; k < (int)threadIdx.x; ++k) region += L.counters[8 + k];
-    s_region[threadIdx.x] = region;
+  static_assert(kConeClasses == 32, "one warp scans the class totals");
+  if (threadIdx.x < 32) {
+    // exclusive scan of the class totals: one load per lane, shuffles
+    const uint32_t total = L.counters[8 + threadIdx.x];
+    uint32_t incl = total;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+      if ((int)threadIdx.x >= o) incl += v;
+    }
+    s_region[threadIdx.x] = incl - total;
   }
   for (uint32_t t0 = blockIdx.x * kScatterTile; t0 < n; t0 += gridDim.x * kScatterTile) {
     if (threadIdx.x < kConeClasses) s_hist[threadIdx.x] = 0u;
