@@ -8,11 +8,14 @@
 // consecutive VPLs). A frame has only a few thousand caches, and per cache
 // only a small share of the blocks can contribute at all (a block none of
 // whose VPLs has positive flux and faces the cache adds exactly zero whatever
-// its shadowing), so the stage is split in three launches:
+// its shadowing), so the stage is split in three steps (five launches):
 //
-//  1. cull_kernel (a CTA per cache): tests every block against the cache and
-//     writes the cache's contributing blocks, in block order, to one
-//     contiguous run of a global pair list (one atomic per cache claims it);
+//  1. cull_records_kernel (K caches per pass against every VPL's plane
+//     record, staged in shared memory; cull_kernel, a CTA per cache over the
+//     VPL arrays, where the records do not fit) tests every block against
+//     the cache and writes the cache's contributing blocks, in block order,
+//     to one contiguous run of a global pair list (one atomic per cache
+//     claims it), and lists the cache's gather units;
 //  2. classify_kernel + scatter_kernel order the pairs by cone class (the
 //     number of steps the cone marches and whether it reaches mip samples),
 //     and cone_kernel (a thread per pair, persistent grid) traces the cones
