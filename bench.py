@@ -844,7 +844,8 @@ def run_ours(args):
             weights, features = surrogate.load_params(), surrogate.load_features()
         except ValueError as e:  # a checkpoint of another model layout: no surrogate variants
             surrogate_note = str(e)
-    extra = [] if args.no_extra_workloads or args.workload != "ns_1080p_4096" else ["c2_production"]
+    extra = ([] if args.no_extra_workloads or args.workload != "ns_1080p_4096"
+             else ["c2_production", "ns_1080p_4096_cav128"])
     with ClockSampler(local) as clk:
         r = measure_workload(w, args, dev, flush, rank, weights, features, full=True)
         others = {name: measure_workload(pipeline.WORKLOADS[name], args, dev, flush, rank, None, features,

@@ -60,6 +60,11 @@ WORKLOADS = {
     "c2_production": Workload("c2_production", 1920, 1080, 64, 256, 3, 512, 3, 0, 4, 0.25, 32, 2, 32, 262144),
     # The headline case: C2 with one light (4096 VPLs) at 1080p.
     "ns_1080p_4096": Workload("ns_1080p_4096", 1920, 1080, 64, 256, 1, 512, 3, 0, 4, 0.25, 32, 2, 32, 262144),
+    # The headline scene with 128^3 cascades of the same sizes: ~22k caches
+    # (cells of 2 mm at cascade 0), toward the tens of thousands of caches
+    # the configuration text expects; 8.3 M contributing pairs.
+    "ns_1080p_4096_cav128": Workload("ns_1080p_4096_cav128", 1920, 1080, 64, 256, 1, 512, 3, 0, 4, 0.25, 128, 2, 32,
+                                     262144),
     # Precision variant of the small configuration: BF16 VPL flux/normal and
     # cache SH, FP16 opacity mips, FP32 Kahan-compensated accumulation.
     "c3_precision": Workload("c3_precision", 256, 256, 12, 64, 1, 32, 0, 0, 1, 2.0, 32, 1, 16, 65536,

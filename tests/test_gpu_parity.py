@@ -601,3 +601,25 @@ def test_atlas_slot_past_the_count_is_reported_not_read(lib, cuda):
     changed = np.any(out != good, axis=-1)
     assert 0 < changed.mean() < 0.5  # only pixels around that one corner lose its contribution
     p.close()
+
+
+# The headline scene with 128^3 cascades: ~22k caches and 8.3 M contributing
+# pairs, so the gather's units and the pair list run at ten times the
+# headline's size.
+@pytest.fixture(scope="module")
+def ns128(lib, oracle, cuda):
+    w = pipeline.scaled(pipeline.WORKLOADS["ns_1080p_4096_cav128"], precision=abi.PRECISION_BF16)
+    return Run(w, oracle)
+
+
+def test_ns_cav128_allocation_bit_exact(ns128, oracle):
+    st, atlas, pos, count = oracle.allocate_caches(ns128.hf.config, ns128.hf.volume, ns128.hf.frame, ns128.depth)
+    assert ns128.count == count > 10000
+    assert _key_set(ns128.positions) == _key_set(pos)
+    assert np.array_equal(ns128.atlas != 0, atlas != 0)
+
+
+def test_ns_cav128_bf16_frame_within_one_percent_of_fp64(ns128, oracle):
+    ref = oracle_frame(ns128, oracle)
+    err = rel_l2(ns128.out, ref)
+    assert err < 1e-2, err
