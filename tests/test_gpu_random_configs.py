@@ -36,7 +36,7 @@ def random_workload(seed: int) -> pipeline.Workload:
         precision=int(r.choice([abi.PRECISION_FP32, abi.PRECISION_BF16])))
 
 
-@pytest.mark.parametrize("seed", range(8))
+@pytest.mark.parametrize("seed", range(16))
 def test_random_configuration_frame_matches_fp64(seed, lib, oracle, cuda):
     w = random_workload(seed)
     r = Run(w, oracle, seed=100 + seed)
