@@ -152,11 +152,12 @@ def sh_flops_per_pair(sh_order: int) -> int:
 
 
 def light_stage_launches(w, surrogate: bool = False) -> int:
-    # split stage: cull, classify, scatter, cone, gather; with the surrogate:
-    # cull, MLP, cone, gather; without indirect shadow: the single kernel.
+    # split stage: cull, classify, scatter, cone, gather; with the surrogate
+    # the MLP runs between the cull and the classify pass (which then sorts
+    # only the re-traced pairs); without indirect shadow: the single kernel.
     if not w.indirect_shadow:
         return 1
-    return 4 if surrogate else 5
+    return 6 if surrogate else 5
 
 
 def kernel_launches_per_frame(w, surrogate: bool = False) -> int:

@@ -150,7 +150,7 @@ cudaError_t alloc_pairs(Context* c, uint64_t cap) {
     return at;
   };
   const size_t o_cache = take(cap * 4), o_block = take(cap * 4), o_shadow = take(cap * 4),
-               o_order = take(cap * 4), o_retrace = take(cap * 4), o_info = take(mc * 8),
+               o_order = take(cap * 4), o_info = take(mc * 8),
                o_counters = take(drv::kPairCounters * 4), o_tickets = take(mc * 4),
                o_partials = take(slots * drv::kGatherSlotFloats * 4), o_units = take(slots * sizeof(uint2)),
                o_cls = take(cap);
@@ -162,7 +162,6 @@ cudaError_t alloc_pairs(Context* c, uint64_t cap) {
   c->pairs.block = reinterpret_cast<uint32_t*>(m + o_block);
   c->pairs.shadow = reinterpret_cast<float*>(m + o_shadow);
   c->pairs.order = reinterpret_cast<uint32_t*>(m + o_order);
-  c->pairs.retrace = reinterpret_cast<uint32_t*>(m + o_retrace);
   c->pairs.info = reinterpret_cast<uint32_t*>(m + o_info);
   c->pairs.counters = reinterpret_cast<uint32_t*>(m + o_counters);
   c->pairs.tickets = reinterpret_cast<uint32_t*>(m + o_tickets);
@@ -966,9 +965,9 @@ drv_status drv_get_light_pairs(DrvContext* ctx, uint32_t* pairs) {
 drv_status drv_get_light_kernel_ms(DrvContext* ctx, float ms[DRV_LK_COUNT]) {
   if (!ctx || !ms) return DRV_ERR_INVALID_ARG;
   if (!ctx->lk_recorded) return fail(ctx, DRV_ERR_INVALID_ARG, "no split light stage ran with time_kernels");
-  DRV_TRY_CUDA(ctx, cudaEventSynchronize(ctx->lk_events[DRV_LK_COUNT]));
+  DRV_TRY_CUDA(ctx, cudaEventSynchronize(ctx->lk_events[2 * DRV_LK_GATHER + 1]));
   for (int k = 0; k < DRV_LK_COUNT; ++k)
-    DRV_TRY_CUDA(ctx, cudaEventElapsedTime(&ms[k], ctx->lk_events[k], ctx->lk_events[k + 1]));
+    DRV_TRY_CUDA(ctx, cudaEventElapsedTime(&ms[k], ctx->lk_events[2 * k], ctx->lk_events[2 * k + 1]));
   return DRV_OK;
 }
 

@@ -98,15 +98,14 @@ struct LightScratch {
 // light stage. Pair i: cache[i], block[i] (kNoPair: unused slot), shadow[i].
 // info[c] = {first pair of cache c, pair count} (count kPairOverflow: the
 // list was full, the gather traces that cache's cones itself).
-// order lists all pairs by cone class (kConeClasses classes of expected
-// step count and width, cls[i]), so that a warp's lanes march cones of one
-// length that take one sampling path; retrace lists the pairs the surrogate
-// is not confident about, narrow cones (every sample on voxel level 0) from
-// its front, wide ones from its back.
+// order lists the pairs to trace by cone class (kConeClasses classes of
+// expected step count and width, cls[i]; 0xFF: not traced), so that a
+// warp's lanes march cones of one length that take one sampling path; with
+// the surrogate only the pairs it is not confident about are classified.
 // counters (zeroed before each light stage): [0] pairs claimed, [1] level-0
 // corner bytes, [2] mip records and [7] plain mip texels the cone pass read
-// (its counting instance only), [3] narrow and [4] wide cones in retrace,
-// [5] pairs the surrogate evaluated, [6] the cone pass's work cursor,
+// (its counting instance only), [3] pairs the surrogate left to the cone
+// ([4] zero), [5] pairs the surrogate evaluated, [6] the cone pass's work cursor,
 // [8 + c] pairs of class c, [8 + kConeClasses + c] class c's scatter cursor,
 // [kGatherUnitsCounter] the gather units listed in units.
 // The gather takes a cache's run in units of kGatherChunk pairs (units[u] =
@@ -128,7 +127,6 @@ struct PairList {
   uint32_t* block;
   float* shadow;
   uint32_t* order;
-  uint32_t* retrace;
   uint8_t* cls;
   uint32_t* info;
   uint32_t* counters;
@@ -227,7 +225,7 @@ struct Context {
   PairList pairs{};
   DrvTuning tuning{};
   // Events between the split light stage's kernels (DrvTuning.time_kernels).
-  cudaEvent_t lk_events[DRV_LK_COUNT + 1] = {};
+  cudaEvent_t lk_events[2 * DRV_LK_COUNT] = {};  // start and end of each light-stage kernel slot
   bool lk_recorded = false;
   // Visibility surrogate: packed BF16 inference weights and their feature set.
   void* sur_weights = nullptr;

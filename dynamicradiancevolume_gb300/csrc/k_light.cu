@@ -436,7 +436,9 @@ __device__ __forceinline__ int cone_class(float light_dist, float voxel_size, fl
 constexpr int kClassThreads = 256;
 
 // Thread per listed pair: its cone class; class totals in counters[8 + c].
-template <bool BF16>
+// MARKED: only the pairs the surrogate left unconfident (cls 0) get a class;
+// the others keep 0xFF and are neither ordered nor traced.
+template <bool BF16, bool MARKED>
 __global__ void __launch_bounds__(kClassThreads) classify_kernel(StageParams p, PairList L) {
   pdl_wait_and_release();
   __shared__ uint32_t s_hist[kConeClasses];
@@ -446,7 +448,7 @@ __global__ void __launch_bounds__(kClassThreads) classify_kernel(StageParams p, 
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const uint32_t b = L.block[i];
     uint8_t c = 0xFF;
-    if (b != kNoPair) {
+    if (b != kNoPair && (!MARKED || L.cls[i] != 0xFF)) {
       float cx, cy, cz;
       cache_position<BF16>(p, L.cache[i], cx, cy, cz);
       const int l = block_light(p, (int)b);
@@ -506,72 +508,50 @@ __global__ void __launch_bounds__(kClassThreads) scatter_kernel(PairList L) {
   }
 }
 
-// Thread per cone, over a cone-order list. RETRACE: L.retrace, its n_front
-// narrow cones from the front and n_back wide ones from the back; otherwise
-// L.order, every listed pair in class order. COUNT (a separate, measuring
-// instance): the voxel loads of all cones are summed into counters[1]
-// (level-0 corner bytes), [2] (16-byte mip records) and [7] (plain mip
-// texels).
-template <bool BF16, bool RETRACE, bool COUNT = false>
+// Thread per cone over L.order, the listed pairs in cone-class order (with
+// the surrogate, the pairs it left unconfident). COUNT (a separate,
+// measuring instance): the voxel loads of all cones are summed into
+// counters[1] (level-0 corner bytes), [2] (16-byte mip records) and [7]
+// (plain mip texels).
+template <bool BF16, bool COUNT = false>
 __global__ void __launch_bounds__(128) cone_kernel(StageParams p, PairList L) {
   pdl_wait_and_release();
-  uint32_t nf = 0, nb = 0;
-  if (RETRACE) {
-    nf = min(L.counters[3], L.cap);
-    nb = min(L.counters[4], L.cap);
-  } else {
+  uint32_t n = 0;
 #pragma unroll
-    for (int c = 0; c < kConeClasses; ++c) nf += L.counters[8 + c];
-  }
-  const uint32_t* ord = RETRACE ? L.retrace : L.order;
-  const uint32_t n = min(nf + nb, L.cap);
+  for (int c = 0; c < kConeClasses; ++c) n += L.counters[8 + c];
+  n = min(n, L.cap);
   typename std::conditional<COUNT, VoxelReads, NoReads>::type reads;
-  auto flush_reads = [&]() {
-    if constexpr (COUNT) {
-      uint32_t a = reads.level0_bytes, b = reads.records, c = reads.texels;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        a += __shfl_xor_sync(0xffffffffu, a, o);
-        b += __shfl_xor_sync(0xffffffffu, b, o);
-        c += __shfl_xor_sync(0xffffffffu, c, o);
-      }
-      if ((threadIdx.x & 31) == 0) {
-        atomicAdd(L.counters + 1, a);
-        atomicAdd(L.counters + 2, b);
-        atomicAdd(L.counters + 7, c);
-      }
-    }
-  };
-  if (!RETRACE) {
-    // Warps take 32 cones at a time from counters[6], from the end of the
-    // class order (the longest cones) to its start, so the short cones fill
-    // the tail of the pass.
-    const int lane = threadIdx.x & 31;
-    for (;;) {
-      uint32_t base = 0;
-      if (lane == 0) base = atomicAdd(L.counters + 6, 32u);
-      base = __shfl_sync(0xffffffffu, base, 0);
-      if (base >= n) break;
-      if (base + lane >= n) continue;
-      const uint32_t i = ord[n - 1u - (base + lane)];
-      const uint32_t b = L.block[i];
-      if (b == kNoPair) continue;
-      float cx, cy, cz;
-      cache_position<BF16>(p, L.cache[i], cx, cy, cz);
-      L.shadow[i] = block_cone(p, (int)b, cx, cy, cz, reads);
-    }
-    flush_reads();
-    return;
-  }
-  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-    const uint32_t i = k < nf ? ord[k] : ord[L.cap - 1u - (k - nf)];
+  // Warps take 32 cones at a time from counters[6], from the end of the
+  // class order (the longest cones) to its start, so the short cones fill
+  // the tail of the pass.
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(L.counters + 6, 32u);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= n) break;
+    if (base + lane >= n) continue;
+    const uint32_t i = L.order[n - 1u - (base + lane)];
     const uint32_t b = L.block[i];
     if (b == kNoPair) continue;
     float cx, cy, cz;
     cache_position<BF16>(p, L.cache[i], cx, cy, cz);
     L.shadow[i] = block_cone(p, (int)b, cx, cy, cz, reads);
   }
-  flush_reads();
+  if constexpr (COUNT) {
+    uint32_t a = reads.level0_bytes, b = reads.records, c = reads.texels;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_xor_sync(0xffffffffu, a, o);
+      b += __shfl_xor_sync(0xffffffffu, b, o);
+      c += __shfl_xor_sync(0xffffffffu, c, o);
+    }
+    if (lane == 0) {
+      atomicAdd(L.counters + 1, a);
+      atomicAdd(L.counters + 2, b);
+      atomicAdd(L.counters + 7, c);
+    }
+  }
 }
 
 // Sum over the warp of each lane's v[0..N-1] (N = 16 or 32), returned in
@@ -965,9 +945,10 @@ cudaError_t set_max_smem(const void* kernel, size_t bytes) {
   return e;
 }
 
-// events (optional, DRV_LK_COUNT + 1): recorded before the first kernel and
-// after each kernel slot, skipped slots included, so slot k's time is
-// elapsed(events[k], events[k + 1]).
+// events (optional, 2 x DRV_LK_COUNT): slot k's kernel runs between
+// events[2k] and events[2k + 1] (both recorded back to back for a slot the
+// stage skips), so its time is elapsed(events[2k], events[2k + 1]) whatever
+// order the slots run in.
 template <int NK, bool BF16>
 cudaError_t split_variant(cudaStream_t s, const StageParams& p, const PairList& L, const SurrogateArgs& sur,
                           const SplitKnobs& knobs, int num_sms, cudaEvent_t* ev, cudaEvent_t voxels_ready) {
@@ -976,9 +957,14 @@ cudaError_t split_variant(cudaStream_t s, const StageParams& p, const PairList& 
   // Only the cone pass and the surrogate's features read the voxels: with
   // voxels_ready, the cull and the ordering passes overlap the voxel build.
   auto wait_voxels = [&]() { return voxels_ready ? cudaStreamWaitEvent(s, voxels_ready, 0) : cudaSuccess; };
-  auto mark = [&](int k) { return ev ? cudaEventRecord(ev[k], s) : cudaSuccess; };
+  auto begin = [&](int k) { return ev ? cudaEventRecord(ev[2 * k], s) : cudaSuccess; };
+  auto end = [&](int k) { return ev ? cudaEventRecord(ev[2 * k + 1], s) : cudaSuccess; };
+  auto skip = [&](int k) {
+    cudaError_t r = begin(k);
+    return r == cudaSuccess ? end(k) : r;
+  };
   cudaError_t e = cudaMemsetAsync(L.counters, 0, kPairCounters * sizeof(uint32_t), s);
-  if (e != cudaSuccess || (e = mark(DRV_LK_CULL)) != cudaSuccess) return e;
+  if (e != cudaSuccess || (e = begin(DRV_LK_CULL)) != cudaSuccess) return e;
   int total_vpls = 0;
   for (int l = 0; l < p.ll.n_lights; ++l) total_vpls += p.ll.lights[l].n_vpls;
   const int words = (p.total_blocks + 31) >> 5;
@@ -997,28 +983,26 @@ cudaError_t split_variant(cudaStream_t s, const StageParams& p, const PairList& 
     const size_t cull_smem = (size_t)words * 2 * sizeof(uint32_t);
     e = launch_persistent(cull_kernel<BF16>, kCullThreads, cull_smem, s, num_sms, p, L);
   }
-  if (e != cudaSuccess) return e;
-  if ((e = mark(DRV_LK_CLASSIFY)) != cudaSuccess) return e;
-  if (!sur.weights) {
-    if ((e = launch_persistent_after(classify_kernel<BF16>, kClassThreads, 0, s, num_sms, p, L)) != cudaSuccess)
-      return e;
-    if ((e = mark(DRV_LK_SCATTER)) != cudaSuccess) return e;
-    if ((e = launch_persistent_after(scatter_kernel, kClassThreads, 0, s, num_sms, L)) != cudaSuccess) return e;
-    if ((e = mark(DRV_LK_MLP)) != cudaSuccess || (e = wait_voxels()) != cudaSuccess ||
-        (e = mark(DRV_LK_CONE)) != cudaSuccess)
-      return e;
-    e = count_reads ? launch_grid(cone_kernel<BF16, false, true>, 128, 0, s, num_sms, cone_ctas, true, p, L)
-                    : launch_grid(cone_kernel<BF16, false>, 128, 0, s, num_sms, cone_ctas, true, p, L);
-  } else {
-    if ((e = mark(DRV_LK_SCATTER)) != cudaSuccess || (e = wait_voxels()) != cudaSuccess ||
-        (e = mark(DRV_LK_MLP)) != cudaSuccess)
-      return e;
+  if (e != cudaSuccess || (e = end(DRV_LK_CULL)) != cudaSuccess) return e;
+  if (sur.weights) {
+    // The MLP first: it sets the confident pairs' shadowing and marks the
+    // others (cls 0); only those are classified, ordered and traced below.
+    if ((e = wait_voxels()) != cudaSuccess || (e = begin(DRV_LK_MLP)) != cudaSuccess) return e;
     if ((e = launch_surrogate_mlp(s, p, L, sur, BF16, num_sms)) != cudaSuccess) return e;
-    if ((e = mark(DRV_LK_CONE)) != cudaSuccess) return e;
-    e = count_reads ? launch_grid(cone_kernel<BF16, true, true>, 128, 0, s, num_sms, cone_ctas, true, p, L)
-                    : launch_grid(cone_kernel<BF16, true>, 128, 0, s, num_sms, cone_ctas, true, p, L);
+    if ((e = end(DRV_LK_MLP)) != cudaSuccess) return e;
   }
-  if (e != cudaSuccess || (e = mark(DRV_LK_GATHER)) != cudaSuccess) return e;
+  if ((e = begin(DRV_LK_CLASSIFY)) != cudaSuccess) return e;
+  e = sur.weights ? launch_persistent_after(classify_kernel<BF16, true>, kClassThreads, 0, s, num_sms, p, L)
+                  : launch_persistent_after(classify_kernel<BF16, false>, kClassThreads, 0, s, num_sms, p, L);
+  if (e != cudaSuccess || (e = end(DRV_LK_CLASSIFY)) != cudaSuccess) return e;
+  if ((e = begin(DRV_LK_SCATTER)) != cudaSuccess) return e;
+  if ((e = launch_persistent_after(scatter_kernel, kClassThreads, 0, s, num_sms, L)) != cudaSuccess) return e;
+  if ((e = end(DRV_LK_SCATTER)) != cudaSuccess) return e;
+  if (!sur.weights && ((e = skip(DRV_LK_MLP)) != cudaSuccess || (e = wait_voxels()) != cudaSuccess)) return e;
+  if ((e = begin(DRV_LK_CONE)) != cudaSuccess) return e;
+  e = count_reads ? launch_grid(cone_kernel<BF16, true>, 128, 0, s, num_sms, cone_ctas, true, p, L)
+                  : launch_grid(cone_kernel<BF16, false>, 128, 0, s, num_sms, cone_ctas, true, p, L);
+  if (e != cudaSuccess || (e = end(DRV_LK_CONE)) != cudaSuccess || (e = begin(DRV_LK_GATHER)) != cudaSuccess) return e;
   {
     const uint32_t staged = gather_staged_vpls(p.ll, BF16);
     const size_t smem = (size_t)staged * vpl_bytes<BF16>();
@@ -1028,7 +1012,7 @@ cudaError_t split_variant(cudaStream_t s, const StageParams& p, const PairList& 
                     true, p, L, staged, knobs.gather_wait_test);
   }
   if (e != cudaSuccess) return e;
-  return mark(DRV_LK_COUNT);
+  return end(DRV_LK_GATHER);
 }
 
 }  // namespace

@@ -14,9 +14,10 @@
 //     applies GELU on bf16x2 pairs and writes the activations over its row
 //     of the A tile: the next layer's A operand. Four layers; the fourth has
 //     N = 16 (the two outputs and zero rows);
-//  4. confident pairs store sigmoid(visibility) as their shadowing, the
-//     others go to the re-trace list (narrow cones at its front, wide ones at
-//     its back) that cone_kernel then traces.
+//  4. confident pairs store sigmoid(visibility) as their shadowing; the
+//     others are marked (cls 0) for the classify pass, which orders them by
+//     cone class like every pair of the plain stage, and cone_kernel traces
+//     them.
 // The weights (27 KB of BF16 B operands) are staged once per CTA by one bulk
 // asynchronous copy (cp.async.bulk, completion on an mbarrier).
 //
@@ -206,7 +207,7 @@ struct PairRows {
   __device__ uint32_t rows() const { return min(L.counters[0], L.cap); }
 
   // Writes the row's 32 inputs; false for an empty list slot (inputs 0).
-  __device__ bool features(uint32_t i, float* f, bool& wide) const {
+  __device__ bool features(uint32_t i, float* f) const {
     const uint32_t b = L.block[i];
     if (b == kNoPair) return false;
     float cx, cy, cz;
@@ -218,30 +219,20 @@ struct PairRows {
     const VplData v = load_vpl<BF16>(la.vpls, lb * la.interval);
     pair_features<FS>(p.vox, p.inv_extent, p.vol_min, p.voxel_size, p.max_steps, cx, cy, cz, cone.x, cone.y, cone.z,
                       v.nx, v.ny, v.nz, cone.w, f);
-    wide = wide_cone(cone.w, p.max_steps);
     return true;
   }
 
   // Called by every thread of a warp (rows past the end are not valid);
   // `evaluated` counts this thread's warp's valid rows (lane 0's copy).
-  __device__ void finish(uint32_t i, bool valid, bool wide, float o_vis, float o_conf, uint32_t& evaluated) const {
+  __device__ void finish(uint32_t i, bool valid, float o_vis, float o_conf, uint32_t& evaluated) const {
     const int lane = threadIdx.x & 31;
     const float vis = sigmoidf(o_vis), conf = sigmoidf(o_conf);
     const bool retrace = valid && !(conf >= threshold);
     if (valid && !retrace) L.shadow[i] = vis;
-    const uint32_t mn = __ballot_sync(0xffffffffu, retrace && !wide), mw = __ballot_sync(0xffffffffu, retrace && wide);
-    if (mn | mw) {
-      uint32_t fn = 0, fw = 0;
-      if (lane == 0) {
-        if (mn) fn = atomicAdd(L.counters + 3, (uint32_t)__popc(mn));
-        if (mw) fw = atomicAdd(L.counters + 4, (uint32_t)__popc(mw));
-      }
-      fn = __shfl_sync(0xffffffffu, fn, 0);
-      fw = __shfl_sync(0xffffffffu, fw, 0);
-      const uint32_t below = (1u << lane) - 1u;
-      if (retrace && !wide) L.retrace[fn + __popc(mn & below)] = i;
-      if (retrace && wide) L.retrace[L.cap - 1u - (fw + __popc(mw & below))] = i;
-    }
+    // cls 0: classified, ordered and traced after this pass; 0xFF: done
+    if (valid) L.cls[i] = retrace ? (uint8_t)0 : (uint8_t)0xFF;
+    const uint32_t m = __ballot_sync(0xffffffffu, retrace);
+    if (lane == 0 && m) atomicAdd(L.counters + 3, (uint32_t)__popc(m));
     evaluated += (uint32_t)__popc(__ballot_sync(0xffffffffu, valid));
   }
 
@@ -258,7 +249,7 @@ struct GivenRows {
   float* out;
 
   __device__ uint32_t rows() const { return n; }
-  __device__ bool features(uint32_t i, float* f, bool& wide) const {
+  __device__ bool features(uint32_t i, float* f) const {
     const float4* x = reinterpret_cast<const float4*>(X + (size_t)i * kMlpIn);
 #pragma unroll
     for (int k = 0; k < kMlpIn / 4; ++k) {
@@ -269,10 +260,9 @@ struct GivenRows {
       f[4 * k + 3] = q.w;
     }
     f[kOneInput] = 1.0f;
-    wide = false;
     return true;
   }
-  __device__ void finish(uint32_t i, bool valid, bool, float o_vis, float o_conf, uint32_t&) const {
+  __device__ void finish(uint32_t i, bool valid, float o_vis, float o_conf, uint32_t&) const {
     if (valid) {
       out[2 * (size_t)i] = sigmoidf(o_vis);
       out[2 * (size_t)i + 1] = sigmoidf(o_conf);
@@ -359,10 +349,10 @@ __global__ void __launch_bounds__(kThreads, 4) mlp_tc_kernel(Rows src, const uin
 
   for (uint32_t tile = blockIdx.x; tile < n_tiles && !abort; tile += gridDim.x) {
     const uint32_t row = tile * kThreads + tid;
-    bool wide = false, valid = false;
+    bool valid = false;
     {
       float f[kMlpIn];
-      if (row < n_rows) valid = src.features(row, f, wide);
+      if (row < n_rows) valid = src.features(row, f);
       if (!valid) {
 #pragma unroll
         for (int k = 0; k < kMlpIn; ++k) f[k] = 0.0f;
@@ -383,7 +373,7 @@ __global__ void __launch_bounds__(kThreads, 4) mlp_tc_kernel(Rows src, const uin
     if (!abort && !(abort = !layer(kW4Off, sbo_a, kKH / 16, instr_desc(kN4)))) {
       float o_vis, o_conf;
       tmem_ld2(t_row, o_vis, o_conf);
-      src.finish(row, valid && row < n_rows, wide, o_vis, o_conf, evaluated);
+      src.finish(row, valid && row < n_rows, o_vis, o_conf, evaluated);
     }
   }
   if (abort) {

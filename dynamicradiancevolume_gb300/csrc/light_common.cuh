@@ -61,7 +61,7 @@ StageParams make_stage_params(const DrvConfig& cfg, const DrvVolumeInfo& vol, co
                               const VoxelInputs& vox);
 
 // Host: the surrogate's pass over the pair list (k_light_surrogate.cu):
-// shadowing of the confident pairs, the others appended to L.retrace.
+// shadowing of the confident pairs, the others marked (cls 0) for the cone.
 cudaError_t launch_surrogate_mlp(cudaStream_t s, const StageParams& p, const PairList& L, const SurrogateArgs& sa,
                                  bool bf16, int num_sms);
 
@@ -118,14 +118,6 @@ __device__ __forceinline__ int block_light(const StageParams& p, int b) {
   int l = 0;
   while (b >= p.block_base[l + 1]) ++l;
   return l;
-}
-
-// True when a cone of this aperture (dsr: sample radius per unit distance)
-// may sample above voxel level 0 within max_steps steps, i.e. its radius
-// passes one voxel. Cones are traced in two groups by this test so that the
-// lanes of a warp take the same sampling path; results do not depend on it.
-__device__ __forceinline__ bool wide_cone(float dsr, int max_steps) {
-  return dsr * (float)(max_steps + 2) > 1.0f;
 }
 
 // World position of cache c (BF16 entries hold the packed cell key).

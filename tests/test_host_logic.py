@@ -43,7 +43,7 @@ def test_autotune_descends_each_knob_and_leaves_the_best_set(monkeypatch):
 def test_light_stage_launch_count():
     ns = pipeline.WORKLOADS["ns_1080p_4096"]
     assert bench.light_stage_launches(ns) == 5  # cull, classify, scatter, cone, gather
-    assert bench.light_stage_launches(ns, surrogate=True) == 4  # cull, MLP, cone, gather
+    assert bench.light_stage_launches(ns, surrogate=True) == 6  # cull, MLP, classify, scatter, cone, gather
     assert bench.light_stage_launches(pipeline.scaled(ns, indirect_shadow=0)) == 1
 
 
