@@ -27,6 +27,15 @@ __device__ __forceinline__ float2 add2(float2 a, float2 b) {
       : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
   return d;
 }
+// a + b rounded toward -infinity, both halves.
+__device__ __forceinline__ float2 add2_rm(float2 a, float2 b) {
+  float2 d;
+  asm("{\n.reg .b64 a, b, d;\nmov.b64 a, {%2, %3};\nmov.b64 b, {%4, %5};\nadd.rm.f32x2 d, a, b;\n"
+      "mov.b64 {%0, %1}, d;\n}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
 __device__ __forceinline__ float2 sub2(float2 a, float2 b) {
   float2 d;
   asm("{\n.reg .b64 a, b, d;\nmov.b64 a, {%2, %3};\nmov.b64 b, {%4, %5};\nsub.rn.f32x2 d, a, b;\n"

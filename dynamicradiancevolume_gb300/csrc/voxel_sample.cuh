@@ -107,11 +107,26 @@ __device__ __forceinline__ Coord level_coord(const Coord& U, int level) {
 // below 0 both taps clamp to texel 0, at or above n - 1 both clamp to n - 1;
 // clamping u itself to [0, n - 1] gives the same sample, because the
 // corner-packed byte / record at n - 1 repeats texel n - 1 for the +1 tap.
-__device__ __forceinline__ int tap(float u, float nm1, float& a) {
-  const float c = fminf(fmaxf(u, 0.0f), nm1);
-  const float f = floorf(c);
-  a = c - f;
-  return (int)f;
+//
+// The floor is taken without a float-to-int conversion: for 0 <= c < 2^23,
+// c + 2^23 rounded toward -infinity is 2^23 + floor(c) exactly (floats in
+// [2^23, 2^24) are the integers), so subtracting 2^23 gives floor(c) and the
+// bit pattern minus that of 2^23 gives it as an integer. The x and y taps go
+// in one packed pair.
+struct Taps {
+  int x, y, z;
+  float ax, ay, az;
+};
+__device__ __forceinline__ Taps taps(float ux, float uy, float uz, float nm1) {
+  constexpr float kTwo23 = 8388608.0f;
+  constexpr int kTwo23Bits = 0x4B000000;
+  const float2 c = make_float2(fminf(fmaxf(ux, 0.0f), nm1), fminf(fmaxf(uy, 0.0f), nm1));
+  const float cz = fminf(fmaxf(uz, 0.0f), nm1);
+  const float2 t = add2_rm(c, make_float2(kTwo23, kTwo23));
+  const float tz = __fadd_rd(cz, kTwo23);
+  const float2 a = sub2(c, sub2(t, make_float2(kTwo23, kTwo23)));
+  return Taps{__float_as_int(t.x) - kTwo23Bits, __float_as_int(t.y) - kTwo23Bits, __float_as_int(tz) - kTwo23Bits,
+              a.x, a.y, cz - (tz - kTwo23)};
 }
 
 // n - 1 as a float for a level of n = 2^ln texels.
@@ -133,10 +148,9 @@ __device__ __forceinline__ float level0_taps(const VoxelView& v, int x, int y, i
 // Level 0 at position U (texel coordinate U - 0.5, exact).
 template <class R>
 __device__ __forceinline__ float level0_at(const VoxelView& v, const Coord& U, R& reads) {
-  const float nm1 = last_texel(v.log2n);
-  float ax, ay, az;
-  const int x = tap(U.x - 0.5f, nm1, ax), y = tap(U.y - 0.5f, nm1, ay), z = tap(U.z - 0.5f, nm1, az);
-  return level0_taps(v, x, y, z, ax, ay, az, reads);
+  const float2 uxy = add2(make_float2(U.x, U.y), make_float2(-0.5f, -0.5f));
+  const Taps t = taps(uxy.x, uxy.y, U.z - 0.5f, last_texel(v.log2n));
+  return level0_taps(v, t.x, t.y, t.z, t.ax, t.ay, t.az, reads);
 }
 
 template <class R>
@@ -176,10 +190,9 @@ template <class R>
 __device__ __forceinline__ float level_record_at(const VoxelView& v, int level, const Coord& u, bool& zero,
                                                  R& reads) {
   reads.on_record();
-  const float nm1 = last_texel(v.log2n - level);
-  float ax, ay, az;
-  const int x = tap(u.x, nm1, ax), y = tap(u.y, nm1, ay), z = tap(u.z, nm1, az);
-  const uint4 r = __ldg(v.records + v.roff[level] + record_index(x, y, z, v.log2n - level));
+  const Taps t = taps(u.x, u.y, u.z, last_texel(v.log2n - level));
+  const float ax = t.ax, ay = t.ay, az = t.az;
+  const uint4 r = __ldg(v.records + v.roff[level] + record_index(t.x, t.y, t.z, v.log2n - level));
   zero = (r.x | r.y | r.z | r.w) == 0u;  // FP16 +0 is the all-zero pattern; texels are >= 0
   if (zero) return 0.0f;
   const float t0 = __low2float(u32_as_half2(r.x)), t1 = __high2float(u32_as_half2(r.x));
