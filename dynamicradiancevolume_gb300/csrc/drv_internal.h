@@ -61,7 +61,7 @@ struct LightLaunch {
 
 // The voxel pyramid as the cone tracer reads it.
 struct VoxelInputs {
-  const uint8_t* corners = nullptr;     // level 0, corner-packed bytes in 4^3 bricks
+  const uint8_t* corners = nullptr;     // level 0, corner-packed bytes, x fastest
   const void* mips = nullptr;           // levels 1..L concatenated (float, or half with BF16 precision)
   const size_t* mip_offsets = nullptr;  // texel offset of each level in mips
   const uint4* records = nullptr;       // corner-packed mip records of levels 1..record_levels (optional)
@@ -183,7 +183,7 @@ struct Context {
   float* srgb = nullptr;  // the GL sRGB decode of the 256 byte values (DRV_ALBEDO_SRGB8)
   unsigned long long* raster_keys = nullptr;  // mesh producers' per-pixel visibility (drv_raster_*)
   size_t raster_keys_cap = 0;
-  uint8_t* vox_corners = nullptr;  // level 0, corner-packed bytes in 4^3 bricks
+  uint8_t* vox_corners = nullptr;  // level 0, corner-packed bytes, x fastest
   void* mips = nullptr;  // levels 1..L concatenated: float (FP32 precision) or half (BF16 precision)
   size_t mip_offset[kMaxVoxelLevels] = {};
   uint4* vox_records = nullptr;  // corner-packed mip records (voxel_sample.cuh)

@@ -352,17 +352,18 @@ __global__ void __launch_bounds__(256) mips_tail_kernel(int N, int first_level, 
 
 // Corner-packed level 0 (see voxel_sample.cuh): byte (x, y, z) = the 8 voxels
 // (x + dx, y + dy, z + dz) with +1 clamped to N - 1, bit dx | dy << 1 | dz << 2,
-// stored in 4x4x4 bricks. One thread per brick: it reads the 5x5 rows of the
-// brick's 5x5x5 neighbourhood from the bitmask and writes its 64 bytes as four
-// 16-byte stores (consecutive threads write consecutive bricks).
+// x fastest. One thread per 4x4x4 block: it reads the 5x5 rows of the
+// block's 5x5x5 neighbourhood from the bitmask and writes its 16 rows of 4
+// bytes (consecutive threads take consecutive blocks along x, so each of the
+// 16 stores of a warp writes 128 contiguous bytes).
 __global__ void __launch_bounds__(256) corners_kernel(int N, int log2n, const uint32_t* __restrict__ bits,
                                                       uint8_t* __restrict__ out) {
   const int lnb = log2n - 2, nb = N >> 2;
-  const uint32_t brick = blockIdx.x * blockDim.x + threadIdx.x;
-  if (brick >= (uint32_t)nb * nb * nb) return;
-  const int x0 = (int)(brick & (nb - 1)) * 4;
-  const int y0 = (int)((brick >> lnb) & (nb - 1)) * 4;
-  const int z0 = (int)(brick >> (2 * lnb)) * 4;
+  const uint32_t blk = blockIdx.x * blockDim.x + threadIdx.x;
+  if (blk >= (uint32_t)nb * nb * nb) return;
+  const int x0 = (int)(blk & (nb - 1)) * 4;
+  const int y0 = (int)((blk >> lnb) & (nb - 1)) * 4;
+  const int z0 = (int)(blk >> (2 * lnb)) * 4;
   const int wpr = N >> 5;
   // rows[dz][dy] = 5 voxel bits x0..x0+4 (x0+4 clamped) of row (y0+dy, z0+dz), clamped
   uint32_t rows[5][5];
@@ -397,15 +398,18 @@ __global__ void __launch_bounds__(256) corners_kernel(int N, int log2n, const ui
       }
       words[lz * 4 + ly] = wv;
     }
-  uint4* dst = reinterpret_cast<uint4*>(out + (size_t)brick * 64);
 #pragma unroll
-  for (int q = 0; q < 4; ++q) dst[q] = make_uint4(words[4 * q], words[4 * q + 1], words[4 * q + 2], words[4 * q + 3]);
+  for (int lz = 0; lz < 4; ++lz)
+#pragma unroll
+    for (int ly = 0; ly < 4; ++ly)
+      *reinterpret_cast<uint32_t*>(out + ((size_t)(z0 + lz) * N + (y0 + ly)) * N + x0) = words[lz * 4 + ly];
 }
 
-// Corner-packed mip records (voxel_sample.cuh): one thread per 2x2x2 brick
-// of records of one level (blockIdx.y = level - 1). It reads the 3x3x3
-// texels its 8 records cover (+1 clamped) once and writes the brick's 128
-// bytes. Records hold FP16 texels: a copy with BF16 precision; with FP32
+// Corner-packed mip records (voxel_sample.cuh), x fastest: one thread per
+// 2x2x2 block of records of one level (blockIdx.y = level - 1). It reads the
+// 3x3x3 texels its 8 records cover (+1 clamped) once and writes the 8
+// records (consecutive threads take consecutive blocks along x, so a warp's
+// record pairs (x0, x0 + 1) fill contiguous rows). Records hold FP16 texels: a copy with BF16 precision; with FP32
 // precision the records cover levels 1..3, whose texels k / 8^l (8^l <= 512)
 // FP16 holds exactly.
 struct RecordLevels {
@@ -420,50 +424,35 @@ __device__ __forceinline__ uint32_t half_bits(__half v) { return (uint32_t)__hal
 template <typename T>
 __global__ void __launch_bounds__(256) records_kernel(const T* __restrict__ mips, MipOffsets mo, RecordLevels rl,
                                                       uint4* __restrict__ out) {
-  // A thread's 8 records go through shared memory (slot r of thread t at
-  // t * 8 + (r ^ (t & 7)), spreading the writes over the banks) so that each
-  // warp stores its 32 bricks' 4 KB as 8 fully coalesced 512-byte rows.
-  __shared__ uint4 s_rec[256 * 8];
   const int level = (int)blockIdx.y + 1;
   const int ln = rl.log2n - level, n = 1 << ln, lb = ln > 0 ? ln - 1 : 0, nb = 1 << lb;
-  const uint32_t n_bricks = (uint32_t)nb * nb * nb;
-  const uint32_t brick = blockIdx.x * blockDim.x + threadIdx.x;
-  const int t = (int)threadIdx.x, lane = t & 31, warp0 = t & ~31;
-  if (blockIdx.x * blockDim.x + warp0 >= n_bricks) return;  // the whole warp is past the level
-  if (brick < n_bricks) {
-    const int x0 = (int)(brick & (nb - 1)) << 1, y0 = (int)((brick >> lb) & (nb - 1)) << 1,
-              z0 = (int)(brick >> (2 * lb)) << 1;
-    const T* src = mips + pick(mo.off, level);
-    uint32_t h[3][3][3];
+  const uint32_t block = blockIdx.x * blockDim.x + threadIdx.x;
+  if (block >= (uint32_t)nb * nb * nb) return;
+  const int x0 = (int)(block & (nb - 1)) << 1, y0 = (int)((block >> lb) & (nb - 1)) << 1,
+            z0 = (int)(block >> (2 * lb)) << 1;
+  const T* src = mips + pick(mo.off, level);
+  uint32_t h[3][3][3];
 #pragma unroll
-    for (int dz = 0; dz < 3; ++dz)
+  for (int dz = 0; dz < 3; ++dz)
 #pragma unroll
-      for (int dy = 0; dy < 3; ++dy) {
-        const T* row = src + ((size_t)min(z0 + dz, n - 1) * n + min(y0 + dy, n - 1)) * n;
+    for (int dy = 0; dy < 3; ++dy) {
+      const T* row = src + ((size_t)min(z0 + dz, n - 1) * n + min(y0 + dy, n - 1)) * n;
 #pragma unroll
-        for (int dx = 0; dx < 3; ++dx) h[dz][dy][dx] = half_bits(row[min(x0 + dx, n - 1)]);
-      }
-#pragma unroll
-    for (int r = 0; r < 8; ++r) {
-      const int rx = r & 1, ry = (r >> 1) & 1, rz = r >> 2;
-      uint32_t w[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int j0 = 2 * q, j1 = 2 * q + 1;  // slot j = dx | dy << 1 | dz << 2
-        w[q] = h[rz + (j0 >> 2)][ry + ((j0 >> 1) & 1)][rx + (j0 & 1)] |
-               h[rz + (j1 >> 2)][ry + ((j1 >> 1) & 1)][rx + (j1 & 1)] << 16;
-      }
-      s_rec[t * 8 + (r ^ (t & 7))] = make_uint4(w[0], w[1], w[2], w[3]);
+      for (int dx = 0; dx < 3; ++dx) h[dz][dy][dx] = half_bits(row[min(x0 + dx, n - 1)]);
     }
-  }
-  __syncwarp();
-  uint4* dst = out + pick(rl.off, level) + (size_t)(blockIdx.x * blockDim.x + warp0) * 8;
-  const uint32_t left = (n > 1 ? n_bricks * 8u : 1u) - (blockIdx.x * blockDim.x + warp0) * 8u;  // a 1-texel level has one record
+  uint4* dst = out + pick(rl.off, level);
 #pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    const int m = k * 32 + lane;  // record of the warp's 256
-    const int src_t = warp0 + (m >> 3), r = m & 7;
-    if ((uint32_t)m < left) dst[m] = s_rec[src_t * 8 + (r ^ (src_t & 7))];
+  for (int r = 0; r < 8; ++r) {
+    const int rx = r & 1, ry = (r >> 1) & 1, rz = r >> 2;
+    if (x0 + rx >= n || y0 + ry >= n || z0 + rz >= n) continue;  // a 1-texel level has one record
+    uint32_t w[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int j0 = 2 * q, j1 = 2 * q + 1;  // slot j = dx | dy << 1 | dz << 2
+      w[q] = h[rz + (j0 >> 2)][ry + ((j0 >> 1) & 1)][rx + (j0 & 1)] |
+             h[rz + (j1 >> 2)][ry + ((j1 >> 1) & 1)][rx + (j1 & 1)] << 16;
+    }
+    dst[((size_t)(z0 + rz) * n + (y0 + ry)) * n + x0 + rx] = make_uint4(w[0], w[1], w[2], w[3]);
   }
 }
 
@@ -478,7 +467,7 @@ cudaError_t launch_build_records(cudaStream_t s, int n, const void* mips, const 
   for (int i = 0; i <= record_levels && i <= kMaxVoxelLevels; ++i) rl.off[i] = record_offsets[i];
   rl.levels = record_levels;
   while ((1 << (rl.log2n + 1)) <= n) ++rl.log2n;
-  const uint32_t nb = (uint32_t)(n >> 2) > 0 ? (uint32_t)(n >> 2) : 1u;  // bricks per axis at level 1
+  const uint32_t nb = (uint32_t)(n >> 2) > 0 ? (uint32_t)(n >> 2) : 1u;  // 2x2x2 record blocks per axis at level 1
   const dim3 grid((nb * nb * nb + 255) / 256, record_levels);
   if (precision == DRV_PRECISION_BF16)
     records_kernel<__half><<<grid, 256, 0, s>>>((const __half*)mips, mo, rl, records);
@@ -490,8 +479,8 @@ cudaError_t launch_build_records(cudaStream_t s, int n, const void* mips, const 
 cudaError_t launch_build_corners(cudaStream_t s, int n, const uint32_t* bits, uint8_t* corners) {
   int l = 0;
   while ((1 << (l + 1)) <= n) ++l;
-  const uint32_t bricks = (uint32_t)(n / 4) * (n / 4) * (n / 4);
-  corners_kernel<<<(bricks + 255) / 256, 256, 0, s>>>(n, l, bits, corners);
+  const uint32_t blocks = (uint32_t)(n / 4) * (n / 4) * (n / 4);
+  corners_kernel<<<(blocks + 255) / 256, 256, 0, s>>>(n, l, bits, corners);
   return cudaGetLastError();
 }
 

@@ -49,9 +49,10 @@ inline VoxelView make_voxel_view(const DrvConfig& cfg, const VoxelInputs& in) {
   v.max_level = L;
   v.half_mips = cfg.precision == DRV_PRECISION_BF16;
   v.records = in.records;
+  v.cbias = 0u - tap_index_bias(L);
   v.record_levels = in.records && in.record_offsets ? in.record_levels : 0;
   for (int i = 0; i < 16; ++i)
-    v.roff[i] = v.record_levels && i <= v.record_levels ? in.record_offsets[i] : 0u;
+    v.roff[i] = v.record_levels && i >= 1 && i <= v.record_levels ? in.record_offsets[i] - tap_index_bias(L - i) : 0u;
   return v;
 }
 

@@ -7,13 +7,12 @@
 //
 // Level 0 is read from the corner-packed byte grid: byte (x, y, z) holds the
 // 8 voxels (x + dx, y + dy, z + dz), dx,dy,dz in {0,1}, with +1 clamped to the
-// last voxel, stored in 4x4x4 bricks of 64 bytes, so one trilinear level-0
-// sample is one byte load. Levels >= 1 are FP32 arrays (x fastest) and, where
-// the context built them, corner-packed records of the same values: record
-// (x, y, z) of level l holds the 8 texels (x + dx, y + dy, z + dz), +1 clamped,
-// slot dx | dy << 1 | dz << 2, as FP16, 16 bytes, in 2x2x2 bricks (one
-// 128-byte line), so one trilinear mip sample is one 16-byte load instead of
-// eight. With BF16 precision the texels are FP16 anyway and every level has
+// last voxel, x fastest, so one trilinear level-0 sample is one byte load.
+// Levels >= 1 are FP32 arrays (x fastest) and, where the context built them,
+// corner-packed records of the same values: record (x, y, z) of level l holds
+// the 8 texels (x + dx, y + dy, z + dz), +1 clamped, slot dx | dy << 1 |
+// dz << 2, as FP16, 16 bytes, x fastest, so one trilinear mip sample is one
+// 16-byte load instead of eight. With BF16 precision the texels are FP16 anyway and every level has
 // records; with FP32 precision levels 1..3 have them: a level-l texel is
 // k / 8^l (a mean of means of binary voxels) and FP16 holds it exactly for
 // 8^l <= 512, so the sample is the same FP32 value bit for bit.
@@ -27,16 +26,27 @@
 
 namespace drv {
 
+// The sampler's taps are integer texel coordinates plus kTapBias (the bit
+// pattern of 2^23, see taps()); the linear index x + (y << ln) + (z << 2 ln)
+// of a level of 2^ln texels per axis, computed from biased taps in 32-bit
+// arithmetic, is the true index plus tap_index_bias(ln) modulo 2^32, which
+// the view's offsets subtract in advance.
+constexpr uint32_t kTapBias = 0x4B000000u;
+__host__ __device__ constexpr uint32_t tap_index_bias(int ln) {
+  return kTapBias * (1u + (1u << ln) + (1u << (2 * ln)));
+}
+
 struct VoxelView {
-  const uint8_t* corners;  // level 0, N^3 bytes, bricked
+  const uint8_t* corners;  // level 0, N^3 bytes, x fastest
   const void* mips;        // levels 1..L concatenated: float, or __half when half_mips
   uint32_t off[16];        // offset (floats) of level l in `mips`
   int N;                   // level-0 resolution (power of two)
   int log2n;
   int max_level;           // L = log2(N)
   int half_mips;
+  uint32_t cbias;          // -tap_index_bias(log2n): corner index of biased taps
   const uint4* records;    // corner-packed mip records (nullptr: none)
-  uint32_t roff[16];       // offset (records) of level l in `records`
+  uint32_t roff[16];       // record offset of level l minus tap_index_bias(log2n - l)
   int record_levels;       // levels 1..record_levels have records
 };
 
@@ -81,13 +91,6 @@ __device__ __forceinline__ float mip_texel(const VoxelView& v, uint32_t i) {
                      : __ldg(static_cast<const float*>(v.mips) + i);
 }
 
-// Byte offset of voxel (x, y, z) in the bricked level-0 corner grid.
-__device__ __forceinline__ uint32_t corner_index(int x, int y, int z, int log2n) {
-  const int lnb = log2n - 2;  // bricks per axis = N / 4
-  uint32_t brick = ((uint32_t)((z >> 2) << lnb | (y >> 2)) << lnb) | (uint32_t)(x >> 2);
-  return (brick << 6) | (uint32_t)((z & 3) << 4 | (y & 3) << 2 | (x & 3));
-}
-
 // A sample position U in level-0 voxel units (U = s * N for texture
 // coordinate s; exact, N is a power of two). Level l reads texel coordinate
 // u_l = U * 2^-l - 0.5 = s * n_l - 0.5, one rounding (exact for |U| < 2^22),
@@ -110,33 +113,37 @@ __device__ __forceinline__ Coord level_coord(const Coord& U, int level) {
 //
 // The floor is taken without a float-to-int conversion: for 0 <= c < 2^23,
 // c + 2^23 rounded toward -infinity is 2^23 + floor(c) exactly (floats in
-// [2^23, 2^24) are the integers), so subtracting 2^23 gives floor(c) and the
-// bit pattern minus that of 2^23 gives it as an integer. The x and y taps go
-// in one packed pair.
+// [2^23, 2^24) are the integers), so subtracting 2^23 gives floor(c), and
+// the bit pattern is floor(c) + kTapBias: the biased tap. The x and y taps
+// go in one packed pair.
 struct Taps {
-  int x, y, z;
+  uint32_t x, y, z;  // texel + kTapBias
   float ax, ay, az;
 };
 __device__ __forceinline__ Taps taps(float ux, float uy, float uz, float nm1) {
   constexpr float kTwo23 = 8388608.0f;
-  constexpr int kTwo23Bits = 0x4B000000;
   const float2 c = make_float2(fminf(fmaxf(ux, 0.0f), nm1), fminf(fmaxf(uy, 0.0f), nm1));
   const float cz = fminf(fmaxf(uz, 0.0f), nm1);
   const float2 t = add2_rm(c, make_float2(kTwo23, kTwo23));
   const float tz = __fadd_rd(cz, kTwo23);
   const float2 a = sub2(c, sub2(t, make_float2(kTwo23, kTwo23)));
-  return Taps{__float_as_int(t.x) - kTwo23Bits, __float_as_int(t.y) - kTwo23Bits, __float_as_int(tz) - kTwo23Bits,
-              a.x, a.y, cz - (tz - kTwo23)};
+  return Taps{__float_as_uint(t.x), __float_as_uint(t.y), __float_as_uint(tz), a.x, a.y, cz - (tz - kTwo23)};
+}
+
+// Linear index x + (y << ln) + (z << 2 ln) of biased taps, plus `base`
+// (an offset that has the taps' bias subtracted).
+__device__ __forceinline__ uint32_t tap_index(const Taps& t, int ln, uint32_t base) {
+  return base + t.x + (t.y << ln) + (t.z << (2 * ln));
 }
 
 // n - 1 as a float for a level of n = 2^ln texels.
 __device__ __forceinline__ float last_texel(int ln) { return __uint_as_float((uint32_t)(127 + ln) << 23) - 1.0f; }
 
 template <class R>
-__device__ __forceinline__ float level0_taps(const VoxelView& v, int x, int y, int z, float ax, float ay, float az,
-                                             R& reads) {
+__device__ __forceinline__ float level0_taps(const VoxelView& v, const Taps& t, R& reads) {
   reads.on_level0();
-  const uint32_t b = __ldg(v.corners + corner_index(x, y, z, v.log2n));
+  const uint32_t b = __ldg(v.corners + tap_index(t, v.log2n, v.cbias));
+  const float ax = t.ax, ay = t.ay, az = t.az;
   // Trilinear weights sum to one, so eight equal corners give that value
   // exactly: empty space (the common case) costs no interpolation.
   if (b == 0u) return 0.0f;
@@ -149,8 +156,7 @@ __device__ __forceinline__ float level0_taps(const VoxelView& v, int x, int y, i
 template <class R>
 __device__ __forceinline__ float level0_at(const VoxelView& v, const Coord& U, R& reads) {
   const float2 uxy = add2(make_float2(U.x, U.y), make_float2(-0.5f, -0.5f));
-  const Taps t = taps(uxy.x, uxy.y, U.z - 0.5f, last_texel(v.log2n));
-  return level0_taps(v, t.x, t.y, t.z, t.ax, t.ay, t.az, reads);
+  return level0_taps(v, taps(uxy.x, uxy.y, U.z - 0.5f, last_texel(v.log2n)), reads);
 }
 
 template <class R>
@@ -170,14 +176,6 @@ __device__ __forceinline__ float level_n_at(const VoxelView& v, int level, const
   return trilerp(t0, t1, t2, t3, t4, t5, t6, t7, ax, ay, az);
 }
 
-// Record index of texel (x, y, z) in a level of 2^ln texels per axis:
-// 2x2x2 bricks of 8 records, bricks x fastest.
-__device__ __forceinline__ uint32_t record_index(int x, int y, int z, int ln) {
-  const int lb = max(ln - 1, 0);  // bricks per axis = 2^(ln-1); a 1-texel level has x = y = z = 0
-  const uint32_t brick = ((uint32_t)((z >> 1) << lb | (y >> 1)) << lb) | (uint32_t)(x >> 1);
-  return brick << 3 | (uint32_t)((z & 1) << 2 | (y & 1) << 1 | (x & 1));
-}
-
 __device__ __forceinline__ __half2 u32_as_half2(uint32_t w) {
   __half2 h;
   memcpy(&h, &w, 4);
@@ -192,7 +190,7 @@ __device__ __forceinline__ float level_record_at(const VoxelView& v, int level, 
   reads.on_record();
   const Taps t = taps(u.x, u.y, u.z, last_texel(v.log2n - level));
   const float ax = t.ax, ay = t.ay, az = t.az;
-  const uint4 r = __ldg(v.records + v.roff[level] + record_index(t.x, t.y, t.z, v.log2n - level));
+  const uint4 r = __ldg(v.records + tap_index(t, v.log2n - level, v.roff[level]));
   zero = (r.x | r.y | r.z | r.w) == 0u;  // FP16 +0 is the all-zero pattern; texels are >= 0
   if (zero) return 0.0f;
   const float t0 = __low2float(u32_as_half2(r.x)), t1 = __high2float(u32_as_half2(r.x));

@@ -339,7 +339,7 @@ typedef struct DrvBuffers {
   DrvCacheCounter* counter;
   uint32_t* voxel_bits;             /* level 0 as a bitmask, bit (x&31) of word ((z*N+y)*N+x)/32 */
   uint8_t* voxel_corners;           /* level 0 corner-packed: byte (x,y,z) = voxels (x+dx,y+dy,z+dz), +1 clamped,
-                                       bit dx|dy<<1|dz<<2, stored in 4x4x4 bricks of 64 bytes */
+                                       bit dx|dy<<1|dz<<2, at (z*N+y)*N+x */
   void* voxel_mips[16];             /* levels 1..L (index 1..L), float (FP32 precision) or half (BF16 precision) */
   int32_t n_voxel_levels;           /* levels including 0 */
   void* vpls[DRV_MAX_LIGHTS];       /* VPL array per light, Morton order: DrvVPL (FP32) or DrvVPLBF16 */
@@ -347,9 +347,9 @@ typedef struct DrvBuffers {
   int32_t n_vpls[DRV_MAX_LIGHTS];
   int32_t n_lights;
   void* voxel_mip_records[16];      /* levels 1..n_record_levels (index 1..): corner-packed 16-byte records, record
-                                       (x,y,z) = texels (x+dx,y+dy,z+dz) of the level, +1 clamped, slot dx|dy<<1|dz<<2,
-                                       2x2x2 bricks of 8 records; FP32 precision: u16 k = texel * 8^l (levels 1..5),
-                                       BF16 precision: the FP16 texels (every level) */
+                                       (x,y,z) = FP16 texels (x+dx,y+dy,z+dz) of the level, +1 clamped, slot
+                                       dx|dy<<1|dz<<2, at (z*n+y)*n+x; FP32 precision: levels 1..3 (FP16 holds
+                                       their texels k / 8^l exactly), BF16 precision: every level */
   int32_t n_record_levels;
   /* The per-cache specular envmap atlas (m_specularEnvmap, renderer.cpp:253-
    * 287): n_specular_levels levels of specular_atlas_size >> level texels

@@ -184,18 +184,14 @@ def test_opacity_mips_exact(case, request, oracle):
 
 @pytest.mark.parametrize("case", ["c1", "c2r"])
 def test_corner_grid_matches_bits(case, request):
-    """The bricked corner-packed level-0 bytes repeat the bitmask exactly."""
+    """The corner-packed level-0 bytes (x fastest) repeat the bitmask exactly."""
     r = request.getfixturevalue(case)
     N = r.w.voxel_res
     b = r.pipe.buffers()
     g = r.pipe._dev_tensor(b.voxel_corners, N ** 3, r.torch.uint8).cpu().numpy()
     vox = np.unpackbits(r.bits.view(np.uint8), bitorder="little").reshape(N, N, N)  # [z][y][x]
     i = np.arange(N ** 3)
-    brick, inn = i >> 6, i & 63
-    nb = N // 4
-    x = (brick % nb) * 4 + (inn & 3)
-    y = ((brick // nb) % nb) * 4 + ((inn >> 2) & 3)
-    z = (brick // (nb * nb)) * 4 + (inn >> 4)
+    x, y, z = i % N, (i // N) % N, i // (N * N)
     exp = np.zeros(N ** 3, np.uint8)
     for k in range(8):
         xx = np.minimum(x + (k & 1), N - 1)
@@ -208,14 +204,10 @@ def test_corner_grid_matches_bits(case, request):
 def expected_records(level_texels, n):
     """Corner-packed mip records of one level (n texels per axis, x fastest
     input): 8 FP16 slots per record, slot dx | dy << 1 | dz << 2 = texel
-    (x + dx, y + dy, z + dz), +1 clamped; records in 2x2x2 bricks."""
+    (x + dx, y + dy, z + dz), +1 clamped; records x fastest."""
     t = np.asarray(level_texels).reshape(n, n, n)  # [z][y][x]
     i = np.arange(n ** 3)
-    inn, brick = i & 7, i >> 3
-    nb = max(n // 2, 1)
-    x = (brick % nb) * 2 + (inn & 1)
-    y = ((brick // nb) % nb) * 2 + ((inn >> 1) & 1)
-    z = (brick // (nb * nb)) * 2 + (inn >> 2)
+    x, y, z = i % n, (i // n) % n, i // (n * n)
     out = np.zeros((n ** 3, 8), np.uint16)
     for j in range(8):
         v = t[np.minimum(z + (j >> 2), n - 1), np.minimum(y + ((j >> 1) & 1), n - 1), np.minimum(x + (j & 1), n - 1)]
