@@ -219,7 +219,6 @@ __global__ void __launch_bounds__(kCullThreads) cull_kernel(StageParams p, PairL
 // tests of three FMAs each.
 constexpr int kCullRecThreads = 512;
 constexpr int kCullRecWarps = kCullRecThreads / 32;
-constexpr int kCullRecCaches = 4;  // default K
 constexpr size_t kCullRecMaxSmem = 220 * 1024;
 
 // Shared memory of cull_records_kernel: the records, then per cache of the
