@@ -38,9 +38,10 @@ METRIC = "caches lit/s and ms/frame at 1080p: plain vs surrogate, at ≤1% rel-L
 UNIT = "caches/s"
 
 # DRAM bytes (read + write) per launch of the light stage's top kernel at
-# ns_1080p_4096, from one `ncu --set full --clock-control none` capture
-# (cold caches) of `bench.py --steps 1 --warmup 1` at that workload.
-NCU_TRAFFIC = {"cone_kernel": 13_395_200}
+# ns_1080p_4096 (BF16), from one `ncu --set full --clock-control none`
+# capture (cold caches) of the second frame's launch of
+# `python -m dynamicradiancevolume_gb300.pipeline ns_1080p_4096 --precision bf16 --frames 2`.
+NCU_TRAFFIC = {"cone_kernel": 16_459_008}
 
 
 def parse():
@@ -752,10 +753,11 @@ def cone_roofline(r, cache_peaks, pk, w_name) -> dict:
             "l1": {"peak_gbs": l1, "frac": achieved / l1},
             "hbm": {"peak_gbs": pk["hbm_gbs"], "frac": achieved / pk["hbm_gbs"],
                     "peak_source": pk["source"] + " (hbm_gbs)",
-                    "note": "the voxel pyramid is L2-resident; one ncu capture of this pass read 13.4 MB "
+                    "note": "the voxel pyramid is L2-resident; one ncu capture of this pass read 16.5 MB "
                             "from DRAM per launch (profiles/)"},
-            "note": "the cone pass is issue-bound (73% issue active, ALU pipe 55%, 23.5 of 32 lanes active): "
-                    "its loads are a small share of either cache's throughput",
+            "note": "the cone pass is bound by issue and load latency (67% issue active, ALU pipe 43%, 23 of 32 "
+                    "lanes active, long_scoreboard the top stall): its loads are a small share of either cache's "
+                    "throughput",
             "gather": gather_roofline(r, pk)}
 
 

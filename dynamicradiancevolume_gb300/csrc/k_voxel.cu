@@ -352,69 +352,63 @@ __global__ void __launch_bounds__(256) mips_tail_kernel(int N, int first_level, 
 
 // Corner-packed level 0 (see voxel_sample.cuh): byte (x, y, z) = the 8 voxels
 // (x + dx, y + dy, z + dz) with +1 clamped to N - 1, bit dx | dy << 1 | dz << 2,
-// x fastest. One thread per 4x4x4 block: it reads the 5x5 rows of the
-// block's 5x5x5 neighbourhood from the bitmask and writes its 16 rows of 4
-// bytes (consecutive threads take consecutive blocks along x, so each of the
-// 16 stores of a warp writes 128 contiguous bytes).
+// x fastest. One thread per 16 bytes of a row: it reads bits x0..x0+16 of
+// the four voxel rows (y, z), (y+1, z), (y, z+1), (y+1, z+1) and writes one
+// 16-byte store (consecutive threads take consecutive 16-byte pieces, so a
+// warp writes 512 contiguous bytes).
+__device__ __forceinline__ uint32_t corner_row_bits(const uint32_t* __restrict__ bits, int N, int y, int z, int x0) {
+  // bits x0..x0+15 of row (y, z) and, in bit 16, voxel x0 + 16 (clamped to N - 1)
+  const uint32_t* row = bits + ((size_t)z * N + y) * (N >> 5);
+  const int w = x0 >> 5, sh = x0 & 31;  // sh is 0 or 16
+  const uint32_t a = __ldg(row + w);
+  const uint32_t r = (a >> sh) & 0xFFFFu;
+  uint32_t next;
+  if (x0 + 16 >= N) next = (r >> 15) & 1u;
+  else next = sh ? (__ldg(row + w + 1) & 1u) : ((a >> 16) & 1u);
+  return r | next << 16;
+}
+
 __global__ void __launch_bounds__(256) corners_kernel(int N, int log2n, const uint32_t* __restrict__ bits,
                                                       uint8_t* __restrict__ out) {
-  const int lnb = log2n - 2, nb = N >> 2;
-  const uint32_t blk = blockIdx.x * blockDim.x + threadIdx.x;
-  if (blk >= (uint32_t)nb * nb * nb) return;
-  const int x0 = (int)(blk & (nb - 1)) * 4;
-  const int y0 = (int)((blk >> lnb) & (nb - 1)) * 4;
-  const int z0 = (int)(blk >> (2 * lnb)) * 4;
-  const int wpr = N >> 5;
-  // rows[dz][dy] = 5 voxel bits x0..x0+4 (x0+4 clamped) of row (y0+dy, z0+dz), clamped
-  uint32_t rows[5][5];
+  const int lq = log2n - 4;  // 16-byte pieces per row = N / 16
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ((uint32_t)N * N << lq)) return;
+  const int x0 = (int)(t & ((1u << lq) - 1u)) << 4;
+  const int y = (int)((t >> lq) & (uint32_t)(N - 1)), z = (int)(t >> (lq + log2n));
+  const int y1 = min(y + 1, N - 1), z1 = min(z + 1, N - 1);
+  // rows[dy | dz << 1]
+  const uint32_t rows[4] = {corner_row_bits(bits, N, y, z, x0), corner_row_bits(bits, N, y1, z, x0),
+                            corner_row_bits(bits, N, y, z1, x0), corner_row_bits(bits, N, y1, z1, x0)};
+  // Word q holds bytes lx = 4q..4q+3; bit k of byte lx is voxel lx + (k & 1)
+  // of row k >> 1. Per k the four bits (one per byte) are spread to bit
+  // positions 0, 8, 16, 24 at once: the product r * 0x204081 places copies of
+  // the 4-bit r at shifts 0, 7, 14, 21 without carries, and the mask keeps
+  // bit j of the copy at shift 7j.
+  uint32_t words[4];
 #pragma unroll
-  for (int dz = 0; dz < 5; ++dz)
+  for (int q = 0; q < 4; ++q) {
+    uint32_t wv = 0;
 #pragma unroll
-    for (int dy = 0; dy < 5; ++dy) {
-      const int y = min(y0 + dy, N - 1), z = min(z0 + dz, N - 1);
-      const uint32_t* row = bits + ((size_t)z * N + y) * wpr;
-      const uint32_t w = __ldg(row + (x0 >> 5));
-      uint32_t r = (w >> (x0 & 31)) & 0xFu;
-      const int x4 = min(x0 + 4, N - 1);
-      const uint32_t w4 = (x4 >> 5) == (x0 >> 5) ? w : __ldg(row + (x4 >> 5));
-      r |= ((w4 >> (x4 & 31)) & 1u) << 4;
-      rows[dz][dy] = r;
+    for (int k = 0; k < 8; ++k) {
+      const uint32_t r = (rows[k >> 1] >> (4 * q + (k & 1))) & 0xFu;
+      wv |= ((r * 0x204081u) & 0x01010101u) << k;
     }
-  // Word (lz, ly) holds the bytes lx = 0..3; bit k of byte lx is voxel
-  // lx + (k & 1) of row (ly + (k >> 1 & 1), lz + (k >> 2)). Per k the four
-  // bits (one per lx) are spread to bit positions 0, 8, 16, 24 at once: the
-  // product r * 0x204081 places copies of the 4-bit r at shifts 0, 7, 14, 21
-  // without carries, and the mask keeps bit j of the copy at shift 7j.
-  uint32_t words[16];
-#pragma unroll
-  for (int lz = 0; lz < 4; ++lz)
-#pragma unroll
-    for (int ly = 0; ly < 4; ++ly) {
-      uint32_t wv = 0;
-#pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        const uint32_t r = (rows[lz + (k >> 2)][ly + ((k >> 1) & 1)] >> (k & 1)) & 0xFu;
-        wv |= ((r * 0x204081u) & 0x01010101u) << k;
-      }
-      words[lz * 4 + ly] = wv;
-    }
-#pragma unroll
-  for (int lz = 0; lz < 4; ++lz)
-#pragma unroll
-    for (int ly = 0; ly < 4; ++ly)
-      *reinterpret_cast<uint32_t*>(out + ((size_t)(z0 + lz) * N + (y0 + ly)) * N + x0) = words[lz * 4 + ly];
+    words[q] = wv;
+  }
+  *reinterpret_cast<uint4*>(out + ((size_t)z * N + y) * N + x0) = make_uint4(words[0], words[1], words[2], words[3]);
 }
 
 // Corner-packed mip records (voxel_sample.cuh), x fastest: one thread per
-// 2x2x2 block of records of one level (blockIdx.y = level - 1). It reads the
-// 3x3x3 texels its 8 records cover (+1 clamped) once and writes the 8
-// records (consecutive threads take consecutive blocks along x, so a warp's
-// record pairs (x0, x0 + 1) fill contiguous rows). Records hold FP16 texels: a copy with BF16 precision; with FP32
-// precision the records cover levels 1..3, whose texels k / 8^l (8^l <= 512)
-// FP16 holds exactly.
+// 2x2x2 block of records, over the blocks of all levels back to back. It
+// reads the 3x3x3 texels its 8 records cover (+1 clamped) once and writes
+// the 8 records (consecutive threads take consecutive blocks along x, so
+// the record pairs (x0, x0 + 1) of a warp fill contiguous rows). Records
+// hold FP16 texels: a copy with BF16 precision; with FP32 precision the
+// records cover levels 1..3, whose texels k / 8^l (8^l <= 512) FP16 holds
+// exactly.
 struct RecordLevels {
-  uint32_t off[kMaxVoxelLevels + 1];  // record offset of level l
-  int levels;                         // K
+  uint32_t blocks;  // 2x2x2 record blocks of levels 1..K
+  int levels;       // K
   int log2n;
 };
 
@@ -424,10 +418,23 @@ __device__ __forceinline__ uint32_t half_bits(__half v) { return (uint32_t)__hal
 template <typename T>
 __global__ void __launch_bounds__(256) records_kernel(const T* __restrict__ mips, MipOffsets mo, RecordLevels rl,
                                                       uint4* __restrict__ out) {
-  const int level = (int)blockIdx.y + 1;
-  const int ln = rl.log2n - level, n = 1 << ln, lb = ln > 0 ? ln - 1 : 0, nb = 1 << lb;
-  const uint32_t block = blockIdx.x * blockDim.x + threadIdx.x;
-  if (block >= (uint32_t)nb * nb * nb) return;
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= rl.blocks) return;
+  // Level of block g: level l has max(n / 2, 1)^3 blocks and n^3 records
+  // (n = N >> l), levels back to back from level 1 (found without indexing
+  // the parameter arrays, which would copy them to local memory).
+  int level = 1, ln = rl.log2n - 1;
+  uint32_t bstart = 0, rstart = 0;
+  for (;;) {
+    const uint32_t nblocks = 1u << (3 * max(ln - 1, 0));
+    if (level == rl.levels || g < bstart + nblocks) break;
+    bstart += nblocks;
+    rstart += 1u << (3 * ln);
+    ++level;
+    --ln;
+  }
+  const int n = 1 << ln, lb = ln > 0 ? ln - 1 : 0, nb = 1 << lb;
+  const uint32_t block = g - bstart;
   const int x0 = (int)(block & (nb - 1)) << 1, y0 = (int)((block >> lb) & (nb - 1)) << 1,
             z0 = (int)(block >> (2 * lb)) << 1;
   const T* src = mips + pick(mo.off, level);
@@ -440,7 +447,7 @@ __global__ void __launch_bounds__(256) records_kernel(const T* __restrict__ mips
 #pragma unroll
       for (int dx = 0; dx < 3; ++dx) h[dz][dy][dx] = half_bits(row[min(x0 + dx, n - 1)]);
     }
-  uint4* dst = out + pick(rl.off, level);
+  uint4* dst = out + rstart;
 #pragma unroll
   for (int r = 0; r < 8; ++r) {
     const int rx = r & 1, ry = (r >> 1) & 1, rz = r >> 2;
@@ -464,11 +471,15 @@ cudaError_t launch_build_records(cudaStream_t s, int n, const void* mips, const 
   MipOffsets mo{};
   RecordLevels rl{};
   for (int i = 0; i < kMaxVoxelLevels; ++i) mo.off[i] = mip_offsets[i];
-  for (int i = 0; i <= record_levels && i <= kMaxVoxelLevels; ++i) rl.off[i] = record_offsets[i];
   rl.levels = record_levels;
   while ((1 << (rl.log2n + 1)) <= n) ++rl.log2n;
-  const uint32_t nb = (uint32_t)(n >> 2) > 0 ? (uint32_t)(n >> 2) : 1u;  // 2x2x2 record blocks per axis at level 1
-  const dim3 grid((nb * nb * nb + 255) / 256, record_levels);
+  // the records of level l at record_offsets[l] = sum of (n >> j)^3 over j < l
+  for (int l = 1, ln = rl.log2n - 1; l <= record_levels; ++l, --ln) {
+    if (record_offsets[l] != (l == 1 ? 0u : record_offsets[l - 1] + (1u << (3 * (ln + 1)))))
+      return cudaErrorInvalidValue;
+    rl.blocks += 1u << (3 * (ln > 0 ? ln - 1 : 0));
+  }
+  const dim3 grid((rl.blocks + 255) / 256);
   if (precision == DRV_PRECISION_BF16)
     records_kernel<__half><<<grid, 256, 0, s>>>((const __half*)mips, mo, rl, records);
   else
@@ -479,8 +490,8 @@ cudaError_t launch_build_records(cudaStream_t s, int n, const void* mips, const 
 cudaError_t launch_build_corners(cudaStream_t s, int n, const uint32_t* bits, uint8_t* corners) {
   int l = 0;
   while ((1 << (l + 1)) <= n) ++l;
-  const uint32_t blocks = (uint32_t)(n / 4) * (n / 4) * (n / 4);
-  corners_kernel<<<(blocks + 255) / 256, 256, 0, s>>>(n, l, bits, corners);
+  const uint32_t pieces = (uint32_t)n * n * (n / 16);  // 16-byte pieces of the grid
+  corners_kernel<<<(pieces + 255) / 256, 256, 0, s>>>(n, l, bits, corners);
   return cudaGetLastError();
 }
 
