@@ -560,10 +560,19 @@ drv_status drv_prepare_rsm(DrvContext* ctx, int32_t li, const DrvSpotLight* L, c
     DRV_TRY_CUDA(ctx, drv::launch_scan_finite(ctx->s(), v->flux, n * 3, ch.half0, ctx->input_err()));
     DRV_TRY_CUDA(ctx, drv::launch_scan_finite(ctx->s(), v->depth_lin_sq, n * 2, ch.half0, ctx->input_err()));
   }
-  for (int k = 0; k < deepest; ++k) {
-    DRV_TRY_CUDA(ctx, drv::launch_downsample_rsm(ctx->s(), R >> k, ch.flux[k], ch.normal[k], ch.dls[k], ch.half(k),
-                                                 static_cast<float*>(ch.flux[k + 1]), ch.normal[k + 1],
-                                                 static_cast<float*>(ch.dls[k + 1])));
+  // The chain in launches of up to three passes each (launch_rsm_chain).
+  for (int k = 0; k < deepest; k += 3) {
+    const int passes = deepest - k < 3 ? deepest - k : 3;
+    float* fo[3] = {};
+    int16_t* no[3] = {};
+    float* dlo[3] = {};
+    for (int q = 0; q < passes; ++q) {
+      fo[q] = static_cast<float*>(ch.flux[k + 1 + q]);
+      no[q] = ch.normal[k + 1 + q];
+      dlo[q] = static_cast<float*>(ch.dls[k + 1 + q]);
+    }
+    DRV_TRY_CUDA(ctx, drv::launch_rsm_chain(ctx->s(), R >> k, passes, ch.flux[k], ch.normal[k], ch.dls[k], ch.half(k),
+                                            fo, no, dlo));
   }
   return DRV_OK;
 }

@@ -254,8 +254,10 @@ cudaError_t launch_raster_gbuffer(cudaStream_t s, const DrvMesh& mesh, RayFrame 
                                   int h, unsigned long long* keys, DrvGBufferOut out, int num_sms);
 cudaError_t launch_raster_rsm(cudaStream_t s, const DrvMesh& mesh, const DrvSpotLight& L, unsigned long long* keys,
                               DrvRSMOut out, int num_sms);
-cudaError_t launch_downsample_rsm(cudaStream_t s, int res, const void* flux, const int16_t* nrm, const void* dls,
-                                  int src_half, float* fo, int16_t* no, float* dlo);
+// Up to three RSM downsample passes res -> res/2 -> ... in one launch;
+// fo/no/dlo[k] receive level k + 1 (F32 flux and (d, d^2), RG16I normals).
+cudaError_t launch_rsm_chain(cudaStream_t s, int res, int passes, const void* flux, const int16_t* nrm,
+                             const void* dls, int src_half, float* const* fo, int16_t* const* no, float* const* dlo);
 cudaError_t launch_extract_vpls(cudaStream_t s, const DrvSpotLight& L, int res, const void* flux, const int16_t* nrm,
                                 const void* dls, int read_half, const void* dls_shadow, int shadow_half, void* vpls,
                                 DrvShadowCone* cones, int precision, float4* records);

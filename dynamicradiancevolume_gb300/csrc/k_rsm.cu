@@ -16,41 +16,99 @@ __device__ __forceinline__ float rsm_at(const void* a, int half, size_t i) {
   return half ? __half2float(static_cast<const __half*>(a)[i]) : static_cast<const float*>(a)[i];
 }
 
-// One downsample pass res -> res/2: flux = sum of the 2x2 children
-// (textureGather), normal = PackNormal16I(normalize(sum of unpacked normals)),
-// (d, d^2) = mean (linear sample at the shared corner).
-__global__ void __launch_bounds__(256) downsample_kernel(int res, const void* __restrict__ flux,
-                                                         const int16_t* __restrict__ nrm, const void* __restrict__ dls,
-                                                         int src_half, float* __restrict__ fo,
-                                                         int16_t* __restrict__ no, float* __restrict__ dlo) {
-  int h = res >> 1;
-  int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-  if (x >= h || y >= h) return;
-  float fs[3] = {0, 0, 0}, d0 = 0, d1 = 0;
-  f3 ns = mkf3(0, 0, 0);
+// The RSM mip chain, downsamplersm.frag:15-33 per pass res -> res/2: flux =
+// sum of the 2x2 children (textureGather), normal = PackNormal16I(normalize(
+// sum of unpacked normals)), (d, d^2) = mean (linear sample at the shared
+// corner). Up to three passes run in one launch: a CTA takes a 32 x 32
+// region of the source level and produces its 16 x 16, 8 x 8 and 4 x 4
+// texels of the next levels (a thread per level-1 texel, then the first 64
+// and 16 threads), keeping each level in shared memory for the next in the
+// form it has in global memory (F32 flux and (d, d^2), packed RG16I
+// normals), so each texel is the one a pass from global memory would give.
+// Every level is written out. P: passes (1..3).
+struct RsmChainArgs {
+  int res;  // source resolution
+  const void* flux;
+  const int16_t* nrm;
+  const void* dls;
+  int src_half;
+  float* fo[3];
+  int16_t* no[3];
+  float* dlo[3];
+};
+
+template <int P>
+__global__ void __launch_bounds__(256) rsm_chain_kernel(RsmChainArgs a) {
+  __shared__ float s_flux[2][3][256];
+  __shared__ float s_dls[2][2][256];
+  __shared__ int16_t s_nrm[2][2][256];
+  const int t = threadIdx.x;
 #pragma unroll
-  for (int dy = 0; dy < 2; ++dy)
+  for (int k = 1; k <= P; ++k) {
+    const int side = 32 >> k;          // this level's texels per CTA row
+    const int res_k = a.res >> k;      // this level's resolution
+    const int src_res = a.res >> (k - 1);
+    if (t < side * side) {
+      const int lx = t & (side - 1), ly = t / side;
+      const int gx = blockIdx.x * side + lx, gy = blockIdx.y * side + ly;
+      float fs[3] = {0, 0, 0}, d0 = 0, d1 = 0;
+      f3 ns = mkf3(0, 0, 0);
+      if (gx < res_k && gy < res_k) {
 #pragma unroll
-    for (int dx = 0; dx < 2; ++dx) {
-      size_t j = (size_t)(2 * y + dy) * res + (2 * x + dx);
-      fs[0] += rsm_at(flux, src_half, 3 * j);
-      fs[1] += rsm_at(flux, src_half, 3 * j + 1);
-      fs[2] += rsm_at(flux, src_half, 3 * j + 2);
-      ns = ns + unpack_normal16i(nrm[2 * j], nrm[2 * j + 1]);
-      d0 += rsm_at(dls, src_half, 2 * j);
-      d1 += rsm_at(dls, src_half, 2 * j + 1);
+        for (int dy = 0; dy < 2; ++dy)
+#pragma unroll
+          for (int dx = 0; dx < 2; ++dx) {
+            if (k == 1) {
+              const size_t j = (size_t)(2 * gy + dy) * src_res + (2 * gx + dx);
+              fs[0] += rsm_at(a.flux, a.src_half, 3 * j);
+              fs[1] += rsm_at(a.flux, a.src_half, 3 * j + 1);
+              fs[2] += rsm_at(a.flux, a.src_half, 3 * j + 2);
+              ns = ns + unpack_normal16i(a.nrm[2 * j], a.nrm[2 * j + 1]);
+              d0 += rsm_at(a.dls, a.src_half, 2 * j);
+              d1 += rsm_at(a.dls, a.src_half, 2 * j + 1);
+            } else {
+              const int b = (k - 2) & 1, ps = 2 * side;  // the previous level's buffer and row
+              const int j = (2 * ly + dy) * ps + (2 * lx + dx);
+              fs[0] += s_flux[b][0][j];
+              fs[1] += s_flux[b][1][j];
+              fs[2] += s_flux[b][2][j];
+              ns = ns + unpack_normal16i(s_nrm[b][0][j], s_nrm[b][1][j]);
+              d0 += s_dls[b][0][j];
+              d1 += s_dls[b][1][j];
+            }
+          }
+        const float len2 = dot3(ns, ns);
+        int16_t pk[2] = {0, 0};
+        if (len2 > 0.0f) pack_normal16i(ns * rsqrtf(len2), pk);
+        d0 *= 0.25f;
+        d1 *= 0.25f;
+        const size_t i = (size_t)gy * res_k + gx;
+        a.fo[k - 1][3 * i] = fs[0];
+        a.fo[k - 1][3 * i + 1] = fs[1];
+        a.fo[k - 1][3 * i + 2] = fs[2];
+        a.no[k - 1][2 * i] = pk[0];
+        a.no[k - 1][2 * i + 1] = pk[1];
+        a.dlo[k - 1][2 * i] = d0;
+        a.dlo[k - 1][2 * i + 1] = d1;
+        if (k < P) {
+          const int b = (k - 1) & 1;
+          s_flux[b][0][t] = fs[0];
+          s_flux[b][1][t] = fs[1];
+          s_flux[b][2][t] = fs[2];
+          s_nrm[b][0][t] = pk[0];
+          s_nrm[b][1][t] = pk[1];
+          s_dls[b][0][t] = d0;
+          s_dls[b][1][t] = d1;
+        }
+      } else if (k < P) {  // outside the level (a ragged edge): never read by an in-range texel
+        const int b = (k - 1) & 1;
+        s_flux[b][0][t] = s_flux[b][1][t] = s_flux[b][2][t] = 0.0f;
+        s_nrm[b][0][t] = s_nrm[b][1][t] = 0;
+        s_dls[b][0][t] = s_dls[b][1][t] = 0.0f;
+      }
     }
-  size_t i = (size_t)y * h + x;
-  fo[3 * i] = fs[0];
-  fo[3 * i + 1] = fs[1];
-  fo[3 * i + 2] = fs[2];
-  float len2 = dot3(ns, ns);
-  int16_t pk[2] = {0, 0};
-  if (len2 > 0.0f) pack_normal16i(ns * rsqrtf(len2), pk);
-  no[2 * i] = pk[0];
-  no[2 * i + 1] = pk[1];
-  dlo[2 * i] = d0 * 0.25f;
-  dlo[2 * i + 1] = d1 * 0.25f;
+    if (k < P) __syncthreads();
+  }
 }
 
 __device__ __forceinline__ f3 unproject_dir(const DrvSpotLight& L, float u, float v) {
@@ -153,11 +211,24 @@ __global__ void __launch_bounds__(256) extract_kernel(DrvSpotLight L, int R, con
 
 }  // namespace
 
-cudaError_t launch_downsample_rsm(cudaStream_t s, int res, const void* flux, const int16_t* nrm, const void* dls,
-                                  int src_half, float* fo, int16_t* no, float* dlo) {
-  int h = res / 2;
-  dim3 block(16, 16), grid((h + 15) / 16, (h + 15) / 16);
-  downsample_kernel<<<grid, block, 0, s>>>(res, flux, nrm, dls, src_half, fo, no, dlo);
+cudaError_t launch_rsm_chain(cudaStream_t s, int res, int passes, const void* flux, const int16_t* nrm,
+                             const void* dls, int src_half, float* const* fo, int16_t* const* no, float* const* dlo) {
+  if (passes < 1 || passes > 3) return cudaErrorInvalidValue;
+  RsmChainArgs a{};
+  a.res = res;
+  a.flux = flux;
+  a.nrm = nrm;
+  a.dls = dls;
+  a.src_half = src_half;
+  for (int k = 0; k < passes; ++k) {
+    a.fo[k] = fo[k];
+    a.no[k] = no[k];
+    a.dlo[k] = dlo[k];
+  }
+  const dim3 grid((res + 31) / 32, (res + 31) / 32);
+  if (passes == 1) rsm_chain_kernel<1><<<grid, 256, 0, s>>>(a);
+  else if (passes == 2) rsm_chain_kernel<2><<<grid, 256, 0, s>>>(a);
+  else rsm_chain_kernel<3><<<grid, 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 

@@ -274,10 +274,12 @@ __global__ void __launch_bounds__(256) mips_kernel(int N, int B, const uint32_t*
                                                    T* __restrict__ mips, MipOffsets mo) {
   __shared__ uint32_t sbits[32 * 32];  // B rows x B slices of (B <= 32)-voxel runs
   __shared__ float lv[2][16 * 16 * 16];
-  const int nbx = N / B;
-  const int bx = blockIdx.x % nbx, by = (blockIdx.x / nbx) % nbx, bz = blockIdx.x / (nbx * nbx);
+  // N and B are powers of two: indices split by shifts and masks (a
+  // division by a runtime divisor costs tens of instructions).
+  const int lB = 31 - __clz(B), lnb = 31 - __clz(N) - lB, nbx = 1 << lnb;
+  const int bx = blockIdx.x & (nbx - 1), by = (blockIdx.x >> lnb) & (nbx - 1), bz = blockIdx.x >> (2 * lnb);
   for (int i = threadIdx.x; i < B * B; i += blockDim.x) {
-    int y = i % B, z = i / B;
+    int y = i & (B - 1), z = i >> lB;
     int gx = bx * B, gy = by * B + y, gz = bz * B + z;
     size_t bit = ((size_t)gz * N + gy) * N + gx;
     uint32_t word = bits[bit >> 5];
@@ -285,9 +287,9 @@ __global__ void __launch_bounds__(256) mips_kernel(int N, int B, const uint32_t*
   }
   __syncthreads();
   // Level 1 from bits.
-  int n = B / 2;
+  int n = B / 2, ln = lB - 1;
   for (int i = threadIdx.x; i < n * n * n; i += blockDim.x) {
-    int x = i % n, y = (i / n) % n, z = i / (n * n);
+    int x = i & (n - 1), y = (i >> ln) & (n - 1), z = i >> (2 * ln);
     int c = 0;
 #pragma unroll
     for (int dz = 0; dz < 2; ++dz)
@@ -305,10 +307,10 @@ __global__ void __launch_bounds__(256) mips_kernel(int N, int B, const uint32_t*
   __syncthreads();
   // Levels 2 .. log2(B).
   int cur = 0, level = 1;
-  for (int m = n / 2; m >= 1; m /= 2) {
+  for (int m = n / 2, lm = ln - 1; m >= 1; m /= 2, --lm) {
     ++level;
     for (int i = threadIdx.x; i < m * m * m; i += blockDim.x) {
-      int x = i % m, y = (i / m) % m, z = i / (m * m);
+      int x = i & (m - 1), y = (i >> lm) & (m - 1), z = i >> (2 * lm);
       int p = 2 * m;
       float s = 0.0f;
 #pragma unroll
@@ -335,11 +337,11 @@ template <typename T>
 __global__ void __launch_bounds__(256) mips_tail_kernel(int N, int first_level, int last_level, T* __restrict__ mips,
                                                         MipOffsets mo) {
   for (int level = first_level; level <= last_level; ++level) {
-    int m = N >> level, p = m * 2;
+    int lm = 31 - __clz(N) - level, m = 1 << lm, p = m * 2;
     const T* src = mips + pick(mo.off, level - 1);
     T* dst = mips + pick(mo.off, level);
     for (int i = threadIdx.x; i < m * m * m; i += blockDim.x) {
-      int x = i % m, y = (i / m) % m, z = i / (m * m);
+      int x = i & (m - 1), y = (i >> lm) & (m - 1), z = i >> (2 * lm);
       float s = 0.0f;
       for (int dz = 0; dz < 2; ++dz)
         for (int dy = 0; dy < 2; ++dy)
