@@ -370,6 +370,18 @@ __device__ __forceinline__ uint32_t corner_row_bits(const uint32_t* __restrict__
   return r | next << 16;
 }
 
+// 8 x 8 bit-matrix transpose (bit j of byte i to bit i of byte j) by three
+// rounds of masked swaps (the classic delta-swap transpose).
+__device__ __forceinline__ uint64_t transpose_bits8x8(uint64_t x) {
+  uint64_t t = (x ^ (x >> 7)) & 0x00AA00AA00AA00AAull;
+  x ^= t ^ (t << 7);
+  t = (x ^ (x >> 14)) & 0x0000CCCC0000CCCCull;
+  x ^= t ^ (t << 14);
+  t = (x ^ (x >> 28)) & 0x00000000F0F0F0F0ull;
+  x ^= t ^ (t << 28);
+  return x;
+}
+
 __global__ void __launch_bounds__(256) corners_kernel(int N, int log2n, const uint32_t* __restrict__ bits,
                                                       uint8_t* __restrict__ out) {
   const int lq = log2n - 4;  // 16-byte pieces per row = N / 16
@@ -381,23 +393,20 @@ __global__ void __launch_bounds__(256) corners_kernel(int N, int log2n, const ui
   // rows[dy | dz << 1]
   const uint32_t rows[4] = {corner_row_bits(bits, N, y, z, x0), corner_row_bits(bits, N, y1, z, x0),
                             corner_row_bits(bits, N, y, z1, x0), corner_row_bits(bits, N, y1, z1, x0)};
-  // Word q holds bytes lx = 4q..4q+3; bit k of byte lx is voxel lx + (k & 1)
-  // of row k >> 1. Per k the four bits (one per byte) are spread to bit
-  // positions 0, 8, 16, 24 at once: the product r * 0x204081 places copies of
-  // the 4-bit r at shifts 0, 7, 14, 21 without carries, and the mask keeps
-  // bit j of the copy at shift 7j.
-  uint32_t words[4];
+  // Bit k of byte lx is voxel lx + (k & 1) of row k >> 1: with vector k =
+  // bits lx (0..7, or 8..15) of row k >> 1 shifted right by k & 1, the 8
+  // bytes of an 8-byte half are the 8 x 8 bit transpose of the 8 vectors.
+  // Byte permutes gather the vectors (byte k = vector k), three rounds of
+  // masked swaps transpose them.
+  uint32_t p[4];
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    uint32_t wv = 0;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      const uint32_t r = (rows[k >> 1] >> (4 * q + (k & 1))) & 0xFu;
-      wv |= ((r * 0x204081u) & 0x01010101u) << k;
-    }
-    words[q] = wv;
-  }
-  *reinterpret_cast<uint4*>(out + ((size_t)z * N + y) * N + x0) = make_uint4(words[0], words[1], words[2], words[3]);
+  for (int q = 0; q < 4; ++q) p[q] = __byte_perm(rows[q], rows[q] >> 1, 0x5140);  // lx 0..7 and 8..15, dx 0, 1
+  const uint64_t lo = transpose_bits8x8((uint64_t)__byte_perm(p[0], p[1], 0x5410) |
+                                        (uint64_t)__byte_perm(p[2], p[3], 0x5410) << 32);
+  const uint64_t hi = transpose_bits8x8((uint64_t)__byte_perm(p[0], p[1], 0x7632) |
+                                        (uint64_t)__byte_perm(p[2], p[3], 0x7632) << 32);
+  *reinterpret_cast<uint4*>(out + ((size_t)z * N + y) * N + x0) =
+      make_uint4((uint32_t)lo, (uint32_t)(lo >> 32), (uint32_t)hi, (uint32_t)(hi >> 32));
 }
 
 // Corner-packed mip records (voxel_sample.cuh), x fastest: one thread per
