@@ -252,8 +252,8 @@ drv_status drv_create(const DrvConfig* cfg, DrvContext** out) {
   c->atlas_words = (size_t)cfg->n_cascades * cfg->cav_res * cfg->cav_res * cfg->cav_res;
   if ((e = cudaMalloc(&c->atlas, c->atlas_words * 4)) != cudaSuccess) return bail(e);
   // counter (16 B) + ticket + error word (cleared by every allocation, 32 B in
-  // all), then the input-check word (read and cleared by drv_get_error), one
-  // allocation.
+  // all), then the input-check word (read and cleared by drv_get_error) and
+  // the opacity mips' ticket (reset by its own kernel), one allocation.
   if ((e = cudaMalloc(&c->counter, 64)) != cudaSuccess) return bail(e);
   c->scratch_words = reinterpret_cast<uint32_t*>(c->counter + 1);
   if ((e = cudaMemset(c->counter, 0, 64)) != cudaSuccess) return bail(e);
@@ -633,7 +633,7 @@ drv_status drv_build_opacity_mips(DrvContext* ctx) {
                  "build_corners");
   drv_status st = cuda_check(ctx,
                              drv::launch_build_mips(s, ctx->cfg.voxel_res, ctx->voxel_bits, ctx->mips, ctx->mip_offset,
-                                                    ctx->n_voxel_levels, ctx->cfg.precision),
+                                                    ctx->n_voxel_levels, ctx->cfg.precision, ctx->mips_ticket()),
                              "build_mips");
   if (st == DRV_OK)
     st = cuda_check(ctx,

@@ -174,7 +174,8 @@ struct Context {
   uint32_t* atlas = nullptr;
   size_t atlas_words = 0;
   DrvCacheCounter* counter = nullptr;
-  uint32_t* scratch_words = nullptr;  // [0] alloc ticket, [1] device error bits, [4] input-check bits
+  uint32_t* scratch_words = nullptr;  // [0] alloc ticket, [1] device error bits, [4] input-check bits, [5] mips ticket
+  uint32_t* mips_ticket() const { return scratch_words + 5; }
   uint32_t* input_err() const { return scratch_words + 4; }
   // Voxels.
   uint32_t* voxel_bits = nullptr;
@@ -265,8 +266,10 @@ cudaError_t launch_voxelize(cudaStream_t s, const DrvBox* boxes, int n_boxes, co
                             uint32_t* bits);
 cudaError_t launch_voxelize_triangles(cudaStream_t s, const float* positions, int n_vertices, const uint32_t* indices,
                                       int n_triangles, const DrvVolumeInfo& vol, int n, uint32_t* bits, int num_sms);
+// ticket: a zeroed word of the context's (the last CTA builds the levels
+// above one 32^3 block and zeroes it again).
 cudaError_t launch_build_mips(cudaStream_t s, int n, const uint32_t* bits, void* mips, const size_t* offsets,
-                              int n_levels, int precision);
+                              int n_levels, int precision, uint32_t* ticket);
 cudaError_t launch_build_corners(cudaStream_t s, int n, const uint32_t* bits, uint8_t* corners);
 cudaError_t launch_build_records(cudaStream_t s, int n, const void* mips, const size_t* mip_offsets, int precision,
                                  uint4* records, const uint32_t* record_offsets, int record_levels);

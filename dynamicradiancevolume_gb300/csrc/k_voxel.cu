@@ -268,10 +268,16 @@ template <>
 __device__ __forceinline__ void store_mip<__half>(__half* p, float v) { *p = __float2half_rn(v); }
 __device__ __forceinline__ float load_mip(const float* p) { return *p; }
 __device__ __forceinline__ float load_mip(const __half* p) { return __half2float(*p); }
+// The same through L2 (another CTA's writes of this launch).
+__device__ __forceinline__ float load_mip_l2(const float* p) { return __ldcg(p); }
+__device__ __forceinline__ float load_mip_l2(const __half* p) {
+  return __half2float(__ushort_as_half(__ldcg(reinterpret_cast<const unsigned short*>(p))));
+}
 
 template <typename T>
 __global__ void __launch_bounds__(256) mips_kernel(int N, int B, const uint32_t* __restrict__ bits,
-                                                   T* __restrict__ mips, MipOffsets mo) {
+                                                   T* __restrict__ mips, MipOffsets mo, uint32_t* ticket,
+                                                   int tail_first, int tail_last) {
   __shared__ uint32_t sbits[32 * 32];  // B rows x B slices of (B <= 32)-voxel runs
   __shared__ float lv[2][16 * 16 * 16];
   // N and B are powers of two: indices split by shifts and masks (a
@@ -328,28 +334,37 @@ __global__ void __launch_bounds__(256) mips_kernel(int N, int B, const uint32_t*
     __syncthreads();
     cur ^= 1;
   }
-}
-
-// Remaining levels above log2(B), from the level written by mips_kernel.
-// Levels are computed from the FP32 level below when stored as FP32, and from
-// the stored FP16 values otherwise (the chain a FP16 texture would hold).
-template <typename T>
-__global__ void __launch_bounds__(256) mips_tail_kernel(int N, int first_level, int last_level, T* __restrict__ mips,
-                                                        MipOffsets mo) {
-  for (int level = first_level; level <= last_level; ++level) {
-    int lm = 31 - __clz(N) - level, m = 1 << lm, p = m * 2;
-    const T* src = mips + pick(mo.off, level - 1);
-    T* dst = mips + pick(mo.off, level);
+  // Levels tail_first..tail_last, above one block: built by the CTA that
+  // finishes last (a ticket per build, reset by that CTA for the next), from
+  // the level below as every CTA wrote it (each CTA fences its writes before
+  // taking its ticket; the last one reads through L2). Like the levels
+  // above, each comes from the level below as stored (FP32, or the FP16
+  // values: the chain an FP16 texture would hold).
+  if (tail_first > tail_last) return;
+  __shared__ bool s_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  const int log2n = lB + lnb;
+  for (int lv = tail_first; lv <= tail_last; ++lv) {
+    const int lm = log2n - lv, m = 1 << lm, p = m * 2;
+    const T* src = mips + pick(mo.off, lv - 1);
+    T* dst = mips + pick(mo.off, lv);
     for (int i = threadIdx.x; i < m * m * m; i += blockDim.x) {
-      int x = i & (m - 1), y = (i >> lm) & (m - 1), z = i >> (2 * lm);
+      const int x = i & (m - 1), y = (i >> lm) & (m - 1), z = i >> (2 * lm);
       float s = 0.0f;
       for (int dz = 0; dz < 2; ++dz)
         for (int dy = 0; dy < 2; ++dy)
-          for (int dx = 0; dx < 2; ++dx) s += load_mip(src + ((size_t)(2 * z + dz) * p + (2 * y + dy)) * p + (2 * x + dx));
+          for (int dx = 0; dx < 2; ++dx)
+            s += load_mip_l2(src + ((size_t)(2 * z + dz) * p + (2 * y + dy)) * p + (2 * x + dx));
       store_mip(dst + i, s * 0.125f);
     }
     __syncthreads();
   }
+  if (threadIdx.x == 0) *ticket = 0u;
 }
 
 // Corner-packed level 0 (see voxel_sample.cuh): byte (x, y, z) = the 8 voxels
@@ -527,7 +542,7 @@ cudaError_t launch_voxelize_triangles(cudaStream_t s, const float* positions, in
 }
 
 cudaError_t launch_build_mips(cudaStream_t s, int n, const uint32_t* bits, void* mips, const size_t* offsets,
-                              int n_levels, int precision) {
+                              int n_levels, int precision, uint32_t* ticket) {
   MipOffsets mo{};
   for (int i = 0; i < n_levels && i < kMaxVoxelLevels; ++i) mo.off[i] = offsets[i];
   int B = n < 32 ? n : 32;
@@ -535,21 +550,12 @@ cudaError_t launch_build_mips(cudaStream_t s, int n, const uint32_t* bits, void*
   while ((1 << (lb + 1)) <= B) ++lb;
   int blocks = (n / B) * (n / B) * (n / B);
   const bool half = precision == DRV_PRECISION_BF16;
+  const int L = n_levels - 1;  // levels lb + 1 .. L by the last CTA
   if (half)
-    mips_kernel<__half><<<blocks, 256, 0, s>>>(n, B, bits, (__half*)mips, mo);
+    mips_kernel<__half><<<blocks, 256, 0, s>>>(n, B, bits, (__half*)mips, mo, ticket, lb + 1, L);
   else
-    mips_kernel<float><<<blocks, 256, 0, s>>>(n, B, bits, (float*)mips, mo);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  int L = n_levels - 1;
-  if (L > lb) {
-    if (half)
-      mips_tail_kernel<__half><<<1, 256, 0, s>>>(n, lb + 1, L, (__half*)mips, mo);
-    else
-      mips_tail_kernel<float><<<1, 256, 0, s>>>(n, lb + 1, L, (float*)mips, mo);
-    e = cudaGetLastError();
-  }
-  return e;
+    mips_kernel<float><<<blocks, 256, 0, s>>>(n, B, bits, (float*)mips, mo, ticket, lb + 1, L);
+  return cudaGetLastError();
 }
 
 }  // namespace drv
