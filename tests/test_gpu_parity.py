@@ -252,6 +252,11 @@ def test_allocation_bit_exact(case, request, oracle):
     g = r.atlas[r.atlas != 0]
     o = atlas[atlas != 0]
     assert np.array_equal(r.positions[g - 1], pos[o - 1])
+    # cachePrepareLighting's dispatch size (DRV_LIGHTING_THREADS_PER_GROUP = 64
+    # caches per group, lightcache.glsl:95), written by the allocation
+    c = r.pipe._dev_tensor(r.pipe.buffers().counter, 4, r.torch.int32).cpu().numpy()
+    lit = min(r.count, r.hf.config.max_caches)
+    assert list(c[:3]) == [(lit + 63) // 64, 1, 1]
     # SH zeroed at allocation then lit: the padding word stays zero
     if r.hf.config.precision == abi.PRECISION_FP32:
         assert np.all(r.entries[:, 3] == 0)
