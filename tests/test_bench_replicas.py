@@ -1,7 +1,7 @@
 """The benchmark's multi-GPU mode is replicas: each rank renders its own
 frame, and only the report is reduced (slowest rank's times, all ranks'
 caches). Checked with two gloo ranks on the CPU; a reference-arm rank other
-than 0 exits without work."""
+than 0 exits without work, and rank 0 prints the CPU arm's line."""
 import os
 import socket
 import subprocess
@@ -55,3 +55,21 @@ def test_reference_arm_rank_one_exits_without_work():
                        env=env, capture_output=True, text=True, timeout=120)
     assert p.returncode == 0
     assert p.stdout.strip() == ""
+
+
+def test_reference_arm_line_on_the_small_workload():
+    """The CPU arm's one JSON line on the small workload: the FP64 oracle
+    alone (the product library never mapped into the process), the
+    workload's config, and its own cpu_baseline and e2e objects."""
+    import json
+    env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK")}
+    p = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--workload", "c1_small",
+                        "--steps", "1", "--warmup", "0"], env=env, capture_output=True, text=True, timeout=300)
+    assert p.returncode == 0, p.stderr[-2000:]
+    d = json.loads(p.stdout.strip().splitlines()[-1])
+    assert d["impl"] == "reference" and d["product_library_loaded"] is False
+    assert d["config"]["workload"] == "c1_small" and d["dtype"] == "f64"
+    assert d["unit"] == "caches/s" and d["higher_is_better"] is True and d["value"] > 0
+    cb = d["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": "caches/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
