@@ -521,3 +521,35 @@ def test_specular_apply_of_a_constant_envmap(oracle):
     np.testing.assert_allclose(out[lit], expect[lit], rtol=1e-6, atol=1e-12)
     assert np.mean(np.abs(wsum[lit] - 1.0) < 1e-6) > 0.9  # most pixels have all 8 corners (pi passed in binary32)
     assert not out[~lit].any()
+
+
+def test_rsm_downsample_known_answers(oracle):
+    """downsamplersm.frag:15-33 on an 8 x 8 RSM: flux is the sum of the 2 x 2
+    children (textureGather), (d, d^2) their mean (the linear sample at the
+    shared corner), the normal the normalised sum of the unpacked children,
+    repacked; three levels chain."""
+    R = 8
+    rng = np.random.default_rng(5)
+    flux = rng.integers(0, 64, size=(R, R, 3)).astype(np.float32) / 8.0  # exact in FP32 sums
+    dls = np.stack([rng.integers(0, 64, size=(R, R)) / 4.0, rng.integers(0, 64, size=(R, R)) / 2.0],
+                   axis=-1).astype(np.float32)
+    up = oracle.pack_normal16i((0.0, 0.0, 1.0))
+    n16 = np.empty((R, R, 2), np.int16)
+    n16[...] = up
+    # block (1, 1) of level 1: two children face +x, two +y: their mean
+    # direction is (1, 1, 0) / sqrt(2)
+    n16[2, 2] = n16[2, 3] = oracle.pack_normal16i((1.0, 0.0, 0.0))
+    n16[3, 2] = n16[3, 3] = oracle.pack_normal16i((0.0, 1.0, 0.0))
+    fo, no, do = oracle.downsample_rsm(flux, n16, dls)
+    blocks = lambda a: a.reshape(R // 2, 2, R // 2, 2, *a.shape[2:])
+    assert np.array_equal(fo, blocks(flux).sum(axis=(1, 3)))
+    assert np.array_equal(do, blocks(dls).mean(axis=(1, 3)).astype(np.float32))
+    d = oracle.unpack_normal16i(tuple(no[1, 1]))
+    assert np.allclose(d, (math.sqrt(0.5), math.sqrt(0.5), 0.0), atol=2e-4)
+    mask = np.ones((R // 2, R // 2), bool)
+    mask[1, 1] = False
+    assert np.all(no[mask] == np.array(up, np.int16))
+    chain = oracle.rsm_chain(flux, n16, dls, 3)
+    assert [c[0].shape[0] for c in chain] == [8, 4, 2, 1]
+    assert np.array_equal(chain[3][0].reshape(3), flux.reshape(-1, 3).sum(axis=0))
+    assert np.allclose(chain[3][2].reshape(2), dls.reshape(-1, 2).mean(axis=0), rtol=1e-6)
