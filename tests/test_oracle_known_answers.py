@@ -553,3 +553,52 @@ def test_rsm_downsample_known_answers(oracle):
     assert [c[0].shape[0] for c in chain] == [8, 4, 2, 1]
     assert np.array_equal(chain[3][0].reshape(3), flux.reshape(-1, 3).sum(axis=0))
     assert np.allclose(chain[3][2].reshape(2), dls.reshape(-1, 2).mean(axis=0), rtol=1e-6)
+
+
+def test_vpl_extraction_known_answers(oracle):
+    """cacheLightingRSM.comp:141-158 and 168-192 on a constant RSM: VPL i is
+    RSM texel morton_decode(i), at the RSM depth d along its texel's ray from
+    the light (inside the spot cone), with area d^2 * ValAreaFactor and the
+    texel's flux and unpacked normal; a shadow block's cone source is at the
+    same depth along its sample ray, and with zero depth variance its spread
+    is the super-VAL width."""
+    d = abi.DrvLightDesc()
+    d.intensity[:] = (1.0, 1.0, 1.0)
+    d.position[:] = (0.5, 0.5, 0.9)
+    d.direction[:] = (0.0, 0.0, -1.0)
+    d.half_angle, d.rsm_resolution, d.rsm_read_lod, d.indirect_shadow_lod = 0.5, 32, 0, 1
+    d.near_plane, d.far_plane = 0.05, 5.0
+    L = oracle.prepare_light(d)
+    R = L.rsm_read_resolution
+    assert R == 32
+    depth = 0.75
+    rng = np.random.default_rng(6)
+    flux = rng.random((R, R, 3)).astype(np.float32)
+    normal = oracle.pack_normal16i((0.0, 0.6, 0.8))
+    n16 = np.empty((R, R, 2), np.int16)
+    n16[...] = normal
+    dls = np.empty((R, R, 2), np.float32)
+    dls[...] = (depth, depth * depth)
+    shadow = dls[::2, ::2].copy()  # level 1 of a constant RSM
+    vpl, cones = oracle.extract_vpls(L, flux, n16, dls, shadow)
+    lp = np.array(L.position, np.float64)
+    un = oracle.unpack_normal16i(normal)
+    for i in range(R * R):
+        x, y = oracle.morton_decode(i)
+        np.testing.assert_array_equal(vpl[i, 0:3], flux[y, x].astype(np.float64))
+        assert vpl[i, 3] == pytest.approx(depth * depth * L.val_area_factor, rel=1e-12)
+        off = vpl[i, 4:7] - lp
+        assert np.linalg.norm(off) == pytest.approx(depth, rel=1e-9)
+        # inside the square RSM frustum around the light's axis
+        assert math.acos(-off[2] / depth) <= 0.5 * math.sqrt(2) + 1e-6
+        np.testing.assert_allclose(vpl[i, 7:10], un, atol=0)
+    # texels mirrored through the RSM centre look in mirrored directions
+    i0 = next(i for i in range(R * R) if oracle.morton_decode(i) == (3, 5))
+    i1 = next(i for i in range(R * R) if oracle.morton_decode(i) == (R - 4, R - 6))
+    a, b = vpl[i0, 4:7] - lp, vpl[i1, 4:7] - lp
+    assert a[0] + b[0] == pytest.approx(0, abs=1e-9) and a[1] + b[1] == pytest.approx(0, abs=1e-9)
+    assert a[2] == pytest.approx(b[2], rel=1e-9)
+    n_blocks = (R * R + L.indirect_shadow_sample_interval - 1) // L.indirect_shadow_sample_interval
+    assert cones.shape == (n_blocks, 4)
+    assert np.allclose(np.linalg.norm(cones[:, 0:3] - lp, axis=1), depth, rtol=1e-6)
+    assert np.allclose(cones[:, 3], L.indirect_shadow_super_val_width, rtol=1e-6)
