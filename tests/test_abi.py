@@ -30,7 +30,7 @@ def test_struct_sizes_match_c(lib):
 
 
 def test_abi_version(lib):
-    assert lib.drv_abi_version() == 9
+    assert lib.drv_abi_version() == 10
 
 
 @pytest.mark.parametrize("name", list(pipeline.WORKLOADS))
