@@ -773,7 +773,11 @@ def stage_rooflines(w, bf16: bool, caches: int, stage_ms: dict, pk) -> dict:
     levels = [(R >> k) ** 2 * 24 for k in range(K + 1)]
     n_vpl = (R >> w.rsm_read_lod) ** 2
     vpl_out = n_vpl * ((32 if bf16 else 48) + 16 + 16)  # VPL, shadow cone, cull record
-    rsm = w.n_lights * (sum(levels[:-1]) + levels[-1] + sum(levels[1:]) + vpl_out)
+    # level 0 read, levels 1..K written (the chain keeps the levels between
+    # its passes on chip), the VPL level and the shadow level read by the
+    # extraction
+    extract_reads = levels[w.rsm_read_lod] + (levels[K] if K > w.rsm_read_lod else 0)
+    rsm = w.n_lights * (levels[0] + sum(levels[1:]) + extract_reads + vpl_out)
     N = w.voxel_res
     L = N.bit_length() - 1
     mip_texels = sum((N >> l) ** 3 for l in range(1, L + 1))

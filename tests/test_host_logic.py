@@ -55,9 +55,9 @@ def test_stage_roofline_bytes_of_the_headline():
     px, atlas = 1920 * 1080, 4 * 32 ** 3 * 4
     assert r["apply"]["bytes"] == px * 32 + atlas + 1814 * 64
     assert r["allocate"]["bytes"] == px * 4 + atlas + 1814 * 64
-    # RSM chain: 512^2 read, levels 1..3 written and read once more, the last read by the extraction
+    # RSM chain: 512^2 read, levels 1..3 written once, level 3 (VPLs and shadow blocks) read by the extraction
     lv = [(512 >> k) ** 2 * 24 for k in range(4)]
-    assert r["rsm+vpl"]["bytes"] == sum(lv[:-1]) + lv[-1] + sum(lv[1:]) + 4096 * (32 + 16 + 16)
+    assert r["rsm+vpl"]["bytes"] == lv[0] + sum(lv[1:]) + lv[3] + 4096 * (32 + 16 + 16)
     # voxels: bit grid x3, FP16 mips written + read, corner grid, every level's records
     texels = sum((256 >> l) ** 3 for l in range(1, 9))
     assert r["voxelize+mips"]["bytes"] == 256 ** 3 // 8 * 3 + texels * 2 * 2 + 256 ** 3 + texels * 16
